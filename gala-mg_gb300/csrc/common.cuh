@@ -1,0 +1,165 @@
+// common.cuh - device helpers shared by the phase-1, contraction and scan
+// kernels of the GB300 Louvain engine (sm_103a).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#define GALA_FULL_MASK 0xffffffffu
+
+namespace gala {
+
+// ---------------------------------------------------------------------------
+// Degree bins of the decide-and-move and weight-update sweeps.
+//   bin 0..3: deg 1-4 / 5-8 / 9-16 / 17-32 -> a group of 4/8/16/32 lanes per
+//             vertex, one neighbour per lane, aggregation with __match_any_sync
+//   bin 4   : deg 33-256     -> one warp per vertex, 512-slot smem hash
+//   bin 5   : deg 257-2048   -> one 256-thread CTA per vertex, 4096-slot smem hash
+//   bin 6   : deg 2049-8192  -> one 1024-thread CTA per vertex, 16384-slot smem hash
+//   bin 7   : deg > 8192     -> one 1024-thread CTA per vertex, hash table in
+//                               global memory (per-CTA slice, L2 resident)
+//   bin 8   : deg 0          -> never processed (the reference bins start at 1,
+//                               louvain_main_process.cu:278)
+// ---------------------------------------------------------------------------
+constexpr int kNumBins = 8;
+constexpr int kNumBinSlots = 9;
+
+__host__ __device__ inline int bin_of_degree(int64_t d)
+{
+    if (d <= 0) return 8;
+    if (d <= 4) return 0;
+    if (d <= 8) return 1;
+    if (d <= 16) return 2;
+    if (d <= 32) return 3;
+    if (d <= 256) return 4;
+    if (d <= 2048) return 5;
+    if (d <= 8192) return 6;
+    return 7;
+}
+
+// Device-side counters of one context (one instance in device memory, mirrored
+// to pinned host memory once per iteration).
+struct DevStats {
+    unsigned long long sum_in;      // sum over vertices of In[v]
+    unsigned long long sum_tot2;    // sum over communities of Tot[c]^2
+    unsigned long long sum_self;    // sum of self-loop weights (level init)
+    unsigned long long sum_k;       // sum of K = total weight m2 (level init)
+    unsigned long long act_edges[2];   // sum of degrees in the active lists
+    int act_vertices[2];
+    int min_tot;                    // min over non-empty communities of Tot
+    int n_movers;                   // movers of the current iteration
+    int err;                        // error bits (kErr*)
+    int max_deg;
+    int num_communities;            // contraction: C
+    int pad0;
+    int bin_start[kNumBinSlots + 1];  // order list: start of each bin
+    int act_count[2][kNumBins];       // active list counts (ping-pong)
+    int small_cnt[3];                 // contraction: communities per size class
+    int pad1;
+    long long large_max_cap;          // contraction: largest capped row of class 2
+    long long total;                  // scratch total of the last scan
+};
+
+constexpr int kErrHashOverflow = 1;
+constexpr int kErrProbeLimit = 2;
+constexpr int kErrBadLabel = 4;
+
+// ---------------------------------------------------------------------------
+// FP64 gain of a candidate community, same operation order as the reference
+// (kernel_functions.cu:136, :171, :202, :362):
+//   2*w - 2*K*((Tot_c - Tot_cur) + K) * (1/m2)
+// Written with explicit round-to-nearest intrinsics so that no FMA contraction
+// changes the rounding; the CPU oracle is compiled with -ffp-contract=off.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double gain_dq(int w_to_c, int ki, int tot_c, int tot_cur,
+                                          double constant)
+{
+    double a = __dmul_rn(2.0, (double)w_to_c);
+    double b = __dmul_rn(2.0, (double)ki);
+    double t = __dadd_rn(__dsub_rn((double)tot_c, (double)tot_cur), (double)ki);
+    return __dsub_rn(a, __dmul_rn(__dmul_rn(b, t), constant));
+}
+
+// (maxdq - 2*w_cur) + 2*Self  (kernel_functions.cu:381 / :532 / :748)
+__device__ __forceinline__ double gain_correct(double maxdq, int w_cur, int self_w)
+{
+    return __dadd_rn(__dsub_rn(maxdq, (double)(2 * w_cur)), (double)(2 * self_w));
+}
+
+// Pruning bound of compute_In (kernel_functions.cu:944, :1028):
+//   2*(In-Self) - (K-Self) + (double)(minTot - (Tot_c - K)) * (1/m2) * K > 0
+__device__ __forceinline__ bool prune_bound(int in_w, int self_w, int ki, int min_tot, int tot_c,
+                                            double constant)
+{
+    int ip = 2 * (in_w - self_w) - (ki - self_w);
+    double d = __dmul_rn(__dmul_rn((double)(min_tot - (tot_c - ki)), constant), (double)ki);
+    return __dadd_rn((double)ip, d) > 0.0;
+}
+
+// Candidate order: larger gain first, then the lower community id.
+__device__ __forceinline__ bool cand_better(double dq_a, int c_a, double dq_b, int c_b)
+{
+    return dq_a > dq_b || (dq_a == dq_b && c_a < c_b);
+}
+
+__device__ __forceinline__ unsigned lanemask_lt()
+{
+    unsigned m;
+    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+    return m;
+}
+
+__host__ __device__ inline int next_pow2_int(long long x)
+{
+    int p = 1;
+    while (p < x) p <<= 1;
+    return p;
+}
+
+// Open-addressing hash table with linear probing; keys int32 (-1 = empty),
+// int32 weight sums.  T is a power of two; at most T probes.
+__device__ __forceinline__ unsigned hash_slot(int key, int log2t)
+{
+    return ((unsigned)key * 0x9E3779B1u) >> (32 - log2t);
+}
+
+__device__ __forceinline__ bool hash_add(int *keys, int *vals, int T, int log2t, int key, int w)
+{
+    unsigned h = hash_slot(key, log2t);
+    for (int p = 0; p < T; ++p) {
+        int k = *(volatile int *)&keys[h];
+        if (k == -1) {
+            k = atomicCAS(&keys[h], -1, key);
+            if (k == -1) k = key;
+        }
+        if (k == key) {
+            atomicAdd(&vals[h], w);
+            return true;
+        }
+        h = (h + 1) & (unsigned)(T - 1);
+    }
+    return false;
+}
+
+// Warp-aggregated append of one item per flagged lane to list[*counter ...].
+// Must be called by all 32 lanes.
+__device__ __forceinline__ void warp_append(bool flag, int value, int *list, int *counter)
+{
+    unsigned b = __ballot_sync(GALA_FULL_MASK, flag);
+    if (b == 0) return;
+    int lane = threadIdx.x & 31;
+    int leader = __ffs(b) - 1;
+    int base = 0;
+    if (lane == leader) base = atomicAdd(counter, __popc(b));
+    base = __shfl_sync(GALA_FULL_MASK, base, leader);
+    if (flag) list[base + __popc(b & lanemask_lt())] = value;
+}
+
+template <typename T>
+__device__ __forceinline__ T warp_sum(T v)
+{
+#pragma unroll
+    for (int o = 16; o >= 1; o >>= 1) v += __shfl_xor_sync(GALA_FULL_MASK, v, o);
+    return v;
+}
+
+}  // namespace gala

@@ -1,0 +1,626 @@
+// engine.cu - host driver of the GB300 Louvain engine and the Louvain entry
+// points of the C ABI (include/gala.h).
+//
+// A gala_context owns one CUDA stream and all device workspace for graphs up
+// to its capacity; nothing is allocated while a run is in progress.  Per
+// phase-1 iteration the host reads back one small counter block (sum of In,
+// sum of Tot^2, error bits) to decide convergence, which is the only
+// device->host traffic of the iteration.
+#include <math.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <algorithm>
+#include <vector>
+
+#include "common.cuh"
+#include "internal.h"
+
+using namespace gala;
+
+struct gala_context {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    int32_t n_cap = 0;
+    int64_t e_cap = 0;
+    int64_t *offs[2] = {nullptr, nullptr};
+    int32_t *nbr[2] = {nullptr, nullptr};
+    int32_t *w[2] = {nullptr, nullptr};
+    int32_t *orig = nullptr;
+    Phase1Buffers p1{};
+    ContractBuffers cb{};
+    DevStats *d_stats = nullptr;
+    DevStats *h_stats = nullptr;
+    int32_t *scratch = nullptr;
+    long long scratch_ints = 0;
+    cudaEvent_t ev[8] = {};
+    std::vector<void *> allocs;
+};
+
+namespace {
+
+// Q from exact integer sums (the same expression as the oracle's
+// orc_q_from_sums); the host is compiled with -ffp-contract=off.
+double q_from_sums(unsigned long long sum_in, unsigned long long sum_tot2, long long m2)
+{
+    double c = 1.0 / (double)m2;
+    return (double)(long long)sum_in * c - (double)(long long)sum_tot2 * c * c;
+}
+
+template <typename T>
+bool dalloc(gala_context *ctx, T **p, size_t count)
+{
+    if (count == 0) count = 1;
+    void *q = nullptr;
+    if (cudaMalloc(&q, count * sizeof(T)) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    ctx->allocs.push_back(q);
+    *p = (T *)q;
+    return true;
+}
+
+__global__ void k_iota(int32_t *a, int n)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) a[i] = i;
+}
+
+struct Counts8 {
+    int c[kNumBins];
+};
+__global__ void k_set_act_counts(DevStats *st, int slot, Counts8 c, int nv, unsigned long long ne)
+{
+    for (int i = 0; i < kNumBins; ++i) st->act_count[slot][i] = c.c[i];
+    st->act_vertices[slot] = nv;
+    st->act_edges[slot] = ne;
+}
+
+gala_status check(cudaError_t e, const char *what)
+{
+    if (e == cudaSuccess) return GALA_OK;
+    return cuda_fail(e, what);
+}
+
+float ev_ms(cudaEvent_t a, cudaEvent_t b)
+{
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, a, b);
+    return ms;
+}
+
+struct Phase1Out {
+    double q = 0;
+    int iterations = 0;
+    double decide_ms = 0, update_ms = 0, total_ms = 0;
+    long long decide_bytes = 0, update_bytes = 0, sweeps = 0;
+};
+
+// Per-vertex and per-edge algorithmic bytes of a decide-and-move sweep:
+// offsets (2 x 8 B), own label, K, Self, label write (4 B each); per edge the
+// neighbour id, its label and (weighted) the weight.
+long long decide_bytes_for(long long nv, long long ne, bool weighted)
+{
+    return nv * (2 * 8 + 4 * 4) + ne * (8 + (weighted ? 4 : 0));
+}
+
+// One phase-1 run on level graph g (louvain_main_process).  The accepted
+// partition is left in ctx->p1.comm.
+gala_status phase1(gala_context *ctx, const LevelGraph &g, long long &m2, double min_mod, bool verbose,
+                   std::vector<double> *trace, Phase1Out *out)
+{
+    cudaStream_t st = ctx->stream;
+    Phase1Buffers &b = ctx->p1;
+    DevStats *h = ctx->h_stats;
+    const bool weighted = g.w != nullptr;
+    gala_status s;
+
+    p1_reset_level_stats(b, st);
+    p1_level_init(g, b, st);
+    if ((s = check(cudaMemcpyAsync(h, b.stats, sizeof(DevStats), cudaMemcpyDeviceToHost, st), "level init")) ||
+        (s = check(cudaStreamSynchronize(st), "level init")))
+        return s;
+    int bin_start[kNumBinSlots + 1];
+    memcpy(bin_start, h->bin_start, sizeof(bin_start));
+    const int max_deg = h->max_deg;
+    p1_level_init_rows(g, b, bin_start, st);
+    if ((s = check(cudaMemcpyAsync(h, b.stats, sizeof(DevStats), cudaMemcpyDeviceToHost, st), "level rows")) ||
+        (s = check(cudaStreamSynchronize(st), "level rows")))
+        return s;
+    if (m2 == 0) {  // first level: total weight m2 = sum of K (louvain.cu:165-167)
+        m2 = (long long)h->sum_k;
+        if (m2 <= 0) {
+            set_error("graph has no edges (total weight 0)");
+            return GALA_ERR_INVALID;
+        }
+        if (m2 > 0x7fffffffLL) {
+            set_error("total weight %lld exceeds the int32 range of community totals", m2);
+            return GALA_ERR_INVALID;
+        }
+    }
+    if ((long long)h->sum_k != m2) {
+        set_error("level weight %llu differs from total weight %lld", h->sum_k, m2);
+        return GALA_ERR_INVALID;
+    }
+    const double constant = 1 / (double)m2;
+    int level_cnt[kNumBins];
+    long long nv_all = 0;
+    for (int i = 0; i < kNumBins; ++i) {
+        level_cnt[i] = bin_start[i + 1] - bin_start[i];
+        nv_all += level_cnt[i];
+    }
+    // hub tables (bin 7) in the scratch pool
+    int hub_tmax = 64;
+    if (level_cnt[7] > 0) {
+        hub_tmax = next_pow2_int(2LL * max_deg);
+        long long per = 2LL * hub_tmax;
+        if ((long long)ctx->scratch_ints < per) {
+            set_error("hub vertex of degree %d needs a %lld-slot table, scratch holds %lld", max_deg, per,
+                      ctx->scratch_ints);
+            return GALA_ERR_CAPACITY;
+        }
+    }
+    b.hub_table = ctx->scratch;
+    b.hub_table_slots = ctx->scratch_ints;
+
+    double q = q_from_sums(h->sum_in, h->sum_tot2, m2);
+    if (trace) trace->push_back(q);
+    if (verbose) printf("Iteration:%d Q:%f\n", 0, q);
+    double prev_q = q;
+    int iteration = 1;
+
+    Counts8 c8;
+    for (int i = 0; i < kNumBins; ++i) c8.c[i] = level_cnt[i];
+    k_set_act_counts<<<1, 1, 0, st>>>(b.stats, 0, c8, (int)nv_all, (unsigned long long)g.E);
+    note_launch(1);
+    long long act_nv = nv_all, act_ne = g.E;
+    int cur = 0;
+    const int min_tot_init = m2 > 0x7fffffffLL ? 0x7fffffff : (int)m2;
+    cudaEventRecord(ctx->ev[0], st);
+    for (;;) {
+        const int nxt = cur ^ 1;
+        p1_iter_reset(b, nxt, min_tot_init, st);
+        cudaEventRecord(ctx->ev[2], st);
+        const int32_t *lists = iteration == 1 ? b.order : b.act[cur];
+        for (int bin = 0; bin < kNumBins; ++bin)
+            p1_decide(g, b, bin, lists + bin_start[bin], &b.stats->act_count[cur][bin], level_cnt[bin], constant,
+                      hub_tmax, st);
+        cudaEventRecord(ctx->ev[3], st);
+        p1_apply_movers(b, +1, g.n, st);
+        p1_tot_reduce(b, g.n, st);
+        cudaEventRecord(ctx->ev[4], st);
+        for (int bin = 0; bin < kNumBins; ++bin)
+            p1_update(g, b, bin, b.order + bin_start[bin], level_cnt[bin], nxt, bin_start[bin], constant, st);
+        cudaEventRecord(ctx->ev[5], st);
+        if ((s = check(cudaMemcpyAsync(h, b.stats, sizeof(DevStats), cudaMemcpyDeviceToHost, st), "iteration")) ||
+            (s = check(cudaStreamSynchronize(st), "iteration")))
+            return s;
+        if (h->err) {
+            set_error("phase 1: device error bits %d", h->err);
+            return GALA_ERR_OVERFLOW;
+        }
+        out->decide_ms += ev_ms(ctx->ev[2], ctx->ev[3]);
+        out->update_ms += ev_ms(ctx->ev[4], ctx->ev[5]);
+        out->decide_bytes += decide_bytes_for(act_nv, act_ne, weighted);
+        out->update_bytes += nv_all * (2 * 8 + 4 * 4) + g.E * (8 + (weighted ? 4 : 0));
+        out->sweeps += 1;
+        act_nv = h->act_vertices[nxt];
+        act_ne = (long long)h->act_edges[nxt];
+        q = q_from_sums(h->sum_in, h->sum_tot2, m2);
+        if (trace) trace->push_back(q);
+        if (verbose) printf("Iteration:%d Q:%f\n", iteration, q);
+        // convergence (louvain_main_process.cu:1004-1007): the partition of
+        // this iteration is dropped when Q did not grow by min_mod
+        if (q - prev_q < min_mod) {
+            p1_apply_movers(b, -1, g.n, st);
+            break;
+        }
+        prev_q = q;
+        cur = nxt;
+        iteration++;
+    }
+    cudaEventRecord(ctx->ev[1], st);
+    if ((s = check(cudaStreamSynchronize(st), "phase 1 end"))) return s;
+    out->total_ms = ev_ms(ctx->ev[0], ctx->ev[1]);
+    out->q = prev_q;
+    out->iterations = iteration;
+    if (verbose) {
+        printf("time without data init = %fms\n", out->total_ms);
+        printf("decideandmove time = %fms weight updating time = %fms remaining time = %fms\n", out->decide_ms,
+               out->update_ms, out->total_ms - out->decide_ms - out->update_ms);
+    }
+    return GALA_OK;
+}
+
+void bind_contract_buffers(gala_context *ctx)
+{
+    ContractBuffers &cb = ctx->cb;
+    cb.stats = ctx->d_stats;
+    cb.scan_partial = ctx->p1.scan_partial;
+    long long half = ctx->scratch_ints / 2;
+    cb.big_table = ctx->scratch;
+    cb.big_table_slots = half;
+    cb.big_bitmap = ctx->scratch + half;
+    cb.big_bitmap_words = half;
+}
+
+struct RunOut {
+    std::vector<double> trace;
+};
+
+// Multi-round loop of louvain.cu:193-226 on a device graph.  Level 0 reads
+// the caller's arrays; later levels live in the context's ping-pong buffers.
+// ctx->orig receives the final community of every level-0 vertex.
+gala_status run_levels(gala_context *ctx, int32_t n0, int64_t E0, const int64_t *offs0, const int32_t *nbr0,
+                       const int32_t *w0, const gala_options *opt, gala_result *res)
+{
+    cudaStream_t st = ctx->stream;
+    gala_status s;
+    const bool verbose = opt && opt->verbose;
+    const double min_mod = opt ? opt->min_modularity : 1e-6;
+    const int max_levels = opt ? opt->max_levels : 0;
+    if (n0 > ctx->n_cap || E0 > ctx->e_cap) {
+        set_error("graph (%d vertices, %lld entries) exceeds context capacity (%d, %lld)", n0, (long long)E0,
+                  ctx->n_cap, (long long)ctx->e_cap);
+        return GALA_ERR_CAPACITY;
+    }
+    bind_contract_buffers(ctx);
+    long long m2 = 0;  // set by the first phase-1 run
+    cudaEvent_t t0 = ctx->ev[6], t1 = ctx->ev[7];
+    cudaEventRecord(t0, st);
+    k_iota<<<std::min(4096, (n0 + 255) / 256), 256, 0, st>>>(ctx->orig, n0);
+    note_launch(1);
+
+    LevelGraph g{n0, E0, offs0, nbr0, w0};
+    int buf = 0;
+    double prev_mod = -1, cur_mod = -1;
+    int round = 0;
+    res->num_levels = 0;
+    res->total_iterations = 0;
+    res->iter_count = 0;
+    std::vector<double> trace;
+    double contract_ms = 0, p1_ms = 0, dec_ms = 0, upd_ms = 0;
+    long long dec_bytes = 0, upd_bytes = 0, sweeps = 0;
+    int C = n0;
+    for (;;) {
+        if (verbose) printf("===============round:%d===============\n", round);
+        Phase1Out po;
+        if ((s = phase1(ctx, g, m2, min_mod, verbose, &trace, &po))) return s;
+        p1_ms += po.total_ms;
+        dec_ms += po.decide_ms;
+        upd_ms += po.update_ms;
+        dec_bytes += po.decide_bytes;
+        upd_bytes += po.update_bytes;
+        sweeps += po.sweeps;
+        if (verbose && round == 0) printf("louvain time in the first round = %fms\n", po.total_ms);
+        // contraction into the other ping-pong buffer
+        cudaEventRecord(ctx->ev[0], st);
+        int64_t newE = 0;
+        gala_status cs = GALA_OK;
+        C = contract_run(g, ctx->p1.comm, ctx->cb, ctx->offs[buf], ctx->nbr[buf], ctx->w[buf], ctx->orig, n0, &newE,
+                         st, &cs);
+        if (C < 0) return cs;
+        cudaEventRecord(ctx->ev[1], st);
+        if ((s = check(cudaStreamSynchronize(st), "contraction"))) return s;
+        float cms = ev_ms(ctx->ev[0], ctx->ev[1]);
+        contract_ms += cms;
+        if (verbose && round == 0) printf("build time in the first round = %fms\n", cms);
+        if (verbose) printf("number of communities:%d modularity:%f\n", C, po.q);
+        if (round < GALA_MAX_LEVELS) {
+            res->level_modularity[round] = po.q;
+            res->level_communities[round] = C;
+            res->level_iterations[round] = po.iterations;
+        }
+        res->total_iterations += po.iterations;
+        round++;
+        prev_mod = cur_mod;
+        cur_mod = po.q;
+        g = LevelGraph{C, newE, ctx->offs[buf], ctx->nbr[buf], ctx->w[buf]};
+        buf ^= 1;
+        // louvain.cu:202: continue while the round gained at least min_mod
+        if (!(cur_mod - prev_mod >= min_mod)) break;
+        if (max_levels > 0 && round >= max_levels) break;
+        if (round >= GALA_MAX_LEVELS) break;
+    }
+    cudaEventRecord(t1, st);
+    if ((s = check(cudaStreamSynchronize(st), "run end"))) return s;
+    double total_ms = ev_ms(t0, t1);
+    if (verbose) {
+        printf("=====================================\n");
+        printf("final number of communities:%d -> %d final modularity:%f\n", n0, C, cur_mod);
+        printf("execution time without data transfer = %fms\n", total_ms);
+    }
+    res->modularity = cur_mod;
+    res->num_vertices = n0;
+    res->num_communities = C;
+    res->num_levels = round;
+    res->time_total_ms = total_ms;
+    res->time_phase1_ms = p1_ms;
+    res->time_decide_ms = dec_ms;
+    res->time_update_ms = upd_ms;
+    res->time_contract_ms = contract_ms;
+    res->decide_bytes = dec_bytes;
+    res->update_bytes = upd_bytes;
+    res->decide_sweeps = sweeps;
+    if (res->iter_modularity && res->iter_capacity > 0) {
+        int k = (int)std::min<size_t>(trace.size(), (size_t)res->iter_capacity);
+        memcpy(res->iter_modularity, trace.data(), (size_t)k * sizeof(double));
+    }
+    res->iter_count = (int)trace.size();
+    return GALA_OK;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// C ABI
+// ---------------------------------------------------------------------------
+extern "C" {
+
+void gala_default_options(gala_options *opt)
+{
+    if (!opt) return;
+    memset(opt, 0, sizeof(*opt));
+    opt->min_modularity = 1e-6;  // gala_main.cu:48
+    opt->max_levels = 0;
+    opt->verbose = 0;
+    opt->use_graphs = 0;
+}
+
+void gala_context_destroy(gala_context *ctx)
+{
+    if (!ctx) return;
+    int prev = 0;
+    cudaGetDevice(&prev);
+    cudaSetDevice(ctx->device);
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    for (void *p : ctx->allocs) cudaFree(p);
+    if (ctx->h_stats) cudaFreeHost(ctx->h_stats);
+    for (auto &e : ctx->ev)
+        if (e) cudaEventDestroy(e);
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    cudaSetDevice(prev);
+    delete ctx;
+}
+
+gala_status gala_context_create(int32_t device, int32_t max_vertices, int64_t max_entries, gala_context **out)
+{
+    clear_error();
+    if (!out || max_vertices <= 0 || max_entries < 0) {
+        set_error("gala_context_create: bad arguments");
+        return GALA_ERR_INVALID;
+    }
+    *out = nullptr;
+    int ndev = 0;
+    cudaError_t ce = cudaGetDeviceCount(&ndev);
+    if (ce != cudaSuccess || ndev <= 0) {
+        cudaGetLastError();
+        set_error("no CUDA device visible");
+        return GALA_ERR_NO_DEVICE;
+    }
+    if (device < 0 || device >= ndev) {
+        set_error("device %d out of range (%d devices)", device, ndev);
+        return GALA_ERR_INVALID;
+    }
+    if ((ce = cudaSetDevice(device)) != cudaSuccess) return cuda_fail(ce, "cudaSetDevice");
+    gala_context *ctx = new gala_context();
+    ctx->device = device;
+    ctx->n_cap = max_vertices;
+    ctx->e_cap = max_entries;
+    const size_t n = (size_t)max_vertices, E = (size_t)(max_entries > 0 ? max_entries : 1);
+    const size_t nblk = (n + 1023) / 1024;
+    const size_t scan_items = std::max(n + 2, (size_t)kNumBinSlots * nblk);
+    const size_t nparts = scan_items / 4096 + 4;
+    bool ok = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) == cudaSuccess;
+    for (auto &e : ctx->ev) ok = ok && cudaEventCreate(&e) == cudaSuccess;
+    ok = ok && cudaMallocHost(&ctx->h_stats, sizeof(DevStats)) == cudaSuccess;
+    for (int i = 0; i < 2 && ok; ++i)
+        ok = dalloc(ctx, &ctx->offs[i], n + 1) && dalloc(ctx, &ctx->nbr[i], E) && dalloc(ctx, &ctx->w[i], E);
+    Phase1Buffers &b = ctx->p1;
+    ok = ok && dalloc(ctx, &ctx->orig, n) && dalloc(ctx, &ctx->d_stats, 1) && dalloc(ctx, &b.comm, n) &&
+         dalloc(ctx, &b.K, n) && dalloc(ctx, &b.Self, n) && dalloc(ctx, &b.Tot, n) && dalloc(ctx, &b.size, n) &&
+         dalloc(ctx, &b.In, n) && dalloc(ctx, &b.order, n) && dalloc(ctx, &b.act[0], n) &&
+         dalloc(ctx, &b.act[1], n) && dalloc(ctx, &b.mv_v, n) && dalloc(ctx, &b.mv_old, n) &&
+         dalloc(ctx, &b.mv_new, n) && dalloc(ctx, &b.blockcnt, kNumBinSlots * nblk) &&
+         dalloc(ctx, &b.blockoff, kNumBinSlots * nblk) && dalloc(ctx, &b.scan_partial, nparts);
+    ContractBuffers &c = ctx->cb;
+    ok = ok && dalloc(ctx, &c.cnt, n + 1) && dalloc(ctx, &c.newid, n + 1) && dalloc(ctx, &c.lab, n) &&
+         dalloc(ctx, &c.csz, n + 1) && dalloc(ctx, &c.moff, n + 1) && dalloc(ctx, &c.cursor, n + 1) &&
+         dalloc(ctx, &c.members, n) && dalloc(ctx, &c.mpos, n) && dalloc(ctx, &c.ec, n + 1) &&
+         dalloc(ctx, &c.medge, n + 1) && dalloc(ctx, &c.stream_key, E) && dalloc(ctx, &c.stream_w, E) &&
+         dalloc(ctx, &c.tmp_off, n + 1) && dalloc(ctx, &c.tmp_nbr, E) && dalloc(ctx, &c.tmp_w, E) &&
+         dalloc(ctx, &c.kc, n + 1) && dalloc(ctx, &c.cls_list, 3 * n);
+    // scratch pool for hub tables (phase 1) and the large-row tables and
+    // bitmaps of the contraction: 8 ints per entry+vertex, 16 MB .. 512 MB
+    long long want = 8LL * ((long long)E + (long long)n);
+    want = std::max(want, 4LL << 20);
+    want = std::min(want, 128LL << 20);
+    ok = ok && dalloc(ctx, &ctx->scratch, (size_t)want);
+    ctx->scratch_ints = want;
+    if (!ok) {
+        cudaGetLastError();
+        gala_context_destroy(ctx);
+        set_error("gala_context_create: device allocation failed (%d vertices, %lld entries)", max_vertices,
+                  (long long)max_entries);
+        return GALA_ERR_OOM;
+    }
+    b.stats = ctx->d_stats;
+    memset(ctx->h_stats, 0, sizeof(DevStats));
+    cudaMemsetAsync(ctx->d_stats, 0, sizeof(DevStats), ctx->stream);
+    p1_configure_kernels();
+    contract_configure_kernels();
+    bind_contract_buffers(ctx);
+    if ((ce = cudaStreamSynchronize(ctx->stream)) != cudaSuccess) {
+        gala_context_destroy(ctx);
+        return cuda_fail(ce, "gala_context_create");
+    }
+    *out = ctx;
+    return GALA_OK;
+}
+
+gala_status gala_louvain_device(gala_context *ctx, int32_t n, const int64_t *d_offsets, const int32_t *d_neighbors,
+                                const int32_t *d_weights, const gala_options *opt, int32_t *d_community_out,
+                                gala_result *res)
+{
+    clear_error();
+    if (!ctx || n <= 0 || !d_offsets || !d_neighbors || !d_community_out) {
+        set_error("gala_louvain_device: bad arguments");
+        return GALA_ERR_INVALID;
+    }
+    gala_result local{};
+    if (!res) res = &local;
+    cudaSetDevice(ctx->device);
+    int64_t E = 0;
+    gala_status s;
+    if ((s = check(cudaMemcpyAsync(&E, d_offsets + n, sizeof(int64_t), cudaMemcpyDeviceToHost, ctx->stream),
+                   "read entry count")) ||
+        (s = check(cudaStreamSynchronize(ctx->stream), "read entry count")))
+        return s;
+    long long l0 = gala_kernel_launch_count();
+    if ((s = run_levels(ctx, n, E, d_offsets, d_neighbors, d_weights, opt, res))) return s;
+    if ((s = check(cudaMemcpyAsync(d_community_out, ctx->orig, (size_t)n * sizeof(int32_t),
+                                   cudaMemcpyDeviceToDevice, ctx->stream),
+                   "labels")) ||
+        (s = check(cudaStreamSynchronize(ctx->stream), "labels")))
+        return s;
+    res->kernel_launches = gala_kernel_launch_count() - l0;
+    return GALA_OK;
+}
+
+gala_status gala_louvain(gala_context *ctx, const gala_graph *g, const gala_options *opt, int32_t *community_out,
+                         gala_result *res)
+{
+    clear_error();
+    if (!g || !community_out || g->n <= 0) {
+        set_error("gala_louvain: bad arguments");
+        return GALA_ERR_INVALID;
+    }
+    gala_context *own = nullptr;
+    gala_status s;
+    if (!ctx) {
+        if ((s = gala_context_create(0, g->n, g->entries(), &own))) return s;
+        ctx = own;
+    }
+    gala_result local{};
+    if (!res) res = &local;
+    cudaSetDevice(ctx->device);
+    const int32_t n = g->n;
+    const int64_t E = g->entries();
+    if (n > ctx->n_cap || E > ctx->e_cap) {
+        if (own) gala_context_destroy(own);
+        set_error("graph (%d vertices, %lld entries) exceeds context capacity", n, (long long)E);
+        return GALA_ERR_CAPACITY;
+    }
+    long long l0 = gala_kernel_launch_count();
+    cudaStream_t st = ctx->stream;
+    // host -> device: offsets with a leading 0, neighbours, weights
+    cudaEventRecord(ctx->ev[6], st);
+    cudaMemsetAsync(ctx->offs[1], 0, sizeof(int64_t), st);
+    cudaMemcpyAsync(ctx->offs[1] + 1, g->offs.data(), (size_t)n * sizeof(int64_t), cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(ctx->nbr[1], g->nbr.data(), (size_t)E * sizeof(int32_t), cudaMemcpyHostToDevice, st);
+    const int32_t *dw = nullptr;
+    if (g->weighted) {
+        cudaMemcpyAsync(ctx->w[1], g->w.data(), (size_t)E * sizeof(int32_t), cudaMemcpyHostToDevice, st);
+        dw = ctx->w[1];
+    }
+    cudaEventRecord(ctx->ev[7], st);
+    if ((s = check(cudaStreamSynchronize(st), "host to device copy"))) {
+        if (own) gala_context_destroy(own);
+        return s;
+    }
+    float h2d = ev_ms(ctx->ev[6], ctx->ev[7]);
+    // level 0 lives in buffer 1; the first contraction writes buffer 0
+    s = run_levels(ctx, n, E, ctx->offs[1], ctx->nbr[1], dw, opt, res);
+    if (s == GALA_OK) {
+        cudaEventRecord(ctx->ev[6], st);
+        cudaMemcpyAsync(community_out, ctx->orig, (size_t)n * sizeof(int32_t), cudaMemcpyDeviceToHost, st);
+        cudaEventRecord(ctx->ev[7], st);
+        s = check(cudaStreamSynchronize(st), "device to host copy");
+        res->time_d2h_ms = ev_ms(ctx->ev[6], ctx->ev[7]);
+    }
+    res->time_h2d_ms = h2d;
+    res->h2d_bytes = (long long)n * 8 + E * 4 + (g->weighted ? E * 4 : 0);
+    res->d2h_bytes = (long long)n * 4;
+    res->kernel_launches = gala_kernel_launch_count() - l0;
+    if (own) gala_context_destroy(own);
+    return s;
+}
+
+gala_status gala_phase1_device(gala_context *ctx, int32_t n, const int64_t *d_offsets, const int32_t *d_neighbors,
+                               const int32_t *d_weights, double min_modularity, int32_t *d_community_out,
+                               double *modularity, double *iter_q, int32_t iter_capacity, int32_t *iterations)
+{
+    clear_error();
+    if (!ctx || n <= 0 || !d_offsets || !d_neighbors || !d_community_out) {
+        set_error("gala_phase1_device: bad arguments");
+        return GALA_ERR_INVALID;
+    }
+    cudaSetDevice(ctx->device);
+    cudaStream_t st = ctx->stream;
+    int64_t E = 0;
+    gala_status s;
+    if ((s = check(cudaMemcpyAsync(&E, d_offsets + n, sizeof(int64_t), cudaMemcpyDeviceToHost, st), "entries")) ||
+        (s = check(cudaStreamSynchronize(st), "entries")))
+        return s;
+    if (n > ctx->n_cap || E > ctx->e_cap) {
+        set_error("graph exceeds context capacity");
+        return GALA_ERR_CAPACITY;
+    }
+    LevelGraph g{n, E, d_offsets, d_neighbors, d_weights};
+    long long m2 = 0;
+    std::vector<double> trace;
+    Phase1Out po;
+    if ((s = phase1(ctx, g, m2, min_modularity, false, &trace, &po))) return s;
+    if ((s = check(cudaMemcpyAsync(d_community_out, ctx->p1.comm, (size_t)n * sizeof(int32_t),
+                                   cudaMemcpyDeviceToDevice, st),
+                   "labels")) ||
+        (s = check(cudaStreamSynchronize(st), "labels")))
+        return s;
+    if (modularity) *modularity = po.q;
+    if (iterations) *iterations = po.iterations;
+    if (iter_q)
+        for (int i = 0; i < iter_capacity && i < (int)trace.size(); ++i) iter_q[i] = trace[i];
+    return GALA_OK;
+}
+
+gala_status gala_contract_device(gala_context *ctx, int32_t n, const int64_t *d_offsets, const int32_t *d_neighbors,
+                                 const int32_t *d_weights, int32_t *d_community, int64_t *d_new_offsets,
+                                 int32_t *d_new_neighbors, int32_t *d_new_weights, int32_t *num_communities,
+                                 int64_t *num_entries)
+{
+    clear_error();
+    if (!ctx || n <= 0 || !d_offsets || !d_neighbors || !d_community || !d_new_offsets || !d_new_neighbors ||
+        !d_new_weights) {
+        set_error("gala_contract_device: bad arguments");
+        return GALA_ERR_INVALID;
+    }
+    cudaSetDevice(ctx->device);
+    cudaStream_t st = ctx->stream;
+    int64_t E = 0;
+    gala_status s;
+    if ((s = check(cudaMemcpyAsync(&E, d_offsets + n, sizeof(int64_t), cudaMemcpyDeviceToHost, st), "entries")) ||
+        (s = check(cudaStreamSynchronize(st), "entries")))
+        return s;
+    if (n > ctx->n_cap || E > ctx->e_cap) {
+        set_error("graph exceeds context capacity");
+        return GALA_ERR_CAPACITY;
+    }
+    bind_contract_buffers(ctx);
+    LevelGraph g{n, E, d_offsets, d_neighbors, d_weights};
+    int64_t newE = 0;
+    gala_status cs = GALA_OK;
+    int C = contract_run(g, d_community, ctx->cb, d_new_offsets, d_new_neighbors, d_new_weights, nullptr, 0, &newE,
+                         st, &cs, true);
+    if (C < 0) return cs;
+    // the reference rewrites the labels with the new ids (build_compressed_graph.cu:22-23)
+    if ((s = check(cudaMemcpyAsync(d_community, ctx->cb.lab, (size_t)n * sizeof(int32_t), cudaMemcpyDeviceToDevice,
+                                   st),
+                   "relabel")) ||
+        (s = check(cudaStreamSynchronize(st), "relabel")))
+        return s;
+    if (num_communities) *num_communities = C;
+    if (num_entries) *num_entries = newE;
+    return GALA_OK;
+}
+
+}  // extern "C"

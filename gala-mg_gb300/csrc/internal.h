@@ -1,0 +1,102 @@
+// internal.h - host-side declarations shared by the translation units of
+// libgala (not part of the public C ABI in include/gala.h).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/gala.h"
+
+// Host graph in the reference layout (src/graph/graph.h:7-19): inclusive
+// offsets without a leading 0; weights optional.
+struct gala_graph {
+    int32_t n = 0;
+    std::vector<int64_t> offs;  // n entries, inclusive prefix sums
+    std::vector<int32_t> nbr;   // offs[n-1] entries
+    std::vector<int32_t> w;     // empty when unweighted
+    bool weighted = false;
+    int64_t entries() const { return n ? offs[n - 1] : 0; }
+};
+
+namespace gala {
+
+// Error text of the last failure on this host thread.
+void set_error(const char *fmt, ...);
+void clear_error();
+gala_status cuda_fail(cudaError_t e, const char *what);
+void note_launch(int k);
+
+struct DevStats;
+
+// Device arrays of one phase-1 level (device layout CSR).
+struct LevelGraph {
+    int32_t n;
+    int64_t E;
+    const int64_t *offs;  // n+1, leading 0
+    const int32_t *nbr;
+    const int32_t *w;     // nullptr = unweighted
+};
+
+// Phase-1 workspace (all device pointers, sized for the context capacity).
+struct Phase1Buffers {
+    int32_t *comm, *K, *Self, *Tot, *size, *In;
+    int32_t *order;            // vertices grouped by degree bin
+    int32_t *act[2];           // active lists (bin segments as in order)
+    int32_t *mv_v, *mv_old, *mv_new;
+    int32_t *blockcnt;         // counting-sort scratch (kNumBinSlots * blocks)
+    int32_t *blockoff;
+    long long *scan_partial;
+    int32_t *hub_table;        // global hash tables of the largest bin
+    long long hub_table_slots; // capacity in int32 pairs
+    DevStats *stats;
+};
+
+// ---- phase 1 kernels (phase1.cu) ----
+void p1_level_init(const LevelGraph &g, Phase1Buffers &b, cudaStream_t st);
+void p1_iter_reset(Phase1Buffers &b, int next, int min_tot_init, cudaStream_t st);
+void p1_decide(const LevelGraph &g, Phase1Buffers &b, int bin, const int32_t *list,
+               const int *count_ptr, int level_count, double constant, int hub_tmax,
+               cudaStream_t st);
+void p1_apply_movers(Phase1Buffers &b, int sign, int n, cudaStream_t st);
+void p1_tot_reduce(Phase1Buffers &b, int n, cudaStream_t st);
+void p1_update(const LevelGraph &g, Phase1Buffers &b, int bin, const int32_t *list, int count, int next,
+               int bin_start, double constant, cudaStream_t st);
+void p1_level_init_rows(const LevelGraph &g, Phase1Buffers &b, const int *bin_start, cudaStream_t st);
+void p1_configure_kernels();
+void contract_configure_kernels();
+void p1_reset_level_stats(Phase1Buffers &b, cudaStream_t st);
+int hub_grid_size();
+
+// ---- contraction (contract.cu) ----
+struct ContractBuffers {
+    int32_t *cnt;        // n+1
+    int32_t *newid;      // n
+    int32_t *lab;        // n
+    int32_t *csz;        // n+1
+    int32_t *moff;       // n+1 member offsets
+    int32_t *cursor;     // n
+    int32_t *members;    // n
+    int32_t *mpos;       // n: member position of each vertex
+    long long *ec;       // n+1 edges per community
+    long long *medge;    // n+1 prefix of member degrees
+    int32_t *stream_key; // E
+    int32_t *stream_w;   // E
+    long long *tmp_off;  // n+1
+    int32_t *tmp_nbr;    // E
+    int32_t *tmp_w;      // E
+    int32_t *kc;         // n+1 distinct neighbours per community
+    int32_t *cls_list;   // n: communities by size class
+    int32_t *big_table;  // per-CTA global hash tables (class 2)
+    long long big_table_slots;
+    int32_t *big_bitmap; // per-CTA bitmaps over communities (class 2)
+    long long big_bitmap_words;
+    long long *scan_partial;
+    DevStats *stats;
+};
+int contract_run(const LevelGraph &g, const int32_t *comm, ContractBuffers &b, int64_t *new_offs,
+                 int32_t *new_nbr, int32_t *new_w, int32_t *orig_map, int32_t n_orig,
+                 int64_t *new_E, cudaStream_t st, gala_status *status, bool validate_labels = false);
+
+}  // namespace gala

@@ -1,0 +1,898 @@
+// phase1.cu - phase-1 kernels of the GB300 Louvain engine (sm_103a).
+//
+// One phase-1 iteration (louvain_main_process.cu:571-1034 in the reference):
+//   decide  : every active vertex aggregates the weights to its neighbour
+//             communities, picks the best gain (ties -> lowest id) and, when it
+//             moves, appends (v, old, new) to a mover list
+//   apply   : movers update comm, Tot and size with integer atomics
+//   reduce  : min over non-empty Tot and sum of Tot^2
+//   update  : In[v] (weight to the own community) for every vertex, the
+//             pruning bound, the next active lists and sum of In
+// All reads of a sweep see the previous iteration's labels (synchronous
+// semantics, as in the reference), so results do not depend on the order in
+// which vertices are processed.
+#include "common.cuh"
+#include "internal.h"
+#include "scan.cuh"
+
+namespace gala {
+
+static int g_num_sms = 0;
+static int num_sms()
+{
+    if (g_num_sms == 0) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev);
+        if (g_num_sms <= 0) g_num_sms = 148;
+    }
+    return g_num_sms;
+}
+int hub_grid_size() { return num_sms(); }
+
+constexpr int kCountBlock = 1024;
+
+// ------------------------------------------------------------------------
+// Block reductions into the device counters (all threads must call).
+// ------------------------------------------------------------------------
+__device__ __forceinline__ void block_add_u64(unsigned long long v, unsigned long long *dst)
+{
+    __shared__ unsigned long long red[32];
+    v = warp_sum(v);
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (lane == 0) red[wid] = v;
+    __syncthreads();
+    if (wid == 0) {
+        unsigned long long t = lane < (int)(blockDim.x >> 5) ? red[lane] : 0ull;
+        t = warp_sum(t);
+        if (lane == 0 && t) atomicAdd(dst, t);
+    }
+    __syncthreads();
+}
+
+__device__ __forceinline__ void block_add_i32(int v, int *dst)
+{
+    __shared__ int red[32];
+    v = warp_sum(v);
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (lane == 0) red[wid] = v;
+    __syncthreads();
+    if (wid == 0) {
+        int t = lane < (int)(blockDim.x >> 5) ? red[lane] : 0;
+        t = warp_sum(t);
+        if (lane == 0 && t) atomicAdd(dst, t);
+    }
+    __syncthreads();
+}
+
+// ------------------------------------------------------------------------
+// Level init: labels = own id, size 1 (louvain_main_process.cu:323-353),
+// then a stable counting sort of the vertices into degree bins (the reference
+// uses 8 count_if + a radix sort_by_key, :298-375).
+// ------------------------------------------------------------------------
+__global__ void k_init_vertices(int n, int32_t *comm, int32_t *K, int32_t *Self, int32_t *Tot,
+                                int32_t *size, int32_t *In)
+{
+    for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) {
+        comm[v] = v;
+        size[v] = 1;
+        K[v] = 0;
+        Self[v] = 0;
+        Tot[v] = 0;
+        In[v] = 0;
+    }
+}
+
+__global__ void __launch_bounds__(kCountBlock) k_bin_count(int n, const int64_t *__restrict__ offs,
+                                                           int32_t *blockcnt, int nblk, DevStats *st)
+{
+    __shared__ int cnt[kNumBinSlots];
+    if (threadIdx.x < kNumBinSlots) cnt[threadIdx.x] = 0;
+    __syncthreads();
+    int v = blockIdx.x * kCountBlock + threadIdx.x;
+    int deg = 0;
+    if (v < n) {
+        deg = (int)(offs[v + 1] - offs[v]);
+        atomicAdd(&cnt[bin_of_degree(deg)], 1);
+    }
+#pragma unroll
+    for (int o = 16; o >= 1; o >>= 1) deg = max(deg, __shfl_xor_sync(GALA_FULL_MASK, deg, o));
+    if ((threadIdx.x & 31) == 0 && deg > 0) atomicMax(&st->max_deg, deg);
+    __syncthreads();
+    if (threadIdx.x < kNumBinSlots) blockcnt[threadIdx.x * nblk + blockIdx.x] = cnt[threadIdx.x];
+}
+
+__global__ void __launch_bounds__(kCountBlock) k_bin_scatter(int n, const int64_t *__restrict__ offs,
+                                                             const int32_t *__restrict__ blockoff, int nblk,
+                                                             int32_t *order, DevStats *st)
+{
+    __shared__ int wcnt[kCountBlock / 32][kNumBinSlots];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    int v = blockIdx.x * kCountBlock + threadIdx.x;
+    int b = -1;
+    if (v < n) b = bin_of_degree(offs[v + 1] - offs[v]);
+    unsigned mine = 0;
+#pragma unroll
+    for (int bb = 0; bb < kNumBinSlots; ++bb) {
+        unsigned bal = __ballot_sync(GALA_FULL_MASK, b == bb);
+        if (b == bb) mine = bal;
+        if (lane == 0) wcnt[wid][bb] = __popc(bal);
+    }
+    __syncthreads();
+    if (threadIdx.x < kNumBinSlots) {
+        int acc = 0;
+        for (int w = 0; w < kCountBlock / 32; ++w) {
+            int t = wcnt[w][threadIdx.x];
+            wcnt[w][threadIdx.x] = acc;
+            acc += t;
+        }
+    }
+    __syncthreads();
+    if (b >= 0) order[blockoff[b * nblk + blockIdx.x] + wcnt[wid][b] + __popc(mine & lanemask_lt())] = v;
+    if (blockIdx.x == 0 && threadIdx.x <= kNumBinSlots)
+        st->bin_start[threadIdx.x] = threadIdx.x < kNumBinSlots ? blockoff[threadIdx.x * nblk] : n;
+}
+
+// K = row weight sum, Self = self-loop weight (init_communities,
+// kernel_functions.cu:34-73); Tot = K, In = Self.  Accumulates sum(K),
+// sum(K^2) and sum(Self) for the modularity of the singleton partition.
+template <int G, bool W>
+__global__ void __launch_bounds__(256) k_init_rows_group(const int32_t *__restrict__ list, int count,
+                                                         const int64_t *__restrict__ offs,
+                                                         const int32_t *__restrict__ nbr,
+                                                         const int32_t *__restrict__ w, int32_t *K,
+                                                         int32_t *Self, int32_t *Tot, int32_t *In,
+                                                         DevStats *st)
+{
+    const int lane = threadIdx.x & 31, sub = lane & (G - 1), gw = lane / G;
+    constexpr int GPW = 32 / G;
+    const int wg = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nw = (gridDim.x * blockDim.x) >> 5;
+    unsigned long long sk = 0, sk2 = 0, ss = 0;
+    for (int base = wg * GPW; base < count; base += nw * GPW) {
+        const int idx = base + gw;
+        const bool has = idx < count;
+        int v = 0;
+        long long s = 0, e = 0;
+        if (has) {
+            v = list[idx];
+            s = offs[v];
+            e = offs[v + 1];
+        }
+        int k = 0, sf = 0;
+        for (long long j = s + sub; j < e; j += G) {
+            int wt = W ? w[j] : 1;
+            k += wt;
+            if (nbr[j] == v) sf = wt;
+        }
+#pragma unroll
+        for (int o = G / 2; o >= 1; o >>= 1) {
+            k += __shfl_xor_sync(GALA_FULL_MASK, k, o);
+            sf += __shfl_xor_sync(GALA_FULL_MASK, sf, o);
+        }
+        if (has && sub == 0) {
+            K[v] = k;
+            Tot[v] = k;
+            Self[v] = sf;
+            In[v] = sf;
+            sk += (unsigned long long)k;
+            sk2 += (unsigned long long)((long long)k * k);
+            ss += (unsigned long long)sf;
+        }
+    }
+    block_add_u64(sk, &st->sum_k);
+    block_add_u64(sk2, &st->sum_tot2);
+    block_add_u64(ss, &st->sum_in);
+}
+
+template <bool W>
+__global__ void __launch_bounds__(256) k_init_rows_cta(const int32_t *__restrict__ list, int count,
+                                                       const int64_t *__restrict__ offs,
+                                                       const int32_t *__restrict__ nbr,
+                                                       const int32_t *__restrict__ w, int32_t *K, int32_t *Self,
+                                                       int32_t *Tot, int32_t *In, DevStats *st)
+{
+    __shared__ int rk[8], rs[8];
+    unsigned long long sk = 0, sk2 = 0, ss = 0;
+    for (int i = blockIdx.x; i < count; i += gridDim.x) {
+        int v = list[i];
+        long long s = offs[v], e = offs[v + 1];
+        int k = 0, sf = 0;
+        for (long long j = s + threadIdx.x; j < e; j += blockDim.x) {
+            int wt = W ? w[j] : 1;
+            k += wt;
+            if (nbr[j] == v) sf = wt;
+        }
+        k = warp_sum(k);
+        sf = warp_sum(sf);
+        if ((threadIdx.x & 31) == 0) {
+            rk[threadIdx.x >> 5] = k;
+            rs[threadIdx.x >> 5] = sf;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            k = 0;
+            sf = 0;
+            for (int q = 0; q < (int)(blockDim.x >> 5); ++q) {
+                k += rk[q];
+                sf += rs[q];
+            }
+            K[v] = k;
+            Tot[v] = k;
+            Self[v] = sf;
+            In[v] = sf;
+            sk += (unsigned long long)k;
+            sk2 += (unsigned long long)((long long)k * k);
+            ss += (unsigned long long)sf;
+        }
+        __syncthreads();
+    }
+    block_add_u64(sk, &st->sum_k);
+    block_add_u64(sk2, &st->sum_tot2);
+    block_add_u64(ss, &st->sum_in);
+}
+
+__global__ void k_reset_level_stats(DevStats *st)
+{
+    st->sum_in = 0;
+    st->sum_tot2 = 0;
+    st->sum_self = 0;
+    st->sum_k = 0;
+    st->max_deg = 0;
+    st->err = 0;
+    st->n_movers = 0;
+}
+
+void p1_reset_level_stats(Phase1Buffers &b, cudaStream_t st)
+{
+    k_reset_level_stats<<<1, 1, 0, st>>>(b.stats);
+    note_launch(1);
+}
+
+static void launch_init_rows(const LevelGraph &g, Phase1Buffers &b, int bin, const int32_t *list, int cnt,
+                             cudaStream_t st)
+{
+    if (cnt <= 0) return;
+    const bool W = g.w != nullptr;
+    const int cap = num_sms() * 8;
+    auto grid_for = [&](int G) {
+        long long blocks = ((long long)cnt * G + 255) / 256;
+        return (int)(blocks < cap ? blocks : cap);
+    };
+#define GALA_INIT_GROUP(GV)                                                                            \
+    do {                                                                                               \
+        if (W)                                                                                         \
+            k_init_rows_group<GV, true><<<grid_for(GV), 256, 0, st>>>(list, cnt, g.offs, g.nbr, g.w,   \
+                                                                      b.K, b.Self, b.Tot, b.In,        \
+                                                                      b.stats);                        \
+        else                                                                                           \
+            k_init_rows_group<GV, false><<<grid_for(GV), 256, 0, st>>>(list, cnt, g.offs, g.nbr, g.w,  \
+                                                                       b.K, b.Self, b.Tot, b.In,       \
+                                                                       b.stats);                       \
+    } while (0)
+    switch (bin) {
+    case 0: GALA_INIT_GROUP(4); break;
+    case 1: GALA_INIT_GROUP(8); break;
+    case 2: GALA_INIT_GROUP(16); break;
+    case 3:
+    case 4:
+    case 5: GALA_INIT_GROUP(32); break;
+    default: {
+        int grid = cnt < cap ? cnt : cap;
+        if (W)
+            k_init_rows_cta<true><<<grid, 256, 0, st>>>(list, cnt, g.offs, g.nbr, g.w, b.K, b.Self, b.Tot,
+                                                        b.In, b.stats);
+        else
+            k_init_rows_cta<false><<<grid, 256, 0, st>>>(list, cnt, g.offs, g.nbr, g.w, b.K, b.Self, b.Tot,
+                                                         b.In, b.stats);
+    }
+    }
+#undef GALA_INIT_GROUP
+    note_launch(1);
+}
+
+// Level init part 1: labels/sizes, degree-bin counting sort.  The caller reads
+// bin_start back before calling p1_level_init_rows.
+void p1_level_init(const LevelGraph &g, Phase1Buffers &b, cudaStream_t st)
+{
+    const int n = g.n;
+    const int nblk = (n + kCountBlock - 1) / kCountBlock;
+    k_init_vertices<<<(n + 255) / 256 < 4096 ? (n + 255) / 256 : 4096, 256, 0, st>>>(n, b.comm, b.K, b.Self,
+                                                                                     b.Tot, b.size, b.In);
+    k_bin_count<<<nblk, kCountBlock, 0, st>>>(n, g.offs, b.blockcnt, nblk, b.stats);
+    exclusive_scan(b.blockcnt, b.blockoff, (long long)kNumBinSlots * nblk, OpIdentity(), b.scan_partial,
+                   &b.stats->total, st);
+    k_bin_scatter<<<nblk, kCountBlock, 0, st>>>(n, g.offs, b.blockoff, nblk, b.order, b.stats);
+    note_launch(3);
+}
+
+void p1_level_init_rows(const LevelGraph &g, Phase1Buffers &b, const int *bin_start, cudaStream_t st)
+{
+    for (int bin = 0; bin < kNumBins; ++bin)
+        launch_init_rows(g, b, bin, b.order + bin_start[bin], bin_start[bin + 1] - bin_start[bin], st);
+}
+
+// ------------------------------------------------------------------------
+// Decide-and-move
+// ------------------------------------------------------------------------
+struct DecideArgs {
+    const int64_t *__restrict__ offs;
+    const int32_t *__restrict__ nbr;
+    const int32_t *__restrict__ w;
+    const int32_t *__restrict__ comm;
+    const int32_t *__restrict__ K;
+    const int32_t *__restrict__ Self;
+    const int32_t *__restrict__ Tot;
+    const int32_t *__restrict__ size;
+    int32_t *mv_v, *mv_old, *mv_new;
+    DevStats *st;
+    double constant;
+};
+
+// Final decision of a vertex (kernel_functions.cu:381-409): move only for a
+// positive corrected gain, and never swap two singletons towards the larger
+// id (the guard at :386).
+__device__ __forceinline__ bool decide_move(const DecideArgs &a, int cur, int best, double maxdq, int w_cur,
+                                            int self_w)
+{
+    if (best == cur) return false;
+    if (!(gain_correct(maxdq, w_cur, self_w) > 0.0)) return false;
+    if (a.size[best] == 1 && a.size[cur] == 1 && best > cur) return false;
+    return true;
+}
+
+__device__ __forceinline__ void append_mover(const DecideArgs &a, bool move, int v, int cur, int best)
+{
+    unsigned b = __ballot_sync(GALA_FULL_MASK, move);
+    if (b == 0) return;
+    const int lane = threadIdx.x & 31;
+    const int leader = __ffs(b) - 1;
+    int base = 0;
+    if (lane == leader) base = atomicAdd(&a.st->n_movers, __popc(b));
+    base = __shfl_sync(GALA_FULL_MASK, base, leader);
+    if (move) {
+        int p = base + __popc(b & lanemask_lt());
+        a.mv_v[p] = v;
+        a.mv_old[p] = cur;
+        a.mv_new[p] = best;
+    }
+}
+
+// Degree <= G: one lane per neighbour.  Lanes holding the same neighbour
+// community are found with __match_any_sync (the key carries the group index
+// so groups of one warp stay apart) and their weights summed with
+// __reduce_add_sync; the lowest lane of each set evaluates the gain.
+template <int G, bool W>
+__global__ void __launch_bounds__(256) k_decide_group(DecideArgs a, const int32_t *__restrict__ list,
+                                                      const int *__restrict__ count_ptr)
+{
+    const int lane = threadIdx.x & 31, sub = lane & (G - 1), gw = lane / G;
+    constexpr int GPW = 32 / G;
+    const int count = *count_ptr;
+    const int wg = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nw = (gridDim.x * blockDim.x) >> 5;
+    for (int base = wg * GPW; base < count; base += nw * GPW) {
+        const int idx = base + gw;
+        const bool has = idx < count;
+        int v = 0, cur = -1, deg = 0, ki = 0, sf = 0, tcur = 0;
+        long long s = 0;
+        if (has) {
+            v = list[idx];
+            s = a.offs[v];
+            deg = (int)(a.offs[v + 1] - s);
+            cur = a.comm[v];
+            ki = a.K[v];
+            sf = a.Self[v];
+            tcur = a.Tot[cur];
+        }
+        const bool valid = has && sub < deg;
+        int c = -1, wt = 0;
+        if (valid) {
+            c = a.comm[a.nbr[s + sub]];
+            wt = W ? a.w[s + sub] : 1;
+        }
+        const unsigned long long key = ((unsigned long long)(unsigned)gw << 32) | (unsigned)c;
+        const unsigned m = __match_any_sync(GALA_FULL_MASK, key);
+        const int wsum = W ? (int)__reduce_add_sync(m, (unsigned)wt) : __popc(m);
+        const bool leader = valid && (__ffs(m) - 1 == lane);
+        int wc = (leader && c == cur) ? wsum : 0;
+        double dq = 0.0;
+        int bc = cur;
+        if (leader && c != cur) {
+            double d = gain_dq(wsum, ki, a.Tot[c], tcur, a.constant);
+            if (d > 0.0) {
+                dq = d;
+                bc = c;
+            }
+        }
+#pragma unroll
+        for (int o = G / 2; o >= 1; o >>= 1) {
+            double od = __shfl_xor_sync(GALA_FULL_MASK, dq, o);
+            int oc = __shfl_xor_sync(GALA_FULL_MASK, bc, o);
+            wc += __shfl_xor_sync(GALA_FULL_MASK, wc, o);
+            if (cand_better(od, oc, dq, bc)) {
+                dq = od;
+                bc = oc;
+            }
+        }
+        bool move = has && sub == 0 && decide_move(a, cur, bc, dq, wc, sf);
+        append_mover(a, move, v, cur, bc);
+    }
+}
+
+// Scan a hash table and return this thread's best candidate and its share of
+// the weight to the own community.
+__device__ __forceinline__ void scan_table(const DecideArgs &a, const int *keys, const int *vals, int T,
+                                           int first, int stride, int cur, int ki, int tcur, double &dq,
+                                           int &bc, int &wc)
+{
+    for (int j = first; j < T; j += stride) {
+        int c = keys[j];
+        if (c < 0) continue;
+        int wv = vals[j];
+        if (c == cur) {
+            wc += wv;
+        } else {
+            double d = gain_dq(wv, ki, a.Tot[c], tcur, a.constant);
+            if (d > 0.0 && cand_better(d, c, dq, bc)) {
+                dq = d;
+                bc = c;
+            }
+        }
+    }
+}
+
+__device__ __forceinline__ void warp_argmax(double &dq, int &bc, int &wc)
+{
+#pragma unroll
+    for (int o = 16; o >= 1; o >>= 1) {
+        double od = __shfl_xor_sync(GALA_FULL_MASK, dq, o);
+        int oc = __shfl_xor_sync(GALA_FULL_MASK, bc, o);
+        wc += __shfl_xor_sync(GALA_FULL_MASK, wc, o);
+        if (cand_better(od, oc, dq, bc)) {
+            dq = od;
+            bc = oc;
+        }
+    }
+}
+
+// Degree 33-256: one warp per vertex with a private shared-memory hash table.
+constexpr int kWarpTable = 512;
+template <bool W>
+__global__ void __launch_bounds__(256) k_decide_warp(DecideArgs a, const int32_t *__restrict__ list,
+                                                     const int *__restrict__ count_ptr)
+{
+    __shared__ int s_keys[8][kWarpTable];
+    __shared__ int s_vals[8][kWarpTable];
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    int *keys = s_keys[wib];
+    int *vals = s_vals[wib];
+    const int count = *count_ptr;
+    const int wg = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nw = (gridDim.x * blockDim.x) >> 5;
+    for (int i = wg; i < count; i += nw) {
+        const int v = list[i];
+        const long long s = a.offs[v];
+        const int deg = (int)(a.offs[v + 1] - s);
+        const int cur = a.comm[v];
+        int T = next_pow2_int(2LL * deg);
+        if (T < 64) T = 64;
+        if (T > kWarpTable) T = kWarpTable;
+        const int lg = __ffs(T) - 1;
+        for (int j = lane; j < T; j += 32) {
+            keys[j] = -1;
+            vals[j] = 0;
+        }
+        __syncwarp();
+        for (int e0 = 0; e0 < deg; e0 += 32) {
+            const int e = e0 + lane;
+            const bool valid = e < deg;
+            int c = -1, wt = 0;
+            if (valid) {
+                c = a.comm[a.nbr[s + e]];
+                wt = W ? a.w[s + e] : 1;
+            }
+            const unsigned m = __match_any_sync(GALA_FULL_MASK, c);
+            const int wsum = W ? (int)__reduce_add_sync(m, (unsigned)wt) : __popc(m);
+            if (valid && __ffs(m) - 1 == lane)
+                if (!hash_add(keys, vals, T, lg, c, wsum)) atomicOr(&a.st->err, kErrHashOverflow);
+        }
+        __syncwarp();
+        const int ki = a.K[v], tcur = a.Tot[cur], sf = a.Self[v];
+        double dq = 0.0;
+        int bc = cur, wc = 0;
+        scan_table(a, keys, vals, T, lane, 32, cur, ki, tcur, dq, bc, wc);
+        warp_argmax(dq, bc, wc);
+        bool move = lane == 0 && decide_move(a, cur, bc, dq, wc, sf);
+        append_mover(a, move, v, cur, bc);
+        __syncwarp();
+    }
+}
+
+// Degree > 256: one CTA per vertex; the hash table lives in dynamic shared
+// memory (GMEM = false) or in a per-CTA slice of global memory (GMEM = true,
+// hub vertices; the slice stays in L2).
+template <int BLOCK, bool GMEM, bool W>
+__global__ void __launch_bounds__(BLOCK) k_decide_cta(DecideArgs a, const int32_t *__restrict__ list,
+                                                      const int *__restrict__ count_ptr, int tmax,
+                                                      int32_t *gtab)
+{
+    extern __shared__ int dyn_smem[];
+    __shared__ double r_dq[BLOCK / 32];
+    __shared__ int r_c[BLOCK / 32];
+    __shared__ int r_w[BLOCK / 32];
+    int *keys = GMEM ? gtab + (long long)blockIdx.x * 2 * tmax : dyn_smem;
+    int *vals = keys + tmax;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int count = *count_ptr;
+    for (int i = blockIdx.x; i < count; i += gridDim.x) {
+        const int v = list[i];
+        const long long s = a.offs[v];
+        const long long e = a.offs[v + 1];
+        const int deg = (int)(e - s);
+        const int cur = a.comm[v];
+        int T = next_pow2_int(2LL * deg);
+        if (T < 64) T = 64;
+        if (T > tmax) {  // cannot happen for the bin limits; recorded, vertex stays
+            if (threadIdx.x == 0) atomicOr(&a.st->err, kErrHashOverflow);
+            continue;
+        }
+        const int lg = __ffs(T) - 1;
+        for (int j = threadIdx.x; j < T; j += BLOCK) {
+            keys[j] = -1;
+            vals[j] = 0;
+        }
+        __syncthreads();
+        for (long long b0 = s; b0 < e; b0 += BLOCK) {
+            const long long j = b0 + threadIdx.x;
+            const bool valid = j < e;
+            int c = -1, wt = 0;
+            if (valid) {
+                c = a.comm[a.nbr[j]];
+                wt = W ? a.w[j] : 1;
+            }
+            const unsigned m = __match_any_sync(GALA_FULL_MASK, c);
+            const int wsum = W ? (int)__reduce_add_sync(m, (unsigned)wt) : __popc(m);
+            if (valid && __ffs(m) - 1 == lane)
+                if (!hash_add(keys, vals, T, lg, c, wsum)) atomicOr(&a.st->err, kErrHashOverflow);
+        }
+        __syncthreads();
+        const int ki = a.K[v], tcur = a.Tot[cur], sf = a.Self[v];
+        double dq = 0.0;
+        int bc = cur, wc = 0;
+        scan_table(a, keys, vals, T, threadIdx.x, BLOCK, cur, ki, tcur, dq, bc, wc);
+        warp_argmax(dq, bc, wc);
+        if (lane == 0) {
+            r_dq[wid] = dq;
+            r_c[wid] = bc;
+            r_w[wid] = wc;
+        }
+        __syncthreads();
+        if (wid == 0) {
+            dq = lane < BLOCK / 32 ? r_dq[lane] : 0.0;
+            bc = lane < BLOCK / 32 ? r_c[lane] : cur;
+            wc = lane < BLOCK / 32 ? r_w[lane] : 0;
+            warp_argmax(dq, bc, wc);
+            bool move = lane == 0 && decide_move(a, cur, bc, dq, wc, sf);
+            append_mover(a, move, v, cur, bc);
+        }
+        __syncthreads();
+    }
+}
+
+constexpr int kCtaTable5 = 4096;
+constexpr int kCtaTable6 = 16384;
+
+void p1_decide(const LevelGraph &g, Phase1Buffers &b, int bin, const int32_t *list, const int *count_ptr,
+               int level_count, double constant, int hub_tmax, cudaStream_t st)
+{
+    if (level_count <= 0) return;
+    DecideArgs a;
+    a.offs = g.offs;
+    a.nbr = g.nbr;
+    a.w = g.w;
+    a.comm = b.comm;
+    a.K = b.K;
+    a.Self = b.Self;
+    a.Tot = b.Tot;
+    a.size = b.size;
+    a.mv_v = b.mv_v;
+    a.mv_old = b.mv_old;
+    a.mv_new = b.mv_new;
+    a.st = b.stats;
+    a.constant = constant;
+    const bool W = g.w != nullptr;
+    const int cap = num_sms() * 8;
+    auto grid_lanes = [&](int lanes_per_item) {
+        long long blocks = ((long long)level_count * lanes_per_item + 255) / 256;
+        return (int)(blocks < cap ? blocks : cap);
+    };
+#define GALA_DG(GV)                                                                                    \
+    do {                                                                                               \
+        if (W)                                                                                         \
+            k_decide_group<GV, true><<<grid_lanes(GV), 256, 0, st>>>(a, list, count_ptr);              \
+        else                                                                                           \
+            k_decide_group<GV, false><<<grid_lanes(GV), 256, 0, st>>>(a, list, count_ptr);             \
+    } while (0)
+    switch (bin) {
+    case 0: GALA_DG(4); break;
+    case 1: GALA_DG(8); break;
+    case 2: GALA_DG(16); break;
+    case 3: GALA_DG(32); break;
+    case 4:
+        if (W)
+            k_decide_warp<true><<<grid_lanes(32), 256, 0, st>>>(a, list, count_ptr);
+        else
+            k_decide_warp<false><<<grid_lanes(32), 256, 0, st>>>(a, list, count_ptr);
+        break;
+    case 5: {
+        int grid = level_count < num_sms() * 6 ? level_count : num_sms() * 6;
+        size_t sm = (size_t)kCtaTable5 * 2 * sizeof(int);
+        if (W)
+            k_decide_cta<256, false, true><<<grid, 256, sm, st>>>(a, list, count_ptr, kCtaTable5, nullptr);
+        else
+            k_decide_cta<256, false, false><<<grid, 256, sm, st>>>(a, list, count_ptr, kCtaTable5, nullptr);
+        break;
+    }
+    case 6: {
+        int grid = level_count < num_sms() ? level_count : num_sms();
+        size_t sm = (size_t)kCtaTable6 * 2 * sizeof(int);
+        if (W)
+            k_decide_cta<1024, false, true><<<grid, 1024, sm, st>>>(a, list, count_ptr, kCtaTable6, nullptr);
+        else
+            k_decide_cta<1024, false, false><<<grid, 1024, sm, st>>>(a, list, count_ptr, kCtaTable6, nullptr);
+        break;
+    }
+    default: {
+        long long grid = level_count < hub_grid_size() ? level_count : hub_grid_size();
+        const long long fit = b.hub_table_slots / (2LL * hub_tmax);
+        if (grid > fit) grid = fit;
+        if (grid < 1) return;  // the caller checked that one table fits
+        if (W)
+            k_decide_cta<1024, true, true><<<grid, 1024, 0, st>>>(a, list, count_ptr, hub_tmax, b.hub_table);
+        else
+            k_decide_cta<1024, true, false><<<grid, 1024, 0, st>>>(a, list, count_ptr, hub_tmax, b.hub_table);
+    }
+    }
+#undef GALA_DG
+    note_launch(1);
+}
+
+void p1_configure_kernels()
+{
+    cudaFuncSetAttribute(k_decide_cta<1024, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         kCtaTable6 * 2 * (int)sizeof(int));
+    cudaFuncSetAttribute(k_decide_cta<1024, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         kCtaTable6 * 2 * (int)sizeof(int));
+}
+
+// ------------------------------------------------------------------------
+// Apply (sign = +1) or revert (sign = -1) the movers of an iteration
+// (Tot += Tot_update, size += size_update, louvain_main_process.cu:949-953).
+// ------------------------------------------------------------------------
+__global__ void k_apply_movers(const int32_t *__restrict__ mv_v, const int32_t *__restrict__ mv_old,
+                               const int32_t *__restrict__ mv_new, const DevStats *__restrict__ stp, int sign,
+                               int32_t *comm, int32_t *Tot, int32_t *size, const int32_t *__restrict__ K)
+{
+    const int nm = stp->n_movers;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nm; i += gridDim.x * blockDim.x) {
+        const int v = mv_v[i];
+        const int from = sign > 0 ? mv_old[i] : mv_new[i];
+        const int to = sign > 0 ? mv_new[i] : mv_old[i];
+        const int k = K[v];
+        comm[v] = to;
+        atomicAdd(&Tot[to], k);
+        atomicSub(&Tot[from], k);
+        atomicAdd(&size[to], 1);
+        atomicSub(&size[from], 1);
+    }
+}
+
+void p1_apply_movers(Phase1Buffers &b, int sign, int n, cudaStream_t st)
+{
+    int grid = (n + 255) / 256;
+    int cap = num_sms() * 4;
+    if (grid > cap) grid = cap;
+    if (grid < 1) grid = 1;
+    k_apply_movers<<<grid, 256, 0, st>>>(b.mv_v, b.mv_old, b.mv_new, b.stats, sign, b.comm, b.Tot, b.size, b.K);
+    note_launch(1);
+}
+
+// min over non-empty Tot (Tot_op, kernel_functions.cuh:112-121) and sum Tot^2.
+__global__ void k_tot_reduce(const int32_t *__restrict__ Tot, int n, DevStats *st)
+{
+    int mn = 0x7fffffff;
+    unsigned long long s2 = 0;
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x) {
+        int t = Tot[c];
+        if (t != 0) {
+            mn = min(mn, t);
+            s2 += (unsigned long long)((long long)t * t);
+        }
+    }
+#pragma unroll
+    for (int o = 16; o >= 1; o >>= 1) mn = min(mn, __shfl_xor_sync(GALA_FULL_MASK, mn, o));
+    if ((threadIdx.x & 31) == 0 && mn != 0x7fffffff) atomicMin(&st->min_tot, mn);
+    block_add_u64(s2, &st->sum_tot2);
+}
+
+void p1_tot_reduce(Phase1Buffers &b, int n, cudaStream_t st)
+{
+    int grid = (n + 1023) / 1024;
+    int cap = num_sms() * 4;
+    if (grid > cap) grid = cap;
+    if (grid < 1) grid = 1;
+    k_tot_reduce<<<grid, 1024, 0, st>>>(b.Tot, n, b.stats);
+    note_launch(1);
+}
+
+__global__ void k_iter_reset(DevStats *st, int next, int min_tot_init)
+{
+    st->n_movers = 0;
+    st->sum_in = 0;
+    st->sum_tot2 = 0;
+    st->min_tot = min_tot_init;
+    st->act_edges[next] = 0;
+    st->act_vertices[next] = 0;
+    for (int i = 0; i < kNumBins; ++i) st->act_count[next][i] = 0;
+}
+
+void p1_iter_reset(Phase1Buffers &b, int next, int min_tot_init, cudaStream_t st)
+{
+    k_iter_reset<<<1, 1, 0, st>>>(b.stats, next, min_tot_init);
+    note_launch(1);
+}
+
+// ------------------------------------------------------------------------
+// Weight update + pruning (compute_In / compute_In_blk,
+// kernel_functions.cu:890-1034): In[v] over the new labels, the pruning
+// bound, next active lists, sum of In.
+// ------------------------------------------------------------------------
+struct UpdateArgs {
+    const int64_t *__restrict__ offs;
+    const int32_t *__restrict__ nbr;
+    const int32_t *__restrict__ w;
+    const int32_t *__restrict__ comm;
+    const int32_t *__restrict__ K;
+    const int32_t *__restrict__ Self;
+    const int32_t *__restrict__ Tot;
+    int32_t *In;
+    int32_t *act_list;  // next active list, segment of this bin
+    int *act_counter;
+    DevStats *st;
+    double constant;
+    int next;
+};
+
+template <int G, bool W>
+__global__ void __launch_bounds__(256) k_update_group(UpdateArgs a, const int32_t *__restrict__ list, int count)
+{
+    const int lane = threadIdx.x & 31, sub = lane & (G - 1), gw = lane / G;
+    constexpr int GPW = 32 / G;
+    const int wg = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nw = (gridDim.x * blockDim.x) >> 5;
+    const int min_tot = a.st->min_tot;
+    unsigned long long s_in = 0, s_edges = 0;
+    int s_act = 0;
+    for (int base = wg * GPW; base < count; base += nw * GPW) {
+        const int idx = base + gw;
+        const bool has = idx < count;
+        int v = 0, cur = -1;
+        long long s = 0, e = 0;
+        if (has) {
+            v = list[idx];
+            s = a.offs[v];
+            e = a.offs[v + 1];
+            cur = a.comm[v];
+        }
+        int sum = 0;
+        for (long long j = s + sub; j < e; j += G)
+            if (a.comm[a.nbr[j]] == cur) sum += W ? a.w[j] : 1;
+#pragma unroll
+        for (int o = G / 2; o >= 1; o >>= 1) sum += __shfl_xor_sync(GALA_FULL_MASK, sum, o);
+        bool active = false;
+        if (has && sub == 0) {
+            a.In[v] = sum;
+            const int ki = a.K[v];
+            active = !prune_bound(sum, a.Self[v], ki, min_tot, a.Tot[cur], a.constant);
+            s_in += (unsigned long long)sum;
+            if (active) {
+                s_edges += (unsigned long long)(e - s);
+                s_act += 1;
+            }
+        }
+        warp_append(active, v, a.act_list, a.act_counter);
+    }
+    block_add_u64(s_in, &a.st->sum_in);
+    block_add_u64(s_edges, &a.st->act_edges[a.next]);
+    block_add_i32(s_act, &a.st->act_vertices[a.next]);
+}
+
+template <bool W>
+__global__ void __launch_bounds__(256) k_update_cta(UpdateArgs a, const int32_t *__restrict__ list, int count)
+{
+    __shared__ int red[8];
+    const int min_tot = a.st->min_tot;
+    unsigned long long s_in = 0, s_edges = 0;
+    int s_act = 0;
+    for (int i = blockIdx.x; i < count; i += gridDim.x) {
+        const int v = list[i];
+        const long long s = a.offs[v], e = a.offs[v + 1];
+        const int cur = a.comm[v];
+        int sum = 0;
+        for (long long j = s + threadIdx.x; j < e; j += blockDim.x)
+            if (a.comm[a.nbr[j]] == cur) sum += W ? a.w[j] : 1;
+        sum = warp_sum(sum);
+        if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = sum;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            sum = 0;
+            for (int q = 0; q < (int)(blockDim.x >> 5); ++q) sum += red[q];
+            a.In[v] = sum;
+            const int ki = a.K[v];
+            bool active = !prune_bound(sum, a.Self[v], ki, min_tot, a.Tot[cur], a.constant);
+            s_in += (unsigned long long)sum;
+            if (active) {
+                a.act_list[atomicAdd(a.act_counter, 1)] = v;
+                s_edges += (unsigned long long)(e - s);
+                s_act += 1;
+            }
+        }
+        __syncthreads();
+    }
+    block_add_u64(s_in, &a.st->sum_in);
+    block_add_u64(s_edges, &a.st->act_edges[a.next]);
+    block_add_i32(s_act, &a.st->act_vertices[a.next]);
+}
+
+void p1_update(const LevelGraph &g, Phase1Buffers &b, int bin, const int32_t *list, int count, int next,
+               int bin_start, double constant, cudaStream_t st)
+{
+    if (count <= 0) return;
+    UpdateArgs a;
+    a.offs = g.offs;
+    a.nbr = g.nbr;
+    a.w = g.w;
+    a.comm = b.comm;
+    a.K = b.K;
+    a.Self = b.Self;
+    a.Tot = b.Tot;
+    a.In = b.In;
+    a.act_list = b.act[next] + bin_start;
+    a.act_counter = &b.stats->act_count[next][bin];
+    a.st = b.stats;
+    a.constant = constant;
+    a.next = next;
+    const bool W = g.w != nullptr;
+    const int cap = num_sms() * 8;
+    auto grid_lanes = [&](int G) {
+        long long blocks = ((long long)count * G + 255) / 256;
+        return (int)(blocks < cap ? blocks : cap);
+    };
+#define GALA_UG(GV)                                                                                    \
+    do {                                                                                               \
+        if (W)                                                                                         \
+            k_update_group<GV, true><<<grid_lanes(GV), 256, 0, st>>>(a, list, count);                  \
+        else                                                                                           \
+            k_update_group<GV, false><<<grid_lanes(GV), 256, 0, st>>>(a, list, count);                 \
+    } while (0)
+    switch (bin) {
+    case 0: GALA_UG(4); break;
+    case 1: GALA_UG(8); break;
+    case 2: GALA_UG(16); break;
+    case 3:
+    case 4:
+    case 5: GALA_UG(32); break;
+    default: {
+        int grid = count < cap ? count : cap;
+        if (W)
+            k_update_cta<true><<<grid, 256, 0, st>>>(a, list, count);
+        else
+            k_update_cta<false><<<grid, 256, 0, st>>>(a, list, count);
+    }
+    }
+#undef GALA_UG
+    note_launch(1);
+}
+
+}  // namespace gala

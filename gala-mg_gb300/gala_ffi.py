@@ -1,0 +1,273 @@
+"""ctypes binding of libgala.so (the C ABI in include/gala.h).
+
+This is the Python face of the engine used by the tests and bench.py; it
+mirrors the reference's entry points (louvain_gpu, louvain_main_process,
+build_compressed_graph) through the C ABI.  There is no Python or CPU
+fallback: if libgala.so is missing, loading fails with an error.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG, "_build", "libgala.so")
+
+GALA_MAX_LEVELS = 64
+STATUS = {0: "GALA_OK", 1: "GALA_ERR_INVALID", 2: "GALA_ERR_IO", 3: "GALA_ERR_FORMAT", 4: "GALA_ERR_CUDA",
+          5: "GALA_ERR_NO_DEVICE", 6: "GALA_ERR_OOM", 7: "GALA_ERR_OVERFLOW", 8: "GALA_ERR_CAPACITY"}
+
+# every symbol include/gala.h declares
+EXPORTS = ["gala_last_error", "gala_status_string", "gala_kernel_launch_count", "gala_default_options",
+           "gala_graph_load_bin", "gala_graph_store_bin", "gala_graph_from_text", "gala_graph_from_csr",
+           "gala_graph_info", "gala_graph_arrays", "gala_graph_destroy", "gala_generate_sbm",
+           "gala_generate_rmat", "gala_context_create", "gala_context_destroy", "gala_louvain",
+           "gala_louvain_device", "gala_phase1_device", "gala_contract_device", "gala_modularity_host"]
+
+_i32p = ctypes.POINTER(ctypes.c_int32)
+_i64p = ctypes.POINTER(ctypes.c_int64)
+_f64p = ctypes.POINTER(ctypes.c_double)
+_vp = ctypes.c_void_p
+
+
+class GalaError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__(f"{STATUS.get(status, status)}: {msg}")
+        self.status = status
+
+
+class Options(ctypes.Structure):
+    _fields_ = [("min_modularity", ctypes.c_double), ("max_levels", ctypes.c_int32),
+                ("verbose", ctypes.c_int32), ("use_graphs", ctypes.c_int32), ("reserved", ctypes.c_int32)]
+
+
+class Result(ctypes.Structure):
+    _fields_ = [("modularity", ctypes.c_double), ("num_vertices", ctypes.c_int32),
+                ("num_communities", ctypes.c_int32), ("num_levels", ctypes.c_int32),
+                ("total_iterations", ctypes.c_int32),
+                ("level_modularity", ctypes.c_double * GALA_MAX_LEVELS),
+                ("level_communities", ctypes.c_int32 * GALA_MAX_LEVELS),
+                ("level_iterations", ctypes.c_int32 * GALA_MAX_LEVELS),
+                ("iter_modularity", _f64p), ("iter_capacity", ctypes.c_int32), ("iter_count", ctypes.c_int32),
+                ("time_total_ms", ctypes.c_double), ("time_phase1_ms", ctypes.c_double),
+                ("time_decide_ms", ctypes.c_double), ("time_update_ms", ctypes.c_double),
+                ("time_contract_ms", ctypes.c_double), ("time_h2d_ms", ctypes.c_double),
+                ("time_d2h_ms", ctypes.c_double), ("decide_sweeps", ctypes.c_int64),
+                ("decide_bytes", ctypes.c_int64), ("update_bytes", ctypes.c_int64),
+                ("kernel_launches", ctypes.c_int64), ("h2d_bytes", ctypes.c_int64),
+                ("d2h_bytes", ctypes.c_int64)]
+
+    def to_dict(self, trace=None):
+        L = self.num_levels
+        d = {"modularity": self.modularity, "num_vertices": self.num_vertices,
+             "num_communities": self.num_communities, "rounds": L, "total_iterations": self.total_iterations,
+             "level_q": list(self.level_modularity[:L]), "level_c": list(self.level_communities[:L]),
+             "level_iters": list(self.level_iterations[:L]),
+             "time_total_ms": self.time_total_ms, "time_phase1_ms": self.time_phase1_ms,
+             "time_decide_ms": self.time_decide_ms, "time_update_ms": self.time_update_ms,
+             "time_contract_ms": self.time_contract_ms, "time_h2d_ms": self.time_h2d_ms,
+             "time_d2h_ms": self.time_d2h_ms, "decide_sweeps": self.decide_sweeps,
+             "decide_bytes": self.decide_bytes, "update_bytes": self.update_bytes,
+             "kernel_launches": self.kernel_launches, "h2d_bytes": self.h2d_bytes, "d2h_bytes": self.d2h_bytes}
+        if trace is not None:
+            d["iter_q"] = trace[:min(self.iter_count, len(trace))].tolist()
+        return d
+
+
+_lib = None
+
+
+def load(path=LIB_PATH):
+    """Load libgala.so (raises OSError when it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise OSError(f"libgala.so not built at {path}; run __graft_entry__.build()")
+    L = ctypes.CDLL(path)
+    L.gala_last_error.restype = ctypes.c_char_p
+    L.gala_status_string.restype = ctypes.c_char_p
+    L.gala_status_string.argtypes = [ctypes.c_int]
+    L.gala_kernel_launch_count.restype = ctypes.c_int64
+    L.gala_default_options.argtypes = [ctypes.POINTER(Options)]
+    L.gala_graph_load_bin.argtypes = [ctypes.c_char_p, ctypes.c_int32, ctypes.POINTER(_vp)]
+    L.gala_graph_store_bin.argtypes = [_vp, ctypes.c_char_p]
+    L.gala_graph_from_text.argtypes = [ctypes.c_char_p, ctypes.c_int32, ctypes.c_int32, ctypes.POINTER(_vp)]
+    L.gala_graph_from_csr.argtypes = [ctypes.c_int32, _i64p, _i32p, _i32p, ctypes.POINTER(_vp)]
+    L.gala_graph_info.argtypes = [_vp, _i32p, _i64p, _i32p]
+    L.gala_graph_arrays.argtypes = [_vp, ctypes.POINTER(_i64p), ctypes.POINTER(_i32p), ctypes.POINTER(_i32p)]
+    L.gala_graph_destroy.argtypes = [_vp]
+    L.gala_graph_destroy.restype = None
+    L.gala_generate_sbm.argtypes = [ctypes.c_int32, ctypes.c_int32, ctypes.c_double, ctypes.c_double,
+                                    ctypes.c_uint64, ctypes.POINTER(_vp)]
+    L.gala_generate_rmat.argtypes = [ctypes.c_int32, ctypes.c_int64, ctypes.c_double, ctypes.c_double,
+                                     ctypes.c_double, ctypes.c_double, ctypes.c_uint64, ctypes.c_int32,
+                                     ctypes.POINTER(_vp)]
+    L.gala_context_create.argtypes = [ctypes.c_int32, ctypes.c_int32, ctypes.c_int64, ctypes.POINTER(_vp)]
+    L.gala_context_destroy.argtypes = [_vp]
+    L.gala_context_destroy.restype = None
+    L.gala_louvain.argtypes = [_vp, _vp, ctypes.POINTER(Options), _i32p, ctypes.POINTER(Result)]
+    L.gala_louvain_device.argtypes = [_vp, ctypes.c_int32, _vp, _vp, _vp, ctypes.POINTER(Options), _vp,
+                                      ctypes.POINTER(Result)]
+    L.gala_phase1_device.argtypes = [_vp, ctypes.c_int32, _vp, _vp, _vp, ctypes.c_double, _vp, _f64p, _f64p,
+                                     ctypes.c_int32, _i32p]
+    L.gala_contract_device.argtypes = [_vp, ctypes.c_int32, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _i32p, _i64p]
+    L.gala_modularity_host.argtypes = [_vp, _i32p, _f64p]
+    for name in ["gala_graph_load_bin", "gala_graph_store_bin", "gala_graph_from_text", "gala_graph_from_csr",
+                 "gala_graph_info", "gala_graph_arrays", "gala_generate_sbm", "gala_generate_rmat",
+                 "gala_context_create", "gala_louvain", "gala_louvain_device", "gala_phase1_device",
+                 "gala_contract_device", "gala_modularity_host"]:
+        getattr(L, name).restype = ctypes.c_int
+    _lib = L
+    return L
+
+
+def _check(status):
+    if status != 0:
+        raise GalaError(status, load().gala_last_error().decode(errors="replace"))
+
+
+def _ptr(a, t):
+    return None if a is None else a.ctypes.data_as(t)
+
+
+def launch_count():
+    return int(load().gala_kernel_launch_count())
+
+
+def default_options(**kw):
+    o = Options()
+    load().gala_default_options(ctypes.byref(o))
+    for k, v in kw.items():
+        setattr(o, k, v)
+    return o
+
+
+class Graph:
+    """Host graph owned by libgala (reference layout: inclusive offsets)."""
+
+    def __init__(self, handle):
+        self.h = handle
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            load().gala_graph_destroy(self.h)
+            self.h = None
+
+    @staticmethod
+    def load_bin(path, weighted=False):
+        h = _vp()
+        _check(load().gala_graph_load_bin(path.encode(), int(weighted), ctypes.byref(h)))
+        return Graph(h)
+
+    @staticmethod
+    def from_text(path, weighted=False, nthreads=0):
+        h = _vp()
+        _check(load().gala_graph_from_text(path.encode(), int(weighted), nthreads, ctypes.byref(h)))
+        return Graph(h)
+
+    @staticmethod
+    def from_csr(offs, nbr, w=None):
+        """offs: n+1 offsets with a leading 0 (converted to the reference's
+        inclusive layout)."""
+        offs = np.ascontiguousarray(offs, dtype=np.int64)
+        incl = np.ascontiguousarray(offs[1:])
+        nbr = np.ascontiguousarray(nbr, dtype=np.int32)
+        w = None if w is None else np.ascontiguousarray(w, dtype=np.int32)
+        h = _vp()
+        _check(load().gala_graph_from_csr(incl.shape[0], _ptr(incl, _i64p), _ptr(nbr, _i32p), _ptr(w, _i32p),
+                                          ctypes.byref(h)))
+        return Graph(h)
+
+    @staticmethod
+    def sbm(n, k, p_in, p_out, seed):
+        h = _vp()
+        _check(load().gala_generate_sbm(n, k, p_in, p_out, seed, ctypes.byref(h)))
+        return Graph(h)
+
+    @staticmethod
+    def rmat(scale, edges, a=0.57, b=0.19, c=0.19, seed=1, nthreads=0, noise=0.0):
+        h = _vp()
+        _check(load().gala_generate_rmat(scale, edges, a, b, c, noise, seed, nthreads, ctypes.byref(h)))
+        return Graph(h)
+
+    def store_bin(self, path):
+        _check(load().gala_graph_store_bin(self.h, path.encode()))
+
+    def info(self):
+        n, e, w = ctypes.c_int32(), ctypes.c_int64(), ctypes.c_int32()
+        _check(load().gala_graph_info(self.h, ctypes.byref(n), ctypes.byref(e), ctypes.byref(w)))
+        return n.value, e.value, bool(w.value)
+
+    def arrays(self):
+        """(offs[n+1] with leading 0, nbr, w or None) as numpy copies."""
+        n, e, weighted = self.info()
+        po, pn, pw = _i64p(), _i32p(), _i32p()
+        _check(load().gala_graph_arrays(self.h, ctypes.byref(po), ctypes.byref(pn), ctypes.byref(pw)))
+        offs = np.zeros(n + 1, dtype=np.int64)
+        offs[1:] = np.ctypeslib.as_array(po, shape=(n,))
+        nbr = np.ctypeslib.as_array(pn, shape=(e,)).copy() if e else np.zeros(0, np.int32)
+        w = np.ctypeslib.as_array(pw, shape=(e,)).copy() if (weighted and e) else None
+        return offs, nbr, w
+
+    def modularity(self, labels):
+        labels = np.ascontiguousarray(labels, dtype=np.int32)
+        q = ctypes.c_double()
+        _check(load().gala_modularity_host(self.h, _ptr(labels, _i32p), ctypes.byref(q)))
+        return q.value
+
+
+class Context:
+    """Device context (one CUDA stream + workspace)."""
+
+    def __init__(self, max_vertices, max_entries, device=0):
+        self.h = _vp()
+        _check(load().gala_context_create(device, int(max_vertices), int(max_entries), ctypes.byref(self.h)))
+
+    def close(self):
+        if getattr(self, "h", None):
+            load().gala_context_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def louvain(self, graph, min_mod=1e-6, max_levels=0, verbose=False, iter_capacity=4096):
+        """gala_louvain: host graph in, host labels out."""
+        n, _, _ = graph.info()
+        labels = np.zeros(n, dtype=np.int32)
+        trace = np.zeros(iter_capacity, dtype=np.float64)
+        r = Result()
+        r.iter_modularity = _ptr(trace, _f64p)
+        r.iter_capacity = iter_capacity
+        o = default_options(min_modularity=min_mod, max_levels=max_levels, verbose=int(verbose))
+        _check(load().gala_louvain(self.h, graph.h, ctypes.byref(o), _ptr(labels, _i32p), ctypes.byref(r)))
+        d = r.to_dict(trace)
+        d["labels"] = labels
+        return d
+
+    def louvain_device(self, n, d_offs, d_nbr, d_w, d_out, min_mod=1e-6, max_levels=0, iter_capacity=4096):
+        """gala_louvain_device on raw device pointers (ints)."""
+        trace = np.zeros(iter_capacity, dtype=np.float64)
+        r = Result()
+        r.iter_modularity = _ptr(trace, _f64p)
+        r.iter_capacity = iter_capacity
+        o = default_options(min_modularity=min_mod, max_levels=max_levels)
+        _check(load().gala_louvain_device(self.h, n, d_offs, d_nbr, d_w or None, ctypes.byref(o), d_out,
+                                          ctypes.byref(r)))
+        return r.to_dict(trace)
+
+    def phase1_device(self, n, d_offs, d_nbr, d_w, d_out, min_mod=1e-6, iter_capacity=4096):
+        q = ctypes.c_double()
+        it = ctypes.c_int32()
+        trace = np.zeros(iter_capacity, dtype=np.float64)
+        _check(load().gala_phase1_device(self.h, n, d_offs, d_nbr, d_w or None, min_mod, d_out, ctypes.byref(q),
+                                         _ptr(trace, _f64p), iter_capacity, ctypes.byref(it)))
+        return {"q": q.value, "iterations": it.value, "iter_q": trace[:it.value + 1].tolist()}
+
+    def contract_device(self, n, d_offs, d_nbr, d_w, d_comm, d_new_offs, d_new_nbr, d_new_w):
+        C = ctypes.c_int32()
+        E = ctypes.c_int64()
+        _check(load().gala_contract_device(self.h, n, d_offs, d_nbr, d_w or None, d_comm, d_new_offs, d_new_nbr,
+                                           d_new_w, ctypes.byref(C), ctypes.byref(E)))
+        return C.value, E.value

@@ -1,0 +1,192 @@
+/*
+ * gala.h - C ABI of the GB300 Louvain engine (libgala.so).
+ *
+ * Plain C, plain pointers and sizes.  Every entry point returns a gala_status
+ * and never aborts; gala_last_error() returns a text for the last failure on
+ * the calling host thread.
+ *
+ * CSR conventions used at this boundary
+ * -------------------------------------
+ *  - "reference layout" (the on-disk .bin layout of the reference,
+ *    src/graph/graph.cpp:153-219): int32 n, then int64 offsets[n] holding
+ *    INCLUSIVE prefix sums of the row lengths (no leading 0), then int32
+ *    neighbours[offsets[n-1]], then optionally int32 weights[offsets[n-1]].
+ *  - "device layout" (used by the *_device entry points): int64
+ *    offsets[n+1] with a leading 0, neighbours and weights as above.  A NULL
+ *    weight pointer means every edge has weight 1.
+ *
+ * Types follow the reference (src/graph/graph_config.h:3-5): vertex ids and
+ * weights are int32, edge offsets are int64.
+ */
+#ifndef GALA_H
+#define GALA_H
+
+#include <stdint.h>
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    GALA_OK = 0,
+    GALA_ERR_INVALID = 1,   /* bad argument or malformed CSR */
+    GALA_ERR_IO = 2,        /* file cannot be opened / read / written */
+    GALA_ERR_FORMAT = 3,    /* .bin file is truncated or inconsistent */
+    GALA_ERR_CUDA = 4,      /* a CUDA runtime call failed */
+    GALA_ERR_NO_DEVICE = 5, /* no CUDA device is visible */
+    GALA_ERR_OOM = 6,       /* device or host allocation failed */
+    GALA_ERR_OVERFLOW = 7,  /* a device hash table or probe limit overflowed */
+    GALA_ERR_CAPACITY = 8   /* graph larger than the context was created for */
+} gala_status;
+
+/* Host-resident graph (owned by the library). */
+typedef struct gala_graph gala_graph;
+/* Device context: one CUDA stream plus all device workspace for graphs of up
+ * to a given size.  One context per host thread at a time. */
+typedef struct gala_context gala_context;
+
+#define GALA_MAX_LEVELS 64
+
+typedef struct {
+    double min_modularity; /* stop threshold on the Q gain; reference: 1e-6
+                              (src/gala_main.cu:48) */
+    int32_t max_levels;    /* 0 = run until the gain is below min_modularity */
+    int32_t verbose;       /* 1 = print the reference's stdout lines
+                              (README.md:59-89, louvain_main_process.cu:1003) */
+    int32_t use_graphs;    /* 1 = replay each phase-1 iteration as a CUDA graph */
+    int32_t reserved;
+} gala_options;
+
+typedef struct {
+    double modularity;                 /* final Q */
+    int32_t num_vertices;              /* input vertex count */
+    int32_t num_communities;           /* final community count */
+    int32_t num_levels;                /* rounds run */
+    int32_t total_iterations;          /* phase-1 iterations over all rounds */
+    double level_modularity[GALA_MAX_LEVELS];
+    int32_t level_communities[GALA_MAX_LEVELS];
+    int32_t level_iterations[GALA_MAX_LEVELS];
+    /* optional per-iteration Q trace, caller-owned (may be NULL) */
+    double *iter_modularity;
+    int32_t iter_capacity;
+    int32_t iter_count;
+    /* timings (ms), measured with CUDA events on the context's stream */
+    double time_total_ms;       /* all rounds, device-resident graph */
+    double time_phase1_ms;      /* all phase-1 work */
+    double time_decide_ms;      /* decide-and-move sweeps only */
+    double time_update_ms;      /* weight update + prune sweeps */
+    double time_contract_ms;    /* phase-2 contraction */
+    double time_h2d_ms;         /* host->device copy (gala_louvain only) */
+    double time_d2h_ms;         /* device->host copy of labels */
+    /* roofline bookkeeping for the decide-and-move sweeps */
+    int64_t decide_sweeps;
+    int64_t decide_bytes;       /* algorithmic bytes over all sweeps */
+    int64_t update_bytes;       /* algorithmic bytes of the update sweeps */
+    int64_t kernel_launches;    /* kernels launched by this call */
+    int64_t h2d_bytes;
+    int64_t d2h_bytes;
+} gala_result;
+
+/* ---- errors / info --------------------------------------------------- */
+const char *gala_last_error(void);
+const char *gala_status_string(gala_status s);
+/* Number of kernels the library launched in this process so far. */
+int64_t gala_kernel_launch_count(void);
+void gala_default_options(gala_options *opt);
+
+/* ---- host graph I/O ---------------------------------------------------- */
+/* Replaces Graph::load_bin_graph (src/graph/graph.cpp:177-219).  weighted=1
+ * reads the weight block (the reference ignores its -w flag here, graph.cpp:200;
+ * this loader honours it).  Rejects truncated or inconsistent files. */
+gala_status gala_graph_load_bin(const char *path, int32_t weighted, gala_graph **out);
+/* Replaces Graph::store_bin_graph (src/graph/graph.cpp:153-174). */
+gala_status gala_graph_store_bin(const gala_graph *g, const char *path);
+/* Replaces Graph::Graph(file, is_wt) (src/graph/graph.cpp:18-151): parse an
+ * edge list "src dst [w]" ('#' lines skipped), symmetrise, deduplicate per
+ * row (weights of duplicates summed when weighted), drop ids without edges
+ * and renumber densely in id order.  nthreads <= 0 uses all cores. */
+gala_status gala_graph_from_text(const char *path, int32_t weighted, int32_t nthreads,
+                                 gala_graph **out);
+/* Copy a caller-owned CSR in reference layout (inclusive offsets, no leading
+ * 0).  weights may be NULL (all 1). */
+gala_status gala_graph_from_csr(int32_t n, const int64_t *offsets_inclusive,
+                                const int32_t *neighbors, const int32_t *weights,
+                                gala_graph **out);
+gala_status gala_graph_info(const gala_graph *g, int32_t *n, int64_t *num_entries,
+                            int32_t *weighted);
+/* Borrow the host arrays (reference layout).  Valid until destroy. */
+gala_status gala_graph_arrays(const gala_graph *g, const int64_t **offsets_inclusive,
+                              const int32_t **neighbors, const int32_t **weights);
+void gala_graph_destroy(gala_graph *g);
+
+/* ---- synthetic graphs (seeded) ---------------------------------------- */
+/* Planted-partition SBM: n vertices in k equal blocks, p_in / p_out. */
+gala_status gala_generate_sbm(int32_t n, int32_t k, double p_in, double p_out,
+                              uint64_t seed, gala_graph **out);
+/* R-MAT with 2^scale ids and `edges` raw undirected samples; duplicates and
+ * self-loops removed, ids without edges dropped and renumbered in order.
+ * noise > 0 perturbs a, b, c, d independently by a factor in
+ * [1 - noise, 1 + noise] at every recursion level of every edge (then
+ * renormalises), which smooths the degree staircase of plain R-MAT.  The
+ * graph depends only on the arguments, not on nthreads. */
+gala_status gala_generate_rmat(int32_t scale, int64_t edges, double a, double b,
+                               double c, double noise, uint64_t seed, int32_t nthreads,
+                               gala_graph **out);
+
+/* ---- device context ---------------------------------------------------- */
+gala_status gala_context_create(int32_t device, int32_t max_vertices, int64_t max_entries,
+                                gala_context **out);
+void gala_context_destroy(gala_context *ctx);
+
+/* ---- Louvain ------------------------------------------------------------ */
+/* Replaces louvain_gpu(Graph&, vertex_t*, double, int, int)
+ * (src/louvain_gpu/louvain.cuh:8, louvain.cu:136-229) running the multi-round
+ * loop of louvain.cu:193-226.  Copies the host graph to the device, runs all
+ * rounds and writes the final community of every input vertex to
+ * community_out (host, length n).  ctx may be NULL (a temporary context is
+ * created on device 0). */
+gala_status gala_louvain(gala_context *ctx, const gala_graph *g, const gala_options *opt,
+                         int32_t *community_out, gala_result *res);
+
+/* Same run on a device-resident CSR in device layout.  community_out is a
+ * device pointer of length n.  The input arrays are not modified. */
+gala_status gala_louvain_device(gala_context *ctx, int32_t n, const int64_t *d_offsets,
+                                const int32_t *d_neighbors, const int32_t *d_weights,
+                                const gala_options *opt, int32_t *d_community_out,
+                                gala_result *res);
+
+/* One phase-1 run (decide-and-move iterations until the Q gain is below
+ * min_modularity) on a device CSR.  Replaces louvain_main_process
+ * (src/louvain_gpu/louvain.cuh:10-16, louvain_main_process.cu:237-1060).
+ * d_community_out (device, length n) receives the accepted partition;
+ * *modularity receives its Q; iter_q (host, optional) the Q of every
+ * iteration including iteration 0. */
+gala_status gala_phase1_device(gala_context *ctx, int32_t n, const int64_t *d_offsets,
+                               const int32_t *d_neighbors, const int32_t *d_weights,
+                               double min_modularity, int32_t *d_community_out,
+                               double *modularity, double *iter_q, int32_t iter_capacity,
+                               int32_t *iterations);
+
+/* Contract a partition into a community graph.  Replaces
+ * build_compressed_graph (src/louvain_gpu/louvain.cuh:18-22,
+ * build_compressed_graph.cu:5-173).  Communities are renumbered densely in
+ * ascending order of their label; d_community (device, length n) is
+ * rewritten in place with the new ids (as the reference does,
+ * build_compressed_graph.cu:22-23).  The output CSR (device layout) goes to
+ * caller buffers: d_new_offsets (n+1), d_new_neighbors / d_new_weights
+ * (capacity >= number of input entries).  Rows are sorted by neighbour id. */
+gala_status gala_contract_device(gala_context *ctx, int32_t n, const int64_t *d_offsets,
+                                 const int32_t *d_neighbors, const int32_t *d_weights,
+                                 int32_t *d_community, int64_t *d_new_offsets,
+                                 int32_t *d_new_neighbors, int32_t *d_new_weights,
+                                 int32_t *num_communities, int64_t *num_entries);
+
+/* Host FP64 modularity of a partition of a host graph (the host check the
+ * reference keeps at src/louvain_gpu/kernel_functions.cu:1037-1079). */
+gala_status gala_modularity_host(const gala_graph *g, const int32_t *community, double *q);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GALA_H */

@@ -1,0 +1,369 @@
+/*
+ * louvain_oracle.c - CPU restatement of the reference's GPU Louvain path.
+ *
+ * TEST INFRASTRUCTURE ONLY: the checker for the CUDA engine and the timed CPU
+ * baseline.  The engine does not link or call this file.
+ *
+ * Reference: LinXi-lx/GALA-mg.  The reference runs each phase-1 iteration
+ * with synchronous (Jacobi) semantics: every vertex decides from the labels
+ * and community totals of the previous iteration (prev_community, Tot), the
+ * moves are applied after the sweep (louvain_main_process.cu:571-1029).  The
+ * restatement below therefore gives the same partition independent of the
+ * order vertices are visited in, and parallelises over vertices.
+ *
+ * Compile with -ffp-contract=off: the FP64 expressions below must round
+ * exactly as written (no fused multiply-add), like the engine's kernels.
+ */
+#include "oracle.h"
+
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+double orc_q_from_sums(int64_t sum_in, int64_t sum_tot2, int64_t m2)
+{
+    /* Q = sum(In)/m2 - sum(Tot^2)/m2^2 (louvain_main_process.cu:990-999 with
+     * modularity_op, kernel_functions.cuh:77-87), from exact integer sums. */
+    double c = 1.0 / (double)m2;
+    return (double)sum_in * c - (double)sum_tot2 * c * c;
+}
+
+/* Gain of moving a vertex into community cn before the correction for the
+ * vertex's own community: kernel_functions.cu:136 / :362 (same order of the
+ * FP64 operations). */
+static inline double dq_of(int32_t w_to_c, int32_t ki, int32_t tot_c, int32_t tot_cur,
+                           double constant)
+{
+    return 2.0 * (double)w_to_c - 2.0 * (double)ki * ((double)tot_c - (double)tot_cur + (double)ki) * constant;
+}
+
+typedef struct {
+    int32_t *acc;     /* dense per-community weight accumulator, zero between uses */
+    int32_t *touched; /* communities with acc != 0 */
+} scratch_t;
+
+/* Decide one vertex: kernel_functions.cu:289-441 (degree < 32),
+ * :473-593 (degree 32-128), :640-813 (degree >= 129).  Returns the new label. */
+static int32_t decide_vertex(int32_t v, const int64_t *offs, const int32_t *nbr, const int32_t *w,
+                             const int32_t *prev, const int32_t *K, const int32_t *Self,
+                             const int32_t *Tot, const int32_t *size, double constant,
+                             scratch_t *s)
+{
+    int32_t cur = prev[v];
+    int32_t ki = K[v];
+    int32_t nt = 0;
+    /* aggregate w(v, c) over neighbour communities (the hash tables of
+     * insert_neighbor_com_info, kernel_functions.cu:102-221, or the shuffle
+     * sum of :321-335) */
+    for (int64_t e = offs[v]; e < offs[v + 1]; ++e) {
+        int32_t c = prev[nbr[e]];
+        int32_t wt = w ? w[e] : 1;
+        if (s->acc[c] == 0) s->touched[nt++] = c;
+        s->acc[c] += wt;
+    }
+    int32_t w_cur = s->acc[cur]; /* find_neighbor_com_info(cur_com), :513 / :684 */
+    /* argmax with ties to the lowest id; only gains > 0 compete with the
+     * initial state (0, cur): :136-142 and :366-379 */
+    double maxdq = 0.0;
+    int32_t best = cur;
+    for (int32_t i = 0; i < nt; ++i) {
+        int32_t c = s->touched[i];
+        if (c != cur) {
+            double dq = dq_of(s->acc[c], ki, Tot[c], Tot[cur], constant);
+            if (dq > 0.0 && (dq > maxdq || (dq == maxdq && c < best))) {
+                maxdq = dq;
+                best = c;
+            }
+        }
+        s->acc[c] = 0;
+    }
+    /* correction for leaving the own community: :381 / :532 / :748 */
+    maxdq = maxdq - 2 * w_cur + 2 * Self[v];
+    if (best >= 0 && best != cur && maxdq > 0) {
+        /* singleton swap guard: :386-390 */
+        if (size[best] == 1 && size[cur] == 1 && best > cur) return cur;
+        return best;
+    }
+    return cur;
+}
+
+int32_t orc_phase1(int32_t n, const int64_t *offs, const int32_t *nbr, const int32_t *w,
+                   int64_t m2, double min_mod, int32_t *labels_out, double *q_out,
+                   double *iter_q, int32_t iter_cap, int32_t *n_iter_q, int32_t nthreads)
+{
+    if (n <= 0 || m2 <= 0) return -1;
+#ifdef _OPENMP
+    if (nthreads <= 0) nthreads = omp_get_max_threads();
+#else
+    nthreads = 1;
+#endif
+    const double constant = 1 / (double)m2; /* louvain_main_process.cu:273 */
+    int32_t *K = (int32_t *)calloc((size_t)n, sizeof(int32_t));
+    int32_t *Self = (int32_t *)calloc((size_t)n, sizeof(int32_t));
+    int32_t *Tot = (int32_t *)calloc((size_t)n, sizeof(int32_t));
+    int32_t *size = (int32_t *)calloc((size_t)n, sizeof(int32_t));
+    int32_t *In = (int32_t *)calloc((size_t)n, sizeof(int32_t));
+    int32_t *prev = (int32_t *)calloc((size_t)n, sizeof(int32_t));
+    int32_t *cur = (int32_t *)calloc((size_t)n, sizeof(int32_t));
+    unsigned char *active = (unsigned char *)calloc((size_t)n, 1);
+    scratch_t *scr = (scratch_t *)calloc((size_t)nthreads, sizeof(scratch_t));
+    for (int t = 0; t < nthreads; ++t) {
+        scr[t].acc = (int32_t *)calloc((size_t)n, sizeof(int32_t));
+        scr[t].touched = (int32_t *)calloc((size_t)n, sizeof(int32_t));
+    }
+
+    /* init_communities (kernel_functions.cu:34-73): K = Tot = row weight sum,
+     * Self = self-loop weight, label = own id, community size 1
+     * (louvain_main_process.cu:337). */
+    int64_t sum_in = 0, sum_tot2 = 0;
+#pragma omp parallel for num_threads(nthreads) schedule(dynamic, 4096) reduction(+ : sum_in, sum_tot2)
+    for (int32_t v = 0; v < n; ++v) {
+        int32_t k = 0, sf = 0;
+        for (int64_t e = offs[v]; e < offs[v + 1]; ++e) {
+            int32_t wt = w ? w[e] : 1;
+            k += wt;
+            if (nbr[e] == v) sf = wt;
+        }
+        K[v] = k;
+        Tot[v] = k;
+        Self[v] = sf;
+        size[v] = 1;
+        prev[v] = v;
+        cur[v] = v;
+        /* the first efficient_weight_updating (louvain_main_process.cu:538)
+         * gives In = Self for the singleton partition */
+        In[v] = sf;
+        sum_in += sf;
+        sum_tot2 += (int64_t)k * (int64_t)k;
+        active[v] = 1;
+    }
+    double q = orc_q_from_sums(sum_in, sum_tot2, m2);
+    int32_t nq = 0;
+    if (iter_q && nq < iter_cap) iter_q[nq] = q;
+    nq++;
+    double prev_q = q;
+
+    for (;;) {
+        /* decide-and-move over the active set (louvain_main_process.cu:594-857):
+         * every decision reads prev / Tot / size of the previous iteration. */
+#pragma omp parallel num_threads(nthreads)
+        {
+            int tid = 0;
+#ifdef _OPENMP
+            tid = omp_get_thread_num();
+#endif
+#pragma omp for schedule(dynamic, 1024)
+            for (int32_t v = 0; v < n; ++v) {
+                int32_t nv = prev[v];
+                if (active[v] && offs[v + 1] > offs[v])
+                    nv = decide_vertex(v, offs, nbr, w, prev, K, Self, Tot, size, constant, &scr[tid]);
+                cur[v] = nv;
+            }
+        }
+        /* Tot += Tot_update, size += size_update (louvain_main_process.cu:949-953) */
+        for (int32_t v = 0; v < n; ++v) {
+            if (cur[v] != prev[v]) {
+                Tot[cur[v]] += K[v];
+                Tot[prev[v]] -= K[v];
+                size[cur[v]] += 1;
+                size[prev[v]] -= 1;
+            }
+        }
+        /* min_Tot over non-empty communities, m2 when none (Tot_op,
+         * kernel_functions.cuh:112-121, louvain_main_process.cu:955) */
+        int64_t min_tot = m2;
+        sum_tot2 = 0;
+#pragma omp parallel for num_threads(nthreads) reduction(min : min_tot) reduction(+ : sum_tot2)
+        for (int32_t c = 0; c < n; ++c) {
+            int64_t t = Tot[c];
+            if (t != 0 && t < min_tot) min_tot = t;
+            sum_tot2 += t * t;
+        }
+        const int32_t min_tot_i = (int32_t)min_tot;
+        /* weight update + pruning (compute_In, kernel_functions.cu:890-955,
+         * compute_In_blk :958-1034): In = weight to the own community, and
+         * the vertex leaves the active set when the bound at :944 holds. */
+        sum_in = 0;
+#pragma omp parallel for num_threads(nthreads) schedule(dynamic, 4096) reduction(+ : sum_in)
+        for (int32_t v = 0; v < n; ++v) {
+            if (offs[v + 1] == offs[v]) { /* in no degree bin: never touched */
+                active[v] = 1;
+                continue;
+            }
+            int32_t c = cur[v], s = 0;
+            for (int64_t e = offs[v]; e < offs[v + 1]; ++e)
+                if (cur[nbr[e]] == c) s += w ? w[e] : 1;
+            In[v] = s;
+            sum_in += s;
+            int32_t ki = K[v];
+            active[v] = !(2 * (s - Self[v]) - (ki - Self[v]) +
+                              (double)(min_tot_i - (Tot[c] - ki)) * constant * ki >
+                          0);
+        }
+        q = orc_q_from_sums(sum_in, sum_tot2, m2);
+        if (iter_q && nq < iter_cap) iter_q[nq] = q;
+        nq++;
+        /* convergence: louvain_main_process.cu:1004-1007; the partition of the
+         * rejected iteration is dropped (prev_community is returned). */
+        if (q - prev_q < min_mod) break;
+        prev_q = q;
+        memcpy(prev, cur, (size_t)n * sizeof(int32_t));
+    }
+
+    memcpy(labels_out, prev, (size_t)n * sizeof(int32_t));
+    if (q_out) *q_out = prev_q;
+    if (n_iter_q) *n_iter_q = nq;
+
+    for (int t = 0; t < nthreads; ++t) {
+        free(scr[t].acc);
+        free(scr[t].touched);
+    }
+    free(scr);
+    free(K); free(Self); free(Tot); free(size); free(In); free(prev); free(cur); free(active);
+    return nq - 1;
+}
+
+static int cmp_i32(const void *a, const void *b)
+{
+    int32_t x = *(const int32_t *)a, y = *(const int32_t *)b;
+    return (x > y) - (x < y);
+}
+
+int32_t orc_contract(int32_t n, const int64_t *offs, const int32_t *nbr, const int32_t *w,
+                     const int32_t *labels, int32_t *relabel_out, int64_t *new_offs,
+                     int32_t *new_nbr, int32_t *new_w, int64_t *new_entries)
+{
+    /* community sizes and dense renumbering in ascending label order
+     * (build_compressed_graph.cu:11-24) */
+    int32_t *newid = (int32_t *)malloc((size_t)n * sizeof(int32_t));
+    int32_t *cnt = (int32_t *)calloc((size_t)n + 1, sizeof(int32_t));
+    for (int32_t v = 0; v < n; ++v) cnt[labels[v]]++;
+    int32_t C = 0;
+    for (int32_t c = 0; c < n; ++c) newid[c] = cnt[c] > 0 ? C++ : -1;
+    for (int32_t v = 0; v < n; ++v) relabel_out[v] = newid[labels[v]];
+    /* members of each community (gather_vertex_by_community, :32-37) */
+    int64_t *moff = (int64_t *)calloc((size_t)C + 1, sizeof(int64_t));
+    for (int32_t v = 0; v < n; ++v) moff[relabel_out[v] + 1]++;
+    for (int32_t c = 0; c < C; ++c) moff[c + 1] += moff[c];
+    int32_t *members = (int32_t *)malloc((size_t)n * sizeof(int32_t));
+    int64_t *pos = (int64_t *)malloc((size_t)C * sizeof(int64_t));
+    for (int32_t c = 0; c < C; ++c) pos[c] = moff[c];
+    for (int32_t v = 0; v < n; ++v) members[pos[relabel_out[v]]++] = v;
+    /* new row of community c: (c', sum of w over member edges into c')
+     * (compute_neighbors_weights*, kernel_functions.cu:1239-1561), listed in
+     * ascending c' */
+    int64_t *acc = (int64_t *)calloc((size_t)C, sizeof(int64_t));
+    int32_t *touched = (int32_t *)malloc((size_t)C * sizeof(int32_t));
+    int64_t out = 0;
+    new_offs[0] = 0;
+    for (int32_t c = 0; c < C; ++c) {
+        int32_t nt = 0;
+        for (int64_t i = moff[c]; i < moff[c + 1]; ++i) {
+            int32_t v = members[i];
+            for (int64_t e = offs[v]; e < offs[v + 1]; ++e) {
+                int32_t cc = relabel_out[nbr[e]];
+                if (acc[cc] == 0) touched[nt++] = cc;
+                acc[cc] += w ? w[e] : 1;
+            }
+        }
+        qsort(touched, (size_t)nt, sizeof(int32_t), cmp_i32);
+        for (int32_t i = 0; i < nt; ++i) {
+            new_nbr[out] = touched[i];
+            new_w[out] = (int32_t)acc[touched[i]];
+            acc[touched[i]] = 0;
+            out++;
+        }
+        new_offs[c + 1] = out;
+    }
+    if (new_entries) *new_entries = out;
+    free(newid); free(cnt); free(moff); free(members); free(pos); free(acc); free(touched);
+    return C;
+}
+
+int32_t orc_louvain(int32_t n, const int64_t *offs, const int32_t *nbr, const int32_t *w,
+                    double min_mod, int32_t max_levels, int32_t *comm_out, double *level_q,
+                    int32_t *level_c, int32_t *level_iters, int32_t level_cap, double *iter_q,
+                    int32_t iter_cap, int32_t *n_iter_q, int32_t nthreads)
+{
+    if (n <= 0) return -1;
+    int64_t E = offs[n];
+    int64_t m2 = 0; /* thrust::reduce of the weights, louvain.cu:165-167 */
+    for (int64_t e = 0; e < E; ++e) m2 += w ? w[e] : 1;
+    if (m2 <= 0) return -1;
+
+    int64_t *go = (int64_t *)malloc(((size_t)n + 1) * sizeof(int64_t));
+    int32_t *gn = (int32_t *)malloc((size_t)(E > 0 ? E : 1) * sizeof(int32_t));
+    int32_t *gw = (int32_t *)malloc((size_t)(E > 0 ? E : 1) * sizeof(int32_t));
+    int64_t *no = (int64_t *)malloc(((size_t)n + 1) * sizeof(int64_t));
+    int32_t *nn = (int32_t *)malloc((size_t)(E > 0 ? E : 1) * sizeof(int32_t));
+    int32_t *nw = (int32_t *)malloc((size_t)(E > 0 ? E : 1) * sizeof(int32_t));
+    int32_t *lab = (int32_t *)malloc((size_t)n * sizeof(int32_t));
+    int32_t *rl = (int32_t *)malloc((size_t)n * sizeof(int32_t));
+    memcpy(go, offs, ((size_t)n + 1) * sizeof(int64_t));
+    memcpy(gn, nbr, (size_t)E * sizeof(int32_t));
+    for (int64_t e = 0; e < E; ++e) gw[e] = w ? w[e] : 1;
+    for (int32_t i = 0; i < n; ++i) comm_out[i] = i;
+
+    int32_t cn = n, rounds = 0, nq_total = 0;
+    double prev_mod = -1, cur_mod = -1;
+    for (;;) {
+        double q = 0;
+        int32_t nq = 0;
+        double *tr = iter_q ? iter_q + (nq_total < iter_cap ? nq_total : iter_cap) : NULL;
+        int32_t cap = iter_q ? (iter_cap > nq_total ? iter_cap - nq_total : 0) : 0;
+        int32_t it = orc_phase1(cn, go, gn, gw, m2, min_mod, lab, &q, tr, cap, &nq, nthreads);
+        nq_total += nq;
+        int64_t ne = 0;
+        int32_t C = orc_contract(cn, go, gn, gw, lab, rl, no, nn, nw, &ne);
+        /* labels of the input vertices follow the contraction (the gather of
+         * louvain.cu:188-189, composed in the intended direction) */
+        for (int32_t i = 0; i < n; ++i) comm_out[i] = rl[comm_out[i]];
+        if (rounds < level_cap) {
+            if (level_q) level_q[rounds] = q;
+            if (level_c) level_c[rounds] = C;
+            if (level_iters) level_iters[rounds] = it;
+        }
+        rounds++;
+        prev_mod = cur_mod;
+        cur_mod = q;
+        int64_t *t64 = go; go = no; no = t64;
+        int32_t *t32 = gn; gn = nn; nn = t32;
+        t32 = gw; gw = nw; nw = t32;
+        cn = C;
+        /* round loop condition, louvain.cu:202 */
+        if (!(cur_mod - prev_mod >= min_mod)) break;
+        if (max_levels > 0 && rounds >= max_levels) break;
+    }
+    if (n_iter_q) *n_iter_q = nq_total;
+    free(go); free(gn); free(gw); free(no); free(nn); free(nw); free(lab); free(rl);
+    return rounds;
+}
+
+double orc_modularity(int32_t n, const int64_t *offs, const int32_t *nbr, const int32_t *w,
+                      const int32_t *labels)
+{
+    /* kernel_functions.cu:1037-1079: In per vertex, Tot per community, then
+     * q += In[i]*c - Tot[i]^2*c^2 vertex by vertex. */
+    int64_t m2 = 0;
+    for (int64_t e = 0; e < offs[n]; ++e) m2 += w ? w[e] : 1;
+    double constant = 1.0 / (double)m2;
+    int64_t *Tot = (int64_t *)calloc((size_t)n, sizeof(int64_t));
+    int64_t *In = (int64_t *)calloc((size_t)n, sizeof(int64_t));
+    for (int32_t i = 0; i < n; ++i) {
+        int64_t degree = 0;
+        for (int64_t j = offs[i]; j < offs[i + 1]; ++j) {
+            int32_t wt = w ? w[j] : 1;
+            degree += wt;
+            if (labels[nbr[j]] == labels[i]) In[i] += wt;
+        }
+        Tot[labels[i]] += degree;
+    }
+    double q = 0;
+    for (int32_t i = 0; i < n; ++i)
+        q += (double)In[i] * constant - (double)Tot[i] * (double)Tot[i] * constant * constant;
+    free(Tot);
+    free(In);
+    return q;
+}

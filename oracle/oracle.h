@@ -1,0 +1,56 @@
+/*
+ * oracle.h - CPU restatement of the reference's Louvain path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This code is the checker for the CUDA engine in
+ * gala-mg_gb300/ and the timed CPU baseline of bench.py; the engine never
+ * calls it.  Only tests/, __graft_entry__.smoke() and bench.py load it.
+ *
+ * Every function restates the reference (LinXi-lx/GALA-mg, src/...) with the
+ * same decision rules and the same FP64 operation order; see the comments in
+ * louvain_oracle.c for the file:line each step follows.
+ *
+ * CSR layout: offs[n+1] with a leading 0, nbr[offs[n]], w[offs[n]] or NULL
+ * (all weights 1).
+ */
+#ifndef GALA_ORACLE_H
+#define GALA_ORACLE_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Q from exact integer sums: sum_in = sum over vertices of In[v],
+ * sum_tot2 = sum over communities of Tot[c]^2, m2 = total weight. */
+double orc_q_from_sums(int64_t sum_in, int64_t sum_tot2, int64_t m2);
+
+/* One phase-1 run (louvain_main_process).  Returns the number of phase-1
+ * iterations run (>= 1), or -1 on bad input.  labels_out[n] receives the
+ * accepted partition, *q_out its modularity, iter_q[] the Q of iteration 0..k. */
+int32_t orc_phase1(int32_t n, const int64_t *offs, const int32_t *nbr, const int32_t *w,
+                   int64_t m2, double min_mod, int32_t *labels_out, double *q_out,
+                   double *iter_q, int32_t iter_cap, int32_t *n_iter_q, int32_t nthreads);
+
+/* Contraction (build_compressed_graph) with rows sorted by neighbour id.
+ * relabel_out[n] receives the new id of every vertex.  new_offs needs n+1
+ * slots, new_nbr/new_w offs[n] slots.  Returns the community count. */
+int32_t orc_contract(int32_t n, const int64_t *offs, const int32_t *nbr, const int32_t *w,
+                     const int32_t *labels, int32_t *relabel_out, int64_t *new_offs,
+                     int32_t *new_nbr, int32_t *new_w, int64_t *new_entries);
+
+/* Multi-round driver (the loop at louvain.cu:193-226).  comm_out[n] receives
+ * the final community of every input vertex.  Returns the number of rounds. */
+int32_t orc_louvain(int32_t n, const int64_t *offs, const int32_t *nbr, const int32_t *w,
+                    double min_mod, int32_t max_levels, int32_t *comm_out, double *level_q,
+                    int32_t *level_c, int32_t *level_iters, int32_t level_cap, double *iter_q,
+                    int32_t iter_cap, int32_t *n_iter_q, int32_t nthreads);
+
+/* Host FP64 modularity, summed vertex by vertex as the reference's host check
+ * (kernel_functions.cu:1037-1079). */
+double orc_modularity(int32_t n, const int64_t *offs, const int32_t *nbr, const int32_t *w,
+                      const int32_t *labels);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,121 @@
+"""ctypes wrapper of the CPU oracle (oracle/_build/liboracle.so).
+
+Test infrastructure: used by the tests, by __graft_entry__.smoke() as the
+checker and by bench.py for the timed CPU baseline.  It is never on the
+engine's path.
+"""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+LIB = os.path.join(ROOT, "oracle", "_build", "liboracle.so")
+
+_i32p = ctypes.POINTER(ctypes.c_int32)
+_i64p = ctypes.POINTER(ctypes.c_int64)
+_f64p = ctypes.POINTER(ctypes.c_double)
+
+
+def _p(a, t):
+    return None if a is None else a.ctypes.data_as(t)
+
+
+def read_bin(path, weighted=False):
+    """Read a .bin in the reference layout (src/graph/graph.cpp:177-219) and
+    return (n, offs[n+1] with leading 0, nbr, w or None)."""
+    with open(path, "rb") as f:
+        raw = f.read()
+    n = int(np.frombuffer(raw, dtype=np.int32, count=1)[0])
+    incl = np.frombuffer(raw, dtype=np.int64, count=n, offset=4)
+    e = int(incl[-1]) if n else 0
+    nbr = np.frombuffer(raw, dtype=np.int32, count=e, offset=4 + 8 * n).copy()
+    w = None
+    if weighted:
+        w = np.frombuffer(raw, dtype=np.int32, count=e, offset=4 + 8 * n + 4 * e).copy()
+    offs = np.zeros(n + 1, dtype=np.int64)
+    offs[1:] = incl
+    return n, offs, nbr, w
+
+
+class Oracle:
+    def __init__(self, build=True):
+        if build and not os.path.exists(LIB):
+            subprocess.check_call(["make", "-s", "-C", os.path.join(ROOT, "oracle")])
+        self.lib = ctypes.CDLL(LIB)
+        L = self.lib
+        L.orc_q_from_sums.restype = ctypes.c_double
+        L.orc_q_from_sums.argtypes = [ctypes.c_int64, ctypes.c_int64, ctypes.c_int64]
+        L.orc_phase1.restype = ctypes.c_int32
+        L.orc_phase1.argtypes = [ctypes.c_int32, _i64p, _i32p, _i32p, ctypes.c_int64, ctypes.c_double,
+                                 _i32p, _f64p, _f64p, ctypes.c_int32, _i32p, ctypes.c_int32]
+        L.orc_contract.restype = ctypes.c_int32
+        L.orc_contract.argtypes = [ctypes.c_int32, _i64p, _i32p, _i32p, _i32p, _i32p, _i64p, _i32p, _i32p,
+                                   _i64p]
+        L.orc_louvain.restype = ctypes.c_int32
+        L.orc_louvain.argtypes = [ctypes.c_int32, _i64p, _i32p, _i32p, ctypes.c_double, ctypes.c_int32,
+                                  _i32p, _f64p, _i32p, _i32p, ctypes.c_int32, _f64p, ctypes.c_int32, _i32p,
+                                  ctypes.c_int32]
+        L.orc_modularity.restype = ctypes.c_double
+        L.orc_modularity.argtypes = [ctypes.c_int32, _i64p, _i32p, _i32p, _i32p]
+
+    @staticmethod
+    def _arrs(offs, nbr, w):
+        offs = np.ascontiguousarray(offs, dtype=np.int64)
+        nbr = np.ascontiguousarray(nbr, dtype=np.int32)
+        w = None if w is None else np.ascontiguousarray(w, dtype=np.int32)
+        return offs, nbr, w
+
+    def phase1(self, offs, nbr, w=None, min_mod=1e-6, nthreads=1, iter_cap=4096):
+        offs, nbr, w = self._arrs(offs, nbr, w)
+        n = offs.shape[0] - 1
+        m2 = int(w.sum(dtype=np.int64)) if w is not None else int(offs[-1])
+        lab = np.zeros(n, dtype=np.int32)
+        q = ctypes.c_double()
+        iq = np.zeros(iter_cap, dtype=np.float64)
+        nq = ctypes.c_int32()
+        it = self.lib.orc_phase1(n, _p(offs, _i64p), _p(nbr, _i32p), _p(w, _i32p), m2, min_mod,
+                                 _p(lab, _i32p), ctypes.byref(q), _p(iq, _f64p), iter_cap, ctypes.byref(nq),
+                                 nthreads)
+        return {"labels": lab, "q": q.value, "iterations": it, "iter_q": iq[:min(nq.value, iter_cap)].tolist()}
+
+    def contract(self, offs, nbr, w, labels):
+        offs, nbr, w = self._arrs(offs, nbr, w)
+        n = offs.shape[0] - 1
+        labels = np.ascontiguousarray(labels, dtype=np.int32)
+        rl = np.zeros(n, dtype=np.int32)
+        no = np.zeros(n + 1, dtype=np.int64)
+        cap = max(int(offs[-1]), 1)
+        nn = np.zeros(cap, dtype=np.int32)
+        nw = np.zeros(cap, dtype=np.int32)
+        ne = ctypes.c_int64()
+        C = self.lib.orc_contract(n, _p(offs, _i64p), _p(nbr, _i32p), _p(w, _i32p), _p(labels, _i32p),
+                                  _p(rl, _i32p), _p(no, _i64p), _p(nn, _i32p), _p(nw, _i32p), ctypes.byref(ne))
+        e = ne.value
+        return {"C": C, "relabel": rl, "offs": no[:C + 1].copy(), "nbr": nn[:e].copy(), "w": nw[:e].copy()}
+
+    def louvain(self, offs, nbr, w=None, min_mod=1e-6, max_levels=0, nthreads=1, iter_cap=65536):
+        offs, nbr, w = self._arrs(offs, nbr, w)
+        n = offs.shape[0] - 1
+        comm = np.zeros(n, dtype=np.int32)
+        lq = np.zeros(64, dtype=np.float64)
+        lc = np.zeros(64, dtype=np.int32)
+        li = np.zeros(64, dtype=np.int32)
+        iq = np.zeros(iter_cap, dtype=np.float64)
+        nq = ctypes.c_int32()
+        r = self.lib.orc_louvain(n, _p(offs, _i64p), _p(nbr, _i32p), _p(w, _i32p), min_mod, max_levels,
+                                 _p(comm, _i32p), _p(lq, _f64p), _p(lc, _i32p), _p(li, _i32p), 64,
+                                 _p(iq, _f64p), iter_cap, ctypes.byref(nq), nthreads)
+        return {"rounds": r, "labels": comm, "level_q": lq[:r].tolist(), "level_c": lc[:r].tolist(),
+                "level_iters": li[:r].tolist(), "iter_q": iq[:min(nq.value, iter_cap)].tolist(),
+                "modularity": float(lq[r - 1]) if r > 0 else float("nan")}
+
+    def modularity(self, offs, nbr, w, labels):
+        offs, nbr, w = self._arrs(offs, nbr, w)
+        labels = np.ascontiguousarray(labels, dtype=np.int32)
+        return self.lib.orc_modularity(offs.shape[0] - 1, _p(offs, _i64p), _p(nbr, _i32p), _p(w, _i32p),
+                                       _p(labels, _i32p))
+
+    def q_from_sums(self, sum_in, sum_tot2, m2):
+        return self.lib.orc_q_from_sums(sum_in, sum_tot2, m2)
