@@ -1,0 +1,298 @@
+"""End-to-end Louvain throughput on one GB300 (and N independent replicas).
+
+Workload: R-MAT, 2^22 ids, a/b/c/d = 0.57/0.19/0.19/0.05, 35.74M raw samples
+-> 34.7M undirected edges after removing duplicates and self-loops (69.4M CSR
+entries), unweighted, seed 1.  A step is one complete Louvain run: every
+round of phase 1 + contraction until the round gain is below 1e-6.
+
+  value   edges/s = m / (device time of one run), CSR already in HBM, timed
+          with CUDA events on the stream the engine runs on
+  e2e     the same through gala_louvain with host buffers: pinned CSR copied
+          host->device, all rounds, labels copied device->host, every step
+  roofline of the decide-and-move sweeps (algorithmic bytes / sweep time)
+  cpu_baseline  the CPU oracle (the reference's algorithm restated on the
+          host) on the same graph
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+N > 1 runs under torchrun: one independent replica per GPU (the path does
+not shard), barrier + max over ranks.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "gala-mg_gb300")
+sys.path.insert(0, PKG)
+sys.path.insert(0, os.path.join(ROOT, "tests"))
+
+WORKLOAD = {"workload": "rmat-s22-m34.7M", "generator": "R-MAT", "scale": 22, "raw_edges": 35_740_000,
+            "a": 0.57, "b": 0.19, "c": 0.19, "d": 0.05, "seed": 1, "keep_isolated_ids": True,
+            "weighted": False, "threshold": 1e-6}
+SMALL = dict(WORKLOAD, workload="rmat-s16-small", scale=16, raw_edges=600_000)
+METRIC = "end-to-end Louvain edges/s (all rounds to dQ<1e-6)"
+FALLBACK_HBM_GBS = 6800.0
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=5)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    p.add_argument("--small", action="store_true", help="tiny workload for a quick check")
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    return p.parse_args()
+
+
+def make_graph(wl):
+    import gala_ffi as ffi
+    return ffi.Graph.rmat(wl["scale"], wl["raw_edges"], wl["a"], wl["b"], wl["c"], seed=wl["seed"],
+                          keep_isolated=wl["keep_isolated_ids"])
+
+
+def measured_peak():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return FALLBACK_HBM_GBS, "fallback"
+
+
+def profile_traffic():
+    """DRAM bytes per decide launch from the committed ncu summary, if any."""
+    p = os.path.join(ROOT, "profiles", "decide_traffic.json")
+    try:
+        return json.load(open(p))
+    except Exception:
+        return None
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.t.join(timeout=2)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_oracle_run(offs, nbr, nthreads):
+    from oracle_ffi import Oracle
+    o = Oracle()
+    t = time.perf_counter()
+    r = o.louvain(offs, nbr, None, 1e-6, nthreads=nthreads)
+    return time.perf_counter() - t, r
+
+
+def reference_arm(args, wl):
+    """The reference's path on the host cores: the oracle port (the
+    reference's GPU algorithm restated on the CPU, all host threads)."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    g = make_graph(wl)
+    offs, nbr, _ = g.arrays()
+    m = int(offs[-1]) // 2
+    threads = os.cpu_count() or 1
+    for _ in range(args.warmup):
+        cpu_oracle_run(offs, nbr, threads)
+    times = []
+    for _ in range(args.steps):
+        dt, r = cpu_oracle_run(offs, nbr, threads)
+        times.append(dt)
+    sec = sum(times) / len(times)
+    val = m / sec
+    cfg = {k: v for k, v in wl.items()}
+    cfg.update({"vertices": int(offs.shape[0] - 1), "edges": m})
+    line = {"impl": "reference", "metric": METRIC, "value": val, "unit": "edges/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": sec * 1000, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "int32/f64", "data": "synthetic", "config": cfg,
+            "modularity": r["modularity"], "communities": r["level_c"][-1], "rounds": r["rounds"],
+            "cpu_baseline": {"value": val, "unit": "edges/s", "cores": threads, "kind": "port",
+                             "sample": "full run on the whole workload (all rounds), oracle/louvain_oracle.c"},
+            "e2e": {"value": val, "unit": "edges/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    wl = SMALL if args.small else WORKLOAD
+    if args.impl == "reference":
+        reference_arm(args, wl)
+        return
+    import torch
+    import gala_ffi as ffi
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+    g = make_graph(wl)
+    offs, nbr, _ = g.arrays()
+    n = offs.shape[0] - 1
+    E = int(offs[-1])
+    m = E // 2
+    max_deg = int((offs[1:] - offs[:-1]).max())
+    g.pin()
+    ctx = ffi.Context(n, E, device=local)
+    stream = torch.cuda.Stream()
+    ctx.set_stream(stream.cuda_stream)
+    d_offs = torch.from_numpy(offs).to(f"cuda:{local}")
+    d_nbr = torch.from_numpy(nbr).to(f"cuda:{local}")
+    d_out = torch.empty(n, dtype=torch.int32, device=f"cuda:{local}")
+    torch.cuda.synchronize()
+
+    def run_device():
+        return ctx.louvain_device(n, d_offs.data_ptr(), d_nbr.data_ptr(), None, d_out.data_ptr())
+
+    for _ in range(args.warmup):
+        r = run_device()
+    # ---- device-resident timed region ----
+    clocks = Clocks(local)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    time.sleep(0.3)
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    l0 = ffi.launch_count()
+    dec_bytes = dec_ms = 0.0
+    sweeps = 0
+    runs = []
+    with torch.cuda.stream(stream):
+        ev0.record(stream)
+        for _ in range(args.steps):
+            r = run_device()
+            runs.append(r)
+            dec_bytes += r["decide_bytes"]
+            dec_ms += r["time_decide_ms"]
+            sweeps += r["decide_sweeps"]
+        ev1.record(stream)
+    torch.cuda.synchronize()
+    launches = ffi.launch_count() - l0
+    clk = clocks.stop()
+    ms = ev0.elapsed_time(ev1) / args.steps
+    if dist:
+        t = torch.tensor([ms], device=f"cuda:{local}")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+        dist.barrier()
+    value = world * m / (ms / 1000.0)
+
+    # ---- end to end through the C ABI with host buffers ----
+    r_e2e = None
+    e2e_ms = []
+    for i in range(args.warmup + args.steps):
+        torch.cuda.synchronize()
+        with torch.cuda.stream(stream):
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            r_e2e = ctx.louvain(g)
+            b.record(stream)
+        torch.cuda.synchronize()
+        if i >= args.warmup:
+            e2e_ms.append(a.elapsed_time(b))
+    e2e_step = sum(e2e_ms) / len(e2e_ms)
+    if dist:
+        t = torch.tensor([e2e_step], device=f"cuda:{local}")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_step = float(t.item())
+
+    peak, peak_kind = measured_peak()
+    achieved = (dec_bytes / (dec_ms / 1000.0)) / 1e9 if dec_ms > 0 else 0.0
+    tr = profile_traffic()
+    roof = {"bound": "hbm", "kernel": "decide-and-move sweep (all degree bins of one iteration)",
+            "achieved": achieved, "peak": peak, "peak_kind": peak_kind, "unit": "GB/s",
+            "frac": achieved / peak, "traffic": (tr or {}).get("traffic_bytes_per_sweep"),
+            "algorithmic_bytes_per_sweep": dec_bytes / max(sweeps, 1),
+            "sweep_ms": dec_ms / max(sweeps, 1), "sweeps_per_run": sweeps / args.steps}
+
+    last = runs[-1]
+    cfg = {k: v for k, v in wl.items()}
+    cfg.update({"vertices": n, "edges": m, "csr_entries": E, "max_degree": max_deg,
+                "l2": "inputs larger than L2 (CSR %.0f MB > 129 MB)" % ((E * 4 + (n + 1) * 8) / 1e6),
+                "parallelism": f"replicas x{world}"})
+    line = {"metric": METRIC, "value": value, "unit": "edges/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "int32/f64", "data": "synthetic", "config": cfg,
+            "seconds_per_run": ms / 1000.0, "modularity": last["modularity"],
+            "communities": last["num_communities"], "rounds": last["rounds"],
+            "iterations": last["total_iterations"],
+            "phase_ms": {"phase1": last["time_phase1_ms"], "decide": last["time_decide_ms"],
+                         "update": last["time_update_ms"], "contract": last["time_contract_ms"]},
+            "e2e": {"value": world * m / (e2e_step / 1000.0), "unit": "edges/s", "ms_per_step": e2e_step,
+                    "h2d_bytes_per_step": r_e2e["h2d_bytes"], "d2h_bytes_per_step": r_e2e["d2h_bytes"]},
+            "roofline": roof, "clocks": clk, "gpu_launches": launches}
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        dt, ro = cpu_oracle_run(offs, nbr, threads)
+        line["cpu_baseline"] = {"value": m / dt, "unit": "edges/s", "cores": threads, "kind": "port",
+                                "sample": "one full run (all rounds) of the oracle on the whole workload",
+                                "seconds": dt, "modularity": ro["modularity"],
+                                "labels_equal_gpu": bool((ro["labels"] == r_e2e["labels"]).all())}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    ctx.close()
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

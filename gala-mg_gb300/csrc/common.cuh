@@ -53,9 +53,8 @@ struct DevStats {
     int pad0;
     int bin_start[kNumBinSlots + 1];  // order list: start of each bin
     int act_count[2][kNumBins];       // active list counts (ping-pong)
-    int small_cnt[3];                 // contraction: communities per size class
-    int pad1;
-    long long large_max_cap;          // contraction: largest capped row of class 2
+    int small_cnt[4];                 // contraction: communities per size class
+    long long total2;                 // scratch total of a second scan
     long long total;                  // scratch total of the last scan
 };
 
@@ -95,6 +94,21 @@ __device__ __forceinline__ bool prune_bound(int in_w, int self_w, int ki, int mi
     return __dadd_rn((double)ip, d) > 0.0;
 }
 
+// The same bound decided in exact integers: P = ip*m2 + (minTot - (Tot_c - K))*K
+// has the sign of the FP64 expression whenever P != 0 and K*m2 < 2^49 (the
+// FP64 error is below K*2^-50, non-zero P/m2 is at least 1/m2 away from 0);
+// otherwise the FP64 expression decides, as in the reference.
+__device__ __forceinline__ bool prune_bound_fast(int in_w, int self_w, int ki, int min_tot, int tot_c,
+                                                 double constant, long long m2)
+{
+    if ((long long)ki * m2 < (1LL << 49)) {
+        const int ip = 2 * (in_w - self_w) - (ki - self_w);
+        const long long p = (long long)ip * m2 + (long long)(min_tot - (tot_c - ki)) * (long long)ki;
+        if (p != 0) return p > 0;
+    }
+    return prune_bound(in_w, self_w, ki, min_tot, tot_c, constant);
+}
+
 // Candidate order: larger gain first, then the lower community id.
 __device__ __forceinline__ bool cand_better(double dq_a, int c_a, double dq_b, int c_b)
 {
@@ -108,11 +122,17 @@ __device__ __forceinline__ unsigned lanemask_lt()
     return m;
 }
 
+// Smallest power of two >= x (x <= 2^40).
+__host__ __device__ inline long long next_pow2_ll(long long x)
+{
+    long long p = 1;
+    while (p < x && p < (1LL << 40)) p <<= 1;
+    return p;
+}
 __host__ __device__ inline int next_pow2_int(long long x)
 {
-    int p = 1;
-    while (p < x) p <<= 1;
-    return p;
+    long long p = next_pow2_ll(x);
+    return p > (1LL << 30) ? (1 << 30) : (int)p;
 }
 
 // Open-addressing hash table with linear probing; keys int32 (-1 = empty),

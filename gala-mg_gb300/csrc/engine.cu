@@ -20,7 +20,8 @@ using namespace gala;
 
 struct gala_context {
     int device = 0;
-    cudaStream_t stream = nullptr;
+    cudaStream_t stream = nullptr;      // stream all work is ordered on
+    cudaStream_t own_stream = nullptr;  // the context's own stream
     int32_t n_cap = 0;
     int64_t e_cap = 0;
     int64_t *offs[2] = {nullptr, nullptr};
@@ -107,7 +108,7 @@ long long decide_bytes_for(long long nv, long long ne, bool weighted)
 // One phase-1 run on level graph g (louvain_main_process).  The accepted
 // partition is left in ctx->p1.comm.
 gala_status phase1(gala_context *ctx, const LevelGraph &g, long long &m2, double min_mod, bool verbose,
-                   std::vector<double> *trace, Phase1Out *out)
+                   std::vector<double> *trace, Phase1Out *out, int fp64_only = 0)
 {
     cudaStream_t st = ctx->stream;
     Phase1Buffers &b = ctx->p1;
@@ -184,13 +185,13 @@ gala_status phase1(gala_context *ctx, const LevelGraph &g, long long &m2, double
         const int32_t *lists = iteration == 1 ? b.order : b.act[cur];
         for (int bin = 0; bin < kNumBins; ++bin)
             p1_decide(g, b, bin, lists + bin_start[bin], &b.stats->act_count[cur][bin], level_cnt[bin], constant,
-                      hub_tmax, st);
+                      m2, fp64_only, hub_tmax, st);
         cudaEventRecord(ctx->ev[3], st);
         p1_apply_movers(b, +1, g.n, st);
         p1_tot_reduce(b, g.n, st);
         cudaEventRecord(ctx->ev[4], st);
         for (int bin = 0; bin < kNumBins; ++bin)
-            p1_update(g, b, bin, b.order + bin_start[bin], level_cnt[bin], nxt, bin_start[bin], constant, st);
+            p1_update(g, b, bin, b.order + bin_start[bin], level_cnt[bin], nxt, bin_start[bin], constant, m2, st);
         cudaEventRecord(ctx->ev[5], st);
         if ((s = check(cudaMemcpyAsync(h, b.stats, sizeof(DevStats), cudaMemcpyDeviceToHost, st), "iteration")) ||
             (s = check(cudaStreamSynchronize(st), "iteration")))
@@ -237,11 +238,8 @@ void bind_contract_buffers(gala_context *ctx)
     ContractBuffers &cb = ctx->cb;
     cb.stats = ctx->d_stats;
     cb.scan_partial = ctx->p1.scan_partial;
-    long long half = ctx->scratch_ints / 2;
-    cb.big_table = ctx->scratch;
-    cb.big_table_slots = half;
-    cb.big_bitmap = ctx->scratch + half;
-    cb.big_bitmap_words = half;
+    cb.big_bitmap = ctx->scratch;
+    cb.big_bitmap_words = ctx->scratch_ints;
 }
 
 struct RunOut {
@@ -285,7 +283,7 @@ gala_status run_levels(gala_context *ctx, int32_t n0, int64_t E0, const int64_t 
     for (;;) {
         if (verbose) printf("===============round:%d===============\n", round);
         Phase1Out po;
-        if ((s = phase1(ctx, g, m2, min_mod, verbose, &trace, &po))) return s;
+        if ((s = phase1(ctx, g, m2, min_mod, verbose, &trace, &po, opt ? opt->fp64_gains : 0))) return s;
         p1_ms += po.total_ms;
         dec_ms += po.decide_ms;
         upd_ms += po.update_ms;
@@ -378,7 +376,7 @@ void gala_context_destroy(gala_context *ctx)
     if (ctx->h_stats) cudaFreeHost(ctx->h_stats);
     for (auto &e : ctx->ev)
         if (e) cudaEventDestroy(e);
-    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
     cudaSetDevice(prev);
     delete ctx;
 }
@@ -411,7 +409,8 @@ gala_status gala_context_create(int32_t device, int32_t max_vertices, int64_t ma
     const size_t nblk = (n + 1023) / 1024;
     const size_t scan_items = std::max(n + 2, (size_t)kNumBinSlots * nblk);
     const size_t nparts = scan_items / 4096 + 4;
-    bool ok = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) == cudaSuccess;
+    bool ok = cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamNonBlocking) == cudaSuccess;
+    ctx->stream = ctx->own_stream;
     for (auto &e : ctx->ev) ok = ok && cudaEventCreate(&e) == cudaSuccess;
     ok = ok && cudaMallocHost(&ctx->h_stats, sizeof(DevStats)) == cudaSuccess;
     for (int i = 0; i < 2 && ok; ++i)
@@ -429,9 +428,16 @@ gala_status gala_context_create(int32_t device, int32_t max_vertices, int64_t ma
          dalloc(ctx, &c.members, n) && dalloc(ctx, &c.mpos, n) && dalloc(ctx, &c.ec, n + 1) &&
          dalloc(ctx, &c.medge, n + 1) && dalloc(ctx, &c.stream_key, E) && dalloc(ctx, &c.stream_w, E) &&
          dalloc(ctx, &c.tmp_off, n + 1) && dalloc(ctx, &c.tmp_nbr, E) && dalloc(ctx, &c.tmp_w, E) &&
-         dalloc(ctx, &c.kc, n + 1) && dalloc(ctx, &c.cls_list, 3 * n);
-    // scratch pool for hub tables (phase 1) and the large-row tables and
-    // bitmaps of the contraction: 8 ints per entry+vertex, 16 MB .. 512 MB
+         dalloc(ctx, &c.kc, n + 1) && dalloc(ctx, &c.cls_list, 4 * n);
+    // tables of the rows longer than 4096 entries: at most 4 slots per entry
+    // (keys + values), chunk list of at most E / 4096 + n entries
+    c.big_pool_ints = 8LL * (long long)E + 64;
+    c.big_work_cap = (long long)E / 4096 + (long long)n + 1;
+    ok = ok && dalloc(ctx, &c.big_pool, (size_t)c.big_pool_ints) && dalloc(ctx, &c.big_T, n) &&
+         dalloc(ctx, &c.big_chunks, n) && dalloc(ctx, &c.big_toff, n + 1) && dalloc(ctx, &c.big_coff, n + 1) &&
+         dalloc(ctx, &c.big_mode, n) && dalloc(ctx, &c.big_work, (size_t)c.big_work_cap);
+    // scratch pool for hub tables (phase 1) and the emission bitmaps of the
+    // contraction: 8 ints per entry+vertex, 16 MB .. 512 MB
     long long want = 8LL * ((long long)E + (long long)n);
     want = std::max(want, 4LL << 20);
     want = std::min(want, 128LL << 20);
@@ -455,6 +461,20 @@ gala_status gala_context_create(int32_t device, int32_t max_vertices, int64_t ma
         return cuda_fail(ce, "gala_context_create");
     }
     *out = ctx;
+    return GALA_OK;
+}
+
+gala_status gala_context_set_stream(gala_context *ctx, void *stream)
+{
+    clear_error();
+    if (!ctx) {
+        set_error("gala_context_set_stream: null context");
+        return GALA_ERR_INVALID;
+    }
+    cudaSetDevice(ctx->device);
+    gala_status s = check(cudaStreamSynchronize(ctx->stream), "gala_context_set_stream");
+    if (s) return s;
+    ctx->stream = stream ? (cudaStream_t)stream : ctx->own_stream;
     return GALA_OK;
 }
 

@@ -103,11 +103,11 @@ static gala_status validate(const gala_graph *g)
 // edges and renumber in id order (graph.cpp:76-107).  A self-loop line adds
 // the loop twice to its row before deduplication, as graph.cpp:47-48 does.
 static gala_graph *build_csr(std::vector<std::pair<int32_t, int32_t>> &edges, const std::vector<int32_t> *wts,
-                             bool weighted, int nthreads)
+                             bool weighted, int nthreads, int64_t keep_ids = 0)
 {
     int32_t maxid = -1;
     for (auto &e : edges) maxid = std::max(maxid, std::max(e.first, e.second));
-    const int64_t nid = (int64_t)maxid + 1;
+    const int64_t nid = std::max((int64_t)maxid + 1, keep_ids);
     std::vector<int64_t> deg(nid + 1, 0);
     for (auto &e : edges) {
         deg[e.first + 1]++;
@@ -153,18 +153,18 @@ static gala_graph *build_csr(std::vector<std::pair<int32_t, int32_t>> &edges, co
             newlen[r] = o - s;
         }
     });
-    // renumber ids with edges, in id order
+    // renumber ids with edges, in id order (all ids when keep_ids is set)
     std::vector<int32_t> renum(nid, -1);
     int32_t n = 0;
     for (int64_t i = 0; i < nid; ++i)
-        if (newlen[i] > 0) renum[i] = n++;
+        if (newlen[i] > 0 || keep_ids > 0) renum[i] = n++;
     gala_graph *g = new gala_graph();
     g->n = n;
     g->weighted = weighted;
     g->offs.resize(n);
     int64_t acc = 0;
     for (int64_t i = 0; i < nid; ++i)
-        if (newlen[i] > 0) {
+        if (renum[i] >= 0) {
             acc += newlen[i];
             g->offs[renum[i]] = acc;
         }
@@ -188,7 +188,39 @@ static gala_graph *build_csr(std::vector<std::pair<int32_t, int32_t>> &edges, co
 
 using namespace gala;
 
+gala_graph::~gala_graph()
+{
+    if (pinned) {
+        if (!offs.empty()) cudaHostUnregister(offs.data());
+        if (!nbr.empty()) cudaHostUnregister(nbr.data());
+        if (!w.empty()) cudaHostUnregister(w.data());
+        cudaGetLastError();
+    }
+}
+
 extern "C" {
+
+gala_status gala_graph_pin(gala_graph *g)
+{
+    clear_error();
+    if (!g) {
+        set_error("gala_graph_pin: null graph");
+        return GALA_ERR_INVALID;
+    }
+    if (g->pinned) return GALA_OK;
+    cudaError_t e = cudaSuccess;
+    if (!g->offs.empty()) e = cudaHostRegister(g->offs.data(), g->offs.size() * sizeof(int64_t), 0);
+    if (e == cudaSuccess && !g->nbr.empty()) e = cudaHostRegister(g->nbr.data(), g->nbr.size() * sizeof(int32_t), 0);
+    if (e == cudaSuccess && !g->w.empty()) e = cudaHostRegister(g->w.data(), g->w.size() * sizeof(int32_t), 0);
+    if (e != cudaSuccess) {
+        cudaHostUnregister(g->offs.data());
+        cudaHostUnregister(g->nbr.data());
+        if (!g->w.empty()) cudaHostUnregister(g->w.data());
+        return cuda_fail(e, "gala_graph_pin");
+    }
+    g->pinned = true;
+    return GALA_OK;
+}
 
 const char *gala_last_error(void) { return g_err.c_str(); }
 
@@ -516,7 +548,7 @@ gala_status gala_generate_sbm(int32_t n, int32_t k, double p_in, double p_out, u
 }
 
 gala_status gala_generate_rmat(int32_t scale, int64_t nedges, double a, double b, double c, double noise,
-                               uint64_t seed, int32_t nthreads, gala_graph **out)
+                               int32_t keep_isolated, uint64_t seed, int32_t nthreads, gala_graph **out)
 {
     clear_error();
     if (!out || scale < 1 || scale > 30 || nedges <= 0 || a < 0 || b < 0 || c < 0 || a + b + c > 1 ||
@@ -572,7 +604,7 @@ gala_status gala_generate_rmat(int32_t scale, int64_t nedges, double a, double b
         if (keep[i]) edges[o++] = edges[i];
     edges.resize(o);
     std::vector<char>().swap(keep);
-    *out = build_csr(edges, nullptr, false, nt);
+    *out = build_csr(edges, nullptr, false, nt, keep_isolated ? (int64_t)1 << scale : 0);
     return GALA_OK;
 }
 

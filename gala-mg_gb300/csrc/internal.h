@@ -17,7 +17,9 @@ struct gala_graph {
     std::vector<int32_t> nbr;   // offs[n-1] entries
     std::vector<int32_t> w;     // empty when unweighted
     bool weighted = false;
+    bool pinned = false;  // arrays registered with cudaHostRegister
     int64_t entries() const { return n ? offs[n - 1] : 0; }
+    ~gala_graph();
 };
 
 namespace gala {
@@ -57,12 +59,12 @@ struct Phase1Buffers {
 void p1_level_init(const LevelGraph &g, Phase1Buffers &b, cudaStream_t st);
 void p1_iter_reset(Phase1Buffers &b, int next, int min_tot_init, cudaStream_t st);
 void p1_decide(const LevelGraph &g, Phase1Buffers &b, int bin, const int32_t *list,
-               const int *count_ptr, int level_count, double constant, int hub_tmax,
-               cudaStream_t st);
+               const int *count_ptr, int level_count, double constant, long long m2,
+               int fp64_only, int hub_tmax, cudaStream_t st);
 void p1_apply_movers(Phase1Buffers &b, int sign, int n, cudaStream_t st);
 void p1_tot_reduce(Phase1Buffers &b, int n, cudaStream_t st);
 void p1_update(const LevelGraph &g, Phase1Buffers &b, int bin, const int32_t *list, int count, int next,
-               int bin_start, double constant, cudaStream_t st);
+               int bin_start, double constant, long long m2, cudaStream_t st);
 void p1_level_init_rows(const LevelGraph &g, Phase1Buffers &b, const int *bin_start, cudaStream_t st);
 void p1_configure_kernels();
 void contract_configure_kernels();
@@ -88,9 +90,18 @@ struct ContractBuffers {
     int32_t *tmp_w;      // E
     int32_t *kc;         // n+1 distinct neighbours per community
     int32_t *cls_list;   // n: communities by size class
-    int32_t *big_table;  // per-CTA global hash tables (class 2)
-    long long big_table_slots;
-    int32_t *big_bitmap; // per-CTA bitmaps over communities (class 2)
+    // rows of more than 4096 entries: one global table per community, filled
+    // by many CTAs (chunks of the stream), then emitted by one CTA each
+    int32_t *big_pool;        // keys then values of all tables
+    long long big_pool_ints;
+    long long *big_T;         // n: table slots per community (list order)
+    long long *big_chunks;    // n: stream chunks per community
+    long long *big_toff;      // n+1: table offsets
+    long long *big_coff;      // n+1: chunk offsets
+    int32_t *big_mode;        // n: 1 = dense table indexed by community id
+    int32_t *big_work;        // chunk -> list index
+    long long big_work_cap;
+    int32_t *big_bitmap;      // per-CTA bitmaps over communities (emission)
     long long big_bitmap_words;
     long long *scan_partial;
     DevStats *stats;

@@ -326,19 +326,89 @@ struct DecideArgs {
     const int32_t *__restrict__ size;
     int32_t *mv_v, *mv_old, *mv_new;
     DevStats *st;
-    double constant;
+    double constant;  // 1 / m2
+    long long m2;
+    int fp64_only;    // 1 = evaluate every vertex with the FP64 expressions
 };
 
-// Final decision of a vertex (kernel_functions.cu:381-409): move only for a
-// positive corrected gain, and never swap two singletons towards the larger
-// id (the guard at :386).
+// Singleton swap guard (kernel_functions.cu:386): two singletons never move
+// towards the larger id.
+__device__ __forceinline__ bool guard_ok(const DecideArgs &a, int cur, int best)
+{
+    return !(a.size[best] == 1 && a.size[cur] == 1 && best > cur);
+}
+
+// Final decision of a vertex from the FP64 gain (kernel_functions.cu:381-409):
+// move only for a positive corrected gain.
 __device__ __forceinline__ bool decide_move(const DecideArgs &a, int cur, int best, double maxdq, int w_cur,
                                             int self_w)
 {
     if (best == cur) return false;
     if (!(gain_correct(maxdq, w_cur, self_w) > 0.0)) return false;
-    if (a.size[best] == 1 && a.size[cur] == 1 && best > cur) return false;
-    return true;
+    return guard_ok(a, cur, best);
+}
+
+// ---- exact integer gains ---------------------------------------------------
+// The reference's gain dq = 2w - 2K((Tot_c - Tot_cur) + K)/m2 equals
+// (2/m2) * X with the integer X = w*m2 - K*((Tot_c - Tot_cur) + K), which fits
+// int64 for m2 < 2^31.  Distinct X differ by at least 2/m2 in dq, while the
+// FP64 evaluation errs by at most K * 2^-50; so for K*m2 < 2^49 the FP64 order
+// of distinct X is the exact order and the sign of a non-zero X (or of the
+// corrected gain) is exact.  Three cases can still round either way and are
+// re-evaluated with the FP64 expressions of the reference: equal best X from
+// different weights (FP64 may order them by value, not by id), X = 0 when
+// the vertex has no other weight in its community, and a corrected gain of
+// exactly 0.  Everything else is decided in integer arithmetic (GB300 runs
+// FP64 at a small fraction of its integer rate).
+__device__ __forceinline__ long long gain_x(int w, int ki, int tc, int tcur, long long m2)
+{
+    return (long long)w * m2 - (long long)ki * ((long long)tc - (long long)tcur + (long long)ki);
+}
+
+// Merge candidate (ox, oc, ow, ot) into (x, c, w, t): larger X first, then the
+// lower id; t records a tie on the best X between different weights.
+// Commutative, so butterfly reductions agree on every lane.
+__device__ __forceinline__ void cand_merge(long long &x, int &c, int &w, int &t, long long ox, int oc, int ow,
+                                           int ot)
+{
+    if (ox == x) {
+        int tie = t | ot | (ow != w);
+        if (oc < c) {
+            c = oc;
+            w = ow;
+        }
+        t = tie;
+    } else if (ox > x) {
+        x = ox;
+        c = oc;
+        w = ow;
+        t = ot;
+    }
+}
+
+// 0 = stay, 1 = move (before the singleton guard), 2 = evaluate in FP64.
+__device__ __forceinline__ int int_decision(const DecideArgs &a, long long x, int t, int cur, int best, int w_cur,
+                                            int self_w, int ki)
+{
+    if (a.fp64_only || (long long)ki * a.m2 >= (1LL << 49)) return 2;
+    if (best == cur) return 0;  // every candidate has X < 0: every FP64 gain is < 0
+    if (x == 0) return w_cur == self_w ? 2 : 0;
+    if (t) return 2;
+    const long long y = x - (long long)(w_cur - self_w) * a.m2;
+    if (y == 0) return 2;
+    return y > 0 ? 1 : 0;
+}
+
+__device__ __forceinline__ void warp_merge_int(long long &x, int &c, int &w, int &t, int &wc, int width)
+{
+    for (int o = width / 2; o >= 1; o >>= 1) {
+        long long ox = __shfl_xor_sync(GALA_FULL_MASK, x, o);
+        int oc = __shfl_xor_sync(GALA_FULL_MASK, c, o);
+        int ow = __shfl_xor_sync(GALA_FULL_MASK, w, o);
+        int ot = __shfl_xor_sync(GALA_FULL_MASK, t, o);
+        wc += __shfl_xor_sync(GALA_FULL_MASK, wc, o);
+        cand_merge(x, c, w, t, ox, oc, ow, ot);
+    }
 }
 
 __device__ __forceinline__ void append_mover(const DecideArgs &a, bool move, int v, int cur, int best)
@@ -395,60 +465,96 @@ __global__ void __launch_bounds__(256) k_decide_group(DecideArgs a, const int32_
         const unsigned m = __match_any_sync(GALA_FULL_MASK, key);
         const int wsum = W ? (int)__reduce_add_sync(m, (unsigned)wt) : __popc(m);
         const bool leader = valid && (__ffs(m) - 1 == lane);
-        int wc = (leader && c == cur) ? wsum : 0;
-        double dq = 0.0;
-        int bc = cur;
+        const int wc_own = (leader && c == cur) ? wsum : 0;
+        int wc = wc_own;
+        int tc = 0;
+        long long x = -1;
+        int bc = cur, bw = 0, bt = 0;
         if (leader && c != cur) {
-            double d = gain_dq(wsum, ki, a.Tot[c], tcur, a.constant);
-            if (d > 0.0) {
-                dq = d;
+            tc = a.Tot[c];
+            const long long xx = gain_x(wsum, ki, tc, tcur, a.m2);
+            if (xx >= 0) {
+                x = xx;
                 bc = c;
+                bw = wsum;
             }
         }
+        warp_merge_int(x, bc, bw, bt, wc, G);
+        int dec = 0;
+        if (has && sub == 0) dec = int_decision(a, x, bt, cur, bc, wc, sf, ki);
+        const bool fp = dec == 2;
+        if (__any_sync(GALA_FULL_MASK, fp)) {
+            // the reference's FP64 evaluation of the same candidates
+            double dq = 0.0;
+            int fc = cur;
+            if (leader && c != cur) {
+                const double d = gain_dq(wsum, ki, tc, tcur, a.constant);
+                if (d > 0.0) {
+                    dq = d;
+                    fc = c;
+                }
+            }
 #pragma unroll
-        for (int o = G / 2; o >= 1; o >>= 1) {
-            double od = __shfl_xor_sync(GALA_FULL_MASK, dq, o);
-            int oc = __shfl_xor_sync(GALA_FULL_MASK, bc, o);
-            wc += __shfl_xor_sync(GALA_FULL_MASK, wc, o);
-            if (cand_better(od, oc, dq, bc)) {
-                dq = od;
-                bc = oc;
+            for (int o = G / 2; o >= 1; o >>= 1) {
+                const double od = __shfl_xor_sync(GALA_FULL_MASK, dq, o);
+                const int oc = __shfl_xor_sync(GALA_FULL_MASK, fc, o);
+                if (cand_better(od, oc, dq, fc)) {
+                    dq = od;
+                    fc = oc;
+                }
+            }
+            if (fp) {
+                bc = fc;
+                dec = (fc != cur && gain_correct(dq, wc, sf) > 0.0) ? 1 : 0;
             }
         }
-        bool move = has && sub == 0 && decide_move(a, cur, bc, dq, wc, sf);
+        const bool move = has && sub == 0 && dec == 1 && guard_ok(a, cur, bc);
         append_mover(a, move, v, cur, bc);
     }
 }
 
-// Scan a hash table and return this thread's best candidate and its share of
+// Scan a hash table: this thread's best candidate by exact X and its share of
 // the weight to the own community.
-__device__ __forceinline__ void scan_table(const DecideArgs &a, const int *keys, const int *vals, int T,
-                                           int first, int stride, int cur, int ki, int tcur, double &dq,
-                                           int &bc, int &wc)
+__device__ __forceinline__ void scan_table_int(const DecideArgs &a, const int *keys, const int *vals, int T,
+                                               int first, int stride, int cur, int ki, int tcur, long long &x,
+                                               int &bc, int &bw, int &bt, int &wc)
 {
     for (int j = first; j < T; j += stride) {
-        int c = keys[j];
+        const int c = keys[j];
         if (c < 0) continue;
-        int wv = vals[j];
+        const int wv = vals[j];
         if (c == cur) {
             wc += wv;
         } else {
-            double d = gain_dq(wv, ki, a.Tot[c], tcur, a.constant);
-            if (d > 0.0 && cand_better(d, c, dq, bc)) {
-                dq = d;
-                bc = c;
-            }
+            const long long xx = gain_x(wv, ki, a.Tot[c], tcur, a.m2);
+            if (xx >= 0) cand_merge(x, bc, bw, bt, xx, c, wv, 0);
         }
     }
 }
 
-__device__ __forceinline__ void warp_argmax(double &dq, int &bc, int &wc)
+// The same scan with the reference's FP64 gains (vertices int_decision
+// cannot settle).
+__device__ __forceinline__ void scan_table(const DecideArgs &a, const int *keys, const int *vals, int T,
+                                           int first, int stride, int cur, int ki, int tcur, double &dq,
+                                           int &bc)
+{
+    for (int j = first; j < T; j += stride) {
+        int c = keys[j];
+        if (c < 0 || c == cur) continue;
+        double d = gain_dq(vals[j], ki, a.Tot[c], tcur, a.constant);
+        if (d > 0.0 && cand_better(d, c, dq, bc)) {
+            dq = d;
+            bc = c;
+        }
+    }
+}
+
+__device__ __forceinline__ void warp_argmax(double &dq, int &bc)
 {
 #pragma unroll
     for (int o = 16; o >= 1; o >>= 1) {
         double od = __shfl_xor_sync(GALA_FULL_MASK, dq, o);
         int oc = __shfl_xor_sync(GALA_FULL_MASK, bc, o);
-        wc += __shfl_xor_sync(GALA_FULL_MASK, wc, o);
         if (cand_better(od, oc, dq, bc)) {
             dq = od;
             bc = oc;
@@ -499,11 +605,20 @@ __global__ void __launch_bounds__(256) k_decide_warp(DecideArgs a, const int32_t
         }
         __syncwarp();
         const int ki = a.K[v], tcur = a.Tot[cur], sf = a.Self[v];
-        double dq = 0.0;
-        int bc = cur, wc = 0;
-        scan_table(a, keys, vals, T, lane, 32, cur, ki, tcur, dq, bc, wc);
-        warp_argmax(dq, bc, wc);
-        bool move = lane == 0 && decide_move(a, cur, bc, dq, wc, sf);
+        long long x = -1;
+        int bc = cur, bw = 0, bt = 0, wc = 0;
+        scan_table_int(a, keys, vals, T, lane, 32, cur, ki, tcur, x, bc, bw, bt, wc);
+        warp_merge_int(x, bc, bw, bt, wc, 32);
+        int dec = int_decision(a, x, bt, cur, bc, wc, sf, ki);  // warp-uniform
+        if (dec == 2) {
+            double dq = 0.0;
+            int fc = cur;
+            scan_table(a, keys, vals, T, lane, 32, cur, ki, tcur, dq, fc);
+            warp_argmax(dq, fc);
+            bc = fc;
+            dec = (fc != cur && gain_correct(dq, wc, sf) > 0.0) ? 1 : 0;
+        }
+        const bool move = lane == 0 && dec == 1 && guard_ok(a, cur, bc);
         append_mover(a, move, v, cur, bc);
         __syncwarp();
     }
@@ -519,8 +634,12 @@ __global__ void __launch_bounds__(BLOCK) k_decide_cta(DecideArgs a, const int32_
 {
     extern __shared__ int dyn_smem[];
     __shared__ double r_dq[BLOCK / 32];
+    __shared__ long long r_x[BLOCK / 32];
     __shared__ int r_c[BLOCK / 32];
     __shared__ int r_w[BLOCK / 32];
+    __shared__ int r_t[BLOCK / 32];
+    __shared__ int r_wc[BLOCK / 32];
+    __shared__ int s_dec, s_bc, s_wc;
     int *keys = GMEM ? gtab + (long long)blockIdx.x * 2 * tmax : dyn_smem;
     int *vals = keys + tmax;
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -558,23 +677,57 @@ __global__ void __launch_bounds__(BLOCK) k_decide_cta(DecideArgs a, const int32_
         }
         __syncthreads();
         const int ki = a.K[v], tcur = a.Tot[cur], sf = a.Self[v];
-        double dq = 0.0;
-        int bc = cur, wc = 0;
-        scan_table(a, keys, vals, T, threadIdx.x, BLOCK, cur, ki, tcur, dq, bc, wc);
-        warp_argmax(dq, bc, wc);
+        constexpr int NW = BLOCK / 32;
+        long long x = -1;
+        int bc = cur, bw = 0, bt = 0, wc = 0;
+        scan_table_int(a, keys, vals, T, threadIdx.x, BLOCK, cur, ki, tcur, x, bc, bw, bt, wc);
+        warp_merge_int(x, bc, bw, bt, wc, 32);
         if (lane == 0) {
-            r_dq[wid] = dq;
+            r_x[wid] = x;
             r_c[wid] = bc;
-            r_w[wid] = wc;
+            r_w[wid] = bw;
+            r_t[wid] = bt;
+            r_wc[wid] = wc;
         }
         __syncthreads();
         if (wid == 0) {
-            dq = lane < BLOCK / 32 ? r_dq[lane] : 0.0;
-            bc = lane < BLOCK / 32 ? r_c[lane] : cur;
-            wc = lane < BLOCK / 32 ? r_w[lane] : 0;
-            warp_argmax(dq, bc, wc);
-            bool move = lane == 0 && decide_move(a, cur, bc, dq, wc, sf);
-            append_mover(a, move, v, cur, bc);
+            x = lane < NW ? r_x[lane] : -1;
+            bc = lane < NW ? r_c[lane] : cur;
+            bw = lane < NW ? r_w[lane] : 0;
+            bt = lane < NW ? r_t[lane] : 0;
+            wc = lane < NW ? r_wc[lane] : 0;
+            warp_merge_int(x, bc, bw, bt, wc, 32);
+            if (lane == 0) {
+                s_dec = int_decision(a, x, bt, cur, bc, wc, sf, ki);
+                s_bc = bc;
+                s_wc = wc;
+            }
+        }
+        __syncthreads();
+        if (s_dec == 2) {  // block-uniform: the reference's FP64 evaluation
+            double dq = 0.0;
+            int fc = cur;
+            scan_table(a, keys, vals, T, threadIdx.x, BLOCK, cur, ki, tcur, dq, fc);
+            warp_argmax(dq, fc);
+            if (lane == 0) {
+                r_dq[wid] = dq;
+                r_c[wid] = fc;
+            }
+            __syncthreads();
+            if (wid == 0) {
+                dq = lane < NW ? r_dq[lane] : 0.0;
+                fc = lane < NW ? r_c[lane] : cur;
+                warp_argmax(dq, fc);
+                if (lane == 0) {
+                    s_bc = fc;
+                    s_dec = (fc != cur && gain_correct(dq, s_wc, sf) > 0.0) ? 1 : 0;
+                }
+            }
+            __syncthreads();
+        }
+        if (wid == 0) {
+            const bool move = lane == 0 && s_dec == 1 && guard_ok(a, cur, s_bc);
+            append_mover(a, move, v, cur, s_bc);
         }
         __syncthreads();
     }
@@ -584,7 +737,7 @@ constexpr int kCtaTable5 = 4096;
 constexpr int kCtaTable6 = 16384;
 
 void p1_decide(const LevelGraph &g, Phase1Buffers &b, int bin, const int32_t *list, const int *count_ptr,
-               int level_count, double constant, int hub_tmax, cudaStream_t st)
+               int level_count, double constant, long long m2, int fp64_only, int hub_tmax, cudaStream_t st)
 {
     if (level_count <= 0) return;
     DecideArgs a;
@@ -601,6 +754,8 @@ void p1_decide(const LevelGraph &g, Phase1Buffers &b, int bin, const int32_t *li
     a.mv_new = b.mv_new;
     a.st = b.stats;
     a.constant = constant;
+    a.m2 = m2;
+    a.fp64_only = fp64_only;
     const bool W = g.w != nullptr;
     const int cap = num_sms() * 8;
     auto grid_lanes = [&](int lanes_per_item) {
@@ -761,6 +916,7 @@ struct UpdateArgs {
     int *act_counter;
     DevStats *st;
     double constant;
+    long long m2;
     int next;
 };
 
@@ -794,7 +950,7 @@ __global__ void __launch_bounds__(256) k_update_group(UpdateArgs a, const int32_
         if (has && sub == 0) {
             a.In[v] = sum;
             const int ki = a.K[v];
-            active = !prune_bound(sum, a.Self[v], ki, min_tot, a.Tot[cur], a.constant);
+            active = !prune_bound_fast(sum, a.Self[v], ki, min_tot, a.Tot[cur], a.constant, a.m2);
             s_in += (unsigned long long)sum;
             if (active) {
                 s_edges += (unsigned long long)(e - s);
@@ -830,7 +986,7 @@ __global__ void __launch_bounds__(256) k_update_cta(UpdateArgs a, const int32_t 
             for (int q = 0; q < (int)(blockDim.x >> 5); ++q) sum += red[q];
             a.In[v] = sum;
             const int ki = a.K[v];
-            bool active = !prune_bound(sum, a.Self[v], ki, min_tot, a.Tot[cur], a.constant);
+            bool active = !prune_bound_fast(sum, a.Self[v], ki, min_tot, a.Tot[cur], a.constant, a.m2);
             s_in += (unsigned long long)sum;
             if (active) {
                 a.act_list[atomicAdd(a.act_counter, 1)] = v;
@@ -846,7 +1002,7 @@ __global__ void __launch_bounds__(256) k_update_cta(UpdateArgs a, const int32_t 
 }
 
 void p1_update(const LevelGraph &g, Phase1Buffers &b, int bin, const int32_t *list, int count, int next,
-               int bin_start, double constant, cudaStream_t st)
+               int bin_start, double constant, long long m2, cudaStream_t st)
 {
     if (count <= 0) return;
     UpdateArgs a;
@@ -862,6 +1018,7 @@ void p1_update(const LevelGraph &g, Phase1Buffers &b, int bin, const int32_t *li
     a.act_counter = &b.stats->act_count[next][bin];
     a.st = b.stats;
     a.constant = constant;
+    a.m2 = m2;
     a.next = next;
     const bool W = g.w != nullptr;
     const int cap = num_sms() * 8;

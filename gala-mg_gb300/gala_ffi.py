@@ -21,8 +21,9 @@ STATUS = {0: "GALA_OK", 1: "GALA_ERR_INVALID", 2: "GALA_ERR_IO", 3: "GALA_ERR_FO
 EXPORTS = ["gala_last_error", "gala_status_string", "gala_kernel_launch_count", "gala_default_options",
            "gala_graph_load_bin", "gala_graph_store_bin", "gala_graph_from_text", "gala_graph_from_csr",
            "gala_graph_info", "gala_graph_arrays", "gala_graph_destroy", "gala_generate_sbm",
-           "gala_generate_rmat", "gala_context_create", "gala_context_destroy", "gala_louvain",
-           "gala_louvain_device", "gala_phase1_device", "gala_contract_device", "gala_modularity_host"]
+           "gala_generate_rmat", "gala_context_create", "gala_context_destroy", "gala_context_set_stream",
+           "gala_graph_pin", "gala_louvain", "gala_louvain_device", "gala_phase1_device", "gala_contract_device",
+           "gala_modularity_host"]
 
 _i32p = ctypes.POINTER(ctypes.c_int32)
 _i64p = ctypes.POINTER(ctypes.c_int64)
@@ -38,7 +39,7 @@ class GalaError(RuntimeError):
 
 class Options(ctypes.Structure):
     _fields_ = [("min_modularity", ctypes.c_double), ("max_levels", ctypes.c_int32),
-                ("verbose", ctypes.c_int32), ("use_graphs", ctypes.c_int32), ("reserved", ctypes.c_int32)]
+                ("verbose", ctypes.c_int32), ("use_graphs", ctypes.c_int32), ("fp64_gains", ctypes.c_int32)]
 
 
 class Result(ctypes.Structure):
@@ -101,11 +102,13 @@ def load(path=LIB_PATH):
     L.gala_generate_sbm.argtypes = [ctypes.c_int32, ctypes.c_int32, ctypes.c_double, ctypes.c_double,
                                     ctypes.c_uint64, ctypes.POINTER(_vp)]
     L.gala_generate_rmat.argtypes = [ctypes.c_int32, ctypes.c_int64, ctypes.c_double, ctypes.c_double,
-                                     ctypes.c_double, ctypes.c_double, ctypes.c_uint64, ctypes.c_int32,
-                                     ctypes.POINTER(_vp)]
+                                     ctypes.c_double, ctypes.c_double, ctypes.c_int32, ctypes.c_uint64,
+                                     ctypes.c_int32, ctypes.POINTER(_vp)]
     L.gala_context_create.argtypes = [ctypes.c_int32, ctypes.c_int32, ctypes.c_int64, ctypes.POINTER(_vp)]
     L.gala_context_destroy.argtypes = [_vp]
     L.gala_context_destroy.restype = None
+    L.gala_context_set_stream.argtypes = [_vp, _vp]
+    L.gala_graph_pin.argtypes = [_vp]
     L.gala_louvain.argtypes = [_vp, _vp, ctypes.POINTER(Options), _i32p, ctypes.POINTER(Result)]
     L.gala_louvain_device.argtypes = [_vp, ctypes.c_int32, _vp, _vp, _vp, ctypes.POINTER(Options), _vp,
                                       ctypes.POINTER(Result)]
@@ -115,8 +118,8 @@ def load(path=LIB_PATH):
     L.gala_modularity_host.argtypes = [_vp, _i32p, _f64p]
     for name in ["gala_graph_load_bin", "gala_graph_store_bin", "gala_graph_from_text", "gala_graph_from_csr",
                  "gala_graph_info", "gala_graph_arrays", "gala_generate_sbm", "gala_generate_rmat",
-                 "gala_context_create", "gala_louvain", "gala_louvain_device", "gala_phase1_device",
-                 "gala_contract_device", "gala_modularity_host"]:
+                 "gala_context_create", "gala_context_set_stream", "gala_graph_pin", "gala_louvain",
+                 "gala_louvain_device", "gala_phase1_device", "gala_contract_device", "gala_modularity_host"]:
         getattr(L, name).restype = ctypes.c_int
     _lib = L
     return L
@@ -186,13 +189,17 @@ class Graph:
         return Graph(h)
 
     @staticmethod
-    def rmat(scale, edges, a=0.57, b=0.19, c=0.19, seed=1, nthreads=0, noise=0.0):
+    def rmat(scale, edges, a=0.57, b=0.19, c=0.19, seed=1, nthreads=0, noise=0.0, keep_isolated=False):
         h = _vp()
-        _check(load().gala_generate_rmat(scale, edges, a, b, c, noise, seed, nthreads, ctypes.byref(h)))
+        _check(load().gala_generate_rmat(scale, edges, a, b, c, noise, int(keep_isolated), seed, nthreads,
+                                         ctypes.byref(h)))
         return Graph(h)
 
     def store_bin(self, path):
         _check(load().gala_graph_store_bin(self.h, path.encode()))
+
+    def pin(self):
+        _check(load().gala_graph_pin(self.h))
 
     def info(self):
         n, e, w = ctypes.c_int32(), ctypes.c_int64(), ctypes.c_int32()
@@ -232,7 +239,12 @@ class Context:
     def __del__(self):
         self.close()
 
-    def louvain(self, graph, min_mod=1e-6, max_levels=0, verbose=False, iter_capacity=4096):
+    def set_stream(self, stream_handle):
+        """Order the context's work on a caller CUDA stream (an int handle,
+        e.g. torch.cuda.Stream().cuda_stream); None = own stream."""
+        _check(load().gala_context_set_stream(self.h, stream_handle))
+
+    def louvain(self, graph, min_mod=1e-6, max_levels=0, verbose=False, iter_capacity=4096, fp64_gains=False):
         """gala_louvain: host graph in, host labels out."""
         n, _, _ = graph.info()
         labels = np.zeros(n, dtype=np.int32)
@@ -240,7 +252,8 @@ class Context:
         r = Result()
         r.iter_modularity = _ptr(trace, _f64p)
         r.iter_capacity = iter_capacity
-        o = default_options(min_modularity=min_mod, max_levels=max_levels, verbose=int(verbose))
+        o = default_options(min_modularity=min_mod, max_levels=max_levels, verbose=int(verbose),
+                            fp64_gains=int(fp64_gains))
         _check(load().gala_louvain(self.h, graph.h, ctypes.byref(o), _ptr(labels, _i32p), ctypes.byref(r)))
         d = r.to_dict(trace)
         d["labels"] = labels

@@ -55,7 +55,10 @@ typedef struct {
     int32_t verbose;       /* 1 = print the reference's stdout lines
                               (README.md:59-89, louvain_main_process.cu:1003) */
     int32_t use_graphs;    /* 1 = replay each phase-1 iteration as a CUDA graph */
-    int32_t reserved;
+    int32_t fp64_gains;    /* 1 = evaluate every gain with the reference's FP64
+                              expressions (default 0: exact integer gains,
+                              FP64 only where rounding could decide; both give
+                              the same partition) */
 } gala_options;
 
 typedef struct {
@@ -128,16 +131,27 @@ gala_status gala_generate_sbm(int32_t n, int32_t k, double p_in, double p_out,
  * self-loops removed, ids without edges dropped and renumbered in order.
  * noise > 0 perturbs a, b, c, d independently by a factor in
  * [1 - noise, 1 + noise] at every recursion level of every edge (then
- * renormalises), which smooths the degree staircase of plain R-MAT.  The
- * graph depends only on the arguments, not on nthreads. */
+ * renormalises), which smooths the degree staircase of plain R-MAT.
+ * keep_isolated = 1 keeps all 2^scale ids (ids without edges become vertices
+ * of degree 0) instead of dropping them.  The graph depends only on the
+ * arguments, not on nthreads. */
 gala_status gala_generate_rmat(int32_t scale, int64_t edges, double a, double b,
-                               double c, double noise, uint64_t seed, int32_t nthreads,
-                               gala_graph **out);
+                               double c, double noise, int32_t keep_isolated, uint64_t seed,
+                               int32_t nthreads, gala_graph **out);
 
 /* ---- device context ---------------------------------------------------- */
 gala_status gala_context_create(int32_t device, int32_t max_vertices, int64_t max_entries,
                                 gala_context **out);
 void gala_context_destroy(gala_context *ctx);
+/* Run the context's work on a caller-owned CUDA stream (a cudaStream_t passed
+ * as void*); NULL goes back to the context's own stream.  The reference runs
+ * everything on the default stream with device-wide syncs
+ * (louvain_main_process.cu:594-857); here all work of a context is ordered
+ * on one stream and only that stream is synchronised. */
+gala_status gala_context_set_stream(gala_context *ctx, void *stream);
+/* Page-lock the host arrays of g so host<->device copies run at full
+ * bandwidth; gala_graph_destroy unpins them.  Needs a CUDA device. */
+gala_status gala_graph_pin(gala_graph *g);
 
 /* ---- Louvain ------------------------------------------------------------ */
 /* Replaces louvain_gpu(Graph&, vertex_t*, double, int, int)

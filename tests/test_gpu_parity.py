@@ -125,6 +125,32 @@ def test_rmat_power_law(ffi, oracle, torch_cuda):
     assert abs(g.modularity(r["labels"]) - r["modularity"]) < 1e-9
 
 
+@pytest.mark.parametrize("case", ["karate", "sbm", "rmat", "weighted", "small_weights"])
+def test_integer_gains_equal_fp64_gains(ffi, golden, torch_cuda, case):
+    """The default exact-integer gain path and the all-FP64 path (the
+    reference's expressions for every candidate) give the same partition."""
+    rng = np.random.default_rng(17)
+    if case == "karate":
+        g = ffi.Graph.load_bin(os.path.join(golden, "karate.txt.bin"))
+    elif case == "sbm":
+        g = ffi.Graph.load_bin(os.path.join(golden, "sbm_s1.txt.bin"))
+    elif case == "rmat":
+        g = ffi.Graph.rmat(15, 250000, seed=11)
+    elif case == "weighted":
+        g = ffi.Graph.from_csr(*_sym_graph(rng, 20000, 150000, True, hubs=[(7, 9000), (8, 3000)]))
+    else:  # many equal gains: all weights 1 or 2 on a ring of cliques
+        offs, nbr, w = _sym_graph(rng, 3000, 9000, True)
+        w = (w % 2 + 1).astype(np.int32)
+        g = ffi.Graph.from_csr(offs, nbr, w)
+    n, e, _ = g.info()
+    ctx = ffi.Context(n, e)
+    a = ctx.louvain(g)
+    b = ctx.louvain(g, fp64_gains=True)
+    assert a["iter_q"] == b["iter_q"]
+    assert a["level_c"] == b["level_c"]
+    assert np.array_equal(a["labels"], b["labels"])
+
+
 def test_deterministic_replay(ffi, torch_cuda):
     g = ffi.Graph.rmat(14, 150000, seed=9)
     n, e, _ = g.info()
@@ -193,6 +219,34 @@ def test_contract_arbitrary_partitions(ffi, oracle, torch_cuda):
         assert np.array_equal(d_no.cpu().numpy()[:C + 1], c["offs"])
         assert np.array_equal(d_nn.cpu().numpy()[:newE], c["nbr"])
         assert np.array_equal(d_nw.cpu().numpy()[:newE], c["w"])
+
+
+@pytest.mark.parametrize("members", [600, 5000])
+def test_contract_large_rows_hash_and_bitmap(ffi, oracle, torch_cuda, members):
+    """Rows of more than 4096 entries in hash mode (the table is smaller than
+    the community count): 600 members -> ~12k entries, sorted in shared
+    memory; 5000 members -> ~45k distinct neighbours, ranked by the bitmap."""
+    torch = torch_cuda
+    rng = np.random.default_rng(members)
+    n = 200000
+    offs, nbr, w = _sym_graph(rng, n, 1000000, True)
+    E = int(offs[-1])
+    lab = np.arange(n, dtype=np.int32)
+    for k in range(4):
+        idx = rng.choice(n, members, replace=False)
+        lab[idx] = idx[0]
+    ctx = ffi.Context(n, E)
+    d_offs, d_nbr, d_w, d_comm = _dev(torch, offs), _dev(torch, nbr), _dev(torch, w), _dev(torch, lab)
+    d_no = torch.zeros(n + 1, dtype=torch.int64, device="cuda")
+    d_nn = torch.zeros(E, dtype=torch.int32, device="cuda")
+    d_nw = torch.zeros(E, dtype=torch.int32, device="cuda")
+    C, newE = ctx.contract_device(n, d_offs.data_ptr(), d_nbr.data_ptr(), d_w.data_ptr(), d_comm.data_ptr(),
+                                  d_no.data_ptr(), d_nn.data_ptr(), d_nw.data_ptr())
+    c = oracle.contract(offs, nbr, w, lab)
+    assert C == c["C"]
+    assert np.array_equal(d_no.cpu().numpy()[:C + 1], c["offs"])
+    assert np.array_equal(d_nn.cpu().numpy()[:newE], c["nbr"])
+    assert np.array_equal(d_nw.cpu().numpy()[:newE], c["w"])
 
 
 def test_louvain_device_equals_host_entry(ffi, torch_cuda):
