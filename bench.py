@@ -47,6 +47,11 @@ def parse():
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
     p.add_argument("--small", action="store_true", help="tiny workload for a quick check")
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--profile", action="store_true",
+                   help="one device-resident run and a short summary (for ncu captures)")
+    p.add_argument("--fp64-gains", action="store_true", help="evaluate every gain in FP64")
+    p.add_argument("--scale", type=int, default=0,
+                   help="R-MAT scale of a smaller case of the same workload (raw samples scaled by 2^(scale-22))")
     return p.parse_args()
 
 
@@ -168,6 +173,9 @@ def reference_arm(args, wl):
 def main():
     args = parse()
     wl = SMALL if args.small else WORKLOAD
+    if args.scale:
+        wl = dict(WORKLOAD, workload=f"rmat-s{args.scale}", scale=args.scale,
+                  raw_edges=WORKLOAD["raw_edges"] >> (22 - args.scale))
     if args.impl == "reference":
         reference_arm(args, wl)
         return
@@ -198,7 +206,19 @@ def main():
     torch.cuda.synchronize()
 
     def run_device():
-        return ctx.louvain_device(n, d_offs.data_ptr(), d_nbr.data_ptr(), None, d_out.data_ptr())
+        return ctx.louvain_device(n, d_offs.data_ptr(), d_nbr.data_ptr(), None, d_out.data_ptr(),
+                                  fp64_gains=args.fp64_gains)
+
+    if args.profile:
+        r = run_device()
+        torch.cuda.synchronize()
+        print(json.dumps({"profile": wl["workload"], "ms": r["time_total_ms"], "rounds": r["rounds"],
+                          "iterations": r["total_iterations"], "modularity": r["modularity"],
+                          "decide_ms": r["time_decide_ms"], "update_ms": r["time_update_ms"],
+                          "contract_ms": r["time_contract_ms"], "decide_bytes": r["decide_bytes"],
+                          "sweeps": r["decide_sweeps"]}), flush=True)
+        ctx.close()
+        return
 
     for _ in range(args.warmup):
         r = run_device()

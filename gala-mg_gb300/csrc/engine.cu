@@ -35,6 +35,12 @@ struct gala_context {
     int32_t *scratch = nullptr;
     long long scratch_ints = 0;
     cudaEvent_t ev[8] = {};
+    // the degree bins of one sweep are independent: they run concurrently on
+    // auxiliary streams, forked from and joined back into `stream`
+    static constexpr int kAux = 4;
+    cudaStream_t aux[kAux] = {};
+    cudaEvent_t fork_ev = nullptr;
+    cudaEvent_t join_ev[kAux] = {};
     std::vector<void *> allocs;
 };
 
@@ -89,6 +95,23 @@ float ev_ms(cudaEvent_t a, cudaEvent_t b)
     cudaEventElapsedTime(&ms, a, b);
     return ms;
 }
+
+// Fork the auxiliary streams off the context stream and join them back.
+void fork(gala_context *ctx)
+{
+    cudaEventRecord(ctx->fork_ev, ctx->stream);
+    for (int i = 0; i < gala_context::kAux; ++i) cudaStreamWaitEvent(ctx->aux[i], ctx->fork_ev, 0);
+}
+void join(gala_context *ctx)
+{
+    for (int i = 0; i < gala_context::kAux; ++i) {
+        cudaEventRecord(ctx->join_ev[i], ctx->aux[i]);
+        cudaStreamWaitEvent(ctx->stream, ctx->join_ev[i], 0);
+    }
+}
+// Heaviest bins first, spread over the auxiliary streams.
+constexpr int kBinLaunchOrder[kNumBins] = {7, 6, 5, 4, 3, 2, 1, 0};
+cudaStream_t aux_for(gala_context *ctx, int k) { return ctx->aux[k % gala_context::kAux]; }
 
 struct Phase1Out {
     double q = 0;
@@ -183,15 +206,24 @@ gala_status phase1(gala_context *ctx, const LevelGraph &g, long long &m2, double
         p1_iter_reset(b, nxt, min_tot_init, st);
         cudaEventRecord(ctx->ev[2], st);
         const int32_t *lists = iteration == 1 ? b.order : b.act[cur];
-        for (int bin = 0; bin < kNumBins; ++bin)
+        fork(ctx);
+        for (int k = 0; k < kNumBins; ++k) {
+            const int bin = kBinLaunchOrder[k];
             p1_decide(g, b, bin, lists + bin_start[bin], &b.stats->act_count[cur][bin], level_cnt[bin], constant,
-                      m2, fp64_only, hub_tmax, st);
+                      m2, fp64_only, hub_tmax, aux_for(ctx, k));
+        }
+        join(ctx);
         cudaEventRecord(ctx->ev[3], st);
         p1_apply_movers(b, +1, g.n, st);
         p1_tot_reduce(b, g.n, st);
         cudaEventRecord(ctx->ev[4], st);
-        for (int bin = 0; bin < kNumBins; ++bin)
-            p1_update(g, b, bin, b.order + bin_start[bin], level_cnt[bin], nxt, bin_start[bin], constant, m2, st);
+        fork(ctx);
+        for (int k = 0; k < kNumBins; ++k) {
+            const int bin = kBinLaunchOrder[k];
+            p1_update(g, b, bin, b.order + bin_start[bin], level_cnt[bin], nxt, bin_start[bin], constant, m2,
+                      aux_for(ctx, k));
+        }
+        join(ctx);
         cudaEventRecord(ctx->ev[5], st);
         if ((s = check(cudaMemcpyAsync(h, b.stats, sizeof(DevStats), cudaMemcpyDeviceToHost, st), "iteration")) ||
             (s = check(cudaStreamSynchronize(st), "iteration")))
@@ -376,6 +408,11 @@ void gala_context_destroy(gala_context *ctx)
     if (ctx->h_stats) cudaFreeHost(ctx->h_stats);
     for (auto &e : ctx->ev)
         if (e) cudaEventDestroy(e);
+    for (int i = 0; i < gala_context::kAux; ++i) {
+        if (ctx->aux[i]) cudaStreamDestroy(ctx->aux[i]);
+        if (ctx->join_ev[i]) cudaEventDestroy(ctx->join_ev[i]);
+    }
+    if (ctx->fork_ev) cudaEventDestroy(ctx->fork_ev);
     if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
     cudaSetDevice(prev);
     delete ctx;
@@ -412,6 +449,11 @@ gala_status gala_context_create(int32_t device, int32_t max_vertices, int64_t ma
     bool ok = cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamNonBlocking) == cudaSuccess;
     ctx->stream = ctx->own_stream;
     for (auto &e : ctx->ev) ok = ok && cudaEventCreate(&e) == cudaSuccess;
+    ok = ok && cudaEventCreateWithFlags(&ctx->fork_ev, cudaEventDisableTiming) == cudaSuccess;
+    for (int i = 0; i < gala_context::kAux; ++i) {
+        ok = ok && cudaStreamCreateWithFlags(&ctx->aux[i], cudaStreamNonBlocking) == cudaSuccess;
+        ok = ok && cudaEventCreateWithFlags(&ctx->join_ev[i], cudaEventDisableTiming) == cudaSuccess;
+    }
     ok = ok && cudaMallocHost(&ctx->h_stats, sizeof(DevStats)) == cudaSuccess;
     for (int i = 0; i < 2 && ok; ++i)
         ok = dalloc(ctx, &ctx->offs[i], n + 1) && dalloc(ctx, &ctx->nbr[i], E) && dalloc(ctx, &ctx->w[i], E);

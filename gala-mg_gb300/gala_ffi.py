@@ -259,13 +259,14 @@ class Context:
         d["labels"] = labels
         return d
 
-    def louvain_device(self, n, d_offs, d_nbr, d_w, d_out, min_mod=1e-6, max_levels=0, iter_capacity=4096):
+    def louvain_device(self, n, d_offs, d_nbr, d_w, d_out, min_mod=1e-6, max_levels=0, iter_capacity=4096,
+                       fp64_gains=False):
         """gala_louvain_device on raw device pointers (ints)."""
         trace = np.zeros(iter_capacity, dtype=np.float64)
         r = Result()
         r.iter_modularity = _ptr(trace, _f64p)
         r.iter_capacity = iter_capacity
-        o = default_options(min_modularity=min_mod, max_levels=max_levels)
+        o = default_options(min_modularity=min_mod, max_levels=max_levels, fp64_gains=int(fp64_gains))
         _check(load().gala_louvain_device(self.h, n, d_offs, d_nbr, d_w or None, ctypes.byref(o), d_out,
                                           ctypes.byref(r)))
         return r.to_dict(trace)
