@@ -216,7 +216,7 @@ def main():
                           "iterations": r["total_iterations"], "modularity": r["modularity"],
                           "decide_ms": r["time_decide_ms"], "update_ms": r["time_update_ms"],
                           "contract_ms": r["time_contract_ms"], "decide_bytes": r["decide_bytes"],
-                          "sweeps": r["decide_sweeps"]}), flush=True)
+                          "sweeps": r["decide_sweeps"], "fp64_decisions": r["fp64_decisions"]}), flush=True)
         ctx.close()
         return
 
@@ -294,7 +294,7 @@ def main():
             "vs_baseline": None, "dtype": "int32/f64", "data": "synthetic", "config": cfg,
             "seconds_per_run": ms / 1000.0, "modularity": last["modularity"],
             "communities": last["num_communities"], "rounds": last["rounds"],
-            "iterations": last["total_iterations"],
+            "iterations": last["total_iterations"], "fp64_decisions": last["fp64_decisions"],
             "phase_ms": {"phase1": last["time_phase1_ms"], "decide": last["time_decide_ms"],
                          "update": last["time_update_ms"], "contract": last["time_contract_ms"]},
             "e2e": {"value": world * m / (e2e_step / 1000.0), "unit": "edges/s", "ms_per_step": e2e_step,

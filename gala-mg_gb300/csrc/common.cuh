@@ -50,17 +50,20 @@ struct DevStats {
     int err;                        // error bits (kErr*)
     int max_deg;
     int num_communities;            // contraction: C
-    int pad0;
+    int nz_rows;                    // contraction: rows with entries (walk list)
     int bin_start[kNumBinSlots + 1];  // order list: start of each bin
     int act_count[2][kNumBins];       // active list counts (ping-pong)
     int small_cnt[4];                 // contraction: communities per size class
     long long total2;                 // scratch total of a second scan
+    long long total3;                 // scratch total of a third scan
     long long total;                  // scratch total of the last scan
+    unsigned long long fp64_decisions; // vertices decided with the FP64 expressions
 };
 
 constexpr int kErrHashOverflow = 1;
 constexpr int kErrProbeLimit = 2;
 constexpr int kErrBadLabel = 4;
+constexpr int kErrBadIndex = 8;
 
 // ---------------------------------------------------------------------------
 // FP64 gain of a candidate community, same operation order as the reference

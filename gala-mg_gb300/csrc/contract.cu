@@ -13,14 +13,23 @@
 //        <= 4096 entries    one 256-thread CTA, shared-memory hash table
 //        larger             a global table per community filled by many CTAs
 //                           (4096-entry chunks of the stream); a dense table
-//                           indexed by community id when the row can hold a
-//                           large share of all communities
+//                           indexed by community id when a hash table would not
+//                           be smaller
 //      and emit the distinct neighbours in ascending id order (rank by
-//      shuffle compare, bitonic sort in shared memory, a scan of the dense
-//      table, or a bitmap over all communities for very long rows)
+//      shuffle compare, bitonic sort in shared memory, or - rows with more
+//      than 16384 distinct neighbours - a bitmap over all communities ranked
+//      by a prefix sum of popcounts, all spread over many CTAs)
 //   5. CSR offsets by scan and a compaction copy.
 // Rows come out sorted by neighbour id, so the contracted graph of a given
 // partition is unique and can be compared bit for bit.
+//
+// The stream fill and the compaction walk contiguous entry ranges: every
+// warp takes 1024 consecutive CSR entries and finds the row of each entry
+// with a 5-step shuffle search over a window of 32 row ends, so the work is
+// balanced whatever the row lengths (hub rows, empty rows of isolated
+// vertices).
+#include <limits.h>
+
 #include "common.cuh"
 #include "internal.h"
 #include "scan.cuh"
@@ -43,7 +52,8 @@ constexpr int kSmallMax = 32;
 constexpr int kMid1Max = 512;
 constexpr int kMid2Max = 4096;
 constexpr int kChunk = 4096;
-constexpr int kEmitList = 16384;
+constexpr int kSortMax = 16384;
+constexpr int kRangeEntries = 1024;  // CSR entries per warp task
 
 struct OpDegOf {
     const int64_t *offs;
@@ -52,6 +62,121 @@ struct OpDegOf {
         return (long long)(offs[v + 1] - offs[v]);
     }
 };
+struct OpPopc {
+    __device__ __forceinline__ long long operator()(unsigned x, long long) const { return __popc(x); }
+};
+struct OpRowNonEmpty {  // in = offs: row idx has entries
+    const int64_t *offs;
+    __device__ __forceinline__ long long operator()(int64_t x, long long idx) const
+    {
+        return offs[idx + 1] > x ? 1 : 0;
+    }
+};
+
+// Walk list of the rows that have entries: nz_rows[i] (row id) and
+// nz_offs[i] (its first entry), nz_offs[count] = E, count in st->nz_rows.
+// Row walks over it never step through runs of empty rows.
+__global__ void k_nz_tail(DevStats *st, long long *nz_offs, long long E)
+{
+    const int cnt = (int)st->total;
+    st->nz_rows = cnt;
+    nz_offs[cnt] = E;
+}
+
+__global__ void k_nz_scatter(const int64_t *__restrict__ offs, int n, const int32_t *__restrict__ pos,
+                             int32_t *nz_rows, long long *nz_offs)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const long long s = offs[i];
+        if (offs[i + 1] > s) {
+            const int p = pos[i];
+            nz_rows[p] = i;
+            nz_offs[p] = s;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Row window: the 32 row ends offs[vbase+1 .. vbase+32] held one per lane.
+// ---------------------------------------------------------------------------
+struct RowWindow {
+    const int64_t *offs;
+    const long long *offs_ll;
+    int n;
+    int vbase;
+    long long rowend;
+    __device__ __forceinline__ long long at(int k) const
+    {
+        return offs ? (long long)offs[k] : offs_ll[k];
+    }
+    __device__ __forceinline__ void load()
+    {
+        const int k = vbase + 1 + (int)(threadIdx.x & 31);
+        rowend = k <= n ? at(k) : LLONG_MAX;
+    }
+    // number of window rows that end at or before entry j (0..32)
+    __device__ __forceinline__ int count_le(long long j) const
+    {
+        int cnt = 0;
+#pragma unroll
+        for (int s = 16; s >= 1; s >>= 1) {
+            const long long r = __shfl_sync(GALA_FULL_MASK, rowend, cnt + s - 1);
+            if (r <= j) cnt += s;
+        }
+        // every lane takes part in the shuffle (a full-mask shuffle behind a
+        // lane-dependent condition is undefined)
+        const long long last = __shfl_sync(GALA_FULL_MASK, rowend, 31);
+        if (cnt == 31 && last <= j) cnt = 32;
+        return cnt;
+    }
+};
+
+// Owner row of entry j0: the last v with offs[v] <= j0 and offs[v+1] > j0.
+__device__ __forceinline__ int owner_row(const int64_t *offs, const long long *offs_ll, int n, long long j0)
+{
+    int lo = 0, hi = n - 1;  // rows [0, n); offs[n] = E > j0
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        const long long o = offs ? (long long)offs[mid] : offs_ll[mid];
+        if (o <= j0)
+            lo = mid;
+        else
+            hi = mid - 1;
+    }
+    return lo;
+}
+
+// Walk entries [j0, j1) of a CSR (rows [0, n), offsets offs or offs_ll) and
+// call f(j, row) for every entry; all 32 lanes of the warp must call.
+template <typename F>
+__device__ __forceinline__ void for_entries(const int64_t *offs, const long long *offs_ll, int n, long long j0,
+                                            long long j1, F f)
+{
+    const int lane = threadIdx.x & 31;
+    RowWindow w{offs, offs_ll, n, 0, 0};
+    w.vbase = owner_row(offs, offs_ll, n, j0);
+    w.load();
+    for (long long jb = j0; jb < j1; jb += 32) {
+        // slide the window to the owner of the round's first entry
+        const int adv = w.count_le(jb);
+        if (adv > 0) {
+            w.vbase += adv;
+            w.load();
+        }
+        const long long j = jb + lane;
+        bool done = j >= j1;
+        while (!__all_sync(GALA_FULL_MASK, done)) {
+            const int idx = w.count_le(j);
+            const bool here = !done && idx < 32;
+            if (here) f(j, w.vbase + idx);
+            done = done || here;
+            if (!__all_sync(GALA_FULL_MASK, done)) {
+                w.vbase += 32;
+                w.load();
+            }
+        }
+    }
+}
 
 // Caller-supplied labels must lie in [0, n) before they index any array.
 __global__ void k_check_labels(const int32_t *__restrict__ comm, int n, DevStats *st)
@@ -97,44 +222,57 @@ __global__ void k_member_scatter(const int32_t *__restrict__ lab, const int64_t 
     }
 }
 
-// Community-ordered edge stream: one warp per vertex (rows read in vertex
-// order, written to the vertex's slot in its community's segment).
+// Community-ordered edge stream over contiguous entry ranges: entry j of row
+// v goes to medge[mpos[v]] + (j - offs[v]).  Rows are walked through the
+// list of rows with entries (nz_rows / nz_offs).
 template <bool W>
-__global__ void __launch_bounds__(256) k_stream_fill(int n, const int64_t *__restrict__ offs,
+__global__ void __launch_bounds__(256) k_stream_fill(int n, long long E, const int64_t *__restrict__ offs,
                                                      const int32_t *__restrict__ nbr,
                                                      const int32_t *__restrict__ w,
                                                      const int32_t *__restrict__ lab,
                                                      const int32_t *__restrict__ mpos,
                                                      const long long *__restrict__ medge, int32_t *skey,
-                                                     int32_t *sw)
+                                                     int32_t *sw, const int32_t *__restrict__ nz_rows,
+                                                     const long long *__restrict__ nz_offs, DevStats *st)
 {
-    const int lane = threadIdx.x & 31;
-    const int wg = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int nw = (gridDim.x * blockDim.x) >> 5;
-    for (int v = wg; v < n; v += nw) {
-        const long long s = offs[v], e = offs[v + 1];
-        if (s == e) continue;
-        const long long base = medge[mpos[v]] - s;
-        for (long long j = s + lane; j < e; j += 32) {
-            skey[base + j] = lab[nbr[j]];
-            sw[base + j] = W ? w[j] : 1;
-        }
+    const long long wg = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
+    const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
+    const int nnz = st->nz_rows;
+    for (long long t = wg; t * kRangeEntries < E; t += nw) {
+        const long long j0 = t * kRangeEntries;
+        const long long j1 = j0 + kRangeEntries < E ? j0 + kRangeEntries : E;
+        for_entries(nullptr, nz_offs, nnz, j0, j1, [&](long long j, int r) {
+            const int v = (r >= 0 && r < nnz) ? nz_rows[r] : -1;
+            if (v < 0 || v >= n) {  // recorded, never written
+                atomicOr(&st->err, kErrBadIndex);
+                return;
+            }
+            const long long dst = medge[mpos[v]] + (j - offs[v]);
+            if (dst < 0 || dst >= E) {
+                atomicOr(&st->err, kErrBadIndex);
+                return;
+            }
+            skey[dst] = lab[nbr[j]];
+            sw[dst] = W ? w[j] : 1;
+        });
     }
 }
 
 __device__ __forceinline__ int row_class(long long E)
 {
-    return E <= kSmallMax ? 0 : (E <= kMid1Max ? 1 : (E <= kMid2Max ? 2 : 3));
+    return E == 0 ? -1 : (E <= kSmallMax ? 0 : (E <= kMid1Max ? 1 : (E <= kMid2Max ? 2 : 3)));
 }
 
-// Size classes with warp-aggregated appends (one atomic per warp and class).
+// Size classes with warp-aggregated appends (one atomic per warp and class);
+// communities without entries get an empty row right away.
 __global__ void __launch_bounds__(256) k_classify(int C, const long long *__restrict__ ec, int32_t *lists,
-                                                  DevStats *st)
+                                                  int32_t *kc, DevStats *st)
 {
     const int stride = gridDim.x * blockDim.x;
     for (int base = blockIdx.x * blockDim.x; base < C; base += stride) {
         const int c = base + threadIdx.x;
-        const int cls = c < C ? row_class(ec[c]) : -1;
+        const int cls = c < C ? row_class(ec[c]) : -2;
+        if (cls == -1) kc[c] = 0;
 #pragma unroll
         for (int k = 0; k < 4; ++k) warp_append(cls == k, c, lists + (long long)k * C, &st->small_cnt[k]);
     }
@@ -213,15 +351,17 @@ __device__ __forceinline__ void bitonic_sort_smem(int *k, int *v, int P)
     }
 }
 
-// Insert stream entries [st + lo, st + hi) into a hash table (or a dense
-// table when keys == nullptr).  Called by all threads of the block.
-__device__ __forceinline__ void agg_insert(const AggArgs &a, long long st, int lo, int hi, int *keys, int *vals,
-                                           int T, int lg)
+// Insert stream entries [st, st + len) into a table (dense when keys is
+// null).  Returns this thread's count of newly created keys.  All threads of
+// the block call it.
+__device__ __forceinline__ int agg_insert(const AggArgs &a, long long st, int len, int *keys, int *vals, int T,
+                                          int lg)
 {
     const int lane = threadIdx.x & 31;
-    for (int b0 = lo; b0 < hi; b0 += blockDim.x) {
+    int created = 0;
+    for (int b0 = 0; b0 < len; b0 += blockDim.x) {
         const int j = b0 + threadIdx.x;
-        const bool valid = j < hi;
+        const bool valid = j < len;
         int key = -1, wt = 0;
         if (valid) {
             key = a.skey[st + j];
@@ -230,12 +370,32 @@ __device__ __forceinline__ void agg_insert(const AggArgs &a, long long st, int l
         const unsigned m = __match_any_sync(GALA_FULL_MASK, key);
         const int sum = (int)__reduce_add_sync(m, (unsigned)wt);
         if (valid && __ffs(m) - 1 == lane) {
-            if (!keys)
-                atomicAdd(&vals[key], sum);
-            else if (!hash_add(keys, vals, T, lg, key, sum))
-                atomicOr(&a.st->err, kErrHashOverflow);
+            if (!keys) {
+                created += atomicAdd(&vals[key], sum) == 0;
+            } else {
+                unsigned h = hash_slot(key, lg);
+                bool ok = false;
+                for (int p = 0; p < T; ++p) {
+                    int k = *(volatile int *)&keys[h];
+                    if (k == -1) {
+                        k = atomicCAS(&keys[h], -1, key);
+                        if (k == -1) {
+                            k = key;
+                            created++;
+                        }
+                    }
+                    if (k == key) {
+                        atomicAdd(&vals[h], sum);
+                        ok = true;
+                        break;
+                    }
+                    h = (h + 1) & (unsigned)(T - 1);
+                }
+                if (!ok) atomicOr(&a.st->err, kErrHashOverflow);
+            }
         }
     }
+    return created;
 }
 
 // Rows of 33..kMid2Max entries: one CTA per community, shared-memory hash
@@ -265,7 +425,7 @@ __global__ void __launch_bounds__(BLOCK) k_agg_mid(AggArgs a, const int32_t *__r
         }
         if (threadIdx.x == 0) s_k = 0;
         __syncthreads();
-        agg_insert(a, st, 0, E, keys, vals, T, lg);
+        agg_insert(a, st, E, keys, vals, T, lg);
         __syncthreads();
         for (int j = threadIdx.x; j < T; j += BLOCK) {
             int kk = keys[j];
@@ -300,15 +460,24 @@ struct BigArgs {
     const int32_t *__restrict__ list;  // class-3 communities
     long long *T;
     long long *chunks;
+    long long *tchunks;
     const long long *__restrict__ toff;
     const long long *__restrict__ coff;
+    const long long *__restrict__ tcoff;
     int32_t *mode;
     int32_t *work;
+    int32_t *twork;
+    int32_t *kdist;
+    int32_t *cursor;
+    long long *gwords;
+    const long long *__restrict__ gofs;
     int32_t *pool;
     long long pool_half;  // keys at pool[0, half), values at pool[half, 2 half)
+    unsigned *bits;       // bitmaps of the rows ranked by bitmap
+    unsigned *pref;       // exclusive prefix of their popcounts
 };
 
-// Table size and chunk count of every class-3 community.  A dense table
+// Table size and chunk counts of every class-3 community.  A dense table
 // (slot = community id) is used when a hash table would not be smaller.
 __global__ void k_big_plan(AggArgs a, BigArgs b)
 {
@@ -322,18 +491,23 @@ __global__ void k_big_plan(AggArgs a, BigArgs b)
         b.T[i] = T;
         b.mode[i] = dense;
         b.chunks[i] = (E + kChunk - 1) / kChunk;
+        b.tchunks[i] = (T + kChunk - 1) / kChunk;
+        b.kdist[i] = 0;
+        b.cursor[i] = 0;
     }
 }
 
 __global__ void k_big_tail(BigArgs b, const DevStats *st)
 {
-    // toff[cnt] / coff[cnt] close the last segments (totals of the scans)
+    // toff[cnt] / coff[cnt] / tcoff[cnt] close the last segments
     const int cnt = st->small_cnt[3];
     ((long long *)b.toff)[cnt] = st->total;
     ((long long *)b.coff)[cnt] = st->total2;
+    ((long long *)b.tcoff)[cnt] = st->total3;
 }
 
-// chunk -> community (list index), one warp per community
+// stream chunk -> community and table chunk -> community, one warp per
+// community (list index)
 __global__ void k_big_work(AggArgs a, BigArgs b)
 {
     const int lane = threadIdx.x & 31;
@@ -341,15 +515,19 @@ __global__ void k_big_work(AggArgs a, BigArgs b)
     const int nw = (gridDim.x * blockDim.x) >> 5;
     const int cnt = a.st->small_cnt[3];
     for (int i = wg; i < cnt; i += nw) {
-        const long long o = b.coff[i], k = b.coff[i + 1] - o;
+        long long o = b.coff[i], k = b.coff[i + 1] - o;
         for (long long j = lane; j < k; j += 32) b.work[o + j] = i;
+        o = b.tcoff[i];
+        k = b.tcoff[i + 1] - o;
+        for (long long j = lane; j < k; j += 32) b.twork[o + j] = i;
     }
 }
 
 // Every CTA inserts one chunk of kChunk stream entries into its community's
-// global table (hash or dense); many CTAs share one community.
+// global table; many CTAs share one community.  New keys are counted.
 __global__ void __launch_bounds__(256) k_big_insert(AggArgs a, BigArgs b, long long nwork)
 {
+    __shared__ int red[8];
     for (long long wi = blockIdx.x; wi < nwork; wi += gridDim.x) {
         const int i = b.work[wi];
         const long long j = wi - b.coff[i];
@@ -360,128 +538,162 @@ __global__ void __launch_bounds__(256) k_big_insert(AggArgs a, BigArgs b, long l
         const long long T = b.T[i];
         int *vals = b.pool + b.pool_half + b.toff[i];
         int *keys = b.mode[i] ? nullptr : b.pool + b.toff[i];
-        agg_insert(a, st, 0, len, keys, vals, (int)T, __ffs((int)T) - 1);
-    }
-}
-
-// One CTA per class-3 community: rank the distinct keys and write the row.
-__global__ void __launch_bounds__(1024) k_big_emit(AggArgs a, BigArgs b, unsigned *gbits, long long bit_words)
-{
-    extern __shared__ int sm[];
-    int *lk = sm;
-    int *lv = sm + kEmitList;
-    __shared__ int s_k;
-    __shared__ long long wt_s[32];
-    __shared__ long long tot_s;
-    unsigned *bits = gbits + (long long)blockIdx.x * 2 * bit_words;
-    unsigned *pref = bits + bit_words;
-    const int cnt = a.st->small_cnt[3];
-    const int nwords = (a.C + 31) >> 5;
-    for (int i = blockIdx.x; i < cnt; i += gridDim.x) {
-        const int c = b.list[i];
-        const long long T = b.T[i];
-        const int *vals = b.pool + b.pool_half + b.toff[i];
-        const int *keys = b.pool + b.toff[i];
-        const long long o = a.tmp_off[c];
-        int k = 0;
-        if (b.mode[i]) {
-            // dense: slot = neighbour community, ascending by construction
-            long long carry = 0;
-            for (long long b0 = 0; b0 < T; b0 += blockDim.x) {
-                const long long x = b0 + threadIdx.x;
-                const int wv = x < T ? vals[x] : 0;
-                const long long f = wv > 0 ? 1 : 0;
-                const long long ex = block_exclusive_scan<long long>(f, wt_s, &tot_s);
-                if (f) {
-                    a.tmp_nbr[o + carry + ex] = (int)x;
-                    a.tmp_w[o + carry + ex] = wv;
-                }
-                carry += tot_s;
-                __syncthreads();
-            }
-            k = (int)carry;
-        } else {
-            if (threadIdx.x == 0) s_k = 0;
-            __syncthreads();
-            int mine = 0;
-            for (long long j = threadIdx.x; j < T; j += blockDim.x) mine += keys[j] >= 0;
-            mine = warp_sum(mine);
-            if ((threadIdx.x & 31) == 0 && mine) atomicAdd(&s_k, mine);
-            __syncthreads();
-            k = s_k;
-            __syncthreads();
-            if (k <= kEmitList) {
-                if (threadIdx.x == 0) s_k = 0;
-                __syncthreads();
-                for (long long j = threadIdx.x; j < T; j += blockDim.x) {
-                    const int kk = keys[j];
-                    if (kk >= 0) {
-                        const int p = atomicAdd(&s_k, 1);
-                        lk[p] = kk;
-                        lv[p] = vals[j];
-                    }
-                }
-                __syncthreads();
-                const int P = next_pow2_int(k);
-                for (int j = k + threadIdx.x; j < P; j += blockDim.x) {
-                    lk[j] = 0x7fffffff;
-                    lv[j] = 0;
-                }
-                __syncthreads();
-                bitonic_sort_smem(lk, lv, P);
-                for (int j = threadIdx.x; j < k; j += blockDim.x) {
-                    a.tmp_nbr[o + j] = lk[j];
-                    a.tmp_w[o + j] = lv[j];
-                }
-            } else {
-                for (int j = threadIdx.x; j < nwords; j += blockDim.x) bits[j] = 0u;
-                __syncthreads();
-                for (long long j = threadIdx.x; j < T; j += blockDim.x) {
-                    const int kk = keys[j];
-                    if (kk >= 0) atomicOr(&bits[kk >> 5], 1u << (kk & 31));
-                }
-                __syncthreads();
-                long long carry = 0;
-                for (int b0 = 0; b0 < nwords; b0 += blockDim.x) {
-                    const int j = b0 + threadIdx.x;
-                    const long long pc = j < nwords ? __popc(bits[j]) : 0;
-                    const long long ex = block_exclusive_scan<long long>(pc, wt_s, &tot_s);
-                    if (j < nwords) pref[j] = (unsigned)(ex + carry);
-                    carry += tot_s;
-                    __syncthreads();
-                }
-                for (long long j = threadIdx.x; j < T; j += blockDim.x) {
-                    const int kk = keys[j];
-                    if (kk >= 0) {
-                        const unsigned r = pref[kk >> 5] + __popc(bits[kk >> 5] & ((1u << (kk & 31)) - 1u));
-                        a.tmp_nbr[o + r] = kk;
-                        a.tmp_w[o + r] = vals[j];
-                    }
-                }
-            }
+        int created = agg_insert(a, st, len, keys, vals, (int)T, __ffs((int)T) - 1);
+        created = warp_sum(created);
+        if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = created;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            int s = 0;
+            for (int q = 0; q < (int)(blockDim.x >> 5); ++q) s += red[q];
+            if (s) atomicAdd(&b.kdist[i], s);
         }
-        if (threadIdx.x == 0) a.kc[c] = k;
         __syncthreads();
     }
 }
 
-__global__ void __launch_bounds__(256) k_compact(int C, const int32_t *__restrict__ kc,
-                                                 const int64_t *__restrict__ new_offs,
+// Rows with more distinct neighbours than a shared-memory sort holds are
+// ranked by a bitmap over all communities: words per row (0 for the others);
+// every class-3 row gets its final length here.
+__global__ void k_big_mark(AggArgs a, BigArgs b)
+{
+    const int cnt = a.st->small_cnt[3];
+    const long long words = ((long long)a.C + 31) >> 5;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < cnt; i += gridDim.x * blockDim.x) {
+        const int k = b.kdist[i];
+        b.gwords[i] = k > kSortMax ? words : 0;
+        a.kc[b.list[i]] = k;
+    }
+}
+
+// Table chunks: distinct entries of sorted rows go to the row unsorted
+// (atomic cursor); rows ranked by bitmap set their bits.
+__global__ void __launch_bounds__(256) k_big_collect(AggArgs a, BigArgs b, long long ntwork)
+{
+    for (long long wi = blockIdx.x; wi < ntwork; wi += gridDim.x) {
+        const int i = b.twork[wi];
+        const long long j0 = (wi - b.tcoff[i]) * kChunk;
+        const long long T = b.T[i];
+        const int c = b.list[i];
+        const int *vals = b.pool + b.pool_half + b.toff[i];
+        const int *keys = b.pool + b.toff[i];
+        const bool dense = b.mode[i];
+        const bool bitmap = b.gwords[i] > 0;
+        const long long o = a.tmp_off[c];
+        unsigned *bits = bitmap ? b.bits + b.gofs[i] : nullptr;
+        for (long long s0 = j0; s0 < j0 + kChunk && s0 < T; s0 += blockDim.x) {
+            const long long s = s0 + threadIdx.x;
+            int key = -1, val = 0;
+            if (s < T && s < j0 + kChunk) {
+                val = vals[s];
+                key = dense ? (val > 0 ? (int)s : -1) : keys[s];
+            }
+            const bool occ = key >= 0;
+            if (bitmap) {
+                if (occ) atomicOr(&bits[key >> 5], 1u << (key & 31));
+            } else {
+                const unsigned bal = __ballot_sync(GALA_FULL_MASK, occ);
+                if (bal) {
+                    const int lane = threadIdx.x & 31, leader = __ffs(bal) - 1;
+                    int base = 0;
+                    if (lane == leader) base = atomicAdd(&b.cursor[i], __popc(bal));
+                    base = __shfl_sync(GALA_FULL_MASK, base, leader);
+                    if (occ) {
+                        const long long p = o + base + __popc(bal & lanemask_lt());
+                        a.tmp_nbr[p] = key;
+                        a.tmp_w[p] = val;
+                    }
+                }
+            }
+        }
+    }
+}
+
+// Table chunks of bitmap-ranked rows: rank = popcounts of the row's bitmap
+// before the key.
+__global__ void __launch_bounds__(256) k_big_rank(AggArgs a, BigArgs b, long long ntwork)
+{
+    for (long long wi = blockIdx.x; wi < ntwork; wi += gridDim.x) {
+        const int i = b.twork[wi];
+        if (b.gwords[i] == 0) continue;
+        const long long j0 = (wi - b.tcoff[i]) * kChunk;
+        const long long T = b.T[i];
+        const int c = b.list[i];
+        const int *vals = b.pool + b.pool_half + b.toff[i];
+        const int *keys = b.pool + b.toff[i];
+        const bool dense = b.mode[i];
+        const long long o = a.tmp_off[c];
+        const unsigned *bits = b.bits + b.gofs[i];
+        const unsigned *pref = b.pref + b.gofs[i];
+        const unsigned base = pref[0];
+        for (long long s = j0 + threadIdx.x; s < j0 + kChunk && s < T; s += blockDim.x) {
+            const int val = vals[s];
+            const int key = dense ? (val > 0 ? (int)s : -1) : keys[s];
+            if (key < 0) continue;
+            const unsigned r = pref[key >> 5] - base + __popc(bits[key >> 5] & ((1u << (key & 31)) - 1u));
+            a.tmp_nbr[o + r] = key;
+            a.tmp_w[o + r] = val;
+        }
+    }
+}
+
+// Rows with at most kSortMax distinct neighbours: one CTA sorts the row in
+// shared memory.
+__global__ void __launch_bounds__(1024) k_big_sort(AggArgs a, BigArgs b)
+{
+    extern __shared__ int sm[];
+    int *lk = sm;
+    int *lv = sm + kSortMax;
+    const int cnt = a.st->small_cnt[3];
+    for (int i = blockIdx.x; i < cnt; i += gridDim.x) {
+        if (b.gwords[i] != 0) continue;
+        const int c = b.list[i];
+        const int k = b.kdist[i];
+        const long long o = a.tmp_off[c];
+        const int P = next_pow2_int(k);
+        for (int j = threadIdx.x; j < P; j += blockDim.x) {
+            lk[j] = j < k ? a.tmp_nbr[o + j] : 0x7fffffff;
+            lv[j] = j < k ? a.tmp_w[o + j] : 0;
+        }
+        __syncthreads();
+        bitonic_sort_smem(lk, lv, P);
+        for (int j = threadIdx.x; j < k; j += blockDim.x) {
+            a.tmp_nbr[o + j] = lk[j];
+            a.tmp_w[o + j] = lv[j];
+        }
+        __syncthreads();
+    }
+}
+
+// Compaction over contiguous output ranges: output entry j of community c
+// comes from tmp_off[c] + (j - new_offs[c]).
+__global__ void __launch_bounds__(256) k_compact(int C, long long Enew, const int64_t *__restrict__ new_offs,
                                                  const long long *__restrict__ tmp_off,
                                                  const int32_t *__restrict__ tmp_nbr,
                                                  const int32_t *__restrict__ tmp_w, int32_t *out_nbr,
-                                                 int32_t *out_w)
+                                                 int32_t *out_w, long long tmp_cap,
+                                                 const int32_t *__restrict__ nz_rows,
+                                                 const long long *__restrict__ nz_offs, DevStats *st)
 {
-    const int lane = threadIdx.x & 31;
-    const int wg = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int nw = (gridDim.x * blockDim.x) >> 5;
-    for (int c = wg; c < C; c += nw) {
-        const int k = kc[c];
-        const long long src = tmp_off[c], dst = new_offs[c];
-        for (int j = lane; j < k; j += 32) {
-            out_nbr[dst + j] = tmp_nbr[src + j];
-            out_w[dst + j] = tmp_w[src + j];
-        }
+    const long long wg = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
+    const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
+    const int nnz = st->nz_rows;
+    for (long long t = wg; t * kRangeEntries < Enew; t += nw) {
+        const long long j0 = t * kRangeEntries;
+        const long long j1 = j0 + kRangeEntries < Enew ? j0 + kRangeEntries : Enew;
+        for_entries(nullptr, nz_offs, nnz, j0, j1, [&](long long j, int r) {
+            const int c = (r >= 0 && r < nnz) ? nz_rows[r] : -1;
+            if (c < 0 || c >= C) {  // recorded, never read or written
+                atomicOr(&st->err, kErrBadIndex);
+                return;
+            }
+            const long long src = tmp_off[c] + (j - new_offs[c]);
+            if (src < 0 || src >= tmp_cap) {
+                atomicOr(&st->err, kErrBadIndex);
+                return;
+            }
+            out_nbr[j] = tmp_nbr[src];
+            out_w[j] = tmp_w[src];
+        });
     }
 }
 
@@ -501,12 +713,12 @@ __global__ void k_contract_reset(DevStats *st)
 
 constexpr size_t kMid1Smem = (2 * 1024 + 2 * kMid1Max) * sizeof(int);
 constexpr size_t kMid2Smem = (2 * 8192 + 2 * kMid2Max) * sizeof(int);
-constexpr size_t kEmitSmem = 2 * kEmitList * sizeof(int);
+constexpr size_t kSortSmem = 2 * kSortMax * sizeof(int);
 
 void contract_configure_kernels()
 {
     cudaFuncSetAttribute(k_agg_mid<256, 8192, kMid2Max>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMid2Smem);
-    cudaFuncSetAttribute(k_big_emit, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kEmitSmem);
+    cudaFuncSetAttribute(k_big_sort, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSortSmem);
 }
 
 static int grid_cap(long long items, int per_block, int cap)
@@ -517,6 +729,16 @@ static int grid_cap(long long items, int per_block, int cap)
     return (int)g;
 }
 
+// Walk list of the rows of (offs, n) that have entries (E entries in total).
+static void build_walk_list(const int64_t *offs, int n, long long E, ContractBuffers &b, cudaStream_t st)
+{
+    const int cap = sm_count() * 8;
+    exclusive_scan(offs, b.nz_pos, n, OpRowNonEmpty{offs}, b.scan_partial, &b.stats->total, st);
+    k_nz_tail<<<1, 1, 0, st>>>(b.stats, b.nz_offs, E);
+    k_nz_scatter<<<grid_cap(n, 256, cap), 256, 0, st>>>(offs, n, b.nz_pos, b.nz_rows, b.nz_offs);
+    note_launch(2);
+}
+
 static bool read_stats(DevStats *h, DevStats *d, cudaStream_t st, gala_status *status, const char *what)
 {
     cudaError_t ce;
@@ -525,6 +747,73 @@ static bool read_stats(DevStats *h, DevStats *d, cudaStream_t st, gala_status *s
         *status = cuda_fail(ce, what);
         return false;
     }
+    return true;
+}
+
+// Rows longer than kMid2Max entries (class 3).  Returns false on failure.
+static bool contract_long_rows(const AggArgs &a, ContractBuffers &b, int cnt3, int C, DevStats &hs,
+                               cudaStream_t st, gala_status *status)
+{
+    const int nsm = sm_count();
+    const int cap = nsm * 8;
+    BigArgs ba{};
+    ba.list = b.cls_list + 3LL * C;
+    ba.T = b.big_T;
+    ba.chunks = b.big_chunks;
+    ba.tchunks = b.big_tchunks;
+    ba.toff = b.big_toff;
+    ba.coff = b.big_coff;
+    ba.tcoff = b.big_tcoff;
+    ba.mode = b.big_mode;
+    ba.work = b.big_work;
+    ba.twork = b.big_twork;
+    ba.kdist = b.big_kdist;
+    ba.cursor = b.big_cursor;
+    ba.gwords = b.big_gwords;
+    ba.gofs = b.big_gofs;
+    ba.pool = b.big_pool;
+    k_big_plan<<<grid_cap(cnt3, 256, cap), 256, 0, st>>>(a, ba);
+    exclusive_scan(b.big_T, b.big_toff, cnt3, OpIdentity(), b.scan_partial, &b.stats->total, st);
+    exclusive_scan(b.big_chunks, b.big_coff, cnt3, OpIdentity(), b.scan_partial, &b.stats->total2, st);
+    exclusive_scan(b.big_tchunks, b.big_tcoff, cnt3, OpIdentity(), b.scan_partial, &b.stats->total3, st);
+    k_big_tail<<<1, 1, 0, st>>>(ba, b.stats);
+    note_launch(2);
+    if (!read_stats(&hs, b.stats, st, status, "contraction: long rows")) return false;
+    const long long slots = hs.total, nwork = hs.total2, ntwork = hs.total3;
+    if (2 * slots > b.big_pool_ints || nwork > b.big_work_cap || ntwork > b.big_twork_cap) {
+        set_error("contraction: long rows need %lld table slots / %lld + %lld chunks, pool holds %lld / %lld / %lld",
+                  slots, nwork, ntwork, b.big_pool_ints / 2, b.big_work_cap, b.big_twork_cap);
+        *status = GALA_ERR_CAPACITY;
+        return false;
+    }
+    ba.pool_half = slots;
+    cudaMemsetAsync(b.big_pool, 0xff, (size_t)slots * sizeof(int32_t), st);
+    cudaMemsetAsync(b.big_pool + slots, 0, (size_t)slots * sizeof(int32_t), st);
+    k_big_work<<<grid_cap((long long)cnt3 * 32, 256, cap), 256, 0, st>>>(a, ba);
+    k_big_insert<<<(int)(nwork < nsm * 8 ? nwork : nsm * 8), 256, 0, st>>>(a, ba, nwork);
+    k_big_mark<<<grid_cap(cnt3, 256, cap), 256, 0, st>>>(a, ba);
+    exclusive_scan(b.big_gwords, b.big_gofs, cnt3, OpIdentity(), b.scan_partial, &b.stats->total, st);
+    note_launch(3);
+    if (!read_stats(&hs, b.stats, st, status, "contraction: long-row bitmaps")) return false;
+    const long long words = hs.total;
+    if (2 * words > b.big_bitmap_words) {
+        set_error("contraction: %lld bitmap words needed, scratch holds %lld", 2 * words, b.big_bitmap_words);
+        *status = GALA_ERR_CAPACITY;
+        return false;
+    }
+    ba.bits = (unsigned *)b.big_bitmap;
+    ba.pref = (unsigned *)b.big_bitmap + words;
+    if (words > 0) cudaMemsetAsync(ba.bits, 0, (size_t)words * sizeof(unsigned), st);
+    const int tgrid = (int)(ntwork < nsm * 8 ? ntwork : nsm * 8);
+    k_big_collect<<<tgrid, 256, 0, st>>>(a, ba, ntwork);
+    note_launch(1);
+    if (words > 0) {
+        exclusive_scan(ba.bits, ba.pref, words, OpPopc(), b.scan_partial, &b.stats->total, st);
+        k_big_rank<<<tgrid, 256, 0, st>>>(a, ba, ntwork);
+        note_launch(1);
+    }
+    k_big_sort<<<cnt3 < nsm * 2 ? cnt3 : nsm * 2, 1024, kSortSmem, st>>>(a, ba);
+    note_launch(1);
     return true;
 }
 
@@ -568,13 +857,19 @@ int contract_run(const LevelGraph &g, const int32_t *comm, ContractBuffers &b, i
     exclusive_scan(b.members, b.medge, n, OpDegOf{g.offs}, b.scan_partial, &b.stats->total, st);
     // moff[C] = n and medge[n] = E close the last segments
     k_contract_set_tail<<<1, 1, 0, st>>>(b.moff, C, n, b.medge, g.E);
-    if (g.w)
-        k_stream_fill<true><<<grid_cap((long long)n * 32, 256, cap), 256, 0, st>>>(
-            n, g.offs, g.nbr, g.w, b.lab, b.mpos, b.medge, b.stream_key, b.stream_w);
-    else
-        k_stream_fill<false><<<grid_cap((long long)n * 32, 256, cap), 256, 0, st>>>(
-            n, g.offs, g.nbr, g.w, b.lab, b.mpos, b.medge, b.stream_key, b.stream_w);
-    k_classify<<<grid_cap(C, 256, cap), 256, 0, st>>>(C, b.ec, b.cls_list, b.stats);
+    const int fill_grid = grid_cap((g.E + kRangeEntries - 1) / kRangeEntries * 32, 256, cap);
+    if (g.E > 0) {
+        build_walk_list(g.offs, n, g.E, b, st);
+        if (g.w)
+            k_stream_fill<true><<<fill_grid, 256, 0, st>>>(n, g.E, g.offs, g.nbr, g.w, b.lab, b.mpos, b.medge,
+                                                          b.stream_key, b.stream_w, b.nz_rows, b.nz_offs,
+                                                          b.stats);
+        else
+            k_stream_fill<false><<<fill_grid, 256, 0, st>>>(n, g.E, g.offs, g.nbr, g.w, b.lab, b.mpos, b.medge,
+                                                           b.stream_key, b.stream_w, b.nz_rows, b.nz_offs,
+                                                           b.stats);
+    }
+    k_classify<<<grid_cap(C, 256, cap), 256, 0, st>>>(C, b.ec, b.cls_list, b.kc, b.stats);
     exclusive_scan(b.ec, b.tmp_off, C, OpCap{C}, b.scan_partial, &b.stats->total, st);
     note_launch(6 + (orig_map ? 1 : 0));
     if (!read_stats(&hs, b.stats, st, status, "contraction: classification")) return -1;
@@ -606,61 +901,25 @@ int contract_run(const LevelGraph &g, const int32_t *comm, ContractBuffers &b, i
         k_agg_mid<256, 8192, kMid2Max><<<grid, 256, kMid2Smem, st>>>(a, b.cls_list + 2LL * C, 2);
         note_launch(1);
     }
-    if (hs.small_cnt[3] > 0) {
-        const int cnt3 = hs.small_cnt[3];
-        BigArgs ba;
-        ba.list = b.cls_list + 3LL * C;
-        ba.T = b.big_T;
-        ba.chunks = b.big_chunks;
-        ba.toff = b.big_toff;
-        ba.coff = b.big_coff;
-        ba.mode = b.big_mode;
-        ba.work = b.big_work;
-        ba.pool = b.big_pool;
-        ba.pool_half = 0;
-        k_big_plan<<<grid_cap(cnt3, 256, cap), 256, 0, st>>>(a, ba);
-        exclusive_scan(b.big_T, b.big_toff, cnt3, OpIdentity(), b.scan_partial, &b.stats->total, st);
-        exclusive_scan(b.big_chunks, b.big_coff, cnt3, OpIdentity(), b.scan_partial, &b.stats->total2, st);
-        k_big_tail<<<1, 1, 0, st>>>(ba, b.stats);
-        note_launch(2);
-        if (!read_stats(&hs, b.stats, st, status, "contraction: large rows")) return -1;
-        const long long slots = hs.total, nwork = hs.total2;
-        if (2 * slots > b.big_pool_ints || nwork > b.big_work_cap) {
-            set_error("contraction: large rows need %lld table slots / %lld chunks, pool holds %lld / %lld", slots,
-                      nwork, b.big_pool_ints / 2, b.big_work_cap);
-            *status = GALA_ERR_CAPACITY;
-            return -1;
-        }
-        ba.pool_half = slots;
-        cudaMemsetAsync(b.big_pool, 0xff, (size_t)slots * sizeof(int32_t), st);
-        cudaMemsetAsync(b.big_pool + slots, 0, (size_t)slots * sizeof(int32_t), st);
-        k_big_work<<<grid_cap((long long)cnt3 * 32, 256, cap), 256, 0, st>>>(a, ba);
-        k_big_insert<<<(int)(nwork < nsm * 8 ? nwork : nsm * 8), 256, 0, st>>>(a, ba, nwork);
-        const long long words = ((long long)C + 31) / 32;
-        long long grid = cnt3 < nsm * 2 ? cnt3 : nsm * 2;
-        const long long fit = b.big_bitmap_words / (2 * words);
-        if (grid > fit) grid = fit;
-        if (grid < 1) {
-            set_error("contraction: %d communities need a %lld-word bitmap, scratch holds %lld", C, 2 * words,
-                      b.big_bitmap_words);
-            *status = GALA_ERR_CAPACITY;
-            return -1;
-        }
-        k_big_emit<<<(int)grid, 1024, kEmitSmem, st>>>(a, ba, (unsigned *)b.big_bitmap, words);
-        note_launch(3);
-    }
+    if (hs.small_cnt[3] > 0 && !contract_long_rows(a, b, hs.small_cnt[3], C, hs, st, status)) return -1;
     exclusive_scan(b.kc, new_offs, C, OpIdentity(), b.scan_partial, &b.stats->total, st);
     k_set_last_offset<<<1, 1, 0, st>>>(new_offs, C, &b.stats->total);
-    k_compact<<<grid_cap((long long)C * 32, 256, cap), 256, 0, st>>>(C, b.kc, new_offs, b.tmp_off, b.tmp_nbr,
-                                                                     b.tmp_w, new_nbr, new_w);
-    note_launch(2);
+    note_launch(1);
+    if (!read_stats(&hs, b.stats, st, status, "contraction: offsets")) return -1;
+    const long long Enew = hs.total;
+    if (Enew > 0) {
+        build_walk_list(new_offs, C, Enew, b, st);
+        k_compact<<<grid_cap((Enew + kRangeEntries - 1) / kRangeEntries * 32, 256, cap), 256, 0, st>>>(
+            C, Enew, new_offs, b.tmp_off, b.tmp_nbr, b.tmp_w, new_nbr, new_w, g.E, b.nz_rows, b.nz_offs, b.stats);
+        note_launch(1);
+    }
     if (!read_stats(&hs, b.stats, st, status, "contraction: compaction")) return -1;
     if (hs.err) {
         set_error("contraction: hash table overflow (error bits %d)", hs.err);
         *status = GALA_ERR_OVERFLOW;
         return -1;
     }
-    *new_E = hs.total;
+    *new_E = Enew;
     return C;
 }
 

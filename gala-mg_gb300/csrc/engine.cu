@@ -34,6 +34,11 @@ struct gala_context {
     DevStats *h_stats = nullptr;
     int32_t *scratch = nullptr;
     long long scratch_ints = 0;
+    // per table chunk of the hub bin: best candidate of the chunk
+    long long *hub_px = nullptr;
+    int32_t *hub_pc = nullptr, *hub_pw = nullptr, *hub_pt = nullptr, *hub_pwc = nullptr;
+    double *hub_pdq = nullptr;
+    int32_t *hub_pfc = nullptr;
     cudaEvent_t ev[8] = {};
     // the degree bins of one sweep are independent: they run concurrently on
     // auxiliary streams, forked from and joined back into `stream`
@@ -173,19 +178,45 @@ gala_status phase1(gala_context *ctx, const LevelGraph &g, long long &m2, double
         level_cnt[i] = bin_start[i + 1] - bin_start[i];
         nv_all += level_cnt[i];
     }
-    // hub tables (bin 7) in the scratch pool
-    int hub_tmax = 64;
-    if (level_cnt[7] > 0) {
-        hub_tmax = next_pow2_int(2LL * max_deg);
-        long long per = 2LL * hub_tmax;
-        if ((long long)ctx->scratch_ints < per) {
-            set_error("hub vertex of degree %d needs a %lld-slot table, scratch holds %lld", max_deg, per,
-                      ctx->scratch_ints);
+    (void)max_deg;
+    // hub vertices (bin 7): per-hub global tables in the long-row pool of the
+    // contraction, which is idle during phase 1
+    HubPlan hp{};
+    hp.H = level_cnt[7];
+    if (hp.H > 0) {
+        ContractBuffers &cb = ctx->cb;
+        hp.hubs = b.order + bin_start[7];
+        hp.T = cb.big_T;
+        hp.chunks = cb.big_chunks;
+        hp.tchunks = cb.big_tchunks;
+        hp.toff = cb.big_toff;
+        hp.coff = cb.big_coff;
+        hp.tcoff = cb.big_tcoff;
+        hp.work = cb.big_work;
+        hp.twork = cb.big_twork;
+        hp.pool = cb.big_pool;
+        hp.px = ctx->hub_px;
+        hp.pc = ctx->hub_pc;
+        hp.pw = ctx->hub_pw;
+        hp.pt = ctx->hub_pt;
+        hp.pwc = ctx->hub_pwc;
+        hp.pdq = ctx->hub_pdq;
+        hp.pfc = ctx->hub_pfc;
+        p1_hub_plan_launch(g, b, hp, st);
+        if ((s = check(cudaMemcpyAsync(h, b.stats, sizeof(DevStats), cudaMemcpyDeviceToHost, st), "hub plan")) ||
+            (s = check(cudaStreamSynchronize(st), "hub plan")))
+            return s;
+        hp.half = h->total;
+        hp.nwork = h->total2;
+        hp.ntwork = h->total3;
+        if (2 * hp.half > cb.big_pool_ints || hp.nwork > cb.big_work_cap || hp.ntwork > cb.big_twork_cap) {
+            set_error("hub tables need %lld slots / %lld + %lld chunks, pool holds %lld / %lld / %lld", hp.half,
+                      hp.nwork, hp.ntwork, cb.big_pool_ints / 2, cb.big_work_cap, cb.big_twork_cap);
             return GALA_ERR_CAPACITY;
         }
+        p1_hub_work_launch(hp, st);
     }
-    b.hub_table = ctx->scratch;
-    b.hub_table_slots = ctx->scratch_ints;
+    cudaMemsetAsync(b.act_flag, 1, (size_t)g.n, st);
 
     double q = q_from_sums(h->sum_in, h->sum_tot2, m2);
     if (trace) trace->push_back(q);
@@ -209,8 +240,11 @@ gala_status phase1(gala_context *ctx, const LevelGraph &g, long long &m2, double
         fork(ctx);
         for (int k = 0; k < kNumBins; ++k) {
             const int bin = kBinLaunchOrder[k];
-            p1_decide(g, b, bin, lists + bin_start[bin], &b.stats->act_count[cur][bin], level_cnt[bin], constant,
-                      m2, fp64_only, hub_tmax, aux_for(ctx, k));
+            if (bin == 7)
+                p1_hub_decide(g, b, hp, constant, m2, fp64_only, aux_for(ctx, k));
+            else
+                p1_decide(g, b, bin, lists + bin_start[bin], &b.stats->act_count[cur][bin], level_cnt[bin],
+                          constant, m2, fp64_only, 64, aux_for(ctx, k));
         }
         join(ctx);
         cudaEventRecord(ctx->ev[3], st);
@@ -299,6 +333,7 @@ gala_status run_levels(gala_context *ctx, int32_t n0, int64_t E0, const int64_t 
     cudaEvent_t t0 = ctx->ev[6], t1 = ctx->ev[7];
     cudaEventRecord(t0, st);
     k_iota<<<std::min(4096, (n0 + 255) / 256), 256, 0, st>>>(ctx->orig, n0);
+    cudaMemsetAsync(&ctx->d_stats->fp64_decisions, 0, sizeof(unsigned long long), st);
     note_launch(1);
 
     LevelGraph g{n0, E0, offs0, nbr0, w0};
@@ -377,6 +412,12 @@ gala_status run_levels(gala_context *ctx, int32_t n0, int64_t E0, const int64_t 
         memcpy(res->iter_modularity, trace.data(), (size_t)k * sizeof(double));
     }
     res->iter_count = (int)trace.size();
+    unsigned long long nfp = 0;
+    if ((s = check(cudaMemcpyAsync(&nfp, &ctx->d_stats->fp64_decisions, sizeof(nfp), cudaMemcpyDeviceToHost, st),
+                   "fp64 count")) ||
+        (s = check(cudaStreamSynchronize(st), "fp64 count")))
+        return s;
+    res->fp64_decisions = (int64_t)nfp;
     return GALA_OK;
 }
 
@@ -444,7 +485,9 @@ gala_status gala_context_create(int32_t device, int32_t max_vertices, int64_t ma
     ctx->e_cap = max_entries;
     const size_t n = (size_t)max_vertices, E = (size_t)(max_entries > 0 ? max_entries : 1);
     const size_t nblk = (n + 1023) / 1024;
-    const size_t scan_items = std::max(n + 2, (size_t)kNumBinSlots * nblk);
+    // scans run over at most max(n, 9 * blocks, scratch words) items (the
+    // scratch pool is at most 2^27 ints)
+    const size_t scan_items = std::max(std::max(n + 2, (size_t)kNumBinSlots * nblk), (size_t)1 << 27);
     const size_t nparts = scan_items / 4096 + 4;
     bool ok = cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamNonBlocking) == cudaSuccess;
     ctx->stream = ctx->own_stream;
@@ -475,9 +518,18 @@ gala_status gala_context_create(int32_t device, int32_t max_vertices, int64_t ma
     // (keys + values), chunk list of at most E / 4096 + n entries
     c.big_pool_ints = 8LL * (long long)E + 64;
     c.big_work_cap = (long long)E / 4096 + (long long)n + 1;
+    c.big_twork_cap = (long long)E / 1024 + (long long)n + 1;  // table slots <= 4E, 4096 per chunk
     ok = ok && dalloc(ctx, &c.big_pool, (size_t)c.big_pool_ints) && dalloc(ctx, &c.big_T, n) &&
          dalloc(ctx, &c.big_chunks, n) && dalloc(ctx, &c.big_toff, n + 1) && dalloc(ctx, &c.big_coff, n + 1) &&
-         dalloc(ctx, &c.big_mode, n) && dalloc(ctx, &c.big_work, (size_t)c.big_work_cap);
+         dalloc(ctx, &c.big_mode, n) && dalloc(ctx, &c.big_work, (size_t)c.big_work_cap) &&
+         dalloc(ctx, &c.big_tchunks, n) && dalloc(ctx, &c.big_tcoff, n + 1) &&
+         dalloc(ctx, &c.big_twork, (size_t)c.big_twork_cap) && dalloc(ctx, &c.big_kdist, n) &&
+         dalloc(ctx, &c.big_cursor, n) && dalloc(ctx, &c.big_gwords, n) && dalloc(ctx, &c.big_gofs, n + 1);
+    ok = ok && dalloc(ctx, &b.act_flag, n) && dalloc(ctx, &ctx->hub_px, (size_t)c.big_twork_cap) &&
+         dalloc(ctx, &ctx->hub_pc, (size_t)c.big_twork_cap) && dalloc(ctx, &ctx->hub_pw, (size_t)c.big_twork_cap) &&
+         dalloc(ctx, &ctx->hub_pt, (size_t)c.big_twork_cap) && dalloc(ctx, &ctx->hub_pwc, (size_t)c.big_twork_cap) &&
+         dalloc(ctx, &ctx->hub_pdq, (size_t)c.big_twork_cap) && dalloc(ctx, &ctx->hub_pfc, (size_t)c.big_twork_cap) &&
+         dalloc(ctx, &c.nz_pos, n + 1) && dalloc(ctx, &c.nz_rows, n + 1) && dalloc(ctx, &c.nz_offs, n + 1);
     // scratch pool for hub tables (phase 1) and the emission bitmaps of the
     // contraction: 8 ints per entry+vertex, 16 MB .. 512 MB
     long long want = 8LL * ((long long)E + (long long)n);

@@ -52,7 +52,25 @@ struct Phase1Buffers {
     long long *scan_partial;
     int32_t *hub_table;        // global hash tables of the largest bin
     long long hub_table_slots; // capacity in int32 pairs
+    uint8_t *act_flag;         // 1 = vertex is in the current active set
     DevStats *stats;
+};
+
+// Hub vertices (largest degree bin): per-hub global tables filled by many
+// CTAs.  Arrays are borrowed from the contraction's long-row buffers, which
+// are idle during phase 1.
+struct HubPlan {
+    const int32_t *hubs;  // the bin's vertices (order segment)
+    int H;
+    long long *T, *chunks, *tchunks, *toff, *coff, *tcoff;
+    int32_t *work, *twork;
+    int32_t *pool;
+    long long half;       // keys at pool[0, half), values at pool[half, 2 half)
+    long long nwork, ntwork;
+    long long *px;        // per table chunk: best exact gain numerator
+    int32_t *pc, *pw, *pt, *pwc;
+    double *pdq;          // per table chunk: best FP64 gain (hubs decided in FP64)
+    int32_t *pfc;
 };
 
 // ---- phase 1 kernels (phase1.cu) ----
@@ -70,6 +88,10 @@ void p1_configure_kernels();
 void contract_configure_kernels();
 void p1_reset_level_stats(Phase1Buffers &b, cudaStream_t st);
 int hub_grid_size();
+void p1_hub_plan_launch(const LevelGraph &g, Phase1Buffers &b, HubPlan &p, cudaStream_t st);
+void p1_hub_work_launch(HubPlan &p, cudaStream_t st);
+void p1_hub_decide(const LevelGraph &g, Phase1Buffers &b, const HubPlan &p, double constant, long long m2,
+                   int fp64_only, cudaStream_t st);
 
 // ---- contraction (contract.cu) ----
 struct ContractBuffers {
@@ -89,6 +111,9 @@ struct ContractBuffers {
     int32_t *tmp_nbr;    // E
     int32_t *tmp_w;      // E
     int32_t *kc;         // n+1 distinct neighbours per community
+    int32_t *nz_pos;     // n+1: rows with entries, compacted (walk list)
+    int32_t *nz_rows;    // n+1
+    long long *nz_offs;  // n+1
     int32_t *cls_list;   // n: communities by size class
     // rows of more than 4096 entries: one global table per community, filled
     // by many CTAs (chunks of the stream), then emitted by one CTA each
@@ -99,8 +124,16 @@ struct ContractBuffers {
     long long *big_toff;      // n+1: table offsets
     long long *big_coff;      // n+1: chunk offsets
     int32_t *big_mode;        // n: 1 = dense table indexed by community id
-    int32_t *big_work;        // chunk -> list index
+    int32_t *big_work;        // stream chunk -> list index
     long long big_work_cap;
+    long long *big_tchunks;   // n: table chunks per community
+    long long *big_tcoff;     // n+1: table chunk offsets
+    int32_t *big_twork;       // table chunk -> list index
+    long long big_twork_cap;
+    int32_t *big_kdist;       // n: distinct neighbour communities
+    int32_t *big_cursor;      // n: unsorted emission cursor
+    long long *big_gwords;    // n: bitmap words of rows ranked by bitmap (0 = sorted in smem)
+    long long *big_gofs;      // n+1: bitmap word offsets
     int32_t *big_bitmap;      // per-CTA bitmaps over communities (emission)
     long long big_bitmap_words;
     long long *scan_partial;

@@ -506,6 +506,7 @@ __global__ void __launch_bounds__(256) k_decide_group(DecideArgs a, const int32_
             if (fp) {
                 bc = fc;
                 dec = (fc != cur && gain_correct(dq, wc, sf) > 0.0) ? 1 : 0;
+                atomicAdd(&a.st->fp64_decisions, 1ull);
             }
         }
         const bool move = has && sub == 0 && dec == 1 && guard_ok(a, cur, bc);
@@ -617,6 +618,7 @@ __global__ void __launch_bounds__(256) k_decide_warp(DecideArgs a, const int32_t
             warp_argmax(dq, fc);
             bc = fc;
             dec = (fc != cur && gain_correct(dq, wc, sf) > 0.0) ? 1 : 0;
+            if (lane == 0) atomicAdd(&a.st->fp64_decisions, 1ull);
         }
         const bool move = lane == 0 && dec == 1 && guard_ok(a, cur, bc);
         append_mover(a, move, v, cur, bc);
@@ -721,6 +723,7 @@ __global__ void __launch_bounds__(BLOCK) k_decide_cta(DecideArgs a, const int32_
                 if (lane == 0) {
                     s_bc = fc;
                     s_dec = (fc != cur && gain_correct(dq, s_wc, sf) > 0.0) ? 1 : 0;
+                    atomicAdd(&a.st->fp64_decisions, 1ull);
                 }
             }
             __syncthreads();
@@ -912,6 +915,7 @@ struct UpdateArgs {
     const int32_t *__restrict__ Self;
     const int32_t *__restrict__ Tot;
     int32_t *In;
+    uint8_t *act_flag;  // per-vertex copy of the next active set
     int32_t *act_list;  // next active list, segment of this bin
     int *act_counter;
     DevStats *st;
@@ -951,6 +955,7 @@ __global__ void __launch_bounds__(256) k_update_group(UpdateArgs a, const int32_
             a.In[v] = sum;
             const int ki = a.K[v];
             active = !prune_bound_fast(sum, a.Self[v], ki, min_tot, a.Tot[cur], a.constant, a.m2);
+            a.act_flag[v] = active;
             s_in += (unsigned long long)sum;
             if (active) {
                 s_edges += (unsigned long long)(e - s);
@@ -987,6 +992,7 @@ __global__ void __launch_bounds__(256) k_update_cta(UpdateArgs a, const int32_t 
             a.In[v] = sum;
             const int ki = a.K[v];
             bool active = !prune_bound_fast(sum, a.Self[v], ki, min_tot, a.Tot[cur], a.constant, a.m2);
+            a.act_flag[v] = active;
             s_in += (unsigned long long)sum;
             if (active) {
                 a.act_list[atomicAdd(a.act_counter, 1)] = v;
@@ -1014,6 +1020,7 @@ void p1_update(const LevelGraph &g, Phase1Buffers &b, int bin, const int32_t *li
     a.Self = b.Self;
     a.Tot = b.Tot;
     a.In = b.In;
+    a.act_flag = b.act_flag;
     a.act_list = b.act[next] + bin_start;
     a.act_counter = &b.stats->act_count[next][bin];
     a.st = b.stats;
@@ -1050,6 +1057,249 @@ void p1_update(const LevelGraph &g, Phase1Buffers &b, int bin, const int32_t *li
     }
 #undef GALA_UG
     note_launch(1);
+}
+
+// ------------------------------------------------------------------------
+// Hub vertices (degree > 8192): one global hash table per hub, filled by
+// many CTAs in 4096-entry chunks of the hub's row, scanned by many CTAs in
+// 4096-slot chunks (each writes the best candidate of its chunk), and merged
+// by one warp per hub.  A hub's work is spread over all SMs instead of one.
+// ------------------------------------------------------------------------
+constexpr int kHubChunk = 4096;
+
+__global__ void k_hub_plan(HubPlan p, const int64_t *__restrict__ offs)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < p.H; i += gridDim.x * blockDim.x) {
+        const int v = p.hubs[i];
+        const long long deg = offs[v + 1] - offs[v];
+        const long long T = next_pow2_ll(2 * deg);
+        p.T[i] = T;
+        p.chunks[i] = (deg + kHubChunk - 1) / kHubChunk;
+        p.tchunks[i] = (T + kHubChunk - 1) / kHubChunk;
+    }
+}
+
+__global__ void k_hub_tail(HubPlan p, const DevStats *st)
+{
+    p.toff[p.H] = st->total;
+    p.coff[p.H] = st->total2;
+    p.tcoff[p.H] = st->total3;
+}
+
+__global__ void k_hub_work(HubPlan p)
+{
+    const int lane = threadIdx.x & 31;
+    const int wg = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nw = (gridDim.x * blockDim.x) >> 5;
+    for (int i = wg; i < p.H; i += nw) {
+        long long o = p.coff[i], k = p.coff[i + 1] - o;
+        for (long long j = lane; j < k; j += 32) p.work[o + j] = i;
+        o = p.tcoff[i];
+        k = p.tcoff[i + 1] - o;
+        for (long long j = lane; j < k; j += 32) p.twork[o + j] = i;
+    }
+}
+
+template <bool W>
+__global__ void __launch_bounds__(256) k_hub_insert(DecideArgs a, HubPlan p, const uint8_t *__restrict__ flag)
+{
+    const int lane = threadIdx.x & 31;
+    for (long long wi = blockIdx.x; wi < p.nwork; wi += gridDim.x) {
+        const int i = p.work[wi];
+        const int v = p.hubs[i];
+        if (!flag[v]) continue;
+        const long long e = a.offs[v + 1];
+        const long long s = a.offs[v] + (wi - p.coff[i]) * kHubChunk;
+        const long long e2 = s + kHubChunk < e ? s + kHubChunk : e;
+        const int T = (int)p.T[i];
+        const int lg = __ffs(T) - 1;
+        int *keys = p.pool + p.toff[i];
+        int *vals = p.pool + p.half + p.toff[i];
+        for (long long b0 = s; b0 < e2; b0 += blockDim.x) {
+            const long long j = b0 + threadIdx.x;
+            const bool valid = j < e2;
+            int c = -1, wt = 0;
+            if (valid) {
+                c = a.comm[a.nbr[j]];
+                wt = W ? a.w[j] : 1;
+            }
+            const unsigned m = __match_any_sync(GALA_FULL_MASK, c);
+            const int wsum = W ? (int)__reduce_add_sync(m, (unsigned)wt) : __popc(m);
+            if (valid && __ffs(m) - 1 == lane)
+                if (!hash_add(keys, vals, T, lg, c, wsum)) atomicOr(&a.st->err, kErrHashOverflow);
+        }
+    }
+}
+
+// FP64 evaluation needed whatever the candidates: K*m2 out of the range where
+// the integer order equals the FP64 order (or FP64 forced).
+__device__ __forceinline__ bool needs_fp64(const DecideArgs &a, int ki)
+{
+    return a.fp64_only || (long long)ki * a.m2 >= (1LL << 49);
+}
+
+__global__ void __launch_bounds__(256) k_hub_scan(DecideArgs a, HubPlan p, const uint8_t *__restrict__ flag)
+{
+    __shared__ long long r_x[8];
+    __shared__ double r_dq[8];
+    __shared__ int r_c[8], r_w[8], r_t[8], r_wc[8];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    for (long long wi = blockIdx.x; wi < p.ntwork; wi += gridDim.x) {
+        const int i = p.twork[wi];
+        const int v = p.hubs[i];
+        if (!flag[v]) continue;
+        const int cur = a.comm[v], ki = a.K[v], tcur = a.Tot[cur];
+        const long long j0 = (wi - p.tcoff[i]) * kHubChunk;
+        const long long T = p.T[i];
+        const long long j1 = j0 + kHubChunk < T ? j0 + kHubChunk : T;
+        const int *keys = p.pool + p.toff[i];
+        const int *vals = p.pool + p.half + p.toff[i];
+        long long x = -1;
+        int bc = cur, bw = 0, bt = 0, wc = 0;
+        scan_table_int(a, keys + j0, vals + j0, (int)(j1 - j0), threadIdx.x, blockDim.x, cur, ki, tcur, x, bc, bw,
+                       bt, wc);
+        warp_merge_int(x, bc, bw, bt, wc, 32);
+        if (lane == 0) {
+            r_x[wid] = x;
+            r_c[wid] = bc;
+            r_w[wid] = bw;
+            r_t[wid] = bt;
+            r_wc[wid] = wc;
+        }
+        __syncthreads();
+        if (wid == 0) {
+            const int nwp = blockDim.x >> 5;
+            x = lane < nwp ? r_x[lane] : -1;
+            bc = lane < nwp ? r_c[lane] : cur;
+            bw = lane < nwp ? r_w[lane] : 0;
+            bt = lane < nwp ? r_t[lane] : 0;
+            wc = lane < nwp ? r_wc[lane] : 0;
+            warp_merge_int(x, bc, bw, bt, wc, 32);
+            if (lane == 0) {
+                p.px[wi] = x;
+                p.pc[wi] = bc;
+                p.pw[wi] = bw;
+                p.pt[wi] = bt;
+                p.pwc[wi] = wc;
+            }
+        }
+        __syncthreads();
+        if (needs_fp64(a, ki)) {  // uniform per chunk: the reference's FP64 gains, chunk-wise
+            double dq = 0.0;
+            int fc = cur;
+            scan_table(a, keys + j0, vals + j0, (int)(j1 - j0), threadIdx.x, blockDim.x, cur, ki, tcur, dq, fc);
+            warp_argmax(dq, fc);
+            if (lane == 0) {
+                r_dq[wid] = dq;
+                r_c[wid] = fc;
+            }
+            __syncthreads();
+            if (wid == 0) {
+                const int nwp = blockDim.x >> 5;
+                dq = lane < nwp ? r_dq[lane] : 0.0;
+                fc = lane < nwp ? r_c[lane] : cur;
+                warp_argmax(dq, fc);
+                if (lane == 0) {
+                    p.pdq[wi] = dq;
+                    p.pfc[wi] = fc;
+                }
+            }
+            __syncthreads();
+        }
+    }
+}
+
+__global__ void __launch_bounds__(256) k_hub_final(DecideArgs a, HubPlan p, const uint8_t *__restrict__ flag)
+{
+    const int lane = threadIdx.x & 31;
+    const int wg = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nw = (gridDim.x * blockDim.x) >> 5;
+    for (int i = wg; i < p.H; i += nw) {
+        const int v = p.hubs[i];
+        if (!flag[v]) continue;
+        const int cur = a.comm[v], ki = a.K[v], sf = a.Self[v], tcur = a.Tot[cur];
+        long long x = -1;
+        int bc = cur, bw = 0, bt = 0, wc = 0;
+        for (long long q = p.tcoff[i] + lane; q < p.tcoff[i + 1]; q += 32) {
+            wc += p.pwc[q];
+            if (p.px[q] >= 0) cand_merge(x, bc, bw, bt, p.px[q], p.pc[q], p.pw[q], p.pt[q]);
+        }
+        warp_merge_int(x, bc, bw, bt, wc, 32);
+        int dec = int_decision(a, x, bt, cur, bc, wc, sf, ki);  // warp-uniform
+        if (dec == 2) {
+            double dq = 0.0;
+            int fc = cur;
+            if (needs_fp64(a, ki)) {  // chunk-wise FP64 partials from k_hub_scan
+                for (long long q = p.tcoff[i] + lane; q < p.tcoff[i + 1]; q += 32)
+                    if (cand_better(p.pdq[q], p.pfc[q], dq, fc)) {
+                        dq = p.pdq[q];
+                        fc = p.pfc[q];
+                    }
+            } else {  // rare rounding cases: rescan the table in FP64
+                scan_table(a, p.pool + p.toff[i], p.pool + p.half + p.toff[i], (int)p.T[i], lane, 32, cur, ki, tcur,
+                           dq, fc);
+            }
+            warp_argmax(dq, fc);
+            bc = fc;
+            dec = (fc != cur && gain_correct(dq, wc, sf) > 0.0) ? 1 : 0;
+            if (lane == 0) atomicAdd(&a.st->fp64_decisions, 1ull);
+        }
+        const bool move = lane == 0 && dec == 1 && guard_ok(a, cur, bc);
+        append_mover(a, move, v, cur, bc);
+    }
+}
+
+// Per level: table sizes, chunk counts and their offsets (the caller reads
+// the three totals from the stats block before p1_hub_work_launch).
+void p1_hub_plan_launch(const LevelGraph &g, Phase1Buffers &b, HubPlan &p, cudaStream_t st)
+{
+    const int grid = (p.H + 255) / 256;
+    k_hub_plan<<<grid, 256, 0, st>>>(p, g.offs);
+    exclusive_scan(p.T, p.toff, p.H, OpIdentity(), b.scan_partial, &b.stats->total, st);
+    exclusive_scan(p.chunks, p.coff, p.H, OpIdentity(), b.scan_partial, &b.stats->total2, st);
+    exclusive_scan(p.tchunks, p.tcoff, p.H, OpIdentity(), b.scan_partial, &b.stats->total3, st);
+    k_hub_tail<<<1, 1, 0, st>>>(p, b.stats);
+    note_launch(2);
+}
+
+void p1_hub_work_launch(HubPlan &p, cudaStream_t st)
+{
+    k_hub_work<<<(p.H * 32 + 255) / 256, 256, 0, st>>>(p);
+    note_launch(1);
+}
+
+// One iteration's decide-and-move of the hub bin.
+void p1_hub_decide(const LevelGraph &g, Phase1Buffers &b, const HubPlan &p, double constant, long long m2,
+                   int fp64_only, cudaStream_t st)
+{
+    if (p.H <= 0) return;
+    DecideArgs a;
+    a.offs = g.offs;
+    a.nbr = g.nbr;
+    a.w = g.w;
+    a.comm = b.comm;
+    a.K = b.K;
+    a.Self = b.Self;
+    a.Tot = b.Tot;
+    a.size = b.size;
+    a.mv_v = b.mv_v;
+    a.mv_old = b.mv_old;
+    a.mv_new = b.mv_new;
+    a.st = b.stats;
+    a.constant = constant;
+    a.m2 = m2;
+    a.fp64_only = fp64_only;
+    const int cap = num_sms() * 8;
+    cudaMemsetAsync(p.pool, 0xff, (size_t)p.half * sizeof(int32_t), st);
+    cudaMemsetAsync(p.pool + p.half, 0, (size_t)p.half * sizeof(int32_t), st);
+    const int g1 = (int)(p.nwork < cap ? p.nwork : cap);
+    if (g.w)
+        k_hub_insert<true><<<g1, 256, 0, st>>>(a, p, b.act_flag);
+    else
+        k_hub_insert<false><<<g1, 256, 0, st>>>(a, p, b.act_flag);
+    k_hub_scan<<<(int)(p.ntwork < cap ? p.ntwork : cap), 256, 0, st>>>(a, p, b.act_flag);
+    k_hub_final<<<(p.H * 32 + 255) / 256, 256, 0, st>>>(a, p, b.act_flag);
+    note_launch(3);
 }
 
 }  // namespace gala

@@ -56,7 +56,7 @@ class Result(ctypes.Structure):
                 ("time_d2h_ms", ctypes.c_double), ("decide_sweeps", ctypes.c_int64),
                 ("decide_bytes", ctypes.c_int64), ("update_bytes", ctypes.c_int64),
                 ("kernel_launches", ctypes.c_int64), ("h2d_bytes", ctypes.c_int64),
-                ("d2h_bytes", ctypes.c_int64)]
+                ("d2h_bytes", ctypes.c_int64), ("fp64_decisions", ctypes.c_int64)]
 
     def to_dict(self, trace=None):
         L = self.num_levels
@@ -69,7 +69,8 @@ class Result(ctypes.Structure):
              "time_contract_ms": self.time_contract_ms, "time_h2d_ms": self.time_h2d_ms,
              "time_d2h_ms": self.time_d2h_ms, "decide_sweeps": self.decide_sweeps,
              "decide_bytes": self.decide_bytes, "update_bytes": self.update_bytes,
-             "kernel_launches": self.kernel_launches, "h2d_bytes": self.h2d_bytes, "d2h_bytes": self.d2h_bytes}
+             "kernel_launches": self.kernel_launches, "h2d_bytes": self.h2d_bytes, "d2h_bytes": self.d2h_bytes,
+             "fp64_decisions": self.fp64_decisions}
         if trace is not None:
             d["iter_q"] = trace[:min(self.iter_count, len(trace))].tolist()
         return d

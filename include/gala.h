@@ -89,6 +89,9 @@ typedef struct {
     int64_t kernel_launches;    /* kernels launched by this call */
     int64_t h2d_bytes;
     int64_t d2h_bytes;
+    /* vertex decisions taken with the FP64 gain expressions (the others use
+       exact integer gains; see gala_options.fp64_gains) */
+    int64_t fp64_decisions;
 } gala_result;
 
 /* ---- errors / info --------------------------------------------------- */
