@@ -23,7 +23,7 @@ EXPORTS = ["gala_last_error", "gala_status_string", "gala_kernel_launch_count", 
            "gala_graph_info", "gala_graph_arrays", "gala_graph_destroy", "gala_generate_sbm",
            "gala_generate_rmat", "gala_context_create", "gala_context_destroy", "gala_context_set_stream",
            "gala_graph_pin", "gala_louvain", "gala_louvain_device", "gala_phase1_device", "gala_contract_device",
-           "gala_modularity_host"]
+           "gala_modularity_host", "gala_modularity_device_static"]
 
 _i32p = ctypes.POINTER(ctypes.c_int32)
 _i64p = ctypes.POINTER(ctypes.c_int64)
@@ -117,6 +117,8 @@ def load(path=LIB_PATH):
                                      ctypes.c_int32, _i32p]
     L.gala_contract_device.argtypes = [_vp, ctypes.c_int32, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _i32p, _i64p]
     L.gala_modularity_host.argtypes = [_vp, _i32p, _f64p]
+    L.gala_modularity_device_static.argtypes = [ctypes.c_int32, _vp, _vp, _vp, _vp, _f64p]
+    L.gala_modularity_device_static.restype = ctypes.c_int
     for name in ["gala_graph_load_bin", "gala_graph_store_bin", "gala_graph_from_text", "gala_graph_from_csr",
                  "gala_graph_info", "gala_graph_arrays", "gala_generate_sbm", "gala_generate_rmat",
                  "gala_context_create", "gala_context_set_stream", "gala_graph_pin", "gala_louvain",
@@ -137,6 +139,14 @@ def _ptr(a, t):
 
 def launch_count():
     return int(load().gala_kernel_launch_count())
+
+
+def modularity_device_static(n, d_offs, d_nbr, d_w, d_comm):
+    """gala_modularity_device_static on raw device pointers (no device
+    allocation inside the call)."""
+    q = ctypes.c_double()
+    _check(load().gala_modularity_device_static(n, d_offs, d_nbr, d_w or None, d_comm, ctypes.byref(q)))
+    return q.value
 
 
 def default_options(**kw):

@@ -203,6 +203,24 @@ gala_status gala_contract_device(gala_context *ctx, int32_t n, const int64_t *d_
  * reference keeps at src/louvain_gpu/kernel_functions.cu:1037-1079). */
 gala_status gala_modularity_host(const gala_graph *g, const int32_t *community, double *q);
 
+/* Modularity of a partition of a device CSR (device layout) on the current
+ * device, for callers that must not allocate device memory - e.g. a host
+ * application whose device memory is all owned by its own pool allocator, or
+ * a latency-bound path where cudaMalloc/cudaFree and the synchronisation they
+ * can cause are not allowed.  No counterpart in the reference.
+ * It calls no cudaMalloc, cudaFree or allocating library routine: its scratch
+ * (per-community totals and three sums) is a file-scope device array that
+ * every GPU loading the library holds until the process exits, sized for at
+ * most 1,048,576 vertices (8 MB); larger n returns GALA_ERR_CAPACITY.
+ * The first call on a device looks up the array's device address (make it
+ * before any stream capture).  All calls on a device share the scratch and
+ * clear it first; calls that overlap on the GPU (several host threads at
+ * once on one device) race.  Runs on the default stream and returns after
+ * the result is on the host. */
+gala_status gala_modularity_device_static(int32_t n, const int64_t *d_offsets,
+                                          const int32_t *d_neighbors, const int32_t *d_weights,
+                                          const int32_t *d_community, double *modularity);
+
 #ifdef __cplusplus
 }
 #endif
