@@ -47,6 +47,8 @@ def parse():
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
     p.add_argument("--small", action="store_true", help="tiny workload for a quick check")
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-learned", action="store_true", help="skip the learned-proposal arm")
+    p.add_argument("--threshold", type=float, default=0.3, help="proposal probability threshold")
     p.add_argument("--profile", action="store_true",
                    help="one device-resident run and a short summary (for ncu captures)")
     p.add_argument("--fp64-gains", action="store_true", help="evaluate every gain in FP64")
@@ -168,6 +170,44 @@ def reference_arm(args, wl):
                              "sample": "full run on the whole workload (all rounds), oracle/louvain_oracle.c"},
             "e2e": {"value": val, "unit": "edges/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
+
+
+WEIGHTS = os.path.join(ROOT, "gala-mg_gb300", "proposal_weights.npy")
+
+
+def learned_arm(ffi, ctx, g, stream, args, torch, plain_ms, plain):
+    """The learned move proposal (SKIP mode) end to end on the same graph:
+    time relative to the plain method and final modularity difference."""
+    import proposal_tool
+    prop = ffi.Proposal(max_samples=1 << 22, seed=7)
+    if os.path.exists(WEIGHTS):
+        import numpy as np
+        prop.set_params(np.load(WEIGHTS))
+        source = "gala-mg_gb300/proposal_weights.npy (proposal_tool.py, 64 R-MAT graphs, seeds 1000-1063)"
+    else:
+        proposal_tool.train_on_rmat(prop, range(1000, 1008), [18, 19, 20], sample_shift=2, epochs=6, ctx=ctx)
+        source = "trained in this run: 8 R-MAT graphs (scales 18-20, seeds 1000-1007)"
+    times, r = [], None
+    for i in range(args.warmup + args.steps):
+        torch.cuda.synchronize()
+        with torch.cuda.stream(stream):
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            r = ctx.louvain(g, proposal=prop, mode=ffi.PROPOSAL_SKIP, threshold=args.threshold)
+            b.record(stream)
+        torch.cuda.synchronize()
+        if i >= args.warmup:
+            times.append(a.elapsed_time(b))
+    ms = sum(times) / len(times)
+    prop.close()
+    return {"mode": "skip", "threshold": args.threshold, "weights": source, "ms_per_step": ms,
+            "time_vs_plain": ms / plain_ms, "modularity": r["modularity"],
+            "dq_vs_plain": r["modularity"] - plain["modularity"], "decisions": r["decisions"],
+            "plain_decisions": plain["decisions"], "skipped": r["skipped"], "verify_sweeps": r["verify_sweeps"],
+            "iterations": r["total_iterations"], "plain_iterations": plain["total_iterations"],
+            "phase_ms": {"decide": r["time_decide_ms"], "update": r["time_update_ms"],
+                         "contract": r["time_contract_ms"]}}
 
 
 def main():
@@ -300,6 +340,8 @@ def main():
             "e2e": {"value": world * m / (e2e_step / 1000.0), "unit": "edges/s", "ms_per_step": e2e_step,
                     "h2d_bytes_per_step": r_e2e["h2d_bytes"], "d2h_bytes_per_step": r_e2e["d2h_bytes"]},
             "roofline": roof, "clocks": clk, "gpu_launches": launches}
+    if not args.no_learned:
+        line["learned"] = learned_arm(ffi, ctx, g, stream, args, torch, e2e_step, r_e2e)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
         dt, ro = cpu_oracle_run(offs, nbr, threads)

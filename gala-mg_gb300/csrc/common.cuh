@@ -58,6 +58,11 @@ struct DevStats {
     long long total3;                 // scratch total of a third scan
     long long total;                  // scratch total of the last scan
     unsigned long long fp64_decisions; // vertices decided with the FP64 expressions
+    // move-proposal modes
+    int prop_count[kNumBins];          // vertices the network proposes, per bin
+    long long trace_mark;              // sample count before the current sweep
+    unsigned long long skipped;        // active vertices not decided (proposal said stay)
+    unsigned long long skipped_edges;  // row entries of the skipped vertices
 };
 
 constexpr int kErrHashOverflow = 1;

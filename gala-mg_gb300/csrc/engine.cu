@@ -123,6 +123,18 @@ struct Phase1Out {
     int iterations = 0;
     double decide_ms = 0, update_ms = 0, total_ms = 0;
     long long decide_bytes = 0, update_bytes = 0, sweeps = 0;
+    long long decisions = 0;      // vertices decided (active, or proposed)
+    long long skipped = 0;        // active vertices the network let stay
+    long long verify_sweeps = 0;  // full plain sweeps run to judge convergence
+};
+
+// Move-proposal settings of one run (mode GALA_PROPOSAL_OFF / TRACE / SKIP).
+struct PropRun {
+    int mode = GALA_PROPOSAL_OFF;
+    ProposalView pv{};
+    float threshold = 0.5f;
+    int sample_shift = 0;
+    int level = 0;
 };
 
 // Per-vertex and per-edge algorithmic bytes of a decide-and-move sweep:
@@ -135,9 +147,18 @@ long long decide_bytes_for(long long nv, long long ne, bool weighted)
 
 // One phase-1 run on level graph g (louvain_main_process).  The accepted
 // partition is left in ctx->p1.comm.
+//
+// With a proposal in SKIP mode, sweeps after the first decide only the
+// vertices the network proposes (hub vertices are always decided).  The
+// first proposal sweep that raises Q by less than min_mod is kept (one that
+// lowers Q is reverted) and the level continues with plain sweeps; only a
+// plain sweep can end the level, with the reference's rule.  So the
+// partition a level returns has passed a plain sweep that found no further
+// gain of min_mod.
 gala_status phase1(gala_context *ctx, const LevelGraph &g, long long &m2, double min_mod, bool verbose,
-                   std::vector<double> *trace, Phase1Out *out, int fp64_only = 0)
+                   std::vector<double> *trace, Phase1Out *out, int fp64_only = 0, const PropRun *pr = nullptr)
 {
+    const int pmode = pr ? pr->mode : GALA_PROPOSAL_OFF;
     cudaStream_t st = ctx->stream;
     Phase1Buffers &b = ctx->p1;
     DevStats *h = ctx->h_stats;
@@ -217,6 +238,8 @@ gala_status phase1(gala_context *ctx, const LevelGraph &g, long long &m2, double
         p1_hub_work_launch(hp, st);
     }
     cudaMemsetAsync(b.act_flag, 1, (size_t)g.n, st);
+    b.features_on = pmode != GALA_PROPOSAL_OFF;
+    if (b.features_on) p1_features_init(b, g.n, st);
 
     double q = q_from_sums(h->sum_in, h->sum_tot2, m2);
     if (trace) trace->push_back(q);
@@ -231,24 +254,46 @@ gala_status phase1(gala_context *ctx, const LevelGraph &g, long long &m2, double
     long long act_nv = nv_all, act_ne = g.E;
     int cur = 0;
     const int min_tot_init = m2 > 0x7fffffffLL ? 0x7fffffff : (int)m2;
+    unsigned long long skipped0 = h->skipped, skipped_e0 = h->skipped_edges;
+    bool verify = false;  // proposals stalled: the rest of the level runs plain sweeps
     cudaEventRecord(ctx->ev[0], st);
     for (;;) {
         const int nxt = cur ^ 1;
+        const int32_t *lists = iteration == 1 ? b.order : b.act[cur];
+        const int *counts = &b.stats->act_count[cur][0];
+        // sweep kind: the first sweep of a level and verification sweeps are plain
+        const bool proposal_sweep = pmode == GALA_PROPOSAL_SKIP && iteration > 1 && !verify;
+        ProposalStep ps{};
+        if (pmode != GALA_PROPOSAL_OFF) {
+            ps.mode = pmode;
+            ps.pv = pr->pv;
+            ps.threshold = pr->threshold;
+            ps.sample_shift = pr->sample_shift;
+            ps.iteration = iteration;
+            ps.level = pr->level;
+        }
         p1_iter_reset(b, nxt, min_tot_init, st);
         cudaEventRecord(ctx->ev[2], st);
-        const int32_t *lists = iteration == 1 ? b.order : b.act[cur];
+        if ((pmode == GALA_PROPOSAL_TRACE && iteration > 1) || proposal_sweep) {
+            p1_proposal_step(g, b, ps, lists, counts, bin_start, level_cnt, st);
+            if (proposal_sweep) {
+                lists = b.prop_list;
+                counts = &b.stats->prop_count[0];
+            }
+        }
         fork(ctx);
         for (int k = 0; k < kNumBins; ++k) {
             const int bin = kBinLaunchOrder[k];
             if (bin == 7)
                 p1_hub_decide(g, b, hp, constant, m2, fp64_only, aux_for(ctx, k));
             else
-                p1_decide(g, b, bin, lists + bin_start[bin], &b.stats->act_count[cur][bin], level_cnt[bin],
-                          constant, m2, fp64_only, 64, aux_for(ctx, k));
+                p1_decide(g, b, bin, lists + bin_start[bin], counts + bin, level_cnt[bin], constant, m2, fp64_only,
+                          64, aux_for(ctx, k));
         }
         join(ctx);
         cudaEventRecord(ctx->ev[3], st);
-        p1_apply_movers(b, +1, g.n, st);
+        p1_apply_movers(b, +1, g.n, st, iteration);
+        if (pmode == GALA_PROPOSAL_TRACE && iteration > 1) p1_trace_labels(b, ps, st);
         p1_tot_reduce(b, g.n, st);
         cudaEventRecord(ctx->ev[4], st);
         fork(ctx);
@@ -266,11 +311,22 @@ gala_status phase1(gala_context *ctx, const LevelGraph &g, long long &m2, double
             set_error("phase 1: device error bits %d", h->err);
             return GALA_ERR_OVERFLOW;
         }
+        long long dec_nv = act_nv, dec_ne = act_ne;
+        if (proposal_sweep) {
+            const long long sk = (long long)(h->skipped - skipped0), ske = (long long)(h->skipped_edges - skipped_e0);
+            dec_nv -= sk;
+            dec_ne -= ske;
+            out->skipped += sk;
+        }
+        skipped0 = h->skipped;
+        skipped_e0 = h->skipped_edges;
+        out->decisions += dec_nv;
         out->decide_ms += ev_ms(ctx->ev[2], ctx->ev[3]);
         out->update_ms += ev_ms(ctx->ev[4], ctx->ev[5]);
-        out->decide_bytes += decide_bytes_for(act_nv, act_ne, weighted);
+        out->decide_bytes += decide_bytes_for(dec_nv, dec_ne, weighted);
         out->update_bytes += nv_all * (2 * 8 + 4 * 4) + g.E * (8 + (weighted ? 4 : 0));
         out->sweeps += 1;
+        if (verify) out->verify_sweeps += 1;
         act_nv = h->act_vertices[nxt];
         act_ne = (long long)h->act_edges[nxt];
         q = q_from_sums(h->sum_in, h->sum_tot2, m2);
@@ -278,9 +334,39 @@ gala_status phase1(gala_context *ctx, const LevelGraph &g, long long &m2, double
         if (verbose) printf("Iteration:%d Q:%f\n", iteration, q);
         // convergence (louvain_main_process.cu:1004-1007): the partition of
         // this iteration is dropped when Q did not grow by min_mod
+        if (q - prev_q < min_mod && proposal_sweep && q > prev_q) {
+            // a proposal sweep that still raised Q: keep it and continue with
+            // plain sweeps, which judge convergence
+            verify = true;
+            prev_q = q;
+            cur = nxt;
+            iteration++;
+            continue;
+        }
         if (q - prev_q < min_mod) {
             p1_apply_movers(b, -1, g.n, st);
-            break;
+            if (!proposal_sweep) break;
+            // a proposal sweep that lowered Q: restore the partition, rebuild
+            // In, the active set and the sums into slot nxt, then judge the
+            // restored partition with a plain sweep
+            p1_iter_reset(b, nxt, min_tot_init, st);
+            p1_tot_reduce(b, g.n, st);
+            fork(ctx);
+            for (int k = 0; k < kNumBins; ++k) {
+                const int bin = kBinLaunchOrder[k];
+                p1_update(g, b, bin, b.order + bin_start[bin], level_cnt[bin], nxt, bin_start[bin], constant, m2,
+                          aux_for(ctx, k));
+            }
+            join(ctx);
+            if ((s = check(cudaMemcpyAsync(h, b.stats, sizeof(DevStats), cudaMemcpyDeviceToHost, st), "restore")) ||
+                (s = check(cudaStreamSynchronize(st), "restore")))
+                return s;
+            act_nv = h->act_vertices[nxt];
+            act_ne = (long long)h->act_edges[nxt];
+            verify = true;
+            cur = nxt;
+            iteration++;
+            continue;
         }
         prev_q = q;
         cur = nxt;
@@ -328,6 +414,25 @@ gala_status run_levels(gala_context *ctx, int32_t n0, int64_t E0, const int64_t 
                   ctx->n_cap, (long long)ctx->e_cap);
         return GALA_ERR_CAPACITY;
     }
+    PropRun pr;
+    if (opt && opt->proposal_mode != GALA_PROPOSAL_OFF) {
+        if (opt->proposal_mode != GALA_PROPOSAL_TRACE && opt->proposal_mode != GALA_PROPOSAL_SKIP) {
+            set_error("unknown proposal mode %d", opt->proposal_mode);
+            return GALA_ERR_INVALID;
+        }
+        if (!opt->proposal) {
+            set_error("proposal mode %d needs a proposal network (options.proposal)", opt->proposal_mode);
+            return GALA_ERR_INVALID;
+        }
+        pr.mode = opt->proposal_mode;
+        pr.pv = proposal_view(opt->proposal);
+        pr.threshold = opt->proposal_threshold;
+        pr.sample_shift = opt->trace_sample_shift;
+        if (pr.mode == GALA_PROPOSAL_TRACE && pr.pv.cap <= 0) {
+            set_error("trace mode needs a proposal with sample capacity");
+            return GALA_ERR_INVALID;
+        }
+    }
     bind_contract_buffers(ctx);
     long long m2 = 0;  // set by the first phase-1 run
     cudaEvent_t t0 = ctx->ev[6], t1 = ctx->ev[7];
@@ -346,11 +451,16 @@ gala_status run_levels(gala_context *ctx, int32_t n0, int64_t E0, const int64_t 
     std::vector<double> trace;
     double contract_ms = 0, p1_ms = 0, dec_ms = 0, upd_ms = 0;
     long long dec_bytes = 0, upd_bytes = 0, sweeps = 0;
+    long long decisions = 0, skipped = 0, verify_sweeps = 0;
     int C = n0;
     for (;;) {
         if (verbose) printf("===============round:%d===============\n", round);
         Phase1Out po;
-        if ((s = phase1(ctx, g, m2, min_mod, verbose, &trace, &po, opt ? opt->fp64_gains : 0))) return s;
+        pr.level = round;
+        if ((s = phase1(ctx, g, m2, min_mod, verbose, &trace, &po, opt ? opt->fp64_gains : 0, &pr))) return s;
+        decisions += po.decisions;
+        skipped += po.skipped;
+        verify_sweeps += po.verify_sweeps;
         p1_ms += po.total_ms;
         dec_ms += po.decide_ms;
         upd_ms += po.update_ms;
@@ -407,6 +517,17 @@ gala_status run_levels(gala_context *ctx, int32_t n0, int64_t E0, const int64_t 
     res->decide_bytes = dec_bytes;
     res->update_bytes = upd_bytes;
     res->decide_sweeps = sweeps;
+    res->decisions = decisions;
+    res->skipped = skipped;
+    res->verify_sweeps = verify_sweeps;
+    res->samples = 0;
+    if (pr.mode == GALA_PROPOSAL_TRACE) {
+        long long cnt = 0;
+        if ((s = check(cudaMemcpyAsync(&cnt, pr.pv.count, sizeof(cnt), cudaMemcpyDeviceToHost, st), "samples")) ||
+            (s = check(cudaStreamSynchronize(st), "samples")))
+            return s;
+        res->samples = std::min<long long>(cnt, pr.pv.cap);
+    }
     if (res->iter_modularity && res->iter_capacity > 0) {
         int k = (int)std::min<size_t>(trace.size(), (size_t)res->iter_capacity);
         memcpy(res->iter_modularity, trace.data(), (size_t)k * sizeof(double));
@@ -506,7 +627,9 @@ gala_status gala_context_create(int32_t device, int32_t max_vertices, int64_t ma
          dalloc(ctx, &b.In, n) && dalloc(ctx, &b.order, n) && dalloc(ctx, &b.act[0], n) &&
          dalloc(ctx, &b.act[1], n) && dalloc(ctx, &b.mv_v, n) && dalloc(ctx, &b.mv_old, n) &&
          dalloc(ctx, &b.mv_new, n) && dalloc(ctx, &b.blockcnt, kNumBinSlots * nblk) &&
-         dalloc(ctx, &b.blockoff, kNumBinSlots * nblk) && dalloc(ctx, &b.scan_partial, nparts);
+         dalloc(ctx, &b.blockoff, kNumBinSlots * nblk) && dalloc(ctx, &b.scan_partial, nparts) &&
+         dalloc(ctx, &b.feat_gain, n) && dalloc(ctx, &b.feat_ndist, n) && dalloc(ctx, &b.last_move, n) &&
+         dalloc(ctx, &b.prop_list, n);
     ContractBuffers &c = ctx->cb;
     ok = ok && dalloc(ctx, &c.cnt, n + 1) && dalloc(ctx, &c.newid, n + 1) && dalloc(ctx, &c.lab, n) &&
          dalloc(ctx, &c.csz, n + 1) && dalloc(ctx, &c.moff, n + 1) && dalloc(ctx, &c.cursor, n + 1) &&

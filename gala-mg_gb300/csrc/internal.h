@@ -24,6 +24,21 @@ struct gala_graph {
 
 namespace gala {
 
+// Move-proposal network: 8 features, 8 -> 32 -> 32 -> 1.
+constexpr int kPropFeatures = 8;
+constexpr int kPropParams = 32 * 8 + 32 + 32 * 32 + 32 + 32 + 1;
+
+// Device view of a proposal's sample set and inference weights.
+struct ProposalView {
+    float *X;           // features, kPropFeatures per sample
+    float *Y;           // labels (1 = moved)
+    int32_t *V;         // vertex of each sample (labelled after the sweep)
+    long long cap;
+    long long *count;   // samples written (may exceed cap; clamp)
+    const void *wb;     // BF16 inference weights
+};
+ProposalView proposal_view(gala_proposal *p);
+
 // Error text of the last failure on this host thread.
 void set_error(const char *fmt, ...);
 void clear_error();
@@ -53,8 +68,32 @@ struct Phase1Buffers {
     int32_t *hub_table;        // global hash tables of the largest bin
     long long hub_table_slots; // capacity in int32 pairs
     uint8_t *act_flag;         // 1 = vertex is in the current active set
+    // move-proposal features (written only when a proposal mode is on)
+    float *feat_gain;          // best corrected gain at the last decision / (K m2)
+    int32_t *feat_ndist;       // distinct neighbour communities at the last decision (-1 = unknown)
+    int32_t *last_move;        // iteration of the vertex's last move
+    int32_t *prop_list;        // proposed vertices (bin segments as in order)
+    int features_on;           // 1 = decide kernels write the features above
     DevStats *stats;
 };
+
+// Per-iteration proposal step: features of the active vertices, then either
+// training samples (mode 1) or the proposed lists (mode 2).
+struct ProposalStep {
+    int mode;                  // GALA_PROPOSAL_TRACE or GALA_PROPOSAL_SKIP
+    ProposalView pv;
+    float threshold;
+    int sample_shift;
+    int iteration, level;
+};
+void p1_features_init(Phase1Buffers &b, int n, cudaStream_t st);
+// Features of the active vertices of bins 0-6 (lists / counts of the current
+// active set); mode TRACE appends sampled rows to the sample set, mode SKIP
+// fills prop_list / prop_count with the vertices the network proposes.
+void p1_proposal_step(const LevelGraph &g, Phase1Buffers &b, const ProposalStep &ps, const int32_t *lists,
+                      const int *counts, const int *bin_start, const int *level_cnt, cudaStream_t st);
+// Labels of the samples of the current sweep (moved in this iteration).
+void p1_trace_labels(Phase1Buffers &b, const ProposalStep &ps, cudaStream_t st);
 
 // Hub vertices (largest degree bin): per-hub global tables filled by many
 // CTAs.  Arrays are borrowed from the contraction's long-row buffers, which
@@ -79,7 +118,7 @@ void p1_iter_reset(Phase1Buffers &b, int next, int min_tot_init, cudaStream_t st
 void p1_decide(const LevelGraph &g, Phase1Buffers &b, int bin, const int32_t *list,
                const int *count_ptr, int level_count, double constant, long long m2,
                int fp64_only, int hub_tmax, cudaStream_t st);
-void p1_apply_movers(Phase1Buffers &b, int sign, int n, cudaStream_t st);
+void p1_apply_movers(Phase1Buffers &b, int sign, int n, cudaStream_t st, int iteration = 0);
 void p1_tot_reduce(Phase1Buffers &b, int n, cudaStream_t st);
 void p1_update(const LevelGraph &g, Phase1Buffers &b, int bin, const int32_t *list, int count, int next,
                int bin_start, double constant, long long m2, cudaStream_t st);

@@ -329,7 +329,21 @@ struct DecideArgs {
     double constant;  // 1 / m2
     long long m2;
     int fp64_only;    // 1 = evaluate every vertex with the FP64 expressions
+    float *feat_gain;   // proposal features (null when no proposal mode is on)
+    int32_t *feat_ndist;
 };
+
+// Proposal features of a decided vertex: its best corrected gain
+// (max(X, 0) - (w_cur - Self) m2, normalised by K m2) and the number of
+// distinct neighbour communities (-1 when the schedule does not count them).
+__device__ __forceinline__ void write_features(const DecideArgs &a, int v, long long x, int w_cur, int self_w,
+                                               int ki, int ndist)
+{
+    if (!a.feat_gain) return;
+    const long long y = (x > 0 ? x : 0) - (long long)(w_cur - self_w) * a.m2;
+    a.feat_gain[v] = ki > 0 ? (float)y / ((float)a.m2 * (float)ki) : 0.f;
+    a.feat_ndist[v] = ndist;
+}
 
 // Singleton swap guard (kernel_functions.cu:386): two singletons never move
 // towards the larger id.
@@ -510,6 +524,11 @@ __global__ void __launch_bounds__(256) k_decide_group(DecideArgs a, const int32_
             }
         }
         const bool move = has && sub == 0 && dec == 1 && guard_ok(a, cur, bc);
+        if (a.feat_gain) {
+            const unsigned lb = __ballot_sync(GALA_FULL_MASK, leader);
+            const unsigned gmask = G == 32 ? GALA_FULL_MASK : (((1u << G) - 1u) << (gw * G));
+            if (has && sub == 0) write_features(a, v, x, wc, sf, ki, __popc(lb & gmask));
+        }
         append_mover(a, move, v, cur, bc);
     }
 }
@@ -621,6 +640,12 @@ __global__ void __launch_bounds__(256) k_decide_warp(DecideArgs a, const int32_t
             if (lane == 0) atomicAdd(&a.st->fp64_decisions, 1ull);
         }
         const bool move = lane == 0 && dec == 1 && guard_ok(a, cur, bc);
+        if (a.feat_gain) {
+            int occ = 0;
+            for (int j = lane; j < T; j += 32) occ += keys[j] >= 0;
+            occ = warp_sum(occ);
+            if (lane == 0) write_features(a, v, x, wc, sf, ki, occ);
+        }
         append_mover(a, move, v, cur, bc);
         __syncwarp();
     }
@@ -730,6 +755,7 @@ __global__ void __launch_bounds__(BLOCK) k_decide_cta(DecideArgs a, const int32_
         }
         if (wid == 0) {
             const bool move = lane == 0 && s_dec == 1 && guard_ok(a, cur, s_bc);
+            if (lane == 0) write_features(a, v, x, s_wc, sf, ki, -1);
             append_mover(a, move, v, cur, s_bc);
         }
         __syncthreads();
@@ -759,6 +785,8 @@ void p1_decide(const LevelGraph &g, Phase1Buffers &b, int bin, const int32_t *li
     a.constant = constant;
     a.m2 = m2;
     a.fp64_only = fp64_only;
+    a.feat_gain = b.features_on ? b.feat_gain : nullptr;
+    a.feat_ndist = b.feat_ndist;
     const bool W = g.w != nullptr;
     const int cap = num_sms() * 8;
     auto grid_lanes = [&](int lanes_per_item) {
@@ -830,7 +858,8 @@ void p1_configure_kernels()
 // ------------------------------------------------------------------------
 __global__ void k_apply_movers(const int32_t *__restrict__ mv_v, const int32_t *__restrict__ mv_old,
                                const int32_t *__restrict__ mv_new, const DevStats *__restrict__ stp, int sign,
-                               int32_t *comm, int32_t *Tot, int32_t *size, const int32_t *__restrict__ K)
+                               int32_t *comm, int32_t *Tot, int32_t *size, const int32_t *__restrict__ K,
+                               int32_t *last_move, int iteration)
 {
     const int nm = stp->n_movers;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nm; i += gridDim.x * blockDim.x) {
@@ -839,6 +868,7 @@ __global__ void k_apply_movers(const int32_t *__restrict__ mv_v, const int32_t *
         const int to = sign > 0 ? mv_new[i] : mv_old[i];
         const int k = K[v];
         comm[v] = to;
+        if (last_move && sign > 0) last_move[v] = iteration;
         atomicAdd(&Tot[to], k);
         atomicSub(&Tot[from], k);
         atomicAdd(&size[to], 1);
@@ -846,13 +876,14 @@ __global__ void k_apply_movers(const int32_t *__restrict__ mv_v, const int32_t *
     }
 }
 
-void p1_apply_movers(Phase1Buffers &b, int sign, int n, cudaStream_t st)
+void p1_apply_movers(Phase1Buffers &b, int sign, int n, cudaStream_t st, int iteration)
 {
     int grid = (n + 255) / 256;
     int cap = num_sms() * 4;
     if (grid > cap) grid = cap;
     if (grid < 1) grid = 1;
-    k_apply_movers<<<grid, 256, 0, st>>>(b.mv_v, b.mv_old, b.mv_new, b.stats, sign, b.comm, b.Tot, b.size, b.K);
+    k_apply_movers<<<grid, 256, 0, st>>>(b.mv_v, b.mv_old, b.mv_new, b.stats, sign, b.comm, b.Tot, b.size, b.K,
+                                         b.features_on ? b.last_move : nullptr, iteration);
     note_launch(1);
 }
 
@@ -1289,6 +1320,8 @@ void p1_hub_decide(const LevelGraph &g, Phase1Buffers &b, const HubPlan &p, doub
     a.constant = constant;
     a.m2 = m2;
     a.fp64_only = fp64_only;
+    a.feat_gain = b.features_on ? b.feat_gain : nullptr;
+    a.feat_ndist = b.feat_ndist;
     const int cap = num_sms() * 8;
     cudaMemsetAsync(p.pool, 0xff, (size_t)p.half * sizeof(int32_t), st);
     cudaMemsetAsync(p.pool + p.half, 0, (size_t)p.half * sizeof(int32_t), st);

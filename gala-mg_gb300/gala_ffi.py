@@ -23,7 +23,13 @@ EXPORTS = ["gala_last_error", "gala_status_string", "gala_kernel_launch_count", 
            "gala_graph_info", "gala_graph_arrays", "gala_graph_destroy", "gala_generate_sbm",
            "gala_generate_rmat", "gala_context_create", "gala_context_destroy", "gala_context_set_stream",
            "gala_graph_pin", "gala_louvain", "gala_louvain_device", "gala_phase1_device", "gala_contract_device",
-           "gala_modularity_host", "gala_modularity_device_static"]
+           "gala_modularity_host", "gala_modularity_device_static", "gala_proposal_create",
+           "gala_proposal_destroy", "gala_proposal_get_params", "gala_proposal_set_params", "gala_proposal_samples",
+           "gala_proposal_clear_samples", "gala_proposal_read_samples", "gala_proposal_gradient",
+           "gala_proposal_logits", "gala_proposal_train"]
+
+PROPOSAL_OFF, PROPOSAL_TRACE, PROPOSAL_SKIP = 0, 1, 2
+PROPOSAL_PARAMS = 32 * 8 + 32 + 32 * 32 + 32 + 32 + 1
 
 _i32p = ctypes.POINTER(ctypes.c_int32)
 _i64p = ctypes.POINTER(ctypes.c_int64)
@@ -39,7 +45,9 @@ class GalaError(RuntimeError):
 
 class Options(ctypes.Structure):
     _fields_ = [("min_modularity", ctypes.c_double), ("max_levels", ctypes.c_int32),
-                ("verbose", ctypes.c_int32), ("use_graphs", ctypes.c_int32), ("fp64_gains", ctypes.c_int32)]
+                ("verbose", ctypes.c_int32), ("use_graphs", ctypes.c_int32), ("fp64_gains", ctypes.c_int32),
+                ("proposal_mode", ctypes.c_int32), ("proposal_threshold", ctypes.c_float),
+                ("trace_sample_shift", ctypes.c_int32), ("reserved", ctypes.c_int32), ("proposal", ctypes.c_void_p)]
 
 
 class Result(ctypes.Structure):
@@ -56,7 +64,9 @@ class Result(ctypes.Structure):
                 ("time_d2h_ms", ctypes.c_double), ("decide_sweeps", ctypes.c_int64),
                 ("decide_bytes", ctypes.c_int64), ("update_bytes", ctypes.c_int64),
                 ("kernel_launches", ctypes.c_int64), ("h2d_bytes", ctypes.c_int64),
-                ("d2h_bytes", ctypes.c_int64), ("fp64_decisions", ctypes.c_int64)]
+                ("d2h_bytes", ctypes.c_int64), ("fp64_decisions", ctypes.c_int64),
+                ("decisions", ctypes.c_int64), ("skipped", ctypes.c_int64), ("verify_sweeps", ctypes.c_int32),
+                ("reserved2", ctypes.c_int32), ("samples", ctypes.c_int64)]
 
     def to_dict(self, trace=None):
         L = self.num_levels
@@ -70,7 +80,8 @@ class Result(ctypes.Structure):
              "time_d2h_ms": self.time_d2h_ms, "decide_sweeps": self.decide_sweeps,
              "decide_bytes": self.decide_bytes, "update_bytes": self.update_bytes,
              "kernel_launches": self.kernel_launches, "h2d_bytes": self.h2d_bytes, "d2h_bytes": self.d2h_bytes,
-             "fp64_decisions": self.fp64_decisions}
+             "fp64_decisions": self.fp64_decisions, "decisions": self.decisions, "skipped": self.skipped,
+             "verify_sweeps": self.verify_sweeps, "samples": self.samples}
         if trace is not None:
             d["iter_q"] = trace[:min(self.iter_count, len(trace))].tolist()
         return d
@@ -119,6 +130,23 @@ def load(path=LIB_PATH):
     L.gala_modularity_host.argtypes = [_vp, _i32p, _f64p]
     L.gala_modularity_device_static.argtypes = [ctypes.c_int32, _vp, _vp, _vp, _vp, _f64p]
     L.gala_modularity_device_static.restype = ctypes.c_int
+    _f32p = ctypes.POINTER(ctypes.c_float)
+    L.gala_proposal_create.argtypes = [ctypes.c_int32, ctypes.c_int64, ctypes.c_uint64, ctypes.POINTER(_vp)]
+    L.gala_proposal_destroy.argtypes = [_vp]
+    L.gala_proposal_destroy.restype = None
+    L.gala_proposal_get_params.argtypes = [_vp, _f32p, ctypes.c_int32, _i32p]
+    L.gala_proposal_set_params.argtypes = [_vp, _f32p, ctypes.c_int32]
+    L.gala_proposal_samples.argtypes = [_vp, _i64p, _i64p]
+    L.gala_proposal_clear_samples.argtypes = [_vp]
+    L.gala_proposal_read_samples.argtypes = [_vp, ctypes.c_int64, ctypes.c_int64, _f32p, _f32p]
+    L.gala_proposal_gradient.argtypes = [_vp, _f32p, _f32p, ctypes.c_int32, ctypes.c_float, _f32p, _f32p]
+    L.gala_proposal_logits.argtypes = [_vp, _f32p, ctypes.c_int32, _f32p]
+    L.gala_proposal_train.argtypes = [_vp, ctypes.c_int32, ctypes.c_int32, ctypes.c_float, ctypes.c_float,
+                                      ctypes.c_uint64, _f32p]
+    for name in ["gala_proposal_create", "gala_proposal_get_params", "gala_proposal_set_params",
+                 "gala_proposal_samples", "gala_proposal_clear_samples", "gala_proposal_read_samples",
+                 "gala_proposal_gradient", "gala_proposal_logits", "gala_proposal_train"]:
+        getattr(L, name).restype = ctypes.c_int
     for name in ["gala_graph_load_bin", "gala_graph_store_bin", "gala_graph_from_text", "gala_graph_from_csr",
                  "gala_graph_info", "gala_graph_arrays", "gala_generate_sbm", "gala_generate_rmat",
                  "gala_context_create", "gala_context_set_stream", "gala_graph_pin", "gala_louvain",
@@ -255,8 +283,11 @@ class Context:
         e.g. torch.cuda.Stream().cuda_stream); None = own stream."""
         _check(load().gala_context_set_stream(self.h, stream_handle))
 
-    def louvain(self, graph, min_mod=1e-6, max_levels=0, verbose=False, iter_capacity=4096, fp64_gains=False):
-        """gala_louvain: host graph in, host labels out."""
+    def louvain(self, graph, min_mod=1e-6, max_levels=0, verbose=False, iter_capacity=4096, fp64_gains=False,
+                proposal=None, mode=PROPOSAL_OFF, threshold=0.5, sample_shift=0):
+        """gala_louvain: host graph in, host labels out.  `proposal` (a
+        Proposal) with mode PROPOSAL_TRACE records training samples, with
+        PROPOSAL_SKIP decides only the vertices it proposes."""
         n, _, _ = graph.info()
         labels = np.zeros(n, dtype=np.int32)
         trace = np.zeros(iter_capacity, dtype=np.float64)
@@ -264,7 +295,9 @@ class Context:
         r.iter_modularity = _ptr(trace, _f64p)
         r.iter_capacity = iter_capacity
         o = default_options(min_modularity=min_mod, max_levels=max_levels, verbose=int(verbose),
-                            fp64_gains=int(fp64_gains))
+                            fp64_gains=int(fp64_gains), proposal_mode=int(mode),
+                            proposal_threshold=float(threshold), trace_sample_shift=int(sample_shift),
+                            proposal=proposal.h if proposal is not None else None)
         _check(load().gala_louvain(self.h, graph.h, ctypes.byref(o), _ptr(labels, _i32p), ctypes.byref(r)))
         d = r.to_dict(trace)
         d["labels"] = labels
@@ -296,3 +329,71 @@ class Context:
         _check(load().gala_contract_device(self.h, n, d_offs, d_nbr, d_w or None, d_comm, d_new_offs, d_new_nbr,
                                            d_new_w, ctypes.byref(C), ctypes.byref(E)))
         return C.value, E.value
+
+
+class Proposal:
+    """The learned move-proposal network (gala_proposal_*): an 8 -> 32 -> 32
+    -> 1 MLP with its training-sample buffer on one device."""
+
+    def __init__(self, max_samples=1 << 20, seed=0, device=0):
+        self.h = _vp()
+        _check(load().gala_proposal_create(device, int(max_samples), int(seed), ctypes.byref(self.h)))
+
+    def close(self):
+        if getattr(self, "h", None):
+            load().gala_proposal_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def params(self):
+        p = np.zeros(PROPOSAL_PARAMS, dtype=np.float32)
+        cnt = ctypes.c_int32()
+        _check(load().gala_proposal_get_params(self.h, _ptr(p, ctypes.POINTER(ctypes.c_float)), p.size,
+                                               ctypes.byref(cnt)))
+        return p
+
+    def set_params(self, p):
+        p = np.ascontiguousarray(p, dtype=np.float32)
+        _check(load().gala_proposal_set_params(self.h, _ptr(p, ctypes.POINTER(ctypes.c_float)), p.size))
+
+    def samples(self):
+        c = ctypes.c_int64()
+        pos = ctypes.c_int64()
+        _check(load().gala_proposal_samples(self.h, ctypes.byref(c), ctypes.byref(pos)))
+        return c.value, pos.value
+
+    def clear_samples(self):
+        _check(load().gala_proposal_clear_samples(self.h))
+
+    def read_samples(self, first=0, n=None):
+        if n is None:
+            n = self.samples()[0] - first
+        X = np.zeros((n, 8), dtype=np.float32)
+        Y = np.zeros(n, dtype=np.float32)
+        f = ctypes.POINTER(ctypes.c_float)
+        _check(load().gala_proposal_read_samples(self.h, first, n, _ptr(X, f), _ptr(Y, f)))
+        return X, Y
+
+    def gradient(self, X, Y, pos_weight=1.0):
+        X = np.ascontiguousarray(X, dtype=np.float32)
+        Y = np.ascontiguousarray(Y, dtype=np.float32)
+        g = np.zeros(PROPOSAL_PARAMS, dtype=np.float32)
+        loss = ctypes.c_float()
+        f = ctypes.POINTER(ctypes.c_float)
+        _check(load().gala_proposal_gradient(self.h, _ptr(X, f), _ptr(Y, f), len(Y), pos_weight, _ptr(g, f),
+                                             ctypes.byref(loss)))
+        return g, loss.value
+
+    def logits(self, X):
+        X = np.ascontiguousarray(X, dtype=np.float32)
+        out = np.zeros(len(X), dtype=np.float32)
+        f = ctypes.POINTER(ctypes.c_float)
+        _check(load().gala_proposal_logits(self.h, _ptr(X, f), len(X), _ptr(out, f)))
+        return out
+
+    def train(self, epochs=4, batch_size=4096, lr=3e-3, pos_weight=1.0, seed=0):
+        loss = ctypes.c_float()
+        _check(load().gala_proposal_train(self.h, epochs, batch_size, lr, pos_weight, seed, ctypes.byref(loss)))
+        return loss.value

@@ -45,8 +45,16 @@ typedef struct gala_graph gala_graph;
 /* Device context: one CUDA stream plus all device workspace for graphs of up
  * to a given size.  One context per host thread at a time. */
 typedef struct gala_context gala_context;
+/* Learned move-proposal network (8 features -> 32 -> 32 -> 1 MLP) and its
+ * training samples, on one device.  No counterpart in the reference. */
+typedef struct gala_proposal gala_proposal;
 
 #define GALA_MAX_LEVELS 64
+
+#define GALA_PROPOSAL_OFF 0
+#define GALA_PROPOSAL_TRACE 1  /* plain run; sampled decisions become training samples */
+#define GALA_PROPOSAL_SKIP 2   /* decide only vertices the network expects to move;
+                                  every convergence is confirmed by a plain sweep */
 
 typedef struct {
     double min_modularity; /* stop threshold on the Q gain; reference: 1e-6
@@ -59,6 +67,11 @@ typedef struct {
                               expressions (default 0: exact integer gains,
                               FP64 only where rounding could decide; both give
                               the same partition) */
+    int32_t proposal_mode;      /* GALA_PROPOSAL_* (needs `proposal`) */
+    float proposal_threshold;   /* SKIP: decide vertices with P(move) >= this */
+    int32_t trace_sample_shift; /* TRACE: keep about one decision in 2^shift */
+    int32_t reserved;
+    gala_proposal *proposal;
 } gala_options;
 
 typedef struct {
@@ -92,6 +105,13 @@ typedef struct {
     /* vertex decisions taken with the FP64 gain expressions (the others use
        exact integer gains; see gala_options.fp64_gains) */
     int64_t fp64_decisions;
+    /* proposal modes */
+    int64_t decisions;          /* vertices decided (all sweeps) */
+    int64_t skipped;            /* active vertices the network skipped (SKIP) */
+    int32_t verify_sweeps;      /* plain sweeps run because a proposal sweep
+                                   gained less than min_modularity (SKIP) */
+    int32_t reserved2;
+    int64_t samples;            /* training samples recorded (TRACE) */
 } gala_result;
 
 /* ---- errors / info --------------------------------------------------- */
@@ -198,6 +218,32 @@ gala_status gala_contract_device(gala_context *ctx, int32_t n, const int64_t *d_
                                  int32_t *d_community, int64_t *d_new_offsets,
                                  int32_t *d_new_neighbors, int32_t *d_new_weights,
                                  int32_t *num_communities, int64_t *num_entries);
+
+/* ---- learned move proposal (no counterpart in the reference) ---------- */
+/* Create a network with seeded random weights and room for max_samples
+ * training samples (8 features + label each) on `device`. */
+gala_status gala_proposal_create(int32_t device, int64_t max_samples, uint64_t seed,
+                                 gala_proposal **out);
+void gala_proposal_destroy(gala_proposal *p);
+/* FP32 master weights (count = 1377: W1[32][8], b1, W2[32][32], b2, w3, b3). */
+gala_status gala_proposal_get_params(gala_proposal *p, float *params, int32_t capacity,
+                                     int32_t *count);
+gala_status gala_proposal_set_params(gala_proposal *p, const float *params, int32_t count);
+/* Samples recorded so far by GALA_PROPOSAL_TRACE runs (and how many moved). */
+gala_status gala_proposal_samples(gala_proposal *p, int64_t *count, int64_t *positives);
+gala_status gala_proposal_clear_samples(gala_proposal *p);
+gala_status gala_proposal_read_samples(gala_proposal *p, int64_t first, int64_t n, float *features,
+                                       float *labels);
+/* Weighted BCE loss and its gradient (summed over the n samples, FP32) of
+ * caller samples under the master weights, computed by the GPU backward
+ * kernel; n <= 65536. */
+gala_status gala_proposal_gradient(gala_proposal *p, const float *features, const float *labels,
+                                   int32_t n, float pos_weight, float *grad_out, float *loss_out);
+/* Logits of caller samples with the BF16 inference weights; n <= 65536. */
+gala_status gala_proposal_logits(gala_proposal *p, const float *features, int32_t n, float *logits);
+/* Adam on the GPU over the recorded samples. */
+gala_status gala_proposal_train(gala_proposal *p, int32_t epochs, int32_t batch_size, float lr,
+                                float pos_weight, uint64_t seed, float *final_loss);
 
 /* Host FP64 modularity of a partition of a host graph (the host check the
  * reference keeps at src/louvain_gpu/kernel_functions.cu:1037-1079). */

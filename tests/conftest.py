@@ -32,5 +32,15 @@ def oracle():
 
 
 @pytest.fixture(scope="session")
+def mlp_oracle():
+    """FP64 CPU restatement of the move-proposal network (oracle/mlp_oracle.py)."""
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("mlp_oracle", os.path.join(ROOT, "oracle", "mlp_oracle.py"))
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod
+
+
+@pytest.fixture(scope="session")
 def golden():
     return GOLDEN

@@ -1,0 +1,208 @@
+"""The learned move-proposal network (no counterpart in the reference).
+
+CPU: the FP64 oracle of the network (oracle/mlp_oracle.py) is pinned by
+central finite differences of its own loss.
+GPU: the library's backward kernel (gala_proposal_gradient) and inference
+(gala_proposal_logits, the engine's k_prop_step path) against the oracle;
+trace mode leaves the plain partition unchanged; a network trained on traces
+of the plain method predicts held-out moves far better than the untrained
+one, and the engine run with it skips decisions and ends no more than 0.002
+below the plain modularity, with every convergence judged by a plain sweep.
+"""
+import numpy as np
+import pytest
+
+import proposal_tool
+
+# gradient tolerance: FP32 accumulation over a few thousand samples
+GRAD_RTOL = 2e-3
+# logit tolerance: FP32 FMA chain of 1.3k terms against FP64
+LOGIT_ATOL = 2e-4
+# learned-skip quality bar: the final modularity may fall at most this far
+# below the plain method's (a higher Q passes)
+DQ_MAX = 0.002
+
+
+def _features(rng, n):
+    """Feature rows in the ranges the engine produces."""
+    X = np.empty((n, 8), dtype=np.float32)
+    X[:, 0] = np.log1p(rng.integers(1, 5000, n))
+    X[:, 1] = rng.random(n)
+    X[:, 2] = rng.normal(0, 0.3, n)
+    X[:, 3] = np.log1p(rng.integers(0, 60, n))
+    X[:, 4] = rng.integers(0, 2, n)
+    X[:, 5] = np.log1p(rng.integers(1, 30, n))
+    X[:, 6] = rng.integers(0, 5, n)
+    X[:, 7] = np.log1p(rng.integers(1, 1000, n))
+    return X
+
+
+def _params(rng, mlp_oracle):
+    p = rng.normal(0, 0.3, mlp_oracle.N_PARAMS).astype(np.float32)
+    return p
+
+
+def test_mlp_oracle_gradient_matches_finite_differences(mlp_oracle):
+    rng = np.random.default_rng(5)
+    p = _params(rng, mlp_oracle).astype(np.float64)
+    X = _features(rng, 64).astype(np.float64)
+    Y = (rng.random(64) < 0.3).astype(np.float64)
+    _, g = mlp_oracle.loss_and_grad(p, X, Y, pos_weight=2.5)
+    h = 1e-6
+    for i in list(range(0, mlp_oracle.N_PARAMS, 37)) + [mlp_oracle.N_PARAMS - 1]:
+        e = np.zeros_like(p)
+        e[i] = h
+        lp, _ = mlp_oracle.loss_and_grad(p + e, X, Y, pos_weight=2.5)
+        lm, _ = mlp_oracle.loss_and_grad(p - e, X, Y, pos_weight=2.5)
+        fd = (lp - lm) / (2 * h)
+        assert abs(fd - g[i]) <= 1e-5 * max(1.0, abs(g[i])), (i, fd, g[i])
+
+
+def test_bf16_round_known_values(mlp_oracle):
+    x = np.array([1.0, 1.00390625, 1.005859375, -2.5, 3.140625, 1e-3], dtype=np.float32)
+    r = mlp_oracle.bf16_round(x)
+    # 1 + 2^-8 is a tie -> even (1.0); 1 + 1.5 * 2^-8 rounds up to 1 + 2^-7
+    assert r[0] == 1.0 and r[1] == 1.0 and r[2] == np.float32(1.0078125)
+    assert r[3] == -2.5 and r[4] == np.float32(3.140625)
+    assert abs(r[5] - 1e-3) < 1e-5
+
+
+@pytest.fixture(scope="module")
+def torch_cuda():
+    import torch
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    torch.cuda.init()
+    return torch
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("pos_weight", [1.0, 3.0])
+def test_gpu_gradient_matches_oracle(ffi, mlp_oracle, torch_cuda, pos_weight):
+    rng = np.random.default_rng(11)
+    prop = ffi.Proposal(max_samples=16, seed=3)
+    p = _params(rng, mlp_oracle)
+    prop.set_params(p)
+    X = _features(rng, 3000)
+    Y = (rng.random(3000) < 0.25).astype(np.float32)
+    g, loss = prop.gradient(X, Y, pos_weight)
+    lo, go = mlp_oracle.loss_and_grad(p, X, Y, pos_weight)
+    scale = np.abs(go).max()
+    assert np.all(np.abs(g - go) <= GRAD_RTOL * scale), np.abs(g - go).max() / scale
+    assert abs(loss - lo) <= 1e-4 * abs(lo)
+
+
+@pytest.mark.gpu
+def test_gpu_logits_match_oracle_with_bf16_weights(ffi, mlp_oracle, torch_cuda):
+    rng = np.random.default_rng(12)
+    prop = ffi.Proposal(max_samples=16, seed=4)
+    p = _params(rng, mlp_oracle)
+    prop.set_params(p)
+    X = _features(rng, 5000)
+    got = prop.logits(X)
+    want = mlp_oracle.forward(mlp_oracle.bf16_round(p), X)
+    assert np.all(np.abs(got - want) <= LOGIT_ATOL * np.maximum(1.0, np.abs(want)))
+
+
+@pytest.mark.gpu
+def test_trace_mode_keeps_plain_partition(ffi, torch_cuda):
+    g = ffi.Graph.sbm(1024, 32, 0.3, 0.005, 7)
+    n, e, _ = g.info()
+    ctx = ffi.Context(n, e)
+    plain = ctx.louvain(g)
+    prop = ffi.Proposal(max_samples=1 << 16, seed=1)
+    tr = ctx.louvain(g, proposal=prop, mode=ffi.PROPOSAL_TRACE)
+    assert np.array_equal(plain["labels"], tr["labels"])
+    assert plain["iter_q"] == tr["iter_q"]
+    cnt, pos = prop.samples()
+    assert cnt == tr["samples"] and cnt > 0 and 0 < pos < cnt
+    X, Y = prop.read_samples()
+    assert set(np.unique(Y)) <= {0.0, 1.0}
+    assert np.all(np.isfinite(X))
+    assert np.all((X[:, 1] >= 0) & (X[:, 1] <= 1))
+    assert np.all((X[:, 4] == 0) | (X[:, 4] == 1))
+
+
+@pytest.fixture(scope="module")
+def trained(ffi, torch_cuda):
+    """A network trained on plain traces of eight seeded R-MAT graphs."""
+    prop = ffi.Proposal(max_samples=1 << 22, seed=2)
+    ctx = ffi.Context(1 << 16, 20 << 16)
+    p0 = prop.params()
+    loss, n, pos = proposal_tool.train_on_rmat(prop, range(1000, 1008), [14, 15, 16], sample_shift=0, epochs=8,
+                                               ctx=ctx)
+    return prop, p0, loss, n, pos
+
+
+@pytest.mark.gpu
+def test_training_lowers_loss(ffi, mlp_oracle, trained):
+    prop, p0, loss, n, pos = trained
+    assert n > 10000 and 0 < pos < n
+    X, Y = prop.read_samples(0, min(n, 60000))
+    w = proposal_tool.balance_weight(prop)
+    l0, _ = mlp_oracle.loss_and_grad(p0, X, Y, w)
+    l1, _ = mlp_oracle.loss_and_grad(prop.params(), X, Y, w)
+    assert l1 < 0.8 * l0
+
+
+def _compare(ffi, prop, g, threshold):
+    n, e, _ = g.info()
+    ctx = ffi.Context(n, e)
+    plain = ctx.louvain(g)
+    learned = ctx.louvain(g, proposal=prop, mode=ffi.PROPOSAL_SKIP, threshold=threshold)
+    ctx.close()
+    return plain, learned
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("seed", [101, 102, 103])
+def test_learned_skip_on_held_out_sbm(ffi, mlp_oracle, trained, seed):
+    prop = trained[0]
+    g = ffi.Graph.sbm(1024, 32, 0.3, 0.005, seed)
+    plain, learned = _compare(ffi, prop, g, 0.3)
+    assert learned["modularity"] >= plain["modularity"] - DQ_MAX
+    q = g.modularity(learned["labels"])
+    assert abs(q - learned["modularity"]) <= 1e-9
+
+
+def _auc(scores, labels):
+    """Area under the ROC curve (rank statistic)."""
+    order = np.argsort(scores, kind="stable")
+    ranks = np.empty(len(scores), dtype=np.float64)
+    ranks[order] = np.arange(1, len(scores) + 1)
+    pos = labels > 0.5
+    npos, nneg = pos.sum(), (~pos).sum()
+    return (ranks[pos].sum() - npos * (npos + 1) / 2) / (npos * nneg)
+
+
+@pytest.mark.gpu
+def test_trained_network_predicts_held_out_moves(ffi, trained):
+    """What training gains: on the traces of a held-out graph, the trained
+    network ranks the vertices that move above those that stay far better
+    than the untrained network, and at the engine's threshold it proposes
+    most movers while skipping part of the active set."""
+    prop, p0 = trained[0], trained[1]
+    g = proposal_tool.rmat_graph(16, 2024)
+    n, e, _ = g.info()
+    ctx = ffi.Context(n, e)
+    held = ffi.Proposal(max_samples=1 << 20, seed=9)
+    ctx.louvain(g, proposal=held, mode=ffi.PROPOSAL_TRACE)
+    cnt, pos = held.samples()
+    X, Y = held.read_samples(0, min(cnt, 65536))
+    trained_logits = prop.logits(X)
+    held.set_params(p0)
+    untrained_logits = held.logits(X)
+    auc_t = _auc(trained_logits, Y)
+    auc_u = _auc(untrained_logits, Y)
+    assert auc_t >= 0.75 and auc_t >= auc_u + 0.1, (auc_t, auc_u)
+    proposed = trained_logits >= np.log(0.3 / 0.7)
+    recall = (proposed & (Y > 0.5)).sum() / max(1, (Y > 0.5).sum())
+    assert recall >= 0.8 and proposed.mean() <= 0.8, (recall, proposed.mean())
+    # the engine run with the network: quality bar, skips, and the partition's
+    # modularity equals a host recomputation
+    plain = ctx.louvain(g)
+    learned = ctx.louvain(g, proposal=prop, mode=ffi.PROPOSAL_SKIP, threshold=0.3)
+    ctx.close()
+    assert learned["modularity"] >= plain["modularity"] - DQ_MAX
+    assert learned["skipped"] > 0
+    assert abs(g.modularity(learned["labels"]) - learned["modularity"]) <= 1e-9
