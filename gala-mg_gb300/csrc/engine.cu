@@ -11,6 +11,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <type_traits>
 #include <vector>
 
 #include "common.cuh"
@@ -137,6 +138,36 @@ struct PropRun {
     int level = 0;
 };
 
+// State of a batch of graphs run as one union graph (gala_louvain_batch).
+struct BatchRun {
+    int G = 0;
+    // device arrays
+    int32_t *gid = nullptr, *gid2 = nullptr;  // graph of each vertex (this / next level)
+    long long *m2g = nullptr;
+    double *cg = nullptr;
+    uint8_t *stop = nullptr, *reject = nullptr;
+    int32_t *min_tot = nullptr, *ncomm = nullptr;
+    unsigned long long *sum_in = nullptr, *sum_tot2 = nullptr, *sum_k = nullptr;
+    int64_t *goff = nullptr;  // G+1 vertex offsets of the current level
+    // pinned host mirrors
+    unsigned long long *h_sum_in = nullptr, *h_sum_tot2 = nullptr, *h_sum_k = nullptr;
+    int32_t *h_ncomm = nullptr;
+    uint8_t *h_stop = nullptr, *h_reject = nullptr;
+    int64_t *h_goff = nullptr;
+    // per-graph host state
+    std::vector<long long> m2;
+    std::vector<double> prev_q;  // accepted Q of the current level
+    std::vector<double> prev_mod, cur_mod;  // round rule per graph
+    std::vector<char> finished;  // no further round
+    std::vector<void *> dev, host;
+    GraphSums sums() const { return GraphSums{sum_in, sum_tot2, sum_k, min_tot, ncomm}; }
+    ~BatchRun()
+    {
+        for (void *p : dev) cudaFree(p);
+        for (void *p : host) cudaFreeHost(p);
+    }
+};
+
 // Per-vertex and per-edge algorithmic bytes of a decide-and-move sweep:
 // offsets (2 x 8 B), own label, K, Self, label write (4 B each); per edge the
 // neighbour id, its label and (weighted) the weight.
@@ -155,8 +186,14 @@ long long decide_bytes_for(long long nv, long long ne, bool weighted)
 // plain sweep can end the level, with the reference's rule.  So the
 // partition a level returns has passed a plain sweep that found no further
 // gain of min_mod.
+//
+// With a batch (bt), every graph of the union has its own m2, min Tot, Q and
+// convergence: a graph whose Q did not grow by min_mod gets this iteration's
+// moves reverted and stops, the others go on; the level ends when all graphs
+// have stopped.
 gala_status phase1(gala_context *ctx, const LevelGraph &g, long long &m2, double min_mod, bool verbose,
-                   std::vector<double> *trace, Phase1Out *out, int fp64_only = 0, const PropRun *pr = nullptr)
+                   std::vector<double> *trace, Phase1Out *out, int fp64_only = 0, const PropRun *pr = nullptr,
+                   BatchRun *bt = nullptr)
 {
     const int pmode = pr ? pr->mode : GALA_PROPOSAL_OFF;
     cudaStream_t st = ctx->stream;
@@ -240,6 +277,38 @@ gala_status phase1(gala_context *ctx, const LevelGraph &g, long long &m2, double
     cudaMemsetAsync(b.act_flag, 1, (size_t)g.n, st);
     b.features_on = pmode != GALA_PROPOSAL_OFF;
     if (b.features_on) p1_features_init(b, g.n, st);
+    const int G = bt ? bt->G : 0;
+    if (bt) {
+        // per-graph m2 (first level), singleton Q, graphs that take part
+        batch_graph_sums(kSumIn | kSumTot2 | kSumK, G, bt->goff, nullptr, b, bt->sums(), st);
+        cudaMemcpyAsync(bt->h_sum_in, bt->sum_in, G * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st);
+        cudaMemcpyAsync(bt->h_sum_tot2, bt->sum_tot2, G * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st);
+        cudaMemcpyAsync(bt->h_sum_k, bt->sum_k, G * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st);
+        if ((s = check(cudaStreamSynchronize(st), "batch level sums"))) return s;
+        const bool first = bt->m2.empty();
+        if (first) {
+            bt->m2.resize(G);
+            std::vector<double> c(G);
+            for (int i = 0; i < G; ++i) {
+                bt->m2[i] = (long long)bt->h_sum_k[i];
+                c[i] = bt->m2[i] > 0 ? 1 / (double)bt->m2[i] : 0.0;
+            }
+            cudaMemcpyAsync(bt->m2g, bt->m2.data(), G * sizeof(long long), cudaMemcpyHostToDevice, st);
+            cudaMemcpyAsync(bt->cg, c.data(), G * sizeof(double), cudaMemcpyHostToDevice, st);
+            if ((s = check(cudaStreamSynchronize(st), "batch m2"))) return s;
+        }
+        bt->prev_q.assign(G, 0.0);
+        for (int i = 0; i < G; ++i) {
+            if (!first && (long long)bt->h_sum_k[i] != bt->m2[i]) {
+                set_error("graph %d: level weight %llu differs from total weight %lld", i, bt->h_sum_k[i],
+                          bt->m2[i]);
+                return GALA_ERR_INVALID;
+            }
+            bt->h_stop[i] = bt->finished[i] || bt->m2[i] <= 0;
+            if (bt->m2[i] > 0) bt->prev_q[i] = q_from_sums(bt->h_sum_in[i], bt->h_sum_tot2[i], bt->m2[i]);
+        }
+        cudaMemcpyAsync(bt->stop, bt->h_stop, G, cudaMemcpyHostToDevice, st);
+    }
 
     double q = q_from_sums(h->sum_in, h->sum_tot2, m2);
     if (trace) trace->push_back(q);
@@ -294,7 +363,10 @@ gala_status phase1(gala_context *ctx, const LevelGraph &g, long long &m2, double
         cudaEventRecord(ctx->ev[3], st);
         p1_apply_movers(b, +1, g.n, st, iteration);
         if (pmode == GALA_PROPOSAL_TRACE && iteration > 1) p1_trace_labels(b, ps, st);
-        p1_tot_reduce(b, g.n, st);
+        if (bt)
+            batch_graph_sums(kMinTot | kSumTot2, G, bt->goff, bt->stop, b, bt->sums(), st);
+        else
+            p1_tot_reduce(b, g.n, st);
         cudaEventRecord(ctx->ev[4], st);
         fork(ctx);
         for (int k = 0; k < kNumBins; ++k) {
@@ -303,6 +375,12 @@ gala_status phase1(gala_context *ctx, const LevelGraph &g, long long &m2, double
                       aux_for(ctx, k));
         }
         join(ctx);
+        if (bt) {
+            batch_graph_sums(kSumIn, G, bt->goff, bt->stop, b, bt->sums(), st);
+            cudaMemcpyAsync(bt->h_sum_in, bt->sum_in, G * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st);
+            cudaMemcpyAsync(bt->h_sum_tot2, bt->sum_tot2, G * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+                            st);
+        }
         cudaEventRecord(ctx->ev[5], st);
         if ((s = check(cudaMemcpyAsync(h, b.stats, sizeof(DevStats), cudaMemcpyDeviceToHost, st), "iteration")) ||
             (s = check(cudaStreamSynchronize(st), "iteration")))
@@ -329,6 +407,36 @@ gala_status phase1(gala_context *ctx, const LevelGraph &g, long long &m2, double
         if (verify) out->verify_sweeps += 1;
         act_nv = h->act_vertices[nxt];
         act_ne = (long long)h->act_edges[nxt];
+        if (bt) {
+            // per-graph convergence (louvain_main_process.cu:1004-1007 for
+            // every graph): a graph whose Q did not grow by min_mod drops
+            // this iteration's moves and stops
+            bool running = false, any_reject = false;
+            for (int i = 0; i < G; ++i) {
+                bt->h_reject[i] = 0;
+                if (bt->h_stop[i]) continue;
+                const double qg = q_from_sums(bt->h_sum_in[i], bt->h_sum_tot2[i], bt->m2[i]);
+                if (qg - bt->prev_q[i] < min_mod) {
+                    bt->h_reject[i] = 1;
+                    bt->h_stop[i] = 1;
+                    any_reject = true;
+                } else {
+                    bt->prev_q[i] = qg;
+                    running = true;
+                }
+            }
+            if (any_reject) {
+                cudaMemcpyAsync(bt->reject, bt->h_reject, G, cudaMemcpyHostToDevice, st);
+                cudaMemcpyAsync(bt->stop, bt->h_stop, G, cudaMemcpyHostToDevice, st);
+                batch_revert(b, bt->gid, bt->reject, g.n, st);
+                // the host arrays must stay unchanged until the copies ran
+                if ((s = check(cudaStreamSynchronize(st), "batch revert"))) return s;
+            }
+            if (!running) break;
+            cur = nxt;
+            iteration++;
+            continue;
+        }
         q = q_from_sums(h->sum_in, h->sum_tot2, m2);
         if (trace) trace->push_back(q);
         if (verbose) printf("Iteration:%d Q:%f\n", iteration, q);
@@ -401,8 +509,13 @@ struct RunOut {
 // Multi-round loop of louvain.cu:193-226 on a device graph.  Level 0 reads
 // the caller's arrays; later levels live in the context's ping-pong buffers.
 // ctx->orig receives the final community of every level-0 vertex.
+//
+// With a batch (bt), each graph follows the round rule on its own Q; the loop
+// ends when every graph has finished.  bt->h_goff then holds the community
+// id range of every graph in ctx->orig's numbering and bt->cur_mod the
+// final modularity of every graph.
 gala_status run_levels(gala_context *ctx, int32_t n0, int64_t E0, const int64_t *offs0, const int32_t *nbr0,
-                       const int32_t *w0, const gala_options *opt, gala_result *res)
+                       const int32_t *w0, const gala_options *opt, gala_result *res, BatchRun *bt = nullptr)
 {
     cudaStream_t st = ctx->stream;
     gala_status s;
@@ -457,7 +570,9 @@ gala_status run_levels(gala_context *ctx, int32_t n0, int64_t E0, const int64_t 
         if (verbose) printf("===============round:%d===============\n", round);
         Phase1Out po;
         pr.level = round;
-        if ((s = phase1(ctx, g, m2, min_mod, verbose, &trace, &po, opt ? opt->fp64_gains : 0, &pr))) return s;
+        if ((s = phase1(ctx, g, m2, min_mod, verbose, &trace, &po, opt ? opt->fp64_gains : 0, &pr, bt))) return s;
+        if (bt)  // communities per graph, for the graphs' id ranges at the next level
+            batch_graph_sums(kCountComm, bt->G, bt->goff, nullptr, ctx->p1, bt->sums(), st);
         decisions += po.decisions;
         skipped += po.skipped;
         verify_sweeps += po.verify_sweeps;
@@ -492,6 +607,38 @@ gala_status run_levels(gala_context *ctx, int32_t n0, int64_t E0, const int64_t 
         cur_mod = po.q;
         g = LevelGraph{C, newE, ctx->offs[buf], ctx->nbr[buf], ctx->w[buf]};
         buf ^= 1;
+        if (bt) {
+            const int G = bt->G;
+            if ((s = check(cudaMemcpyAsync(bt->h_ncomm, bt->ncomm, G * sizeof(int32_t), cudaMemcpyDeviceToHost, st),
+                           "batch communities")) ||
+                (s = check(cudaStreamSynchronize(st), "batch communities")))
+                return s;
+            bt->h_goff[0] = 0;
+            bool running = false;
+            for (int i = 0; i < G; ++i) {
+                bt->h_goff[i + 1] = bt->h_goff[i] + bt->h_ncomm[i];
+                if (bt->finished[i]) continue;
+                // louvain.cu:202 per graph
+                bt->prev_mod[i] = bt->cur_mod[i];
+                bt->cur_mod[i] = bt->prev_q[i];
+                if (!(bt->cur_mod[i] - bt->prev_mod[i] >= min_mod)) bt->finished[i] = 1;
+                else running = true;
+            }
+            if (bt->h_goff[G] != C) {
+                set_error("batch: per-graph communities sum to %lld, contraction made %d", (long long)bt->h_goff[G],
+                          C);
+                return GALA_ERR_INVALID;
+            }
+            cudaMemcpyAsync(bt->goff, bt->h_goff, (G + 1) * sizeof(int64_t), cudaMemcpyHostToDevice, st);
+            batch_gid_fill(G, bt->goff, bt->gid2, st);
+            std::swap(bt->gid, bt->gid2);
+            ctx->p1.gid = bt->gid;
+            if ((s = check(cudaStreamSynchronize(st), "batch ranges"))) return s;
+            if (!running) break;
+            if (max_levels > 0 && round >= max_levels) break;
+            if (round >= GALA_MAX_LEVELS) break;
+            continue;
+        }
         // louvain.cu:202: continue while the round gained at least min_mod
         if (!(cur_mod - prev_mod >= min_mod)) break;
         if (max_levels > 0 && round >= max_levels) break;
@@ -781,6 +928,187 @@ gala_status gala_louvain(gala_context *ctx, const gala_graph *g, const gala_opti
     res->kernel_launches = gala_kernel_launch_count() - l0;
     if (own) gala_context_destroy(own);
     return s;
+}
+
+gala_status gala_louvain_batch(gala_context *ctx, const gala_graph *const *graphs, int32_t count,
+                               const gala_options *opt, int32_t *community_out, double *modularity_out,
+                               int32_t *communities_out, gala_batch_result *res)
+{
+    clear_error();
+    if (!graphs || count <= 0 || !community_out) {
+        set_error("gala_louvain_batch: bad arguments");
+        return GALA_ERR_INVALID;
+    }
+    if (opt && opt->proposal_mode != GALA_PROPOSAL_OFF) {
+        set_error("gala_louvain_batch: proposal modes are not available for a batch");
+        return GALA_ERR_INVALID;
+    }
+    long long n_tot = 0, e_tot = 0;
+    bool weighted = false;
+    for (int i = 0; i < count; ++i) {
+        if (!graphs[i] || graphs[i]->n <= 0) {
+            set_error("gala_louvain_batch: graph %d is empty", i);
+            return GALA_ERR_INVALID;
+        }
+        n_tot += graphs[i]->n;
+        e_tot += graphs[i]->entries();
+        weighted = weighted || graphs[i]->weighted;
+    }
+    if (n_tot > 0x7fffffffLL) {
+        set_error("gala_louvain_batch: %lld vertices exceed the int32 id range", n_tot);
+        return GALA_ERR_INVALID;
+    }
+    gala_context *own = nullptr;
+    gala_status s;
+    if (!ctx) {
+        if ((s = gala_context_create(0, (int32_t)n_tot, e_tot, &own))) return s;
+        ctx = own;
+    }
+    struct OwnGuard {
+        gala_context *c;
+        ~OwnGuard()
+        {
+            if (c) gala_context_destroy(c);
+        }
+    } guard{own};
+    if (n_tot > ctx->n_cap || e_tot > ctx->e_cap) {
+        set_error("batch (%lld vertices, %lld entries) exceeds context capacity (%d, %lld)", n_tot, e_tot, ctx->n_cap,
+                  (long long)ctx->e_cap);
+        return GALA_ERR_CAPACITY;
+    }
+    gala_batch_result local{};
+    if (!res) res = &local;
+    memset(res, 0, sizeof(*res));
+    cudaSetDevice(ctx->device);
+    cudaStream_t st = ctx->stream;
+    const int G = count;
+    const int32_t n = (int32_t)n_tot;
+    // union CSR on the host (device layout: leading 0, ids shifted per graph)
+    std::vector<int64_t> offs((size_t)n + 1);
+    std::vector<int32_t> nbr((size_t)e_tot);
+    std::vector<int32_t> w(weighted ? (size_t)e_tot : 0);
+    std::vector<int64_t> vstart((size_t)G + 1);
+    {
+        long long v0 = 0, e0 = 0;
+        offs[0] = 0;
+        for (int i = 0; i < G; ++i) {
+            const gala_graph *gg = graphs[i];
+            vstart[i] = v0;
+            const long long E = gg->entries();
+            for (int v = 0; v < gg->n; ++v) offs[v0 + v + 1] = e0 + gg->offs[v];
+            for (long long j = 0; j < E; ++j) nbr[e0 + j] = (int32_t)(gg->nbr[j] + v0);
+            if (weighted) {
+                if (gg->weighted)
+                    memcpy(w.data() + e0, gg->w.data(), (size_t)E * sizeof(int32_t));
+                else
+                    std::fill(w.begin() + e0, w.begin() + e0 + E, 1);
+            }
+            v0 += gg->n;
+            e0 += E;
+        }
+        vstart[G] = v0;
+    }
+    BatchRun bt;
+    bt.G = G;
+    bool ok = true;
+    auto dal = [&](auto **p, size_t cnt) {
+        void *q = nullptr;
+        if (ok && cudaMalloc(&q, (cnt ? cnt : 1) * sizeof(**p)) == cudaSuccess) {
+            bt.dev.push_back(q);
+            *p = (std::remove_reference_t<decltype(*p)>)q;
+        } else {
+            ok = false;
+        }
+    };
+    auto hal = [&](auto **p, size_t cnt) {
+        void *q = nullptr;
+        if (ok && cudaMallocHost(&q, (cnt ? cnt : 1) * sizeof(**p)) == cudaSuccess) {
+            bt.host.push_back(q);
+            *p = (std::remove_reference_t<decltype(*p)>)q;
+        } else {
+            ok = false;
+        }
+    };
+    dal(&bt.gid, n);
+    dal(&bt.gid2, n);
+    dal(&bt.m2g, G);
+    dal(&bt.cg, G);
+    dal(&bt.stop, G);
+    dal(&bt.reject, G);
+    dal(&bt.min_tot, G);
+    dal(&bt.ncomm, G);
+    dal(&bt.sum_in, G);
+    dal(&bt.sum_tot2, G);
+    dal(&bt.sum_k, G);
+    dal(&bt.goff, (size_t)G + 1);
+    hal(&bt.h_sum_in, G);
+    hal(&bt.h_sum_tot2, G);
+    hal(&bt.h_sum_k, G);
+    hal(&bt.h_ncomm, G);
+    hal(&bt.h_stop, G);
+    hal(&bt.h_reject, G);
+    hal(&bt.h_goff, (size_t)G + 1);
+    if (!ok) {
+        cudaGetLastError();
+        set_error("gala_louvain_batch: allocation of the per-graph state failed (%d graphs)", G);
+        return GALA_ERR_OOM;
+    }
+    bt.finished.assign(G, 0);
+    bt.prev_mod.assign(G, -1.0);
+    bt.cur_mod.assign(G, -1.0);
+    memcpy(bt.h_goff, vstart.data(), ((size_t)G + 1) * sizeof(int64_t));
+    long long l0 = gala_kernel_launch_count();
+    cudaEventRecord(ctx->ev[6], st);
+    cudaMemcpyAsync(ctx->offs[1], offs.data(), ((size_t)n + 1) * sizeof(int64_t), cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(ctx->nbr[1], nbr.data(), (size_t)e_tot * sizeof(int32_t), cudaMemcpyHostToDevice, st);
+    const int32_t *dw = nullptr;
+    if (weighted) {
+        cudaMemcpyAsync(ctx->w[1], w.data(), (size_t)e_tot * sizeof(int32_t), cudaMemcpyHostToDevice, st);
+        dw = ctx->w[1];
+    }
+    cudaMemcpyAsync(bt.goff, bt.h_goff, ((size_t)G + 1) * sizeof(int64_t), cudaMemcpyHostToDevice, st);
+    cudaEventRecord(ctx->ev[7], st);
+    batch_gid_fill(G, bt.goff, bt.gid, st);
+    if ((s = check(cudaStreamSynchronize(st), "batch host to device copy"))) return s;
+    res->time_h2d_ms = ev_ms(ctx->ev[6], ctx->ev[7]);
+    Phase1Buffers &b = ctx->p1;
+    b.gid = bt.gid;
+    b.m2g = bt.m2g;
+    b.cg = bt.cg;
+    b.gstop = bt.stop;
+    b.min_tot_g = bt.min_tot;
+    gala_result r{};
+    s = run_levels(ctx, n, e_tot, ctx->offs[1], ctx->nbr[1], dw, opt, &r, &bt);
+    b.gid = nullptr;
+    b.m2g = nullptr;
+    b.cg = nullptr;
+    b.gstop = nullptr;
+    b.min_tot_g = nullptr;
+    if (s) return s;
+    cudaEventRecord(ctx->ev[6], st);
+    cudaMemcpyAsync(community_out, ctx->orig, (size_t)n * sizeof(int32_t), cudaMemcpyDeviceToHost, st);
+    cudaEventRecord(ctx->ev[7], st);
+    if ((s = check(cudaStreamSynchronize(st), "batch device to host copy"))) return s;
+    res->time_d2h_ms = ev_ms(ctx->ev[6], ctx->ev[7]);
+    // union community ids -> ids local to each graph
+    for (int i = 0; i < G; ++i) {
+        const int32_t base = (int32_t)bt.h_goff[i];
+        for (long long v = vstart[i]; v < vstart[i + 1]; ++v) community_out[v] -= base;
+        if (modularity_out) modularity_out[i] = bt.m2[i] > 0 ? bt.cur_mod[i] : 0.0;
+        if (communities_out) communities_out[i] = (int32_t)(bt.h_goff[i + 1] - bt.h_goff[i]);
+    }
+    res->num_graphs = G;
+    res->num_levels = r.num_levels;
+    res->total_iterations = r.total_iterations;
+    res->vertices = n;
+    res->entries = e_tot;
+    res->time_total_ms = r.time_total_ms;
+    res->time_phase1_ms = r.time_phase1_ms;
+    res->time_contract_ms = r.time_contract_ms;
+    res->h2d_bytes = ((long long)n + 1) * 8 + e_tot * 4 * (weighted ? 2 : 1) + ((long long)G + 1) * 8;
+    res->d2h_bytes = (long long)n * 4;
+    res->kernel_launches = gala_kernel_launch_count() - l0;
+    return GALA_OK;
 }
 
 gala_status gala_phase1_device(gala_context *ctx, int32_t n, const int64_t *d_offsets, const int32_t *d_neighbors,

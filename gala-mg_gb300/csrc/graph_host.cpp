@@ -547,6 +547,70 @@ gala_status gala_generate_sbm(int32_t n, int32_t k, double p_in, double p_out, u
     return GALA_OK;
 }
 
+gala_status gala_generate_sbm_batch(int32_t count, int32_t n_min, int32_t n_max, int32_t k_min, int32_t k_max,
+                                    double deg_min, double deg_max, double mix_min, double mix_max, uint64_t seed,
+                                    int32_t nthreads, gala_graph **out)
+{
+    clear_error();
+    if (!out || count <= 0 || n_min < 4 || n_max < n_min || k_min < 1 || k_max < k_min || deg_min <= 0 ||
+        deg_max < deg_min || mix_min < 0 || mix_max > 1 || mix_max < mix_min) {
+        set_error("gala_generate_sbm_batch: bad arguments");
+        return GALA_ERR_INVALID;
+    }
+    for (int i = 0; i < count; ++i) out[i] = nullptr;
+    // parameters drawn serially (graph i depends only on seed and i)
+    struct P {
+        int32_t n, k;
+        double pin, pout;
+        uint64_t seed;
+    };
+    std::vector<P> ps((size_t)count);
+    uint64_t s = seed * 0x9E3779B97F4A7C15ULL + 0x632BE59BD9B4E019ULL;
+    const double l0 = std::log((double)n_min), l1 = std::log((double)n_max);
+    for (int i = 0; i < count; ++i) {
+        P &p = ps[i];
+        p.n = (int32_t)std::llround(std::exp(l0 + (l1 - l0) * u01(s)));
+        p.n = std::max(n_min, std::min(n_max, p.n));
+        int32_t k = k_min + (int32_t)std::floor((k_max - k_min + 1) * u01(s));
+        k = std::min(k, k_max);
+        const double d = deg_min + (deg_max - deg_min) * u01(s);
+        const double mu = mix_min + (mix_max - mix_min) * u01(s);
+        // blocks large enough to hold the intra-block degree
+        const int32_t kmax_fit = std::max(1, (int32_t)(p.n / (d * (1 - mu) + 2)));
+        p.k = std::max(1, std::min(k, kmax_fit));
+        const double bs = (double)p.n / p.k;
+        p.pin = std::min(1.0, d * (1 - mu) / std::max(1.0, bs - 1));
+        p.pout = p.k > 1 ? std::min(1.0, d * mu / std::max(1.0, p.n - bs)) : 0.0;
+        p.seed = seed * 1000003ULL + (uint64_t)i;
+    }
+    std::atomic<int> failed{-1};
+    const int nt = hw_threads(nthreads);
+    std::vector<std::thread> th;
+    std::atomic<int> next{0};
+    for (int t = 0; t < std::min(nt, count); ++t)
+        th.emplace_back([&] {
+            for (int i = next++; i < count; i = next++) {
+                gala_graph *g = nullptr;
+                if (gala_generate_sbm(ps[i].n, ps[i].k, ps[i].pin, ps[i].pout, ps[i].seed, &g) != GALA_OK) {
+                    failed = i;
+                    continue;
+                }
+                out[i] = g;
+            }
+        });
+    for (auto &x : th) x.join();
+    if (failed >= 0) {
+        const int i = failed;
+        for (int j = 0; j < count; ++j) {
+            gala_graph_destroy(out[j]);
+            out[j] = nullptr;
+        }
+        set_error("gala_generate_sbm_batch: graph %d (n %d, k %d) drew no edges", i, ps[i].n, ps[i].k);
+        return GALA_ERR_INVALID;
+    }
+    return GALA_OK;
+}
+
 gala_status gala_generate_rmat(int32_t scale, int64_t nedges, double a, double b, double c, double noise,
                                int32_t keep_isolated, uint64_t seed, int32_t nthreads, gala_graph **out)
 {

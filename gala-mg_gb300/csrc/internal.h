@@ -74,6 +74,13 @@ struct Phase1Buffers {
     int32_t *last_move;        // iteration of the vertex's last move
     int32_t *prop_list;        // proposed vertices (bin segments as in order)
     int features_on;           // 1 = decide kernels write the features above
+    // batched graphs (all null for one graph): graph of each vertex, the
+    // graph's m2 and 1/m2, stopped graphs, per-graph min Tot
+    const int32_t *gid;
+    const long long *m2g;
+    const double *cg;
+    const uint8_t *gstop;
+    const int32_t *min_tot_g;
     DevStats *stats;
 };
 
@@ -131,6 +138,17 @@ void p1_hub_plan_launch(const LevelGraph &g, Phase1Buffers &b, HubPlan &p, cudaS
 void p1_hub_work_launch(HubPlan &p, cudaStream_t st);
 void p1_hub_decide(const LevelGraph &g, Phase1Buffers &b, const HubPlan &p, double constant, long long m2,
                    int fp64_only, cudaStream_t st);
+
+// ---- batched graphs (batch.cu) ----
+constexpr int kSumIn = 1, kSumTot2 = 2, kMinTot = 4, kSumK = 8, kCountComm = 16;
+struct GraphSums {  // per-graph outputs (device arrays of G entries)
+    unsigned long long *sum_in, *sum_tot2, *sum_k;
+    int32_t *min_tot, *ncomm;
+};
+void batch_graph_sums(int what, int G, const int64_t *goff, const uint8_t *stop, const Phase1Buffers &b,
+                      const GraphSums &out, cudaStream_t st);
+void batch_revert(Phase1Buffers &b, const int32_t *gid, const uint8_t *reject, int n, cudaStream_t st);
+void batch_gid_fill(int G, const int64_t *goff, int32_t *gid, cudaStream_t st);
 
 // ---- contraction (contract.cu) ----
 struct ContractBuffers {

@@ -331,17 +331,39 @@ struct DecideArgs {
     int fp64_only;    // 1 = evaluate every vertex with the FP64 expressions
     float *feat_gain;   // proposal features (null when no proposal mode is on)
     int32_t *feat_ndist;
+    // batched graphs (null for one graph): graph of each vertex, its total
+    // weight m2 and 1/m2, and the graphs whose phase 1 has stopped
+    const int32_t *__restrict__ gid;
+    const long long *__restrict__ m2g;
+    const double *__restrict__ cg;
+    const uint8_t *__restrict__ stop;
 };
+
+// Gain scale of a vertex: m2 and 1/m2 of its graph.
+struct Scale {
+    long long m2;
+    double c;
+};
+__device__ __forceinline__ Scale scale_of(const DecideArgs &a, int v)
+{
+    if (a.gid) {
+        const int g = a.gid[v];
+        return Scale{a.m2g[g], a.cg[g]};
+    }
+    return Scale{a.m2, a.constant};
+}
+// Vertex of a batched graph whose phase 1 has stopped: not decided.
+__device__ __forceinline__ bool stopped(const DecideArgs &a, int v) { return a.stop && a.stop[a.gid[v]]; }
 
 // Proposal features of a decided vertex: its best corrected gain
 // (max(X, 0) - (w_cur - Self) m2, normalised by K m2) and the number of
 // distinct neighbour communities (-1 when the schedule does not count them).
-__device__ __forceinline__ void write_features(const DecideArgs &a, int v, long long x, int w_cur, int self_w,
-                                               int ki, int ndist)
+__device__ __forceinline__ void write_features(const DecideArgs &a, const Scale &sc, int v, long long x, int w_cur,
+                                               int self_w, int ki, int ndist)
 {
     if (!a.feat_gain) return;
-    const long long y = (x > 0 ? x : 0) - (long long)(w_cur - self_w) * a.m2;
-    a.feat_gain[v] = ki > 0 ? (float)y / ((float)a.m2 * (float)ki) : 0.f;
+    const long long y = (x > 0 ? x : 0) - (long long)(w_cur - self_w) * sc.m2;
+    a.feat_gain[v] = ki > 0 ? (float)y / ((float)sc.m2 * (float)ki) : 0.f;
     a.feat_ndist[v] = ndist;
 }
 
@@ -401,14 +423,14 @@ __device__ __forceinline__ void cand_merge(long long &x, int &c, int &w, int &t,
 }
 
 // 0 = stay, 1 = move (before the singleton guard), 2 = evaluate in FP64.
-__device__ __forceinline__ int int_decision(const DecideArgs &a, long long x, int t, int cur, int best, int w_cur,
-                                            int self_w, int ki)
+__device__ __forceinline__ int int_decision(const DecideArgs &a, const Scale &sc, long long x, int t, int cur,
+                                            int best, int w_cur, int self_w, int ki)
 {
-    if (a.fp64_only || (long long)ki * a.m2 >= (1LL << 49)) return 2;
+    if (a.fp64_only || (long long)ki * sc.m2 >= (1LL << 49)) return 2;
     if (best == cur) return 0;  // every candidate has X < 0: every FP64 gain is < 0
     if (x == 0) return w_cur == self_w ? 2 : 0;
     if (t) return 2;
-    const long long y = x - (long long)(w_cur - self_w) * a.m2;
+    const long long y = x - (long long)(w_cur - self_w) * sc.m2;
     if (y == 0) return 2;
     return y > 0 ? 1 : 0;
 }
@@ -457,11 +479,16 @@ __global__ void __launch_bounds__(256) k_decide_group(DecideArgs a, const int32_
     const int nw = (gridDim.x * blockDim.x) >> 5;
     for (int base = wg * GPW; base < count; base += nw * GPW) {
         const int idx = base + gw;
-        const bool has = idx < count;
+        bool has = idx < count;
         int v = 0, cur = -1, deg = 0, ki = 0, sf = 0, tcur = 0;
         long long s = 0;
+        Scale sc{a.m2, a.constant};
         if (has) {
             v = list[idx];
+            has = !stopped(a, v);
+        }
+        if (has) {
+            sc = scale_of(a, v);
             s = a.offs[v];
             deg = (int)(a.offs[v + 1] - s);
             cur = a.comm[v];
@@ -486,7 +513,7 @@ __global__ void __launch_bounds__(256) k_decide_group(DecideArgs a, const int32_
         int bc = cur, bw = 0, bt = 0;
         if (leader && c != cur) {
             tc = a.Tot[c];
-            const long long xx = gain_x(wsum, ki, tc, tcur, a.m2);
+            const long long xx = gain_x(wsum, ki, tc, tcur, sc.m2);
             if (xx >= 0) {
                 x = xx;
                 bc = c;
@@ -495,14 +522,14 @@ __global__ void __launch_bounds__(256) k_decide_group(DecideArgs a, const int32_
         }
         warp_merge_int(x, bc, bw, bt, wc, G);
         int dec = 0;
-        if (has && sub == 0) dec = int_decision(a, x, bt, cur, bc, wc, sf, ki);
+        if (has && sub == 0) dec = int_decision(a, sc, x, bt, cur, bc, wc, sf, ki);
         const bool fp = dec == 2;
         if (__any_sync(GALA_FULL_MASK, fp)) {
             // the reference's FP64 evaluation of the same candidates
             double dq = 0.0;
             int fc = cur;
             if (leader && c != cur) {
-                const double d = gain_dq(wsum, ki, tc, tcur, a.constant);
+                const double d = gain_dq(wsum, ki, tc, tcur, sc.c);
                 if (d > 0.0) {
                     dq = d;
                     fc = c;
@@ -527,7 +554,7 @@ __global__ void __launch_bounds__(256) k_decide_group(DecideArgs a, const int32_
         if (a.feat_gain) {
             const unsigned lb = __ballot_sync(GALA_FULL_MASK, leader);
             const unsigned gmask = G == 32 ? GALA_FULL_MASK : (((1u << G) - 1u) << (gw * G));
-            if (has && sub == 0) write_features(a, v, x, wc, sf, ki, __popc(lb & gmask));
+            if (has && sub == 0) write_features(a, sc, v, x, wc, sf, ki, __popc(lb & gmask));
         }
         append_mover(a, move, v, cur, bc);
     }
@@ -535,9 +562,9 @@ __global__ void __launch_bounds__(256) k_decide_group(DecideArgs a, const int32_
 
 // Scan a hash table: this thread's best candidate by exact X and its share of
 // the weight to the own community.
-__device__ __forceinline__ void scan_table_int(const DecideArgs &a, const int *keys, const int *vals, int T,
-                                               int first, int stride, int cur, int ki, int tcur, long long &x,
-                                               int &bc, int &bw, int &bt, int &wc)
+__device__ __forceinline__ void scan_table_int(const DecideArgs &a, const Scale &sc, const int *keys,
+                                               const int *vals, int T, int first, int stride, int cur, int ki,
+                                               int tcur, long long &x, int &bc, int &bw, int &bt, int &wc)
 {
     for (int j = first; j < T; j += stride) {
         const int c = keys[j];
@@ -546,7 +573,7 @@ __device__ __forceinline__ void scan_table_int(const DecideArgs &a, const int *k
         if (c == cur) {
             wc += wv;
         } else {
-            const long long xx = gain_x(wv, ki, a.Tot[c], tcur, a.m2);
+            const long long xx = gain_x(wv, ki, a.Tot[c], tcur, sc.m2);
             if (xx >= 0) cand_merge(x, bc, bw, bt, xx, c, wv, 0);
         }
     }
@@ -554,14 +581,14 @@ __device__ __forceinline__ void scan_table_int(const DecideArgs &a, const int *k
 
 // The same scan with the reference's FP64 gains (vertices int_decision
 // cannot settle).
-__device__ __forceinline__ void scan_table(const DecideArgs &a, const int *keys, const int *vals, int T,
-                                           int first, int stride, int cur, int ki, int tcur, double &dq,
+__device__ __forceinline__ void scan_table(const DecideArgs &a, const Scale &sc, const int *keys, const int *vals,
+                                           int T, int first, int stride, int cur, int ki, int tcur, double &dq,
                                            int &bc)
 {
     for (int j = first; j < T; j += stride) {
         int c = keys[j];
         if (c < 0 || c == cur) continue;
-        double d = gain_dq(vals[j], ki, a.Tot[c], tcur, a.constant);
+        double d = gain_dq(vals[j], ki, a.Tot[c], tcur, sc.c);
         if (d > 0.0 && cand_better(d, c, dq, bc)) {
             dq = d;
             bc = c;
@@ -598,6 +625,8 @@ __global__ void __launch_bounds__(256) k_decide_warp(DecideArgs a, const int32_t
     const int nw = (gridDim.x * blockDim.x) >> 5;
     for (int i = wg; i < count; i += nw) {
         const int v = list[i];
+        if (stopped(a, v)) continue;
+        const Scale sc = scale_of(a, v);
         const long long s = a.offs[v];
         const int deg = (int)(a.offs[v + 1] - s);
         const int cur = a.comm[v];
@@ -627,13 +656,13 @@ __global__ void __launch_bounds__(256) k_decide_warp(DecideArgs a, const int32_t
         const int ki = a.K[v], tcur = a.Tot[cur], sf = a.Self[v];
         long long x = -1;
         int bc = cur, bw = 0, bt = 0, wc = 0;
-        scan_table_int(a, keys, vals, T, lane, 32, cur, ki, tcur, x, bc, bw, bt, wc);
+        scan_table_int(a, sc, keys, vals, T, lane, 32, cur, ki, tcur, x, bc, bw, bt, wc);
         warp_merge_int(x, bc, bw, bt, wc, 32);
-        int dec = int_decision(a, x, bt, cur, bc, wc, sf, ki);  // warp-uniform
+        int dec = int_decision(a, sc, x, bt, cur, bc, wc, sf, ki);  // warp-uniform
         if (dec == 2) {
             double dq = 0.0;
             int fc = cur;
-            scan_table(a, keys, vals, T, lane, 32, cur, ki, tcur, dq, fc);
+            scan_table(a, sc, keys, vals, T, lane, 32, cur, ki, tcur, dq, fc);
             warp_argmax(dq, fc);
             bc = fc;
             dec = (fc != cur && gain_correct(dq, wc, sf) > 0.0) ? 1 : 0;
@@ -644,7 +673,7 @@ __global__ void __launch_bounds__(256) k_decide_warp(DecideArgs a, const int32_t
             int occ = 0;
             for (int j = lane; j < T; j += 32) occ += keys[j] >= 0;
             occ = warp_sum(occ);
-            if (lane == 0) write_features(a, v, x, wc, sf, ki, occ);
+            if (lane == 0) write_features(a, sc, v, x, wc, sf, ki, occ);
         }
         append_mover(a, move, v, cur, bc);
         __syncwarp();
@@ -673,6 +702,8 @@ __global__ void __launch_bounds__(BLOCK) k_decide_cta(DecideArgs a, const int32_
     const int count = *count_ptr;
     for (int i = blockIdx.x; i < count; i += gridDim.x) {
         const int v = list[i];
+        if (stopped(a, v)) continue;
+        const Scale sc = scale_of(a, v);
         const long long s = a.offs[v];
         const long long e = a.offs[v + 1];
         const int deg = (int)(e - s);
@@ -707,7 +738,7 @@ __global__ void __launch_bounds__(BLOCK) k_decide_cta(DecideArgs a, const int32_
         constexpr int NW = BLOCK / 32;
         long long x = -1;
         int bc = cur, bw = 0, bt = 0, wc = 0;
-        scan_table_int(a, keys, vals, T, threadIdx.x, BLOCK, cur, ki, tcur, x, bc, bw, bt, wc);
+        scan_table_int(a, sc, keys, vals, T, threadIdx.x, BLOCK, cur, ki, tcur, x, bc, bw, bt, wc);
         warp_merge_int(x, bc, bw, bt, wc, 32);
         if (lane == 0) {
             r_x[wid] = x;
@@ -725,7 +756,7 @@ __global__ void __launch_bounds__(BLOCK) k_decide_cta(DecideArgs a, const int32_
             wc = lane < NW ? r_wc[lane] : 0;
             warp_merge_int(x, bc, bw, bt, wc, 32);
             if (lane == 0) {
-                s_dec = int_decision(a, x, bt, cur, bc, wc, sf, ki);
+                s_dec = int_decision(a, sc, x, bt, cur, bc, wc, sf, ki);
                 s_bc = bc;
                 s_wc = wc;
             }
@@ -734,7 +765,7 @@ __global__ void __launch_bounds__(BLOCK) k_decide_cta(DecideArgs a, const int32_
         if (s_dec == 2) {  // block-uniform: the reference's FP64 evaluation
             double dq = 0.0;
             int fc = cur;
-            scan_table(a, keys, vals, T, threadIdx.x, BLOCK, cur, ki, tcur, dq, fc);
+            scan_table(a, sc, keys, vals, T, threadIdx.x, BLOCK, cur, ki, tcur, dq, fc);
             warp_argmax(dq, fc);
             if (lane == 0) {
                 r_dq[wid] = dq;
@@ -755,7 +786,7 @@ __global__ void __launch_bounds__(BLOCK) k_decide_cta(DecideArgs a, const int32_
         }
         if (wid == 0) {
             const bool move = lane == 0 && s_dec == 1 && guard_ok(a, cur, s_bc);
-            if (lane == 0) write_features(a, v, x, s_wc, sf, ki, -1);
+            if (lane == 0) write_features(a, sc, v, x, s_wc, sf, ki, -1);
             append_mover(a, move, v, cur, s_bc);
         }
         __syncthreads();
@@ -787,6 +818,10 @@ void p1_decide(const LevelGraph &g, Phase1Buffers &b, int bin, const int32_t *li
     a.fp64_only = fp64_only;
     a.feat_gain = b.features_on ? b.feat_gain : nullptr;
     a.feat_ndist = b.feat_ndist;
+    a.gid = b.gid;
+    a.m2g = b.m2g;
+    a.cg = b.cg;
+    a.stop = b.gstop;
     const bool W = g.w != nullptr;
     const int cap = num_sms() * 8;
     auto grid_lanes = [&](int lanes_per_item) {
@@ -953,7 +988,30 @@ struct UpdateArgs {
     double constant;
     long long m2;
     int next;
+    // batched graphs (null for one graph)
+    const int32_t *__restrict__ gid;
+    const long long *__restrict__ m2g;
+    const double *__restrict__ cg;
+    const uint8_t *__restrict__ stop;
+    const int32_t *__restrict__ min_tot_g;
 };
+
+// Per-vertex prune parameters: the graph's m2, 1/m2 and min Tot; `stop` when
+// the vertex's graph has stopped (no update, never active).
+struct PruneScale {
+    long long m2;
+    double c;
+    int min_tot;
+    bool stop;
+};
+__device__ __forceinline__ PruneScale prune_scale(const UpdateArgs &a, int v, int min_tot)
+{
+    if (a.gid) {
+        const int g = a.gid[v];
+        return PruneScale{a.m2g[g], a.cg[g], a.min_tot_g[g], a.stop[g] != 0};
+    }
+    return PruneScale{a.m2, a.constant, min_tot, false};
+}
 
 template <int G, bool W>
 __global__ void __launch_bounds__(256) k_update_group(UpdateArgs a, const int32_t *__restrict__ list, int count)
@@ -967,11 +1025,16 @@ __global__ void __launch_bounds__(256) k_update_group(UpdateArgs a, const int32_
     int s_act = 0;
     for (int base = wg * GPW; base < count; base += nw * GPW) {
         const int idx = base + gw;
-        const bool has = idx < count;
+        bool has = idx < count;
         int v = 0, cur = -1;
         long long s = 0, e = 0;
+        PruneScale ps{a.m2, a.constant, min_tot, false};
         if (has) {
             v = list[idx];
+            ps = prune_scale(a, v, min_tot);
+            if (ps.stop) has = false;
+        }
+        if (has) {
             s = a.offs[v];
             e = a.offs[v + 1];
             cur = a.comm[v];
@@ -982,10 +1045,11 @@ __global__ void __launch_bounds__(256) k_update_group(UpdateArgs a, const int32_
 #pragma unroll
         for (int o = G / 2; o >= 1; o >>= 1) sum += __shfl_xor_sync(GALA_FULL_MASK, sum, o);
         bool active = false;
+        if (ps.stop && sub == 0) a.act_flag[v] = 0;
         if (has && sub == 0) {
             a.In[v] = sum;
             const int ki = a.K[v];
-            active = !prune_bound_fast(sum, a.Self[v], ki, min_tot, a.Tot[cur], a.constant, a.m2);
+            active = !prune_bound_fast(sum, a.Self[v], ki, ps.min_tot, a.Tot[cur], ps.c, ps.m2);
             a.act_flag[v] = active;
             s_in += (unsigned long long)sum;
             if (active) {
@@ -1009,6 +1073,11 @@ __global__ void __launch_bounds__(256) k_update_cta(UpdateArgs a, const int32_t 
     int s_act = 0;
     for (int i = blockIdx.x; i < count; i += gridDim.x) {
         const int v = list[i];
+        const PruneScale ps = prune_scale(a, v, min_tot);
+        if (ps.stop) {  // block-uniform
+            if (threadIdx.x == 0) a.act_flag[v] = 0;
+            continue;
+        }
         const long long s = a.offs[v], e = a.offs[v + 1];
         const int cur = a.comm[v];
         int sum = 0;
@@ -1022,7 +1091,7 @@ __global__ void __launch_bounds__(256) k_update_cta(UpdateArgs a, const int32_t 
             for (int q = 0; q < (int)(blockDim.x >> 5); ++q) sum += red[q];
             a.In[v] = sum;
             const int ki = a.K[v];
-            bool active = !prune_bound_fast(sum, a.Self[v], ki, min_tot, a.Tot[cur], a.constant, a.m2);
+            bool active = !prune_bound_fast(sum, a.Self[v], ki, ps.min_tot, a.Tot[cur], ps.c, ps.m2);
             a.act_flag[v] = active;
             s_in += (unsigned long long)sum;
             if (active) {
@@ -1058,6 +1127,11 @@ void p1_update(const LevelGraph &g, Phase1Buffers &b, int bin, const int32_t *li
     a.constant = constant;
     a.m2 = m2;
     a.next = next;
+    a.gid = b.gid;
+    a.m2g = b.m2g;
+    a.cg = b.cg;
+    a.stop = b.gstop;
+    a.min_tot_g = b.min_tot_g;
     const bool W = g.w != nullptr;
     const int cap = num_sms() * 8;
     auto grid_lanes = [&](int G) {
@@ -1138,7 +1212,7 @@ __global__ void __launch_bounds__(256) k_hub_insert(DecideArgs a, HubPlan p, con
     for (long long wi = blockIdx.x; wi < p.nwork; wi += gridDim.x) {
         const int i = p.work[wi];
         const int v = p.hubs[i];
-        if (!flag[v]) continue;
+        if (!flag[v] || stopped(a, v)) continue;
         const long long e = a.offs[v + 1];
         const long long s = a.offs[v] + (wi - p.coff[i]) * kHubChunk;
         const long long e2 = s + kHubChunk < e ? s + kHubChunk : e;
@@ -1164,9 +1238,9 @@ __global__ void __launch_bounds__(256) k_hub_insert(DecideArgs a, HubPlan p, con
 
 // FP64 evaluation needed whatever the candidates: K*m2 out of the range where
 // the integer order equals the FP64 order (or FP64 forced).
-__device__ __forceinline__ bool needs_fp64(const DecideArgs &a, int ki)
+__device__ __forceinline__ bool needs_fp64(const DecideArgs &a, const Scale &sc, int ki)
 {
-    return a.fp64_only || (long long)ki * a.m2 >= (1LL << 49);
+    return a.fp64_only || (long long)ki * sc.m2 >= (1LL << 49);
 }
 
 __global__ void __launch_bounds__(256) k_hub_scan(DecideArgs a, HubPlan p, const uint8_t *__restrict__ flag)
@@ -1178,7 +1252,8 @@ __global__ void __launch_bounds__(256) k_hub_scan(DecideArgs a, HubPlan p, const
     for (long long wi = blockIdx.x; wi < p.ntwork; wi += gridDim.x) {
         const int i = p.twork[wi];
         const int v = p.hubs[i];
-        if (!flag[v]) continue;
+        if (!flag[v] || stopped(a, v)) continue;
+        const Scale sc = scale_of(a, v);
         const int cur = a.comm[v], ki = a.K[v], tcur = a.Tot[cur];
         const long long j0 = (wi - p.tcoff[i]) * kHubChunk;
         const long long T = p.T[i];
@@ -1187,8 +1262,8 @@ __global__ void __launch_bounds__(256) k_hub_scan(DecideArgs a, HubPlan p, const
         const int *vals = p.pool + p.half + p.toff[i];
         long long x = -1;
         int bc = cur, bw = 0, bt = 0, wc = 0;
-        scan_table_int(a, keys + j0, vals + j0, (int)(j1 - j0), threadIdx.x, blockDim.x, cur, ki, tcur, x, bc, bw,
-                       bt, wc);
+        scan_table_int(a, sc, keys + j0, vals + j0, (int)(j1 - j0), threadIdx.x, blockDim.x, cur, ki, tcur, x, bc,
+                       bw, bt, wc);
         warp_merge_int(x, bc, bw, bt, wc, 32);
         if (lane == 0) {
             r_x[wid] = x;
@@ -1215,10 +1290,10 @@ __global__ void __launch_bounds__(256) k_hub_scan(DecideArgs a, HubPlan p, const
             }
         }
         __syncthreads();
-        if (needs_fp64(a, ki)) {  // uniform per chunk: the reference's FP64 gains, chunk-wise
+        if (needs_fp64(a, sc, ki)) {  // uniform per chunk: the reference's FP64 gains, chunk-wise
             double dq = 0.0;
             int fc = cur;
-            scan_table(a, keys + j0, vals + j0, (int)(j1 - j0), threadIdx.x, blockDim.x, cur, ki, tcur, dq, fc);
+            scan_table(a, sc, keys + j0, vals + j0, (int)(j1 - j0), threadIdx.x, blockDim.x, cur, ki, tcur, dq, fc);
             warp_argmax(dq, fc);
             if (lane == 0) {
                 r_dq[wid] = dq;
@@ -1247,7 +1322,8 @@ __global__ void __launch_bounds__(256) k_hub_final(DecideArgs a, HubPlan p, cons
     const int nw = (gridDim.x * blockDim.x) >> 5;
     for (int i = wg; i < p.H; i += nw) {
         const int v = p.hubs[i];
-        if (!flag[v]) continue;
+        if (!flag[v] || stopped(a, v)) continue;
+        const Scale sc = scale_of(a, v);
         const int cur = a.comm[v], ki = a.K[v], sf = a.Self[v], tcur = a.Tot[cur];
         long long x = -1;
         int bc = cur, bw = 0, bt = 0, wc = 0;
@@ -1256,19 +1332,19 @@ __global__ void __launch_bounds__(256) k_hub_final(DecideArgs a, HubPlan p, cons
             if (p.px[q] >= 0) cand_merge(x, bc, bw, bt, p.px[q], p.pc[q], p.pw[q], p.pt[q]);
         }
         warp_merge_int(x, bc, bw, bt, wc, 32);
-        int dec = int_decision(a, x, bt, cur, bc, wc, sf, ki);  // warp-uniform
+        int dec = int_decision(a, sc, x, bt, cur, bc, wc, sf, ki);  // warp-uniform
         if (dec == 2) {
             double dq = 0.0;
             int fc = cur;
-            if (needs_fp64(a, ki)) {  // chunk-wise FP64 partials from k_hub_scan
+            if (needs_fp64(a, sc, ki)) {  // chunk-wise FP64 partials from k_hub_scan
                 for (long long q = p.tcoff[i] + lane; q < p.tcoff[i + 1]; q += 32)
                     if (cand_better(p.pdq[q], p.pfc[q], dq, fc)) {
                         dq = p.pdq[q];
                         fc = p.pfc[q];
                     }
             } else {  // rare rounding cases: rescan the table in FP64
-                scan_table(a, p.pool + p.toff[i], p.pool + p.half + p.toff[i], (int)p.T[i], lane, 32, cur, ki, tcur,
-                           dq, fc);
+                scan_table(a, sc, p.pool + p.toff[i], p.pool + p.half + p.toff[i], (int)p.T[i], lane, 32, cur, ki,
+                           tcur, dq, fc);
             }
             warp_argmax(dq, fc);
             bc = fc;
@@ -1322,6 +1398,10 @@ void p1_hub_decide(const LevelGraph &g, Phase1Buffers &b, const HubPlan &p, doub
     a.fp64_only = fp64_only;
     a.feat_gain = b.features_on ? b.feat_gain : nullptr;
     a.feat_ndist = b.feat_ndist;
+    a.gid = b.gid;
+    a.m2g = b.m2g;
+    a.cg = b.cg;
+    a.stop = b.gstop;
     const int cap = num_sms() * 8;
     cudaMemsetAsync(p.pool, 0xff, (size_t)p.half * sizeof(int32_t), st);
     cudaMemsetAsync(p.pool + p.half, 0, (size_t)p.half * sizeof(int32_t), st);

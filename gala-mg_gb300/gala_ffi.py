@@ -26,7 +26,7 @@ EXPORTS = ["gala_last_error", "gala_status_string", "gala_kernel_launch_count", 
            "gala_modularity_host", "gala_modularity_device_static", "gala_proposal_create",
            "gala_proposal_destroy", "gala_proposal_get_params", "gala_proposal_set_params", "gala_proposal_samples",
            "gala_proposal_clear_samples", "gala_proposal_read_samples", "gala_proposal_gradient",
-           "gala_proposal_logits", "gala_proposal_train"]
+           "gala_proposal_logits", "gala_proposal_train", "gala_louvain_batch", "gala_generate_sbm_batch"]
 
 PROPOSAL_OFF, PROPOSAL_TRACE, PROPOSAL_SKIP = 0, 1, 2
 PROPOSAL_PARAMS = 32 * 8 + 32 + 32 * 32 + 32 + 32 + 1
@@ -87,6 +87,16 @@ class Result(ctypes.Structure):
         return d
 
 
+class BatchResult(ctypes.Structure):
+    _fields_ = [("num_graphs", ctypes.c_int32), ("num_levels", ctypes.c_int32),
+                ("total_iterations", ctypes.c_int32), ("reserved", ctypes.c_int32),
+                ("vertices", ctypes.c_int64), ("entries", ctypes.c_int64),
+                ("time_total_ms", ctypes.c_double), ("time_phase1_ms", ctypes.c_double),
+                ("time_contract_ms", ctypes.c_double), ("time_h2d_ms", ctypes.c_double),
+                ("time_d2h_ms", ctypes.c_double), ("kernel_launches", ctypes.c_int64),
+                ("h2d_bytes", ctypes.c_int64), ("d2h_bytes", ctypes.c_int64)]
+
+
 _lib = None
 
 
@@ -143,6 +153,13 @@ def load(path=LIB_PATH):
     L.gala_proposal_logits.argtypes = [_vp, _f32p, ctypes.c_int32, _f32p]
     L.gala_proposal_train.argtypes = [_vp, ctypes.c_int32, ctypes.c_int32, ctypes.c_float, ctypes.c_float,
                                       ctypes.c_uint64, _f32p]
+    L.gala_louvain_batch.argtypes = [_vp, ctypes.POINTER(_vp), ctypes.c_int32, ctypes.POINTER(Options), _i32p,
+                                     _f64p, _i32p, ctypes.POINTER(BatchResult)]
+    L.gala_generate_sbm_batch.argtypes = [ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
+                                          ctypes.c_int32, ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                                          ctypes.c_double, ctypes.c_uint64, ctypes.c_int32, ctypes.POINTER(_vp)]
+    L.gala_louvain_batch.restype = ctypes.c_int
+    L.gala_generate_sbm_batch.restype = ctypes.c_int
     for name in ["gala_proposal_create", "gala_proposal_get_params", "gala_proposal_set_params",
                  "gala_proposal_samples", "gala_proposal_clear_samples", "gala_proposal_read_samples",
                  "gala_proposal_gradient", "gala_proposal_logits", "gala_proposal_train"]:
@@ -228,6 +245,15 @@ class Graph:
         return Graph(h)
 
     @staticmethod
+    def sbm_batch(count, n_min=200, n_max=200000, k_min=8, k_max=64, deg_min=12.0, deg_max=40.0, mix_min=0.1,
+                  mix_max=0.4, seed=0, nthreads=0):
+        """gala_generate_sbm_batch: `count` planted-partition graphs."""
+        hs = (_vp * count)()
+        _check(load().gala_generate_sbm_batch(count, n_min, n_max, k_min, k_max, deg_min, deg_max, mix_min, mix_max,
+                                              seed, nthreads, hs))
+        return [Graph(_vp(h)) for h in hs]
+
+    @staticmethod
     def rmat(scale, edges, a=0.57, b=0.19, c=0.19, seed=1, nthreads=0, noise=0.0, keep_isolated=False):
         h = _vp()
         _check(load().gala_generate_rmat(scale, edges, a, b, c, noise, int(keep_isolated), seed, nthreads,
@@ -301,6 +327,26 @@ class Context:
         _check(load().gala_louvain(self.h, graph.h, ctypes.byref(o), _ptr(labels, _i32p), ctypes.byref(r)))
         d = r.to_dict(trace)
         d["labels"] = labels
+        return d
+
+    def louvain_batch(self, graphs, min_mod=1e-6, max_levels=0):
+        """gala_louvain_batch: many host graphs in one union run.  Returns the
+        per-graph labels (local community ids), modularity and community
+        counts plus the batch timings."""
+        G = len(graphs)
+        sizes = [g.info()[0] for g in graphs]
+        labels = np.zeros(sum(sizes), dtype=np.int32)
+        q = np.zeros(G, dtype=np.float64)
+        c = np.zeros(G, dtype=np.int32)
+        hs = (_vp * G)(*[g.h for g in graphs])
+        r = BatchResult()
+        o = default_options(min_modularity=min_mod, max_levels=max_levels)
+        _check(load().gala_louvain_batch(self.h, hs, G, ctypes.byref(o), _ptr(labels, _i32p), _ptr(q, _f64p),
+                                         _ptr(c, _i32p), ctypes.byref(r)))
+        starts = np.concatenate([[0], np.cumsum(sizes)])
+        d = {f: getattr(r, f) for f, _ in BatchResult._fields_ if f != "reserved"}
+        d.update({"labels": [labels[starts[i]:starts[i + 1]] for i in range(G)], "modularity": q,
+                  "communities": c})
         return d
 
     def louvain_device(self, n, d_offs, d_nbr, d_w, d_out, min_mod=1e-6, max_levels=0, iter_capacity=4096,

@@ -150,6 +150,16 @@ void gala_graph_destroy(gala_graph *g);
 /* Planted-partition SBM: n vertices in k equal blocks, p_in / p_out. */
 gala_status gala_generate_sbm(int32_t n, int32_t k, double p_in, double p_out,
                               uint64_t seed, gala_graph **out);
+/* `count` planted-partition graphs of uneven sizes (no counterpart in the
+ * reference): graph i has n log-uniform in [n_min, n_max], k uniform in
+ * [k_min, k_max] equal blocks (fewer when the blocks could not hold the
+ * degree), expected degree d uniform in [deg_min, deg_max] and mixing mu
+ * uniform in [mix_min, mix_max] (p_in = d (1 - mu) / (n/k - 1),
+ * p_out = d mu / (n - n/k)).  out receives count graphs; graph i depends only
+ * on seed and i. */
+gala_status gala_generate_sbm_batch(int32_t count, int32_t n_min, int32_t n_max, int32_t k_min,
+                                    int32_t k_max, double deg_min, double deg_max, double mix_min,
+                                    double mix_max, uint64_t seed, int32_t nthreads, gala_graph **out);
 /* R-MAT with 2^scale ids and `edges` raw undirected samples; duplicates and
  * self-loops removed, ids without edges dropped and renumbered in order.
  * noise > 0 perturbs a, b, c, d independently by a factor in
@@ -192,6 +202,38 @@ gala_status gala_louvain_device(gala_context *ctx, int32_t n, const int64_t *d_o
                                 const int32_t *d_neighbors, const int32_t *d_weights,
                                 const gala_options *opt, int32_t *d_community_out,
                                 gala_result *res);
+
+/* Batched graphs (no counterpart in the reference): `count` independent
+ * graphs run together as one block-diagonal union graph, every sweep of
+ * every level being one set of launches for all graphs.  Each graph keeps
+ * its own total weight m2, minimum community weight, modularity, iteration
+ * convergence and round rule, so its partition equals the one gala_louvain
+ * gives for it alone.  community_out (host, sum of the graphs' vertex
+ * counts, graph after graph) receives each vertex's community id local to
+ * its graph (dense from 0); modularity_out / communities_out (host, count
+ * entries, optional) the final Q and community count of each graph.  The
+ * context must hold the union (sum of vertices and entries); ctx may be NULL.
+ * Proposal modes are not available in a batch. */
+typedef struct {
+    int32_t num_graphs;
+    int32_t num_levels;        /* rounds run (the longest graph's) */
+    int32_t total_iterations;  /* phase-1 sweeps over all rounds */
+    int32_t reserved;
+    int64_t vertices;          /* union vertices */
+    int64_t entries;           /* union CSR entries */
+    double time_total_ms;      /* all rounds, device-resident union */
+    double time_phase1_ms;
+    double time_contract_ms;
+    double time_h2d_ms;
+    double time_d2h_ms;
+    int64_t kernel_launches;
+    int64_t h2d_bytes;
+    int64_t d2h_bytes;
+} gala_batch_result;
+gala_status gala_louvain_batch(gala_context *ctx, const gala_graph *const *graphs, int32_t count,
+                               const gala_options *opt, int32_t *community_out,
+                               double *modularity_out, int32_t *communities_out,
+                               gala_batch_result *res);
 
 /* One phase-1 run (decide-and-move iterations until the Q gain is below
  * min_modularity) on a device CSR.  Replaces louvain_main_process

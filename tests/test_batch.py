@@ -1,0 +1,104 @@
+"""Batched graphs (gala_louvain_batch, no counterpart in the reference).
+
+Every graph of a batch follows the single-graph rules with its own m2, min
+Tot, modularity, iteration convergence and round rule, so its partition must
+equal, bit for bit, the one the single-graph entry point and the CPU oracle
+give for it alone; its modularity must match a host FP64 recomputation.
+"""
+import numpy as np
+import pytest
+
+
+def test_sbm_batch_generator_deterministic_and_in_range(ffi):
+    a = ffi.Graph.sbm_batch(24, n_min=200, n_max=3000, seed=5)
+    b = ffi.Graph.sbm_batch(24, n_min=200, n_max=3000, seed=5)
+    sizes = []
+    for ga, gb in zip(a, b):
+        na, ea, _ = ga.info()
+        nb, eb, _ = gb.info()
+        assert (na, ea) == (nb, eb)
+        oa, ca, _ = ga.arrays()
+        ob, cb, _ = gb.arrays()
+        assert np.array_equal(oa, ob) and np.array_equal(ca, cb)
+        assert na <= 3000 and ea > 0
+        sizes.append(na)
+        deg = ea / na
+        assert 4 <= deg <= 60
+    assert max(sizes) > 2 * min(sizes)
+
+
+@pytest.fixture(scope="module")
+def torch_cuda():
+    import torch
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    torch.cuda.init()
+    return torch
+
+
+def _singles(ffi, graphs):
+    out = []
+    for g in graphs:
+        n, e, _ = g.info()
+        ctx = ffi.Context(n, e)
+        out.append(ctx.louvain(g))
+        ctx.close()
+    return out
+
+
+@pytest.mark.gpu
+def test_batch_equals_single_runs(ffi, oracle, torch_cuda):
+    graphs = ffi.Graph.sbm_batch(48, n_min=200, n_max=20000, seed=11)
+    # plus graphs of the other families: a karate-sized SBM and random weighted graphs
+    graphs.append(ffi.Graph.sbm(1024, 32, 0.3, 0.005, 3))
+    rng = np.random.default_rng(4)
+    for n in (300, 2500):
+        u = rng.integers(0, n, 6 * n)
+        v = rng.integers(0, n, 6 * n)
+        keep = u != v
+        u, v = u[keep], v[keep]
+        key = np.unique(np.minimum(u, v).astype(np.int64) * n + np.maximum(u, v))
+        a, b = key // n, key % n
+        rows = np.concatenate([a, b])
+        cols = np.concatenate([b, a]).astype(np.int32)
+        wt = rng.integers(1, 7, a.shape[0])
+        ww = np.concatenate([wt, wt]).astype(np.int32)
+        order = np.lexsort((cols, rows))
+        rows, cols, ww = rows[order], cols[order], ww[order]
+        offs = np.zeros(n + 1, dtype=np.int64)
+        np.add.at(offs, rows + 1, 1)
+        graphs.append(ffi.Graph.from_csr(np.cumsum(offs), cols, ww))
+    tot_n = sum(g.info()[0] for g in graphs)
+    tot_e = sum(g.info()[1] for g in graphs)
+    ctx = ffi.Context(tot_n, tot_e)
+    r = ctx.louvain_batch(graphs)
+    ctx.close()
+    assert r["num_graphs"] == len(graphs)
+    singles = _singles(ffi, graphs)
+    for i, (g, s) in enumerate(zip(graphs, singles)):
+        assert np.array_equal(r["labels"][i], s["labels"]), i
+        assert r["modularity"][i] == s["modularity"], i
+        assert r["communities"][i] == s["num_communities"], i
+        assert abs(g.modularity(r["labels"][i]) - r["modularity"][i]) <= 1e-9
+    # the oracle on a few of them
+    for i in (0, len(graphs) - 3, len(graphs) - 1):
+        offs, nbr, w = graphs[i].arrays()
+        o = oracle.louvain(offs, nbr, w)
+        assert np.array_equal(r["labels"][i], o["labels"])
+
+
+@pytest.mark.gpu
+def test_batch_max_levels_and_single_graph(ffi, torch_cuda):
+    g = ffi.Graph.sbm(1024, 32, 0.3, 0.005, 9)
+    n, e, _ = g.info()
+    ctx = ffi.Context(n, e)
+    r = ctx.louvain_batch([g])
+    s = ctx.louvain(g)
+    assert np.array_equal(r["labels"][0], s["labels"]) and r["modularity"][0] == s["modularity"]
+    r1 = ctx.louvain_batch([g], max_levels=1)
+    s1 = ctx.louvain(g, max_levels=1)
+    assert np.array_equal(r1["labels"][0], s1["labels"]) and r1["num_levels"] == 1
+    # the context still runs single graphs correctly after a batch
+    s2 = ctx.louvain(g)
+    assert np.array_equal(s2["labels"], s["labels"])
+    ctx.close()
