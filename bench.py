@@ -48,6 +48,7 @@ def parse():
     p.add_argument("--small", action="store_true", help="tiny workload for a quick check")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-learned", action="store_true", help="skip the learned-proposal arm")
+    p.add_argument("--no-batch", action="store_true", help="skip the batched-graphs arm")
     p.add_argument("--threshold", type=float, default=0.3, help="proposal probability threshold")
     p.add_argument("--profile", action="store_true",
                    help="one device-resident run and a short summary (for ncu captures)")
@@ -210,6 +211,53 @@ def learned_arm(ffi, ctx, g, stream, args, torch, plain_ms, plain):
                          "contract": r["time_contract_ms"]}}
 
 
+BATCH = {"workload": "sbm-batch-4096", "graphs": 4096, "n_min": 200, "n_max": 3500, "k_min": 8, "k_max": 64,
+         "deg_min": 12.0, "deg_max": 40.0, "mix_min": 0.1, "mix_max": 0.4, "seed": 1}
+
+
+def batch_arm(ffi, args, torch, device):
+    """4096 uneven planted-partition graphs (about 60M edges) in one batched
+    run (gala_louvain_batch, host graphs in, host labels out), against
+    single-graph runs of a sample of the same graphs."""
+    b = BATCH
+    gs = ffi.Graph.sbm_batch(b["graphs"], b["n_min"], b["n_max"], b["k_min"], b["k_max"], b["deg_min"],
+                             b["deg_max"], b["mix_min"], b["mix_max"], seed=b["seed"])
+    ns = [g.info()[0] for g in gs]
+    es = [g.info()[1] for g in gs]
+    m = sum(es) // 2
+    ctx = ffi.Context(sum(ns), sum(es), device=device)
+    times, r = [], None
+    for i in range(args.warmup + args.steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        r = ctx.louvain_batch(gs)
+        torch.cuda.synchronize()
+        if i >= args.warmup:
+            times.append(time.perf_counter() - t0)
+    ctx.close()
+    sec = statistics.median(times)
+    sample = list(range(0, b["graphs"], 128))
+    single = ffi.Context(max(ns), max(es), device=device)
+    st, equal, maxdq = 0.0, 0, 0.0
+    for i in sample:
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        s1 = single.louvain(gs[i])
+        torch.cuda.synchronize()
+        st += time.perf_counter() - t0
+        equal += int((s1["labels"] == r["labels"][i]).all())
+        maxdq = max(maxdq, abs(s1["modularity"] - r["modularity"][i]))
+    single.close()
+    seq_est = st / len(sample) * b["graphs"]
+    return {"config": dict(b, vertices=sum(ns), edges=m, max_vertices=max(ns), min_vertices=min(ns)),
+            "metric": "batched Louvain edges/s (host graphs in, labels out)", "value": m / sec, "unit": "edges/s",
+            "seconds": sec, "device_ms": r["time_total_ms"], "phase1_ms": r["time_phase1_ms"],
+            "contract_ms": r["time_contract_ms"], "levels": r["num_levels"], "iterations": r["total_iterations"],
+            "kernel_launches": r["kernel_launches"],
+            "sequential_single_runs_s_est": seq_est, "speedup_vs_sequential": seq_est / sec,
+            "checked_graphs": len(sample), "labels_equal_single_runs": equal, "max_dq_vs_single": maxdq}
+
+
 def main():
     args = parse()
     wl = SMALL if args.small else WORKLOAD
@@ -342,6 +390,8 @@ def main():
             "roofline": roof, "clocks": clk, "gpu_launches": launches}
     if not args.no_learned:
         line["learned"] = learned_arm(ffi, ctx, g, stream, args, torch, e2e_step, r_e2e)
+    if not args.no_batch:
+        line["batch"] = batch_arm(ffi, args, torch, local)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
         dt, ro = cpu_oracle_run(offs, nbr, threads)

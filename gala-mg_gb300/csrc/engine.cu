@@ -11,6 +11,8 @@
 #include <string.h>
 
 #include <algorithm>
+#include <atomic>
+#include <thread>
 #include <type_traits>
 #include <vector>
 
@@ -987,26 +989,35 @@ gala_status gala_louvain_batch(gala_context *ctx, const gala_graph *const *graph
     std::vector<int64_t> offs((size_t)n + 1);
     std::vector<int32_t> nbr((size_t)e_tot);
     std::vector<int32_t> w(weighted ? (size_t)e_tot : 0);
-    std::vector<int64_t> vstart((size_t)G + 1);
+    std::vector<int64_t> vstart((size_t)G + 1), estart((size_t)G + 1);
+    vstart[0] = estart[0] = 0;
+    for (int i = 0; i < G; ++i) {
+        vstart[i + 1] = vstart[i] + graphs[i]->n;
+        estart[i + 1] = estart[i] + graphs[i]->entries();
+    }
+    offs[0] = 0;
     {
-        long long v0 = 0, e0 = 0;
-        offs[0] = 0;
-        for (int i = 0; i < G; ++i) {
-            const gala_graph *gg = graphs[i];
-            vstart[i] = v0;
-            const long long E = gg->entries();
-            for (int v = 0; v < gg->n; ++v) offs[v0 + v + 1] = e0 + gg->offs[v];
-            for (long long j = 0; j < E; ++j) nbr[e0 + j] = (int32_t)(gg->nbr[j] + v0);
-            if (weighted) {
-                if (gg->weighted)
-                    memcpy(w.data() + e0, gg->w.data(), (size_t)E * sizeof(int32_t));
-                else
-                    std::fill(w.begin() + e0, w.begin() + e0 + E, 1);
+        std::atomic<int> next{0};
+        auto copy = [&] {
+            for (int i = next++; i < G; i = next++) {
+                const gala_graph *gg = graphs[i];
+                const long long v0 = vstart[i], e0 = estart[i], E = gg->entries();
+                for (int v = 0; v < gg->n; ++v) offs[v0 + v + 1] = e0 + gg->offs[v];
+                for (long long j = 0; j < E; ++j) nbr[e0 + j] = (int32_t)(gg->nbr[j] + v0);
+                if (weighted) {
+                    if (gg->weighted)
+                        memcpy(w.data() + e0, gg->w.data(), (size_t)E * sizeof(int32_t));
+                    else
+                        std::fill(w.begin() + e0, w.begin() + e0 + E, 1);
+                }
             }
-            v0 += gg->n;
-            e0 += E;
-        }
-        vstart[G] = v0;
+        };
+        const unsigned hw = std::thread::hardware_concurrency();
+        const int nt = std::max(1, std::min<int>(G, hw ? (int)hw : 1));
+        std::vector<std::thread> th;
+        for (int t = 1; t < nt; ++t) th.emplace_back(copy);
+        copy();
+        for (auto &x : th) x.join();
     }
     BatchRun bt;
     bt.G = G;
