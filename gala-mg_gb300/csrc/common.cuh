@@ -40,12 +40,13 @@ __host__ __device__ inline int bin_of_degree(int64_t d)
 // to pinned host memory once per iteration).
 struct DevStats {
     unsigned long long sum_in;      // sum over vertices of In[v]
-    unsigned long long sum_tot2;    // sum over communities of Tot[c]^2
+    unsigned long long sum_tot2;    // sum over communities of Tot[c]^2 (low word)
+    unsigned long long sum_tot2_hi; // high word (64-bit fixed-point weights)
     unsigned long long sum_self;    // sum of self-loop weights (level init)
     unsigned long long sum_k;       // sum of K = total weight m2 (level init)
     unsigned long long act_edges[2];   // sum of degrees in the active lists
     int act_vertices[2];
-    int min_tot;                    // min over non-empty communities of Tot
+    long long min_tot;              // min over non-empty communities of Tot
     int n_movers;                   // movers of the current iteration
     int err;                        // error bits (kErr*)
     int max_deg;
@@ -71,14 +72,47 @@ constexpr int kErrBadLabel = 4;
 constexpr int kErrBadIndex = 8;
 
 // ---------------------------------------------------------------------------
+// Weight types.  Integer graphs (the reference's int32 weights) run with
+// WT = int32_t: weights, K, Self, Tot and In are int32 and most decisions are
+// taken in exact integer arithmetic.  Float-weight graphs run with
+// WT = int64_t: every float weight is held as an exact 64-bit fixed-point
+// integer (weight * 2^S), so all sums (K, Tot, In, contracted weights) are
+// exact and independent of the order of the atomics, and every gain is
+// evaluated with the FP64 expressions.
+// ---------------------------------------------------------------------------
+template <typename WT>
+struct WideOf {
+    static constexpr bool exact = sizeof(WT) == 4;  // exact-integer decisions available
+};
+
+// Sum of w over the lanes of mask m (all lanes of m call with their w).
+__device__ __forceinline__ int group_sum(unsigned m, int w) { return (int)__reduce_add_sync(m, (unsigned)w); }
+// 64-bit values (0 <= w < 2^63) in three 21-bit limbs: a limb sum over 32
+// lanes stays below 2^26.
+__device__ __forceinline__ long long group_sum(unsigned m, long long w)
+{
+    const unsigned long long u = (unsigned long long)w;
+    const unsigned l0 = __reduce_add_sync(m, (unsigned)(u & 0x1fffff));
+    const unsigned l1 = __reduce_add_sync(m, (unsigned)((u >> 21) & 0x1fffff));
+    const unsigned l2 = __reduce_add_sync(m, (unsigned)(u >> 42));
+    return (long long)((unsigned long long)l0 + ((unsigned long long)l1 << 21) + ((unsigned long long)l2 << 42));
+}
+
+__device__ __forceinline__ void atomic_add_w(int *p, int v) { atomicAdd(p, v); }
+__device__ __forceinline__ void atomic_add_w(long long *p, long long v)
+{
+    atomicAdd((unsigned long long *)p, (unsigned long long)v);  // two's complement: also subtracts
+}
+
+// ---------------------------------------------------------------------------
 // FP64 gain of a candidate community, same operation order as the reference
 // (kernel_functions.cu:136, :171, :202, :362):
 //   2*w - 2*K*((Tot_c - Tot_cur) + K) * (1/m2)
 // Written with explicit round-to-nearest intrinsics so that no FMA contraction
 // changes the rounding; the CPU oracle is compiled with -ffp-contract=off.
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ double gain_dq(int w_to_c, int ki, int tot_c, int tot_cur,
-                                          double constant)
+template <typename WT>
+__device__ __forceinline__ double gain_dq(WT w_to_c, WT ki, WT tot_c, WT tot_cur, double constant)
 {
     double a = __dmul_rn(2.0, (double)w_to_c);
     double b = __dmul_rn(2.0, (double)ki);
@@ -87,17 +121,18 @@ __device__ __forceinline__ double gain_dq(int w_to_c, int ki, int tot_c, int tot
 }
 
 // (maxdq - 2*w_cur) + 2*Self  (kernel_functions.cu:381 / :532 / :748)
-__device__ __forceinline__ double gain_correct(double maxdq, int w_cur, int self_w)
+template <typename WT>
+__device__ __forceinline__ double gain_correct(double maxdq, WT w_cur, WT self_w)
 {
     return __dadd_rn(__dsub_rn(maxdq, (double)(2 * w_cur)), (double)(2 * self_w));
 }
 
 // Pruning bound of compute_In (kernel_functions.cu:944, :1028):
 //   2*(In-Self) - (K-Self) + (double)(minTot - (Tot_c - K)) * (1/m2) * K > 0
-__device__ __forceinline__ bool prune_bound(int in_w, int self_w, int ki, int min_tot, int tot_c,
-                                            double constant)
+template <typename WT>
+__device__ __forceinline__ bool prune_bound(WT in_w, WT self_w, WT ki, WT min_tot, WT tot_c, double constant)
 {
-    int ip = 2 * (in_w - self_w) - (ki - self_w);
+    WT ip = 2 * (in_w - self_w) - (ki - self_w);
     double d = __dmul_rn(__dmul_rn((double)(min_tot - (tot_c - ki)), constant), (double)ki);
     return __dadd_rn((double)ip, d) > 0.0;
 }
@@ -106,13 +141,16 @@ __device__ __forceinline__ bool prune_bound(int in_w, int self_w, int ki, int mi
 // has the sign of the FP64 expression whenever P != 0 and K*m2 < 2^49 (the
 // FP64 error is below K*2^-50, non-zero P/m2 is at least 1/m2 away from 0);
 // otherwise the FP64 expression decides, as in the reference.
-__device__ __forceinline__ bool prune_bound_fast(int in_w, int self_w, int ki, int min_tot, int tot_c,
-                                                 double constant, long long m2)
+template <typename WT>
+__device__ __forceinline__ bool prune_bound_fast(WT in_w, WT self_w, WT ki, WT min_tot, WT tot_c, double constant,
+                                                 long long m2)
 {
-    if ((long long)ki * m2 < (1LL << 49)) {
-        const int ip = 2 * (in_w - self_w) - (ki - self_w);
-        const long long p = (long long)ip * m2 + (long long)(min_tot - (tot_c - ki)) * (long long)ki;
-        if (p != 0) return p > 0;
+    if constexpr (WideOf<WT>::exact) {
+        if ((long long)ki * m2 < (1LL << 49)) {
+            const int ip = 2 * (in_w - self_w) - (ki - self_w);
+            const long long p = (long long)ip * m2 + (long long)(min_tot - (tot_c - ki)) * (long long)ki;
+            if (p != 0) return p > 0;
+        }
     }
     return prune_bound(in_w, self_w, ki, min_tot, tot_c, constant);
 }
@@ -150,7 +188,8 @@ __device__ __forceinline__ unsigned hash_slot(int key, int log2t)
     return ((unsigned)key * 0x9E3779B1u) >> (32 - log2t);
 }
 
-__device__ __forceinline__ bool hash_add(int *keys, int *vals, int T, int log2t, int key, int w)
+template <typename VT>
+__device__ __forceinline__ bool hash_add(int *keys, VT *vals, int T, int log2t, int key, VT w)
 {
     unsigned h = hash_slot(key, log2t);
     for (int p = 0; p < T; ++p) {
@@ -160,7 +199,7 @@ __device__ __forceinline__ bool hash_add(int *keys, int *vals, int T, int log2t,
             if (k == -1) k = key;
         }
         if (k == key) {
-            atomicAdd(&vals[h], w);
+            atomic_add_w(&vals[h], w);
             return true;
         }
         h = (h + 1) & (unsigned)(T - 1);

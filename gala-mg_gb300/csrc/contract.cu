@@ -225,14 +225,13 @@ __global__ void k_member_scatter(const int32_t *__restrict__ lab, const int64_t 
 // Community-ordered edge stream over contiguous entry ranges: entry j of row
 // v goes to medge[mpos[v]] + (j - offs[v]).  Rows are walked through the
 // list of rows with entries (nz_rows / nz_offs).
-template <bool W>
+template <typename WT, bool W>
 __global__ void __launch_bounds__(256) k_stream_fill(int n, long long E, const int64_t *__restrict__ offs,
-                                                     const int32_t *__restrict__ nbr,
-                                                     const int32_t *__restrict__ w,
+                                                     const int32_t *__restrict__ nbr, const WT *__restrict__ w,
                                                      const int32_t *__restrict__ lab,
                                                      const int32_t *__restrict__ mpos,
-                                                     const long long *__restrict__ medge, int32_t *skey,
-                                                     int32_t *sw, const int32_t *__restrict__ nz_rows,
+                                                     const long long *__restrict__ medge, int32_t *skey, WT *sw,
+                                                     const int32_t *__restrict__ nz_rows,
                                                      const long long *__restrict__ nz_offs, DevStats *st)
 {
     const long long wg = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
@@ -278,15 +277,16 @@ __global__ void __launch_bounds__(256) k_classify(int C, const long long *__rest
     }
 }
 
+template <typename WT>
 struct AggArgs {
     const int32_t *__restrict__ moff;
     const long long *__restrict__ medge;
     const long long *__restrict__ ec;
     const int32_t *__restrict__ skey;
-    const int32_t *__restrict__ sw;
+    const WT *__restrict__ sw;
     const long long *__restrict__ tmp_off;
     int32_t *tmp_nbr;
-    int32_t *tmp_w;
+    WT *tmp_w;
     int32_t *kc;
     DevStats *st;
     int C;
@@ -294,7 +294,8 @@ struct AggArgs {
 
 // Rows of at most 32 entries: one warp, rank of each distinct key by a
 // shuffle compare against all others.
-__global__ void __launch_bounds__(256) k_agg_small(AggArgs a, const int32_t *__restrict__ list)
+template <typename WT>
+__global__ void __launch_bounds__(256) k_agg_small(AggArgs<WT> a, const int32_t *__restrict__ list)
 {
     const int lane = threadIdx.x & 31;
     const int wg = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -305,13 +306,14 @@ __global__ void __launch_bounds__(256) k_agg_small(AggArgs a, const int32_t *__r
         const long long st = a.medge[a.moff[c]];
         const int E = (int)a.ec[c];
         const bool valid = lane < E;
-        int key = -1, wt = 0;
+        int key = -1;
+        WT wt = 0;
         if (valid) {
             key = a.skey[st + lane];
             wt = a.sw[st + lane];
         }
         const unsigned m = __match_any_sync(GALA_FULL_MASK, key);
-        const int sum = (int)__reduce_add_sync(m, (unsigned)wt);
+        const WT sum = group_sum(m, wt);
         const bool head = valid && (__ffs(m) - 1 == lane);
         const unsigned hm = __ballot_sync(GALA_FULL_MASK, head);
         int rank = 0;
@@ -329,7 +331,8 @@ __global__ void __launch_bounds__(256) k_agg_small(AggArgs a, const int32_t *__r
 }
 
 // Sort (key, val) pairs in shared memory by key, P a power of two.
-__device__ __forceinline__ void bitonic_sort_smem(int *k, int *v, int P)
+template <typename VT>
+__device__ __forceinline__ void bitonic_sort_smem(int *k, VT *v, int P)
 {
     for (int size = 2; size <= P; size <<= 1) {
         for (int stride = size >> 1; stride > 0; stride >>= 1) {
@@ -341,7 +344,7 @@ __device__ __forceinline__ void bitonic_sort_smem(int *k, int *v, int P)
                 if ((ki > kj) == asc) {
                     k[i] = kj;
                     k[j] = ki;
-                    int tv = v[i];
+                    VT tv = v[i];
                     v[i] = v[j];
                     v[j] = tv;
                 }
@@ -354,7 +357,14 @@ __device__ __forceinline__ void bitonic_sort_smem(int *k, int *v, int P)
 // Insert stream entries [st, st + len) into a table (dense when keys is
 // null).  Returns this thread's count of newly created keys.  All threads of
 // the block call it.
-__device__ __forceinline__ int agg_insert(const AggArgs &a, long long st, int len, int *keys, int *vals, int T,
+__device__ __forceinline__ bool add_was_zero(int *p, int v) { return atomicAdd(p, v) == 0; }
+__device__ __forceinline__ bool add_was_zero(long long *p, long long v)
+{
+    return atomicAdd((unsigned long long *)p, (unsigned long long)v) == 0ull;
+}
+
+template <typename WT>
+__device__ __forceinline__ int agg_insert(const AggArgs<WT> &a, long long st, int len, int *keys, WT *vals, int T,
                                           int lg)
 {
     const int lane = threadIdx.x & 31;
@@ -362,16 +372,17 @@ __device__ __forceinline__ int agg_insert(const AggArgs &a, long long st, int le
     for (int b0 = 0; b0 < len; b0 += blockDim.x) {
         const int j = b0 + threadIdx.x;
         const bool valid = j < len;
-        int key = -1, wt = 0;
+        int key = -1;
+        WT wt = 0;
         if (valid) {
             key = a.skey[st + j];
             wt = a.sw[st + j];
         }
         const unsigned m = __match_any_sync(GALA_FULL_MASK, key);
-        const int sum = (int)__reduce_add_sync(m, (unsigned)wt);
+        const WT sum = group_sum(m, wt);
         if (valid && __ffs(m) - 1 == lane) {
             if (!keys) {
-                created += atomicAdd(&vals[key], sum) == 0;
+                created += add_was_zero(&vals[key], sum);
             } else {
                 unsigned h = hash_slot(key, lg);
                 bool ok = false;
@@ -385,7 +396,7 @@ __device__ __forceinline__ int agg_insert(const AggArgs &a, long long st, int le
                         }
                     }
                     if (k == key) {
-                        atomicAdd(&vals[h], sum);
+                        atomic_add_w(&vals[h], sum);
                         ok = true;
                         break;
                     }
@@ -400,14 +411,14 @@ __device__ __forceinline__ int agg_insert(const AggArgs &a, long long st, int le
 
 // Rows of 33..kMid2Max entries: one CTA per community, shared-memory hash
 // table of TMAX slots, distinct keys sorted by a bitonic sort of LMAX slots.
-template <int BLOCK, int TMAX, int LMAX>
-__global__ void __launch_bounds__(BLOCK) k_agg_mid(AggArgs a, const int32_t *__restrict__ list, int cls)
+template <typename WT, int BLOCK, int TMAX, int LMAX>
+__global__ void __launch_bounds__(BLOCK) k_agg_mid(AggArgs<WT> a, const int32_t *__restrict__ list, int cls)
 {
-    extern __shared__ int sm[];
-    int *keys = sm;
-    int *vals = sm + TMAX;
-    int *lk = sm + 2 * TMAX;
-    int *lv = lk + LMAX;
+    extern __shared__ long long sm_ll[];
+    int *keys = (int *)sm_ll;
+    WT *vals = (WT *)(keys + TMAX);
+    int *lk = (int *)(vals + TMAX);
+    WT *lv = (WT *)(lk + LMAX);
     __shared__ int s_k;
     const int cnt = a.st->small_cnt[cls];
     for (int i = blockIdx.x; i < cnt; i += gridDim.x) {
@@ -479,7 +490,8 @@ struct BigArgs {
 
 // Table size and chunk counts of every class-3 community.  A dense table
 // (slot = community id) is used when a hash table would not be smaller.
-__global__ void k_big_plan(AggArgs a, BigArgs b)
+template <typename WT>
+__global__ void k_big_plan(AggArgs<WT> a, BigArgs b)
 {
     const int cnt = a.st->small_cnt[3];
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < cnt; i += gridDim.x * blockDim.x) {
@@ -508,7 +520,8 @@ __global__ void k_big_tail(BigArgs b, const DevStats *st)
 
 // stream chunk -> community and table chunk -> community, one warp per
 // community (list index)
-__global__ void k_big_work(AggArgs a, BigArgs b)
+template <typename WT>
+__global__ void k_big_work(AggArgs<WT> a, BigArgs b)
 {
     const int lane = threadIdx.x & 31;
     const int wg = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -525,7 +538,14 @@ __global__ void k_big_work(AggArgs a, BigArgs b)
 
 // Every CTA inserts one chunk of kChunk stream entries into its community's
 // global table; many CTAs share one community.  New keys are counted.
-__global__ void __launch_bounds__(256) k_big_insert(AggArgs a, BigArgs b, long long nwork)
+template <typename WT>
+__device__ __forceinline__ WT *big_vals(const BigArgs &b, long long i)
+{
+    return (WT *)(b.pool + b.pool_half) + b.toff[i];
+}
+
+template <typename WT>
+__global__ void __launch_bounds__(256) k_big_insert(AggArgs<WT> a, BigArgs b, long long nwork)
 {
     __shared__ int red[8];
     for (long long wi = blockIdx.x; wi < nwork; wi += gridDim.x) {
@@ -536,7 +556,7 @@ __global__ void __launch_bounds__(256) k_big_insert(AggArgs a, BigArgs b, long l
         const long long st = a.medge[a.moff[c]] + j * kChunk;
         const int len = (int)((E - j * kChunk) < kChunk ? (E - j * kChunk) : kChunk);
         const long long T = b.T[i];
-        int *vals = b.pool + b.pool_half + b.toff[i];
+        WT *vals = big_vals<WT>(b, i);
         int *keys = b.mode[i] ? nullptr : b.pool + b.toff[i];
         int created = agg_insert(a, st, len, keys, vals, (int)T, __ffs((int)T) - 1);
         created = warp_sum(created);
@@ -554,7 +574,8 @@ __global__ void __launch_bounds__(256) k_big_insert(AggArgs a, BigArgs b, long l
 // Rows with more distinct neighbours than a shared-memory sort holds are
 // ranked by a bitmap over all communities: words per row (0 for the others);
 // every class-3 row gets its final length here.
-__global__ void k_big_mark(AggArgs a, BigArgs b)
+template <typename WT>
+__global__ void k_big_mark(AggArgs<WT> a, BigArgs b)
 {
     const int cnt = a.st->small_cnt[3];
     const long long words = ((long long)a.C + 31) >> 5;
@@ -567,14 +588,15 @@ __global__ void k_big_mark(AggArgs a, BigArgs b)
 
 // Table chunks: distinct entries of sorted rows go to the row unsorted
 // (atomic cursor); rows ranked by bitmap set their bits.
-__global__ void __launch_bounds__(256) k_big_collect(AggArgs a, BigArgs b, long long ntwork)
+template <typename WT>
+__global__ void __launch_bounds__(256) k_big_collect(AggArgs<WT> a, BigArgs b, long long ntwork)
 {
     for (long long wi = blockIdx.x; wi < ntwork; wi += gridDim.x) {
         const int i = b.twork[wi];
         const long long j0 = (wi - b.tcoff[i]) * kChunk;
         const long long T = b.T[i];
         const int c = b.list[i];
-        const int *vals = b.pool + b.pool_half + b.toff[i];
+        const WT *vals = big_vals<WT>(b, i);
         const int *keys = b.pool + b.toff[i];
         const bool dense = b.mode[i];
         const bool bitmap = b.gwords[i] > 0;
@@ -582,7 +604,8 @@ __global__ void __launch_bounds__(256) k_big_collect(AggArgs a, BigArgs b, long 
         unsigned *bits = bitmap ? b.bits + b.gofs[i] : nullptr;
         for (long long s0 = j0; s0 < j0 + kChunk && s0 < T; s0 += blockDim.x) {
             const long long s = s0 + threadIdx.x;
-            int key = -1, val = 0;
+            int key = -1;
+            WT val = 0;
             if (s < T && s < j0 + kChunk) {
                 val = vals[s];
                 key = dense ? (val > 0 ? (int)s : -1) : keys[s];
@@ -610,7 +633,8 @@ __global__ void __launch_bounds__(256) k_big_collect(AggArgs a, BigArgs b, long 
 
 // Table chunks of bitmap-ranked rows: rank = popcounts of the row's bitmap
 // before the key.
-__global__ void __launch_bounds__(256) k_big_rank(AggArgs a, BigArgs b, long long ntwork)
+template <typename WT>
+__global__ void __launch_bounds__(256) k_big_rank(AggArgs<WT> a, BigArgs b, long long ntwork)
 {
     for (long long wi = blockIdx.x; wi < ntwork; wi += gridDim.x) {
         const int i = b.twork[wi];
@@ -618,7 +642,7 @@ __global__ void __launch_bounds__(256) k_big_rank(AggArgs a, BigArgs b, long lon
         const long long j0 = (wi - b.tcoff[i]) * kChunk;
         const long long T = b.T[i];
         const int c = b.list[i];
-        const int *vals = b.pool + b.pool_half + b.toff[i];
+        const WT *vals = big_vals<WT>(b, i);
         const int *keys = b.pool + b.toff[i];
         const bool dense = b.mode[i];
         const long long o = a.tmp_off[c];
@@ -626,7 +650,7 @@ __global__ void __launch_bounds__(256) k_big_rank(AggArgs a, BigArgs b, long lon
         const unsigned *pref = b.pref + b.gofs[i];
         const unsigned base = pref[0];
         for (long long s = j0 + threadIdx.x; s < j0 + kChunk && s < T; s += blockDim.x) {
-            const int val = vals[s];
+            const WT val = vals[s];
             const int key = dense ? (val > 0 ? (int)s : -1) : keys[s];
             if (key < 0) continue;
             const unsigned r = pref[key >> 5] - base + __popc(bits[key >> 5] & ((1u << (key & 31)) - 1u));
@@ -638,11 +662,12 @@ __global__ void __launch_bounds__(256) k_big_rank(AggArgs a, BigArgs b, long lon
 
 // Rows with at most kSortMax distinct neighbours: one CTA sorts the row in
 // shared memory.
-__global__ void __launch_bounds__(1024) k_big_sort(AggArgs a, BigArgs b)
+template <typename WT>
+__global__ void __launch_bounds__(1024) k_big_sort(AggArgs<WT> a, BigArgs b)
 {
-    extern __shared__ int sm[];
-    int *lk = sm;
-    int *lv = sm + kSortMax;
+    extern __shared__ long long sm_ll[];
+    int *lk = (int *)sm_ll;
+    WT *lv = (WT *)(lk + kSortMax);
     const int cnt = a.st->small_cnt[3];
     for (int i = blockIdx.x; i < cnt; i += gridDim.x) {
         if (b.gwords[i] != 0) continue;
@@ -666,11 +691,11 @@ __global__ void __launch_bounds__(1024) k_big_sort(AggArgs a, BigArgs b)
 
 // Compaction over contiguous output ranges: output entry j of community c
 // comes from tmp_off[c] + (j - new_offs[c]).
+template <typename WT>
 __global__ void __launch_bounds__(256) k_compact(int C, long long Enew, const int64_t *__restrict__ new_offs,
                                                  const long long *__restrict__ tmp_off,
-                                                 const int32_t *__restrict__ tmp_nbr,
-                                                 const int32_t *__restrict__ tmp_w, int32_t *out_nbr,
-                                                 int32_t *out_w, long long tmp_cap,
+                                                 const int32_t *__restrict__ tmp_nbr, const WT *__restrict__ tmp_w,
+                                                 int32_t *out_nbr, WT *out_w, long long tmp_cap,
                                                  const int32_t *__restrict__ nz_rows,
                                                  const long long *__restrict__ nz_offs, DevStats *st)
 {
@@ -711,14 +736,37 @@ __global__ void k_contract_reset(DevStats *st)
     st->err = 0;
 }
 
-constexpr size_t kMid1Smem = (2 * 1024 + 2 * kMid1Max) * sizeof(int);
-constexpr size_t kMid2Smem = (2 * 8192 + 2 * kMid2Max) * sizeof(int);
-constexpr size_t kSortSmem = 2 * kSortMax * sizeof(int);
+// Shared memory of the table kernels: int keys plus WT values per slot.
+template <typename WT>
+constexpr size_t mid1_smem()
+{
+    return (1024 + kMid1Max) * (sizeof(int) + sizeof(WT));
+}
+template <typename WT>
+constexpr size_t mid2_smem()
+{
+    return (8192 + kMid2Max) * (sizeof(int) + sizeof(WT));
+}
+template <typename WT>
+constexpr size_t sort_smem()
+{
+    return kSortMax * (sizeof(int) + sizeof(WT));
+}
+
+template <typename WT>
+static void configure_t()
+{
+    cudaFuncSetAttribute(k_agg_mid<WT, 128, 1024, kMid1Max>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)mid1_smem<WT>());
+    cudaFuncSetAttribute(k_agg_mid<WT, 256, 8192, kMid2Max>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)mid2_smem<WT>());
+    cudaFuncSetAttribute(k_big_sort<WT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sort_smem<WT>());
+}
 
 void contract_configure_kernels()
 {
-    cudaFuncSetAttribute(k_agg_mid<256, 8192, kMid2Max>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMid2Smem);
-    cudaFuncSetAttribute(k_big_sort, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSortSmem);
+    configure_t<int>();
+    configure_t<long long>();
 }
 
 static int grid_cap(long long items, int per_block, int cap)
@@ -751,7 +799,8 @@ static bool read_stats(DevStats *h, DevStats *d, cudaStream_t st, gala_status *s
 }
 
 // Rows longer than kMid2Max entries (class 3).  Returns false on failure.
-static bool contract_long_rows(const AggArgs &a, ContractBuffers &b, int cnt3, int C, DevStats &hs,
+template <typename WT>
+static bool contract_long_rows(const AggArgs<WT> &a, ContractBuffers &b, int cnt3, int C, DevStats &hs,
                                cudaStream_t st, gala_status *status)
 {
     const int nsm = sm_count();
@@ -772,7 +821,7 @@ static bool contract_long_rows(const AggArgs &a, ContractBuffers &b, int cnt3, i
     ba.gwords = b.big_gwords;
     ba.gofs = b.big_gofs;
     ba.pool = b.big_pool;
-    k_big_plan<<<grid_cap(cnt3, 256, cap), 256, 0, st>>>(a, ba);
+    k_big_plan<WT><<<grid_cap(cnt3, 256, cap), 256, 0, st>>>(a, ba);
     exclusive_scan(b.big_T, b.big_toff, cnt3, OpIdentity(), b.scan_partial, &b.stats->total, st);
     exclusive_scan(b.big_chunks, b.big_coff, cnt3, OpIdentity(), b.scan_partial, &b.stats->total2, st);
     exclusive_scan(b.big_tchunks, b.big_tcoff, cnt3, OpIdentity(), b.scan_partial, &b.stats->total3, st);
@@ -780,18 +829,22 @@ static bool contract_long_rows(const AggArgs &a, ContractBuffers &b, int cnt3, i
     note_launch(2);
     if (!read_stats(&hs, b.stats, st, status, "contraction: long rows")) return false;
     const long long slots = hs.total, nwork = hs.total2, ntwork = hs.total3;
-    if (2 * slots > b.big_pool_ints || nwork > b.big_work_cap || ntwork > b.big_twork_cap) {
-        set_error("contraction: long rows need %lld table slots / %lld + %lld chunks, pool holds %lld / %lld / %lld",
-                  slots, nwork, ntwork, b.big_pool_ints / 2, b.big_work_cap, b.big_twork_cap);
+    // keys, then the values 8-byte aligned (slot count rounded up to even)
+    const long long half = (slots + 1) & ~1LL;
+    constexpr long long vints = sizeof(WT) / sizeof(int32_t);
+    if (half + vints * slots > b.big_pool_ints || nwork > b.big_work_cap || ntwork > b.big_twork_cap) {
+        set_error("contraction: long rows need %lld table slots / %lld + %lld chunks, pool holds %lld ints / %lld / "
+                  "%lld",
+                  slots, nwork, ntwork, b.big_pool_ints, b.big_work_cap, b.big_twork_cap);
         *status = GALA_ERR_CAPACITY;
         return false;
     }
-    ba.pool_half = slots;
+    ba.pool_half = half;
     cudaMemsetAsync(b.big_pool, 0xff, (size_t)slots * sizeof(int32_t), st);
-    cudaMemsetAsync(b.big_pool + slots, 0, (size_t)slots * sizeof(int32_t), st);
-    k_big_work<<<grid_cap((long long)cnt3 * 32, 256, cap), 256, 0, st>>>(a, ba);
-    k_big_insert<<<(int)(nwork < nsm * 8 ? nwork : nsm * 8), 256, 0, st>>>(a, ba, nwork);
-    k_big_mark<<<grid_cap(cnt3, 256, cap), 256, 0, st>>>(a, ba);
+    cudaMemsetAsync(b.big_pool + half, 0, (size_t)slots * sizeof(WT), st);
+    k_big_work<WT><<<grid_cap((long long)cnt3 * 32, 256, cap), 256, 0, st>>>(a, ba);
+    k_big_insert<WT><<<(int)(nwork < nsm * 8 ? nwork : nsm * 8), 256, 0, st>>>(a, ba, nwork);
+    k_big_mark<WT><<<grid_cap(cnt3, 256, cap), 256, 0, st>>>(a, ba);
     exclusive_scan(b.big_gwords, b.big_gofs, cnt3, OpIdentity(), b.scan_partial, &b.stats->total, st);
     note_launch(3);
     if (!read_stats(&hs, b.stats, st, status, "contraction: long-row bitmaps")) return false;
@@ -805,14 +858,14 @@ static bool contract_long_rows(const AggArgs &a, ContractBuffers &b, int cnt3, i
     ba.pref = (unsigned *)b.big_bitmap + words;
     if (words > 0) cudaMemsetAsync(ba.bits, 0, (size_t)words * sizeof(unsigned), st);
     const int tgrid = (int)(ntwork < nsm * 8 ? ntwork : nsm * 8);
-    k_big_collect<<<tgrid, 256, 0, st>>>(a, ba, ntwork);
+    k_big_collect<WT><<<tgrid, 256, 0, st>>>(a, ba, ntwork);
     note_launch(1);
     if (words > 0) {
         exclusive_scan(ba.bits, ba.pref, words, OpPopc(), b.scan_partial, &b.stats->total, st);
-        k_big_rank<<<tgrid, 256, 0, st>>>(a, ba, ntwork);
+        k_big_rank<WT><<<tgrid, 256, 0, st>>>(a, ba, ntwork);
         note_launch(1);
     }
-    k_big_sort<<<cnt3 < nsm * 2 ? cnt3 : nsm * 2, 1024, kSortSmem, st>>>(a, ba);
+    k_big_sort<WT><<<cnt3 < nsm * 2 ? cnt3 : nsm * 2, 1024, sort_smem<WT>(), st>>>(a, ba);
     note_launch(1);
     return true;
 }
@@ -820,9 +873,10 @@ static bool contract_long_rows(const AggArgs &a, ContractBuffers &b, int cnt3, i
 // Returns the community count C (>= 1) or -1 on failure (*status set).
 // new_offs receives C+1 offsets (leading 0).  orig_map (length n_orig) is
 // composed with the new labels.
-int contract_run(const LevelGraph &g, const int32_t *comm, ContractBuffers &b, int64_t *new_offs,
-                 int32_t *new_nbr, int32_t *new_w, int32_t *orig_map, int32_t n_orig, int64_t *new_E,
-                 cudaStream_t st, gala_status *status, bool validate_labels)
+template <typename WT>
+static int contract_t(const LevelGraph &g, const int32_t *comm, ContractBuffers &b, int64_t *new_offs,
+                      int32_t *new_nbr, WT *new_w, int32_t *orig_map, int32_t n_orig, int64_t *new_E,
+                      cudaStream_t st, gala_status *status, bool validate_labels)
 {
     const int n = g.n;
     const int cap = sm_count() * 8;
@@ -860,45 +914,46 @@ int contract_run(const LevelGraph &g, const int32_t *comm, ContractBuffers &b, i
     const int fill_grid = grid_cap((g.E + kRangeEntries - 1) / kRangeEntries * 32, 256, cap);
     if (g.E > 0) {
         build_walk_list(g.offs, n, g.E, b, st);
+        WT *sw = (WT *)b.stream_w;
         if (g.w)
-            k_stream_fill<true><<<fill_grid, 256, 0, st>>>(n, g.E, g.offs, g.nbr, g.w, b.lab, b.mpos, b.medge,
-                                                          b.stream_key, b.stream_w, b.nz_rows, b.nz_offs,
-                                                          b.stats);
+            k_stream_fill<WT, true><<<fill_grid, 256, 0, st>>>(n, g.E, g.offs, g.nbr, (const WT *)g.w, b.lab, b.mpos,
+                                                              b.medge, b.stream_key, sw, b.nz_rows, b.nz_offs,
+                                                              b.stats);
         else
-            k_stream_fill<false><<<fill_grid, 256, 0, st>>>(n, g.E, g.offs, g.nbr, g.w, b.lab, b.mpos, b.medge,
-                                                           b.stream_key, b.stream_w, b.nz_rows, b.nz_offs,
-                                                           b.stats);
+            k_stream_fill<WT, false><<<fill_grid, 256, 0, st>>>(n, g.E, g.offs, g.nbr, (const WT *)g.w, b.lab,
+                                                               b.mpos, b.medge, b.stream_key, sw, b.nz_rows,
+                                                               b.nz_offs, b.stats);
     }
     k_classify<<<grid_cap(C, 256, cap), 256, 0, st>>>(C, b.ec, b.cls_list, b.kc, b.stats);
     exclusive_scan(b.ec, b.tmp_off, C, OpCap{C}, b.scan_partial, &b.stats->total, st);
     note_launch(6 + (orig_map ? 1 : 0));
     if (!read_stats(&hs, b.stats, st, status, "contraction: classification")) return -1;
 
-    AggArgs a;
+    AggArgs<WT> a;
     a.moff = b.moff;
     a.medge = b.medge;
     a.ec = b.ec;
     a.skey = b.stream_key;
-    a.sw = b.stream_w;
+    a.sw = (const WT *)b.stream_w;
     a.tmp_off = b.tmp_off;
     a.tmp_nbr = b.tmp_nbr;
-    a.tmp_w = b.tmp_w;
+    a.tmp_w = (WT *)b.tmp_w;
     a.kc = b.kc;
     a.st = b.stats;
     a.C = C;
     const int nsm = sm_count();
     if (hs.small_cnt[0] > 0) {
-        k_agg_small<<<grid_cap((long long)hs.small_cnt[0] * 32, 256, cap), 256, 0, st>>>(a, b.cls_list);
+        k_agg_small<WT><<<grid_cap((long long)hs.small_cnt[0] * 32, 256, cap), 256, 0, st>>>(a, b.cls_list);
         note_launch(1);
     }
     if (hs.small_cnt[1] > 0) {
         int grid = hs.small_cnt[1] < nsm * 12 ? hs.small_cnt[1] : nsm * 12;
-        k_agg_mid<128, 1024, kMid1Max><<<grid, 128, kMid1Smem, st>>>(a, b.cls_list + (long long)C, 1);
+        k_agg_mid<WT, 128, 1024, kMid1Max><<<grid, 128, mid1_smem<WT>(), st>>>(a, b.cls_list + (long long)C, 1);
         note_launch(1);
     }
     if (hs.small_cnt[2] > 0) {
         int grid = hs.small_cnt[2] < nsm * 2 ? hs.small_cnt[2] : nsm * 2;
-        k_agg_mid<256, 8192, kMid2Max><<<grid, 256, kMid2Smem, st>>>(a, b.cls_list + 2LL * C, 2);
+        k_agg_mid<WT, 256, 8192, kMid2Max><<<grid, 256, mid2_smem<WT>(), st>>>(a, b.cls_list + 2LL * C, 2);
         note_launch(1);
     }
     if (hs.small_cnt[3] > 0 && !contract_long_rows(a, b, hs.small_cnt[3], C, hs, st, status)) return -1;
@@ -909,8 +964,9 @@ int contract_run(const LevelGraph &g, const int32_t *comm, ContractBuffers &b, i
     const long long Enew = hs.total;
     if (Enew > 0) {
         build_walk_list(new_offs, C, Enew, b, st);
-        k_compact<<<grid_cap((Enew + kRangeEntries - 1) / kRangeEntries * 32, 256, cap), 256, 0, st>>>(
-            C, Enew, new_offs, b.tmp_off, b.tmp_nbr, b.tmp_w, new_nbr, new_w, g.E, b.nz_rows, b.nz_offs, b.stats);
+        k_compact<WT><<<grid_cap((Enew + kRangeEntries - 1) / kRangeEntries * 32, 256, cap), 256, 0, st>>>(
+            C, Enew, new_offs, b.tmp_off, b.tmp_nbr, (const WT *)b.tmp_w, new_nbr, new_w, g.E, b.nz_rows, b.nz_offs,
+            b.stats);
         note_launch(1);
     }
     if (!read_stats(&hs, b.stats, st, status, "contraction: compaction")) return -1;
@@ -921,6 +977,17 @@ int contract_run(const LevelGraph &g, const int32_t *comm, ContractBuffers &b, i
     }
     *new_E = Enew;
     return C;
+}
+
+int contract_run(const LevelGraph &g, const int32_t *comm, ContractBuffers &b, int64_t *new_offs,
+                 int32_t *new_nbr, void *new_w, int32_t *orig_map, int32_t n_orig, int64_t *new_E,
+                 cudaStream_t st, gala_status *status, bool validate_labels)
+{
+    if (g.wide)
+        return contract_t<long long>(g, comm, b, new_offs, new_nbr, (long long *)new_w, orig_map, n_orig, new_E, st,
+                                     status, validate_labels);
+    return contract_t<int>(g, comm, b, new_offs, new_nbr, (int *)new_w, orig_map, n_orig, new_E, st, status,
+                           validate_labels);
 }
 
 }  // namespace gala

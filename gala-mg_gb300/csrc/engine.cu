@@ -56,10 +56,14 @@ namespace {
 
 // Q from exact integer sums (the same expression as the oracle's
 // orc_q_from_sums); the host is compiled with -ffp-contract=off.
-double q_from_sums(unsigned long long sum_in, unsigned long long sum_tot2, long long m2)
+// The sum of Tot^2 is (hi, lo): 128 bits for fixed-point weights, hi = 0
+// otherwise; hi * 2^64 + lo is the oracle's orc_q_from_sums128 expression.
+double q_from_sums(unsigned long long sum_in, unsigned long long sum_tot2, long long m2,
+                   unsigned long long sum_tot2_hi = 0)
 {
     double c = 1.0 / (double)m2;
-    return (double)(long long)sum_in * c - (double)(long long)sum_tot2 * c * c;
+    double t2 = (double)sum_tot2_hi * 18446744073709551616.0 + (double)sum_tot2;
+    return (double)(long long)sum_in * c - t2 * c * c;
 }
 
 template <typename T>
@@ -73,6 +77,32 @@ bool dalloc(gala_context *ctx, T **p, size_t count)
     }
     ctx->allocs.push_back(q);
     *p = (T *)q;
+    return true;
+}
+
+// Float weights -> 64-bit fixed point round(w * 2^shift) (w * 2^shift is exact
+// in FP64, so the rounding is the host's llrint).
+__global__ void k_fixed_from_f32(const float *__restrict__ in, long long *out, long long E, double scale)
+{
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < E; i += (long long)gridDim.x * blockDim.x)
+        out[i] = __double2ll_rn((double)in[i] * scale);
+}
+void fixed_from_f32(const float *in, long long *out, long long E, int shift, cudaStream_t st)
+{
+    if (E <= 0) return;
+    long long grid = (E + 255) / 256;
+    if (grid > 4096) grid = 4096;
+    k_fixed_from_f32<<<(int)grid, 256, 0, st>>>(in, out, E, ldexp(1.0, shift));
+    note_launch(1);
+}
+
+// Arrays that hold int32 values, or int64 values for fixed-point weights:
+// 8 bytes per element.
+bool dalloc8(gala_context *ctx, int32_t **p, size_t count)
+{
+    long long *q = nullptr;
+    if (!dalloc(ctx, &q, count)) return false;
+    *p = (int32_t *)q;
     return true;
 }
 
@@ -222,7 +252,7 @@ gala_status phase1(gala_context *ctx, const LevelGraph &g, long long &m2, double
             set_error("graph has no edges (total weight 0)");
             return GALA_ERR_INVALID;
         }
-        if (m2 > 0x7fffffffLL) {
+        if (!g.wide && m2 > 0x7fffffffLL) {
             set_error("total weight %lld exceeds the int32 range of community totals", m2);
             return GALA_ERR_INVALID;
         }
@@ -269,7 +299,9 @@ gala_status phase1(gala_context *ctx, const LevelGraph &g, long long &m2, double
         hp.half = h->total;
         hp.nwork = h->total2;
         hp.ntwork = h->total3;
-        if (2 * hp.half > cb.big_pool_ints || hp.nwork > cb.big_work_cap || hp.ntwork > cb.big_twork_cap) {
+        const long long vints = g.wide ? 2 : 1;  // int32 per table value
+        if ((1 + vints) * hp.half > cb.big_pool_ints || hp.nwork > cb.big_work_cap ||
+            hp.ntwork > cb.big_twork_cap) {
             set_error("hub tables need %lld slots / %lld + %lld chunks, pool holds %lld / %lld / %lld", hp.half,
                       hp.nwork, hp.ntwork, cb.big_pool_ints / 2, cb.big_work_cap, cb.big_twork_cap);
             return GALA_ERR_CAPACITY;
@@ -278,6 +310,7 @@ gala_status phase1(gala_context *ctx, const LevelGraph &g, long long &m2, double
     }
     cudaMemsetAsync(b.act_flag, 1, (size_t)g.n, st);
     b.features_on = pmode != GALA_PROPOSAL_OFF;
+    b.wide = g.wide;
     if (b.features_on) p1_features_init(b, g.n, st);
     const int G = bt ? bt->G : 0;
     if (bt) {
@@ -312,7 +345,7 @@ gala_status phase1(gala_context *ctx, const LevelGraph &g, long long &m2, double
         cudaMemcpyAsync(bt->stop, bt->h_stop, G, cudaMemcpyHostToDevice, st);
     }
 
-    double q = q_from_sums(h->sum_in, h->sum_tot2, m2);
+    double q = q_from_sums(h->sum_in, h->sum_tot2, m2, h->sum_tot2_hi);
     if (trace) trace->push_back(q);
     if (verbose) printf("Iteration:%d Q:%f\n", 0, q);
     double prev_q = q;
@@ -324,7 +357,7 @@ gala_status phase1(gala_context *ctx, const LevelGraph &g, long long &m2, double
     note_launch(1);
     long long act_nv = nv_all, act_ne = g.E;
     int cur = 0;
-    const int min_tot_init = m2 > 0x7fffffffLL ? 0x7fffffff : (int)m2;
+    const long long min_tot_init = (!g.wide && m2 > 0x7fffffffLL) ? 0x7fffffffLL : m2;
     unsigned long long skipped0 = h->skipped, skipped_e0 = h->skipped_edges;
     bool verify = false;  // proposals stalled: the rest of the level runs plain sweeps
     cudaEventRecord(ctx->ev[0], st);
@@ -439,7 +472,7 @@ gala_status phase1(gala_context *ctx, const LevelGraph &g, long long &m2, double
             iteration++;
             continue;
         }
-        q = q_from_sums(h->sum_in, h->sum_tot2, m2);
+        q = q_from_sums(h->sum_in, h->sum_tot2, m2, h->sum_tot2_hi);
         if (trace) trace->push_back(q);
         if (verbose) printf("Iteration:%d Q:%f\n", iteration, q);
         // convergence (louvain_main_process.cu:1004-1007): the partition of
@@ -517,7 +550,8 @@ struct RunOut {
 // id range of every graph in ctx->orig's numbering and bt->cur_mod the
 // final modularity of every graph.
 gala_status run_levels(gala_context *ctx, int32_t n0, int64_t E0, const int64_t *offs0, const int32_t *nbr0,
-                       const int32_t *w0, const gala_options *opt, gala_result *res, BatchRun *bt = nullptr)
+                       const void *w0, const gala_options *opt, gala_result *res, BatchRun *bt = nullptr,
+                       bool wide = false)
 {
     cudaStream_t st = ctx->stream;
     gala_status s;
@@ -556,7 +590,11 @@ gala_status run_levels(gala_context *ctx, int32_t n0, int64_t E0, const int64_t 
     cudaMemsetAsync(&ctx->d_stats->fp64_decisions, 0, sizeof(unsigned long long), st);
     note_launch(1);
 
-    LevelGraph g{n0, E0, offs0, nbr0, w0};
+    if (wide && pr.mode != GALA_PROPOSAL_OFF) {
+        set_error("proposal modes are not available for float-weight graphs");
+        return GALA_ERR_INVALID;
+    }
+    LevelGraph g{n0, E0, offs0, nbr0, w0, wide};
     int buf = 0;
     double prev_mod = -1, cur_mod = -1;
     int round = 0;
@@ -607,7 +645,7 @@ gala_status run_levels(gala_context *ctx, int32_t n0, int64_t E0, const int64_t 
         round++;
         prev_mod = cur_mod;
         cur_mod = po.q;
-        g = LevelGraph{C, newE, ctx->offs[buf], ctx->nbr[buf], ctx->w[buf]};
+        g = LevelGraph{C, newE, ctx->offs[buf], ctx->nbr[buf], ctx->w[buf], wide};
         buf ^= 1;
         if (bt) {
             const int G = bt->G;
@@ -769,11 +807,11 @@ gala_status gala_context_create(int32_t device, int32_t max_vertices, int64_t ma
     }
     ok = ok && cudaMallocHost(&ctx->h_stats, sizeof(DevStats)) == cudaSuccess;
     for (int i = 0; i < 2 && ok; ++i)
-        ok = dalloc(ctx, &ctx->offs[i], n + 1) && dalloc(ctx, &ctx->nbr[i], E) && dalloc(ctx, &ctx->w[i], E);
+        ok = dalloc(ctx, &ctx->offs[i], n + 1) && dalloc(ctx, &ctx->nbr[i], E) && dalloc8(ctx, &ctx->w[i], E);
     Phase1Buffers &b = ctx->p1;
     ok = ok && dalloc(ctx, &ctx->orig, n) && dalloc(ctx, &ctx->d_stats, 1) && dalloc(ctx, &b.comm, n) &&
-         dalloc(ctx, &b.K, n) && dalloc(ctx, &b.Self, n) && dalloc(ctx, &b.Tot, n) && dalloc(ctx, &b.size, n) &&
-         dalloc(ctx, &b.In, n) && dalloc(ctx, &b.order, n) && dalloc(ctx, &b.act[0], n) &&
+         dalloc8(ctx, &b.K, n) && dalloc8(ctx, &b.Self, n) && dalloc8(ctx, &b.Tot, n) && dalloc(ctx, &b.size, n) &&
+         dalloc8(ctx, &b.In, n) && dalloc(ctx, &b.order, n) && dalloc(ctx, &b.act[0], n) &&
          dalloc(ctx, &b.act[1], n) && dalloc(ctx, &b.mv_v, n) && dalloc(ctx, &b.mv_old, n) &&
          dalloc(ctx, &b.mv_new, n) && dalloc(ctx, &b.blockcnt, kNumBinSlots * nblk) &&
          dalloc(ctx, &b.blockoff, kNumBinSlots * nblk) && dalloc(ctx, &b.scan_partial, nparts) &&
@@ -783,8 +821,8 @@ gala_status gala_context_create(int32_t device, int32_t max_vertices, int64_t ma
     ok = ok && dalloc(ctx, &c.cnt, n + 1) && dalloc(ctx, &c.newid, n + 1) && dalloc(ctx, &c.lab, n) &&
          dalloc(ctx, &c.csz, n + 1) && dalloc(ctx, &c.moff, n + 1) && dalloc(ctx, &c.cursor, n + 1) &&
          dalloc(ctx, &c.members, n) && dalloc(ctx, &c.mpos, n) && dalloc(ctx, &c.ec, n + 1) &&
-         dalloc(ctx, &c.medge, n + 1) && dalloc(ctx, &c.stream_key, E) && dalloc(ctx, &c.stream_w, E) &&
-         dalloc(ctx, &c.tmp_off, n + 1) && dalloc(ctx, &c.tmp_nbr, E) && dalloc(ctx, &c.tmp_w, E) &&
+         dalloc(ctx, &c.medge, n + 1) && dalloc(ctx, &c.stream_key, E) && dalloc8(ctx, &c.stream_w, E) &&
+         dalloc(ctx, &c.tmp_off, n + 1) && dalloc(ctx, &c.tmp_nbr, E) && dalloc8(ctx, &c.tmp_w, E) &&
          dalloc(ctx, &c.kc, n + 1) && dalloc(ctx, &c.cls_list, 4 * n);
     // tables of the rows longer than 4096 entries: at most 4 slots per entry
     // (keys + values), chunk list of at most E / 4096 + n entries
@@ -798,8 +836,8 @@ gala_status gala_context_create(int32_t device, int32_t max_vertices, int64_t ma
          dalloc(ctx, &c.big_twork, (size_t)c.big_twork_cap) && dalloc(ctx, &c.big_kdist, n) &&
          dalloc(ctx, &c.big_cursor, n) && dalloc(ctx, &c.big_gwords, n) && dalloc(ctx, &c.big_gofs, n + 1);
     ok = ok && dalloc(ctx, &b.act_flag, n) && dalloc(ctx, &ctx->hub_px, (size_t)c.big_twork_cap) &&
-         dalloc(ctx, &ctx->hub_pc, (size_t)c.big_twork_cap) && dalloc(ctx, &ctx->hub_pw, (size_t)c.big_twork_cap) &&
-         dalloc(ctx, &ctx->hub_pt, (size_t)c.big_twork_cap) && dalloc(ctx, &ctx->hub_pwc, (size_t)c.big_twork_cap) &&
+         dalloc(ctx, &ctx->hub_pc, (size_t)c.big_twork_cap) && dalloc8(ctx, &ctx->hub_pw, (size_t)c.big_twork_cap) &&
+         dalloc(ctx, &ctx->hub_pt, (size_t)c.big_twork_cap) && dalloc8(ctx, &ctx->hub_pwc, (size_t)c.big_twork_cap) &&
          dalloc(ctx, &ctx->hub_pdq, (size_t)c.big_twork_cap) && dalloc(ctx, &ctx->hub_pfc, (size_t)c.big_twork_cap) &&
          dalloc(ctx, &c.nz_pos, n + 1) && dalloc(ctx, &c.nz_rows, n + 1) && dalloc(ctx, &c.nz_offs, n + 1);
     // scratch pool for hub tables (phase 1) and the emission bitmaps of the
@@ -904,9 +942,14 @@ gala_status gala_louvain(gala_context *ctx, const gala_graph *g, const gala_opti
     cudaMemsetAsync(ctx->offs[1], 0, sizeof(int64_t), st);
     cudaMemcpyAsync(ctx->offs[1] + 1, g->offs.data(), (size_t)n * sizeof(int64_t), cudaMemcpyHostToDevice, st);
     cudaMemcpyAsync(ctx->nbr[1], g->nbr.data(), (size_t)E * sizeof(int32_t), cudaMemcpyHostToDevice, st);
-    const int32_t *dw = nullptr;
+    const void *dw = nullptr;
     if (g->weighted) {
         cudaMemcpyAsync(ctx->w[1], g->w.data(), (size_t)E * sizeof(int32_t), cudaMemcpyHostToDevice, st);
+        dw = ctx->w[1];
+    } else if (g->float_w) {
+        // float weights staged in the other level buffer, converted to fixed point
+        cudaMemcpyAsync(ctx->w[0], g->wf.data(), (size_t)E * sizeof(float), cudaMemcpyHostToDevice, st);
+        fixed_from_f32((const float *)ctx->w[0], (long long *)ctx->w[1], E, g->fixed_shift, st);
         dw = ctx->w[1];
     }
     cudaEventRecord(ctx->ev[7], st);
@@ -916,7 +959,7 @@ gala_status gala_louvain(gala_context *ctx, const gala_graph *g, const gala_opti
     }
     float h2d = ev_ms(ctx->ev[6], ctx->ev[7]);
     // level 0 lives in buffer 1; the first contraction writes buffer 0
-    s = run_levels(ctx, n, E, ctx->offs[1], ctx->nbr[1], dw, opt, res);
+    s = run_levels(ctx, n, E, ctx->offs[1], ctx->nbr[1], dw, opt, res, nullptr, g->float_w);
     if (s == GALA_OK) {
         cudaEventRecord(ctx->ev[6], st);
         cudaMemcpyAsync(community_out, ctx->orig, (size_t)n * sizeof(int32_t), cudaMemcpyDeviceToHost, st);
@@ -925,7 +968,7 @@ gala_status gala_louvain(gala_context *ctx, const gala_graph *g, const gala_opti
         res->time_d2h_ms = ev_ms(ctx->ev[6], ctx->ev[7]);
     }
     res->time_h2d_ms = h2d;
-    res->h2d_bytes = (long long)n * 8 + E * 4 + (g->weighted ? E * 4 : 0);
+    res->h2d_bytes = (long long)n * 8 + E * 4 + ((g->weighted || g->float_w) ? E * 4 : 0);
     res->d2h_bytes = (long long)n * 4;
     res->kernel_launches = gala_kernel_launch_count() - l0;
     if (own) gala_context_destroy(own);
@@ -950,6 +993,10 @@ gala_status gala_louvain_batch(gala_context *ctx, const gala_graph *const *graph
     for (int i = 0; i < count; ++i) {
         if (!graphs[i] || graphs[i]->n <= 0) {
             set_error("gala_louvain_batch: graph %d is empty", i);
+            return GALA_ERR_INVALID;
+        }
+        if (graphs[i]->float_w) {
+            set_error("gala_louvain_batch: graph %d has float weights (batches take int32 weights)", i);
             return GALA_ERR_INVALID;
         }
         n_tot += graphs[i]->n;

@@ -10,6 +10,7 @@
 #include <atomic>
 #include <cmath>
 #include <fstream>
+#include <functional>
 #include <random>
 #include <string>
 #include <thread>
@@ -94,7 +95,36 @@ static gala_status validate(const gala_graph *g)
                 set_error("weight %d at entry %lld is not positive", g->w[e], (long long)e);
                 return GALA_ERR_FORMAT;
             }
+    if (g->float_w) {
+        const int32_t s = fixed_shift_of(g->wf.data(), E);
+        if (s < 0) {
+            set_error("float weights must be positive, finite and not below 2^-(fixed-point shift)");
+            return GALA_ERR_FORMAT;
+        }
+        const_cast<gala_graph *>(g)->fixed_shift = s;
+    }
     return GALA_OK;
+}
+
+// Float weights are held as round(w * 2^S) in int64: S = 61 - e with
+// 2^e >= sum(w) (frexp of the sum in entry order), capped to [0, 40], so the
+// total weight stays below 2^62.
+int32_t fixed_shift_of(const float *w, int64_t E)
+{
+    double sum = 0, mn = INFINITY;
+    for (int64_t e = 0; e < E; ++e) {
+        const double x = (double)w[e];
+        if (!(x > 0) || !std::isfinite(x)) return -1;
+        sum += x;
+        if (x < mn) mn = x;
+    }
+    int ex = 0;
+    std::frexp(sum > 0 ? sum : 1.0, &ex);
+    int s = 61 - ex;
+    if (s > 40) s = 40;
+    if (s < 0) s = 0;
+    if (E > 0 && std::llrint(mn * std::ldexp(1.0, s)) <= 0) return -1;
+    return s;
 }
 
 // Build a CSR (reference layout) from an undirected edge list: symmetrise,
@@ -194,6 +224,7 @@ gala_graph::~gala_graph()
         if (!offs.empty()) cudaHostUnregister(offs.data());
         if (!nbr.empty()) cudaHostUnregister(nbr.data());
         if (!w.empty()) cudaHostUnregister(w.data());
+        if (!wf.empty()) cudaHostUnregister(wf.data());
         cudaGetLastError();
     }
 }
@@ -212,10 +243,12 @@ gala_status gala_graph_pin(gala_graph *g)
     if (!g->offs.empty()) e = cudaHostRegister(g->offs.data(), g->offs.size() * sizeof(int64_t), 0);
     if (e == cudaSuccess && !g->nbr.empty()) e = cudaHostRegister(g->nbr.data(), g->nbr.size() * sizeof(int32_t), 0);
     if (e == cudaSuccess && !g->w.empty()) e = cudaHostRegister(g->w.data(), g->w.size() * sizeof(int32_t), 0);
+    if (e == cudaSuccess && !g->wf.empty()) e = cudaHostRegister(g->wf.data(), g->wf.size() * sizeof(float), 0);
     if (e != cudaSuccess) {
         cudaHostUnregister(g->offs.data());
         cudaHostUnregister(g->nbr.data());
         if (!g->w.empty()) cudaHostUnregister(g->w.data());
+        if (!g->wf.empty()) cudaHostUnregister(g->wf.data());
         return cuda_fail(e, "gala_graph_pin");
     }
     g->pinned = true;
@@ -252,7 +285,17 @@ gala_status gala_graph_info(const gala_graph *g, int32_t *n, int64_t *num_entrie
     }
     if (n) *n = g->n;
     if (num_entries) *num_entries = g->entries();
-    if (weighted) *weighted = g->weighted ? 1 : 0;
+    if (weighted) *weighted = g->float_w ? 2 : (g->weighted ? 1 : 0);
+    return GALA_OK;
+}
+
+gala_status gala_graph_weights_f32(const gala_graph *g, const float **weights)
+{
+    if (!g || !weights) {
+        set_error("gala_graph_weights_f32: bad arguments");
+        return GALA_ERR_INVALID;
+    }
+    *weights = g->float_w ? g->wf.data() : nullptr;
     return GALA_OK;
 }
 
@@ -306,6 +349,12 @@ gala_status gala_graph_load_bin(const char *path, int32_t weighted, gala_graph *
         return GALA_ERR_FORMAT;
     }
     const int64_t E = g->offs[n - 1];
+    if (weighted < 0 || weighted > 2) {
+        fclose(f);
+        delete g;
+        set_error("gala_graph_load_bin: weighted must be 0, 1 (int32) or 2 (float32)");
+        return GALA_ERR_INVALID;
+    }
     const long long need = 4LL + 8LL * n + 4LL * E * (weighted ? 2 : 1);
     if (E < 0 || E % 2 != 0 || need > fsize) {
         fclose(f);
@@ -316,10 +365,14 @@ gala_status gala_graph_load_bin(const char *path, int32_t weighted, gala_graph *
     }
     g->nbr.resize(E);
     size_t got = fread(g->nbr.data(), sizeof(int32_t), (size_t)E, f);
-    g->weighted = weighted != 0;
-    if (weighted) {
+    g->weighted = weighted == 1;
+    g->float_w = weighted == 2;
+    if (weighted == 1) {
         g->w.resize(E);
         got += fread(g->w.data(), sizeof(int32_t), (size_t)E, f);
+    } else if (weighted == 2) {
+        g->wf.resize(E);
+        got += fread(g->wf.data(), sizeof(float), (size_t)E, f);
     }
     fclose(f);
     if (got != (size_t)E * (weighted ? 2 : 1)) {
@@ -353,6 +406,7 @@ gala_status gala_graph_store_bin(const gala_graph *g, const char *path)
               fwrite(g->offs.data(), sizeof(int64_t), (size_t)g->n, f) == (size_t)g->n &&
               fwrite(g->nbr.data(), sizeof(int32_t), (size_t)E, f) == (size_t)E;
     if (ok && g->weighted) ok = fwrite(g->w.data(), sizeof(int32_t), (size_t)E, f) == (size_t)E;
+    if (ok && g->float_w) ok = fwrite(g->wf.data(), sizeof(float), (size_t)E, f) == (size_t)E;
     ok = (fclose(f) == 0) && ok;
     if (!ok) {
         set_error("write error on %s", path);
@@ -383,6 +437,35 @@ gala_status gala_graph_from_csr(int32_t n, const int64_t *offsets_inclusive, con
         g->weighted = true;
         g->w.assign(weights, weights + E);
     }
+    gala_status s = validate(g);
+    if (s != GALA_OK) {
+        delete g;
+        return s;
+    }
+    *out = g;
+    return GALA_OK;
+}
+
+gala_status gala_graph_from_csr_f32(int32_t n, const int64_t *offsets_inclusive, const int32_t *neighbors,
+                                    const float *weights, gala_graph **out)
+{
+    clear_error();
+    if (!out || n <= 0 || !offsets_inclusive || !weights || (!neighbors && offsets_inclusive[n - 1] > 0)) {
+        set_error("gala_graph_from_csr_f32: bad arguments");
+        return GALA_ERR_INVALID;
+    }
+    gala_graph *g = new gala_graph();
+    g->n = n;
+    g->offs.assign(offsets_inclusive, offsets_inclusive + n);
+    const int64_t E = g->offs[n - 1];
+    if (E < 0) {
+        delete g;
+        set_error("negative entry count");
+        return GALA_ERR_INVALID;
+    }
+    g->nbr.assign(neighbors, neighbors + E);
+    g->float_w = true;
+    g->wf.assign(weights, weights + E);
     gala_status s = validate(g);
     if (s != GALA_OK) {
         delete g;
@@ -611,6 +694,272 @@ gala_status gala_generate_sbm_batch(int32_t count, int32_t n_min, int32_t n_max,
     return GALA_OK;
 }
 
+// ---- LFR-style planted graph ---------------------------------------------
+// Power-law degree d ~ x^-tau1 on [dmin, dmax] and community size ~ x^-tau2
+// on [cmin, cmax] (continuous inverse-CDF draws, rounded down); a fraction
+// 1 - mu of every vertex's stubs stays inside its community.  Vertices are
+// placed, largest internal degree first, into random communities large
+// enough to hold that degree; stubs are paired by the configuration model
+// inside every community and, for the mixing stubs, across random buckets.
+// Self-loops are dropped and parallel edges merged (weights summed).
+// Weights are lognormal(0, 1) float32 (Box-Muller on splitmix64).  The graph
+// depends only on the arguments, not on nthreads.
+static inline double powerlaw_draw(uint64_t &s, double lo, double hi, double tau)
+{
+    const double a = std::pow(lo, 1 - tau), b = std::pow(hi, 1 - tau);
+    return std::pow(a + (b - a) * u01(s), 1 / (1 - tau));
+}
+
+static inline float lognormal_draw(uint64_t &s)
+{
+    double u1 = u01(s);
+    const double u2 = u01(s);
+    if (u1 < 1e-300) u1 = 1e-300;
+    const double z = std::sqrt(-2 * std::log(u1)) * std::cos(6.283185307179586 * u2);
+    return (float)std::exp(z);
+}
+
+gala_status gala_generate_lfr(int32_t n, double tau1, int32_t dmin, int32_t dmax, double tau2, int32_t cmin,
+                              int32_t cmax, double mu, int32_t float_weights, uint64_t seed, int32_t nthreads,
+                              gala_graph **out)
+{
+    clear_error();
+    if (!out || n < 2 || dmin < 1 || dmax < dmin || cmin < 2 || cmax < cmin || tau1 <= 1 || tau2 <= 1 || mu < 0 ||
+        mu > 1 || cmin > n) {
+        set_error("gala_generate_lfr: bad arguments");
+        return GALA_ERR_INVALID;
+    }
+    *out = nullptr;
+    const int nt = hw_threads(nthreads);
+    const int64_t chunk = 1 << 16;
+    const int64_t nchunks = (n + chunk - 1) / chunk;
+    auto par = [&](int64_t items, const std::function<void(int64_t)> &f) {
+        std::atomic<int64_t> next{0};
+        std::vector<std::thread> th;
+        auto run = [&] {
+            for (int64_t i = next++; i < items; i = next++) f(i);
+        };
+        for (int t = 1; t < std::min<int64_t>(nt, items); ++t) th.emplace_back(run);
+        run();
+        for (auto &x : th) x.join();
+    };
+    // degrees and internal degrees
+    std::vector<int32_t> deg(n), kin(n);
+    par(nchunks, [&](int64_t c) {
+        uint64_t s = seed * 0xD1B54A32D192ED03ULL + (uint64_t)c * 0x9E3779B97F4A7C15ULL + 1;
+        for (int64_t v = c * chunk; v < std::min<int64_t>(n, (c + 1) * chunk); ++v) {
+            int32_t d = (int32_t)powerlaw_draw(s, dmin, dmax + 1.0, tau1);
+            d = std::max(dmin, std::min(dmax, d));
+            deg[v] = d;
+            kin[v] = (int32_t)std::llround((1 - mu) * d);
+        }
+    });
+    // community sizes summing to n
+    std::vector<int32_t> csize;
+    {
+        uint64_t s = seed * 0x9E3779B97F4A7C15ULL + 7;
+        int64_t tot = 0;
+        while (tot < n) {
+            int32_t c = (int32_t)powerlaw_draw(s, cmin, cmax + 1.0, tau2);
+            c = std::max(cmin, std::min(cmax, c));
+            if (tot + c > n) c = (int32_t)(n - tot);
+            csize.push_back(c);
+            tot += c;
+        }
+        if (csize.size() > 1 && csize.back() < cmin) {  // fold a short last community into the previous one
+            csize[csize.size() - 2] += csize.back();
+            csize.pop_back();
+        }
+        std::sort(csize.begin(), csize.end(), std::greater<int32_t>());
+    }
+    const int32_t K = (int32_t)csize.size();
+    // placement: vertices by internal degree (descending), each into a random
+    // community with room whose size exceeds the internal degree
+    std::vector<int32_t> order(n);
+    {
+        std::vector<int64_t> cnt((size_t)dmax + 2, 0);
+        for (int32_t v = 0; v < n; ++v) cnt[kin[v]]++;
+        int64_t acc = 0;
+        for (int32_t k = dmax + 1; k >= 0; --k) {  // descending k
+            const int64_t c = cnt[k];
+            cnt[k] = acc;
+            acc += c;
+        }
+        for (int32_t v = 0; v < n; ++v) order[cnt[kin[v]]++] = v;
+    }
+    std::vector<int32_t> comm(n), room(csize.begin(), csize.end());
+    {
+        uint64_t s = seed * 0xA24BAED4963EE407ULL + 11;
+        std::vector<int32_t> eligible;  // communities with room, size > current k
+        int32_t next_c = 0;
+        for (int32_t idx = 0; idx < n; ++idx) {
+            const int32_t v = order[idx];
+            while (next_c < K && csize[next_c] > kin[v]) eligible.push_back(next_c++);
+            int32_t c = -1;
+            while (!eligible.empty()) {
+                const size_t r = (size_t)(splitmix64(s) % eligible.size());
+                if (room[eligible[r]] > 0) {
+                    c = eligible[r];
+                    break;
+                }
+                eligible[r] = eligible.back();
+                eligible.pop_back();
+            }
+            if (c < 0) {  // no community large enough left: the largest one with room
+                for (int32_t q = 0; q < K && c < 0; ++q)
+                    if (room[q] > 0) c = q;
+                kin[v] = std::min(kin[v], csize[c] - 1);
+                while (next_c < K && csize[next_c] > kin[v]) eligible.push_back(next_c++);
+            }
+            comm[v] = c;
+            room[c]--;
+        }
+    }
+    // members per community
+    std::vector<int64_t> coff((size_t)K + 1, 0);
+    for (int32_t v = 0; v < n; ++v) coff[comm[v] + 1]++;
+    for (int32_t c = 0; c < K; ++c) coff[c + 1] += coff[c];
+    std::vector<int32_t> members(n);
+    {
+        std::vector<int64_t> pos(coff.begin(), coff.end() - 1);
+        for (int32_t v = 0; v < n; ++v) members[pos[comm[v]]++] = v;
+    }
+    // edges: intra-community pairing per community, mixing pairing per bucket
+    constexpr int kBuckets = 256;
+    std::vector<std::vector<int32_t>> eu((size_t)K + kBuckets), ev((size_t)K + kBuckets);
+    std::vector<std::vector<float>> ew((size_t)K + kBuckets);
+    auto pair_up = [&](std::vector<int32_t> &stubs, uint64_t s, size_t slot) {
+        for (size_t i = stubs.size(); i > 1; --i) std::swap(stubs[i - 1], stubs[splitmix64(s) % i]);
+        for (size_t i = 0; i + 1 < stubs.size(); i += 2) {
+            const int32_t a = stubs[i], b = stubs[i + 1];
+            if (a == b) continue;
+            eu[slot].push_back(std::min(a, b));
+            ev[slot].push_back(std::max(a, b));
+            ew[slot].push_back(float_weights ? lognormal_draw(s) : 1.0f);
+        }
+    };
+    par(K, [&](int64_t c) {
+        std::vector<int32_t> stubs;
+        for (int64_t i = coff[c]; i < coff[c + 1]; ++i)
+            for (int32_t k = 0; k < kin[members[i]]; ++k) stubs.push_back(members[i]);
+        pair_up(stubs, seed * 0x94D049BB133111EBULL + (uint64_t)c * 0x9E3779B97F4A7C15ULL + 3, (size_t)c);
+    });
+    {
+        // mixing stubs: bucket of every stub drawn per vertex chunk
+        std::vector<int64_t> bcnt((size_t)nchunks * kBuckets, 0);
+        auto stub_bucket_rng = [&](int64_t c) {
+            return seed * 0xBF58476D1CE4E5B9ULL + (uint64_t)c * 0x9E3779B97F4A7C15ULL + 5;
+        };
+        par(nchunks, [&](int64_t c) {
+            uint64_t s = stub_bucket_rng(c);
+            for (int64_t v = c * chunk; v < std::min<int64_t>(n, (c + 1) * chunk); ++v)
+                for (int32_t k = kin[v]; k < deg[v]; ++k) bcnt[(size_t)c * kBuckets + splitmix64(s) % kBuckets]++;
+        });
+        std::vector<int64_t> boff((size_t)nchunks * kBuckets + 1, 0);  // bucket-major
+        std::vector<int64_t> bstart(kBuckets + 1, 0);
+        int64_t acc = 0;
+        for (int b = 0; b < kBuckets; ++b) {
+            bstart[b] = acc;
+            for (int64_t c = 0; c < nchunks; ++c) {
+                boff[(size_t)b * nchunks + c] = acc;
+                acc += bcnt[(size_t)c * kBuckets + b];
+            }
+        }
+        bstart[kBuckets] = acc;
+        std::vector<int32_t> mix((size_t)acc);
+        par(nchunks, [&](int64_t c) {
+            uint64_t s = stub_bucket_rng(c);
+            std::vector<int64_t> pos(kBuckets);
+            for (int b = 0; b < kBuckets; ++b) pos[b] = boff[(size_t)b * nchunks + c];
+            for (int64_t v = c * chunk; v < std::min<int64_t>(n, (c + 1) * chunk); ++v)
+                for (int32_t k = kin[v]; k < deg[v]; ++k) mix[pos[splitmix64(s) % kBuckets]++] = (int32_t)v;
+        });
+        par(kBuckets, [&](int64_t b) {
+            std::vector<int32_t> stubs(mix.begin() + bstart[b], mix.begin() + bstart[b + 1]);
+            pair_up(stubs, seed * 0x2545F4914F6CDD1DULL + (uint64_t)b * 0x9E3779B97F4A7C15ULL + 9, (size_t)K + b);
+        });
+    }
+    // CSR: both directions, rows sorted by (neighbour, weight), parallel
+    // edges merged with summed weights
+    std::vector<int64_t> slot_off(eu.size() + 1, 0);
+    for (size_t i = 0; i < eu.size(); ++i) slot_off[i + 1] = slot_off[i] + (int64_t)eu[i].size();
+    std::vector<int64_t> rdeg((size_t)n + 1, 0);
+    for (size_t i = 0; i < eu.size(); ++i)
+        for (size_t j = 0; j < eu[i].size(); ++j) {
+            rdeg[eu[i][j] + 1]++;
+            rdeg[ev[i][j] + 1]++;
+        }
+    for (int32_t v = 0; v < n; ++v) rdeg[v + 1] += rdeg[v];
+    std::vector<int32_t> col((size_t)rdeg[n]);
+    std::vector<float> cw((size_t)rdeg[n]);
+    {
+        std::vector<int64_t> pos(rdeg.begin(), rdeg.end() - 1);
+        for (size_t i = 0; i < eu.size(); ++i) {
+            for (size_t j = 0; j < eu[i].size(); ++j) {
+                const int32_t a = eu[i][j], b = ev[i][j];
+                const float w = ew[i][j];
+                col[pos[a]] = b;
+                cw[pos[a]++] = w;
+                col[pos[b]] = a;
+                cw[pos[b]++] = w;
+            }
+            std::vector<int32_t>().swap(eu[i]);
+            std::vector<int32_t>().swap(ev[i]);
+            std::vector<float>().swap(ew[i]);
+        }
+    }
+    std::vector<int64_t> newlen(n, 0);
+    par(nchunks, [&](int64_t c) {
+        std::vector<std::pair<int32_t, float>> tmp;
+        for (int64_t r = c * chunk; r < std::min<int64_t>(n, (c + 1) * chunk); ++r) {
+            const int64_t s0 = rdeg[r], e0 = rdeg[r + 1];
+            tmp.clear();
+            for (int64_t j = s0; j < e0; ++j) tmp.emplace_back(col[j], cw[j]);
+            std::sort(tmp.begin(), tmp.end());
+            int64_t o = s0;
+            for (size_t k = 0; k < tmp.size(); ++k) {
+                if (k > 0 && tmp[k].first == tmp[k - 1].first) {
+                    cw[o - 1] += tmp[k].second;
+                    continue;
+                }
+                col[o] = tmp[k].first;
+                cw[o] = tmp[k].second;
+                ++o;
+            }
+            newlen[r] = o - s0;
+        }
+    });
+    gala_graph *g = new gala_graph();
+    g->n = n;
+    g->offs.resize(n);
+    int64_t acc = 0;
+    for (int32_t v = 0; v < n; ++v) {
+        acc += newlen[v];
+        g->offs[v] = acc;
+    }
+    g->nbr.resize((size_t)acc);
+    if (float_weights) {
+        g->float_w = true;
+        g->wf.resize((size_t)acc);
+    }
+    par(nchunks, [&](int64_t c) {
+        for (int64_t r = c * chunk; r < std::min<int64_t>(n, (c + 1) * chunk); ++r) {
+            const int64_t o = r == 0 ? 0 : g->offs[r - 1];
+            for (int64_t k = 0; k < newlen[r]; ++k) {
+                g->nbr[o + k] = col[rdeg[r] + k];
+                if (float_weights) g->wf[o + k] = cw[rdeg[r] + k];
+            }
+        }
+    });
+    gala_status st = validate(g);
+    if (st != GALA_OK) {
+        delete g;
+        return st;
+    }
+    *out = g;
+    return GALA_OK;
+}
+
 gala_status gala_generate_rmat(int32_t scale, int64_t nedges, double a, double b, double c, double noise,
                                int32_t keep_isolated, uint64_t seed, int32_t nthreads, gala_graph **out)
 {
@@ -685,6 +1034,25 @@ gala_status gala_modularity_host(const gala_graph *g, const int32_t *community, 
             set_error("community id %d of vertex %d out of range", community[v], v);
             return GALA_ERR_INVALID;
         }
+    if (g->float_w) {  // FP64 sums of the float weights
+        double m2f = 0;
+        for (int64_t e = 0; e < g->entries(); ++e) m2f += (double)g->wf[e];
+        const double cf = 1.0 / m2f;
+        std::vector<double> Tf(n, 0.0), If(n, 0.0);
+        for (int32_t i = 0; i < n; ++i) {
+            int64_t s = i == 0 ? 0 : g->offs[i - 1], e = g->offs[i];
+            double degree = 0;
+            for (int64_t j = s; j < e; ++j) {
+                degree += (double)g->wf[j];
+                if (community[g->nbr[j]] == community[i]) If[i] += (double)g->wf[j];
+            }
+            Tf[community[i]] += degree;
+        }
+        double acc = 0;
+        for (int32_t i = 0; i < n; ++i) acc += If[i] * cf - Tf[i] * Tf[i] * cf * cf;
+        *q = acc;
+        return GALA_OK;
+    }
     // kernel_functions.cu:1037-1079: In per vertex, Tot per community
     int64_t m2 = 0;
     for (int64_t e = 0; e < g->entries(); ++e) m2 += g->weighted ? g->w[e] : 1;

@@ -16,11 +16,20 @@ struct gala_graph {
     std::vector<int64_t> offs;  // n entries, inclusive prefix sums
     std::vector<int32_t> nbr;   // offs[n-1] entries
     std::vector<int32_t> w;     // empty when unweighted
-    bool weighted = false;
+    std::vector<float> wf;      // float weights (float graphs; w is then empty)
+    bool weighted = false;      // int32 weights
+    bool float_w = false;       // float32 weights, run as 64-bit fixed point
+    int32_t fixed_shift = 0;    // float graphs: weights are round(w * 2^fixed_shift)
     bool pinned = false;  // arrays registered with cudaHostRegister
     int64_t entries() const { return n ? offs[n - 1] : 0; }
     ~gala_graph();
 };
+
+namespace gala {
+// Fixed-point shift of float weights (the same rule as the oracle's
+// orc_fixed_shift); -1 when a weight is not positive and finite or rounds to 0.
+int32_t fixed_shift_of(const float *w, int64_t E);
+}
 
 namespace gala {
 
@@ -53,7 +62,8 @@ struct LevelGraph {
     int64_t E;
     const int64_t *offs;  // n+1, leading 0
     const int32_t *nbr;
-    const int32_t *w;     // nullptr = unweighted
+    const void *w;        // nullptr = unweighted; int32, or int64 fixed point when wide
+    bool wide = false;
 };
 
 // Phase-1 workspace (all device pointers, sized for the context capacity).
@@ -74,6 +84,7 @@ struct Phase1Buffers {
     int32_t *last_move;        // iteration of the vertex's last move
     int32_t *prop_list;        // proposed vertices (bin segments as in order)
     int features_on;           // 1 = decide kernels write the features above
+    int wide;                  // 1 = K, Self, Tot, In and weights are 64-bit fixed point
     // batched graphs (all null for one graph): graph of each vertex, the
     // graph's m2 and 1/m2, stopped graphs, per-graph min Tot
     const int32_t *gid;
@@ -121,7 +132,7 @@ struct HubPlan {
 
 // ---- phase 1 kernels (phase1.cu) ----
 void p1_level_init(const LevelGraph &g, Phase1Buffers &b, cudaStream_t st);
-void p1_iter_reset(Phase1Buffers &b, int next, int min_tot_init, cudaStream_t st);
+void p1_iter_reset(Phase1Buffers &b, int next, long long min_tot_init, cudaStream_t st);
 void p1_decide(const LevelGraph &g, Phase1Buffers &b, int bin, const int32_t *list,
                const int *count_ptr, int level_count, double constant, long long m2,
                int fp64_only, int hub_tmax, cudaStream_t st);
@@ -163,10 +174,10 @@ struct ContractBuffers {
     long long *ec;       // n+1 edges per community
     long long *medge;    // n+1 prefix of member degrees
     int32_t *stream_key; // E
-    int32_t *stream_w;   // E
+    int32_t *stream_w;   // E weights (int32, or int64 when wide: allocated 8 bytes per entry)
     long long *tmp_off;  // n+1
     int32_t *tmp_nbr;    // E
-    int32_t *tmp_w;      // E
+    int32_t *tmp_w;      // E weights (as stream_w)
     int32_t *kc;         // n+1 distinct neighbours per community
     int32_t *nz_pos;     // n+1: rows with entries, compacted (walk list)
     int32_t *nz_rows;    // n+1
@@ -197,7 +208,7 @@ struct ContractBuffers {
     DevStats *stats;
 };
 int contract_run(const LevelGraph &g, const int32_t *comm, ContractBuffers &b, int64_t *new_offs,
-                 int32_t *new_nbr, int32_t *new_w, int32_t *orig_map, int32_t n_orig,
+                 int32_t *new_nbr, void *new_w, int32_t *orig_map, int32_t n_orig,
                  int64_t *new_E, cudaStream_t st, gala_status *status, bool validate_labels = false);
 
 }  // namespace gala

@@ -65,13 +65,62 @@ __device__ __forceinline__ void block_add_i32(int v, int *dst)
     __syncthreads();
 }
 
+// Exact 128-bit block sum added to the (lo, hi) counter pair (carry from the
+// low word's atomic result, so the total does not depend on the order).
+__device__ __forceinline__ void block_add_u128(unsigned __int128 v, unsigned long long *lo, unsigned long long *hi)
+{
+    __shared__ unsigned long long rlo[32], rhi[32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int o = 16; o >= 1; o >>= 1) {
+        const unsigned long long l = __shfl_xor_sync(GALA_FULL_MASK, (unsigned long long)v, o);
+        const unsigned long long h = __shfl_xor_sync(GALA_FULL_MASK, (unsigned long long)(v >> 64), o);
+        v += ((unsigned __int128)h << 64) | l;
+    }
+    if (lane == 0) {
+        rlo[wid] = (unsigned long long)v;
+        rhi[wid] = (unsigned long long)(v >> 64);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned __int128 t = 0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += ((unsigned __int128)rhi[w] << 64) | rlo[w];
+        const unsigned long long l = (unsigned long long)t;
+        unsigned long long h = (unsigned long long)(t >> 64);
+        if (l) {
+            const unsigned long long old = atomicAdd(lo, l);
+            if (old + l < old) h += 1;
+        }
+        if (h) atomicAdd(hi, h);
+    }
+    __syncthreads();
+}
+
+// Square sums of community weights: u64 for int32 weights, exact u128 for
+// 64-bit fixed-point weights (Tot^2 up to 2^124).
+template <typename WT>
+struct SqSum {
+    using T = unsigned long long;
+    static __device__ __forceinline__ T sq(WT t) { return (T)((long long)t * t); }
+    static __device__ __forceinline__ void add(T v, DevStats *st) { block_add_u64(v, &st->sum_tot2); }
+};
+template <>
+struct SqSum<long long> {
+    using T = unsigned __int128;
+    static __device__ __forceinline__ T sq(long long t)
+    {
+        return (T)(unsigned long long)t * (unsigned long long)t;
+    }
+    static __device__ __forceinline__ void add(T v, DevStats *st) { block_add_u128(v, &st->sum_tot2, &st->sum_tot2_hi); }
+};
+
 // ------------------------------------------------------------------------
 // Level init: labels = own id, size 1 (louvain_main_process.cu:323-353),
 // then a stable counting sort of the vertices into degree bins (the reference
 // uses 8 count_if + a radix sort_by_key, :298-375).
 // ------------------------------------------------------------------------
-__global__ void k_init_vertices(int n, int32_t *comm, int32_t *K, int32_t *Self, int32_t *Tot,
-                                int32_t *size, int32_t *In)
+template <typename WT>
+__global__ void k_init_vertices(int n, int32_t *comm, WT *K, WT *Self, WT *Tot, int32_t *size, WT *In)
 {
     for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) {
         comm[v] = v;
@@ -136,19 +185,19 @@ __global__ void __launch_bounds__(kCountBlock) k_bin_scatter(int n, const int64_
 // K = row weight sum, Self = self-loop weight (init_communities,
 // kernel_functions.cu:34-73); Tot = K, In = Self.  Accumulates sum(K),
 // sum(K^2) and sum(Self) for the modularity of the singleton partition.
-template <int G, bool W>
+template <typename WT, int G, bool W>
 __global__ void __launch_bounds__(256) k_init_rows_group(const int32_t *__restrict__ list, int count,
                                                          const int64_t *__restrict__ offs,
                                                          const int32_t *__restrict__ nbr,
-                                                         const int32_t *__restrict__ w, int32_t *K,
-                                                         int32_t *Self, int32_t *Tot, int32_t *In,
-                                                         DevStats *st)
+                                                         const WT *__restrict__ w, WT *K, WT *Self, WT *Tot,
+                                                         WT *In, DevStats *st)
 {
     const int lane = threadIdx.x & 31, sub = lane & (G - 1), gw = lane / G;
     constexpr int GPW = 32 / G;
     const int wg = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int nw = (gridDim.x * blockDim.x) >> 5;
-    unsigned long long sk = 0, sk2 = 0, ss = 0;
+    unsigned long long sk = 0, ss = 0;
+    typename SqSum<WT>::T sk2 = 0;
     for (int base = wg * GPW; base < count; base += nw * GPW) {
         const int idx = base + gw;
         const bool has = idx < count;
@@ -159,9 +208,9 @@ __global__ void __launch_bounds__(256) k_init_rows_group(const int32_t *__restri
             s = offs[v];
             e = offs[v + 1];
         }
-        int k = 0, sf = 0;
+        WT k = 0, sf = 0;
         for (long long j = s + sub; j < e; j += G) {
-            int wt = W ? w[j] : 1;
+            WT wt = W ? w[j] : 1;
             k += wt;
             if (nbr[j] == v) sf = wt;
         }
@@ -176,30 +225,31 @@ __global__ void __launch_bounds__(256) k_init_rows_group(const int32_t *__restri
             Self[v] = sf;
             In[v] = sf;
             sk += (unsigned long long)k;
-            sk2 += (unsigned long long)((long long)k * k);
+            sk2 += SqSum<WT>::sq(k);
             ss += (unsigned long long)sf;
         }
     }
     block_add_u64(sk, &st->sum_k);
-    block_add_u64(sk2, &st->sum_tot2);
+    SqSum<WT>::add(sk2, st);
     block_add_u64(ss, &st->sum_in);
 }
 
-template <bool W>
+template <typename WT, bool W>
 __global__ void __launch_bounds__(256) k_init_rows_cta(const int32_t *__restrict__ list, int count,
                                                        const int64_t *__restrict__ offs,
                                                        const int32_t *__restrict__ nbr,
-                                                       const int32_t *__restrict__ w, int32_t *K, int32_t *Self,
-                                                       int32_t *Tot, int32_t *In, DevStats *st)
+                                                       const WT *__restrict__ w, WT *K, WT *Self, WT *Tot, WT *In,
+                                                       DevStats *st)
 {
-    __shared__ int rk[8], rs[8];
-    unsigned long long sk = 0, sk2 = 0, ss = 0;
+    __shared__ WT rk[8], rs[8];
+    unsigned long long sk = 0, ss = 0;
+    typename SqSum<WT>::T sk2 = 0;
     for (int i = blockIdx.x; i < count; i += gridDim.x) {
         int v = list[i];
         long long s = offs[v], e = offs[v + 1];
-        int k = 0, sf = 0;
+        WT k = 0, sf = 0;
         for (long long j = s + threadIdx.x; j < e; j += blockDim.x) {
-            int wt = W ? w[j] : 1;
+            WT wt = W ? w[j] : 1;
             k += wt;
             if (nbr[j] == v) sf = wt;
         }
@@ -222,13 +272,13 @@ __global__ void __launch_bounds__(256) k_init_rows_cta(const int32_t *__restrict
             Self[v] = sf;
             In[v] = sf;
             sk += (unsigned long long)k;
-            sk2 += (unsigned long long)((long long)k * k);
+            sk2 += SqSum<WT>::sq(k);
             ss += (unsigned long long)sf;
         }
         __syncthreads();
     }
     block_add_u64(sk, &st->sum_k);
-    block_add_u64(sk2, &st->sum_tot2);
+    SqSum<WT>::add(sk2, st);
     block_add_u64(ss, &st->sum_in);
 }
 
@@ -236,6 +286,7 @@ __global__ void k_reset_level_stats(DevStats *st)
 {
     st->sum_in = 0;
     st->sum_tot2 = 0;
+    st->sum_tot2_hi = 0;
     st->sum_self = 0;
     st->sum_k = 0;
     st->max_deg = 0;
@@ -249,26 +300,27 @@ void p1_reset_level_stats(Phase1Buffers &b, cudaStream_t st)
     note_launch(1);
 }
 
+template <typename WT>
 static void launch_init_rows(const LevelGraph &g, Phase1Buffers &b, int bin, const int32_t *list, int cnt,
                              cudaStream_t st)
 {
     if (cnt <= 0) return;
     const bool W = g.w != nullptr;
+    const WT *w = (const WT *)g.w;
+    WT *K = (WT *)b.K, *Self = (WT *)b.Self, *Tot = (WT *)b.Tot, *In = (WT *)b.In;
     const int cap = num_sms() * 8;
     auto grid_for = [&](int G) {
         long long blocks = ((long long)cnt * G + 255) / 256;
         return (int)(blocks < cap ? blocks : cap);
     };
-#define GALA_INIT_GROUP(GV)                                                                            \
-    do {                                                                                               \
-        if (W)                                                                                         \
-            k_init_rows_group<GV, true><<<grid_for(GV), 256, 0, st>>>(list, cnt, g.offs, g.nbr, g.w,   \
-                                                                      b.K, b.Self, b.Tot, b.In,        \
-                                                                      b.stats);                        \
-        else                                                                                           \
-            k_init_rows_group<GV, false><<<grid_for(GV), 256, 0, st>>>(list, cnt, g.offs, g.nbr, g.w,  \
-                                                                       b.K, b.Self, b.Tot, b.In,       \
-                                                                       b.stats);                       \
+#define GALA_INIT_GROUP(GV)                                                                              \
+    do {                                                                                                 \
+        if (W)                                                                                           \
+            k_init_rows_group<WT, GV, true><<<grid_for(GV), 256, 0, st>>>(list, cnt, g.offs, g.nbr, w, K,  \
+                                                                          Self, Tot, In, b.stats);       \
+        else                                                                                             \
+            k_init_rows_group<WT, GV, false><<<grid_for(GV), 256, 0, st>>>(list, cnt, g.offs, g.nbr, w, K, \
+                                                                           Self, Tot, In, b.stats);      \
     } while (0)
     switch (bin) {
     case 0: GALA_INIT_GROUP(4); break;
@@ -280,11 +332,9 @@ static void launch_init_rows(const LevelGraph &g, Phase1Buffers &b, int bin, con
     default: {
         int grid = cnt < cap ? cnt : cap;
         if (W)
-            k_init_rows_cta<true><<<grid, 256, 0, st>>>(list, cnt, g.offs, g.nbr, g.w, b.K, b.Self, b.Tot,
-                                                        b.In, b.stats);
+            k_init_rows_cta<WT, true><<<grid, 256, 0, st>>>(list, cnt, g.offs, g.nbr, w, K, Self, Tot, In, b.stats);
         else
-            k_init_rows_cta<false><<<grid, 256, 0, st>>>(list, cnt, g.offs, g.nbr, g.w, b.K, b.Self, b.Tot,
-                                                         b.In, b.stats);
+            k_init_rows_cta<WT, false><<<grid, 256, 0, st>>>(list, cnt, g.offs, g.nbr, w, K, Self, Tot, In, b.stats);
     }
     }
 #undef GALA_INIT_GROUP
@@ -297,8 +347,12 @@ void p1_level_init(const LevelGraph &g, Phase1Buffers &b, cudaStream_t st)
 {
     const int n = g.n;
     const int nblk = (n + kCountBlock - 1) / kCountBlock;
-    k_init_vertices<<<(n + 255) / 256 < 4096 ? (n + 255) / 256 : 4096, 256, 0, st>>>(n, b.comm, b.K, b.Self,
-                                                                                     b.Tot, b.size, b.In);
+    const int grid = (n + 255) / 256 < 4096 ? (n + 255) / 256 : 4096;
+    if (g.wide)
+        k_init_vertices<long long><<<grid, 256, 0, st>>>(n, b.comm, (long long *)b.K, (long long *)b.Self,
+                                                         (long long *)b.Tot, b.size, (long long *)b.In);
+    else
+        k_init_vertices<int><<<grid, 256, 0, st>>>(n, b.comm, b.K, b.Self, b.Tot, b.size, b.In);
     k_bin_count<<<nblk, kCountBlock, 0, st>>>(n, g.offs, b.blockcnt, nblk, b.stats);
     exclusive_scan(b.blockcnt, b.blockoff, (long long)kNumBinSlots * nblk, OpIdentity(), b.scan_partial,
                    &b.stats->total, st);
@@ -308,21 +362,26 @@ void p1_level_init(const LevelGraph &g, Phase1Buffers &b, cudaStream_t st)
 
 void p1_level_init_rows(const LevelGraph &g, Phase1Buffers &b, const int *bin_start, cudaStream_t st)
 {
-    for (int bin = 0; bin < kNumBins; ++bin)
-        launch_init_rows(g, b, bin, b.order + bin_start[bin], bin_start[bin + 1] - bin_start[bin], st);
+    for (int bin = 0; bin < kNumBins; ++bin) {
+        if (g.wide)
+            launch_init_rows<long long>(g, b, bin, b.order + bin_start[bin], bin_start[bin + 1] - bin_start[bin], st);
+        else
+            launch_init_rows<int>(g, b, bin, b.order + bin_start[bin], bin_start[bin + 1] - bin_start[bin], st);
+    }
 }
 
 // ------------------------------------------------------------------------
 // Decide-and-move
 // ------------------------------------------------------------------------
+template <typename WT>
 struct DecideArgs {
     const int64_t *__restrict__ offs;
     const int32_t *__restrict__ nbr;
-    const int32_t *__restrict__ w;
+    const WT *__restrict__ w;
     const int32_t *__restrict__ comm;
-    const int32_t *__restrict__ K;
-    const int32_t *__restrict__ Self;
-    const int32_t *__restrict__ Tot;
+    const WT *__restrict__ K;
+    const WT *__restrict__ Self;
+    const WT *__restrict__ Tot;
     const int32_t *__restrict__ size;
     int32_t *mv_v, *mv_old, *mv_new;
     DevStats *st;
@@ -344,7 +403,8 @@ struct Scale {
     long long m2;
     double c;
 };
-__device__ __forceinline__ Scale scale_of(const DecideArgs &a, int v)
+template <typename WT>
+__device__ __forceinline__ Scale scale_of(const DecideArgs<WT> &a, int v)
 {
     if (a.gid) {
         const int g = a.gid[v];
@@ -353,14 +413,20 @@ __device__ __forceinline__ Scale scale_of(const DecideArgs &a, int v)
     return Scale{a.m2, a.constant};
 }
 // Vertex of a batched graph whose phase 1 has stopped: not decided.
-__device__ __forceinline__ bool stopped(const DecideArgs &a, int v) { return a.stop && a.stop[a.gid[v]]; }
+template <typename WT>
+__device__ __forceinline__ bool stopped(const DecideArgs<WT> &a, int v)
+{
+    return a.stop && a.stop[a.gid[v]];
+}
 
 // Proposal features of a decided vertex: its best corrected gain
 // (max(X, 0) - (w_cur - Self) m2, normalised by K m2) and the number of
 // distinct neighbour communities (-1 when the schedule does not count them).
-__device__ __forceinline__ void write_features(const DecideArgs &a, const Scale &sc, int v, long long x, int w_cur,
-                                               int self_w, int ki, int ndist)
+template <typename WT>
+__device__ __forceinline__ void write_features(const DecideArgs<WT> &a, const Scale &sc, int v, long long x, WT w_cur,
+                                               WT self_w, WT ki, int ndist)
 {
+    if constexpr (!WideOf<WT>::exact) return;  // no proposal modes on fixed-point weights
     if (!a.feat_gain) return;
     const long long y = (x > 0 ? x : 0) - (long long)(w_cur - self_w) * sc.m2;
     a.feat_gain[v] = ki > 0 ? (float)y / ((float)sc.m2 * (float)ki) : 0.f;
@@ -369,19 +435,10 @@ __device__ __forceinline__ void write_features(const DecideArgs &a, const Scale 
 
 // Singleton swap guard (kernel_functions.cu:386): two singletons never move
 // towards the larger id.
-__device__ __forceinline__ bool guard_ok(const DecideArgs &a, int cur, int best)
+template <typename WT>
+__device__ __forceinline__ bool guard_ok(const DecideArgs<WT> &a, int cur, int best)
 {
     return !(a.size[best] == 1 && a.size[cur] == 1 && best > cur);
-}
-
-// Final decision of a vertex from the FP64 gain (kernel_functions.cu:381-409):
-// move only for a positive corrected gain.
-__device__ __forceinline__ bool decide_move(const DecideArgs &a, int cur, int best, double maxdq, int w_cur,
-                                            int self_w)
-{
-    if (best == cur) return false;
-    if (!(gain_correct(maxdq, w_cur, self_w) > 0.0)) return false;
-    return guard_ok(a, cur, best);
 }
 
 // ---- exact integer gains ---------------------------------------------------
@@ -396,16 +453,20 @@ __device__ __forceinline__ bool decide_move(const DecideArgs &a, int cur, int be
 // the vertex has no other weight in its community, and a corrected gain of
 // exactly 0.  Everything else is decided in integer arithmetic (GB300 runs
 // FP64 at a small fraction of its integer rate).
-__device__ __forceinline__ long long gain_x(int w, int ki, int tc, int tcur, long long m2)
+// (Fixed-point weights have no exact-integer path: X is 0 for every
+// candidate and int_decision sends the vertex to the FP64 evaluation.)
+template <typename WT>
+__device__ __forceinline__ long long gain_x(WT w, WT ki, WT tc, WT tcur, long long m2)
 {
+    if constexpr (!WideOf<WT>::exact) return 0;
     return (long long)w * m2 - (long long)ki * ((long long)tc - (long long)tcur + (long long)ki);
 }
 
 // Merge candidate (ox, oc, ow, ot) into (x, c, w, t): larger X first, then the
 // lower id; t records a tie on the best X between different weights.
 // Commutative, so butterfly reductions agree on every lane.
-__device__ __forceinline__ void cand_merge(long long &x, int &c, int &w, int &t, long long ox, int oc, int ow,
-                                           int ot)
+template <typename WT>
+__device__ __forceinline__ void cand_merge(long long &x, int &c, WT &w, int &t, long long ox, int oc, WT ow, int ot)
 {
     if (ox == x) {
         int tie = t | ot | (ow != w);
@@ -423,9 +484,11 @@ __device__ __forceinline__ void cand_merge(long long &x, int &c, int &w, int &t,
 }
 
 // 0 = stay, 1 = move (before the singleton guard), 2 = evaluate in FP64.
-__device__ __forceinline__ int int_decision(const DecideArgs &a, const Scale &sc, long long x, int t, int cur,
-                                            int best, int w_cur, int self_w, int ki)
+template <typename WT>
+__device__ __forceinline__ int int_decision(const DecideArgs<WT> &a, const Scale &sc, long long x, int t, int cur,
+                                            int best, WT w_cur, WT self_w, WT ki)
 {
+    if constexpr (!WideOf<WT>::exact) return 2;
     if (a.fp64_only || (long long)ki * sc.m2 >= (1LL << 49)) return 2;
     if (best == cur) return 0;  // every candidate has X < 0: every FP64 gain is < 0
     if (x == 0) return w_cur == self_w ? 2 : 0;
@@ -435,19 +498,21 @@ __device__ __forceinline__ int int_decision(const DecideArgs &a, const Scale &sc
     return y > 0 ? 1 : 0;
 }
 
-__device__ __forceinline__ void warp_merge_int(long long &x, int &c, int &w, int &t, int &wc, int width)
+template <typename WT>
+__device__ __forceinline__ void warp_merge_int(long long &x, int &c, WT &w, int &t, WT &wc, int width)
 {
     for (int o = width / 2; o >= 1; o >>= 1) {
         long long ox = __shfl_xor_sync(GALA_FULL_MASK, x, o);
         int oc = __shfl_xor_sync(GALA_FULL_MASK, c, o);
-        int ow = __shfl_xor_sync(GALA_FULL_MASK, w, o);
+        WT ow = __shfl_xor_sync(GALA_FULL_MASK, w, o);
         int ot = __shfl_xor_sync(GALA_FULL_MASK, t, o);
         wc += __shfl_xor_sync(GALA_FULL_MASK, wc, o);
         cand_merge(x, c, w, t, ox, oc, ow, ot);
     }
 }
 
-__device__ __forceinline__ void append_mover(const DecideArgs &a, bool move, int v, int cur, int best)
+template <typename WT>
+__device__ __forceinline__ void append_mover(const DecideArgs<WT> &a, bool move, int v, int cur, int best)
 {
     unsigned b = __ballot_sync(GALA_FULL_MASK, move);
     if (b == 0) return;
@@ -468,8 +533,8 @@ __device__ __forceinline__ void append_mover(const DecideArgs &a, bool move, int
 // community are found with __match_any_sync (the key carries the group index
 // so groups of one warp stay apart) and their weights summed with
 // __reduce_add_sync; the lowest lane of each set evaluates the gain.
-template <int G, bool W>
-__global__ void __launch_bounds__(256) k_decide_group(DecideArgs a, const int32_t *__restrict__ list,
+template <typename WT, int G, bool W>
+__global__ void __launch_bounds__(256) k_decide_group(DecideArgs<WT> a, const int32_t *__restrict__ list,
                                                       const int *__restrict__ count_ptr)
 {
     const int lane = threadIdx.x & 31, sub = lane & (G - 1), gw = lane / G;
@@ -480,7 +545,8 @@ __global__ void __launch_bounds__(256) k_decide_group(DecideArgs a, const int32_
     for (int base = wg * GPW; base < count; base += nw * GPW) {
         const int idx = base + gw;
         bool has = idx < count;
-        int v = 0, cur = -1, deg = 0, ki = 0, sf = 0, tcur = 0;
+        int v = 0, cur = -1, deg = 0;
+        WT ki = 0, sf = 0, tcur = 0;
         long long s = 0;
         Scale sc{a.m2, a.constant};
         if (has) {
@@ -497,20 +563,22 @@ __global__ void __launch_bounds__(256) k_decide_group(DecideArgs a, const int32_
             tcur = a.Tot[cur];
         }
         const bool valid = has && sub < deg;
-        int c = -1, wt = 0;
+        int c = -1;
+        WT wt = 0;
         if (valid) {
             c = a.comm[a.nbr[s + sub]];
             wt = W ? a.w[s + sub] : 1;
         }
         const unsigned long long key = ((unsigned long long)(unsigned)gw << 32) | (unsigned)c;
         const unsigned m = __match_any_sync(GALA_FULL_MASK, key);
-        const int wsum = W ? (int)__reduce_add_sync(m, (unsigned)wt) : __popc(m);
+        const WT wsum = W ? group_sum(m, wt) : (WT)__popc(m);
         const bool leader = valid && (__ffs(m) - 1 == lane);
-        const int wc_own = (leader && c == cur) ? wsum : 0;
-        int wc = wc_own;
-        int tc = 0;
+        const WT wc_own = (leader && c == cur) ? wsum : 0;
+        WT wc = wc_own;
+        WT tc = 0;
         long long x = -1;
-        int bc = cur, bw = 0, bt = 0;
+        int bc = cur, bt = 0;
+        WT bw = 0;
         if (leader && c != cur) {
             tc = a.Tot[c];
             const long long xx = gain_x(wsum, ki, tc, tcur, sc.m2);
@@ -562,14 +630,15 @@ __global__ void __launch_bounds__(256) k_decide_group(DecideArgs a, const int32_
 
 // Scan a hash table: this thread's best candidate by exact X and its share of
 // the weight to the own community.
-__device__ __forceinline__ void scan_table_int(const DecideArgs &a, const Scale &sc, const int *keys,
-                                               const int *vals, int T, int first, int stride, int cur, int ki,
-                                               int tcur, long long &x, int &bc, int &bw, int &bt, int &wc)
+template <typename WT>
+__device__ __forceinline__ void scan_table_int(const DecideArgs<WT> &a, const Scale &sc, const int *keys,
+                                               const WT *vals, int T, int first, int stride, int cur, WT ki,
+                                               WT tcur, long long &x, int &bc, WT &bw, int &bt, WT &wc)
 {
     for (int j = first; j < T; j += stride) {
         const int c = keys[j];
         if (c < 0) continue;
-        const int wv = vals[j];
+        const WT wv = vals[j];
         if (c == cur) {
             wc += wv;
         } else {
@@ -581,8 +650,9 @@ __device__ __forceinline__ void scan_table_int(const DecideArgs &a, const Scale 
 
 // The same scan with the reference's FP64 gains (vertices int_decision
 // cannot settle).
-__device__ __forceinline__ void scan_table(const DecideArgs &a, const Scale &sc, const int *keys, const int *vals,
-                                           int T, int first, int stride, int cur, int ki, int tcur, double &dq,
+template <typename WT>
+__device__ __forceinline__ void scan_table(const DecideArgs<WT> &a, const Scale &sc, const int *keys, const WT *vals,
+                                           int T, int first, int stride, int cur, WT ki, WT tcur, double &dq,
                                            int &bc)
 {
     for (int j = first; j < T; j += stride) {
@@ -611,15 +681,15 @@ __device__ __forceinline__ void warp_argmax(double &dq, int &bc)
 
 // Degree 33-256: one warp per vertex with a private shared-memory hash table.
 constexpr int kWarpTable = 512;
-template <bool W>
-__global__ void __launch_bounds__(256) k_decide_warp(DecideArgs a, const int32_t *__restrict__ list,
+template <typename WT, bool W>
+__global__ void __launch_bounds__(256) k_decide_warp(DecideArgs<WT> a, const int32_t *__restrict__ list,
                                                      const int *__restrict__ count_ptr)
 {
     __shared__ int s_keys[8][kWarpTable];
-    __shared__ int s_vals[8][kWarpTable];
+    __shared__ WT s_vals[8][kWarpTable];
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     int *keys = s_keys[wib];
-    int *vals = s_vals[wib];
+    WT *vals = s_vals[wib];
     const int count = *count_ptr;
     const int wg = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int nw = (gridDim.x * blockDim.x) >> 5;
@@ -642,20 +712,22 @@ __global__ void __launch_bounds__(256) k_decide_warp(DecideArgs a, const int32_t
         for (int e0 = 0; e0 < deg; e0 += 32) {
             const int e = e0 + lane;
             const bool valid = e < deg;
-            int c = -1, wt = 0;
+            int c = -1;
+            WT wt = 0;
             if (valid) {
                 c = a.comm[a.nbr[s + e]];
                 wt = W ? a.w[s + e] : 1;
             }
             const unsigned m = __match_any_sync(GALA_FULL_MASK, c);
-            const int wsum = W ? (int)__reduce_add_sync(m, (unsigned)wt) : __popc(m);
+            const WT wsum = W ? group_sum(m, wt) : (WT)__popc(m);
             if (valid && __ffs(m) - 1 == lane)
                 if (!hash_add(keys, vals, T, lg, c, wsum)) atomicOr(&a.st->err, kErrHashOverflow);
         }
         __syncwarp();
-        const int ki = a.K[v], tcur = a.Tot[cur], sf = a.Self[v];
+        const WT ki = a.K[v], tcur = a.Tot[cur], sf = a.Self[v];
         long long x = -1;
-        int bc = cur, bw = 0, bt = 0, wc = 0;
+        int bc = cur, bt = 0;
+        WT bw = 0, wc = 0;
         scan_table_int(a, sc, keys, vals, T, lane, 32, cur, ki, tcur, x, bc, bw, bt, wc);
         warp_merge_int(x, bc, bw, bt, wc, 32);
         int dec = int_decision(a, sc, x, bt, cur, bc, wc, sf, ki);  // warp-uniform
@@ -680,24 +752,23 @@ __global__ void __launch_bounds__(256) k_decide_warp(DecideArgs a, const int32_t
     }
 }
 
-// Degree > 256: one CTA per vertex; the hash table lives in dynamic shared
-// memory (GMEM = false) or in a per-CTA slice of global memory (GMEM = true,
-// hub vertices; the slice stays in L2).
-template <int BLOCK, bool GMEM, bool W>
-__global__ void __launch_bounds__(BLOCK) k_decide_cta(DecideArgs a, const int32_t *__restrict__ list,
-                                                      const int *__restrict__ count_ptr, int tmax,
-                                                      int32_t *gtab)
+// Degree 257-8192: one CTA per vertex with the hash table in dynamic shared
+// memory (tmax slots: int keys, then WT values).
+template <typename WT, int BLOCK, bool W>
+__global__ void __launch_bounds__(BLOCK) k_decide_cta(DecideArgs<WT> a, const int32_t *__restrict__ list,
+                                                      const int *__restrict__ count_ptr, int tmax)
 {
-    extern __shared__ int dyn_smem[];
+    extern __shared__ long long dyn_smem_ll[];
     __shared__ double r_dq[BLOCK / 32];
     __shared__ long long r_x[BLOCK / 32];
     __shared__ int r_c[BLOCK / 32];
-    __shared__ int r_w[BLOCK / 32];
+    __shared__ WT r_w[BLOCK / 32];
     __shared__ int r_t[BLOCK / 32];
-    __shared__ int r_wc[BLOCK / 32];
-    __shared__ int s_dec, s_bc, s_wc;
-    int *keys = GMEM ? gtab + (long long)blockIdx.x * 2 * tmax : dyn_smem;
-    int *vals = keys + tmax;
+    __shared__ WT r_wc[BLOCK / 32];
+    __shared__ int s_dec, s_bc;
+    __shared__ WT s_wc;
+    int *keys = (int *)dyn_smem_ll;
+    WT *vals = (WT *)(keys + tmax);
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     const int count = *count_ptr;
     for (int i = blockIdx.x; i < count; i += gridDim.x) {
@@ -723,21 +794,23 @@ __global__ void __launch_bounds__(BLOCK) k_decide_cta(DecideArgs a, const int32_
         for (long long b0 = s; b0 < e; b0 += BLOCK) {
             const long long j = b0 + threadIdx.x;
             const bool valid = j < e;
-            int c = -1, wt = 0;
+            int c = -1;
+            WT wt = 0;
             if (valid) {
                 c = a.comm[a.nbr[j]];
                 wt = W ? a.w[j] : 1;
             }
             const unsigned m = __match_any_sync(GALA_FULL_MASK, c);
-            const int wsum = W ? (int)__reduce_add_sync(m, (unsigned)wt) : __popc(m);
+            const WT wsum = W ? group_sum(m, wt) : (WT)__popc(m);
             if (valid && __ffs(m) - 1 == lane)
                 if (!hash_add(keys, vals, T, lg, c, wsum)) atomicOr(&a.st->err, kErrHashOverflow);
         }
         __syncthreads();
-        const int ki = a.K[v], tcur = a.Tot[cur], sf = a.Self[v];
+        const WT ki = a.K[v], tcur = a.Tot[cur], sf = a.Self[v];
         constexpr int NW = BLOCK / 32;
         long long x = -1;
-        int bc = cur, bw = 0, bt = 0, wc = 0;
+        int bc = cur, bt = 0;
+        WT bw = 0, wc = 0;
         scan_table_int(a, sc, keys, vals, T, threadIdx.x, BLOCK, cur, ki, tcur, x, bc, bw, bt, wc);
         warp_merge_int(x, bc, bw, bt, wc, 32);
         if (lane == 0) {
@@ -796,18 +869,19 @@ __global__ void __launch_bounds__(BLOCK) k_decide_cta(DecideArgs a, const int32_
 constexpr int kCtaTable5 = 4096;
 constexpr int kCtaTable6 = 16384;
 
-void p1_decide(const LevelGraph &g, Phase1Buffers &b, int bin, const int32_t *list, const int *count_ptr,
-               int level_count, double constant, long long m2, int fp64_only, int hub_tmax, cudaStream_t st)
+// Arguments of the decide kernels for the weight type WT.
+template <typename WT>
+static DecideArgs<WT> decide_args(const LevelGraph &g, Phase1Buffers &b, double constant, long long m2,
+                                  int fp64_only)
 {
-    if (level_count <= 0) return;
-    DecideArgs a;
+    DecideArgs<WT> a;
     a.offs = g.offs;
     a.nbr = g.nbr;
-    a.w = g.w;
+    a.w = (const WT *)g.w;
     a.comm = b.comm;
-    a.K = b.K;
-    a.Self = b.Self;
-    a.Tot = b.Tot;
+    a.K = (const WT *)b.K;
+    a.Self = (const WT *)b.Self;
+    a.Tot = (const WT *)b.Tot;
     a.size = b.size;
     a.mv_v = b.mv_v;
     a.mv_old = b.mv_old;
@@ -822,6 +896,14 @@ void p1_decide(const LevelGraph &g, Phase1Buffers &b, int bin, const int32_t *li
     a.m2g = b.m2g;
     a.cg = b.cg;
     a.stop = b.gstop;
+    return a;
+}
+
+template <typename WT>
+static void decide_t(const LevelGraph &g, Phase1Buffers &b, int bin, const int32_t *list, const int *count_ptr,
+                     int level_count, double constant, long long m2, int fp64_only, cudaStream_t st)
+{
+    const DecideArgs<WT> a = decide_args<WT>(g, b, constant, m2, fp64_only);
     const bool W = g.w != nullptr;
     const int cap = num_sms() * 8;
     auto grid_lanes = [&](int lanes_per_item) {
@@ -831,10 +913,11 @@ void p1_decide(const LevelGraph &g, Phase1Buffers &b, int bin, const int32_t *li
 #define GALA_DG(GV)                                                                                    \
     do {                                                                                               \
         if (W)                                                                                         \
-            k_decide_group<GV, true><<<grid_lanes(GV), 256, 0, st>>>(a, list, count_ptr);              \
+            k_decide_group<WT, GV, true><<<grid_lanes(GV), 256, 0, st>>>(a, list, count_ptr);          \
         else                                                                                           \
-            k_decide_group<GV, false><<<grid_lanes(GV), 256, 0, st>>>(a, list, count_ptr);             \
+            k_decide_group<WT, GV, false><<<grid_lanes(GV), 256, 0, st>>>(a, list, count_ptr);         \
     } while (0)
+    constexpr size_t slot = sizeof(int) + sizeof(WT);
     switch (bin) {
     case 0: GALA_DG(4); break;
     case 1: GALA_DG(8); break;
@@ -842,58 +925,73 @@ void p1_decide(const LevelGraph &g, Phase1Buffers &b, int bin, const int32_t *li
     case 3: GALA_DG(32); break;
     case 4:
         if (W)
-            k_decide_warp<true><<<grid_lanes(32), 256, 0, st>>>(a, list, count_ptr);
+            k_decide_warp<WT, true><<<grid_lanes(32), 256, 0, st>>>(a, list, count_ptr);
         else
-            k_decide_warp<false><<<grid_lanes(32), 256, 0, st>>>(a, list, count_ptr);
+            k_decide_warp<WT, false><<<grid_lanes(32), 256, 0, st>>>(a, list, count_ptr);
         break;
     case 5: {
         int grid = level_count < num_sms() * 6 ? level_count : num_sms() * 6;
-        size_t sm = (size_t)kCtaTable5 * 2 * sizeof(int);
+        const size_t sm = (size_t)kCtaTable5 * slot;
         if (W)
-            k_decide_cta<256, false, true><<<grid, 256, sm, st>>>(a, list, count_ptr, kCtaTable5, nullptr);
+            k_decide_cta<WT, 256, true><<<grid, 256, sm, st>>>(a, list, count_ptr, kCtaTable5);
         else
-            k_decide_cta<256, false, false><<<grid, 256, sm, st>>>(a, list, count_ptr, kCtaTable5, nullptr);
+            k_decide_cta<WT, 256, false><<<grid, 256, sm, st>>>(a, list, count_ptr, kCtaTable5);
         break;
     }
     case 6: {
         int grid = level_count < num_sms() ? level_count : num_sms();
-        size_t sm = (size_t)kCtaTable6 * 2 * sizeof(int);
+        const size_t sm = (size_t)kCtaTable6 * slot;
         if (W)
-            k_decide_cta<1024, false, true><<<grid, 1024, sm, st>>>(a, list, count_ptr, kCtaTable6, nullptr);
+            k_decide_cta<WT, 1024, true><<<grid, 1024, sm, st>>>(a, list, count_ptr, kCtaTable6);
         else
-            k_decide_cta<1024, false, false><<<grid, 1024, sm, st>>>(a, list, count_ptr, kCtaTable6, nullptr);
+            k_decide_cta<WT, 1024, false><<<grid, 1024, sm, st>>>(a, list, count_ptr, kCtaTable6);
         break;
     }
-    default: {
-        long long grid = level_count < hub_grid_size() ? level_count : hub_grid_size();
-        const long long fit = b.hub_table_slots / (2LL * hub_tmax);
-        if (grid > fit) grid = fit;
-        if (grid < 1) return;  // the caller checked that one table fits
-        if (W)
-            k_decide_cta<1024, true, true><<<grid, 1024, 0, st>>>(a, list, count_ptr, hub_tmax, b.hub_table);
-        else
-            k_decide_cta<1024, true, false><<<grid, 1024, 0, st>>>(a, list, count_ptr, hub_tmax, b.hub_table);
-    }
+    default: return;  // hub vertices: p1_hub_decide
     }
 #undef GALA_DG
     note_launch(1);
 }
 
+void p1_decide(const LevelGraph &g, Phase1Buffers &b, int bin, const int32_t *list, const int *count_ptr,
+               int level_count, double constant, long long m2, int fp64_only, int hub_tmax, cudaStream_t st)
+{
+    (void)hub_tmax;
+    if (level_count <= 0) return;
+    if (g.wide)
+        decide_t<long long>(g, b, bin, list, count_ptr, level_count, constant, m2, fp64_only, st);
+    else
+        decide_t<int>(g, b, bin, list, count_ptr, level_count, constant, m2, fp64_only, st);
+}
+
+template <typename WT>
+static void configure_t()
+{
+    constexpr int slot = (int)(sizeof(int) + sizeof(WT));
+    cudaFuncSetAttribute(k_decide_cta<WT, 1024, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         kCtaTable6 * slot);
+    cudaFuncSetAttribute(k_decide_cta<WT, 1024, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         kCtaTable6 * slot);
+    cudaFuncSetAttribute(k_decide_cta<WT, 256, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         kCtaTable5 * slot);
+    cudaFuncSetAttribute(k_decide_cta<WT, 256, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         kCtaTable5 * slot);
+}
+
 void p1_configure_kernels()
 {
-    cudaFuncSetAttribute(k_decide_cta<1024, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         kCtaTable6 * 2 * (int)sizeof(int));
-    cudaFuncSetAttribute(k_decide_cta<1024, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         kCtaTable6 * 2 * (int)sizeof(int));
+    configure_t<int>();
+    configure_t<long long>();
 }
 
 // ------------------------------------------------------------------------
 // Apply (sign = +1) or revert (sign = -1) the movers of an iteration
 // (Tot += Tot_update, size += size_update, louvain_main_process.cu:949-953).
 // ------------------------------------------------------------------------
+template <typename WT>
 __global__ void k_apply_movers(const int32_t *__restrict__ mv_v, const int32_t *__restrict__ mv_old,
                                const int32_t *__restrict__ mv_new, const DevStats *__restrict__ stp, int sign,
-                               int32_t *comm, int32_t *Tot, int32_t *size, const int32_t *__restrict__ K,
+                               int32_t *comm, WT *Tot, int32_t *size, const WT *__restrict__ K,
                                int32_t *last_move, int iteration)
 {
     const int nm = stp->n_movers;
@@ -901,11 +999,11 @@ __global__ void k_apply_movers(const int32_t *__restrict__ mv_v, const int32_t *
         const int v = mv_v[i];
         const int from = sign > 0 ? mv_old[i] : mv_new[i];
         const int to = sign > 0 ? mv_new[i] : mv_old[i];
-        const int k = K[v];
+        const WT k = K[v];
         comm[v] = to;
         if (last_move && sign > 0) last_move[v] = iteration;
-        atomicAdd(&Tot[to], k);
-        atomicSub(&Tot[from], k);
+        atomic_add_w(&Tot[to], k);
+        atomic_add_w(&Tot[from], (WT)-k);
         atomicAdd(&size[to], 1);
         atomicSub(&size[from], 1);
     }
@@ -917,27 +1015,33 @@ void p1_apply_movers(Phase1Buffers &b, int sign, int n, cudaStream_t st, int ite
     int cap = num_sms() * 4;
     if (grid > cap) grid = cap;
     if (grid < 1) grid = 1;
-    k_apply_movers<<<grid, 256, 0, st>>>(b.mv_v, b.mv_old, b.mv_new, b.stats, sign, b.comm, b.Tot, b.size, b.K,
-                                         b.features_on ? b.last_move : nullptr, iteration);
+    if (b.wide)
+        k_apply_movers<long long><<<grid, 256, 0, st>>>(b.mv_v, b.mv_old, b.mv_new, b.stats, sign, b.comm,
+                                                        (long long *)b.Tot, b.size, (const long long *)b.K, nullptr,
+                                                        iteration);
+    else
+        k_apply_movers<int><<<grid, 256, 0, st>>>(b.mv_v, b.mv_old, b.mv_new, b.stats, sign, b.comm, b.Tot, b.size,
+                                                  b.K, b.features_on ? b.last_move : nullptr, iteration);
     note_launch(1);
 }
 
 // min over non-empty Tot (Tot_op, kernel_functions.cuh:112-121) and sum Tot^2.
-__global__ void k_tot_reduce(const int32_t *__restrict__ Tot, int n, DevStats *st)
+template <typename WT>
+__global__ void k_tot_reduce(const WT *__restrict__ Tot, int n, DevStats *st)
 {
-    int mn = 0x7fffffff;
-    unsigned long long s2 = 0;
+    long long mn = 0x7fffffffffffffffLL;
+    typename SqSum<WT>::T s2 = 0;
     for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x) {
-        int t = Tot[c];
+        const WT t = Tot[c];
         if (t != 0) {
-            mn = min(mn, t);
-            s2 += (unsigned long long)((long long)t * t);
+            mn = min(mn, (long long)t);
+            s2 += SqSum<WT>::sq(t);
         }
     }
 #pragma unroll
     for (int o = 16; o >= 1; o >>= 1) mn = min(mn, __shfl_xor_sync(GALA_FULL_MASK, mn, o));
-    if ((threadIdx.x & 31) == 0 && mn != 0x7fffffff) atomicMin(&st->min_tot, mn);
-    block_add_u64(s2, &st->sum_tot2);
+    if ((threadIdx.x & 31) == 0 && mn != 0x7fffffffffffffffLL) atomicMin(&st->min_tot, mn);
+    SqSum<WT>::add(s2, st);
 }
 
 void p1_tot_reduce(Phase1Buffers &b, int n, cudaStream_t st)
@@ -946,22 +1050,26 @@ void p1_tot_reduce(Phase1Buffers &b, int n, cudaStream_t st)
     int cap = num_sms() * 4;
     if (grid > cap) grid = cap;
     if (grid < 1) grid = 1;
-    k_tot_reduce<<<grid, 1024, 0, st>>>(b.Tot, n, b.stats);
+    if (b.wide)
+        k_tot_reduce<long long><<<grid, 1024, 0, st>>>((const long long *)b.Tot, n, b.stats);
+    else
+        k_tot_reduce<int><<<grid, 1024, 0, st>>>(b.Tot, n, b.stats);
     note_launch(1);
 }
 
-__global__ void k_iter_reset(DevStats *st, int next, int min_tot_init)
+__global__ void k_iter_reset(DevStats *st, int next, long long min_tot_init)
 {
     st->n_movers = 0;
     st->sum_in = 0;
     st->sum_tot2 = 0;
+    st->sum_tot2_hi = 0;
     st->min_tot = min_tot_init;
     st->act_edges[next] = 0;
     st->act_vertices[next] = 0;
     for (int i = 0; i < kNumBins; ++i) st->act_count[next][i] = 0;
 }
 
-void p1_iter_reset(Phase1Buffers &b, int next, int min_tot_init, cudaStream_t st)
+void p1_iter_reset(Phase1Buffers &b, int next, long long min_tot_init, cudaStream_t st)
 {
     k_iter_reset<<<1, 1, 0, st>>>(b.stats, next, min_tot_init);
     note_launch(1);
@@ -972,15 +1080,16 @@ void p1_iter_reset(Phase1Buffers &b, int next, int min_tot_init, cudaStream_t st
 // kernel_functions.cu:890-1034): In[v] over the new labels, the pruning
 // bound, next active lists, sum of In.
 // ------------------------------------------------------------------------
+template <typename WT>
 struct UpdateArgs {
     const int64_t *__restrict__ offs;
     const int32_t *__restrict__ nbr;
-    const int32_t *__restrict__ w;
+    const WT *__restrict__ w;
     const int32_t *__restrict__ comm;
-    const int32_t *__restrict__ K;
-    const int32_t *__restrict__ Self;
-    const int32_t *__restrict__ Tot;
-    int32_t *In;
+    const WT *__restrict__ K;
+    const WT *__restrict__ Self;
+    const WT *__restrict__ Tot;
+    WT *In;
     uint8_t *act_flag;  // per-vertex copy of the next active set
     int32_t *act_list;  // next active list, segment of this bin
     int *act_counter;
@@ -1001,10 +1110,11 @@ struct UpdateArgs {
 struct PruneScale {
     long long m2;
     double c;
-    int min_tot;
+    long long min_tot;
     bool stop;
 };
-__device__ __forceinline__ PruneScale prune_scale(const UpdateArgs &a, int v, int min_tot)
+template <typename WT>
+__device__ __forceinline__ PruneScale prune_scale(const UpdateArgs<WT> &a, int v, long long min_tot)
 {
     if (a.gid) {
         const int g = a.gid[v];
@@ -1013,14 +1123,14 @@ __device__ __forceinline__ PruneScale prune_scale(const UpdateArgs &a, int v, in
     return PruneScale{a.m2, a.constant, min_tot, false};
 }
 
-template <int G, bool W>
-__global__ void __launch_bounds__(256) k_update_group(UpdateArgs a, const int32_t *__restrict__ list, int count)
+template <typename WT, int G, bool W>
+__global__ void __launch_bounds__(256) k_update_group(UpdateArgs<WT> a, const int32_t *__restrict__ list, int count)
 {
     const int lane = threadIdx.x & 31, sub = lane & (G - 1), gw = lane / G;
     constexpr int GPW = 32 / G;
     const int wg = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int nw = (gridDim.x * blockDim.x) >> 5;
-    const int min_tot = a.st->min_tot;
+    const long long min_tot = a.st->min_tot;
     unsigned long long s_in = 0, s_edges = 0;
     int s_act = 0;
     for (int base = wg * GPW; base < count; base += nw * GPW) {
@@ -1039,7 +1149,7 @@ __global__ void __launch_bounds__(256) k_update_group(UpdateArgs a, const int32_
             e = a.offs[v + 1];
             cur = a.comm[v];
         }
-        int sum = 0;
+        WT sum = 0;
         for (long long j = s + sub; j < e; j += G)
             if (a.comm[a.nbr[j]] == cur) sum += W ? a.w[j] : 1;
 #pragma unroll
@@ -1048,8 +1158,8 @@ __global__ void __launch_bounds__(256) k_update_group(UpdateArgs a, const int32_
         if (ps.stop && sub == 0) a.act_flag[v] = 0;
         if (has && sub == 0) {
             a.In[v] = sum;
-            const int ki = a.K[v];
-            active = !prune_bound_fast(sum, a.Self[v], ki, ps.min_tot, a.Tot[cur], ps.c, ps.m2);
+            const WT ki = a.K[v];
+            active = !prune_bound_fast<WT>(sum, a.Self[v], ki, (WT)ps.min_tot, a.Tot[cur], ps.c, ps.m2);
             a.act_flag[v] = active;
             s_in += (unsigned long long)sum;
             if (active) {
@@ -1064,11 +1174,11 @@ __global__ void __launch_bounds__(256) k_update_group(UpdateArgs a, const int32_
     block_add_i32(s_act, &a.st->act_vertices[a.next]);
 }
 
-template <bool W>
-__global__ void __launch_bounds__(256) k_update_cta(UpdateArgs a, const int32_t *__restrict__ list, int count)
+template <typename WT, bool W>
+__global__ void __launch_bounds__(256) k_update_cta(UpdateArgs<WT> a, const int32_t *__restrict__ list, int count)
 {
-    __shared__ int red[8];
-    const int min_tot = a.st->min_tot;
+    __shared__ WT red[8];
+    const long long min_tot = a.st->min_tot;
     unsigned long long s_in = 0, s_edges = 0;
     int s_act = 0;
     for (int i = blockIdx.x; i < count; i += gridDim.x) {
@@ -1080,7 +1190,7 @@ __global__ void __launch_bounds__(256) k_update_cta(UpdateArgs a, const int32_t 
         }
         const long long s = a.offs[v], e = a.offs[v + 1];
         const int cur = a.comm[v];
-        int sum = 0;
+        WT sum = 0;
         for (long long j = s + threadIdx.x; j < e; j += blockDim.x)
             if (a.comm[a.nbr[j]] == cur) sum += W ? a.w[j] : 1;
         sum = warp_sum(sum);
@@ -1090,8 +1200,8 @@ __global__ void __launch_bounds__(256) k_update_cta(UpdateArgs a, const int32_t 
             sum = 0;
             for (int q = 0; q < (int)(blockDim.x >> 5); ++q) sum += red[q];
             a.In[v] = sum;
-            const int ki = a.K[v];
-            bool active = !prune_bound_fast(sum, a.Self[v], ki, ps.min_tot, a.Tot[cur], ps.c, ps.m2);
+            const WT ki = a.K[v];
+            bool active = !prune_bound_fast<WT>(sum, a.Self[v], ki, (WT)ps.min_tot, a.Tot[cur], ps.c, ps.m2);
             a.act_flag[v] = active;
             s_in += (unsigned long long)sum;
             if (active) {
@@ -1107,19 +1217,19 @@ __global__ void __launch_bounds__(256) k_update_cta(UpdateArgs a, const int32_t 
     block_add_i32(s_act, &a.st->act_vertices[a.next]);
 }
 
-void p1_update(const LevelGraph &g, Phase1Buffers &b, int bin, const int32_t *list, int count, int next,
-               int bin_start, double constant, long long m2, cudaStream_t st)
+template <typename WT>
+static void update_t(const LevelGraph &g, Phase1Buffers &b, int bin, const int32_t *list, int count, int next,
+                     int bin_start, double constant, long long m2, cudaStream_t st)
 {
-    if (count <= 0) return;
-    UpdateArgs a;
+    UpdateArgs<WT> a;
     a.offs = g.offs;
     a.nbr = g.nbr;
-    a.w = g.w;
+    a.w = (const WT *)g.w;
     a.comm = b.comm;
-    a.K = b.K;
-    a.Self = b.Self;
-    a.Tot = b.Tot;
-    a.In = b.In;
+    a.K = (const WT *)b.K;
+    a.Self = (const WT *)b.Self;
+    a.Tot = (const WT *)b.Tot;
+    a.In = (WT *)b.In;
     a.act_flag = b.act_flag;
     a.act_list = b.act[next] + bin_start;
     a.act_counter = &b.stats->act_count[next][bin];
@@ -1141,9 +1251,9 @@ void p1_update(const LevelGraph &g, Phase1Buffers &b, int bin, const int32_t *li
 #define GALA_UG(GV)                                                                                    \
     do {                                                                                               \
         if (W)                                                                                         \
-            k_update_group<GV, true><<<grid_lanes(GV), 256, 0, st>>>(a, list, count);                  \
+            k_update_group<WT, GV, true><<<grid_lanes(GV), 256, 0, st>>>(a, list, count);              \
         else                                                                                           \
-            k_update_group<GV, false><<<grid_lanes(GV), 256, 0, st>>>(a, list, count);                 \
+            k_update_group<WT, GV, false><<<grid_lanes(GV), 256, 0, st>>>(a, list, count);             \
     } while (0)
     switch (bin) {
     case 0: GALA_UG(4); break;
@@ -1155,13 +1265,23 @@ void p1_update(const LevelGraph &g, Phase1Buffers &b, int bin, const int32_t *li
     default: {
         int grid = count < cap ? count : cap;
         if (W)
-            k_update_cta<true><<<grid, 256, 0, st>>>(a, list, count);
+            k_update_cta<WT, true><<<grid, 256, 0, st>>>(a, list, count);
         else
-            k_update_cta<false><<<grid, 256, 0, st>>>(a, list, count);
+            k_update_cta<WT, false><<<grid, 256, 0, st>>>(a, list, count);
     }
     }
 #undef GALA_UG
     note_launch(1);
+}
+
+void p1_update(const LevelGraph &g, Phase1Buffers &b, int bin, const int32_t *list, int count, int next,
+               int bin_start, double constant, long long m2, cudaStream_t st)
+{
+    if (count <= 0) return;
+    if (g.wide)
+        update_t<long long>(g, b, bin, list, count, next, bin_start, constant, m2, st);
+    else
+        update_t<int>(g, b, bin, list, count, next, bin_start, constant, m2, st);
 }
 
 // ------------------------------------------------------------------------
@@ -1205,8 +1325,15 @@ __global__ void k_hub_work(HubPlan p)
     }
 }
 
-template <bool W>
-__global__ void __launch_bounds__(256) k_hub_insert(DecideArgs a, HubPlan p, const uint8_t *__restrict__ flag)
+// Values of a hub table (WT per slot, after the keys of all tables).
+template <typename WT>
+__device__ __forceinline__ WT *hub_vals(const HubPlan &p, long long i)
+{
+    return (WT *)(p.pool + p.half) + p.toff[i];
+}
+
+template <typename WT, bool W>
+__global__ void __launch_bounds__(256) k_hub_insert(DecideArgs<WT> a, HubPlan p, const uint8_t *__restrict__ flag)
 {
     const int lane = threadIdx.x & 31;
     for (long long wi = blockIdx.x; wi < p.nwork; wi += gridDim.x) {
@@ -1219,17 +1346,18 @@ __global__ void __launch_bounds__(256) k_hub_insert(DecideArgs a, HubPlan p, con
         const int T = (int)p.T[i];
         const int lg = __ffs(T) - 1;
         int *keys = p.pool + p.toff[i];
-        int *vals = p.pool + p.half + p.toff[i];
+        WT *vals = hub_vals<WT>(p, i);
         for (long long b0 = s; b0 < e2; b0 += blockDim.x) {
             const long long j = b0 + threadIdx.x;
             const bool valid = j < e2;
-            int c = -1, wt = 0;
+            int c = -1;
+            WT wt = 0;
             if (valid) {
                 c = a.comm[a.nbr[j]];
                 wt = W ? a.w[j] : 1;
             }
             const unsigned m = __match_any_sync(GALA_FULL_MASK, c);
-            const int wsum = W ? (int)__reduce_add_sync(m, (unsigned)wt) : __popc(m);
+            const WT wsum = W ? group_sum(m, wt) : (WT)__popc(m);
             if (valid && __ffs(m) - 1 == lane)
                 if (!hash_add(keys, vals, T, lg, c, wsum)) atomicOr(&a.st->err, kErrHashOverflow);
         }
@@ -1238,30 +1366,37 @@ __global__ void __launch_bounds__(256) k_hub_insert(DecideArgs a, HubPlan p, con
 
 // FP64 evaluation needed whatever the candidates: K*m2 out of the range where
 // the integer order equals the FP64 order (or FP64 forced).
-__device__ __forceinline__ bool needs_fp64(const DecideArgs &a, const Scale &sc, int ki)
+template <typename WT>
+__device__ __forceinline__ bool needs_fp64(const DecideArgs<WT> &a, const Scale &sc, WT ki)
 {
+    if constexpr (!WideOf<WT>::exact) return true;
     return a.fp64_only || (long long)ki * sc.m2 >= (1LL << 49);
 }
 
-__global__ void __launch_bounds__(256) k_hub_scan(DecideArgs a, HubPlan p, const uint8_t *__restrict__ flag)
+template <typename WT>
+__global__ void __launch_bounds__(256) k_hub_scan(DecideArgs<WT> a, HubPlan p, const uint8_t *__restrict__ flag)
 {
     __shared__ long long r_x[8];
     __shared__ double r_dq[8];
-    __shared__ int r_c[8], r_w[8], r_t[8], r_wc[8];
+    __shared__ int r_c[8], r_t[8];
+    __shared__ WT r_w[8], r_wc[8];
+    WT *pw = (WT *)p.pw, *pwc = (WT *)p.pwc;
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     for (long long wi = blockIdx.x; wi < p.ntwork; wi += gridDim.x) {
         const int i = p.twork[wi];
         const int v = p.hubs[i];
         if (!flag[v] || stopped(a, v)) continue;
         const Scale sc = scale_of(a, v);
-        const int cur = a.comm[v], ki = a.K[v], tcur = a.Tot[cur];
+        const int cur = a.comm[v];
+        const WT ki = a.K[v], tcur = a.Tot[cur];
         const long long j0 = (wi - p.tcoff[i]) * kHubChunk;
         const long long T = p.T[i];
         const long long j1 = j0 + kHubChunk < T ? j0 + kHubChunk : T;
         const int *keys = p.pool + p.toff[i];
-        const int *vals = p.pool + p.half + p.toff[i];
+        const WT *vals = hub_vals<WT>(p, i);
         long long x = -1;
-        int bc = cur, bw = 0, bt = 0, wc = 0;
+        int bc = cur, bt = 0;
+        WT bw = 0, wc = 0;
         scan_table_int(a, sc, keys + j0, vals + j0, (int)(j1 - j0), threadIdx.x, blockDim.x, cur, ki, tcur, x, bc,
                        bw, bt, wc);
         warp_merge_int(x, bc, bw, bt, wc, 32);
@@ -1284,9 +1419,9 @@ __global__ void __launch_bounds__(256) k_hub_scan(DecideArgs a, HubPlan p, const
             if (lane == 0) {
                 p.px[wi] = x;
                 p.pc[wi] = bc;
-                p.pw[wi] = bw;
+                pw[wi] = bw;
                 p.pt[wi] = bt;
-                p.pwc[wi] = wc;
+                pwc[wi] = wc;
             }
         }
         __syncthreads();
@@ -1315,8 +1450,10 @@ __global__ void __launch_bounds__(256) k_hub_scan(DecideArgs a, HubPlan p, const
     }
 }
 
-__global__ void __launch_bounds__(256) k_hub_final(DecideArgs a, HubPlan p, const uint8_t *__restrict__ flag)
+template <typename WT>
+__global__ void __launch_bounds__(256) k_hub_final(DecideArgs<WT> a, HubPlan p, const uint8_t *__restrict__ flag)
 {
+    const WT *pw = (const WT *)p.pw, *pwc = (const WT *)p.pwc;
     const int lane = threadIdx.x & 31;
     const int wg = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int nw = (gridDim.x * blockDim.x) >> 5;
@@ -1324,12 +1461,14 @@ __global__ void __launch_bounds__(256) k_hub_final(DecideArgs a, HubPlan p, cons
         const int v = p.hubs[i];
         if (!flag[v] || stopped(a, v)) continue;
         const Scale sc = scale_of(a, v);
-        const int cur = a.comm[v], ki = a.K[v], sf = a.Self[v], tcur = a.Tot[cur];
+        const int cur = a.comm[v];
+        const WT ki = a.K[v], sf = a.Self[v], tcur = a.Tot[cur];
         long long x = -1;
-        int bc = cur, bw = 0, bt = 0, wc = 0;
+        int bc = cur, bt = 0;
+        WT bw = 0, wc = 0;
         for (long long q = p.tcoff[i] + lane; q < p.tcoff[i + 1]; q += 32) {
-            wc += p.pwc[q];
-            if (p.px[q] >= 0) cand_merge(x, bc, bw, bt, p.px[q], p.pc[q], p.pw[q], p.pt[q]);
+            wc += pwc[q];
+            if (p.px[q] >= 0) cand_merge(x, bc, bw, bt, p.px[q], p.pc[q], pw[q], p.pt[q]);
         }
         warp_merge_int(x, bc, bw, bt, wc, 32);
         int dec = int_decision(a, sc, x, bt, cur, bc, wc, sf, ki);  // warp-uniform
@@ -1343,8 +1482,8 @@ __global__ void __launch_bounds__(256) k_hub_final(DecideArgs a, HubPlan p, cons
                         fc = p.pfc[q];
                     }
             } else {  // rare rounding cases: rescan the table in FP64
-                scan_table(a, sc, p.pool + p.toff[i], p.pool + p.half + p.toff[i], (int)p.T[i], lane, 32, cur, ki,
-                           tcur, dq, fc);
+                scan_table(a, sc, p.pool + p.toff[i], hub_vals<WT>(p, i), (int)p.T[i], lane, 32, cur, ki, tcur, dq,
+                           fc);
             }
             warp_argmax(dq, fc);
             bc = fc;
@@ -1375,44 +1514,35 @@ void p1_hub_work_launch(HubPlan &p, cudaStream_t st)
     note_launch(1);
 }
 
-// One iteration's decide-and-move of the hub bin.
+template <typename WT>
+static void hub_decide_t(const LevelGraph &g, Phase1Buffers &b, const HubPlan &p, double constant, long long m2,
+                         int fp64_only, cudaStream_t st)
+{
+    const DecideArgs<WT> a = decide_args<WT>(g, b, constant, m2, fp64_only);
+    const int cap = num_sms() * 8;
+    cudaMemsetAsync(p.pool, 0xff, (size_t)p.half * sizeof(int32_t), st);
+    cudaMemsetAsync(p.pool + p.half, 0, (size_t)p.half * sizeof(WT), st);
+    const int g1 = (int)(p.nwork < cap ? p.nwork : cap);
+    if (g.w)
+        k_hub_insert<WT, true><<<g1, 256, 0, st>>>(a, p, b.act_flag);
+    else
+        k_hub_insert<WT, false><<<g1, 256, 0, st>>>(a, p, b.act_flag);
+    k_hub_scan<WT><<<(int)(p.ntwork < cap ? p.ntwork : cap), 256, 0, st>>>(a, p, b.act_flag);
+    k_hub_final<WT><<<(p.H * 32 + 255) / 256, 256, 0, st>>>(a, p, b.act_flag);
+    note_launch(3);
+}
+
+// One iteration's decide-and-move of the hub bin.  The values of the hub
+// tables follow all keys: p.half int32 keys, then p.half values of the
+// weight type (the caller sized the pool for it).
 void p1_hub_decide(const LevelGraph &g, Phase1Buffers &b, const HubPlan &p, double constant, long long m2,
                    int fp64_only, cudaStream_t st)
 {
     if (p.H <= 0) return;
-    DecideArgs a;
-    a.offs = g.offs;
-    a.nbr = g.nbr;
-    a.w = g.w;
-    a.comm = b.comm;
-    a.K = b.K;
-    a.Self = b.Self;
-    a.Tot = b.Tot;
-    a.size = b.size;
-    a.mv_v = b.mv_v;
-    a.mv_old = b.mv_old;
-    a.mv_new = b.mv_new;
-    a.st = b.stats;
-    a.constant = constant;
-    a.m2 = m2;
-    a.fp64_only = fp64_only;
-    a.feat_gain = b.features_on ? b.feat_gain : nullptr;
-    a.feat_ndist = b.feat_ndist;
-    a.gid = b.gid;
-    a.m2g = b.m2g;
-    a.cg = b.cg;
-    a.stop = b.gstop;
-    const int cap = num_sms() * 8;
-    cudaMemsetAsync(p.pool, 0xff, (size_t)p.half * sizeof(int32_t), st);
-    cudaMemsetAsync(p.pool + p.half, 0, (size_t)p.half * sizeof(int32_t), st);
-    const int g1 = (int)(p.nwork < cap ? p.nwork : cap);
-    if (g.w)
-        k_hub_insert<true><<<g1, 256, 0, st>>>(a, p, b.act_flag);
+    if (g.wide)
+        hub_decide_t<long long>(g, b, p, constant, m2, fp64_only, st);
     else
-        k_hub_insert<false><<<g1, 256, 0, st>>>(a, p, b.act_flag);
-    k_hub_scan<<<(int)(p.ntwork < cap ? p.ntwork : cap), 256, 0, st>>>(a, p, b.act_flag);
-    k_hub_final<<<(p.H * 32 + 255) / 256, 256, 0, st>>>(a, p, b.act_flag);
-    note_launch(3);
+        hub_decide_t<int>(g, b, p, constant, m2, fp64_only, st);
 }
 
 }  // namespace gala

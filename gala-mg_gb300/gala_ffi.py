@@ -26,7 +26,8 @@ EXPORTS = ["gala_last_error", "gala_status_string", "gala_kernel_launch_count", 
            "gala_modularity_host", "gala_modularity_device_static", "gala_proposal_create",
            "gala_proposal_destroy", "gala_proposal_get_params", "gala_proposal_set_params", "gala_proposal_samples",
            "gala_proposal_clear_samples", "gala_proposal_read_samples", "gala_proposal_gradient",
-           "gala_proposal_logits", "gala_proposal_train", "gala_louvain_batch", "gala_generate_sbm_batch"]
+           "gala_proposal_logits", "gala_proposal_train", "gala_louvain_batch", "gala_generate_sbm_batch",
+           "gala_graph_from_csr_f32", "gala_graph_weights_f32", "gala_generate_lfr"]
 
 PROPOSAL_OFF, PROPOSAL_TRACE, PROPOSAL_SKIP = 0, 1, 2
 PROPOSAL_PARAMS = 32 * 8 + 32 + 32 * 32 + 32 + 32 + 1
@@ -159,6 +160,14 @@ def load(path=LIB_PATH):
                                           ctypes.c_int32, ctypes.c_double, ctypes.c_double, ctypes.c_double,
                                           ctypes.c_double, ctypes.c_uint64, ctypes.c_int32, ctypes.POINTER(_vp)]
     L.gala_louvain_batch.restype = ctypes.c_int
+    L.gala_graph_from_csr_f32.argtypes = [ctypes.c_int32, _i64p, _i32p, _f32p, ctypes.POINTER(_vp)]
+    L.gala_graph_from_csr_f32.restype = ctypes.c_int
+    L.gala_graph_weights_f32.argtypes = [_vp, ctypes.POINTER(_f32p)]
+    L.gala_graph_weights_f32.restype = ctypes.c_int
+    L.gala_generate_lfr.argtypes = [ctypes.c_int32, ctypes.c_double, ctypes.c_int32, ctypes.c_int32, ctypes.c_double,
+                                    ctypes.c_int32, ctypes.c_int32, ctypes.c_double, ctypes.c_int32, ctypes.c_uint64,
+                                    ctypes.c_int32, ctypes.POINTER(_vp)]
+    L.gala_generate_lfr.restype = ctypes.c_int
     L.gala_generate_sbm_batch.restype = ctypes.c_int
     for name in ["gala_proposal_create", "gala_proposal_get_params", "gala_proposal_set_params",
                  "gala_proposal_samples", "gala_proposal_clear_samples", "gala_proposal_read_samples",
@@ -245,6 +254,27 @@ class Graph:
         return Graph(h)
 
     @staticmethod
+    def from_csr_f32(offs, nbr, wf):
+        """Float-weight graph; offs with a leading 0."""
+        offs = np.ascontiguousarray(offs, dtype=np.int64)
+        incl = np.ascontiguousarray(offs[1:])
+        nbr = np.ascontiguousarray(nbr, dtype=np.int32)
+        wf = np.ascontiguousarray(wf, dtype=np.float32)
+        h = _vp()
+        _check(load().gala_graph_from_csr_f32(len(incl), _ptr(incl, _i64p), _ptr(nbr, _i32p),
+                                              _ptr(wf, ctypes.POINTER(ctypes.c_float)), ctypes.byref(h)))
+        return Graph(h)
+
+    @staticmethod
+    def lfr(n, tau1=2.5, dmin=4, dmax=20000, tau2=1.5, cmin=20, cmax=50000, mu=0.3, float_weights=True, seed=0,
+            nthreads=0):
+        """gala_generate_lfr: LFR-style planted graph (lognormal float weights)."""
+        h = _vp()
+        _check(load().gala_generate_lfr(n, tau1, dmin, dmax, tau2, cmin, cmax, mu, int(float_weights), seed, nthreads,
+                                        ctypes.byref(h)))
+        return Graph(h)
+
+    @staticmethod
     def sbm_batch(count, n_min=200, n_max=200000, k_min=8, k_max=64, deg_min=12.0, deg_max=40.0, mix_min=0.1,
                   mix_max=0.4, seed=0, nthreads=0):
         """gala_generate_sbm_batch: `count` planted-partition graphs."""
@@ -269,7 +299,7 @@ class Graph:
     def info(self):
         n, e, w = ctypes.c_int32(), ctypes.c_int64(), ctypes.c_int32()
         _check(load().gala_graph_info(self.h, ctypes.byref(n), ctypes.byref(e), ctypes.byref(w)))
-        return n.value, e.value, bool(w.value)
+        return n.value, e.value, w.value  # 0 unweighted, 1 int32, 2 float32 weights
 
     def arrays(self):
         """(offs[n+1] with leading 0, nbr, w or None) as numpy copies."""
@@ -279,8 +309,17 @@ class Graph:
         offs = np.zeros(n + 1, dtype=np.int64)
         offs[1:] = np.ctypeslib.as_array(po, shape=(n,))
         nbr = np.ctypeslib.as_array(pn, shape=(e,)).copy() if e else np.zeros(0, np.int32)
-        w = np.ctypeslib.as_array(pw, shape=(e,)).copy() if (weighted and e) else None
+        w = np.ctypeslib.as_array(pw, shape=(e,)).copy() if (weighted == 1 and e) else None
         return offs, nbr, w
+
+    def weights_f32(self):
+        """Float weights (numpy copy) of a float-weight graph, else None."""
+        n, e, weighted = self.info()
+        if weighted != 2:
+            return None
+        p = ctypes.POINTER(ctypes.c_float)()
+        _check(load().gala_graph_weights_f32(self.h, ctypes.byref(p)))
+        return np.ctypeslib.as_array(p, shape=(e,)).copy() if e else np.zeros(0, np.float32)
 
     def modularity(self, labels):
         labels = np.ascontiguousarray(labels, dtype=np.int32)

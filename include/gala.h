@@ -139,8 +139,22 @@ gala_status gala_graph_from_text(const char *path, int32_t weighted, int32_t nth
 gala_status gala_graph_from_csr(int32_t n, const int64_t *offsets_inclusive,
                                 const int32_t *neighbors, const int32_t *weights,
                                 gala_graph **out);
+/* weighted: 0 = unweighted, 1 = int32 weights, 2 = float32 weights. */
 gala_status gala_graph_info(const gala_graph *g, int32_t *n, int64_t *num_entries,
                             int32_t *weighted);
+/* Float-weight graphs (no counterpart in the reference, whose weights are
+ * int32): weights must be positive and finite.  The engine holds them as
+ * exact 64-bit fixed-point integers round(w * 2^S) (S chosen from the total
+ * weight so that it stays below 2^62), accumulates K, Tot, In and contracted
+ * weights exactly in those integers and evaluates every gain and the pruning
+ * bound with the FP64 expressions.  Results repeat bit-exactly; modularity is
+ * reported from the fixed-point sums.  gala_graph_load_bin / store_bin with
+ * weighted = 2 read / write the .bin layout with a float32 weight block. */
+gala_status gala_graph_from_csr_f32(int32_t n, const int64_t *offsets_inclusive,
+                                    const int32_t *neighbors, const float *weights,
+                                    gala_graph **out);
+/* Borrow the float weights (NULL for graphs without float weights). */
+gala_status gala_graph_weights_f32(const gala_graph *g, const float **weights);
 /* Borrow the host arrays (reference layout).  Valid until destroy. */
 gala_status gala_graph_arrays(const gala_graph *g, const int64_t **offsets_inclusive,
                               const int32_t **neighbors, const int32_t **weights);
@@ -160,6 +174,16 @@ gala_status gala_generate_sbm(int32_t n, int32_t k, double p_in, double p_out,
 gala_status gala_generate_sbm_batch(int32_t count, int32_t n_min, int32_t n_max, int32_t k_min,
                                     int32_t k_max, double deg_min, double deg_max, double mix_min,
                                     double mix_max, uint64_t seed, int32_t nthreads, gala_graph **out);
+/* LFR-style planted graph (no counterpart in the reference): n vertices,
+ * degrees power-law with exponent tau1 on [dmin, dmax], community sizes
+ * power-law with exponent tau2 on [cmin, cmax], mixing mu (a fraction 1 - mu
+ * of every vertex's edges inside its community), configuration-model
+ * pairing, self-loops dropped, parallel edges merged.  float_weights = 1
+ * gives lognormal(0, 1) float32 weights (parallel edges sum), 0 no weights.
+ * Depends only on the arguments, not on nthreads. */
+gala_status gala_generate_lfr(int32_t n, double tau1, int32_t dmin, int32_t dmax, double tau2,
+                              int32_t cmin, int32_t cmax, double mu, int32_t float_weights,
+                              uint64_t seed, int32_t nthreads, gala_graph **out);
 /* R-MAT with 2^scale ids and `edges` raw undirected samples; duplicates and
  * self-loops removed, ids without edges dropped and renumbered in order.
  * noise > 0 perturbs a, b, c, d independently by a factor in

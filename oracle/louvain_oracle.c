@@ -13,11 +13,20 @@
  *
  * Compile with -ffp-contract=off: the FP64 expressions below must round
  * exactly as written (no fused multiply-add), like the engine's kernels.
+ *
+ * Weights are held as int64 internally: the reference's int32 weights
+ * promote exactly, and float-weight graphs (no counterpart in the reference)
+ * enter as 64-bit fixed-point integers (orc_fixed_shift / orc_fixed_weights),
+ * the representation the engine uses for them.  Sums of Tot^2 are exact in
+ * 128 bits.
  */
 #include "oracle.h"
 
+#include <math.h>
 #include <stdlib.h>
 #include <string.h>
+
+typedef unsigned __int128 u128;
 #ifdef _OPENMP
 #include <omp.h>
 #endif
@@ -30,40 +39,82 @@ double orc_q_from_sums(int64_t sum_in, int64_t sum_tot2, int64_t m2)
     return (double)sum_in * c - (double)sum_tot2 * c * c;
 }
 
+/* The same with a 128-bit sum of Tot^2 given as (hi, lo) words, converted
+ * as hi * 2^64 + lo (the engine's host code uses the same expression). */
+double orc_q_from_sums128(int64_t sum_in, uint64_t tot2_lo, uint64_t tot2_hi, int64_t m2)
+{
+    double c = 1.0 / (double)m2;
+    double t2 = (double)tot2_hi * 18446744073709551616.0 + (double)tot2_lo;
+    return (double)sum_in * c - t2 * c * c;
+}
+
+static double q_of(int64_t sum_in, u128 sum_tot2, int64_t m2)
+{
+    return orc_q_from_sums128(sum_in, (uint64_t)sum_tot2, (uint64_t)(sum_tot2 >> 64), m2);
+}
+
+/* Fixed-point shift S of a float-weight graph: the weights are held as
+ * round(w * 2^S) in int64 with S = 61 - e, 2^e >= sum(w) (frexp), capped to
+ * [0, 40], so the total stays below 2^62.  The sum runs in entry order.
+ * Returns -1 when a weight is not positive and finite or rounds to 0. */
+int32_t orc_fixed_shift(const float *w, int64_t E)
+{
+    double sum = 0, mn = INFINITY;
+    for (int64_t e = 0; e < E; ++e) {
+        const double x = (double)w[e];
+        if (!(x > 0) || !isfinite(x)) return -1;
+        sum += x;
+        if (x < mn) mn = x;
+    }
+    int ex = 0;
+    frexp(sum > 0 ? sum : 1.0, &ex);
+    int s = 61 - ex;
+    if (s > 40) s = 40;
+    if (s < 0) s = 0;
+    if (E > 0 && llrint(mn * ldexp(1.0, s)) <= 0) return -1;
+    return s;
+}
+
+void orc_fixed_weights(const float *w, int64_t E, int32_t shift, int64_t *out)
+{
+    const double scale = ldexp(1.0, shift);
+    for (int64_t e = 0; e < E; ++e) out[e] = llrint((double)w[e] * scale);
+}
+
 /* Gain of moving a vertex into community cn before the correction for the
  * vertex's own community: kernel_functions.cu:136 / :362 (same order of the
  * FP64 operations). */
-static inline double dq_of(int32_t w_to_c, int32_t ki, int32_t tot_c, int32_t tot_cur,
+static inline double dq_of(int64_t w_to_c, int64_t ki, int64_t tot_c, int64_t tot_cur,
                            double constant)
 {
     return 2.0 * (double)w_to_c - 2.0 * (double)ki * ((double)tot_c - (double)tot_cur + (double)ki) * constant;
 }
 
 typedef struct {
-    int32_t *acc;     /* dense per-community weight accumulator, zero between uses */
+    int64_t *acc;     /* dense per-community weight accumulator, zero between uses */
     int32_t *touched; /* communities with acc != 0 */
 } scratch_t;
 
 /* Decide one vertex: kernel_functions.cu:289-441 (degree < 32),
  * :473-593 (degree 32-128), :640-813 (degree >= 129).  Returns the new label. */
-static int32_t decide_vertex(int32_t v, const int64_t *offs, const int32_t *nbr, const int32_t *w,
-                             const int32_t *prev, const int32_t *K, const int32_t *Self,
-                             const int32_t *Tot, const int32_t *size, double constant,
+static int32_t decide_vertex(int32_t v, const int64_t *offs, const int32_t *nbr, const int64_t *w,
+                             const int32_t *prev, const int64_t *K, const int64_t *Self,
+                             const int64_t *Tot, const int32_t *size, double constant,
                              scratch_t *s)
 {
     int32_t cur = prev[v];
-    int32_t ki = K[v];
+    int64_t ki = K[v];
     int32_t nt = 0;
     /* aggregate w(v, c) over neighbour communities (the hash tables of
      * insert_neighbor_com_info, kernel_functions.cu:102-221, or the shuffle
      * sum of :321-335) */
     for (int64_t e = offs[v]; e < offs[v + 1]; ++e) {
         int32_t c = prev[nbr[e]];
-        int32_t wt = w ? w[e] : 1;
+        int64_t wt = w ? w[e] : 1;
         if (s->acc[c] == 0) s->touched[nt++] = c;
         s->acc[c] += wt;
     }
-    int32_t w_cur = s->acc[cur]; /* find_neighbor_com_info(cur_com), :513 / :684 */
+    int64_t w_cur = s->acc[cur]; /* find_neighbor_com_info(cur_com), :513 / :684 */
     /* argmax with ties to the lowest id; only gains > 0 compete with the
      * initial state (0, cur): :136-142 and :366-379 */
     double maxdq = 0.0;
@@ -89,9 +140,9 @@ static int32_t decide_vertex(int32_t v, const int64_t *offs, const int32_t *nbr,
     return cur;
 }
 
-int32_t orc_phase1(int32_t n, const int64_t *offs, const int32_t *nbr, const int32_t *w,
-                   int64_t m2, double min_mod, int32_t *labels_out, double *q_out,
-                   double *iter_q, int32_t iter_cap, int32_t *n_iter_q, int32_t nthreads)
+static int32_t phase1_w64(int32_t n, const int64_t *offs, const int32_t *nbr, const int64_t *w,
+                          int64_t m2, double min_mod, int32_t *labels_out, double *q_out,
+                          double *iter_q, int32_t iter_cap, int32_t *n_iter_q, int32_t nthreads)
 {
     if (n <= 0 || m2 <= 0) return -1;
 #ifdef _OPENMP
@@ -100,29 +151,31 @@ int32_t orc_phase1(int32_t n, const int64_t *offs, const int32_t *nbr, const int
     nthreads = 1;
 #endif
     const double constant = 1 / (double)m2; /* louvain_main_process.cu:273 */
-    int32_t *K = (int32_t *)calloc((size_t)n, sizeof(int32_t));
-    int32_t *Self = (int32_t *)calloc((size_t)n, sizeof(int32_t));
-    int32_t *Tot = (int32_t *)calloc((size_t)n, sizeof(int32_t));
+    int64_t *K = (int64_t *)calloc((size_t)n, sizeof(int64_t));
+    int64_t *Self = (int64_t *)calloc((size_t)n, sizeof(int64_t));
+    int64_t *Tot = (int64_t *)calloc((size_t)n, sizeof(int64_t));
     int32_t *size = (int32_t *)calloc((size_t)n, sizeof(int32_t));
-    int32_t *In = (int32_t *)calloc((size_t)n, sizeof(int32_t));
+    int64_t *In = (int64_t *)calloc((size_t)n, sizeof(int64_t));
     int32_t *prev = (int32_t *)calloc((size_t)n, sizeof(int32_t));
     int32_t *cur = (int32_t *)calloc((size_t)n, sizeof(int32_t));
     unsigned char *active = (unsigned char *)calloc((size_t)n, 1);
     scratch_t *scr = (scratch_t *)calloc((size_t)nthreads, sizeof(scratch_t));
     for (int t = 0; t < nthreads; ++t) {
-        scr[t].acc = (int32_t *)calloc((size_t)n, sizeof(int32_t));
+        scr[t].acc = (int64_t *)calloc((size_t)n, sizeof(int64_t));
         scr[t].touched = (int32_t *)calloc((size_t)n, sizeof(int32_t));
     }
 
     /* init_communities (kernel_functions.cu:34-73): K = Tot = row weight sum,
      * Self = self-loop weight, label = own id, community size 1
      * (louvain_main_process.cu:337). */
-    int64_t sum_in = 0, sum_tot2 = 0;
-#pragma omp parallel for num_threads(nthreads) schedule(dynamic, 4096) reduction(+ : sum_in, sum_tot2)
+    int64_t sum_in = 0;
+    u128 sum_tot2 = 0;
+    /* (the 128-bit square sum is accumulated outside the parallel loop) */
+#pragma omp parallel for num_threads(nthreads) schedule(dynamic, 4096) reduction(+ : sum_in)
     for (int32_t v = 0; v < n; ++v) {
-        int32_t k = 0, sf = 0;
+        int64_t k = 0, sf = 0;
         for (int64_t e = offs[v]; e < offs[v + 1]; ++e) {
-            int32_t wt = w ? w[e] : 1;
+            int64_t wt = w ? w[e] : 1;
             k += wt;
             if (nbr[e] == v) sf = wt;
         }
@@ -136,10 +189,10 @@ int32_t orc_phase1(int32_t n, const int64_t *offs, const int32_t *nbr, const int
          * gives In = Self for the singleton partition */
         In[v] = sf;
         sum_in += sf;
-        sum_tot2 += (int64_t)k * (int64_t)k;
         active[v] = 1;
     }
-    double q = orc_q_from_sums(sum_in, sum_tot2, m2);
+    for (int32_t v = 0; v < n; ++v) sum_tot2 += (u128)(uint64_t)K[v] * (uint64_t)K[v];
+    double q = q_of(sum_in, sum_tot2, m2);
     int32_t nq = 0;
     if (iter_q && nq < iter_cap) iter_q[nq] = q;
     nq++;
@@ -175,13 +228,14 @@ int32_t orc_phase1(int32_t n, const int64_t *offs, const int32_t *nbr, const int
          * kernel_functions.cuh:112-121, louvain_main_process.cu:955) */
         int64_t min_tot = m2;
         sum_tot2 = 0;
-#pragma omp parallel for num_threads(nthreads) reduction(min : min_tot) reduction(+ : sum_tot2)
+#pragma omp parallel for num_threads(nthreads) reduction(min : min_tot)
         for (int32_t c = 0; c < n; ++c) {
             int64_t t = Tot[c];
             if (t != 0 && t < min_tot) min_tot = t;
-            sum_tot2 += t * t;
         }
-        const int32_t min_tot_i = (int32_t)min_tot;
+        for (int32_t c = 0; c < n; ++c) sum_tot2 += (u128)(uint64_t)Tot[c] * (uint64_t)Tot[c];
+        /* (the reference holds minTot in the int32 weight type) */
+        const int64_t min_tot_i = min_tot;
         /* weight update + pruning (compute_In, kernel_functions.cu:890-955,
          * compute_In_blk :958-1034): In = weight to the own community, and
          * the vertex leaves the active set when the bound at :944 holds. */
@@ -192,17 +246,18 @@ int32_t orc_phase1(int32_t n, const int64_t *offs, const int32_t *nbr, const int
                 active[v] = 1;
                 continue;
             }
-            int32_t c = cur[v], s = 0;
+            int32_t c = cur[v];
+            int64_t s = 0;
             for (int64_t e = offs[v]; e < offs[v + 1]; ++e)
                 if (cur[nbr[e]] == c) s += w ? w[e] : 1;
             In[v] = s;
             sum_in += s;
-            int32_t ki = K[v];
+            int64_t ki = K[v];
             active[v] = !(2 * (s - Self[v]) - (ki - Self[v]) +
                               (double)(min_tot_i - (Tot[c] - ki)) * constant * ki >
                           0);
         }
-        q = orc_q_from_sums(sum_in, sum_tot2, m2);
+        q = q_of(sum_in, sum_tot2, m2);
         if (iter_q && nq < iter_cap) iter_q[nq] = q;
         nq++;
         /* convergence: louvain_main_process.cu:1004-1007; the partition of the
@@ -225,15 +280,35 @@ int32_t orc_phase1(int32_t n, const int64_t *offs, const int32_t *nbr, const int
     return nq - 1;
 }
 
+static int64_t *promote(const int32_t *w, int64_t E)
+{
+    if (!w) return NULL;
+    int64_t *o = (int64_t *)malloc((size_t)(E > 0 ? E : 1) * sizeof(int64_t));
+    for (int64_t e = 0; e < E; ++e) o[e] = w[e];
+    return o;
+}
+
+int32_t orc_phase1(int32_t n, const int64_t *offs, const int32_t *nbr, const int32_t *w,
+                   int64_t m2, double min_mod, int32_t *labels_out, double *q_out,
+                   double *iter_q, int32_t iter_cap, int32_t *n_iter_q, int32_t nthreads)
+{
+    if (n <= 0) return -1;
+    int64_t *w64 = promote(w, offs[n]);
+    int32_t r = phase1_w64(n, offs, nbr, w64, m2, min_mod, labels_out, q_out, iter_q, iter_cap, n_iter_q,
+                           nthreads);
+    free(w64);
+    return r;
+}
+
 static int cmp_i32(const void *a, const void *b)
 {
     int32_t x = *(const int32_t *)a, y = *(const int32_t *)b;
     return (x > y) - (x < y);
 }
 
-int32_t orc_contract(int32_t n, const int64_t *offs, const int32_t *nbr, const int32_t *w,
-                     const int32_t *labels, int32_t *relabel_out, int64_t *new_offs,
-                     int32_t *new_nbr, int32_t *new_w, int64_t *new_entries)
+static int32_t contract_w64(int32_t n, const int64_t *offs, const int32_t *nbr, const int64_t *w,
+                            const int32_t *labels, int32_t *relabel_out, int64_t *new_offs,
+                            int32_t *new_nbr, int64_t *new_w, int64_t *new_entries)
 {
     /* community sizes and dense renumbering in ascending label order
      * (build_compressed_graph.cu:11-24) */
@@ -271,7 +346,7 @@ int32_t orc_contract(int32_t n, const int64_t *offs, const int32_t *nbr, const i
         qsort(touched, (size_t)nt, sizeof(int32_t), cmp_i32);
         for (int32_t i = 0; i < nt; ++i) {
             new_nbr[out] = touched[i];
-            new_w[out] = (int32_t)acc[touched[i]];
+            new_w[out] = acc[touched[i]];
             acc[touched[i]] = 0;
             out++;
         }
@@ -282,10 +357,27 @@ int32_t orc_contract(int32_t n, const int64_t *offs, const int32_t *nbr, const i
     return C;
 }
 
-int32_t orc_louvain(int32_t n, const int64_t *offs, const int32_t *nbr, const int32_t *w,
-                    double min_mod, int32_t max_levels, int32_t *comm_out, double *level_q,
-                    int32_t *level_c, int32_t *level_iters, int32_t level_cap, double *iter_q,
-                    int32_t iter_cap, int32_t *n_iter_q, int32_t nthreads)
+int32_t orc_contract(int32_t n, const int64_t *offs, const int32_t *nbr, const int32_t *w,
+                     const int32_t *labels, int32_t *relabel_out, int64_t *new_offs,
+                     int32_t *new_nbr, int32_t *new_w, int64_t *new_entries)
+{
+    const int64_t E = offs[n];
+    int64_t *w64 = promote(w, E);
+    int64_t *nw64 = (int64_t *)malloc((size_t)(E > 0 ? E : 1) * sizeof(int64_t));
+    int64_t ne = 0;
+    int32_t C = contract_w64(n, offs, nbr, w64, labels, relabel_out, new_offs, new_nbr, nw64, &ne);
+    for (int64_t e = 0; e < ne; ++e) new_w[e] = (int32_t)nw64[e];
+    if (new_entries) *new_entries = ne;
+    free(w64);
+    free(nw64);
+    return C;
+}
+
+/* Multi-round driver on int64 weights (NULL = all 1). */
+static int32_t louvain_w64(int32_t n, const int64_t *offs, const int32_t *nbr, const int64_t *w,
+                           double min_mod, int32_t max_levels, int32_t *comm_out, double *level_q,
+                           int32_t *level_c, int32_t *level_iters, int32_t level_cap, double *iter_q,
+                           int32_t iter_cap, int32_t *n_iter_q, int32_t nthreads)
 {
     if (n <= 0) return -1;
     int64_t E = offs[n];
@@ -295,10 +387,10 @@ int32_t orc_louvain(int32_t n, const int64_t *offs, const int32_t *nbr, const in
 
     int64_t *go = (int64_t *)malloc(((size_t)n + 1) * sizeof(int64_t));
     int32_t *gn = (int32_t *)malloc((size_t)(E > 0 ? E : 1) * sizeof(int32_t));
-    int32_t *gw = (int32_t *)malloc((size_t)(E > 0 ? E : 1) * sizeof(int32_t));
+    int64_t *gw = (int64_t *)malloc((size_t)(E > 0 ? E : 1) * sizeof(int64_t));
     int64_t *no = (int64_t *)malloc(((size_t)n + 1) * sizeof(int64_t));
     int32_t *nn = (int32_t *)malloc((size_t)(E > 0 ? E : 1) * sizeof(int32_t));
-    int32_t *nw = (int32_t *)malloc((size_t)(E > 0 ? E : 1) * sizeof(int32_t));
+    int64_t *nw = (int64_t *)malloc((size_t)(E > 0 ? E : 1) * sizeof(int64_t));
     int32_t *lab = (int32_t *)malloc((size_t)n * sizeof(int32_t));
     int32_t *rl = (int32_t *)malloc((size_t)n * sizeof(int32_t));
     memcpy(go, offs, ((size_t)n + 1) * sizeof(int64_t));
@@ -313,10 +405,10 @@ int32_t orc_louvain(int32_t n, const int64_t *offs, const int32_t *nbr, const in
         int32_t nq = 0;
         double *tr = iter_q ? iter_q + (nq_total < iter_cap ? nq_total : iter_cap) : NULL;
         int32_t cap = iter_q ? (iter_cap > nq_total ? iter_cap - nq_total : 0) : 0;
-        int32_t it = orc_phase1(cn, go, gn, gw, m2, min_mod, lab, &q, tr, cap, &nq, nthreads);
+        int32_t it = phase1_w64(cn, go, gn, gw, m2, min_mod, lab, &q, tr, cap, &nq, nthreads);
         nq_total += nq;
         int64_t ne = 0;
-        int32_t C = orc_contract(cn, go, gn, gw, lab, rl, no, nn, nw, &ne);
+        int32_t C = contract_w64(cn, go, gn, gw, lab, rl, no, nn, nw, &ne);
         /* labels of the input vertices follow the contraction (the gather of
          * louvain.cu:188-189, composed in the intended direction) */
         for (int32_t i = 0; i < n; ++i) comm_out[i] = rl[comm_out[i]];
@@ -330,7 +422,7 @@ int32_t orc_louvain(int32_t n, const int64_t *offs, const int32_t *nbr, const in
         cur_mod = q;
         int64_t *t64 = go; go = no; no = t64;
         int32_t *t32 = gn; gn = nn; nn = t32;
-        t32 = gw; gw = nw; nw = t32;
+        t64 = gw; gw = nw; nw = t64;
         cn = C;
         /* round loop condition, louvain.cu:202 */
         if (!(cur_mod - prev_mod >= min_mod)) break;
@@ -339,6 +431,53 @@ int32_t orc_louvain(int32_t n, const int64_t *offs, const int32_t *nbr, const in
     if (n_iter_q) *n_iter_q = nq_total;
     free(go); free(gn); free(gw); free(no); free(nn); free(nw); free(lab); free(rl);
     return rounds;
+}
+
+int32_t orc_louvain(int32_t n, const int64_t *offs, const int32_t *nbr, const int32_t *w,
+                    double min_mod, int32_t max_levels, int32_t *comm_out, double *level_q,
+                    int32_t *level_c, int32_t *level_iters, int32_t level_cap, double *iter_q,
+                    int32_t iter_cap, int32_t *n_iter_q, int32_t nthreads)
+{
+    if (n <= 0) return -1;
+    int64_t *w64 = promote(w, offs[n]);
+    int32_t r = louvain_w64(n, offs, nbr, w64, min_mod, max_levels, comm_out, level_q, level_c, level_iters,
+                            level_cap, iter_q, iter_cap, n_iter_q, nthreads);
+    free(w64);
+    return r;
+}
+
+int32_t orc_louvain_fixed(int32_t n, const int64_t *offs, const int32_t *nbr, const int64_t *w,
+                          double min_mod, int32_t max_levels, int32_t *comm_out, double *level_q,
+                          int32_t *level_c, int32_t *level_iters, int32_t level_cap, double *iter_q,
+                          int32_t iter_cap, int32_t *n_iter_q, int32_t nthreads)
+{
+    return louvain_w64(n, offs, nbr, w, min_mod, max_levels, comm_out, level_q, level_c, level_iters, level_cap,
+                       iter_q, iter_cap, n_iter_q, nthreads);
+}
+
+double orc_modularity_f32(int32_t n, const int64_t *offs, const int32_t *nbr, const float *w,
+                          const int32_t *labels)
+{
+    /* the host check of kernel_functions.cu:1037-1079 with FP64 sums of the
+     * float weights */
+    double m2 = 0;
+    for (int64_t e = 0; e < offs[n]; ++e) m2 += (double)w[e];
+    double constant = 1.0 / m2;
+    double *Tot = (double *)calloc((size_t)n, sizeof(double));
+    double *In = (double *)calloc((size_t)n, sizeof(double));
+    for (int32_t i = 0; i < n; ++i) {
+        double degree = 0;
+        for (int64_t j = offs[i]; j < offs[i + 1]; ++j) {
+            degree += (double)w[j];
+            if (labels[nbr[j]] == labels[i]) In[i] += (double)w[j];
+        }
+        Tot[labels[i]] += degree;
+    }
+    double q = 0;
+    for (int32_t i = 0; i < n; ++i) q += In[i] * constant - Tot[i] * Tot[i] * constant * constant;
+    free(Tot);
+    free(In);
+    return q;
 }
 
 double orc_modularity(int32_t n, const int64_t *offs, const int32_t *nbr, const int32_t *w,

@@ -50,6 +50,22 @@ int32_t orc_louvain(int32_t n, const int64_t *offs, const int32_t *nbr, const in
 double orc_modularity(int32_t n, const int64_t *offs, const int32_t *nbr, const int32_t *w,
                       const int32_t *labels);
 
+/* Float-weight graphs (no counterpart in the reference): weights held as
+ * 64-bit fixed-point integers round(w * 2^shift).  orc_fixed_shift returns
+ * the shift (-1 for a weight that is not positive and finite or rounds to
+ * 0); orc_louvain_fixed runs the multi-round driver on int64 weights;
+ * orc_modularity_f32 is the FP64 host modularity of the float weights. */
+int32_t orc_fixed_shift(const float *w, int64_t E);
+void orc_fixed_weights(const float *w, int64_t E, int32_t shift, int64_t *out);
+int32_t orc_louvain_fixed(int32_t n, const int64_t *offs, const int32_t *nbr, const int64_t *w,
+                          double min_mod, int32_t max_levels, int32_t *comm_out, double *level_q,
+                          int32_t *level_c, int32_t *level_iters, int32_t level_cap, double *iter_q,
+                          int32_t iter_cap, int32_t *n_iter_q, int32_t nthreads);
+double orc_modularity_f32(int32_t n, const int64_t *offs, const int32_t *nbr, const float *w,
+                          const int32_t *labels);
+/* Q from a 128-bit sum of Tot^2 (hi, lo words): hi * 2^64 + lo in FP64. */
+double orc_q_from_sums128(int64_t sum_in, uint64_t tot2_lo, uint64_t tot2_hi, int64_t m2);
+
 #ifdef __cplusplus
 }
 #endif

@@ -59,6 +59,17 @@ class Oracle:
                                   ctypes.c_int32]
         L.orc_modularity.restype = ctypes.c_double
         L.orc_modularity.argtypes = [ctypes.c_int32, _i64p, _i32p, _i32p, _i32p]
+        _f32p = ctypes.POINTER(ctypes.c_float)
+        L.orc_fixed_shift.restype = ctypes.c_int32
+        L.orc_fixed_shift.argtypes = [_f32p, ctypes.c_int64]
+        L.orc_fixed_weights.restype = None
+        L.orc_fixed_weights.argtypes = [_f32p, ctypes.c_int64, ctypes.c_int32, _i64p]
+        L.orc_louvain_fixed.restype = ctypes.c_int32
+        L.orc_louvain_fixed.argtypes = [ctypes.c_int32, _i64p, _i32p, _i64p, ctypes.c_double, ctypes.c_int32,
+                                        _i32p, _f64p, _i32p, _i32p, ctypes.c_int32, _f64p, ctypes.c_int32,
+                                        ctypes.POINTER(ctypes.c_int32), ctypes.c_int32]
+        L.orc_modularity_f32.restype = ctypes.c_double
+        L.orc_modularity_f32.argtypes = [ctypes.c_int32, _i64p, _i32p, _f32p, _i32p]
 
     @staticmethod
     def _arrs(offs, nbr, w):
@@ -116,6 +127,44 @@ class Oracle:
         labels = np.ascontiguousarray(labels, dtype=np.int32)
         return self.lib.orc_modularity(offs.shape[0] - 1, _p(offs, _i64p), _p(nbr, _i32p), _p(w, _i32p),
                                        _p(labels, _i32p))
+
+    def fixed_weights(self, wf):
+        """(shift, int64 fixed-point weights) of float weights, as the engine
+        holds them."""
+        wf = np.ascontiguousarray(wf, dtype=np.float32)
+        f32 = ctypes.POINTER(ctypes.c_float)
+        shift = self.lib.orc_fixed_shift(_p(wf, f32), wf.shape[0])
+        out = np.zeros(wf.shape[0], dtype=np.int64)
+        self.lib.orc_fixed_weights(_p(wf, f32), wf.shape[0], shift, _p(out, _i64p))
+        return shift, out
+
+    def louvain_f32(self, offs, nbr, wf, min_mod=1e-6, max_levels=0, nthreads=1, iter_cap=65536):
+        """Multi-round run of a float-weight graph on its fixed-point weights."""
+        offs = np.ascontiguousarray(offs, dtype=np.int64)
+        nbr = np.ascontiguousarray(nbr, dtype=np.int32)
+        shift, w64 = self.fixed_weights(wf)
+        assert shift >= 0
+        n = offs.shape[0] - 1
+        comm = np.zeros(n, dtype=np.int32)
+        lq = np.zeros(64, dtype=np.float64)
+        lc = np.zeros(64, dtype=np.int32)
+        li = np.zeros(64, dtype=np.int32)
+        iq = np.zeros(iter_cap, dtype=np.float64)
+        nq = ctypes.c_int32()
+        r = self.lib.orc_louvain_fixed(n, _p(offs, _i64p), _p(nbr, _i32p), _p(w64, _i64p), min_mod, max_levels,
+                                       _p(comm, _i32p), _p(lq, _f64p), _p(lc, _i32p), _p(li, _i32p), 64,
+                                       _p(iq, _f64p), iter_cap, ctypes.byref(nq), nthreads)
+        return {"rounds": r, "labels": comm, "level_q": lq[:r].tolist(), "level_c": lc[:r].tolist(),
+                "level_iters": li[:r].tolist(), "iter_q": iq[:min(nq.value, iter_cap)].tolist(),
+                "modularity": float(lq[r - 1]) if r > 0 else float("nan"), "shift": shift}
+
+    def modularity_f32(self, offs, nbr, wf, labels):
+        offs = np.ascontiguousarray(offs, dtype=np.int64)
+        nbr = np.ascontiguousarray(nbr, dtype=np.int32)
+        wf = np.ascontiguousarray(wf, dtype=np.float32)
+        labels = np.ascontiguousarray(labels, dtype=np.int32)
+        return self.lib.orc_modularity_f32(offs.shape[0] - 1, _p(offs, _i64p), _p(nbr, _i32p),
+                                           _p(wf, ctypes.POINTER(ctypes.c_float)), _p(labels, _i32p))
 
     def q_from_sums(self, sum_in, sum_tot2, m2):
         return self.lib.orc_q_from_sums(sum_in, sum_tot2, m2)
