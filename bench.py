@@ -49,6 +49,7 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-learned", action="store_true", help="skip the learned-proposal arm")
     p.add_argument("--no-batch", action="store_true", help="skip the batched-graphs arm")
+    p.add_argument("--no-weighted", action="store_true", help="skip the float-weight LFR arm")
     p.add_argument("--threshold", type=float, default=0.3, help="proposal probability threshold")
     p.add_argument("--profile", action="store_true",
                    help="one device-resident run and a short summary (for ncu captures)")
@@ -209,6 +210,47 @@ def learned_arm(ffi, ctx, g, stream, args, torch, plain_ms, plain):
             "iterations": r["total_iterations"], "plain_iterations": plain["total_iterations"],
             "phase_ms": {"decide": r["time_decide_ms"], "update": r["time_update_ms"],
                          "contract": r["time_contract_ms"]}}
+
+
+WEIGHTED = {"workload": "lfr-16M-200M-f32", "generator": "LFR-style", "vertices": 16_000_000, "tau1": 2.5,
+            "dmin": 10, "dmax": 20000, "tau2": 1.5, "cmin": 20, "cmax": 50000, "mu": 0.3,
+            "weights": "lognormal(0,1) float32", "seed": 1}
+
+
+def weighted_arm(ffi, args, torch, device):
+    """Float-weight LFR-style graph (16M vertices, about 200M edges): the
+    whole run through gala_louvain (host graph in, labels out), weights as
+    64-bit fixed point, gains in FP64; modularity against the host FP64
+    recomputation on the float weights."""
+    c = WEIGHTED
+    t0 = time.perf_counter()
+    g = ffi.Graph.lfr(c["vertices"], c["tau1"], c["dmin"], c["dmax"], c["tau2"], c["cmin"], c["cmax"], c["mu"],
+                      True, c["seed"])
+    gen_s = time.perf_counter() - t0
+    n, e, _ = g.info()
+    m = e // 2
+    g.pin()
+    ctx = ffi.Context(n, e, device=device)
+    steps = max(1, min(args.steps, 2))
+    times, r = [], None
+    for i in range(1 + steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        r = ctx.louvain(g)
+        torch.cuda.synchronize()
+        if i >= 1:
+            times.append(time.perf_counter() - t0)
+    ctx.close()
+    sec = statistics.median(times)
+    q_host = g.modularity(r["labels"])
+    return {"config": dict(c, edges=m, csr_entries=e, generation_s=gen_s),
+            "metric": "end-to-end Louvain edges/s (float weights, all rounds to dQ<1e-6)", "value": m / sec,
+            "unit": "edges/s", "seconds": sec, "device_ms": r["time_total_ms"], "steps": steps, "warmup": 1,
+            "phase_ms": {"decide": r["time_decide_ms"], "update": r["time_update_ms"],
+                         "contract": r["time_contract_ms"]},
+            "modularity": r["modularity"], "modularity_host_fp64": q_host,
+            "abs_diff_vs_host": abs(q_host - r["modularity"]), "rounds": r["rounds"],
+            "iterations": r["total_iterations"], "communities": r["num_communities"]}
 
 
 BATCH = {"workload": "sbm-batch-4096", "graphs": 4096, "n_min": 200, "n_max": 3500, "k_min": 8, "k_max": 64,
@@ -392,6 +434,8 @@ def main():
         line["learned"] = learned_arm(ffi, ctx, g, stream, args, torch, e2e_step, r_e2e)
     if not args.no_batch:
         line["batch"] = batch_arm(ffi, args, torch, local)
+    if not args.no_weighted:
+        line["weighted"] = weighted_arm(ffi, args, torch, local)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
         dt, ro = cpu_oracle_run(offs, nbr, threads)
