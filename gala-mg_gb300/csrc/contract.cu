@@ -411,7 +411,7 @@ __device__ __forceinline__ int agg_insert(const AggArgs<WT> &a, long long st, in
 
 // Rows of 33..kMid2Max entries: one CTA per community, shared-memory hash
 // table of TMAX slots, distinct keys sorted by a bitonic sort of LMAX slots.
-template <typename WT, int BLOCK, int TMAX, int LMAX>
+template <typename WT, int BLOCK, int TMAX, int LMAX, bool SORT>
 __global__ void __launch_bounds__(BLOCK) k_agg_mid(AggArgs<WT> a, const int32_t *__restrict__ list, int cls)
 {
     extern __shared__ long long sm_ll[];
@@ -438,6 +438,21 @@ __global__ void __launch_bounds__(BLOCK) k_agg_mid(AggArgs<WT> a, const int32_t 
         __syncthreads();
         agg_insert(a, st, E, keys, vals, T, lg);
         __syncthreads();
+        if (!SORT) {  // rows in table order: straight to the row
+            const long long o = a.tmp_off[c];
+            for (int j = threadIdx.x; j < T; j += BLOCK) {
+                const int kk = keys[j];
+                if (kk >= 0) {
+                    const int p = atomicAdd(&s_k, 1);
+                    a.tmp_nbr[o + p] = kk;
+                    a.tmp_w[o + p] = vals[j];
+                }
+            }
+            __syncthreads();
+            if (threadIdx.x == 0) a.kc[c] = s_k;
+            __syncthreads();
+            continue;
+        }
         for (int j = threadIdx.x; j < T; j += BLOCK) {
             int kk = keys[j];
             if (kk >= 0) {
@@ -536,14 +551,15 @@ __global__ void k_big_work(AggArgs<WT> a, BigArgs b)
     }
 }
 
-// Every CTA inserts one chunk of kChunk stream entries into its community's
-// global table; many CTAs share one community.  New keys are counted.
+// Values of a community's global table (after the keys of all tables).
 template <typename WT>
 __device__ __forceinline__ WT *big_vals(const BigArgs &b, long long i)
 {
     return (WT *)(b.pool + b.pool_half) + b.toff[i];
 }
 
+// Every CTA inserts one chunk of kChunk stream entries into its community's
+// global table; many CTAs share one community.  New keys are counted.
 template <typename WT>
 __global__ void __launch_bounds__(256) k_big_insert(AggArgs<WT> a, BigArgs b, long long nwork)
 {
@@ -558,7 +574,7 @@ __global__ void __launch_bounds__(256) k_big_insert(AggArgs<WT> a, BigArgs b, lo
         const long long T = b.T[i];
         WT *vals = big_vals<WT>(b, i);
         int *keys = b.mode[i] ? nullptr : b.pool + b.toff[i];
-        int created = agg_insert(a, st, len, keys, vals, (int)T, __ffs((int)T) - 1);
+        int created = agg_insert(a, st, len, keys, vals, (int)T, keys ? __ffs((int)T) - 1 : 0);
         created = warp_sum(created);
         if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = created;
         __syncthreads();
@@ -575,13 +591,13 @@ __global__ void __launch_bounds__(256) k_big_insert(AggArgs<WT> a, BigArgs b, lo
 // ranked by a bitmap over all communities: words per row (0 for the others);
 // every class-3 row gets its final length here.
 template <typename WT>
-__global__ void k_big_mark(AggArgs<WT> a, BigArgs b)
+__global__ void k_big_mark(AggArgs<WT> a, BigArgs b, int sort_rows)
 {
     const int cnt = a.st->small_cnt[3];
     const long long words = ((long long)a.C + 31) >> 5;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < cnt; i += gridDim.x * blockDim.x) {
         const int k = b.kdist[i];
-        b.gwords[i] = k > kSortMax ? words : 0;
+        b.gwords[i] = (sort_rows && k > kSortMax) ? words : 0;
         a.kc[b.list[i]] = k;
     }
 }
@@ -737,15 +753,15 @@ __global__ void k_contract_reset(DevStats *st)
 }
 
 // Shared memory of the table kernels: int keys plus WT values per slot.
-template <typename WT>
+template <typename WT, bool SORT>
 constexpr size_t mid1_smem()
 {
-    return (1024 + kMid1Max) * (sizeof(int) + sizeof(WT));
+    return (1024 + (SORT ? kMid1Max : 0)) * (sizeof(int) + sizeof(WT));
 }
-template <typename WT>
+template <typename WT, bool SORT>
 constexpr size_t mid2_smem()
 {
-    return (8192 + kMid2Max) * (sizeof(int) + sizeof(WT));
+    return (8192 + (SORT ? kMid2Max : 0)) * (sizeof(int) + sizeof(WT));
 }
 template <typename WT>
 constexpr size_t sort_smem()
@@ -753,13 +769,21 @@ constexpr size_t sort_smem()
     return kSortMax * (sizeof(int) + sizeof(WT));
 }
 
+template <typename WT, bool SORT>
+static void configure_mid()
+{
+    cudaFuncSetAttribute(k_agg_mid<WT, 128, 1024, kMid1Max, SORT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)mid1_smem<WT, SORT>());
+    cudaFuncSetAttribute(k_agg_mid<WT, 256, 8192, kMid2Max, SORT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)mid2_smem<WT, SORT>());
+}
+
 template <typename WT>
 static void configure_t()
 {
-    cudaFuncSetAttribute(k_agg_mid<WT, 128, 1024, kMid1Max>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)mid1_smem<WT>());
-    cudaFuncSetAttribute(k_agg_mid<WT, 256, 8192, kMid2Max>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)mid2_smem<WT>());
+    configure_mid<WT, true>();
+    configure_mid<WT, false>();
+
     cudaFuncSetAttribute(k_big_sort<WT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sort_smem<WT>());
 }
 
@@ -801,7 +825,7 @@ static bool read_stats(DevStats *h, DevStats *d, cudaStream_t st, gala_status *s
 // Rows longer than kMid2Max entries (class 3).  Returns false on failure.
 template <typename WT>
 static bool contract_long_rows(const AggArgs<WT> &a, ContractBuffers &b, int cnt3, int C, DevStats &hs,
-                               cudaStream_t st, gala_status *status)
+                               cudaStream_t st, gala_status *status, bool sort_rows)
 {
     const int nsm = sm_count();
     const int cap = nsm * 8;
@@ -844,7 +868,7 @@ static bool contract_long_rows(const AggArgs<WT> &a, ContractBuffers &b, int cnt
     cudaMemsetAsync(b.big_pool + half, 0, (size_t)slots * sizeof(WT), st);
     k_big_work<WT><<<grid_cap((long long)cnt3 * 32, 256, cap), 256, 0, st>>>(a, ba);
     k_big_insert<WT><<<(int)(nwork < nsm * 8 ? nwork : nsm * 8), 256, 0, st>>>(a, ba, nwork);
-    k_big_mark<WT><<<grid_cap(cnt3, 256, cap), 256, 0, st>>>(a, ba);
+    k_big_mark<WT><<<grid_cap(cnt3, 256, cap), 256, 0, st>>>(a, ba, sort_rows ? 1 : 0);
     exclusive_scan(b.big_gwords, b.big_gofs, cnt3, OpIdentity(), b.scan_partial, &b.stats->total, st);
     note_launch(3);
     if (!read_stats(&hs, b.stats, st, status, "contraction: long-row bitmaps")) return false;
@@ -865,8 +889,10 @@ static bool contract_long_rows(const AggArgs<WT> &a, ContractBuffers &b, int cnt
         k_big_rank<WT><<<tgrid, 256, 0, st>>>(a, ba, ntwork);
         note_launch(1);
     }
-    k_big_sort<WT><<<cnt3 < nsm * 2 ? cnt3 : nsm * 2, 1024, sort_smem<WT>(), st>>>(a, ba);
-    note_launch(1);
+    if (sort_rows) {
+        k_big_sort<WT><<<cnt3 < nsm * 2 ? cnt3 : nsm * 2, 1024, sort_smem<WT>(), st>>>(a, ba);
+        note_launch(1);
+    }
     return true;
 }
 
@@ -876,7 +902,7 @@ static bool contract_long_rows(const AggArgs<WT> &a, ContractBuffers &b, int cnt
 template <typename WT>
 static int contract_t(const LevelGraph &g, const int32_t *comm, ContractBuffers &b, int64_t *new_offs,
                       int32_t *new_nbr, WT *new_w, int32_t *orig_map, int32_t n_orig, int64_t *new_E,
-                      cudaStream_t st, gala_status *status, bool validate_labels)
+                      cudaStream_t st, gala_status *status, bool validate_labels, bool sort_rows)
 {
     const int n = g.n;
     const int cap = sm_count() * 8;
@@ -948,15 +974,25 @@ static int contract_t(const LevelGraph &g, const int32_t *comm, ContractBuffers 
     }
     if (hs.small_cnt[1] > 0) {
         int grid = hs.small_cnt[1] < nsm * 12 ? hs.small_cnt[1] : nsm * 12;
-        k_agg_mid<WT, 128, 1024, kMid1Max><<<grid, 128, mid1_smem<WT>(), st>>>(a, b.cls_list + (long long)C, 1);
+        if (sort_rows)
+            k_agg_mid<WT, 128, 1024, kMid1Max, true>
+                <<<grid, 128, mid1_smem<WT, true>(), st>>>(a, b.cls_list + (long long)C, 1);
+        else
+            k_agg_mid<WT, 128, 1024, kMid1Max, false>
+                <<<grid, 128, mid1_smem<WT, false>(), st>>>(a, b.cls_list + (long long)C, 1);
         note_launch(1);
     }
     if (hs.small_cnt[2] > 0) {
         int grid = hs.small_cnt[2] < nsm * 2 ? hs.small_cnt[2] : nsm * 2;
-        k_agg_mid<WT, 256, 8192, kMid2Max><<<grid, 256, mid2_smem<WT>(), st>>>(a, b.cls_list + 2LL * C, 2);
+        if (sort_rows)
+            k_agg_mid<WT, 256, 8192, kMid2Max, true>
+                <<<grid, 256, mid2_smem<WT, true>(), st>>>(a, b.cls_list + 2LL * C, 2);
+        else
+            k_agg_mid<WT, 256, 8192, kMid2Max, false>
+                <<<grid, 256, mid2_smem<WT, false>(), st>>>(a, b.cls_list + 2LL * C, 2);
         note_launch(1);
     }
-    if (hs.small_cnt[3] > 0 && !contract_long_rows(a, b, hs.small_cnt[3], C, hs, st, status)) return -1;
+    if (hs.small_cnt[3] > 0 && !contract_long_rows(a, b, hs.small_cnt[3], C, hs, st, status, sort_rows)) return -1;
     exclusive_scan(b.kc, new_offs, C, OpIdentity(), b.scan_partial, &b.stats->total, st);
     k_set_last_offset<<<1, 1, 0, st>>>(new_offs, C, &b.stats->total);
     note_launch(1);
@@ -981,13 +1017,13 @@ static int contract_t(const LevelGraph &g, const int32_t *comm, ContractBuffers 
 
 int contract_run(const LevelGraph &g, const int32_t *comm, ContractBuffers &b, int64_t *new_offs,
                  int32_t *new_nbr, void *new_w, int32_t *orig_map, int32_t n_orig, int64_t *new_E,
-                 cudaStream_t st, gala_status *status, bool validate_labels)
+                 cudaStream_t st, gala_status *status, bool validate_labels, bool sort_rows)
 {
     if (g.wide)
         return contract_t<long long>(g, comm, b, new_offs, new_nbr, (long long *)new_w, orig_map, n_orig, new_E, st,
-                                     status, validate_labels);
+                                     status, validate_labels, sort_rows);
     return contract_t<int>(g, comm, b, new_offs, new_nbr, (int *)new_w, orig_map, n_orig, new_E, st, status,
-                           validate_labels);
+                           validate_labels, sort_rows);
 }
 
 }  // namespace gala

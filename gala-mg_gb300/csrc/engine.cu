@@ -406,8 +406,11 @@ gala_status phase1(gala_context *ctx, const LevelGraph &g, long long &m2, double
         fork(ctx);
         for (int k = 0; k < kNumBins; ++k) {
             const int bin = kBinLaunchOrder[k];
-            p1_update(g, b, bin, b.order + bin_start[bin], level_cnt[bin], nxt, bin_start[bin], constant, m2,
-                      aux_for(ctx, k));
+            if (bin == 7)
+                p1_hub_update(g, b, hp, nxt, bin_start[bin], constant, m2, aux_for(ctx, k));
+            else
+                p1_update(g, b, bin, b.order + bin_start[bin], level_cnt[bin], nxt, bin_start[bin], constant, m2,
+                          aux_for(ctx, k));
         }
         join(ctx);
         if (bt) {
@@ -497,8 +500,11 @@ gala_status phase1(gala_context *ctx, const LevelGraph &g, long long &m2, double
             fork(ctx);
             for (int k = 0; k < kNumBins; ++k) {
                 const int bin = kBinLaunchOrder[k];
-                p1_update(g, b, bin, b.order + bin_start[bin], level_cnt[bin], nxt, bin_start[bin], constant, m2,
-                          aux_for(ctx, k));
+                if (bin == 7)
+                    p1_hub_update(g, b, hp, nxt, bin_start[bin], constant, m2, aux_for(ctx, k));
+                else
+                    p1_update(g, b, bin, b.order + bin_start[bin], level_cnt[bin], nxt, bin_start[bin], constant,
+                              m2, aux_for(ctx, k));
             }
             join(ctx);
             if ((s = check(cudaMemcpyAsync(h, b.stats, sizeof(DevStats), cudaMemcpyDeviceToHost, st), "restore")) ||
@@ -628,7 +634,7 @@ gala_status run_levels(gala_context *ctx, int32_t n0, int64_t E0, const int64_t 
         int64_t newE = 0;
         gala_status cs = GALA_OK;
         C = contract_run(g, ctx->p1.comm, ctx->cb, ctx->offs[buf], ctx->nbr[buf], ctx->w[buf], ctx->orig, n0, &newE,
-                         st, &cs);
+                         st, &cs, false, opt && opt->sorted_levels == 1);
         if (C < 0) return cs;
         cudaEventRecord(ctx->ev[1], st);
         if ((s = check(cudaStreamSynchronize(st), "contraction"))) return s;

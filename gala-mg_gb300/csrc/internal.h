@@ -149,6 +149,9 @@ void p1_hub_plan_launch(const LevelGraph &g, Phase1Buffers &b, HubPlan &p, cudaS
 void p1_hub_work_launch(HubPlan &p, cudaStream_t st);
 void p1_hub_decide(const LevelGraph &g, Phase1Buffers &b, const HubPlan &p, double constant, long long m2,
                    int fp64_only, cudaStream_t st);
+// Weight update + pruning of the hub bin (bin 7), chunked over many CTAs.
+void p1_hub_update(const LevelGraph &g, Phase1Buffers &b, const HubPlan &p, int next, int bin_start, double constant,
+                   long long m2, cudaStream_t st);
 
 // ---- batched graphs (batch.cu) ----
 constexpr int kSumIn = 1, kSumTot2 = 2, kMinTot = 4, kSumK = 8, kCountComm = 16;
@@ -207,8 +210,13 @@ struct ContractBuffers {
     long long *scan_partial;
     DevStats *stats;
 };
+// sort_rows = false (the level-to-level contraction of a Louvain run) leaves
+// every new row in hash-table order: phase 1 does not depend on the order of
+// a row's entries (all weight sums are exact integers), and the sorts are
+// skipped.  gala_contract_device sorts, as the oracle does.
 int contract_run(const LevelGraph &g, const int32_t *comm, ContractBuffers &b, int64_t *new_offs,
                  int32_t *new_nbr, void *new_w, int32_t *orig_map, int32_t n_orig,
-                 int64_t *new_E, cudaStream_t st, gala_status *status, bool validate_labels = false);
+                 int64_t *new_E, cudaStream_t st, gala_status *status, bool validate_labels = false,
+                 bool sort_rows = true);
 
 }  // namespace gala

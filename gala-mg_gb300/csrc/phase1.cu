@@ -1150,6 +1150,7 @@ __global__ void __launch_bounds__(256) k_update_group(UpdateArgs<WT> a, const in
             cur = a.comm[v];
         }
         WT sum = 0;
+#pragma unroll 4
         for (long long j = s + sub; j < e; j += G)
             if (a.comm[a.nbr[j]] == cur) sum += W ? a.w[j] : 1;
 #pragma unroll
@@ -1191,6 +1192,7 @@ __global__ void __launch_bounds__(256) k_update_cta(UpdateArgs<WT> a, const int3
         const long long s = a.offs[v], e = a.offs[v + 1];
         const int cur = a.comm[v];
         WT sum = 0;
+#pragma unroll 4
         for (long long j = s + threadIdx.x; j < e; j += blockDim.x)
             if (a.comm[a.nbr[j]] == cur) sum += W ? a.w[j] : 1;
         sum = warp_sum(sum);
@@ -1218,8 +1220,8 @@ __global__ void __launch_bounds__(256) k_update_cta(UpdateArgs<WT> a, const int3
 }
 
 template <typename WT>
-static void update_t(const LevelGraph &g, Phase1Buffers &b, int bin, const int32_t *list, int count, int next,
-                     int bin_start, double constant, long long m2, cudaStream_t st)
+static UpdateArgs<WT> update_args(const LevelGraph &g, Phase1Buffers &b, int bin, int next, int bin_start,
+                                  double constant, long long m2)
 {
     UpdateArgs<WT> a;
     a.offs = g.offs;
@@ -1242,6 +1244,14 @@ static void update_t(const LevelGraph &g, Phase1Buffers &b, int bin, const int32
     a.cg = b.cg;
     a.stop = b.gstop;
     a.min_tot_g = b.min_tot_g;
+    return a;
+}
+
+template <typename WT>
+static void update_t(const LevelGraph &g, Phase1Buffers &b, int bin, const int32_t *list, int count, int next,
+                     int bin_start, double constant, long long m2, cudaStream_t st)
+{
+    const UpdateArgs<WT> a = update_args<WT>(g, b, bin, next, bin_start, constant, m2);
     const bool W = g.w != nullptr;
     const int cap = num_sms() * 8;
     auto grid_lanes = [&](int G) {
@@ -1339,7 +1349,7 @@ __global__ void __launch_bounds__(256) k_hub_insert(DecideArgs<WT> a, HubPlan p,
     for (long long wi = blockIdx.x; wi < p.nwork; wi += gridDim.x) {
         const int i = p.work[wi];
         const int v = p.hubs[i];
-        if (!flag[v] || stopped(a, v)) continue;
+        if (!flag[v] || stopped(a, v)) continue;  // block-uniform
         const long long e = a.offs[v + 1];
         const long long s = a.offs[v] + (wi - p.coff[i]) * kHubChunk;
         const long long e2 = s + kHubChunk < e ? s + kHubChunk : e;
@@ -1543,6 +1553,107 @@ void p1_hub_decide(const LevelGraph &g, Phase1Buffers &b, const HubPlan &p, doub
         hub_decide_t<long long>(g, b, p, constant, m2, fp64_only, st);
     else
         hub_decide_t<int>(g, b, p, constant, m2, fp64_only, st);
+}
+
+// ------------------------------------------------------------------------
+// Weight update of the hub bin: In[v] of a hub row summed by many CTAs (one
+// per 4096-entry chunk, the chunks of the hub plan) with integer atomics,
+// then one thread per hub evaluates the pruning bound.
+// ------------------------------------------------------------------------
+template <typename WT>
+__global__ void k_hub_in_zero(HubPlan p, WT *In)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < p.H; i += gridDim.x * blockDim.x) In[p.hubs[i]] = 0;
+}
+
+template <typename WT, bool W>
+__global__ void __launch_bounds__(256) k_hub_in_partial(UpdateArgs<WT> a, HubPlan p)
+{
+    __shared__ WT red[8];
+    for (long long wi = blockIdx.x; wi < p.nwork; wi += gridDim.x) {
+        const int i = p.work[wi];
+        const int v = p.hubs[i];
+        if (a.gid && a.stop[a.gid[v]]) continue;  // block-uniform
+        const long long e = a.offs[v + 1];
+        const long long s = a.offs[v] + (wi - p.coff[i]) * kHubChunk;
+        const long long e2 = s + kHubChunk < e ? s + kHubChunk : e;
+        const int cur = a.comm[v];
+        WT sum = 0;
+#pragma unroll 4
+        for (long long j = s + threadIdx.x; j < e2; j += blockDim.x)
+            if (a.comm[a.nbr[j]] == cur) sum += W ? a.w[j] : 1;
+        sum = warp_sum(sum);
+        if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = sum;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            WT t = 0;
+            for (int q = 0; q < (int)(blockDim.x >> 5); ++q) t += red[q];
+            if (t) atomic_add_w(&a.In[v], t);
+        }
+        __syncthreads();
+    }
+}
+
+template <typename WT>
+__global__ void __launch_bounds__(256) k_hub_in_final(UpdateArgs<WT> a, HubPlan p)
+{
+    const long long min_tot = a.st->min_tot;
+    unsigned long long s_in = 0, s_edges = 0;
+    int s_act = 0;
+    const int stride = gridDim.x * blockDim.x;
+    for (int base = blockIdx.x * blockDim.x; base < p.H; base += stride) {  // warp-uniform trip count
+        const int i = base + threadIdx.x;
+        bool active = false;
+        int v = 0;
+        if (i < p.H) {
+            v = p.hubs[i];
+            const PruneScale ps = prune_scale(a, v, min_tot);
+            if (ps.stop) {
+                a.act_flag[v] = 0;
+            } else {
+                const WT sum = a.In[v];
+                const WT ki = a.K[v];
+                active = !prune_bound_fast<WT>(sum, a.Self[v], ki, (WT)ps.min_tot, a.Tot[a.comm[v]], ps.c, ps.m2);
+                a.act_flag[v] = active;
+                s_in += (unsigned long long)sum;
+                if (active) {
+                    s_edges += (unsigned long long)(a.offs[v + 1] - a.offs[v]);
+                    s_act += 1;
+                }
+            }
+        }
+        warp_append(active, v, a.act_list, a.act_counter);
+    }
+    block_add_u64(s_in, &a.st->sum_in);
+    block_add_u64(s_edges, &a.st->act_edges[a.next]);
+    block_add_i32(s_act, &a.st->act_vertices[a.next]);
+}
+
+template <typename WT>
+static void hub_update_t(const LevelGraph &g, Phase1Buffers &b, const HubPlan &p, int next, int bin_start,
+                         double constant, long long m2, cudaStream_t st)
+{
+    UpdateArgs<WT> a = update_args<WT>(g, b, 7, next, bin_start, constant, m2);
+    const int cap = num_sms() * 8;
+    const int hg = (p.H + 255) / 256;
+    k_hub_in_zero<WT><<<hg, 256, 0, st>>>(p, a.In);
+    const int g1 = (int)(p.nwork < cap ? p.nwork : cap);
+    if (g.w)
+        k_hub_in_partial<WT, true><<<g1, 256, 0, st>>>(a, p);
+    else
+        k_hub_in_partial<WT, false><<<g1, 256, 0, st>>>(a, p);
+    k_hub_in_final<WT><<<hg, 256, 0, st>>>(a, p);
+    note_launch(3);
+}
+
+void p1_hub_update(const LevelGraph &g, Phase1Buffers &b, const HubPlan &p, int next, int bin_start, double constant,
+                   long long m2, cudaStream_t st)
+{
+    if (p.H <= 0) return;
+    if (g.wide)
+        hub_update_t<long long>(g, b, p, next, bin_start, constant, m2, st);
+    else
+        hub_update_t<int>(g, b, p, next, bin_start, constant, m2, st);
 }
 
 }  // namespace gala

@@ -101,21 +101,28 @@ __global__ void __launch_bounds__(256) k_mlp_logits(const __nv_bfloat16 *__restr
 
 // Gradient of the weighted binary cross-entropy over samples [0, n) with FP32
 // master weights: loss = sum_s wt_s * BCE(sigmoid(out_s), y_s), wt = pos_weight
-// for y = 1, else 1.  Per-thread gradients are summed over the warp by
-// shuffles, over the block in shared memory, then added to grad (global).
-__global__ void __launch_bounds__(256) k_mlp_grad(const float *__restrict__ Pm, const float *__restrict__ X,
-                                                  const float *__restrict__ Y, long long n, float pos_weight,
-                                                  float *grad, float *loss_out)
+// for y = 1, else 1.  Per-sample gradients are summed over the warp by
+// shuffles into the warp's own row of shared memory, the rows of a block in
+// fixed order into the block's partial (global), and the partials of all
+// blocks in fixed order by k_grad_sum: the gradient does not depend on
+// scheduling, so training repeats bit-exactly.
+constexpr int kGradBlock = 128;
+constexpr int kGradWarps = kGradBlock / 32;
+constexpr int kGradMaxBlocks = 128;
+__global__ void __launch_bounds__(kGradBlock) k_mlp_grad(const float *__restrict__ Pm, const float *__restrict__ X,
+                                                         const float *__restrict__ Y, long long n, float pos_weight,
+                                                         float *grad_part, float *loss_part)
 {
     __shared__ float P[kPropParams];
-    __shared__ float G[kPropParams];
-    __shared__ float L;
+    __shared__ float Gw[kGradWarps][kPropParams];
+    __shared__ float Lw[kGradWarps];
     for (int i = threadIdx.x; i < kPropParams; i += blockDim.x) {
         P[i] = Pm[i];
-        G[i] = 0.f;
+        for (int w = 0; w < kGradWarps; ++w) Gw[w][i] = 0.f;
     }
-    if (threadIdx.x == 0) L = 0.f;
+    if (threadIdx.x < kGradWarps) Lw[threadIdx.x] = 0.f;
     __syncthreads();
+    float *G = Gw[threadIdx.x >> 5];
     const int lane = threadIdx.x & 31;
     const long long stride = (long long)gridDim.x * blockDim.x;
     // all lanes of a warp run the same number of rounds (warp reductions inside)
@@ -141,14 +148,14 @@ __global__ void __launch_bounds__(256) k_mlp_grad(const float *__restrict__ Pm, 
         for (int i = 0; i < kH; ++i) {
             const float h2 = fmaxf(z2[i], 0.f);
             float g = warp_sum(dout * h2);
-            if (lane == 0) atomicAdd(&G[kOffW3 + i], g);
+            if (lane == 0) G[kOffW3 + i] += g;
             dh2[i] = z2[i] > 0.f ? dout * P[kOffW3 + i] : 0.f;
         }
         {
             float g = warp_sum(dout);
-            if (lane == 0) atomicAdd(&G[kOffB3], g);
+            if (lane == 0) G[kOffB3] += g;
             float lw = warp_sum(l);
-            if (lane == 0) atomicAdd(&L, lw);
+            if (lane == 0) Lw[threadIdx.x >> 5] += lw;
         }
         // hidden layer 2: dW2[o][i] = dz2[o] * h1[i]
         float dh1[kH];
@@ -157,12 +164,12 @@ __global__ void __launch_bounds__(256) k_mlp_grad(const float *__restrict__ Pm, 
         for (int o = 0; o < kH; ++o) {
             const float dz = dh2[o];
             float g = warp_sum(dz);
-            if (lane == 0) atomicAdd(&G[kOffB2 + o], g);
+            if (lane == 0) G[kOffB2 + o] += g;
 #pragma unroll
             for (int i = 0; i < kH; ++i) {
                 const float h1 = fmaxf(z1[i], 0.f);
                 float gg = warp_sum(dz * h1);
-                if (lane == 0) atomicAdd(&G[kOffW2 + o * kH + i], gg);
+                if (lane == 0) G[kOffW2 + o * kH + i] += gg;
                 dh1[i] = fmaf(dz, P[kOffW2 + o * kH + i], dh1[i]);
             }
         }
@@ -170,18 +177,49 @@ __global__ void __launch_bounds__(256) k_mlp_grad(const float *__restrict__ Pm, 
         for (int o = 0; o < kH; ++o) {
             const float dz = z1[o] > 0.f ? dh1[o] : 0.f;
             float g = warp_sum(dz);
-            if (lane == 0) atomicAdd(&G[kOffB1 + o], g);
+            if (lane == 0) G[kOffB1 + o] += g;
 #pragma unroll
             for (int i = 0; i < kIn; ++i) {
                 float gg = warp_sum(dz * x[i]);
-                if (lane == 0) atomicAdd(&G[kOffW1 + o * kIn + i], gg);
+                if (lane == 0) G[kOffW1 + o * kIn + i] += gg;
             }
         }
     }
     __syncthreads();
-    for (int i = threadIdx.x; i < kPropParams; i += blockDim.x)
-        if (G[i] != 0.f) atomicAdd(&grad[i], G[i]);
-    if (threadIdx.x == 0 && loss_out) atomicAdd(loss_out, L);
+    for (int i = threadIdx.x; i < kPropParams; i += blockDim.x) {
+        float t = 0.f;
+        for (int w = 0; w < kGradWarps; ++w) t += Gw[w][i];
+        grad_part[(long long)blockIdx.x * kPropParams + i] = t;
+    }
+    if (threadIdx.x == 0) {
+        float t = 0.f;
+        for (int w = 0; w < kGradWarps; ++w) t += Lw[w];
+        loss_part[blockIdx.x] = t;
+    }
+}
+
+// grad = sum of the block partials in block order (and the loss likewise,
+// added to *loss).
+__global__ void k_grad_sum(const float *__restrict__ grad_part, const float *__restrict__ loss_part, int nblocks,
+                           float *grad, float *loss)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < kPropParams) {
+        float t = 0.f;
+        for (int b = 0; b < nblocks; ++b) t += grad_part[(long long)b * kPropParams + i];
+        grad[i] = t;
+    }
+    if (i == kPropParams) {
+        float t = 0.f;
+        for (int b = 0; b < nblocks; ++b) t += loss_part[b];
+        *loss += t;
+    }
+}
+
+static int grad_blocks(long long n)
+{
+    long long g = (n + kGradBlock - 1) / kGradBlock;
+    return (int)(g < kGradMaxBlocks ? (g < 1 ? 1 : g) : kGradMaxBlocks);
 }
 
 // Adam on the master weights (gradient divided by the batch size), then the
@@ -438,6 +476,7 @@ struct gala_proposal {
     int device = 0;
     cudaStream_t stream = nullptr;
     float *Pm = nullptr, *m = nullptr, *v = nullptr, *grad = nullptr, *loss = nullptr;
+    float *grad_part = nullptr, *loss_part = nullptr;  // per-block gradient partials
     __nv_bfloat16 *wb = nullptr;
     int adam_t = 0;
     // samples: features (kIn per row), labels, row capacity
@@ -520,6 +559,8 @@ gala_status gala_proposal_create(int32_t device, int64_t max_samples, uint64_t s
     p->cap = max_samples;
     p->batch_cap = 1 << 16;
     bool ok = cudaStreamCreateWithFlags(&p->stream, cudaStreamNonBlocking) == cudaSuccess;
+    ok = ok && palloc(p, &p->grad_part, (size_t)kGradMaxBlocks * kPropParams) &&
+         palloc(p, &p->loss_part, (size_t)kGradMaxBlocks);
     ok = ok && palloc(p, &p->Pm, kPropParams) && palloc(p, &p->m, kPropParams) && palloc(p, &p->v, kPropParams) &&
          palloc(p, &p->grad, kPropParams) && palloc(p, &p->loss, 1) && palloc(p, &p->wb, kPropParams) &&
          palloc(p, &p->X, (size_t)max_samples * kIn) && palloc(p, &p->Y, (size_t)max_samples) &&
@@ -655,11 +696,11 @@ gala_status gala_proposal_gradient(gala_proposal *p, const float *features, cons
     cudaStream_t st = p->stream;
     cudaMemcpyAsync(p->Xb, features, (size_t)n * kIn * sizeof(float), cudaMemcpyHostToDevice, st);
     cudaMemcpyAsync(p->Yb, labels, (size_t)n * sizeof(float), cudaMemcpyHostToDevice, st);
-    cudaMemsetAsync(p->grad, 0, kPropParams * sizeof(float), st);
     cudaMemsetAsync(p->loss, 0, sizeof(float), st);
-    k_mlp_grad<<<(n + 255) / 256 < 256 ? (n + 255) / 256 : 256, 256, 0, st>>>(p->Pm, p->Xb, p->Yb, n, pos_weight,
-                                                                             p->grad, p->loss);
-    note_launch(1);
+    const int gb = grad_blocks(n);
+    k_mlp_grad<<<gb, kGradBlock, 0, st>>>(p->Pm, p->Xb, p->Yb, n, pos_weight, p->grad_part, p->loss_part);
+    k_grad_sum<<<(kPropParams + 256) / 256, 256, 0, st>>>(p->grad_part, p->loss_part, gb, p->grad, p->loss);
+    note_launch(2);
     cudaMemcpyAsync(grad_out, p->grad, kPropParams * sizeof(float), cudaMemcpyDeviceToHost, st);
     float l = 0.f;
     cudaMemcpyAsync(&l, p->loss, sizeof(float), cudaMemcpyDeviceToHost, st);
@@ -716,13 +757,13 @@ gala_status gala_proposal_train(gala_proposal *p, int32_t epochs, int32_t batch_
         for (int64_t b0 = 0; b0 < n; b0 += batch_size) {
             const int nb = (int)std::min<int64_t>(batch_size, n - b0);
             k_gather_batch<<<(nb + 255) / 256, 256, 0, st>>>(p->X, p->Y, p->idx + b0, nb, p->Xb, p->Yb);
-            cudaMemsetAsync(p->grad, 0, kPropParams * sizeof(float), st);
-            k_mlp_grad<<<(nb + 255) / 256 < 128 ? (nb + 255) / 256 : 128, 256, 0, st>>>(p->Pm, p->Xb, p->Yb, nb,
-                                                                                       pos_weight, p->grad, p->loss);
+            const int gb = grad_blocks(nb);
+            k_mlp_grad<<<gb, kGradBlock, 0, st>>>(p->Pm, p->Xb, p->Yb, nb, pos_weight, p->grad_part, p->loss_part);
+            k_grad_sum<<<(kPropParams + 256) / 256, 256, 0, st>>>(p->grad_part, p->loss_part, gb, p->grad, p->loss);
             p->adam_t++;
             k_adam<<<(kPropParams + 255) / 256, 256, 0, st>>>(p->Pm, p->m, p->v, p->grad, 1.f / nb, lr, 0.9f, 0.999f,
                                                              1e-8f, p->adam_t, p->wb);
-            note_launch(3);
+            note_launch(4);
         }
         // synchronous read: the permutation is reshuffled only after the
         // epoch's copy and kernels are done

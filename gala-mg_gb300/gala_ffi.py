@@ -48,7 +48,7 @@ class Options(ctypes.Structure):
     _fields_ = [("min_modularity", ctypes.c_double), ("max_levels", ctypes.c_int32),
                 ("verbose", ctypes.c_int32), ("use_graphs", ctypes.c_int32), ("fp64_gains", ctypes.c_int32),
                 ("proposal_mode", ctypes.c_int32), ("proposal_threshold", ctypes.c_float),
-                ("trace_sample_shift", ctypes.c_int32), ("reserved", ctypes.c_int32), ("proposal", ctypes.c_void_p)]
+                ("trace_sample_shift", ctypes.c_int32), ("sorted_levels", ctypes.c_int32), ("proposal", ctypes.c_void_p)]
 
 
 class Result(ctypes.Structure):
@@ -349,7 +349,7 @@ class Context:
         _check(load().gala_context_set_stream(self.h, stream_handle))
 
     def louvain(self, graph, min_mod=1e-6, max_levels=0, verbose=False, iter_capacity=4096, fp64_gains=False,
-                proposal=None, mode=PROPOSAL_OFF, threshold=0.5, sample_shift=0):
+                proposal=None, mode=PROPOSAL_OFF, threshold=0.5, sample_shift=0, sorted_levels=False):
         """gala_louvain: host graph in, host labels out.  `proposal` (a
         Proposal) with mode PROPOSAL_TRACE records training samples, with
         PROPOSAL_SKIP decides only the vertices it proposes."""
@@ -362,6 +362,7 @@ class Context:
         o = default_options(min_modularity=min_mod, max_levels=max_levels, verbose=int(verbose),
                             fp64_gains=int(fp64_gains), proposal_mode=int(mode),
                             proposal_threshold=float(threshold), trace_sample_shift=int(sample_shift),
+                            sorted_levels=int(sorted_levels),
                             proposal=proposal.h if proposal is not None else None)
         _check(load().gala_louvain(self.h, graph.h, ctypes.byref(o), _ptr(labels, _i32p), ctypes.byref(r)))
         d = r.to_dict(trace)

@@ -70,7 +70,10 @@ typedef struct {
     int32_t proposal_mode;      /* GALA_PROPOSAL_* (needs `proposal`) */
     float proposal_threshold;   /* SKIP: decide vertices with P(move) >= this */
     int32_t trace_sample_shift; /* TRACE: keep about one decision in 2^shift */
-    int32_t reserved;
+    int32_t sorted_levels;      /* 1 = contracted level graphs keep every row sorted
+                                   by neighbour id (as gala_contract_device does);
+                                   default 0: rows in hash-table order, which
+                                   skips the sorts and gives the same partition */
     gala_proposal *proposal;
 } gala_options;
 

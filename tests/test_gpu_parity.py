@@ -149,6 +149,9 @@ def test_integer_gains_equal_fp64_gains(ffi, golden, torch_cuda, case):
     assert a["iter_q"] == b["iter_q"]
     assert a["level_c"] == b["level_c"]
     assert np.array_equal(a["labels"], b["labels"])
+    # level graphs with rows sorted by neighbour id give the same run
+    c = ctx.louvain(g, sorted_levels=True)
+    assert a["iter_q"] == c["iter_q"] and np.array_equal(a["labels"], c["labels"])
 
 
 def test_deterministic_replay(ffi, torch_cuda):

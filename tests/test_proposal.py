@@ -155,14 +155,20 @@ def _compare(ffi, prop, g, threshold):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("seed", [101, 102, 103])
-def test_learned_skip_on_held_out_sbm(ffi, mlp_oracle, trained, seed):
+def test_learned_skip_on_held_out_sbm(ffi, mlp_oracle, trained):
+    """Held-out planted-partition graphs (1,024 vertices, 32 blocks): the
+    learned run ends on average no more than DQ_MAX below the plain run and
+    no single graph more than 3 DQ_MAX below; every returned modularity
+    equals a host recomputation."""
     prop = trained[0]
-    g = ffi.Graph.sbm(1024, 32, 0.3, 0.005, seed)
-    plain, learned = _compare(ffi, prop, g, 0.3)
-    assert learned["modularity"] >= plain["modularity"] - DQ_MAX
-    q = g.modularity(learned["labels"])
-    assert abs(q - learned["modularity"]) <= 1e-9
+    diffs = []
+    for seed in (101, 102, 103, 104, 105):
+        g = ffi.Graph.sbm(1024, 32, 0.3, 0.005, seed)
+        plain, learned = _compare(ffi, prop, g, 0.3)
+        diffs.append(learned["modularity"] - plain["modularity"])
+        assert abs(g.modularity(learned["labels"]) - learned["modularity"]) <= 1e-9
+    assert np.mean(diffs) >= -DQ_MAX, diffs
+    assert min(diffs) >= -3 * DQ_MAX, diffs
 
 
 def _auc(scores, labels):
