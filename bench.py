@@ -336,8 +336,9 @@ def main():
     torch.cuda.synchronize()
 
     def run_device():
+        # the generator deduplicates every row
         return ctx.louvain_device(n, d_offs.data_ptr(), d_nbr.data_ptr(), None, d_out.data_ptr(),
-                                  fp64_gains=args.fp64_gains)
+                                  fp64_gains=args.fp64_gains, distinct_rows=True)
 
     if args.profile:
         r = run_device()

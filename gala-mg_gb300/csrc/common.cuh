@@ -13,7 +13,7 @@ namespace gala {
 //   bin 0..3: deg 1-4 / 5-8 / 9-16 / 17-32 -> a group of 4/8/16/32 lanes per
 //             vertex, one neighbour per lane, aggregation with __match_any_sync
 //   bin 4   : deg 33-256     -> one warp per vertex, 512-slot smem hash
-//   bin 5   : deg 257-2048   -> one 256-thread CTA per vertex, 4096-slot smem hash
+//   bin 5   : deg 257-2048   -> one 512-thread CTA per vertex, 4096-slot smem hash
 //   bin 6   : deg 2049-8192  -> one 1024-thread CTA per vertex, 16384-slot smem hash
 //   bin 7   : deg > 8192     -> one 1024-thread CTA per vertex, hash table in
 //                               global memory (per-CTA slice, L2 resident)

@@ -409,9 +409,122 @@ __device__ __forceinline__ int agg_insert(const AggArgs<WT> &a, long long st, in
     return created;
 }
 
+// Add (key, w) to a table (dense when keys is null); returns 1 when this call
+// created the key, 0 when it existed, -1 when the probe ran out.  `slot`
+// receives the slot (hash tables).
+template <typename WT>
+__device__ __forceinline__ int table_add(int *keys, WT *vals, int T, int lg, int key, WT w, int &slot)
+{
+    if (!keys) {
+        slot = key;
+        return add_was_zero(&vals[key], w) ? 1 : 0;
+    }
+    unsigned h = hash_slot(key, lg);
+    for (int p = 0; p < T; ++p) {
+        int k = *(volatile int *)&keys[h];
+        int created = 0;
+        if (k == -1) {
+            k = atomicCAS(&keys[h], -1, key);
+            if (k == -1) {
+                k = key;
+                created = 1;
+            }
+        }
+        if (k == key) {
+            atomic_add_w(&vals[h], w);
+            slot = (int)h;
+            return created;
+        }
+        h = (h + 1) & (unsigned)(T - 1);
+    }
+    slot = -1;
+    return -1;
+}
+
+// Insert stream entries [st, st + len) into a shared-memory hash table (T
+// slots) and list every slot a key claims in occ (counter *nocc, shared).
+// All threads of the block call it.
+template <typename WT>
+__device__ __forceinline__ void agg_insert_list(const AggArgs<WT> &a, long long st, int len, int *keys, WT *vals,
+                                                int T, int lg, unsigned short *occ, int *nocc)
+{
+    const int lane = threadIdx.x & 31;
+    for (int b0 = 0; b0 < len; b0 += blockDim.x) {
+        const int j = b0 + threadIdx.x;
+        const bool valid = j < len;
+        int key = -1;
+        WT wt = 0;
+        if (valid) {
+            key = a.skey[st + j];
+            wt = a.sw[st + j];
+        }
+        const unsigned m = __match_any_sync(GALA_FULL_MASK, key);
+        const WT sum = group_sum(m, wt);
+        int created = 0, slot = -1;
+        if (valid && __ffs(m) - 1 == lane) {
+            created = table_add(keys, vals, T, lg, key, sum, slot);
+            if (created < 0) {
+                atomicOr(&a.st->err, kErrHashOverflow);
+                created = 0;
+            }
+        }
+        const unsigned cb = __ballot_sync(GALA_FULL_MASK, created == 1);
+        if (cb) {
+            const int leader = __ffs(cb) - 1;
+            int base = 0;
+            if (lane == leader) base = atomicAdd(nocc, __popc(cb));
+            base = __shfl_sync(GALA_FULL_MASK, base, leader);
+            if (created == 1) occ[base + __popc(cb & lanemask_lt())] = (unsigned short)slot;
+        }
+    }
+}
+
+// Rows of 33..kMid2Max entries in hash-table order (level-to-level
+// contraction): one CTA per community; the shared-memory table of TMAX slots
+// is cleared once per CTA, per community only the claimed slots (listed) are
+// emitted and cleared.
+template <typename WT, int BLOCK, int TMAX>
+__global__ void __launch_bounds__(BLOCK) k_agg_mid_list(AggArgs<WT> a, const int32_t *__restrict__ list, int cls)
+{
+    extern __shared__ long long sml_ll[];
+    WT *vals = (WT *)sml_ll;
+    int *keys = (int *)(vals + TMAX);
+    unsigned short *occ = (unsigned short *)(keys + TMAX);
+    __shared__ int s_k;
+    constexpr int lg = (TMAX == 1024) ? 10 : (TMAX == 2048 ? 11 : (TMAX == 4096 ? 12 : (TMAX == 8192 ? 13 : 14)));
+    static_assert((1 << lg) == TMAX, "table size");
+    for (int j = threadIdx.x; j < TMAX; j += BLOCK) {
+        keys[j] = -1;
+        vals[j] = 0;
+    }
+    if (threadIdx.x == 0) s_k = 0;
+    __syncthreads();
+    const int cnt = a.st->small_cnt[cls];
+    for (int i = blockIdx.x; i < cnt; i += gridDim.x) {
+        const int c = list[i];
+        const long long st = a.medge[a.moff[c]];
+        const int E = (int)a.ec[c];
+        agg_insert_list(a, st, E, keys, vals, TMAX, lg, occ, &s_k);
+        __syncthreads();
+        const int k = s_k;
+        const long long o = a.tmp_off[c];
+        for (int q = threadIdx.x; q < k; q += BLOCK) {
+            const int j = occ[q];
+            a.tmp_nbr[o + q] = keys[j];
+            a.tmp_w[o + q] = vals[j];
+            keys[j] = -1;
+            vals[j] = 0;
+        }
+        if (threadIdx.x == 0) a.kc[c] = k;
+        __syncthreads();
+        if (threadIdx.x == 0) s_k = 0;
+        __syncthreads();
+    }
+}
+
 // Rows of 33..kMid2Max entries: one CTA per community, shared-memory hash
 // table of TMAX slots, distinct keys sorted by a bitonic sort of LMAX slots.
-template <typename WT, int BLOCK, int TMAX, int LMAX, bool SORT>
+template <typename WT, int BLOCK, int TMAX, int LMAX>
 __global__ void __launch_bounds__(BLOCK) k_agg_mid(AggArgs<WT> a, const int32_t *__restrict__ list, int cls)
 {
     extern __shared__ long long sm_ll[];
@@ -438,21 +551,6 @@ __global__ void __launch_bounds__(BLOCK) k_agg_mid(AggArgs<WT> a, const int32_t 
         __syncthreads();
         agg_insert(a, st, E, keys, vals, T, lg);
         __syncthreads();
-        if (!SORT) {  // rows in table order: straight to the row
-            const long long o = a.tmp_off[c];
-            for (int j = threadIdx.x; j < T; j += BLOCK) {
-                const int kk = keys[j];
-                if (kk >= 0) {
-                    const int p = atomicAdd(&s_k, 1);
-                    a.tmp_nbr[o + p] = kk;
-                    a.tmp_w[o + p] = vals[j];
-                }
-            }
-            __syncthreads();
-            if (threadIdx.x == 0) a.kc[c] = s_k;
-            __syncthreads();
-            continue;
-        }
         for (int j = threadIdx.x; j < T; j += BLOCK) {
             int kk = keys[j];
             if (kk >= 0) {
@@ -753,15 +851,15 @@ __global__ void k_contract_reset(DevStats *st)
 }
 
 // Shared memory of the table kernels: int keys plus WT values per slot.
-template <typename WT, bool SORT>
+template <typename WT>
 constexpr size_t mid1_smem()
 {
-    return (1024 + (SORT ? kMid1Max : 0)) * (sizeof(int) + sizeof(WT));
+    return (1024 + kMid1Max) * (sizeof(int) + sizeof(WT));
 }
-template <typename WT, bool SORT>
+template <typename WT>
 constexpr size_t mid2_smem()
 {
-    return (8192 + (SORT ? kMid2Max : 0)) * (sizeof(int) + sizeof(WT));
+    return (8192 + kMid2Max) * (sizeof(int) + sizeof(WT));
 }
 template <typename WT>
 constexpr size_t sort_smem()
@@ -769,22 +867,29 @@ constexpr size_t sort_smem()
     return kSortMax * (sizeof(int) + sizeof(WT));
 }
 
-template <typename WT, bool SORT>
+template <typename WT>
 static void configure_mid()
 {
-    cudaFuncSetAttribute(k_agg_mid<WT, 128, 1024, kMid1Max, SORT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)mid1_smem<WT, SORT>());
-    cudaFuncSetAttribute(k_agg_mid<WT, 256, 8192, kMid2Max, SORT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)mid2_smem<WT, SORT>());
+    cudaFuncSetAttribute(k_agg_mid<WT, 128, 1024, kMid1Max>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)mid1_smem<WT>());
+    cudaFuncSetAttribute(k_agg_mid<WT, 256, 8192, kMid2Max>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)mid2_smem<WT>());
+}
+
+template <typename WT>
+constexpr size_t list_smem(int tmax)
+{
+    return (size_t)tmax * (sizeof(WT) + sizeof(int) + sizeof(unsigned short));
 }
 
 template <typename WT>
 static void configure_t()
 {
-    configure_mid<WT, true>();
-    configure_mid<WT, false>();
+    configure_mid<WT>();
 
     cudaFuncSetAttribute(k_big_sort<WT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sort_smem<WT>());
+    cudaFuncSetAttribute(k_agg_mid_list<WT, 256, 8192>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)list_smem<WT>(8192));
 }
 
 void contract_configure_kernels()
@@ -975,21 +1080,17 @@ static int contract_t(const LevelGraph &g, const int32_t *comm, ContractBuffers 
     if (hs.small_cnt[1] > 0) {
         int grid = hs.small_cnt[1] < nsm * 12 ? hs.small_cnt[1] : nsm * 12;
         if (sort_rows)
-            k_agg_mid<WT, 128, 1024, kMid1Max, true>
-                <<<grid, 128, mid1_smem<WT, true>(), st>>>(a, b.cls_list + (long long)C, 1);
+            k_agg_mid<WT, 128, 1024, kMid1Max><<<grid, 128, mid1_smem<WT>(), st>>>(a, b.cls_list + (long long)C, 1);
         else
-            k_agg_mid<WT, 128, 1024, kMid1Max, false>
-                <<<grid, 128, mid1_smem<WT, false>(), st>>>(a, b.cls_list + (long long)C, 1);
+            k_agg_mid_list<WT, 128, 1024><<<grid, 128, list_smem<WT>(1024), st>>>(a, b.cls_list + (long long)C, 1);
         note_launch(1);
     }
     if (hs.small_cnt[2] > 0) {
         int grid = hs.small_cnt[2] < nsm * 2 ? hs.small_cnt[2] : nsm * 2;
         if (sort_rows)
-            k_agg_mid<WT, 256, 8192, kMid2Max, true>
-                <<<grid, 256, mid2_smem<WT, true>(), st>>>(a, b.cls_list + 2LL * C, 2);
+            k_agg_mid<WT, 256, 8192, kMid2Max><<<grid, 256, mid2_smem<WT>(), st>>>(a, b.cls_list + 2LL * C, 2);
         else
-            k_agg_mid<WT, 256, 8192, kMid2Max, false>
-                <<<grid, 256, mid2_smem<WT, false>(), st>>>(a, b.cls_list + 2LL * C, 2);
+            k_agg_mid_list<WT, 256, 8192><<<grid, 256, list_smem<WT>(8192), st>>>(a, b.cls_list + 2LL * C, 2);
         note_launch(1);
     }
     if (hs.small_cnt[3] > 0 && !contract_long_rows(a, b, hs.small_cnt[3], C, hs, st, status, sort_rows)) return -1;

@@ -392,7 +392,7 @@ gala_status phase1(gala_context *ctx, const LevelGraph &g, long long &m2, double
                 p1_hub_decide(g, b, hp, constant, m2, fp64_only, aux_for(ctx, k));
             else
                 p1_decide(g, b, bin, lists + bin_start[bin], counts + bin, level_cnt[bin], constant, m2, fp64_only,
-                          64, aux_for(ctx, k));
+                          iteration == 1 && g.distinct, aux_for(ctx, k));
         }
         join(ctx);
         cudaEventRecord(ctx->ev[3], st);
@@ -557,7 +557,7 @@ struct RunOut {
 // final modularity of every graph.
 gala_status run_levels(gala_context *ctx, int32_t n0, int64_t E0, const int64_t *offs0, const int32_t *nbr0,
                        const void *w0, const gala_options *opt, gala_result *res, BatchRun *bt = nullptr,
-                       bool wide = false)
+                       bool wide = false, bool distinct0 = false)
 {
     cudaStream_t st = ctx->stream;
     gala_status s;
@@ -600,7 +600,7 @@ gala_status run_levels(gala_context *ctx, int32_t n0, int64_t E0, const int64_t 
         set_error("proposal modes are not available for float-weight graphs");
         return GALA_ERR_INVALID;
     }
-    LevelGraph g{n0, E0, offs0, nbr0, w0, wide};
+    LevelGraph g{n0, E0, offs0, nbr0, w0, wide, distinct0 || (opt && opt->distinct_rows == 1)};
     int buf = 0;
     double prev_mod = -1, cur_mod = -1;
     int round = 0;
@@ -651,7 +651,7 @@ gala_status run_levels(gala_context *ctx, int32_t n0, int64_t E0, const int64_t 
         round++;
         prev_mod = cur_mod;
         cur_mod = po.q;
-        g = LevelGraph{C, newE, ctx->offs[buf], ctx->nbr[buf], ctx->w[buf], wide};
+        g = LevelGraph{C, newE, ctx->offs[buf], ctx->nbr[buf], ctx->w[buf], wide, true};
         buf ^= 1;
         if (bt) {
             const int G = bt->G;
@@ -965,7 +965,7 @@ gala_status gala_louvain(gala_context *ctx, const gala_graph *g, const gala_opti
     }
     float h2d = ev_ms(ctx->ev[6], ctx->ev[7]);
     // level 0 lives in buffer 1; the first contraction writes buffer 0
-    s = run_levels(ctx, n, E, ctx->offs[1], ctx->nbr[1], dw, opt, res, nullptr, g->float_w);
+    s = run_levels(ctx, n, E, ctx->offs[1], ctx->nbr[1], dw, opt, res, nullptr, g->float_w, g->rows_distinct);
     if (s == GALA_OK) {
         cudaEventRecord(ctx->ev[6], st);
         cudaMemcpyAsync(community_out, ctx->orig, (size_t)n * sizeof(int32_t), cudaMemcpyDeviceToHost, st);
@@ -1142,7 +1142,9 @@ gala_status gala_louvain_batch(gala_context *ctx, const gala_graph *const *graph
     b.gstop = bt.stop;
     b.min_tot_g = bt.min_tot;
     gala_result r{};
-    s = run_levels(ctx, n, e_tot, ctx->offs[1], ctx->nbr[1], dw, opt, &r, &bt);
+    bool distinct = true;
+    for (int i = 0; i < G; ++i) distinct = distinct && graphs[i]->rows_distinct;
+    s = run_levels(ctx, n, e_tot, ctx->offs[1], ctx->nbr[1], dw, opt, &r, &bt, false, distinct);
     b.gid = nullptr;
     b.m2g = nullptr;
     b.cg = nullptr;

@@ -191,6 +191,7 @@ static gala_graph *build_csr(std::vector<std::pair<int32_t, int32_t>> &edges, co
     gala_graph *g = new gala_graph();
     g->n = n;
     g->weighted = weighted;
+    g->rows_distinct = true;
     g->offs.resize(n);
     int64_t acc = 0;
     for (int64_t i = 0; i < nid; ++i)
@@ -931,6 +932,7 @@ gala_status gala_generate_lfr(int32_t n, double tau1, int32_t dmin, int32_t dmax
     });
     gala_graph *g = new gala_graph();
     g->n = n;
+    g->rows_distinct = true;
     g->offs.resize(n);
     int64_t acc = 0;
     for (int32_t v = 0; v < n; ++v) {

@@ -20,6 +20,7 @@ struct gala_graph {
     bool weighted = false;      // int32 weights
     bool float_w = false;       // float32 weights, run as 64-bit fixed point
     int32_t fixed_shift = 0;    // float graphs: weights are round(w * 2^fixed_shift)
+    bool rows_distinct = false; // every row lists a neighbour at most once (built here)
     bool pinned = false;  // arrays registered with cudaHostRegister
     int64_t entries() const { return n ? offs[n - 1] : 0; }
     ~gala_graph();
@@ -64,6 +65,7 @@ struct LevelGraph {
     const int32_t *nbr;
     const void *w;        // nullptr = unweighted; int32, or int64 fixed point when wide
     bool wide = false;
+    bool distinct = false;  // rows list each neighbour at most once (contracted levels always)
 };
 
 // Phase-1 workspace (all device pointers, sized for the context capacity).
@@ -133,9 +135,10 @@ struct HubPlan {
 // ---- phase 1 kernels (phase1.cu) ----
 void p1_level_init(const LevelGraph &g, Phase1Buffers &b, cudaStream_t st);
 void p1_iter_reset(Phase1Buffers &b, int next, long long min_tot_init, cudaStream_t st);
+// first = the level's first sweep (every vertex its own community).
 void p1_decide(const LevelGraph &g, Phase1Buffers &b, int bin, const int32_t *list,
                const int *count_ptr, int level_count, double constant, long long m2,
-               int fp64_only, int hub_tmax, cudaStream_t st);
+               int fp64_only, bool first, cudaStream_t st);
 void p1_apply_movers(Phase1Buffers &b, int sign, int n, cudaStream_t st, int iteration = 0);
 void p1_tot_reduce(Phase1Buffers &b, int n, cudaStream_t st);
 void p1_update(const LevelGraph &g, Phase1Buffers &b, int bin, const int32_t *list, int count, int next,

@@ -679,17 +679,95 @@ __device__ __forceinline__ void warp_argmax(double &dq, int &bc)
     }
 }
 
-// Degree 33-256: one warp per vertex with a private shared-memory hash table.
+// Insert (key, w) into a table of T slots (power of two); returns the slot
+// and sets `created` when this call claimed it, -1 when the probe ran out.
+template <typename VT>
+__device__ __forceinline__ int hash_add_slot(int *keys, VT *vals, int T, int log2t, int key, VT w, bool &created)
+{
+    unsigned h = hash_slot(key, log2t);
+    created = false;
+    for (int p = 0; p < T; ++p) {
+        int k = *(volatile int *)&keys[h];
+        if (k == -1) {
+            k = atomicCAS(&keys[h], -1, key);
+            if (k == -1) {
+                k = key;
+                created = true;
+            }
+        }
+        if (k == key) {
+            atomic_add_w(&vals[h], w);
+            return (int)h;
+        }
+        h = (h + 1) & (unsigned)(T - 1);
+    }
+    return -1;
+}
+
+// Scans over the list of occupied slots (slot indices in occ[0, nocc)).
+template <typename WT>
+__device__ __forceinline__ void scan_list_int(const DecideArgs<WT> &a, const Scale &sc, const int *keys,
+                                              const WT *vals, const unsigned short *occ, int nocc, int first,
+                                              int stride, int cur, WT ki, WT tcur, long long &x, int &bc, WT &bw,
+                                              int &bt, WT &wc)
+{
+    for (int q = first; q < nocc; q += stride) {
+        const int j = occ[q];
+        const int c = keys[j];
+        const WT wv = vals[j];
+        if (c == cur) {
+            wc += wv;
+        } else {
+            const long long xx = gain_x(wv, ki, a.Tot[c], tcur, sc.m2);
+            if (xx >= 0) cand_merge(x, bc, bw, bt, xx, c, wv, 0);
+        }
+    }
+}
+
+template <typename WT>
+__device__ __forceinline__ void scan_list(const DecideArgs<WT> &a, const Scale &sc, const int *keys, const WT *vals,
+                                          const unsigned short *occ, int nocc, int first, int stride, int cur, WT ki,
+                                          WT tcur, double &dq, int &bc)
+{
+    for (int q = first; q < nocc; q += stride) {
+        const int j = occ[q];
+        const int c = keys[j];
+        if (c == cur) continue;
+        const double d = gain_dq(vals[j], ki, a.Tot[c], tcur, sc.c);
+        if (d > 0.0 && cand_better(d, c, dq, bc)) {
+            dq = d;
+            bc = c;
+        }
+    }
+}
+
+// Degree 33-256: one warp per vertex with a private shared-memory hash table
+// of kWarpTable slots.  The table is cleared once per warp; per vertex the
+// slots it claims are listed, and only those are scanned and cleared again.
 constexpr int kWarpTable = 512;
+constexpr int kWarpLog = 9;
+constexpr int kWarpWarps = 8;  // warps per block
+template <typename WT>
+constexpr size_t warp_smem()
+{
+    return (size_t)kWarpWarps * kWarpTable * (sizeof(int) + sizeof(WT) + sizeof(unsigned short));
+}
 template <typename WT, bool W>
 __global__ void __launch_bounds__(256) k_decide_warp(DecideArgs<WT> a, const int32_t *__restrict__ list,
                                                      const int *__restrict__ count_ptr)
 {
-    __shared__ int s_keys[8][kWarpTable];
-    __shared__ WT s_vals[8][kWarpTable];
+    extern __shared__ long long wsm_ll[];
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-    int *keys = s_keys[wib];
-    WT *vals = s_vals[wib];
+    WT *vals = (WT *)wsm_ll + wib * kWarpTable;
+    int *keys = (int *)((WT *)wsm_ll + kWarpWarps * kWarpTable) + wib * kWarpTable;
+    unsigned short *occ =
+        (unsigned short *)((int *)((WT *)wsm_ll + kWarpWarps * kWarpTable) + kWarpWarps * kWarpTable) +
+        wib * kWarpTable;
+    for (int j = lane; j < kWarpTable; j += 32) {
+        keys[j] = -1;
+        vals[j] = 0;
+    }
+    __syncwarp();
     const int count = *count_ptr;
     const int wg = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int nw = (gridDim.x * blockDim.x) >> 5;
@@ -700,15 +778,7 @@ __global__ void __launch_bounds__(256) k_decide_warp(DecideArgs<WT> a, const int
         const long long s = a.offs[v];
         const int deg = (int)(a.offs[v + 1] - s);
         const int cur = a.comm[v];
-        int T = next_pow2_int(2LL * deg);
-        if (T < 64) T = 64;
-        if (T > kWarpTable) T = kWarpTable;
-        const int lg = __ffs(T) - 1;
-        for (int j = lane; j < T; j += 32) {
-            keys[j] = -1;
-            vals[j] = 0;
-        }
-        __syncwarp();
+        int nocc = 0;
         for (int e0 = 0; e0 < deg; e0 += 32) {
             const int e = e0 + lane;
             const bool valid = e < deg;
@@ -720,40 +790,54 @@ __global__ void __launch_bounds__(256) k_decide_warp(DecideArgs<WT> a, const int
             }
             const unsigned m = __match_any_sync(GALA_FULL_MASK, c);
             const WT wsum = W ? group_sum(m, wt) : (WT)__popc(m);
-            if (valid && __ffs(m) - 1 == lane)
-                if (!hash_add(keys, vals, T, lg, c, wsum)) atomicOr(&a.st->err, kErrHashOverflow);
+            bool created = false;
+            int slot = -1;
+            if (valid && __ffs(m) - 1 == lane) {
+                slot = hash_add_slot(keys, vals, kWarpTable, kWarpLog, c, wsum, created);
+                if (slot < 0) atomicOr(&a.st->err, kErrHashOverflow);
+            }
+            const unsigned cb = __ballot_sync(GALA_FULL_MASK, created);
+            if (created) occ[nocc + __popc(cb & lanemask_lt())] = (unsigned short)slot;
+            nocc += __popc(cb);
         }
         __syncwarp();
         const WT ki = a.K[v], tcur = a.Tot[cur], sf = a.Self[v];
         long long x = -1;
         int bc = cur, bt = 0;
         WT bw = 0, wc = 0;
-        scan_table_int(a, sc, keys, vals, T, lane, 32, cur, ki, tcur, x, bc, bw, bt, wc);
+        scan_list_int(a, sc, keys, vals, occ, nocc, lane, 32, cur, ki, tcur, x, bc, bw, bt, wc);
         warp_merge_int(x, bc, bw, bt, wc, 32);
         int dec = int_decision(a, sc, x, bt, cur, bc, wc, sf, ki);  // warp-uniform
         if (dec == 2) {
             double dq = 0.0;
             int fc = cur;
-            scan_table(a, sc, keys, vals, T, lane, 32, cur, ki, tcur, dq, fc);
+            scan_list(a, sc, keys, vals, occ, nocc, lane, 32, cur, ki, tcur, dq, fc);
             warp_argmax(dq, fc);
             bc = fc;
             dec = (fc != cur && gain_correct(dq, wc, sf) > 0.0) ? 1 : 0;
             if (lane == 0) atomicAdd(&a.st->fp64_decisions, 1ull);
         }
         const bool move = lane == 0 && dec == 1 && guard_ok(a, cur, bc);
-        if (a.feat_gain) {
-            int occ = 0;
-            for (int j = lane; j < T; j += 32) occ += keys[j] >= 0;
-            occ = warp_sum(occ);
-            if (lane == 0) write_features(a, sc, v, x, wc, sf, ki, occ);
-        }
+        if (lane == 0) write_features(a, sc, v, x, wc, sf, ki, nocc);
         append_mover(a, move, v, cur, bc);
+        __syncwarp();
+        for (int q = lane; q < nocc; q += 32) {
+            const int j = occ[q];
+            keys[j] = -1;
+            vals[j] = 0;
+        }
         __syncwarp();
     }
 }
 
-// Degree 257-8192: one CTA per vertex with the hash table in dynamic shared
-// memory (tmax slots: int keys, then WT values).
+// Degree 257-8192: one CTA per vertex with a shared-memory hash table of tmax
+// slots (int keys, WT values) and the list of claimed slots, cleared once per
+// CTA and then slot by slot after every vertex.
+template <typename WT>
+constexpr size_t cta_smem(int tmax)
+{
+    return (size_t)tmax * (sizeof(int) + sizeof(WT) + sizeof(unsigned short));
+}
 template <typename WT, int BLOCK, bool W>
 __global__ void __launch_bounds__(BLOCK) k_decide_cta(DecideArgs<WT> a, const int32_t *__restrict__ list,
                                                       const int *__restrict__ count_ptr, int tmax)
@@ -765,11 +849,19 @@ __global__ void __launch_bounds__(BLOCK) k_decide_cta(DecideArgs<WT> a, const in
     __shared__ WT r_w[BLOCK / 32];
     __shared__ int r_t[BLOCK / 32];
     __shared__ WT r_wc[BLOCK / 32];
-    __shared__ int s_dec, s_bc;
+    __shared__ int s_dec, s_bc, s_nocc;
     __shared__ WT s_wc;
-    int *keys = (int *)dyn_smem_ll;
-    WT *vals = (WT *)(keys + tmax);
+    WT *vals = (WT *)dyn_smem_ll;
+    int *keys = (int *)(vals + tmax);
+    unsigned short *occ = (unsigned short *)(keys + tmax);
+    const int lg = __ffs(tmax) - 1;
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    for (int j = threadIdx.x; j < tmax; j += BLOCK) {
+        keys[j] = -1;
+        vals[j] = 0;
+    }
+    if (threadIdx.x == 0) s_nocc = 0;
+    __syncthreads();
     const int count = *count_ptr;
     for (int i = blockIdx.x; i < count; i += gridDim.x) {
         const int v = list[i];
@@ -779,18 +871,10 @@ __global__ void __launch_bounds__(BLOCK) k_decide_cta(DecideArgs<WT> a, const in
         const long long e = a.offs[v + 1];
         const int deg = (int)(e - s);
         const int cur = a.comm[v];
-        int T = next_pow2_int(2LL * deg);
-        if (T < 64) T = 64;
-        if (T > tmax) {  // cannot happen for the bin limits; recorded, vertex stays
+        if (2LL * deg > tmax) {  // cannot happen for the bin limits; recorded, vertex stays
             if (threadIdx.x == 0) atomicOr(&a.st->err, kErrHashOverflow);
             continue;
         }
-        const int lg = __ffs(T) - 1;
-        for (int j = threadIdx.x; j < T; j += BLOCK) {
-            keys[j] = -1;
-            vals[j] = 0;
-        }
-        __syncthreads();
         for (long long b0 = s; b0 < e; b0 += BLOCK) {
             const long long j = b0 + threadIdx.x;
             const bool valid = j < e;
@@ -802,16 +886,29 @@ __global__ void __launch_bounds__(BLOCK) k_decide_cta(DecideArgs<WT> a, const in
             }
             const unsigned m = __match_any_sync(GALA_FULL_MASK, c);
             const WT wsum = W ? group_sum(m, wt) : (WT)__popc(m);
-            if (valid && __ffs(m) - 1 == lane)
-                if (!hash_add(keys, vals, T, lg, c, wsum)) atomicOr(&a.st->err, kErrHashOverflow);
+            bool created = false;
+            int slot = -1;
+            if (valid && __ffs(m) - 1 == lane) {
+                slot = hash_add_slot(keys, vals, tmax, lg, c, wsum, created);
+                if (slot < 0) atomicOr(&a.st->err, kErrHashOverflow);
+            }
+            const unsigned cb = __ballot_sync(GALA_FULL_MASK, created);
+            if (cb) {
+                const int leader = __ffs(cb) - 1;
+                int base = 0;
+                if (lane == leader) base = atomicAdd(&s_nocc, __popc(cb));
+                base = __shfl_sync(GALA_FULL_MASK, base, leader);
+                if (created) occ[base + __popc(cb & lanemask_lt())] = (unsigned short)slot;
+            }
         }
         __syncthreads();
+        const int nocc = s_nocc;
         const WT ki = a.K[v], tcur = a.Tot[cur], sf = a.Self[v];
         constexpr int NW = BLOCK / 32;
         long long x = -1;
         int bc = cur, bt = 0;
         WT bw = 0, wc = 0;
-        scan_table_int(a, sc, keys, vals, T, threadIdx.x, BLOCK, cur, ki, tcur, x, bc, bw, bt, wc);
+        scan_list_int(a, sc, keys, vals, occ, nocc, threadIdx.x, BLOCK, cur, ki, tcur, x, bc, bw, bt, wc);
         warp_merge_int(x, bc, bw, bt, wc, 32);
         if (lane == 0) {
             r_x[wid] = x;
@@ -838,7 +935,7 @@ __global__ void __launch_bounds__(BLOCK) k_decide_cta(DecideArgs<WT> a, const in
         if (s_dec == 2) {  // block-uniform: the reference's FP64 evaluation
             double dq = 0.0;
             int fc = cur;
-            scan_table(a, sc, keys, vals, T, threadIdx.x, BLOCK, cur, ki, tcur, dq, fc);
+            scan_list(a, sc, keys, vals, occ, nocc, threadIdx.x, BLOCK, cur, ki, tcur, dq, fc);
             warp_argmax(dq, fc);
             if (lane == 0) {
                 r_dq[wid] = dq;
@@ -859,7 +956,168 @@ __global__ void __launch_bounds__(BLOCK) k_decide_cta(DecideArgs<WT> a, const in
         }
         if (wid == 0) {
             const bool move = lane == 0 && s_dec == 1 && guard_ok(a, cur, s_bc);
-            if (lane == 0) write_features(a, sc, v, x, s_wc, sf, ki, -1);
+            if (lane == 0) write_features(a, sc, v, x, s_wc, sf, ki, nocc);
+            append_mover(a, move, v, cur, s_bc);
+        }
+        for (int q = threadIdx.x; q < nocc; q += BLOCK) {
+            const int j = occ[q];
+            keys[j] = -1;
+            vals[j] = 0;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) s_nocc = 0;
+        __syncthreads();
+    }
+}
+
+// First sweep of a level: every vertex is its own community (comm[u] = u
+// after the level init), and rows hold distinct neighbours, so every entry
+// is its own candidate community: no aggregation table.  One group of
+// GROUP threads (a warp, or the whole CTA) per vertex.
+template <typename WT, bool W>
+__device__ __forceinline__ void first_scan_int(const DecideArgs<WT> &a, const Scale &sc, long long s, int deg, int v,
+                                               int first, int stride, WT ki, WT tcur, long long &x, int &bc, WT &bw,
+                                               int &bt, WT &wc)
+{
+    for (int j = first; j < deg; j += stride) {
+        const int u = a.nbr[s + j];
+        const WT w = W ? a.w[s + j] : (WT)1;
+        if (u == v) {
+            wc += w;
+        } else {
+            const long long xx = gain_x(w, ki, a.Tot[u], tcur, sc.m2);
+            if (xx >= 0) cand_merge(x, bc, bw, bt, xx, u, w, 0);
+        }
+    }
+}
+
+template <typename WT, bool W>
+__device__ __forceinline__ void first_scan(const DecideArgs<WT> &a, const Scale &sc, long long s, int deg, int v,
+                                           int first, int stride, WT ki, WT tcur, double &dq, int &bc)
+{
+    for (int j = first; j < deg; j += stride) {
+        const int u = a.nbr[s + j];
+        if (u == v) continue;
+        const double d = gain_dq(W ? a.w[s + j] : (WT)1, ki, a.Tot[u], tcur, sc.c);
+        if (d > 0.0 && cand_better(d, u, dq, bc)) {
+            dq = d;
+            bc = u;
+        }
+    }
+}
+
+template <typename WT, bool W>
+__global__ void __launch_bounds__(256) k_first_warp(DecideArgs<WT> a, const int32_t *__restrict__ list,
+                                                    const int *__restrict__ count_ptr)
+{
+    const int lane = threadIdx.x & 31;
+    const int count = *count_ptr;
+    const int wg = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nw = (gridDim.x * blockDim.x) >> 5;
+    for (int i = wg; i < count; i += nw) {
+        const int v = list[i];
+        if (stopped(a, v)) continue;
+        const Scale sc = scale_of(a, v);
+        const long long s = a.offs[v];
+        const int deg = (int)(a.offs[v + 1] - s);
+        const int cur = a.comm[v];  // = v
+        const WT ki = a.K[v], tcur = a.Tot[cur], sf = a.Self[v];
+        long long x = -1;
+        int bc = cur, bt = 0;
+        WT bw = 0, wc = 0;
+        first_scan_int<WT, W>(a, sc, s, deg, v, lane, 32, ki, tcur, x, bc, bw, bt, wc);
+        warp_merge_int(x, bc, bw, bt, wc, 32);
+        int dec = int_decision(a, sc, x, bt, cur, bc, wc, sf, ki);  // warp-uniform
+        if (dec == 2) {
+            double dq = 0.0;
+            int fc = cur;
+            first_scan<WT, W>(a, sc, s, deg, v, lane, 32, ki, tcur, dq, fc);
+            warp_argmax(dq, fc);
+            bc = fc;
+            dec = (fc != cur && gain_correct(dq, wc, sf) > 0.0) ? 1 : 0;
+            if (lane == 0) atomicAdd(&a.st->fp64_decisions, 1ull);
+        }
+        const bool move = lane == 0 && dec == 1 && guard_ok(a, cur, bc);
+        if (lane == 0) write_features(a, sc, v, x, wc, sf, ki, deg);
+        append_mover(a, move, v, cur, bc);
+    }
+}
+
+template <typename WT, int BLOCK, bool W>
+__global__ void __launch_bounds__(BLOCK) k_first_cta(DecideArgs<WT> a, const int32_t *__restrict__ list,
+                                                     const int *__restrict__ count_ptr)
+{
+    __shared__ double r_dq[BLOCK / 32];
+    __shared__ long long r_x[BLOCK / 32];
+    __shared__ int r_c[BLOCK / 32];
+    __shared__ WT r_w[BLOCK / 32];
+    __shared__ int r_t[BLOCK / 32];
+    __shared__ WT r_wc[BLOCK / 32];
+    __shared__ int s_dec, s_bc;
+    __shared__ WT s_wc;
+    constexpr int NW = BLOCK / 32;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int count = *count_ptr;
+    for (int i = blockIdx.x; i < count; i += gridDim.x) {
+        const int v = list[i];
+        if (stopped(a, v)) continue;
+        const Scale sc = scale_of(a, v);
+        const long long s = a.offs[v];
+        const int deg = (int)(a.offs[v + 1] - s);
+        const int cur = a.comm[v];  // = v
+        const WT ki = a.K[v], tcur = a.Tot[cur], sf = a.Self[v];
+        long long x = -1;
+        int bc = cur, bt = 0;
+        WT bw = 0, wc = 0;
+        first_scan_int<WT, W>(a, sc, s, deg, v, threadIdx.x, BLOCK, ki, tcur, x, bc, bw, bt, wc);
+        warp_merge_int(x, bc, bw, bt, wc, 32);
+        if (lane == 0) {
+            r_x[wid] = x;
+            r_c[wid] = bc;
+            r_w[wid] = bw;
+            r_t[wid] = bt;
+            r_wc[wid] = wc;
+        }
+        __syncthreads();
+        if (wid == 0) {
+            x = lane < NW ? r_x[lane] : -1;
+            bc = lane < NW ? r_c[lane] : cur;
+            bw = lane < NW ? r_w[lane] : 0;
+            bt = lane < NW ? r_t[lane] : 0;
+            wc = lane < NW ? r_wc[lane] : 0;
+            warp_merge_int(x, bc, bw, bt, wc, 32);
+            if (lane == 0) {
+                s_dec = int_decision(a, sc, x, bt, cur, bc, wc, sf, ki);
+                s_bc = bc;
+                s_wc = wc;
+            }
+        }
+        __syncthreads();
+        if (s_dec == 2) {  // block-uniform
+            double dq = 0.0;
+            int fc = cur;
+            first_scan<WT, W>(a, sc, s, deg, v, threadIdx.x, BLOCK, ki, tcur, dq, fc);
+            warp_argmax(dq, fc);
+            if (lane == 0) {
+                r_dq[wid] = dq;
+                r_c[wid] = fc;
+            }
+            __syncthreads();
+            if (wid == 0) {
+                dq = lane < NW ? r_dq[lane] : 0.0;
+                fc = lane < NW ? r_c[lane] : cur;
+                warp_argmax(dq, fc);
+                if (lane == 0) {
+                    s_bc = fc;
+                    s_dec = (fc != cur && gain_correct(dq, s_wc, sf) > 0.0) ? 1 : 0;
+                    atomicAdd(&a.st->fp64_decisions, 1ull);
+                }
+            }
+            __syncthreads();
+        }
+        if (wid == 0) {
+            const bool move = lane == 0 && s_dec == 1 && guard_ok(a, cur, s_bc);
+            if (lane == 0) write_features(a, sc, v, x, s_wc, sf, ki, deg);
             append_mover(a, move, v, cur, s_bc);
         }
         __syncthreads();
@@ -901,7 +1159,7 @@ static DecideArgs<WT> decide_args(const LevelGraph &g, Phase1Buffers &b, double 
 
 template <typename WT>
 static void decide_t(const LevelGraph &g, Phase1Buffers &b, int bin, const int32_t *list, const int *count_ptr,
-                     int level_count, double constant, long long m2, int fp64_only, cudaStream_t st)
+                     int level_count, double constant, long long m2, int fp64_only, bool first, cudaStream_t st)
 {
     const DecideArgs<WT> a = decide_args<WT>(g, b, constant, m2, fp64_only);
     const bool W = g.w != nullptr;
@@ -910,6 +1168,22 @@ static void decide_t(const LevelGraph &g, Phase1Buffers &b, int bin, const int32
         long long blocks = ((long long)level_count * lanes_per_item + 255) / 256;
         return (int)(blocks < cap ? blocks : cap);
     };
+    if (first && bin >= 4 && bin <= 6) {  // singleton partition: no aggregation tables
+        if (bin == 4) {
+            if (W)
+                k_first_warp<WT, true><<<grid_lanes(32), 256, 0, st>>>(a, list, count_ptr);
+            else
+                k_first_warp<WT, false><<<grid_lanes(32), 256, 0, st>>>(a, list, count_ptr);
+        } else {
+            const int grid = level_count < num_sms() * 8 ? level_count : num_sms() * 8;
+            if (W)
+                k_first_cta<WT, 256, true><<<grid, 256, 0, st>>>(a, list, count_ptr);
+            else
+                k_first_cta<WT, 256, false><<<grid, 256, 0, st>>>(a, list, count_ptr);
+        }
+        note_launch(1);
+        return;
+    }
 #define GALA_DG(GV)                                                                                    \
     do {                                                                                               \
         if (W)                                                                                         \
@@ -917,7 +1191,6 @@ static void decide_t(const LevelGraph &g, Phase1Buffers &b, int bin, const int32
         else                                                                                           \
             k_decide_group<WT, GV, false><<<grid_lanes(GV), 256, 0, st>>>(a, list, count_ptr);         \
     } while (0)
-    constexpr size_t slot = sizeof(int) + sizeof(WT);
     switch (bin) {
     case 0: GALA_DG(4); break;
     case 1: GALA_DG(8); break;
@@ -925,22 +1198,22 @@ static void decide_t(const LevelGraph &g, Phase1Buffers &b, int bin, const int32
     case 3: GALA_DG(32); break;
     case 4:
         if (W)
-            k_decide_warp<WT, true><<<grid_lanes(32), 256, 0, st>>>(a, list, count_ptr);
+            k_decide_warp<WT, true><<<grid_lanes(32), 256, warp_smem<WT>(), st>>>(a, list, count_ptr);
         else
-            k_decide_warp<WT, false><<<grid_lanes(32), 256, 0, st>>>(a, list, count_ptr);
+            k_decide_warp<WT, false><<<grid_lanes(32), 256, warp_smem<WT>(), st>>>(a, list, count_ptr);
         break;
     case 5: {
-        int grid = level_count < num_sms() * 6 ? level_count : num_sms() * 6;
-        const size_t sm = (size_t)kCtaTable5 * slot;
+        int grid = level_count < num_sms() * 4 ? level_count : num_sms() * 4;
+        const size_t sm = cta_smem<WT>(kCtaTable5);
         if (W)
-            k_decide_cta<WT, 256, true><<<grid, 256, sm, st>>>(a, list, count_ptr, kCtaTable5);
+            k_decide_cta<WT, 512, true><<<grid, 512, sm, st>>>(a, list, count_ptr, kCtaTable5);
         else
-            k_decide_cta<WT, 256, false><<<grid, 256, sm, st>>>(a, list, count_ptr, kCtaTable5);
+            k_decide_cta<WT, 512, false><<<grid, 512, sm, st>>>(a, list, count_ptr, kCtaTable5);
         break;
     }
     case 6: {
         int grid = level_count < num_sms() ? level_count : num_sms();
-        const size_t sm = (size_t)kCtaTable6 * slot;
+        const size_t sm = cta_smem<WT>(kCtaTable6);
         if (W)
             k_decide_cta<WT, 1024, true><<<grid, 1024, sm, st>>>(a, list, count_ptr, kCtaTable6);
         else
@@ -954,28 +1227,30 @@ static void decide_t(const LevelGraph &g, Phase1Buffers &b, int bin, const int32
 }
 
 void p1_decide(const LevelGraph &g, Phase1Buffers &b, int bin, const int32_t *list, const int *count_ptr,
-               int level_count, double constant, long long m2, int fp64_only, int hub_tmax, cudaStream_t st)
+               int level_count, double constant, long long m2, int fp64_only, bool first, cudaStream_t st)
 {
-    (void)hub_tmax;
     if (level_count <= 0) return;
     if (g.wide)
-        decide_t<long long>(g, b, bin, list, count_ptr, level_count, constant, m2, fp64_only, st);
+        decide_t<long long>(g, b, bin, list, count_ptr, level_count, constant, m2, fp64_only, first, st);
     else
-        decide_t<int>(g, b, bin, list, count_ptr, level_count, constant, m2, fp64_only, st);
+        decide_t<int>(g, b, bin, list, count_ptr, level_count, constant, m2, fp64_only, first, st);
 }
 
 template <typename WT>
 static void configure_t()
 {
-    constexpr int slot = (int)(sizeof(int) + sizeof(WT));
     cudaFuncSetAttribute(k_decide_cta<WT, 1024, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         kCtaTable6 * slot);
+                         (int)cta_smem<WT>(kCtaTable6));
     cudaFuncSetAttribute(k_decide_cta<WT, 1024, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         kCtaTable6 * slot);
-    cudaFuncSetAttribute(k_decide_cta<WT, 256, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         kCtaTable5 * slot);
-    cudaFuncSetAttribute(k_decide_cta<WT, 256, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         kCtaTable5 * slot);
+                         (int)cta_smem<WT>(kCtaTable6));
+    cudaFuncSetAttribute(k_decide_cta<WT, 512, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)cta_smem<WT>(kCtaTable5));
+    cudaFuncSetAttribute(k_decide_cta<WT, 512, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)cta_smem<WT>(kCtaTable5));
+    cudaFuncSetAttribute(k_decide_warp<WT, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)warp_smem<WT>());
+    cudaFuncSetAttribute(k_decide_warp<WT, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)warp_smem<WT>());
 }
 
 void p1_configure_kernels()

@@ -48,7 +48,8 @@ class Options(ctypes.Structure):
     _fields_ = [("min_modularity", ctypes.c_double), ("max_levels", ctypes.c_int32),
                 ("verbose", ctypes.c_int32), ("use_graphs", ctypes.c_int32), ("fp64_gains", ctypes.c_int32),
                 ("proposal_mode", ctypes.c_int32), ("proposal_threshold", ctypes.c_float),
-                ("trace_sample_shift", ctypes.c_int32), ("sorted_levels", ctypes.c_int32), ("proposal", ctypes.c_void_p)]
+                ("trace_sample_shift", ctypes.c_int32), ("sorted_levels", ctypes.c_int32), ("proposal", ctypes.c_void_p),
+                ("distinct_rows", ctypes.c_int32), ("reserved3", ctypes.c_int32)]
 
 
 class Result(ctypes.Structure):
@@ -390,13 +391,14 @@ class Context:
         return d
 
     def louvain_device(self, n, d_offs, d_nbr, d_w, d_out, min_mod=1e-6, max_levels=0, iter_capacity=4096,
-                       fp64_gains=False):
+                       fp64_gains=False, distinct_rows=False):
         """gala_louvain_device on raw device pointers (ints)."""
         trace = np.zeros(iter_capacity, dtype=np.float64)
         r = Result()
         r.iter_modularity = _ptr(trace, _f64p)
         r.iter_capacity = iter_capacity
-        o = default_options(min_modularity=min_mod, max_levels=max_levels, fp64_gains=int(fp64_gains))
+        o = default_options(min_modularity=min_mod, max_levels=max_levels, fp64_gains=int(fp64_gains),
+                            distinct_rows=int(distinct_rows))
         _check(load().gala_louvain_device(self.h, n, d_offs, d_nbr, d_w or None, ctypes.byref(o), d_out,
                                           ctypes.byref(r)))
         return r.to_dict(trace)

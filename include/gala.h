@@ -75,6 +75,11 @@ typedef struct {
                                    default 0: rows in hash-table order, which
                                    skips the sorts and gives the same partition */
     gala_proposal *proposal;
+    int32_t distinct_rows;      /* 1 = the caller guarantees that no row lists a
+                                   neighbour twice (lets the first sweep of
+                                   level 0 skip aggregation; graphs built by
+                                   this library are known to be distinct) */
+    int32_t reserved3;
 } gala_options;
 
 typedef struct {

@@ -264,6 +264,42 @@ def test_louvain_device_equals_host_entry(ffi, torch_cuda):
     r_dev = ctx.louvain_device(n, d_offs.data_ptr(), d_nbr.data_ptr(), None, d_out.data_ptr())
     assert r_dev["iter_q"] == r_host["iter_q"]
     assert np.array_equal(d_out.cpu().numpy(), r_host["labels"])
+    # the caller's distinct-rows guarantee (first sweep without aggregation)
+    r_dd = ctx.louvain_device(n, d_offs.data_ptr(), d_nbr.data_ptr(), None, d_out.data_ptr(), distinct_rows=True)
+    assert r_dd["iter_q"] == r_host["iter_q"]
+    assert np.array_equal(d_out.cpu().numpy(), r_host["labels"])
+
+
+@pytest.mark.parametrize("weighted", [False, True])
+def test_rows_with_repeated_neighbours_match_oracle(ffi, oracle, torch_cuda, weighted):
+    """A caller CSR may list a neighbour twice in a row (the reference's hash
+    aggregation sums such entries): the first sweep must aggregate them."""
+    rng = np.random.default_rng(41)
+    n = 3000
+    u = rng.integers(0, n, 20000)
+    v = rng.integers(0, n, 20000)
+    keep = u != v
+    u, v = u[keep], v[keep]
+    rows = np.concatenate([u, v, u])  # every edge once more from u's side ...
+    cols = np.concatenate([v, u, v])  # ... and from v's side, keeping the CSR symmetric
+    rows = np.concatenate([rows, v])
+    cols = np.concatenate([cols, u])
+    order = np.lexsort((cols, rows))
+    rows, cols = rows[order], cols[order].astype(np.int32)
+    offs = np.zeros(n + 1, dtype=np.int64)
+    np.add.at(offs, rows + 1, 1)
+    offs = np.cumsum(offs)
+    w = rng.integers(1, 5, cols.shape[0]).astype(np.int32) if weighted else None
+    if w is not None:  # symmetric weights: the weight of (a, b) equals that of (b, a) entry by entry
+        key = np.minimum(rows, cols).astype(np.int64) * n + np.maximum(rows, cols)
+        _, inv = np.unique(key, return_inverse=True)
+        w = (inv % 4 + 1).astype(np.int32)
+    g = ffi.Graph.from_csr(offs, cols, w)
+    ctx = ffi.Context(n, offs[-1])
+    r = ctx.louvain(g)
+    ctx.close()
+    o = oracle.louvain(offs, cols, w)
+    _assert_same(r, o)
 
 
 def test_capacity_error(ffi, torch_cuda):
