@@ -15,8 +15,8 @@ namespace gala {
 //   bin 4   : deg 33-256     -> one warp per vertex, 512-slot smem hash
 //   bin 5   : deg 257-2048   -> one 512-thread CTA per vertex, 4096-slot smem hash
 //   bin 6   : deg 2049-8192  -> one 1024-thread CTA per vertex, 16384-slot smem hash
-//   bin 7   : deg > 8192     -> one 1024-thread CTA per vertex, hash table in
-//                               global memory (per-CTA slice, L2 resident)
+//   bin 7   : deg > 8192     -> hub rows: global hash tables filled and scanned
+//                               by many CTAs (4096-entry / 4096-slot chunks)
 //   bin 8   : deg 0          -> never processed (the reference bins start at 1,
 //                               louvain_main_process.cu:278)
 // ---------------------------------------------------------------------------

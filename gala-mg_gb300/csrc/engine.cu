@@ -225,7 +225,7 @@ long long decide_bytes_for(long long nv, long long ne, bool weighted)
 // have stopped.
 gala_status phase1(gala_context *ctx, const LevelGraph &g, long long &m2, double min_mod, bool verbose,
                    std::vector<double> *trace, Phase1Out *out, int fp64_only = 0, const PropRun *pr = nullptr,
-                   BatchRun *bt = nullptr)
+                   BatchRun *bt = nullptr, bool use_graphs = false)
 {
     const int pmode = pr ? pr->mode : GALA_PROPOSAL_OFF;
     cudaStream_t st = ctx->stream;
@@ -360,6 +360,18 @@ gala_status phase1(gala_context *ctx, const LevelGraph &g, long long &m2, double
     const long long min_tot_init = (!g.wide && m2 > 0x7fffffffLL) ? 0x7fffffffLL : m2;
     unsigned long long skipped0 = h->skipped, skipped_e0 = h->skipped_edges;
     bool verify = false;  // proposals stalled: the rest of the level runs plain sweeps
+    // CUDA graphs of the repeated sweeps (plain runs): one per active-list slot
+    const bool graphs = use_graphs && pmode == GALA_PROPOSAL_OFF;
+    cudaGraphExec_t gexec[2] = {nullptr, nullptr};
+    long long glaunch[2] = {0, 0};
+    struct GraphGuard {
+        cudaGraphExec_t *e;
+        ~GraphGuard()
+        {
+            for (int i = 0; i < 2; ++i)
+                if (e[i]) cudaGraphExecDestroy(e[i]);
+        }
+    } gguard{gexec};
     cudaEventRecord(ctx->ev[0], st);
     for (;;) {
         const int nxt = cur ^ 1;
@@ -376,53 +388,84 @@ gala_status phase1(gala_context *ctx, const LevelGraph &g, long long &m2, double
             ps.iteration = iteration;
             ps.level = pr->level;
         }
-        p1_iter_reset(b, nxt, min_tot_init, st);
-        cudaEventRecord(ctx->ev[2], st);
-        if ((pmode == GALA_PROPOSAL_TRACE && iteration > 1) || proposal_sweep) {
-            p1_proposal_step(g, b, ps, lists, counts, bin_start, level_cnt, st);
-            if (proposal_sweep) {
-                lists = b.prop_list;
-                counts = &b.stats->prop_count[0];
+        // the sweep: decide, apply, reductions, update, counters to the host
+        auto enqueue = [&](bool capturing) {
+            // timing events become event nodes of a captured graph
+            auto rec = [&](cudaEvent_t e) {
+                if (capturing)
+                    cudaEventRecordWithFlags(e, st, cudaEventRecordExternal);
+                else
+                    cudaEventRecord(e, st);
+            };
+            p1_iter_reset(b, nxt, min_tot_init, st);
+            rec(ctx->ev[2]);
+            if ((pmode == GALA_PROPOSAL_TRACE && iteration > 1) || proposal_sweep) {
+                p1_proposal_step(g, b, ps, lists, counts, bin_start, level_cnt, st);
+                if (proposal_sweep) {
+                    lists = b.prop_list;
+                    counts = &b.stats->prop_count[0];
+                }
             }
-        }
-        fork(ctx);
-        for (int k = 0; k < kNumBins; ++k) {
-            const int bin = kBinLaunchOrder[k];
-            if (bin == 7)
-                p1_hub_decide(g, b, hp, constant, m2, fp64_only, aux_for(ctx, k));
+            fork(ctx);
+            for (int k = 0; k < kNumBins; ++k) {
+                const int bin = kBinLaunchOrder[k];
+                if (bin == 7)
+                    p1_hub_decide(g, b, hp, constant, m2, fp64_only, aux_for(ctx, k));
+                else
+                    p1_decide(g, b, bin, lists + bin_start[bin], counts + bin, level_cnt[bin], constant, m2,
+                              fp64_only, iteration == 1 && g.distinct, aux_for(ctx, k));
+            }
+            join(ctx);
+            rec(ctx->ev[3]);
+            p1_apply_movers(b, +1, g.n, st, iteration);
+            if (pmode == GALA_PROPOSAL_TRACE && iteration > 1) p1_trace_labels(b, ps, st);
+            if (bt)
+                batch_graph_sums(kMinTot | kSumTot2, G, bt->goff, bt->stop, b, bt->sums(), st);
             else
-                p1_decide(g, b, bin, lists + bin_start[bin], counts + bin, level_cnt[bin], constant, m2, fp64_only,
-                          iteration == 1 && g.distinct, aux_for(ctx, k));
+                p1_tot_reduce(b, g.n, st);
+            rec(ctx->ev[4]);
+            fork(ctx);
+            for (int k = 0; k < kNumBins; ++k) {
+                const int bin = kBinLaunchOrder[k];
+                if (bin == 7)
+                    p1_hub_update(g, b, hp, nxt, bin_start[bin], constant, m2, aux_for(ctx, k));
+                else
+                    p1_update(g, b, bin, b.order + bin_start[bin], level_cnt[bin], nxt, bin_start[bin], constant,
+                              m2, aux_for(ctx, k));
+            }
+            join(ctx);
+            if (bt) {
+                batch_graph_sums(kSumIn, G, bt->goff, bt->stop, b, bt->sums(), st);
+                cudaMemcpyAsync(bt->h_sum_in, bt->sum_in, G * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+                                st);
+                cudaMemcpyAsync(bt->h_sum_tot2, bt->sum_tot2, G * sizeof(unsigned long long),
+                                cudaMemcpyDeviceToHost, st);
+            }
+            rec(ctx->ev[5]);
+            cudaMemcpyAsync(h, b.stats, sizeof(DevStats), cudaMemcpyDeviceToHost, st);
+        };
+        if (graphs && iteration > 1) {
+            // sweeps after the first repeat the same launches with the active
+            // lists of slot `cur`: captured once per level and slot, replayed
+            if (!gexec[cur]) {
+                const long long l0 = gala_kernel_launch_count();
+                cudaGraph_t gr = nullptr;
+                if ((s = check(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal), "graph capture")))
+                    return s;
+                enqueue(true);
+                if ((s = check(cudaStreamEndCapture(st, &gr), "graph capture"))) return s;
+                const cudaError_t ie = cudaGraphInstantiate(&gexec[cur], gr, 0);
+                cudaGraphDestroy(gr);
+                if ((s = check(ie, "graph instantiate"))) return s;
+                glaunch[cur] = gala_kernel_launch_count() - l0;
+                note_launch((int)-glaunch[cur]);  // counted when replayed
+            }
+            if ((s = check(cudaGraphLaunch(gexec[cur], st), "graph launch"))) return s;
+            note_launch((int)glaunch[cur]);
+        } else {
+            enqueue(false);
         }
-        join(ctx);
-        cudaEventRecord(ctx->ev[3], st);
-        p1_apply_movers(b, +1, g.n, st, iteration);
-        if (pmode == GALA_PROPOSAL_TRACE && iteration > 1) p1_trace_labels(b, ps, st);
-        if (bt)
-            batch_graph_sums(kMinTot | kSumTot2, G, bt->goff, bt->stop, b, bt->sums(), st);
-        else
-            p1_tot_reduce(b, g.n, st);
-        cudaEventRecord(ctx->ev[4], st);
-        fork(ctx);
-        for (int k = 0; k < kNumBins; ++k) {
-            const int bin = kBinLaunchOrder[k];
-            if (bin == 7)
-                p1_hub_update(g, b, hp, nxt, bin_start[bin], constant, m2, aux_for(ctx, k));
-            else
-                p1_update(g, b, bin, b.order + bin_start[bin], level_cnt[bin], nxt, bin_start[bin], constant, m2,
-                          aux_for(ctx, k));
-        }
-        join(ctx);
-        if (bt) {
-            batch_graph_sums(kSumIn, G, bt->goff, bt->stop, b, bt->sums(), st);
-            cudaMemcpyAsync(bt->h_sum_in, bt->sum_in, G * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st);
-            cudaMemcpyAsync(bt->h_sum_tot2, bt->sum_tot2, G * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
-                            st);
-        }
-        cudaEventRecord(ctx->ev[5], st);
-        if ((s = check(cudaMemcpyAsync(h, b.stats, sizeof(DevStats), cudaMemcpyDeviceToHost, st), "iteration")) ||
-            (s = check(cudaStreamSynchronize(st), "iteration")))
-            return s;
+        if ((s = check(cudaStreamSynchronize(st), "iteration"))) return s;
         if (h->err) {
             set_error("phase 1: device error bits %d", h->err);
             return GALA_ERR_OVERFLOW;
@@ -616,7 +659,9 @@ gala_status run_levels(gala_context *ctx, int32_t n0, int64_t E0, const int64_t 
         if (verbose) printf("===============round:%d===============\n", round);
         Phase1Out po;
         pr.level = round;
-        if ((s = phase1(ctx, g, m2, min_mod, verbose, &trace, &po, opt ? opt->fp64_gains : 0, &pr, bt))) return s;
+        if ((s = phase1(ctx, g, m2, min_mod, verbose, &trace, &po, opt ? opt->fp64_gains : 0, &pr, bt,
+                        opt && opt->use_graphs)))
+            return s;
         if (bt)  // communities per graph, for the graphs' id ranges at the next level
             batch_graph_sums(kCountComm, bt->G, bt->goff, nullptr, ctx->p1, bt->sums(), st);
         decisions += po.decisions;

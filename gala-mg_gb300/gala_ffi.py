@@ -350,7 +350,8 @@ class Context:
         _check(load().gala_context_set_stream(self.h, stream_handle))
 
     def louvain(self, graph, min_mod=1e-6, max_levels=0, verbose=False, iter_capacity=4096, fp64_gains=False,
-                proposal=None, mode=PROPOSAL_OFF, threshold=0.5, sample_shift=0, sorted_levels=False):
+                proposal=None, mode=PROPOSAL_OFF, threshold=0.5, sample_shift=0, sorted_levels=False,
+                use_graphs=False):
         """gala_louvain: host graph in, host labels out.  `proposal` (a
         Proposal) with mode PROPOSAL_TRACE records training samples, with
         PROPOSAL_SKIP decides only the vertices it proposes."""
@@ -363,14 +364,14 @@ class Context:
         o = default_options(min_modularity=min_mod, max_levels=max_levels, verbose=int(verbose),
                             fp64_gains=int(fp64_gains), proposal_mode=int(mode),
                             proposal_threshold=float(threshold), trace_sample_shift=int(sample_shift),
-                            sorted_levels=int(sorted_levels),
+                            sorted_levels=int(sorted_levels), use_graphs=int(use_graphs),
                             proposal=proposal.h if proposal is not None else None)
         _check(load().gala_louvain(self.h, graph.h, ctypes.byref(o), _ptr(labels, _i32p), ctypes.byref(r)))
         d = r.to_dict(trace)
         d["labels"] = labels
         return d
 
-    def louvain_batch(self, graphs, min_mod=1e-6, max_levels=0):
+    def louvain_batch(self, graphs, min_mod=1e-6, max_levels=0, use_graphs=False):
         """gala_louvain_batch: many host graphs in one union run.  Returns the
         per-graph labels (local community ids), modularity and community
         counts plus the batch timings."""
@@ -381,7 +382,7 @@ class Context:
         c = np.zeros(G, dtype=np.int32)
         hs = (_vp * G)(*[g.h for g in graphs])
         r = BatchResult()
-        o = default_options(min_modularity=min_mod, max_levels=max_levels)
+        o = default_options(min_modularity=min_mod, max_levels=max_levels, use_graphs=int(use_graphs))
         _check(load().gala_louvain_batch(self.h, hs, G, ctypes.byref(o), _ptr(labels, _i32p), _ptr(q, _f64p),
                                          _ptr(c, _i32p), ctypes.byref(r)))
         starts = np.concatenate([[0], np.cumsum(sizes)])

@@ -62,7 +62,9 @@ typedef struct {
     int32_t max_levels;    /* 0 = run until the gain is below min_modularity */
     int32_t verbose;       /* 1 = print the reference's stdout lines
                               (README.md:59-89, louvain_main_process.cu:1003) */
-    int32_t use_graphs;    /* 1 = replay each phase-1 iteration as a CUDA graph */
+    int32_t use_graphs;    /* 1 = the phase-1 sweeps after the first of a level are
+                              captured once per level (per active-list slot)
+                              as CUDA graphs and replayed (plain runs) */
     int32_t fp64_gains;    /* 1 = evaluate every gain with the reference's FP64
                               expressions (default 0: exact integer gains,
                               FP64 only where rounding could decide; both give

@@ -72,8 +72,11 @@ def test_batch_equals_single_runs(ffi, oracle, torch_cuda):
     tot_e = sum(g.info()[1] for g in graphs)
     ctx = ffi.Context(tot_n, tot_e)
     r = ctx.louvain_batch(graphs)
+    rg = ctx.louvain_batch(graphs, use_graphs=True)
     ctx.close()
     assert r["num_graphs"] == len(graphs)
+    for i in range(len(graphs)):
+        assert np.array_equal(r["labels"][i], rg["labels"][i]) and r["modularity"][i] == rg["modularity"][i]
     singles = _singles(ffi, graphs)
     for i, (g, s) in enumerate(zip(graphs, singles)):
         assert np.array_equal(r["labels"][i], s["labels"]), i

@@ -152,6 +152,9 @@ def test_integer_gains_equal_fp64_gains(ffi, golden, torch_cuda, case):
     # level graphs with rows sorted by neighbour id give the same run
     c = ctx.louvain(g, sorted_levels=True)
     assert a["iter_q"] == c["iter_q"] and np.array_equal(a["labels"], c["labels"])
+    # so do sweeps replayed from CUDA graphs
+    d = ctx.louvain(g, use_graphs=True)
+    assert a["iter_q"] == d["iter_q"] and np.array_equal(a["labels"], d["labels"])
 
 
 def test_deterministic_replay(ffi, torch_cuda):
