@@ -26,7 +26,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CU_UNITS = ["phase1.cu", "contract.cu", "engine.cu", "modularity_static.cu", "proposal.cu", "batch.cu"]
 CPP_UNITS = ["graph_host.cpp"]
 CLIS = ["gala_main.cpp", "gala_preprocess.cpp"]
-HEADERS = ["common.cuh", "scan.cuh", "internal.h"]
+HEADERS = ["common.cuh", "scan.cuh", "internal.h", "binlimits.h"]
 
 
 def _nvcc():

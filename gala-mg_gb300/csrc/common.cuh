@@ -4,6 +4,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "binlimits.h"
+
 #define GALA_FULL_MASK 0xffffffffu
 
 namespace gala {
@@ -22,6 +24,19 @@ namespace gala {
 // ---------------------------------------------------------------------------
 constexpr int kNumBins = 8;
 constexpr int kNumBinSlots = 9;
+
+__host__ __device__ inline int bin_of_degree(int64_t d, const BinLimits &l)
+{
+    if (d <= 0) return 8;
+    if (d <= 4) return 0;
+    if (d <= 8) return 1;
+    if (d <= 16) return 2;
+    if (d <= 32) return 3;
+    if (d <= l.m4) return 4;
+    if (d <= l.m5) return 5;
+    if (d <= l.m6) return 6;
+    return 7;
+}
 
 __host__ __device__ inline int bin_of_degree(int64_t d)
 {

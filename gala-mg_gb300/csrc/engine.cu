@@ -612,6 +612,28 @@ gala_status run_levels(gala_context *ctx, int32_t n0, int64_t E0, const int64_t 
                   ctx->n_cap, (long long)ctx->e_cap);
         return GALA_ERR_CAPACITY;
     }
+    // degree-bin tuning
+    {
+        BinLimits lim;
+        if (opt) {
+            if (opt->bin_max[0] > 0) lim.m4 = opt->bin_max[0];
+            if (opt->bin_max[1] > 0) lim.m5 = opt->bin_max[1];
+            if (opt->bin_max[2] > 0) lim.m6 = opt->bin_max[2];
+        }
+        if (lim.m4 < 32 || lim.m4 > kMaxWarpDeg || lim.m5 < lim.m4 || lim.m5 > kMaxCta5Deg || lim.m6 < lim.m5 ||
+            lim.m6 > kMaxCta6Deg) {
+            set_error("bin limits %d / %d / %d outside 32 <= b4 <= 256, b4 <= b5 <= 2048, b5 <= b6 <= 8192", lim.m4,
+                      lim.m5, lim.m6);
+            return GALA_ERR_INVALID;
+        }
+        const int b5 = opt && opt->bin5_block ? opt->bin5_block : 512;
+        if (b5 != 256 && b5 != 512) {
+            set_error("bin5_block must be 256 or 512");
+            return GALA_ERR_INVALID;
+        }
+        ctx->p1.lim = lim;
+        ctx->p1.b5_block = b5;
+    }
     PropRun pr;
     if (opt && opt->proposal_mode != GALA_PROPOSAL_OFF) {
         if (opt->proposal_mode != GALA_PROPOSAL_TRACE && opt->proposal_mode != GALA_PROPOSAL_SKIP) {
@@ -1026,6 +1048,90 @@ gala_status gala_louvain(gala_context *ctx, const gala_graph *g, const gala_opti
     return s;
 }
 
+gala_status gala_autotune(gala_context *ctx, const gala_graph *const *graphs, int32_t count,
+                          const gala_options *opt, int32_t repeats, gala_tuning *out)
+{
+    clear_error();
+    if (!ctx || !graphs || count <= 0 || !out) {
+        set_error("gala_autotune: bad arguments");
+        return GALA_ERR_INVALID;
+    }
+    if (repeats <= 0) repeats = 1;
+    long long n_tot = 0;
+    for (int i = 0; i < count; ++i) {
+        if (!graphs[i]) {
+            set_error("gala_autotune: graph %d is null", i);
+            return GALA_ERR_INVALID;
+        }
+        n_tot += graphs[i]->n;
+    }
+    gala_options base;
+    if (opt)
+        base = *opt;
+    else
+        gala_default_options(&base);
+    base.verbose = 0;
+    std::vector<int32_t> labels((size_t)n_tot);
+    struct Point {
+        int m4, m5, m6, b5;
+        bool operator<(const Point &o) const
+        {
+            return m4 != o.m4 ? m4 < o.m4 : m5 != o.m5 ? m5 < o.m5 : m6 != o.m6 ? m6 < o.m6 : b5 < o.b5;
+        }
+    };
+    std::vector<std::pair<Point, double>> seen;
+    gala_status s = GALA_OK;
+    // device time of one configuration: minimum over the repeats
+    auto time_of = [&](const Point &p) -> double {
+        for (auto &e : seen)
+            if (!(e.first < p) && !(p < e.first)) return e.second;
+        gala_options o = base;
+        o.bin_max[0] = p.m4;
+        o.bin_max[1] = p.m5;
+        o.bin_max[2] = p.m6;
+        o.bin5_block = p.b5;
+        double best = 1e300;
+        for (int r = 0; r < repeats && s == GALA_OK; ++r) {
+            double ms = 0;
+            if (count == 1) {
+                gala_result res{};
+                s = gala_louvain(ctx, graphs[0], &o, labels.data(), &res);
+                ms = res.time_total_ms;
+            } else {
+                gala_batch_result br{};
+                s = gala_louvain_batch(ctx, graphs, count, &o, labels.data(), nullptr, nullptr, &br);
+                ms = br.time_total_ms;
+            }
+            best = std::min(best, ms);
+        }
+        seen.push_back({p, best});
+        return best;
+    };
+    Point cur{kMaxWarpDeg, kMaxCta5Deg, kMaxCta6Deg, 512};
+    const double def_ms = time_of(cur);
+    double cur_ms = def_ms;
+    auto consider = [&](Point p) {
+        const double t = time_of(p);
+        if (s == GALA_OK && t < cur_ms) {
+            cur_ms = t;
+            cur = p;
+        }
+    };
+    for (int m4 : {64, 128, 256}) consider(Point{m4, cur.m5, cur.m6, cur.b5});
+    for (int m5 : {1024, 2048}) consider(Point{cur.m4, m5, cur.m6, cur.b5});
+    for (int m6 : {4096, 8192}) consider(Point{cur.m4, cur.m5, m6, cur.b5});
+    for (int b5 : {256, 512}) consider(Point{cur.m4, cur.m5, cur.m6, b5});
+    if (s) return s;
+    out->bin_max[0] = cur.m4;
+    out->bin_max[1] = cur.m5;
+    out->bin_max[2] = cur.m6;
+    out->bin5_block = cur.b5;
+    out->ms = cur_ms;
+    out->default_ms = def_ms;
+    out->candidates = (int32_t)seen.size();
+    return GALA_OK;
+}
+
 gala_status gala_louvain_batch(gala_context *ctx, const gala_graph *const *graphs, int32_t count,
                                const gala_options *opt, int32_t *community_out, double *modularity_out,
                                int32_t *communities_out, gala_batch_result *res)
@@ -1243,6 +1349,8 @@ gala_status gala_phase1_device(gala_context *ctx, int32_t n, const int64_t *d_of
         return GALA_ERR_CAPACITY;
     }
     LevelGraph g{n, E, d_offsets, d_neighbors, d_weights};
+    ctx->p1.lim = BinLimits();
+    ctx->p1.b5_block = 512;
     long long m2 = 0;
     std::vector<double> trace;
     Phase1Out po;

@@ -8,6 +8,7 @@
 #include <vector>
 
 #include "../../include/gala.h"
+#include "binlimits.h"
 
 // Host graph in the reference layout (src/graph/graph.h:7-19): inclusive
 // offsets without a leading 0; weights optional.
@@ -87,6 +88,8 @@ struct Phase1Buffers {
     int32_t *prop_list;        // proposed vertices (bin segments as in order)
     int features_on;           // 1 = decide kernels write the features above
     int wide;                  // 1 = K, Self, Tot, In and weights are 64-bit fixed point
+    BinLimits lim;             // upper degrees of bins 4-6 (tuning)
+    int b5_block;              // threads per vertex in bin 5: 512 or 256 (tuning)
     // batched graphs (all null for one graph): graph of each vertex, the
     // graph's m2 and 1/m2, stopped graphs, per-graph min Tot
     const int32_t *gid;

@@ -133,7 +133,7 @@ __global__ void k_init_vertices(int n, int32_t *comm, WT *K, WT *Self, WT *Tot, 
 }
 
 __global__ void __launch_bounds__(kCountBlock) k_bin_count(int n, const int64_t *__restrict__ offs,
-                                                           int32_t *blockcnt, int nblk, DevStats *st)
+                                                           int32_t *blockcnt, int nblk, DevStats *st, BinLimits lim)
 {
     __shared__ int cnt[kNumBinSlots];
     if (threadIdx.x < kNumBinSlots) cnt[threadIdx.x] = 0;
@@ -142,7 +142,7 @@ __global__ void __launch_bounds__(kCountBlock) k_bin_count(int n, const int64_t 
     int deg = 0;
     if (v < n) {
         deg = (int)(offs[v + 1] - offs[v]);
-        atomicAdd(&cnt[bin_of_degree(deg)], 1);
+        atomicAdd(&cnt[bin_of_degree(deg, lim)], 1);
     }
 #pragma unroll
     for (int o = 16; o >= 1; o >>= 1) deg = max(deg, __shfl_xor_sync(GALA_FULL_MASK, deg, o));
@@ -153,13 +153,13 @@ __global__ void __launch_bounds__(kCountBlock) k_bin_count(int n, const int64_t 
 
 __global__ void __launch_bounds__(kCountBlock) k_bin_scatter(int n, const int64_t *__restrict__ offs,
                                                              const int32_t *__restrict__ blockoff, int nblk,
-                                                             int32_t *order, DevStats *st)
+                                                             int32_t *order, DevStats *st, BinLimits lim)
 {
     __shared__ int wcnt[kCountBlock / 32][kNumBinSlots];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     int v = blockIdx.x * kCountBlock + threadIdx.x;
     int b = -1;
-    if (v < n) b = bin_of_degree(offs[v + 1] - offs[v]);
+    if (v < n) b = bin_of_degree(offs[v + 1] - offs[v], lim);
     unsigned mine = 0;
 #pragma unroll
     for (int bb = 0; bb < kNumBinSlots; ++bb) {
@@ -353,10 +353,10 @@ void p1_level_init(const LevelGraph &g, Phase1Buffers &b, cudaStream_t st)
                                                          (long long *)b.Tot, b.size, (long long *)b.In);
     else
         k_init_vertices<int><<<grid, 256, 0, st>>>(n, b.comm, b.K, b.Self, b.Tot, b.size, b.In);
-    k_bin_count<<<nblk, kCountBlock, 0, st>>>(n, g.offs, b.blockcnt, nblk, b.stats);
+    k_bin_count<<<nblk, kCountBlock, 0, st>>>(n, g.offs, b.blockcnt, nblk, b.stats, b.lim);
     exclusive_scan(b.blockcnt, b.blockoff, (long long)kNumBinSlots * nblk, OpIdentity(), b.scan_partial,
                    &b.stats->total, st);
-    k_bin_scatter<<<nblk, kCountBlock, 0, st>>>(n, g.offs, b.blockoff, nblk, b.order, b.stats);
+    k_bin_scatter<<<nblk, kCountBlock, 0, st>>>(n, g.offs, b.blockoff, nblk, b.order, b.stats, b.lim);
     note_launch(3);
 }
 
@@ -1202,13 +1202,21 @@ static void decide_t(const LevelGraph &g, Phase1Buffers &b, int bin, const int32
         else
             k_decide_warp<WT, false><<<grid_lanes(32), 256, warp_smem<WT>(), st>>>(a, list, count_ptr);
         break;
-    case 5: {
-        int grid = level_count < num_sms() * 4 ? level_count : num_sms() * 4;
+    case 5: {  // 512 (default) or 256 threads per vertex
         const size_t sm = cta_smem<WT>(kCtaTable5);
-        if (W)
-            k_decide_cta<WT, 512, true><<<grid, 512, sm, st>>>(a, list, count_ptr, kCtaTable5);
-        else
-            k_decide_cta<WT, 512, false><<<grid, 512, sm, st>>>(a, list, count_ptr, kCtaTable5);
+        if (b.b5_block == 256) {
+            int grid = level_count < num_sms() * 8 ? level_count : num_sms() * 8;
+            if (W)
+                k_decide_cta<WT, 256, true><<<grid, 256, sm, st>>>(a, list, count_ptr, kCtaTable5);
+            else
+                k_decide_cta<WT, 256, false><<<grid, 256, sm, st>>>(a, list, count_ptr, kCtaTable5);
+        } else {
+            int grid = level_count < num_sms() * 4 ? level_count : num_sms() * 4;
+            if (W)
+                k_decide_cta<WT, 512, true><<<grid, 512, sm, st>>>(a, list, count_ptr, kCtaTable5);
+            else
+                k_decide_cta<WT, 512, false><<<grid, 512, sm, st>>>(a, list, count_ptr, kCtaTable5);
+        }
         break;
     }
     case 6: {
@@ -1244,6 +1252,10 @@ static void configure_t()
     cudaFuncSetAttribute(k_decide_cta<WT, 1024, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)cta_smem<WT>(kCtaTable6));
     cudaFuncSetAttribute(k_decide_cta<WT, 512, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)cta_smem<WT>(kCtaTable5));
+    cudaFuncSetAttribute(k_decide_cta<WT, 256, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)cta_smem<WT>(kCtaTable5));
+    cudaFuncSetAttribute(k_decide_cta<WT, 256, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)cta_smem<WT>(kCtaTable5));
     cudaFuncSetAttribute(k_decide_cta<WT, 512, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)cta_smem<WT>(kCtaTable5));

@@ -27,7 +27,7 @@ EXPORTS = ["gala_last_error", "gala_status_string", "gala_kernel_launch_count", 
            "gala_proposal_destroy", "gala_proposal_get_params", "gala_proposal_set_params", "gala_proposal_samples",
            "gala_proposal_clear_samples", "gala_proposal_read_samples", "gala_proposal_gradient",
            "gala_proposal_logits", "gala_proposal_train", "gala_louvain_batch", "gala_generate_sbm_batch",
-           "gala_graph_from_csr_f32", "gala_graph_weights_f32", "gala_generate_lfr"]
+           "gala_graph_from_csr_f32", "gala_graph_weights_f32", "gala_generate_lfr", "gala_autotune"]
 
 PROPOSAL_OFF, PROPOSAL_TRACE, PROPOSAL_SKIP = 0, 1, 2
 PROPOSAL_PARAMS = 32 * 8 + 32 + 32 * 32 + 32 + 32 + 1
@@ -49,7 +49,17 @@ class Options(ctypes.Structure):
                 ("verbose", ctypes.c_int32), ("use_graphs", ctypes.c_int32), ("fp64_gains", ctypes.c_int32),
                 ("proposal_mode", ctypes.c_int32), ("proposal_threshold", ctypes.c_float),
                 ("trace_sample_shift", ctypes.c_int32), ("sorted_levels", ctypes.c_int32), ("proposal", ctypes.c_void_p),
-                ("distinct_rows", ctypes.c_int32), ("reserved3", ctypes.c_int32)]
+                ("distinct_rows", ctypes.c_int32), ("bin5_block", ctypes.c_int32),
+                ("bin_max", ctypes.c_int32 * 3), ("reserved3", ctypes.c_int32)]
+
+
+class Tuning(ctypes.Structure):
+    _fields_ = [("bin_max", ctypes.c_int32 * 3), ("bin5_block", ctypes.c_int32), ("ms", ctypes.c_double),
+                ("default_ms", ctypes.c_double), ("candidates", ctypes.c_int32), ("reserved", ctypes.c_int32)]
+
+    def to_dict(self):
+        return {"bin_max": list(self.bin_max), "bin5_block": self.bin5_block, "ms": self.ms,
+                "default_ms": self.default_ms, "candidates": self.candidates}
 
 
 class Result(ctypes.Structure):
@@ -169,6 +179,9 @@ def load(path=LIB_PATH):
                                     ctypes.c_int32, ctypes.c_int32, ctypes.c_double, ctypes.c_int32, ctypes.c_uint64,
                                     ctypes.c_int32, ctypes.POINTER(_vp)]
     L.gala_generate_lfr.restype = ctypes.c_int
+    L.gala_autotune.argtypes = [_vp, ctypes.POINTER(_vp), ctypes.c_int32, ctypes.POINTER(Options), ctypes.c_int32,
+                                ctypes.POINTER(Tuning)]
+    L.gala_autotune.restype = ctypes.c_int
     L.gala_generate_sbm_batch.restype = ctypes.c_int
     for name in ["gala_proposal_create", "gala_proposal_get_params", "gala_proposal_set_params",
                  "gala_proposal_samples", "gala_proposal_clear_samples", "gala_proposal_read_samples",
@@ -351,7 +364,7 @@ class Context:
 
     def louvain(self, graph, min_mod=1e-6, max_levels=0, verbose=False, iter_capacity=4096, fp64_gains=False,
                 proposal=None, mode=PROPOSAL_OFF, threshold=0.5, sample_shift=0, sorted_levels=False,
-                use_graphs=False):
+                use_graphs=False, tuning=None):
         """gala_louvain: host graph in, host labels out.  `proposal` (a
         Proposal) with mode PROPOSAL_TRACE records training samples, with
         PROPOSAL_SKIP decides only the vertices it proposes."""
@@ -366,12 +379,26 @@ class Context:
                             proposal_threshold=float(threshold), trace_sample_shift=int(sample_shift),
                             sorted_levels=int(sorted_levels), use_graphs=int(use_graphs),
                             proposal=proposal.h if proposal is not None else None)
+        if tuning:
+            o.bin_max = (ctypes.c_int32 * 3)(*tuning["bin_max"])
+            o.bin5_block = tuning["bin5_block"]
         _check(load().gala_louvain(self.h, graph.h, ctypes.byref(o), _ptr(labels, _i32p), ctypes.byref(r)))
         d = r.to_dict(trace)
         d["labels"] = labels
         return d
 
-    def louvain_batch(self, graphs, min_mod=1e-6, max_levels=0, use_graphs=False):
+    def autotune(self, graphs, repeats=2, **opts):
+        """gala_autotune over one graph or a batch; returns the tuning dict
+        (pass its bin_max / bin5_block as options)."""
+        if isinstance(graphs, Graph):
+            graphs = [graphs]
+        hs = (_vp * len(graphs))(*[g.h for g in graphs])
+        t = Tuning()
+        o = default_options(**opts)
+        _check(load().gala_autotune(self.h, hs, len(graphs), ctypes.byref(o), repeats, ctypes.byref(t)))
+        return t.to_dict()
+
+    def louvain_batch(self, graphs, min_mod=1e-6, max_levels=0, use_graphs=False, tuning=None):
         """gala_louvain_batch: many host graphs in one union run.  Returns the
         per-graph labels (local community ids), modularity and community
         counts plus the batch timings."""
@@ -383,6 +410,9 @@ class Context:
         hs = (_vp * G)(*[g.h for g in graphs])
         r = BatchResult()
         o = default_options(min_modularity=min_mod, max_levels=max_levels, use_graphs=int(use_graphs))
+        if tuning:
+            o.bin_max = (ctypes.c_int32 * 3)(*tuning["bin_max"])
+            o.bin5_block = tuning["bin5_block"]
         _check(load().gala_louvain_batch(self.h, hs, G, ctypes.byref(o), _ptr(labels, _i32p), _ptr(q, _f64p),
                                          _ptr(c, _i32p), ctypes.byref(r)))
         starts = np.concatenate([[0], np.cumsum(sizes)])

@@ -81,8 +81,26 @@ typedef struct {
                                    neighbour twice (lets the first sweep of
                                    level 0 skip aggregation; graphs built by
                                    this library are known to be distinct) */
+    int32_t bin5_block;         /* threads per vertex of degree bin 5: 512
+                                   (default, 0) or 256 */
+    int32_t bin_max[3];         /* upper degrees of bins 4, 5, 6 (0 = default
+                                   256 / 2048 / 8192; each at most its default,
+                                   non-decreasing, bin 4 at least 32); larger
+                                   rows go to the next bin, above bin 6 to the
+                                   multi-CTA hub path.  Any values give the same
+                                   partition; gala_autotune picks fast ones. */
     int32_t reserved3;
 } gala_options;
+
+/* Tuning of the degree bins (the fields of gala_options they set). */
+typedef struct {
+    int32_t bin_max[3];
+    int32_t bin5_block;
+    double ms;                  /* device time of one run with this tuning */
+    double default_ms;          /* device time of one run with the defaults */
+    int32_t candidates;         /* configurations timed */
+    int32_t reserved;
+} gala_tuning;
 
 typedef struct {
     double modularity;                 /* final Q */
@@ -264,6 +282,16 @@ typedef struct {
     int64_t h2d_bytes;
     int64_t d2h_bytes;
 } gala_batch_result;
+/* Autotuner of the degree bins (no counterpart in the reference): times full
+ * runs (gala_louvain for one graph, gala_louvain_batch for count > 1) with
+ * candidate bin limits and bin-5 block sizes - a coordinate search over the
+ * bin-4 upper degree {64, 128, 256}, bin 5 {1024, 2048}, bin 6 {4096, 8192}
+ * and the bin-5 block {256, 512}, each point the minimum of `repeats` runs -
+ * and returns the fastest (every candidate gives the same partition).  The
+ * other fields of opt apply to every run. */
+gala_status gala_autotune(gala_context *ctx, const gala_graph *const *graphs, int32_t count,
+                          const gala_options *opt, int32_t repeats, gala_tuning *out);
+
 gala_status gala_louvain_batch(gala_context *ctx, const gala_graph *const *graphs, int32_t count,
                                const gala_options *opt, int32_t *community_out,
                                double *modularity_out, int32_t *communities_out,

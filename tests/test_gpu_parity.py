@@ -329,3 +329,23 @@ def test_gala_main_cli_prints_reference_format(ffi, golden, torch_cuda, tmp_path
     assert lines[-1].startswith("elapsed time = ")
     labels = np.fromfile(out_labels, dtype=np.int32)
     assert labels.shape == (34,) and len(np.unique(labels)) == 4
+
+
+def test_bin_limits_and_autotune_keep_the_partition(ffi, torch_cuda):
+    """Degree-bin limits move rows between schedules (warp, CTA, multi-CTA hub
+    path) without changing any decision; the autotuner returns limits inside
+    the allowed ranges."""
+    rng = np.random.default_rng(23)
+    offs, nbr, w = _sym_graph(rng, 20000, 160000, True, hubs=[(5, 9000), (6, 5000), (7, 3000)])
+    g = ffi.Graph.from_csr(offs, nbr, w)
+    ctx = ffi.Context(offs.shape[0] - 1, offs[-1])
+    base = ctx.louvain(g)
+    for t in ({"bin_max": [64, 1024, 4096], "bin5_block": 256}, {"bin_max": [32, 256, 2048], "bin5_block": 512},
+              {"bin_max": [128, 2048, 8192], "bin5_block": 256}):
+        r = ctx.louvain(g, tuning=t)
+        assert r["iter_q"] == base["iter_q"] and np.array_equal(r["labels"], base["labels"]), t
+    tun = ctx.autotune(g, repeats=1)
+    m4, m5, m6 = tun["bin_max"]
+    assert 32 <= m4 <= m5 <= m6 <= 8192 and tun["bin5_block"] in (256, 512)
+    assert tun["ms"] <= tun["default_ms"] and tun["candidates"] >= 4
+    ctx.close()
