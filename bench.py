@@ -39,6 +39,19 @@ METRIC = "end-to-end Louvain edges/s (all rounds to dQ<1e-6)"
 FALLBACK_HBM_GBS = 6800.0
 
 
+def max_over_ranks(dist, torch, value, device):
+    """The slowest rank's value (every rank gets it)."""
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_throughput(world, units_per_replica, ms):
+    """Whole-job throughput of `world` independent replicas that each process
+    `units_per_replica` in `ms` (the slowest rank's time)."""
+    return world * units_per_replica / (ms / 1000.0)
+
+
 def parse():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
@@ -394,11 +407,9 @@ def main():
     clk = clocks.stop()
     ms = ev0.elapsed_time(ev1) / args.steps
     if dist:
-        t = torch.tensor([ms], device=f"cuda:{local}")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+        ms = max_over_ranks(dist, torch, ms, f"cuda:{local}")
         dist.barrier()
-    value = world * m / (ms / 1000.0)
+    value = replica_throughput(world, m, ms)
 
     # ---- end to end through the C ABI with host buffers ----
     r_e2e = None
@@ -416,9 +427,7 @@ def main():
             e2e_ms.append(a.elapsed_time(b))
     e2e_step = sum(e2e_ms) / len(e2e_ms)
     if dist:
-        t = torch.tensor([e2e_step], device=f"cuda:{local}")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_step = float(t.item())
+        e2e_step = max_over_ranks(dist, torch, e2e_step, f"cuda:{local}")
 
     peak, peak_kind = measured_peak()
     achieved = (dec_bytes / (dec_ms / 1000.0)) / 1e9 if dec_ms > 0 else 0.0
