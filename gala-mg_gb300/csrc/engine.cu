@@ -590,6 +590,40 @@ struct RunOut {
     std::vector<double> trace;
 };
 
+// Checkpoint of the level graph reached after `round` rounds: the graph in
+// the .bin layout (inclusive offsets, int32 weights) and the community of
+// every input vertex in it.
+gala_status write_level(gala_context *ctx, const LevelGraph &g, int32_t n0, const char *dir, int round)
+{
+    cudaStream_t st = ctx->stream;
+    std::vector<int64_t> offs((size_t)g.n + 1);
+    std::vector<int32_t> nbr((size_t)g.E), w((size_t)g.E), lab((size_t)n0);
+    gala_status s;
+    cudaMemcpyAsync(offs.data(), g.offs, offs.size() * sizeof(int64_t), cudaMemcpyDeviceToHost, st);
+    if (g.E) {
+        cudaMemcpyAsync(nbr.data(), g.nbr, nbr.size() * sizeof(int32_t), cudaMemcpyDeviceToHost, st);
+        cudaMemcpyAsync(w.data(), g.w, w.size() * sizeof(int32_t), cudaMemcpyDeviceToHost, st);
+    }
+    cudaMemcpyAsync(lab.data(), ctx->orig, lab.size() * sizeof(int32_t), cudaMemcpyDeviceToHost, st);
+    if ((s = check(cudaStreamSynchronize(st), "level checkpoint"))) return s;
+    char path[4096];
+    snprintf(path, sizeof(path), "%s/level_%d.bin", dir, round);
+    gala_graph *h = nullptr;
+    if ((s = gala_graph_from_csr(g.n, offs.data() + 1, nbr.data(), w.data(), &h))) return s;
+    s = gala_graph_store_bin(h, path);
+    gala_graph_destroy(h);
+    if (s) return s;
+    snprintf(path, sizeof(path), "%s/labels_%d.bin", dir, round);
+    FILE *f = fopen(path, "wb");
+    const bool ok = f && fwrite(lab.data(), sizeof(int32_t), lab.size(), f) == lab.size();
+    if (f) fclose(f);
+    if (!ok) {
+        set_error("cannot write %s", path);
+        return GALA_ERR_IO;
+    }
+    return GALA_OK;
+}
+
 // Multi-round loop of louvain.cu:193-226 on a device graph.  Level 0 reads
 // the caller's arrays; later levels live in the context's ping-pong buffers.
 // ctx->orig receives the final community of every level-0 vertex.
@@ -661,6 +695,11 @@ gala_status run_levels(gala_context *ctx, int32_t n0, int64_t E0, const int64_t 
     cudaMemsetAsync(&ctx->d_stats->fp64_decisions, 0, sizeof(unsigned long long), st);
     note_launch(1);
 
+    const char *level_dir = opt ? opt->level_dir : nullptr;
+    if (level_dir && (wide || bt)) {
+        set_error("level checkpoints are not available for batches or float-weight graphs");
+        return GALA_ERR_INVALID;
+    }
     if (wide && pr.mode != GALA_PROPOSAL_OFF) {
         set_error("proposal modes are not available for float-weight graphs");
         return GALA_ERR_INVALID;
@@ -720,6 +759,7 @@ gala_status run_levels(gala_context *ctx, int32_t n0, int64_t E0, const int64_t 
         cur_mod = po.q;
         g = LevelGraph{C, newE, ctx->offs[buf], ctx->nbr[buf], ctx->w[buf], wide, true};
         buf ^= 1;
+        if (level_dir && (s = write_level(ctx, g, n0, level_dir, round))) return s;
         if (bt) {
             const int G = bt->G;
             if ((s = check(cudaMemcpyAsync(bt->h_ncomm, bt->ncomm, G * sizeof(int32_t), cudaMemcpyDeviceToHost, st),

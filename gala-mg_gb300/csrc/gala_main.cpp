@@ -4,7 +4,8 @@
 // prints the reference's per-round / per-iteration lines (README.md:59-89).
 // Extra options: -o <file> writes the final community of every vertex (one
 // int32 per vertex, binary), -t <threshold> (default 1e-6), -l <max rounds>,
-// -d <device>.
+// -d <device>, -s <dir> writes every round's contracted graph and labels
+// (checkpoints to resume from).
 #include <stdio.h>
 #include <stdlib.h>
 #include <sys/time.h>
@@ -27,7 +28,7 @@ int main(int argc, char **argv)
     int weighted = 0, device = 0, opt;
     gala_options o;
     gala_default_options(&o);
-    while ((opt = getopt(argc, argv, "f:wo:t:l:d:")) != -1) {
+    while ((opt = getopt(argc, argv, "f:wo:t:l:d:s:")) != -1) {
         switch (opt) {
         case 'f': file = optarg; break;
         case 'w': weighted = 1; break;
@@ -35,8 +36,11 @@ int main(int argc, char **argv)
         case 't': o.min_modularity = atof(optarg); break;
         case 'l': o.max_levels = atoi(optarg); break;
         case 'd': device = atoi(optarg); break;
+        case 's': o.level_dir = optarg; break;
         default:
-            fprintf(stderr, "Usage: %s -f <graph.bin> [-w] [-o labels.bin] [-t threshold] [-l rounds] [-d device]\n",
+            fprintf(stderr,
+                    "Usage: %s -f <graph.bin> [-w] [-o labels.bin] [-t threshold] [-l rounds] [-d device] "
+                    "[-s level_dir]\n",
                     argv[0]);
             return 1;
         }

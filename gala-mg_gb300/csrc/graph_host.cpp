@@ -357,11 +357,14 @@ gala_status gala_graph_load_bin(const char *path, int32_t weighted, gala_graph *
         return GALA_ERR_INVALID;
     }
     const long long need = 4LL + 8LL * n + 4LL * E * (weighted ? 2 : 1);
-    if (E < 0 || E % 2 != 0 || need > fsize) {
+    // (an odd entry count is legal - a contracted graph has one self-loop
+    // entry per community - but the reference's writer drops the last entry
+    // of such a graph, graph.cpp:75,166, which the size check catches)
+    if (E < 0 || need > fsize) {
         fclose(f);
         delete g;
         set_error("%s: %lld CSR entries need %lld bytes, file has %lld%s", path, (long long)E, need, fsize,
-                  (E % 2) ? " (odd entry count: the writer dropped the last entry)" : "");
+                  (E % 2) ? " (odd entry count: a writer that drops the last entry made this file)" : "");
         return GALA_ERR_FORMAT;
     }
     g->nbr.resize(E);

@@ -50,7 +50,7 @@ class Options(ctypes.Structure):
                 ("proposal_mode", ctypes.c_int32), ("proposal_threshold", ctypes.c_float),
                 ("trace_sample_shift", ctypes.c_int32), ("sorted_levels", ctypes.c_int32), ("proposal", ctypes.c_void_p),
                 ("distinct_rows", ctypes.c_int32), ("bin5_block", ctypes.c_int32),
-                ("bin_max", ctypes.c_int32 * 3), ("reserved3", ctypes.c_int32)]
+                ("bin_max", ctypes.c_int32 * 3), ("reserved3", ctypes.c_int32), ("level_dir", ctypes.c_char_p)]
 
 
 class Tuning(ctypes.Structure):
@@ -364,7 +364,7 @@ class Context:
 
     def louvain(self, graph, min_mod=1e-6, max_levels=0, verbose=False, iter_capacity=4096, fp64_gains=False,
                 proposal=None, mode=PROPOSAL_OFF, threshold=0.5, sample_shift=0, sorted_levels=False,
-                use_graphs=False, tuning=None):
+                use_graphs=False, tuning=None, level_dir=None):
         """gala_louvain: host graph in, host labels out.  `proposal` (a
         Proposal) with mode PROPOSAL_TRACE records training samples, with
         PROPOSAL_SKIP decides only the vertices it proposes."""
@@ -382,6 +382,8 @@ class Context:
         if tuning:
             o.bin_max = (ctypes.c_int32 * 3)(*tuning["bin_max"])
             o.bin5_block = tuning["bin5_block"]
+        if level_dir:
+            o.level_dir = level_dir.encode()
         _check(load().gala_louvain(self.h, graph.h, ctypes.byref(o), _ptr(labels, _i32p), ctypes.byref(r)))
         d = r.to_dict(trace)
         d["labels"] = labels

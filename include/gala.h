@@ -90,6 +90,15 @@ typedef struct {
                                    multi-CTA hub path.  Any values give the same
                                    partition; gala_autotune picks fast ones. */
     int32_t reserved3;
+    /* Checkpoints (no counterpart in the reference, which never writes its
+       partition, louvain.cu:226): when set, after every round r the
+       contracted graph is written to <level_dir>/level_<r+1>.bin (the .bin
+       layout with int32 weights) and the community of every input vertex in
+       that graph to <level_dir>/labels_<r+1>.bin (int32 per input vertex).
+       A run resumes from round r+1 on level_<r+1>.bin (weighted); its labels
+       composed with labels_<r+1> are the full run's.  Not for batches or
+       float-weight graphs. */
+    const char *level_dir;
 } gala_options;
 
 /* Tuning of the degree bins (the fields of gala_options they set). */

@@ -349,3 +349,22 @@ def test_bin_limits_and_autotune_keep_the_partition(ffi, torch_cuda):
     assert 32 <= m4 <= m5 <= m6 <= 8192 and tun["bin5_block"] in (256, 512)
     assert tun["ms"] <= tun["default_ms"] and tun["candidates"] >= 4
     ctx.close()
+
+
+def test_level_checkpoints_resume(ffi, torch_cuda, tmp_path):
+    """gala_options.level_dir: every round's contracted graph and the input
+    vertices' labels in it; a run resumed from level 1 continues exactly."""
+    g = ffi.Graph.rmat(14, 120000, seed=6)
+    n, e, _ = g.info()
+    ctx = ffi.Context(n, e)
+    full = ctx.louvain(g, level_dir=str(tmp_path))
+    assert full["rounds"] >= 3
+    lab1 = np.fromfile(str(tmp_path / "labels_1.bin"), dtype=np.int32)
+    g1 = ffi.Graph.load_bin(str(tmp_path / "level_1.bin"), weighted=True)
+    n1, _, _ = g1.info()
+    assert n1 == full["level_c"][0] and lab1.shape[0] == n and lab1.max() == n1 - 1
+    res = ctx.louvain(g1)
+    assert np.array_equal(res["labels"][lab1], full["labels"])
+    assert res["modularity"] == full["modularity"]
+    assert res["level_q"] == full["level_q"][1:]
+    ctx.close()
