@@ -161,6 +161,18 @@ def cpu_oracle_run(offs, nbr, nthreads):
     return time.perf_counter() - t, r
 
 
+def cpu_model():
+    """Host CPU model name (lscpu), for the CPU baseline record."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.strip().startswith("Model name"):
+                return line.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    return "unknown"
+
+
 def reference_arm(args, wl):
     """The reference's path on the host cores: the oracle port (the
     reference's GPU algorithm restated on the CPU, all host threads)."""
@@ -186,6 +198,7 @@ def reference_arm(args, wl):
             "scaling": "weak", "vs_baseline": None, "dtype": "int32/f64", "data": "synthetic", "config": cfg,
             "modularity": r["modularity"], "communities": r["level_c"][-1], "rounds": r["rounds"],
             "cpu_baseline": {"value": val, "unit": "edges/s", "cores": threads, "kind": "port",
+                             "cpu_model": cpu_model(),
                              "sample": "full run on the whole workload (all rounds), oracle/louvain_oracle.c"},
             "e2e": {"value": val, "unit": "edges/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -467,6 +480,7 @@ def main():
         threads = os.cpu_count() or 1
         dt, ro = cpu_oracle_run(offs, nbr, threads)
         line["cpu_baseline"] = {"value": m / dt, "unit": "edges/s", "cores": threads, "kind": "port",
+                                "cpu_model": cpu_model(),
                                 "sample": "one full run (all rounds) of the oracle on the whole workload",
                                 "seconds": dt, "modularity": ro["modularity"],
                                 "labels_equal_gpu": bool((ro["labels"] == r_e2e["labels"]).all())}
