@@ -51,6 +51,8 @@ static int sm_count()
 constexpr int kSmallMax = 32;
 constexpr int kMid1Max = 512;
 constexpr int kMid2Max = 4096;
+constexpr int kMid3Max = 8192;  // rows in hash-table order only (a 16384-slot table)
+constexpr int kLongCls = 4;     // class of the rows aggregated in global tables
 constexpr int kChunk = 4096;
 constexpr int kSortMax = 16384;
 constexpr int kRangeEntries = 1024;  // CSR entries per warp task
@@ -257,23 +259,28 @@ __global__ void __launch_bounds__(256) k_stream_fill(int n, long long E, const i
     }
 }
 
-__device__ __forceinline__ int row_class(long long E)
+__device__ __forceinline__ int row_class(long long E, int sort_rows)
 {
-    return E == 0 ? -1 : (E <= kSmallMax ? 0 : (E <= kMid1Max ? 1 : (E <= kMid2Max ? 2 : 3)));
+    if (E == 0) return -1;
+    if (E <= kSmallMax) return 0;
+    if (E <= kMid1Max) return 1;
+    if (E <= kMid2Max) return 2;
+    if (E <= kMid3Max && !sort_rows) return 3;
+    return kLongCls;
 }
 
 // Size classes with warp-aggregated appends (one atomic per warp and class);
 // communities without entries get an empty row right away.
 __global__ void __launch_bounds__(256) k_classify(int C, const long long *__restrict__ ec, int32_t *lists,
-                                                  int32_t *kc, DevStats *st)
+                                                  int32_t *kc, DevStats *st, int sort_rows)
 {
     const int stride = gridDim.x * blockDim.x;
     for (int base = blockIdx.x * blockDim.x; base < C; base += stride) {
         const int c = base + threadIdx.x;
-        const int cls = c < C ? row_class(ec[c]) : -2;
+        const int cls = c < C ? row_class(ec[c], sort_rows) : -2;
         if (cls == -1) kc[c] = 0;
 #pragma unroll
-        for (int k = 0; k < 4; ++k) warp_append(cls == k, c, lists + (long long)k * C, &st->small_cnt[k]);
+        for (int k = 0; k <= kLongCls; ++k) warp_append(cls == k, c, lists + (long long)k * C, &st->small_cnt[k]);
     }
 }
 
@@ -606,7 +613,7 @@ struct BigArgs {
 template <typename WT>
 __global__ void k_big_plan(AggArgs<WT> a, BigArgs b)
 {
-    const int cnt = a.st->small_cnt[3];
+    const int cnt = a.st->small_cnt[kLongCls];
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < cnt; i += gridDim.x * blockDim.x) {
         const long long E = a.ec[b.list[i]];
         const long long cap = E < a.C ? E : a.C;
@@ -625,7 +632,7 @@ __global__ void k_big_plan(AggArgs<WT> a, BigArgs b)
 __global__ void k_big_tail(BigArgs b, const DevStats *st)
 {
     // toff[cnt] / coff[cnt] / tcoff[cnt] close the last segments
-    const int cnt = st->small_cnt[3];
+    const int cnt = st->small_cnt[kLongCls];
     ((long long *)b.toff)[cnt] = st->total;
     ((long long *)b.coff)[cnt] = st->total2;
     ((long long *)b.tcoff)[cnt] = st->total3;
@@ -639,7 +646,7 @@ __global__ void k_big_work(AggArgs<WT> a, BigArgs b)
     const int lane = threadIdx.x & 31;
     const int wg = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int nw = (gridDim.x * blockDim.x) >> 5;
-    const int cnt = a.st->small_cnt[3];
+    const int cnt = a.st->small_cnt[kLongCls];
     for (int i = wg; i < cnt; i += nw) {
         long long o = b.coff[i], k = b.coff[i + 1] - o;
         for (long long j = lane; j < k; j += 32) b.work[o + j] = i;
@@ -691,7 +698,7 @@ __global__ void __launch_bounds__(256) k_big_insert(AggArgs<WT> a, BigArgs b, lo
 template <typename WT>
 __global__ void k_big_mark(AggArgs<WT> a, BigArgs b, int sort_rows)
 {
-    const int cnt = a.st->small_cnt[3];
+    const int cnt = a.st->small_cnt[kLongCls];
     const long long words = ((long long)a.C + 31) >> 5;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < cnt; i += gridDim.x * blockDim.x) {
         const int k = b.kdist[i];
@@ -782,7 +789,7 @@ __global__ void __launch_bounds__(1024) k_big_sort(AggArgs<WT> a, BigArgs b)
     extern __shared__ long long sm_ll[];
     int *lk = (int *)sm_ll;
     WT *lv = (WT *)(lk + kSortMax);
-    const int cnt = a.st->small_cnt[3];
+    const int cnt = a.st->small_cnt[kLongCls];
     for (int i = blockIdx.x; i < cnt; i += gridDim.x) {
         if (b.gwords[i] != 0) continue;
         const int c = b.list[i];
@@ -846,7 +853,7 @@ __global__ void k_set_last_offset(int64_t *offs, int C, const long long *total) 
 
 __global__ void k_contract_reset(DevStats *st)
 {
-    st->small_cnt[0] = st->small_cnt[1] = st->small_cnt[2] = st->small_cnt[3] = 0;
+    for (int k = 0; k <= kLongCls; ++k) st->small_cnt[k] = 0;
     st->err = 0;
 }
 
@@ -890,6 +897,8 @@ static void configure_t()
     cudaFuncSetAttribute(k_big_sort<WT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sort_smem<WT>());
     cudaFuncSetAttribute(k_agg_mid_list<WT, 256, 8192>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)list_smem<WT>(8192));
+    cudaFuncSetAttribute(k_agg_mid_list<WT, 1024, 16384>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)list_smem<WT>(16384));
 }
 
 void contract_configure_kernels()
@@ -927,7 +936,8 @@ static bool read_stats(DevStats *h, DevStats *d, cudaStream_t st, gala_status *s
     return true;
 }
 
-// Rows longer than kMid2Max entries (class 3).  Returns false on failure.
+// Rows longer than kMid3Max entries (kMid2Max when sorted; class kLongCls).
+// Returns false on failure.
 template <typename WT>
 static bool contract_long_rows(const AggArgs<WT> &a, ContractBuffers &b, int cnt3, int C, DevStats &hs,
                                cudaStream_t st, gala_status *status, bool sort_rows)
@@ -935,7 +945,7 @@ static bool contract_long_rows(const AggArgs<WT> &a, ContractBuffers &b, int cnt
     const int nsm = sm_count();
     const int cap = nsm * 8;
     BigArgs ba{};
-    ba.list = b.cls_list + 3LL * C;
+    ba.list = b.cls_list + (long long)kLongCls * C;
     ba.T = b.big_T;
     ba.chunks = b.big_chunks;
     ba.tchunks = b.big_tchunks;
@@ -1055,7 +1065,7 @@ static int contract_t(const LevelGraph &g, const int32_t *comm, ContractBuffers 
                                                                b.mpos, b.medge, b.stream_key, sw, b.nz_rows,
                                                                b.nz_offs, b.stats);
     }
-    k_classify<<<grid_cap(C, 256, cap), 256, 0, st>>>(C, b.ec, b.cls_list, b.kc, b.stats);
+    k_classify<<<grid_cap(C, 256, cap), 256, 0, st>>>(C, b.ec, b.cls_list, b.kc, b.stats, sort_rows ? 1 : 0);
     exclusive_scan(b.ec, b.tmp_off, C, OpCap{C}, b.scan_partial, &b.stats->total, st);
     note_launch(6 + (orig_map ? 1 : 0));
     if (!read_stats(&hs, b.stats, st, status, "contraction: classification")) return -1;
@@ -1093,7 +1103,14 @@ static int contract_t(const LevelGraph &g, const int32_t *comm, ContractBuffers 
             k_agg_mid_list<WT, 256, 8192><<<grid, 256, list_smem<WT>(8192), st>>>(a, b.cls_list + 2LL * C, 2);
         note_launch(1);
     }
-    if (hs.small_cnt[3] > 0 && !contract_long_rows(a, b, hs.small_cnt[3], C, hs, st, status, sort_rows)) return -1;
+    if (hs.small_cnt[3] > 0) {  // 4097-8192 entries, rows in table order
+        int grid = hs.small_cnt[3] < nsm ? hs.small_cnt[3] : nsm;
+        k_agg_mid_list<WT, 1024, 16384><<<grid, 1024, list_smem<WT>(16384), st>>>(a, b.cls_list + 3LL * C, 3);
+        note_launch(1);
+    }
+    if (hs.small_cnt[kLongCls] > 0 &&
+        !contract_long_rows(a, b, hs.small_cnt[kLongCls], C, hs, st, status, sort_rows))
+        return -1;
     exclusive_scan(b.kc, new_offs, C, OpIdentity(), b.scan_partial, &b.stats->total, st);
     k_set_last_offset<<<1, 1, 0, st>>>(new_offs, C, &b.stats->total);
     note_launch(1);

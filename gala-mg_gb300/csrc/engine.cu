@@ -936,7 +936,7 @@ gala_status gala_context_create(int32_t device, int32_t max_vertices, int64_t ma
          dalloc(ctx, &c.members, n) && dalloc(ctx, &c.mpos, n) && dalloc(ctx, &c.ec, n + 1) &&
          dalloc(ctx, &c.medge, n + 1) && dalloc(ctx, &c.stream_key, E) && dalloc8(ctx, &c.stream_w, E) &&
          dalloc(ctx, &c.tmp_off, n + 1) && dalloc(ctx, &c.tmp_nbr, E) && dalloc8(ctx, &c.tmp_w, E) &&
-         dalloc(ctx, &c.kc, n + 1) && dalloc(ctx, &c.cls_list, 4 * n);
+         dalloc(ctx, &c.kc, n + 1) && dalloc(ctx, &c.cls_list, 5 * n);
     // tables of the rows longer than 4096 entries: at most 4 slots per entry
     // (keys + values), chunk list of at most E / 4096 + n entries
     c.big_pool_ints = 8LL * (long long)E + 64;
