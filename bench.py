@@ -387,7 +387,8 @@ def main():
                           "iterations": r["total_iterations"], "modularity": r["modularity"],
                           "decide_ms": r["time_decide_ms"], "update_ms": r["time_update_ms"],
                           "contract_ms": r["time_contract_ms"], "decide_bytes": r["decide_bytes"],
-                          "sweeps": r["decide_sweeps"], "fp64_decisions": r["fp64_decisions"]}), flush=True)
+                          "sweeps": r["decide_sweeps"], "fp64_decisions": r["fp64_decisions"],
+                          "levels": r["levels"]}), flush=True)
         ctx.close()
         return
 

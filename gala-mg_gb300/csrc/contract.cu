@@ -195,13 +195,22 @@ __global__ void k_hist(const int32_t *__restrict__ comm, int n, int32_t *cnt)
         atomicAdd(&cnt[comm[v]], 1);
 }
 
+// New label of every vertex and member count of every new community; with
+// tot/k_out, K_new of community c is its total Tot[c] (the weight of the new
+// row equals the weighted degrees of its members, exactly).
+template <typename WT>
 __global__ void k_relabel(const int32_t *__restrict__ comm, const int32_t *__restrict__ newid,
-                          const int32_t *__restrict__ cnt, int n, int32_t *lab, int32_t *csz)
+                          const int32_t *__restrict__ cnt, int n, int32_t *lab, int32_t *csz,
+                          const WT *__restrict__ tot, WT *k_out)
 {
     for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) {
         lab[v] = newid[comm[v]];
         int k = cnt[v];
-        if (k > 0) csz[newid[v]] = k;
+        if (k > 0) {
+            const int c = newid[v];
+            csz[c] = k;
+            if (k_out) k_out[c] = tot[v];
+        }
     }
 }
 
@@ -818,7 +827,8 @@ __global__ void __launch_bounds__(256) k_compact(int C, long long Enew, const in
                                                  const int32_t *__restrict__ tmp_nbr, const WT *__restrict__ tmp_w,
                                                  int32_t *out_nbr, WT *out_w, long long tmp_cap,
                                                  const int32_t *__restrict__ nz_rows,
-                                                 const long long *__restrict__ nz_offs, DevStats *st)
+                                                 const long long *__restrict__ nz_offs, DevStats *st,
+                                                 WT *self_out)
 {
     const long long wg = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
     const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
@@ -837,8 +847,11 @@ __global__ void __launch_bounds__(256) k_compact(int C, long long Enew, const in
                 atomicOr(&st->err, kErrBadIndex);
                 return;
             }
-            out_nbr[j] = tmp_nbr[src];
-            out_w[j] = tmp_w[src];
+            const int32_t u = tmp_nbr[src];
+            const WT wt = tmp_w[src];
+            out_nbr[j] = u;
+            out_w[j] = wt;
+            if (self_out && u == c) self_out[c] = wt;
         });
     }
 }
@@ -1017,7 +1030,8 @@ static bool contract_long_rows(const AggArgs<WT> &a, ContractBuffers &b, int cnt
 template <typename WT>
 static int contract_t(const LevelGraph &g, const int32_t *comm, ContractBuffers &b, int64_t *new_offs,
                       int32_t *new_nbr, WT *new_w, int32_t *orig_map, int32_t n_orig, int64_t *new_E,
-                      cudaStream_t st, gala_status *status, bool validate_labels, bool sort_rows)
+                      cudaStream_t st, gala_status *status, bool validate_labels, bool sort_rows,
+                      const NextLevelInit &nli)
 {
     const int n = g.n;
     const int cap = sm_count() * 8;
@@ -1043,7 +1057,9 @@ static int contract_t(const LevelGraph &g, const int32_t *comm, ContractBuffers 
     if (!read_stats(&hs, b.stats, st, status, "contraction: community count")) return -1;
     const int C = (int)hs.total;
 
-    k_relabel<<<grid_cap(n, 256, cap), 256, 0, st>>>(comm, b.newid, b.cnt, n, b.lab, b.csz);
+    k_relabel<WT><<<grid_cap(n, 256, cap), 256, 0, st>>>(comm, b.newid, b.cnt, n, b.lab, b.csz,
+                                                         (const WT *)nli.tot, (WT *)nli.k);
+    if (nli.self) cudaMemsetAsync(nli.self, 0, (size_t)C * sizeof(WT), st);
     if (orig_map) k_compose<<<grid_cap(n_orig, 256, cap), 256, 0, st>>>(orig_map, n_orig, b.lab);
     exclusive_scan(b.csz, b.moff, C, OpIdentity(), b.scan_partial, &b.stats->total, st);
     cudaMemcpyAsync(b.cursor, b.moff, (size_t)C * sizeof(int32_t), cudaMemcpyDeviceToDevice, st);
@@ -1120,7 +1136,7 @@ static int contract_t(const LevelGraph &g, const int32_t *comm, ContractBuffers 
         build_walk_list(new_offs, C, Enew, b, st);
         k_compact<WT><<<grid_cap((Enew + kRangeEntries - 1) / kRangeEntries * 32, 256, cap), 256, 0, st>>>(
             C, Enew, new_offs, b.tmp_off, b.tmp_nbr, (const WT *)b.tmp_w, new_nbr, new_w, g.E, b.nz_rows, b.nz_offs,
-            b.stats);
+            b.stats, (WT *)nli.self);
         note_launch(1);
     }
     if (!read_stats(&hs, b.stats, st, status, "contraction: compaction")) return -1;
@@ -1135,13 +1151,19 @@ static int contract_t(const LevelGraph &g, const int32_t *comm, ContractBuffers 
 
 int contract_run(const LevelGraph &g, const int32_t *comm, ContractBuffers &b, int64_t *new_offs,
                  int32_t *new_nbr, void *new_w, int32_t *orig_map, int32_t n_orig, int64_t *new_E,
-                 cudaStream_t st, gala_status *status, bool validate_labels, bool sort_rows)
+                 cudaStream_t st, gala_status *status, bool validate_labels, bool sort_rows,
+                 const NextLevelInit &nli)
 {
+    if ((nli.k != nullptr) != (nli.tot != nullptr)) {
+        set_error("contraction: K_new needs the community totals");
+        *status = GALA_ERR_INVALID;
+        return -1;
+    }
     if (g.wide)
         return contract_t<long long>(g, comm, b, new_offs, new_nbr, (long long *)new_w, orig_map, n_orig, new_E, st,
-                                     status, validate_labels, sort_rows);
+                                     status, validate_labels, sort_rows, nli);
     return contract_t<int>(g, comm, b, new_offs, new_nbr, (int *)new_w, orig_map, n_orig, new_E, st, status,
-                           validate_labels, sort_rows);
+                           validate_labels, sort_rows, nli);
 }
 
 }  // namespace gala

@@ -159,6 +159,8 @@ struct Phase1Out {
     long long decisions = 0;      // vertices decided (active, or proposed)
     long long skipped = 0;        // active vertices the network let stay
     long long verify_sweeps = 0;  // full plain sweeps run to judge convergence
+    long long movers = 0;         // moves applied (kept or dropped)
+    long long active_entries = 0; // row entries decided
 };
 
 // Move-proposal settings of one run (mode GALA_PROPOSAL_OFF / TRACE / SKIP).
@@ -242,10 +244,12 @@ gala_status phase1(gala_context *ctx, const LevelGraph &g, long long &m2, double
     int bin_start[kNumBinSlots + 1];
     memcpy(bin_start, h->bin_start, sizeof(bin_start));
     const int max_deg = h->max_deg;
-    p1_level_init_rows(g, b, bin_start, st);
-    if ((s = check(cudaMemcpyAsync(h, b.stats, sizeof(DevStats), cudaMemcpyDeviceToHost, st), "level rows")) ||
-        (s = check(cudaStreamSynchronize(st), "level rows")))
-        return s;
+    if (!g.ks_ready) {
+        p1_level_init_rows(g, b, bin_start, st);
+        if ((s = check(cudaMemcpyAsync(h, b.stats, sizeof(DevStats), cudaMemcpyDeviceToHost, st), "level rows")) ||
+            (s = check(cudaStreamSynchronize(st), "level rows")))
+            return s;
+    }
     if (m2 == 0) {  // first level: total weight m2 = sum of K (louvain.cu:165-167)
         m2 = (long long)h->sum_k;
         if (m2 <= 0) {
@@ -480,6 +484,8 @@ gala_status phase1(gala_context *ctx, const LevelGraph &g, long long &m2, double
         skipped0 = h->skipped;
         skipped_e0 = h->skipped_edges;
         out->decisions += dec_nv;
+        out->movers += h->n_movers;
+        out->active_entries += dec_ne;
         out->decide_ms += ev_ms(ctx->ev[2], ctx->ev[3]);
         out->update_ms += ev_ms(ctx->ev[4], ctx->ev[5]);
         out->decide_bytes += decide_bytes_for(dec_nv, dec_ne, weighted);
@@ -740,7 +746,8 @@ gala_status run_levels(gala_context *ctx, int32_t n0, int64_t E0, const int64_t 
         int64_t newE = 0;
         gala_status cs = GALA_OK;
         C = contract_run(g, ctx->p1.comm, ctx->cb, ctx->offs[buf], ctx->nbr[buf], ctx->w[buf], ctx->orig, n0, &newE,
-                         st, &cs, false, opt && opt->sorted_levels == 1);
+                         st, &cs, false, opt && opt->sorted_levels == 1,
+                         NextLevelInit{ctx->p1.Tot, ctx->p1.K, ctx->p1.Self});
         if (C < 0) return cs;
         cudaEventRecord(ctx->ev[1], st);
         if ((s = check(cudaStreamSynchronize(st), "contraction"))) return s;
@@ -752,12 +759,20 @@ gala_status run_levels(gala_context *ctx, int32_t n0, int64_t E0, const int64_t 
             res->level_modularity[round] = po.q;
             res->level_communities[round] = C;
             res->level_iterations[round] = po.iterations;
+            res->level_vertices[round] = g.n;
+            res->level_entries[round] = g.E;
+            res->level_phase1_ms[round] = po.total_ms;
+            res->level_decide_ms[round] = po.decide_ms;
+            res->level_update_ms[round] = po.update_ms;
+            res->level_contract_ms[round] = cms;
+            res->level_movers[round] = po.movers;
+            res->level_active_entries[round] = po.active_entries;
         }
         res->total_iterations += po.iterations;
         round++;
         prev_mod = cur_mod;
         cur_mod = po.q;
-        g = LevelGraph{C, newE, ctx->offs[buf], ctx->nbr[buf], ctx->w[buf], wide, true};
+        g = LevelGraph{C, newE, ctx->offs[buf], ctx->nbr[buf], ctx->w[buf], wide, true, true};
         buf ^= 1;
         if (level_dir && (s = write_level(ctx, g, n0, level_dir, round))) return s;
         if (bt) {

@@ -67,6 +67,7 @@ struct LevelGraph {
     const void *w;        // nullptr = unweighted; int32, or int64 fixed point when wide
     bool wide = false;
     bool distinct = false;  // rows list each neighbour at most once (contracted levels always)
+    bool ks_ready = false;  // K and Self of every vertex are already in the phase-1 buffers
 };
 
 // Phase-1 workspace (all device pointers, sized for the context capacity).
@@ -220,9 +221,18 @@ struct ContractBuffers {
 // every new row in hash-table order: phase 1 does not depend on the order of
 // a row's entries (all weight sums are exact integers), and the sorts are
 // skipped.  gala_contract_device sorts, as the oracle does.
+// Optional by-products for the next level's phase 1 (all null: none): the
+// weighted degree of every new vertex (K_new[c'] = Tot[c], the community
+// total of the level contracted) and its self-loop weight (the weight of the
+// row entry c' -> c'), so that the next level needs no row scan for them.
+struct NextLevelInit {
+    const void *tot = nullptr;  // Tot of the contracted level (WT per vertex)
+    void *k = nullptr;          // receives K_new (WT per new vertex)
+    void *self = nullptr;       // receives Self_new (WT per new vertex)
+};
 int contract_run(const LevelGraph &g, const int32_t *comm, ContractBuffers &b, int64_t *new_offs,
                  int32_t *new_nbr, void *new_w, int32_t *orig_map, int32_t n_orig,
                  int64_t *new_E, cudaStream_t st, gala_status *status, bool validate_labels = false,
-                 bool sort_rows = true);
+                 bool sort_rows = true, const NextLevelInit &nli = NextLevelInit());
 
 }  // namespace gala

@@ -132,6 +132,31 @@ __global__ void k_init_vertices(int n, int32_t *comm, WT *K, WT *Self, WT *Tot, 
     }
 }
 
+// Level init of a contracted level whose K and Self the contraction wrote:
+// labels and sizes as above, Tot = K, In = Self, and the sums sum(K),
+// sum(K^2), sum(Self) of the singleton partition without a row scan.
+template <typename WT>
+__global__ void __launch_bounds__(256) k_init_vertices_ks(int n, int32_t *comm, const WT *__restrict__ K,
+                                                          const WT *__restrict__ Self, WT *Tot, int32_t *size,
+                                                          WT *In, DevStats *st)
+{
+    unsigned long long sk = 0, ss = 0;
+    typename SqSum<WT>::T sk2 = 0;
+    for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) {
+        const WT k = K[v], sf = Self[v];
+        comm[v] = v;
+        size[v] = 1;
+        Tot[v] = k;
+        In[v] = sf;
+        sk += (unsigned long long)k;
+        sk2 += SqSum<WT>::sq(k);
+        ss += (unsigned long long)sf;
+    }
+    block_add_u64(sk, &st->sum_k);
+    SqSum<WT>::add(sk2, st);
+    block_add_u64(ss, &st->sum_in);
+}
+
 __global__ void __launch_bounds__(kCountBlock) k_bin_count(int n, const int64_t *__restrict__ offs,
                                                            int32_t *blockcnt, int nblk, DevStats *st, BinLimits lim)
 {
@@ -348,7 +373,13 @@ void p1_level_init(const LevelGraph &g, Phase1Buffers &b, cudaStream_t st)
     const int n = g.n;
     const int nblk = (n + kCountBlock - 1) / kCountBlock;
     const int grid = (n + 255) / 256 < 4096 ? (n + 255) / 256 : 4096;
-    if (g.wide)
+    if (g.ks_ready && g.wide)
+        k_init_vertices_ks<long long><<<grid, 256, 0, st>>>(n, b.comm, (const long long *)b.K,
+                                                            (const long long *)b.Self, (long long *)b.Tot, b.size,
+                                                            (long long *)b.In, b.stats);
+    else if (g.ks_ready)
+        k_init_vertices_ks<int><<<grid, 256, 0, st>>>(n, b.comm, b.K, b.Self, b.Tot, b.size, b.In, b.stats);
+    else if (g.wide)
         k_init_vertices<long long><<<grid, 256, 0, st>>>(n, b.comm, (long long *)b.K, (long long *)b.Self,
                                                          (long long *)b.Tot, b.size, (long long *)b.In);
     else
@@ -362,6 +393,7 @@ void p1_level_init(const LevelGraph &g, Phase1Buffers &b, cudaStream_t st)
 
 void p1_level_init_rows(const LevelGraph &g, Phase1Buffers &b, const int *bin_start, cudaStream_t st)
 {
+    if (g.ks_ready) return;  // K, Self, Tot, In and the sums came with the level init
     for (int bin = 0; bin < kNumBins; ++bin) {
         if (g.wide)
             launch_init_rows<long long>(g, b, bin, b.order + bin_start[bin], bin_start[bin + 1] - bin_start[bin], st);
@@ -1281,18 +1313,36 @@ __global__ void k_apply_movers(const int32_t *__restrict__ mv_v, const int32_t *
                                int32_t *comm, WT *Tot, int32_t *size, const WT *__restrict__ K,
                                int32_t *last_move, int iteration)
 {
+    // whole warps step together: movers of one warp that share a source or a
+    // target community add to its Tot and size once (many movers of a sweep
+    // head for the same large community)
     const int nm = stp->n_movers;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nm; i += gridDim.x * blockDim.x) {
-        const int v = mv_v[i];
-        const int from = sign > 0 ? mv_old[i] : mv_new[i];
-        const int to = sign > 0 ? mv_new[i] : mv_old[i];
-        const WT k = K[v];
-        comm[v] = to;
-        if (last_move && sign > 0) last_move[v] = iteration;
-        atomic_add_w(&Tot[to], k);
-        atomic_add_w(&Tot[from], (WT)-k);
-        atomicAdd(&size[to], 1);
-        atomicSub(&size[from], 1);
+    const int lane = threadIdx.x & 31;
+    for (int i0 = blockIdx.x * blockDim.x + threadIdx.x - lane; i0 < nm; i0 += gridDim.x * blockDim.x) {
+        const int i = i0 + lane;
+        const bool valid = i < nm;
+        int from = -1, to = -1;
+        WT k = 0;
+        if (valid) {
+            const int v = mv_v[i];
+            from = sign > 0 ? mv_old[i] : mv_new[i];
+            to = sign > 0 ? mv_new[i] : mv_old[i];
+            k = K[v];
+            comm[v] = to;
+            if (last_move && sign > 0) last_move[v] = iteration;
+        }
+        const unsigned mt = __match_any_sync(GALA_FULL_MASK, to);
+        const WT kt = group_sum(mt, k);
+        if (valid && lane == __ffs(mt) - 1) {
+            atomic_add_w(&Tot[to], kt);
+            atomicAdd(&size[to], __popc(mt));
+        }
+        const unsigned mf = __match_any_sync(GALA_FULL_MASK, from);
+        const WT kf = group_sum(mf, k);
+        if (valid && lane == __ffs(mf) - 1) {
+            atomic_add_w(&Tot[from], (WT)-kf);
+            atomicSub(&size[from], __popc(mf));
+        }
     }
 }
 

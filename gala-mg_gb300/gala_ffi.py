@@ -78,7 +78,15 @@ class Result(ctypes.Structure):
                 ("kernel_launches", ctypes.c_int64), ("h2d_bytes", ctypes.c_int64),
                 ("d2h_bytes", ctypes.c_int64), ("fp64_decisions", ctypes.c_int64),
                 ("decisions", ctypes.c_int64), ("skipped", ctypes.c_int64), ("verify_sweeps", ctypes.c_int32),
-                ("reserved2", ctypes.c_int32), ("samples", ctypes.c_int64)]
+                ("reserved2", ctypes.c_int32), ("samples", ctypes.c_int64),
+                ("level_vertices", ctypes.c_int32 * GALA_MAX_LEVELS),
+                ("level_entries", ctypes.c_int64 * GALA_MAX_LEVELS),
+                ("level_phase1_ms", ctypes.c_double * GALA_MAX_LEVELS),
+                ("level_decide_ms", ctypes.c_double * GALA_MAX_LEVELS),
+                ("level_update_ms", ctypes.c_double * GALA_MAX_LEVELS),
+                ("level_contract_ms", ctypes.c_double * GALA_MAX_LEVELS),
+                ("level_movers", ctypes.c_int64 * GALA_MAX_LEVELS),
+                ("level_active_entries", ctypes.c_int64 * GALA_MAX_LEVELS)]
 
     def to_dict(self, trace=None):
         L = self.num_levels
@@ -93,7 +101,12 @@ class Result(ctypes.Structure):
              "decide_bytes": self.decide_bytes, "update_bytes": self.update_bytes,
              "kernel_launches": self.kernel_launches, "h2d_bytes": self.h2d_bytes, "d2h_bytes": self.d2h_bytes,
              "fp64_decisions": self.fp64_decisions, "decisions": self.decisions, "skipped": self.skipped,
-             "verify_sweeps": self.verify_sweeps, "samples": self.samples}
+             "verify_sweeps": self.verify_sweeps, "samples": self.samples,
+             "levels": [{"vertices": self.level_vertices[i], "entries": self.level_entries[i],
+                         "phase1_ms": self.level_phase1_ms[i], "decide_ms": self.level_decide_ms[i],
+                         "update_ms": self.level_update_ms[i], "contract_ms": self.level_contract_ms[i],
+                         "movers": self.level_movers[i], "active_entries": self.level_active_entries[i]}
+                        for i in range(min(L, GALA_MAX_LEVELS))]}
         if trace is not None:
             d["iter_q"] = trace[:min(self.iter_count, len(trace))].tolist()
         return d

@@ -149,6 +149,15 @@ typedef struct {
                                    gained less than min_modularity (SKIP) */
     int32_t reserved2;
     int64_t samples;            /* training samples recorded (TRACE) */
+    /* per round: the level graph it ran on, its times and its moves */
+    int32_t level_vertices[GALA_MAX_LEVELS];
+    int64_t level_entries[GALA_MAX_LEVELS];      /* CSR entries (2x edges) */
+    double level_phase1_ms[GALA_MAX_LEVELS];
+    double level_decide_ms[GALA_MAX_LEVELS];
+    double level_update_ms[GALA_MAX_LEVELS];
+    double level_contract_ms[GALA_MAX_LEVELS];
+    int64_t level_movers[GALA_MAX_LEVELS];       /* moves applied, all sweeps */
+    int64_t level_active_entries[GALA_MAX_LEVELS]; /* row entries decided, all sweeps */
 } gala_result;
 
 /* ---- errors / info --------------------------------------------------- */
