@@ -236,6 +236,42 @@ __device__ __forceinline__ void warp_append(bool flag, int value, int *list, int
     if (flag) list[base + __popc(b & lanemask_lt())] = value;
 }
 
+// Per-warp staging of list appends: a warp gathers its items in a
+// shared-memory buffer of N slots and hands them out with one counter atomic
+// per full buffer (appends of a whole grid to one counter otherwise queue on
+// that counter).  All 32 lanes call push and flush; flush is needed at the end.
+template <int N, int K>
+struct WarpStage {
+    int *buf;  // K * N ints of shared memory, this warp's
+    int n;     // items held (warp-uniform)
+    __device__ __forceinline__ void flush(int *const *lists, int *counter)
+    {
+        __syncwarp();
+        if (n == 0) return;
+        const int lane = threadIdx.x & 31;
+        int base = 0;
+        if (lane == 0) base = atomicAdd(counter, n);
+        base = __shfl_sync(GALA_FULL_MASK, base, 0);
+#pragma unroll
+        for (int k = 0; k < K; ++k)
+            for (int i = lane; i < n; i += 32) lists[k][base + i] = buf[k * N + i];
+        __syncwarp();
+        n = 0;
+    }
+    __device__ __forceinline__ void push(bool flag, const int (&vals)[K], int *const *lists, int *counter)
+    {
+        const unsigned b = __ballot_sync(GALA_FULL_MASK, flag);
+        if (b == 0) return;
+        if (n + 32 > N) flush(lists, counter);
+        if (flag) {
+            const int p = n + __popc(b & lanemask_lt());
+#pragma unroll
+            for (int k = 0; k < K; ++k) buf[k * N + p] = vals[k];
+        }
+        n += __popc(b);
+    }
+};
+
 template <typename T>
 __device__ __forceinline__ T warp_sum(T v)
 {

@@ -10,7 +10,9 @@
 //   4. per community, sum the weights per neighbour community, by row length:
 //        <= 32 entries      one warp, __match_any_sync + __reduce_add_sync
 //        <= 512 entries     one 128-thread CTA, shared-memory hash table
-//        <= 4096 entries    one 256-thread CTA, shared-memory hash table
+//        <= 4096 entries    one CTA (1024 threads; 256 when rows are sorted),
+//                           shared-memory hash table
+//        <= 8192 entries    one 1024-thread CTA (rows in table order only)
 //        larger             a global table per community filled by many CTAs
 //                           (4096-entry chunks of the stream); a dense table
 //                           indexed by community id when a hash table would not
@@ -908,7 +910,7 @@ static void configure_t()
     configure_mid<WT>();
 
     cudaFuncSetAttribute(k_big_sort<WT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sort_smem<WT>());
-    cudaFuncSetAttribute(k_agg_mid_list<WT, 256, 8192>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    cudaFuncSetAttribute(k_agg_mid_list<WT, 1024, 8192>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)list_smem<WT>(8192));
     cudaFuncSetAttribute(k_agg_mid_list<WT, 1024, 16384>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)list_smem<WT>(16384));
@@ -941,7 +943,8 @@ static void build_walk_list(const int64_t *offs, int n, long long E, ContractBuf
 static bool read_stats(DevStats *h, DevStats *d, cudaStream_t st, gala_status *status, const char *what)
 {
     cudaError_t ce;
-    if ((ce = cudaMemcpyAsync(h, d, sizeof(DevStats), cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
+    if ((ce = cudaGetLastError()) != cudaSuccess ||  // a failed launch
+        (ce = cudaMemcpyAsync(h, d, sizeof(DevStats), cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
         (ce = cudaStreamSynchronize(st)) != cudaSuccess) {
         *status = cuda_fail(ce, what);
         return false;
@@ -1116,7 +1119,7 @@ static int contract_t(const LevelGraph &g, const int32_t *comm, ContractBuffers 
         if (sort_rows)
             k_agg_mid<WT, 256, 8192, kMid2Max><<<grid, 256, mid2_smem<WT>(), st>>>(a, b.cls_list + 2LL * C, 2);
         else
-            k_agg_mid_list<WT, 256, 8192><<<grid, 256, list_smem<WT>(8192), st>>>(a, b.cls_list + 2LL * C, 2);
+            k_agg_mid_list<WT, 1024, 8192><<<grid, 1024, list_smem<WT>(8192), st>>>(a, b.cls_list + 2LL * C, 2);
         note_launch(1);
     }
     if (hs.small_cnt[3] > 0) {  // 4097-8192 entries, rows in table order

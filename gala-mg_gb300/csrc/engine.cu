@@ -127,6 +127,16 @@ gala_status check(cudaError_t e, const char *what)
     return cuda_fail(e, what);
 }
 
+// Waits for the stream; a kernel launch that failed since the last check (an
+// invalid configuration or missing resources, which the synchronize alone
+// would not report) fails the call too.
+gala_status sync_check(cudaStream_t st, const char *what)
+{
+    const cudaError_t le = cudaGetLastError();
+    if (le != cudaSuccess) return cuda_fail(le, what);
+    return check(cudaStreamSynchronize(st), what);
+}
+
 float ev_ms(cudaEvent_t a, cudaEvent_t b)
 {
     float ms = 0.f;
@@ -239,7 +249,7 @@ gala_status phase1(gala_context *ctx, const LevelGraph &g, long long &m2, double
     p1_reset_level_stats(b, st);
     p1_level_init(g, b, st);
     if ((s = check(cudaMemcpyAsync(h, b.stats, sizeof(DevStats), cudaMemcpyDeviceToHost, st), "level init")) ||
-        (s = check(cudaStreamSynchronize(st), "level init")))
+        (s = sync_check(st, "level init")))
         return s;
     int bin_start[kNumBinSlots + 1];
     memcpy(bin_start, h->bin_start, sizeof(bin_start));
@@ -247,7 +257,7 @@ gala_status phase1(gala_context *ctx, const LevelGraph &g, long long &m2, double
     if (!g.ks_ready) {
         p1_level_init_rows(g, b, bin_start, st);
         if ((s = check(cudaMemcpyAsync(h, b.stats, sizeof(DevStats), cudaMemcpyDeviceToHost, st), "level rows")) ||
-            (s = check(cudaStreamSynchronize(st), "level rows")))
+            (s = sync_check(st, "level rows")))
             return s;
     }
     if (m2 == 0) {  // first level: total weight m2 = sum of K (louvain.cu:165-167)
@@ -298,7 +308,7 @@ gala_status phase1(gala_context *ctx, const LevelGraph &g, long long &m2, double
         hp.pfc = ctx->hub_pfc;
         p1_hub_plan_launch(g, b, hp, st);
         if ((s = check(cudaMemcpyAsync(h, b.stats, sizeof(DevStats), cudaMemcpyDeviceToHost, st), "hub plan")) ||
-            (s = check(cudaStreamSynchronize(st), "hub plan")))
+            (s = sync_check(st, "hub plan")))
             return s;
         hp.half = h->total;
         hp.nwork = h->total2;
@@ -323,7 +333,7 @@ gala_status phase1(gala_context *ctx, const LevelGraph &g, long long &m2, double
         cudaMemcpyAsync(bt->h_sum_in, bt->sum_in, G * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st);
         cudaMemcpyAsync(bt->h_sum_tot2, bt->sum_tot2, G * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st);
         cudaMemcpyAsync(bt->h_sum_k, bt->sum_k, G * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st);
-        if ((s = check(cudaStreamSynchronize(st), "batch level sums"))) return s;
+        if ((s = sync_check(st, "batch level sums"))) return s;
         const bool first = bt->m2.empty();
         if (first) {
             bt->m2.resize(G);
@@ -334,7 +344,7 @@ gala_status phase1(gala_context *ctx, const LevelGraph &g, long long &m2, double
             }
             cudaMemcpyAsync(bt->m2g, bt->m2.data(), G * sizeof(long long), cudaMemcpyHostToDevice, st);
             cudaMemcpyAsync(bt->cg, c.data(), G * sizeof(double), cudaMemcpyHostToDevice, st);
-            if ((s = check(cudaStreamSynchronize(st), "batch m2"))) return s;
+            if ((s = sync_check(st, "batch m2"))) return s;
         }
         bt->prev_q.assign(G, 0.0);
         for (int i = 0; i < G; ++i) {
@@ -469,7 +479,7 @@ gala_status phase1(gala_context *ctx, const LevelGraph &g, long long &m2, double
         } else {
             enqueue(false);
         }
-        if ((s = check(cudaStreamSynchronize(st), "iteration"))) return s;
+        if ((s = sync_check(st, "iteration"))) return s;
         if (h->err) {
             set_error("phase 1: device error bits %d", h->err);
             return GALA_ERR_OVERFLOW;
@@ -517,7 +527,7 @@ gala_status phase1(gala_context *ctx, const LevelGraph &g, long long &m2, double
                 cudaMemcpyAsync(bt->stop, bt->h_stop, G, cudaMemcpyHostToDevice, st);
                 batch_revert(b, bt->gid, bt->reject, g.n, st);
                 // the host arrays must stay unchanged until the copies ran
-                if ((s = check(cudaStreamSynchronize(st), "batch revert"))) return s;
+                if ((s = sync_check(st, "batch revert"))) return s;
             }
             if (!running) break;
             cur = nxt;
@@ -557,7 +567,7 @@ gala_status phase1(gala_context *ctx, const LevelGraph &g, long long &m2, double
             }
             join(ctx);
             if ((s = check(cudaMemcpyAsync(h, b.stats, sizeof(DevStats), cudaMemcpyDeviceToHost, st), "restore")) ||
-                (s = check(cudaStreamSynchronize(st), "restore")))
+                (s = sync_check(st, "restore")))
                 return s;
             act_nv = h->act_vertices[nxt];
             act_ne = (long long)h->act_edges[nxt];
@@ -571,7 +581,7 @@ gala_status phase1(gala_context *ctx, const LevelGraph &g, long long &m2, double
         iteration++;
     }
     cudaEventRecord(ctx->ev[1], st);
-    if ((s = check(cudaStreamSynchronize(st), "phase 1 end"))) return s;
+    if ((s = sync_check(st, "phase 1 end"))) return s;
     out->total_ms = ev_ms(ctx->ev[0], ctx->ev[1]);
     out->q = prev_q;
     out->iterations = iteration;
@@ -611,7 +621,7 @@ gala_status write_level(gala_context *ctx, const LevelGraph &g, int32_t n0, cons
         cudaMemcpyAsync(w.data(), g.w, w.size() * sizeof(int32_t), cudaMemcpyDeviceToHost, st);
     }
     cudaMemcpyAsync(lab.data(), ctx->orig, lab.size() * sizeof(int32_t), cudaMemcpyDeviceToHost, st);
-    if ((s = check(cudaStreamSynchronize(st), "level checkpoint"))) return s;
+    if ((s = sync_check(st, "level checkpoint"))) return s;
     char path[4096];
     snprintf(path, sizeof(path), "%s/level_%d.bin", dir, round);
     gala_graph *h = nullptr;
@@ -666,7 +676,7 @@ gala_status run_levels(gala_context *ctx, int32_t n0, int64_t E0, const int64_t 
                       lim.m5, lim.m6);
             return GALA_ERR_INVALID;
         }
-        const int b5 = opt && opt->bin5_block ? opt->bin5_block : 512;
+        const int b5 = opt && opt->bin5_block ? opt->bin5_block : 256;
         if (b5 != 256 && b5 != 512) {
             set_error("bin5_block must be 256 or 512");
             return GALA_ERR_INVALID;
@@ -750,7 +760,7 @@ gala_status run_levels(gala_context *ctx, int32_t n0, int64_t E0, const int64_t 
                          NextLevelInit{ctx->p1.Tot, ctx->p1.K, ctx->p1.Self});
         if (C < 0) return cs;
         cudaEventRecord(ctx->ev[1], st);
-        if ((s = check(cudaStreamSynchronize(st), "contraction"))) return s;
+        if ((s = sync_check(st, "contraction"))) return s;
         float cms = ev_ms(ctx->ev[0], ctx->ev[1]);
         contract_ms += cms;
         if (verbose && round == 0) printf("build time in the first round = %fms\n", cms);
@@ -779,7 +789,7 @@ gala_status run_levels(gala_context *ctx, int32_t n0, int64_t E0, const int64_t 
             const int G = bt->G;
             if ((s = check(cudaMemcpyAsync(bt->h_ncomm, bt->ncomm, G * sizeof(int32_t), cudaMemcpyDeviceToHost, st),
                            "batch communities")) ||
-                (s = check(cudaStreamSynchronize(st), "batch communities")))
+                (s = sync_check(st, "batch communities")))
                 return s;
             bt->h_goff[0] = 0;
             bool running = false;
@@ -801,7 +811,7 @@ gala_status run_levels(gala_context *ctx, int32_t n0, int64_t E0, const int64_t 
             batch_gid_fill(G, bt->goff, bt->gid2, st);
             std::swap(bt->gid, bt->gid2);
             ctx->p1.gid = bt->gid;
-            if ((s = check(cudaStreamSynchronize(st), "batch ranges"))) return s;
+            if ((s = sync_check(st, "batch ranges"))) return s;
             if (!running) break;
             if (max_levels > 0 && round >= max_levels) break;
             if (round >= GALA_MAX_LEVELS) break;
@@ -813,7 +823,7 @@ gala_status run_levels(gala_context *ctx, int32_t n0, int64_t E0, const int64_t 
         if (round >= GALA_MAX_LEVELS) break;
     }
     cudaEventRecord(t1, st);
-    if ((s = check(cudaStreamSynchronize(st), "run end"))) return s;
+    if ((s = sync_check(st, "run end"))) return s;
     double total_ms = ev_ms(t0, t1);
     if (verbose) {
         printf("=====================================\n");
@@ -839,7 +849,7 @@ gala_status run_levels(gala_context *ctx, int32_t n0, int64_t E0, const int64_t 
     if (pr.mode == GALA_PROPOSAL_TRACE) {
         long long cnt = 0;
         if ((s = check(cudaMemcpyAsync(&cnt, pr.pv.count, sizeof(cnt), cudaMemcpyDeviceToHost, st), "samples")) ||
-            (s = check(cudaStreamSynchronize(st), "samples")))
+            (s = sync_check(st, "samples")))
             return s;
         res->samples = std::min<long long>(cnt, pr.pv.cap);
     }
@@ -851,7 +861,7 @@ gala_status run_levels(gala_context *ctx, int32_t n0, int64_t E0, const int64_t 
     unsigned long long nfp = 0;
     if ((s = check(cudaMemcpyAsync(&nfp, &ctx->d_stats->fp64_decisions, sizeof(nfp), cudaMemcpyDeviceToHost, st),
                    "fp64 count")) ||
-        (s = check(cudaStreamSynchronize(st), "fp64 count")))
+        (s = sync_check(st, "fp64 count")))
         return s;
     res->fp64_decisions = (int64_t)nfp;
     return GALA_OK;
@@ -1004,7 +1014,7 @@ gala_status gala_context_set_stream(gala_context *ctx, void *stream)
         return GALA_ERR_INVALID;
     }
     cudaSetDevice(ctx->device);
-    gala_status s = check(cudaStreamSynchronize(ctx->stream), "gala_context_set_stream");
+    gala_status s = sync_check(ctx->stream, "gala_context_set_stream");
     if (s) return s;
     ctx->stream = stream ? (cudaStream_t)stream : ctx->own_stream;
     return GALA_OK;
@@ -1026,14 +1036,14 @@ gala_status gala_louvain_device(gala_context *ctx, int32_t n, const int64_t *d_o
     gala_status s;
     if ((s = check(cudaMemcpyAsync(&E, d_offsets + n, sizeof(int64_t), cudaMemcpyDeviceToHost, ctx->stream),
                    "read entry count")) ||
-        (s = check(cudaStreamSynchronize(ctx->stream), "read entry count")))
+        (s = sync_check(ctx->stream, "read entry count")))
         return s;
     long long l0 = gala_kernel_launch_count();
     if ((s = run_levels(ctx, n, E, d_offsets, d_neighbors, d_weights, opt, res))) return s;
     if ((s = check(cudaMemcpyAsync(d_community_out, ctx->orig, (size_t)n * sizeof(int32_t),
                                    cudaMemcpyDeviceToDevice, ctx->stream),
                    "labels")) ||
-        (s = check(cudaStreamSynchronize(ctx->stream), "labels")))
+        (s = sync_check(ctx->stream, "labels")))
         return s;
     res->kernel_launches = gala_kernel_launch_count() - l0;
     return GALA_OK;
@@ -1081,7 +1091,7 @@ gala_status gala_louvain(gala_context *ctx, const gala_graph *g, const gala_opti
         dw = ctx->w[1];
     }
     cudaEventRecord(ctx->ev[7], st);
-    if ((s = check(cudaStreamSynchronize(st), "host to device copy"))) {
+    if ((s = sync_check(st, "host to device copy"))) {
         if (own) gala_context_destroy(own);
         return s;
     }
@@ -1092,7 +1102,7 @@ gala_status gala_louvain(gala_context *ctx, const gala_graph *g, const gala_opti
         cudaEventRecord(ctx->ev[6], st);
         cudaMemcpyAsync(community_out, ctx->orig, (size_t)n * sizeof(int32_t), cudaMemcpyDeviceToHost, st);
         cudaEventRecord(ctx->ev[7], st);
-        s = check(cudaStreamSynchronize(st), "device to host copy");
+        s = sync_check(st, "device to host copy");
         res->time_d2h_ms = ev_ms(ctx->ev[6], ctx->ev[7]);
     }
     res->time_h2d_ms = h2d;
@@ -1162,7 +1172,7 @@ gala_status gala_autotune(gala_context *ctx, const gala_graph *const *graphs, in
         seen.push_back({p, best});
         return best;
     };
-    Point cur{kMaxWarpDeg, kMaxCta5Deg, kMaxCta6Deg, 512};
+    Point cur{kMaxWarpDeg, kMaxCta5Deg, kMaxCta6Deg, 256};
     const double def_ms = time_of(cur);
     double cur_ms = def_ms;
     auto consider = [&](Point p) {
@@ -1339,7 +1349,7 @@ gala_status gala_louvain_batch(gala_context *ctx, const gala_graph *const *graph
     cudaMemcpyAsync(bt.goff, bt.h_goff, ((size_t)G + 1) * sizeof(int64_t), cudaMemcpyHostToDevice, st);
     cudaEventRecord(ctx->ev[7], st);
     batch_gid_fill(G, bt.goff, bt.gid, st);
-    if ((s = check(cudaStreamSynchronize(st), "batch host to device copy"))) return s;
+    if ((s = sync_check(st, "batch host to device copy"))) return s;
     res->time_h2d_ms = ev_ms(ctx->ev[6], ctx->ev[7]);
     Phase1Buffers &b = ctx->p1;
     b.gid = bt.gid;
@@ -1360,7 +1370,7 @@ gala_status gala_louvain_batch(gala_context *ctx, const gala_graph *const *graph
     cudaEventRecord(ctx->ev[6], st);
     cudaMemcpyAsync(community_out, ctx->orig, (size_t)n * sizeof(int32_t), cudaMemcpyDeviceToHost, st);
     cudaEventRecord(ctx->ev[7], st);
-    if ((s = check(cudaStreamSynchronize(st), "batch device to host copy"))) return s;
+    if ((s = sync_check(st, "batch device to host copy"))) return s;
     res->time_d2h_ms = ev_ms(ctx->ev[6], ctx->ev[7]);
     // union community ids -> ids local to each graph
     for (int i = 0; i < G; ++i) {
@@ -1397,7 +1407,7 @@ gala_status gala_phase1_device(gala_context *ctx, int32_t n, const int64_t *d_of
     int64_t E = 0;
     gala_status s;
     if ((s = check(cudaMemcpyAsync(&E, d_offsets + n, sizeof(int64_t), cudaMemcpyDeviceToHost, st), "entries")) ||
-        (s = check(cudaStreamSynchronize(st), "entries")))
+        (s = sync_check(st, "entries")))
         return s;
     if (n > ctx->n_cap || E > ctx->e_cap) {
         set_error("graph exceeds context capacity");
@@ -1405,7 +1415,7 @@ gala_status gala_phase1_device(gala_context *ctx, int32_t n, const int64_t *d_of
     }
     LevelGraph g{n, E, d_offsets, d_neighbors, d_weights};
     ctx->p1.lim = BinLimits();
-    ctx->p1.b5_block = 512;
+    ctx->p1.b5_block = 256;
     long long m2 = 0;
     std::vector<double> trace;
     Phase1Out po;
@@ -1413,7 +1423,7 @@ gala_status gala_phase1_device(gala_context *ctx, int32_t n, const int64_t *d_of
     if ((s = check(cudaMemcpyAsync(d_community_out, ctx->p1.comm, (size_t)n * sizeof(int32_t),
                                    cudaMemcpyDeviceToDevice, st),
                    "labels")) ||
-        (s = check(cudaStreamSynchronize(st), "labels")))
+        (s = sync_check(st, "labels")))
         return s;
     if (modularity) *modularity = po.q;
     if (iterations) *iterations = po.iterations;
@@ -1438,7 +1448,7 @@ gala_status gala_contract_device(gala_context *ctx, int32_t n, const int64_t *d_
     int64_t E = 0;
     gala_status s;
     if ((s = check(cudaMemcpyAsync(&E, d_offsets + n, sizeof(int64_t), cudaMemcpyDeviceToHost, st), "entries")) ||
-        (s = check(cudaStreamSynchronize(st), "entries")))
+        (s = sync_check(st, "entries")))
         return s;
     if (n > ctx->n_cap || E > ctx->e_cap) {
         set_error("graph exceeds context capacity");
@@ -1455,7 +1465,7 @@ gala_status gala_contract_device(gala_context *ctx, int32_t n, const int64_t *d_
     if ((s = check(cudaMemcpyAsync(d_community, ctx->cb.lab, (size_t)n * sizeof(int32_t), cudaMemcpyDeviceToDevice,
                                    st),
                    "relabel")) ||
-        (s = check(cudaStreamSynchronize(st), "relabel")))
+        (s = sync_check(st, "relabel")))
         return s;
     if (num_communities) *num_communities = C;
     if (num_entries) *num_entries = newE;

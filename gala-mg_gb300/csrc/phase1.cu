@@ -565,6 +565,8 @@ __device__ __forceinline__ void append_mover(const DecideArgs<WT> &a, bool move,
 // community are found with __match_any_sync (the key carries the group index
 // so groups of one warp stay apart) and their weights summed with
 // __reduce_add_sync; the lowest lane of each set evaluates the gain.
+constexpr int kStageN = 256;  // staged active-list appends per warp
+constexpr int kStageM = 128;  // staged movers per warp
 template <typename WT, int G, bool W>
 __global__ void __launch_bounds__(256) k_decide_group(DecideArgs<WT> a, const int32_t *__restrict__ list,
                                                       const int *__restrict__ count_ptr)
@@ -574,6 +576,9 @@ __global__ void __launch_bounds__(256) k_decide_group(DecideArgs<WT> a, const in
     const int count = *count_ptr;
     const int wg = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int nw = (gridDim.x * blockDim.x) >> 5;
+    __shared__ int stage_buf[8][3 * kStageM];
+    WarpStage<kStageM, 3> stage{stage_buf[threadIdx.x >> 5], 0};
+    int *const mlists[3] = {a.mv_v, a.mv_old, a.mv_new};
     for (int base = wg * GPW; base < count; base += nw * GPW) {
         const int idx = base + gw;
         bool has = idx < count;
@@ -656,8 +661,10 @@ __global__ void __launch_bounds__(256) k_decide_group(DecideArgs<WT> a, const in
             const unsigned gmask = G == 32 ? GALA_FULL_MASK : (((1u << G) - 1u) << (gw * G));
             if (has && sub == 0) write_features(a, sc, v, x, wc, sf, ki, __popc(lb & gmask));
         }
-        append_mover(a, move, v, cur, bc);
+        const int item[3] = {v, cur, bc};
+        stage.push(move, item, mlists, &a.st->n_movers);
     }
+    stage.flush(mlists, &a.st->n_movers);
 }
 
 // Scan a hash table: this thread's best candidate by exact X and its share of
@@ -716,18 +723,14 @@ __device__ __forceinline__ void warp_argmax(double &dq, int &bc)
 template <typename VT>
 __device__ __forceinline__ int hash_add_slot(int *keys, VT *vals, int T, int log2t, int key, VT w, bool &created)
 {
+    // one compare-and-swap per probe: it claims an empty slot or returns the
+    // key that holds it
     unsigned h = hash_slot(key, log2t);
     created = false;
     for (int p = 0; p < T; ++p) {
-        int k = *(volatile int *)&keys[h];
-        if (k == -1) {
-            k = atomicCAS(&keys[h], -1, key);
-            if (k == -1) {
-                k = key;
-                created = true;
-            }
-        }
-        if (k == key) {
+        const int k = atomicCAS(&keys[h], -1, key);
+        if (k == -1 || k == key) {
+            created = k == -1;
             atomic_add_w(&vals[h], w);
             return (int)h;
         }
@@ -1234,7 +1237,7 @@ static void decide_t(const LevelGraph &g, Phase1Buffers &b, int bin, const int32
         else
             k_decide_warp<WT, false><<<grid_lanes(32), 256, warp_smem<WT>(), st>>>(a, list, count_ptr);
         break;
-    case 5: {  // 512 (default) or 256 threads per vertex
+    case 5: {  // 256 (default) or 512 threads per vertex
         const size_t sm = cta_smem<WT>(kCtaTable5);
         if (b.b5_block == 256) {
             int grid = level_count < num_sms() * 8 ? level_count : num_sms() * 8;
@@ -1470,6 +1473,9 @@ __global__ void __launch_bounds__(256) k_update_group(UpdateArgs<WT> a, const in
     const long long min_tot = a.st->min_tot;
     unsigned long long s_in = 0, s_edges = 0;
     int s_act = 0;
+    __shared__ int stage_buf[8][kStageN];
+    WarpStage<kStageN, 1> stage{stage_buf[threadIdx.x >> 5], 0};
+    int *const lists[1] = {a.act_list};
     for (int base = wg * GPW; base < count; base += nw * GPW) {
         const int idx = base + gw;
         bool has = idx < count;
@@ -1505,8 +1511,10 @@ __global__ void __launch_bounds__(256) k_update_group(UpdateArgs<WT> a, const in
                 s_act += 1;
             }
         }
-        warp_append(active, v, a.act_list, a.act_counter);
+        const int item[1] = {v};
+        stage.push(active, item, lists, a.act_counter);
     }
+    stage.flush(lists, a.act_counter);
     block_add_u64(s_in, &a.st->sum_in);
     block_add_u64(s_edges, &a.st->act_edges[a.next]);
     block_add_i32(s_act, &a.st->act_vertices[a.next]);

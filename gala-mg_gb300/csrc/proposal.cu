@@ -704,7 +704,8 @@ gala_status gala_proposal_gradient(gala_proposal *p, const float *features, cons
     cudaMemcpyAsync(grad_out, p->grad, kPropParams * sizeof(float), cudaMemcpyDeviceToHost, st);
     float l = 0.f;
     cudaMemcpyAsync(&l, p->loss, sizeof(float), cudaMemcpyDeviceToHost, st);
-    cudaError_t ce = cudaStreamSynchronize(st);
+    cudaError_t ce = cudaGetLastError();  // a failed launch, else the stream's status
+    if (ce == cudaSuccess) ce = cudaStreamSynchronize(st);
     if (ce != cudaSuccess) return cuda_fail(ce, "gala_proposal_gradient");
     if (loss_out) *loss_out = l;
     return GALA_OK;
@@ -724,7 +725,8 @@ gala_status gala_proposal_logits(gala_proposal *p, const float *features, int32_
     k_mlp_logits<<<(n + 255) / 256, 256, 0, st>>>(p->wb, p->Xb, n, p->Yb);
     note_launch(1);
     cudaMemcpyAsync(logits, p->Yb, (size_t)n * sizeof(float), cudaMemcpyDeviceToHost, st);
-    cudaError_t ce = cudaStreamSynchronize(st);
+    cudaError_t ce = cudaGetLastError();  // a failed launch, else the stream's status
+    if (ce == cudaSuccess) ce = cudaStreamSynchronize(st);
     return ce == cudaSuccess ? GALA_OK : cuda_fail(ce, "gala_proposal_logits");
 }
 
@@ -772,7 +774,8 @@ gala_status gala_proposal_train(gala_proposal *p, int32_t epochs, int32_t batch_
         if (ce != cudaSuccess) return cuda_fail(ce, "gala_proposal_train");
         epoch_loss /= (float)n;
     }
-    cudaError_t ce = cudaStreamSynchronize(st);
+    cudaError_t ce = cudaGetLastError();  // a failed launch, else the stream's status
+    if (ce == cudaSuccess) ce = cudaStreamSynchronize(st);
     if (ce != cudaSuccess) return cuda_fail(ce, "gala_proposal_train");
     if (final_loss) *final_loss = epoch_loss;
     return GALA_OK;

@@ -81,8 +81,8 @@ typedef struct {
                                    neighbour twice (lets the first sweep of
                                    level 0 skip aggregation; graphs built by
                                    this library are known to be distinct) */
-    int32_t bin5_block;         /* threads per vertex of degree bin 5: 512
-                                   (default, 0) or 256 */
+    int32_t bin5_block;         /* threads per vertex of degree bin 5: 256
+                                   (default, 0) or 512 */
     int32_t bin_max[3];         /* upper degrees of bins 4, 5, 6 (0 = default
                                    256 / 2048 / 8192; each at most its default,
                                    non-decreasing, bin 4 at least 32); larger
