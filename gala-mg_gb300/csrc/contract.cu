@@ -476,11 +476,12 @@ __device__ __forceinline__ void agg_insert_list(const AggArgs<WT> &a, long long 
             key = a.skey[st + j];
             wt = a.sw[st + j];
         }
-        const unsigned m = __match_any_sync(GALA_FULL_MASK, key);
-        const WT sum = group_sum(m, wt);
+        // shared-memory tables take every entry on its own (cheaper than a
+        // warp-level match of equal keys); the global tables of long rows do
+        // match first, where repeated keys would queue on one address
         int created = 0, slot = -1;
-        if (valid && __ffs(m) - 1 == lane) {
-            created = table_add(keys, vals, T, lg, key, sum, slot);
+        if (valid) {
+            created = table_add(keys, vals, T, lg, key, wt, slot);
             if (created < 0) {
                 atomicOr(&a.st->err, kErrHashOverflow);
                 created = 0;

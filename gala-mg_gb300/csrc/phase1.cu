@@ -746,6 +746,8 @@ __device__ __forceinline__ void scan_list_int(const DecideArgs<WT> &a, const Sca
                                               int stride, int cur, WT ki, WT tcur, long long &x, int &bc, WT &bw,
                                               int &bt, WT &wc)
 {
+    // X = w m2 - K Tot_c - K (K - Tot_cur): the last term is per vertex
+    const long long xbase = WideOf<WT>::exact ? (long long)ki * ((long long)ki - (long long)tcur) : 0;
     for (int q = first; q < nocc; q += stride) {
         const int j = occ[q];
         const int c = keys[j];
@@ -753,7 +755,9 @@ __device__ __forceinline__ void scan_list_int(const DecideArgs<WT> &a, const Sca
         if (c == cur) {
             wc += wv;
         } else {
-            const long long xx = gain_x(wv, ki, a.Tot[c], tcur, sc.m2);
+            const long long xx = WideOf<WT>::exact
+                                     ? (long long)wv * sc.m2 - (long long)ki * (long long)a.Tot[c] - xbase
+                                     : 0;
             if (xx >= 0) cand_merge(x, bc, bw, bt, xx, c, wv, 0);
         }
     }
@@ -814,21 +818,24 @@ __global__ void __launch_bounds__(256) k_decide_warp(DecideArgs<WT> a, const int
         const int deg = (int)(a.offs[v + 1] - s);
         const int cur = a.comm[v];
         int nocc = 0;
+        const int32_t *rn = a.nbr + s;
+        const WT *rw = W ? a.w + s : nullptr;
         for (int e0 = 0; e0 < deg; e0 += 32) {
             const int e = e0 + lane;
             const bool valid = e < deg;
             int c = -1;
             WT wt = 0;
             if (valid) {
-                c = a.comm[a.nbr[s + e]];
-                wt = W ? a.w[s + e] : 1;
+                c = a.comm[rn[e]];
+                wt = W ? rw[e] : 1;
             }
-            const unsigned m = __match_any_sync(GALA_FULL_MASK, c);
-            const WT wsum = W ? group_sum(m, wt) : (WT)__popc(m);
+            // every entry goes to the table on its own: repeated communities
+            // meet at their slot (a warp-level match of equal keys costs more
+            // than the repeated adds it saves)
             bool created = false;
             int slot = -1;
-            if (valid && __ffs(m) - 1 == lane) {
-                slot = hash_add_slot(keys, vals, kWarpTable, kWarpLog, c, wsum, created);
+            if (valid) {
+                slot = hash_add_slot(keys, vals, kWarpTable, kWarpLog, c, wt, created);
                 if (slot < 0) atomicOr(&a.st->err, kErrHashOverflow);
             }
             const unsigned cb = __ballot_sync(GALA_FULL_MASK, created);
@@ -919,12 +926,10 @@ __global__ void __launch_bounds__(BLOCK) k_decide_cta(DecideArgs<WT> a, const in
                 c = a.comm[a.nbr[j]];
                 wt = W ? a.w[j] : 1;
             }
-            const unsigned m = __match_any_sync(GALA_FULL_MASK, c);
-            const WT wsum = W ? group_sum(m, wt) : (WT)__popc(m);
             bool created = false;
             int slot = -1;
-            if (valid && __ffs(m) - 1 == lane) {
-                slot = hash_add_slot(keys, vals, tmax, lg, c, wsum, created);
+            if (valid) {
+                slot = hash_add_slot(keys, vals, tmax, lg, c, wt, created);
                 if (slot < 0) atomicOr(&a.st->err, kErrHashOverflow);
             }
             const unsigned cb = __ballot_sync(GALA_FULL_MASK, created);
