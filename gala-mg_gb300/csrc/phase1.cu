@@ -606,10 +606,30 @@ __global__ void __launch_bounds__(256) k_decide_group(DecideArgs<WT> a, const in
             c = a.comm[a.nbr[s + sub]];
             wt = W ? a.w[s + sub] : 1;
         }
-        const unsigned long long key = ((unsigned long long)(unsigned)gw << 32) | (unsigned)c;
-        const unsigned m = __match_any_sync(GALA_FULL_MASK, key);
-        const WT wsum = W ? group_sum(m, wt) : (WT)__popc(m);
-        const bool leader = valid && (__ffs(m) - 1 == lane);
+        // lanes of the group holding the same community: the lowest leads and
+        // sums the weights (G - 1 shuffles for small groups, a key match for
+        // whole warps)
+        WT wsum;
+        bool leader;
+        if constexpr (G == 32) {
+            const unsigned m = __match_any_sync(GALA_FULL_MASK, c);
+            wsum = W ? group_sum(m, wt) : (WT)__popc(m);
+            leader = valid && (__ffs(m) - 1 == lane);
+        } else {
+            wsum = wt;
+            leader = valid;
+#pragma unroll
+            for (int o = 1; o < G; ++o) {
+                const int osub = (sub + o) & (G - 1);
+                const int src = (lane & ~(G - 1)) | osub;
+                const int oc = __shfl_sync(GALA_FULL_MASK, c, src);
+                const WT ow = __shfl_sync(GALA_FULL_MASK, wt, src);
+                if (oc == c) {
+                    wsum += ow;
+                    if (osub < sub) leader = false;
+                }
+            }
+        }
         const WT wc_own = (leader && c == cur) ? wsum : 0;
         WT wc = wc_own;
         WT tc = 0;
@@ -1716,10 +1736,10 @@ __global__ void __launch_bounds__(256) k_hub_insert(DecideArgs<WT> a, HubPlan p,
                 c = a.comm[a.nbr[j]];
                 wt = W ? a.w[j] : 1;
             }
-            const unsigned m = __match_any_sync(GALA_FULL_MASK, c);
-            const WT wsum = W ? group_sum(m, wt) : (WT)__popc(m);
-            if (valid && __ffs(m) - 1 == lane)
-                if (!hash_add(keys, vals, T, lg, c, wsum)) atomicOr(&a.st->err, kErrHashOverflow);
+            // entries go to the hub's table one by one (no warp-level key
+            // match: measured faster on the hub rows of R-MAT levels)
+            if (valid)
+                if (!hash_add(keys, vals, T, lg, c, wt)) atomicOr(&a.st->err, kErrHashOverflow);
         }
     }
 }
