@@ -675,12 +675,32 @@ __device__ __forceinline__ WT *big_vals(const BigArgs &b, long long i)
     return (WT *)(b.pool + b.pool_half) + b.toff[i];
 }
 
-// Every CTA inserts one chunk of kChunk stream entries into its community's
-// global table; many CTAs share one community.  New keys are counted.
+// Every CTA aggregates one chunk of kChunk stream entries of a long row in a
+// shared-memory table first, then adds the chunk's distinct keys to the row's
+// global table (many CTAs share one row); new keys are counted.
+constexpr int kSmT = 8192;  // shared-memory slots for a kChunk-entry chunk
 template <typename WT>
-__global__ void __launch_bounds__(256) k_big_insert(AggArgs<WT> a, BigArgs b, long long nwork)
+constexpr size_t big_sm_smem()
 {
-    __shared__ int red[8];
+    return (size_t)kSmT * (sizeof(WT) + sizeof(int) + sizeof(unsigned short));
+}
+template <typename WT>
+__global__ void __launch_bounds__(512) k_big_insert_sm(AggArgs<WT> a, BigArgs b, long long nwork)
+{
+    extern __shared__ long long bsm_ll[];
+    WT *svals = (WT *)bsm_ll;
+    int *skeys = (int *)(svals + kSmT);
+    unsigned short *socc = (unsigned short *)(skeys + kSmT);
+    __shared__ int s_n;
+    __shared__ int red[16];
+    for (int q = threadIdx.x; q < kSmT; q += blockDim.x) {
+        skeys[q] = -1;
+        svals[q] = 0;
+    }
+    if (threadIdx.x == 0) s_n = 0;
+    __syncthreads();
+    constexpr int slg = 13;
+    static_assert((1 << slg) == kSmT, "table size");
     for (long long wi = blockIdx.x; wi < nwork; wi += gridDim.x) {
         const int i = b.work[wi];
         const long long j = wi - b.coff[i];
@@ -691,7 +711,33 @@ __global__ void __launch_bounds__(256) k_big_insert(AggArgs<WT> a, BigArgs b, lo
         const long long T = b.T[i];
         WT *vals = big_vals<WT>(b, i);
         int *keys = b.mode[i] ? nullptr : b.pool + b.toff[i];
-        int created = agg_insert(a, st, len, keys, vals, (int)T, keys ? __ffs((int)T) - 1 : 0);
+        const int lg = keys ? __ffs((int)T) - 1 : 0;
+        for (int q = threadIdx.x; q < len; q += blockDim.x) {
+            const int key = a.skey[st + q];
+            const WT wt = a.sw[st + q];
+            unsigned h = hash_slot(key, slg);
+            for (int p = 0; p < kSmT; ++p) {
+                const int k = atomicCAS(&skeys[h], -1, key);
+                if (k == -1 || k == key) {
+                    atomic_add_w(&svals[h], wt);
+                    if (k == -1) socc[atomicAdd(&s_n, 1)] = (unsigned short)h;
+                    break;
+                }
+                h = (h + 1) & (unsigned)(kSmT - 1);
+            }
+        }
+        __syncthreads();
+        const int n = s_n;
+        int created = 0;
+        for (int q = threadIdx.x; q < n; q += blockDim.x) {
+            const int h = socc[q];
+            int slot;
+            const int r = table_add(keys, vals, (int)T, lg, skeys[h], svals[h], slot);
+            if (r < 0) atomicOr(&a.st->err, kErrHashOverflow);
+            created += r == 1;
+            skeys[h] = -1;
+            svals[h] = 0;
+        }
         created = warp_sum(created);
         if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = created;
         __syncthreads();
@@ -699,6 +745,7 @@ __global__ void __launch_bounds__(256) k_big_insert(AggArgs<WT> a, BigArgs b, lo
             int s = 0;
             for (int q = 0; q < (int)(blockDim.x >> 5); ++q) s += red[q];
             if (s) atomicAdd(&b.kdist[i], s);
+            s_n = 0;
         }
         __syncthreads();
     }
@@ -911,6 +958,7 @@ static void configure_t()
     configure_mid<WT>();
 
     cudaFuncSetAttribute(k_big_sort<WT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sort_smem<WT>());
+    cudaFuncSetAttribute(k_big_insert_sm<WT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)big_sm_smem<WT>());
     cudaFuncSetAttribute(k_agg_mid_list<WT, 1024, 8192>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)list_smem<WT>(8192));
     cudaFuncSetAttribute(k_agg_mid_list<WT, 1024, 16384>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -999,7 +1047,7 @@ static bool contract_long_rows(const AggArgs<WT> &a, ContractBuffers &b, int cnt
     cudaMemsetAsync(b.big_pool, 0xff, (size_t)slots * sizeof(int32_t), st);
     cudaMemsetAsync(b.big_pool + half, 0, (size_t)slots * sizeof(WT), st);
     k_big_work<WT><<<grid_cap((long long)cnt3 * 32, 256, cap), 256, 0, st>>>(a, ba);
-    k_big_insert<WT><<<(int)(nwork < nsm * 8 ? nwork : nsm * 8), 256, 0, st>>>(a, ba, nwork);
+    k_big_insert_sm<WT><<<(int)(nwork < nsm * 2 ? nwork : nsm * 2), 512, big_sm_smem<WT>(), st>>>(a, ba, nwork);
     k_big_mark<WT><<<grid_cap(cnt3, 256, cap), 256, 0, st>>>(a, ba, sort_rows ? 1 : 0);
     exclusive_scan(b.big_gwords, b.big_gofs, cnt3, OpIdentity(), b.scan_partial, &b.stats->total, st);
     note_launch(3);
