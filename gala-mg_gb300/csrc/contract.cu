@@ -1083,7 +1083,7 @@ template <typename WT>
 static int contract_t(const LevelGraph &g, const int32_t *comm, ContractBuffers &b, int64_t *new_offs,
                       int32_t *new_nbr, WT *new_w, int32_t *orig_map, int32_t n_orig, int64_t *new_E,
                       cudaStream_t st, gala_status *status, bool validate_labels, bool sort_rows,
-                      const NextLevelInit &nli)
+                      const NextLevelInit &nli, bool labels_only)
 {
     const int n = g.n;
     const int cap = sm_count() * 8;
@@ -1113,6 +1113,11 @@ static int contract_t(const LevelGraph &g, const int32_t *comm, ContractBuffers 
                                                          (const WT *)nli.tot, (WT *)nli.k);
     if (nli.self) cudaMemsetAsync(nli.self, 0, (size_t)C * sizeof(WT), st);
     if (orig_map) k_compose<<<grid_cap(n_orig, 256, cap), 256, 0, st>>>(orig_map, n_orig, b.lab);
+    if (labels_only) {
+        note_launch(1 + (orig_map ? 1 : 0));
+        *new_E = 0;
+        return C;
+    }
     exclusive_scan(b.csz, b.moff, C, OpIdentity(), b.scan_partial, &b.stats->total, st);
     cudaMemcpyAsync(b.cursor, b.moff, (size_t)C * sizeof(int32_t), cudaMemcpyDeviceToDevice, st);
     cudaMemsetAsync(b.ec, 0, ((size_t)C + 1) * sizeof(long long), st);
@@ -1204,7 +1209,7 @@ static int contract_t(const LevelGraph &g, const int32_t *comm, ContractBuffers 
 int contract_run(const LevelGraph &g, const int32_t *comm, ContractBuffers &b, int64_t *new_offs,
                  int32_t *new_nbr, void *new_w, int32_t *orig_map, int32_t n_orig, int64_t *new_E,
                  cudaStream_t st, gala_status *status, bool validate_labels, bool sort_rows,
-                 const NextLevelInit &nli)
+                 const NextLevelInit &nli, bool labels_only)
 {
     if ((nli.k != nullptr) != (nli.tot != nullptr)) {
         set_error("contraction: K_new needs the community totals");
@@ -1213,9 +1218,9 @@ int contract_run(const LevelGraph &g, const int32_t *comm, ContractBuffers &b, i
     }
     if (g.wide)
         return contract_t<long long>(g, comm, b, new_offs, new_nbr, (long long *)new_w, orig_map, n_orig, new_E, st,
-                                     status, validate_labels, sort_rows, nli);
+                                     status, validate_labels, sort_rows, nli, labels_only);
     return contract_t<int>(g, comm, b, new_offs, new_nbr, (int *)new_w, orig_map, n_orig, new_E, st, status,
-                           validate_labels, sort_rows, nli);
+                           validate_labels, sort_rows, nli, labels_only);
 }
 
 }  // namespace gala

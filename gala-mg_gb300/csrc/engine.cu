@@ -751,13 +751,18 @@ gala_status run_levels(gala_context *ctx, int32_t n0, int64_t E0, const int64_t 
         upd_bytes += po.update_bytes;
         sweeps += po.sweeps;
         if (verbose && round == 0) printf("louvain time in the first round = %fms\n", po.total_ms);
-        // contraction into the other ping-pong buffer
+        // contraction into the other ping-pong buffer; the last round (the
+        // stop rule below decides it from this round's Q already) only needs
+        // the labels, unless the level graph is checkpointed
+        const bool last = !bt && !level_dir &&
+                          (!(po.q - cur_mod >= min_mod) || (max_levels > 0 && round + 1 >= max_levels) ||
+                           round + 1 >= GALA_MAX_LEVELS);
         cudaEventRecord(ctx->ev[0], st);
         int64_t newE = 0;
         gala_status cs = GALA_OK;
         C = contract_run(g, ctx->p1.comm, ctx->cb, ctx->offs[buf], ctx->nbr[buf], ctx->w[buf], ctx->orig, n0, &newE,
                          st, &cs, false, opt && opt->sorted_levels == 1,
-                         NextLevelInit{ctx->p1.Tot, ctx->p1.K, ctx->p1.Self});
+                         NextLevelInit{ctx->p1.Tot, ctx->p1.K, ctx->p1.Self}, last);
         if (C < 0) return cs;
         cudaEventRecord(ctx->ev[1], st);
         if ((s = sync_check(st, "contraction"))) return s;

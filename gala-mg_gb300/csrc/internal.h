@@ -221,6 +221,9 @@ struct ContractBuffers {
 // every new row in hash-table order: phase 1 does not depend on the order of
 // a row's entries (all weight sums are exact integers), and the sorts are
 // skipped.  gala_contract_device sorts, as the oracle does.
+// labels_only: the new labels (renumbering and orig_map composition) and the
+// community count only, no rows (the last round of a run, whose graph nobody
+// reads); *new_E is 0.
 // Optional by-products for the next level's phase 1 (all null: none): the
 // weighted degree of every new vertex (K_new[c'] = Tot[c], the community
 // total of the level contracted) and its self-loop weight (the weight of the
@@ -233,6 +236,6 @@ struct NextLevelInit {
 int contract_run(const LevelGraph &g, const int32_t *comm, ContractBuffers &b, int64_t *new_offs,
                  int32_t *new_nbr, void *new_w, int32_t *orig_map, int32_t n_orig,
                  int64_t *new_E, cudaStream_t st, gala_status *status, bool validate_labels = false,
-                 bool sort_rows = true, const NextLevelInit &nli = NextLevelInit());
+                 bool sort_rows = true, const NextLevelInit &nli = NextLevelInit(), bool labels_only = false);
 
 }  // namespace gala
