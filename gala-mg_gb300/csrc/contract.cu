@@ -1161,7 +1161,7 @@ static int contract_t(const LevelGraph &g, const int32_t *comm, ContractBuffers 
         note_launch(1);
     }
     if (hs.small_cnt[1] > 0) {
-        int grid = hs.small_cnt[1] < nsm * 12 ? hs.small_cnt[1] : nsm * 12;
+        int grid = hs.small_cnt[1] < nsm * 16 ? hs.small_cnt[1] : nsm * 16;
         if (sort_rows)
             k_agg_mid<WT, 128, 1024, kMid1Max><<<grid, 128, mid1_smem<WT>(), st>>>(a, b.cls_list + (long long)C, 1);
         else
