@@ -115,7 +115,7 @@ class Clocks:
     def start(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "50"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
@@ -125,6 +125,10 @@ class Clocks:
     def _read(self):
         for line in self.proc.stdout:
             self.lines.append(line.strip())
+
+    def mark(self):
+        """Samples before this call (warm-up) are not reported."""
+        self.first = len(self.lines)
 
     def stop(self):
         if not self.proc:
@@ -137,7 +141,11 @@ class Clocks:
         self.t.join(timeout=2)
         sm, smax, reasons = [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for ln in self.lines:
+        # samples of the timed region; if it was shorter than one sampling
+        # period, the last warm-up sample (taken under the same load)
+        first = getattr(self, "first", 0)
+        lines = self.lines[first:] or self.lines[max(first - 1, 0):first]
+        for ln in lines:
             f = [x.strip() for x in ln.split(",")]
             if len(f) < 9:
                 continue
@@ -392,15 +400,17 @@ def main():
         ctx.close()
         return
 
+    # the clock sampler starts before the warm-up: its start-up (NVML
+    # initialisation in a separate process) stays out of the timed region
+    clocks = Clocks(local)
+    clocks.start()
     for _ in range(args.warmup):
         r = run_device()
     # ---- device-resident timed region ----
-    clocks = Clocks(local)
     if dist:
         dist.barrier()
     torch.cuda.synchronize()
-    clocks.start()
-    time.sleep(0.3)
+    clocks.mark()
     ev0 = torch.cuda.Event(enable_timing=True)
     ev1 = torch.cuda.Event(enable_timing=True)
     l0 = ffi.launch_count()

@@ -1256,16 +1256,19 @@ static void decide_t(const LevelGraph &g, Phase1Buffers &b, int bin, const int32
     case 1: GALA_DG(8); break;
     case 2: GALA_DG(16); break;
     case 3: GALA_DG(32); break;
-    case 4:
+    case 4: {
+        // as many CTAs as the tables let reside (5 per SM): no second wave
+        const int g4 = grid_lanes(32) < num_sms() * 5 ? grid_lanes(32) : num_sms() * 5;
         if (W)
-            k_decide_warp<WT, true><<<grid_lanes(32), 256, warp_smem<WT>(), st>>>(a, list, count_ptr);
+            k_decide_warp<WT, true><<<g4, 256, warp_smem<WT>(), st>>>(a, list, count_ptr);
         else
-            k_decide_warp<WT, false><<<grid_lanes(32), 256, warp_smem<WT>(), st>>>(a, list, count_ptr);
+            k_decide_warp<WT, false><<<g4, 256, warp_smem<WT>(), st>>>(a, list, count_ptr);
         break;
+    }
     case 5: {  // 256 (default) or 512 threads per vertex
         const size_t sm = cta_smem<WT>(kCtaTable5);
         if (b.b5_block == 256) {
-            int grid = level_count < num_sms() * 8 ? level_count : num_sms() * 8;
+            int grid = level_count < num_sms() * 5 ? level_count : num_sms() * 5;
             if (W)
                 k_decide_cta<WT, 256, true><<<grid, 256, sm, st>>>(a, list, count_ptr, kCtaTable5);
             else
