@@ -123,6 +123,16 @@ def test_rmat_power_law(ffi, oracle, torch_cuda):
     o = oracle.louvain(offs, nbr, None, nthreads=0)
     _assert_same(r, o)
     assert abs(g.modularity(r["labels"]) - r["modularity"]) < 1e-9
+    # per-round diagnostics: round 0 runs on the input graph, every later round
+    # on the previous round's communities; moves and decided entries add up
+    lv = r["levels"]
+    assert len(lv) == r["rounds"] and lv[0]["vertices"] == offs.shape[0] - 1 and lv[0]["entries"] == offs[-1]
+    for k in range(1, len(lv)):
+        assert lv[k]["vertices"] == r["level_c"][k - 1]
+        assert lv[k]["entries"] <= lv[k - 1]["entries"]
+    assert sum(x["active_entries"] for x in lv) >= sum(x["entries"] for x in lv)
+    assert all(x["decide_ms"] + x["update_ms"] <= x["phase1_ms"] + 1e-3 for x in lv)
+    assert abs(sum(x["contract_ms"] for x in lv) - r["time_contract_ms"]) < 1e-3
 
 
 @pytest.mark.parametrize("case", ["karate", "sbm", "rmat", "weighted", "small_weights"])
