@@ -685,13 +685,13 @@ constexpr size_t big_sm_smem()
     return (size_t)kSmT * (sizeof(WT) + sizeof(int) + sizeof(unsigned short));
 }
 template <typename WT>
-__global__ void __launch_bounds__(512) k_big_insert_sm(AggArgs<WT> a, BigArgs b, long long nwork)
+__global__ void __launch_bounds__(512) k_big_insert_sm(AggArgs<WT> a, BigArgs b, long long nwork, int lists)
 {
     extern __shared__ long long bsm_ll[];
     WT *svals = (WT *)bsm_ll;
     int *skeys = (int *)(svals + kSmT);
     unsigned short *socc = (unsigned short *)(skeys + kSmT);
-    __shared__ int s_n;
+    __shared__ int s_n, s_base;
     __shared__ int red[16];
     for (int q = threadIdx.x; q < kSmT; q += blockDim.x) {
         skeys[q] = -1;
@@ -728,24 +728,57 @@ __global__ void __launch_bounds__(512) k_big_insert_sm(AggArgs<WT> a, BigArgs b,
         }
         __syncthreads();
         const int n = s_n;
-        int created = 0;
-        for (int q = threadIdx.x; q < n; q += blockDim.x) {
-            const int h = socc[q];
-            int slot;
-            const int r = table_add(keys, vals, (int)T, lg, skeys[h], svals[h], slot);
-            if (r < 0) atomicOr(&a.st->err, kErrHashOverflow);
-            created += r == 1;
-            skeys[h] = -1;
-            svals[h] = 0;
+        // the chunk's distinct keys go to the global table; with lists, the
+        // slots this chunk created are appended to the row's slot list (in the
+        // row's own tmp range), one counter add per chunk
+        constexpr int kIt = kChunk / 512;
+        int made[kIt];
+        unsigned mask = 0;
+#pragma unroll
+        for (int it = 0; it < kIt; ++it) {
+            const int q = threadIdx.x + it * 512;
+            made[it] = 0;
+            if (q < n) {
+                const int h = socc[q];
+                int slot;
+                const int r = table_add(keys, vals, (int)T, lg, skeys[h], svals[h], slot);
+                if (r < 0) atomicOr(&a.st->err, kErrHashOverflow);
+                if (r == 1) {
+                    mask |= 1u << it;
+                    made[it] = slot;
+                }
+                skeys[h] = -1;
+                svals[h] = 0;
+            }
         }
-        created = warp_sum(created);
-        if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = created;
+        const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+        const int mine = __popc(mask);
+        int incl = mine;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int t = __shfl_up_sync(GALA_FULL_MASK, incl, o);
+            if (lane >= o) incl += t;
+        }
+        if (lane == 31) red[wid] = incl;
         __syncthreads();
         if (threadIdx.x == 0) {
-            int s = 0;
-            for (int q = 0; q < (int)(blockDim.x >> 5); ++q) s += red[q];
-            if (s) atomicAdd(&b.kdist[i], s);
+            int tot = 0;
+            for (int q = 0; q < (int)(blockDim.x >> 5); ++q) {
+                const int t = red[q];
+                red[q] = tot;
+                tot += t;
+            }
+            if (tot) atomicAdd(&b.kdist[i], tot);
+            s_base = (lists && tot) ? atomicAdd(&b.cursor[i], tot) : 0;
             s_n = 0;
+        }
+        __syncthreads();
+        if (lists && mask) {
+            int p = s_base + red[wid] + incl - mine;
+            const long long o = a.tmp_off[c];
+#pragma unroll
+            for (int it = 0; it < kIt; ++it)
+                if (mask & (1u << it)) a.tmp_nbr[o + p++] = made[it];
         }
         __syncthreads();
     }
@@ -764,6 +797,55 @@ __global__ void k_big_mark(AggArgs<WT> a, BigArgs b, int sort_rows)
         b.gwords[i] = (sort_rows && k > kSortMax) ? words : 0;
         a.kc[b.list[i]] = k;
     }
+}
+
+// Rows in table order: every kChunk entries of a row's slot list (written by
+// the inserts into the row's own tmp range) are replaced in place by the
+// (key, value) of their slot.  Work items: lcoff is the exclusive scan of
+// the list chunks per row, *total their number.
+template <typename WT>
+__global__ void __launch_bounds__(256) k_big_collect_list(AggArgs<WT> a, BigArgs b, const long long *lcoff,
+                                                          const long long *total)
+{
+    const int cnt = a.st->small_cnt[kLongCls];
+    const long long nw = *total;
+    for (long long w = blockIdx.x; w < nw; w += gridDim.x) {
+        int lo = 0, hi = cnt - 1;  // last row with lcoff <= w
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (lcoff[mid] <= w) lo = mid;
+            else hi = mid - 1;
+        }
+        const int i = lo;
+        const int c = b.list[i];
+        const long long q0 = (w - lcoff[i]) * kChunk;
+        const long long k = b.cursor[i];
+        const long long q1 = q0 + kChunk < k ? q0 + kChunk : k;
+        const long long o = a.tmp_off[c];
+        const bool dense = b.mode[i];
+        const WT *vals = big_vals<WT>(b, i);
+        const int *keys = b.pool + b.toff[i];
+        for (long long q = q0 + threadIdx.x; q < q1; q += blockDim.x) {
+            const int slot = a.tmp_nbr[o + q];
+            a.tmp_nbr[o + q] = dense ? slot : keys[slot];
+            a.tmp_w[o + q] = vals[slot];
+        }
+    }
+}
+
+// Row length of every long row in table order: its slot-list length.
+template <typename WT>
+__global__ void k_big_len(AggArgs<WT> a, BigArgs b)
+{
+    const int cnt = a.st->small_cnt[kLongCls];
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < cnt; i += gridDim.x * blockDim.x)
+        a.kc[b.list[i]] = b.cursor[i];
+}
+
+__global__ void k_big_lchunks(const int *cursor, int cnt, long long *lch)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < cnt; i += gridDim.x * blockDim.x)
+        lch[i] = (cursor[i] + kChunk - 1) / kChunk;
 }
 
 // Table chunks: distinct entries of sorted rows go to the row unsorted
@@ -1047,7 +1129,19 @@ static bool contract_long_rows(const AggArgs<WT> &a, ContractBuffers &b, int cnt
     cudaMemsetAsync(b.big_pool, 0xff, (size_t)slots * sizeof(int32_t), st);
     cudaMemsetAsync(b.big_pool + half, 0, (size_t)slots * sizeof(WT), st);
     k_big_work<WT><<<grid_cap((long long)cnt3 * 32, 256, cap), 256, 0, st>>>(a, ba);
-    k_big_insert_sm<WT><<<(int)(nwork < nsm * 2 ? nwork : nsm * 2), 512, big_sm_smem<WT>(), st>>>(a, ba, nwork);
+    k_big_insert_sm<WT><<<(int)(nwork < nsm * 2 ? nwork : nsm * 2), 512, big_sm_smem<WT>(), st>>>(
+        a, ba, nwork, sort_rows ? 0 : 1);
+    if (!sort_rows) {
+        // rows in table order: collect from the slot lists, no table scans
+        long long *lch = b.big_tchunks, *lcoff = b.big_tcoff;
+        k_big_lchunks<<<grid_cap(cnt3, 256, cap), 256, 0, st>>>(ba.cursor, cnt3, lch);
+        exclusive_scan(lch, lcoff, cnt3, OpIdentity(), b.scan_partial, &b.stats->total3, st);
+        k_big_collect_list<WT><<<(int)(nwork < nsm * 8 ? nwork : nsm * 8), 256, 0, st>>>(a, ba, lcoff,
+                                                                                          &b.stats->total3);
+        k_big_len<WT><<<grid_cap(cnt3, 256, cap), 256, 0, st>>>(a, ba);
+        note_launch(4);
+        return true;
+    }
     k_big_mark<WT><<<grid_cap(cnt3, 256, cap), 256, 0, st>>>(a, ba, sort_rows ? 1 : 0);
     exclusive_scan(b.big_gwords, b.big_gofs, cnt3, OpIdentity(), b.scan_partial, &b.stats->total, st);
     note_launch(3);
