@@ -33,6 +33,7 @@ struct gala_context {
     int32_t *orig = nullptr;
     Phase1Buffers p1{};
     ContractBuffers cb{};
+    RefineBuffers ref{};  // allocated on the first run with gala_options.refine
     DevStats *d_stats = nullptr;
     DevStats *h_stats = nullptr;
     int32_t *scratch = nullptr;
@@ -237,7 +238,7 @@ long long decide_bytes_for(long long nv, long long ne, bool weighted)
 // have stopped.
 gala_status phase1(gala_context *ctx, const LevelGraph &g, long long &m2, double min_mod, bool verbose,
                    std::vector<double> *trace, Phase1Out *out, int fp64_only = 0, const PropRun *pr = nullptr,
-                   BatchRun *bt = nullptr, bool use_graphs = false)
+                   BatchRun *bt = nullptr, bool use_graphs = false, const int32_t *init = nullptr)
 {
     const int pmode = pr ? pr->mode : GALA_PROPOSAL_OFF;
     cudaStream_t st = ctx->stream;
@@ -359,6 +360,27 @@ gala_status phase1(gala_context *ctx, const LevelGraph &g, long long &m2, double
         cudaMemcpyAsync(bt->stop, bt->h_stop, G, cudaMemcpyHostToDevice, st);
     }
 
+    if (init) {
+        // a refined level starts from its parent communities: Tot and size
+        // follow them, the weight update gives In and the sums, and every
+        // vertex starts active
+        p1_iter_reset(b, 1, (!g.wide && m2 > 0x7fffffffLL) ? 0x7fffffffLL : m2, st);
+        p1_start_partition(b, init, g.n, st);
+        p1_tot_reduce(b, g.n, st);
+        fork(ctx);
+        for (int k = 0; k < kNumBins; ++k) {
+            const int bin = kBinLaunchOrder[k];
+            if (bin == 7)
+                p1_hub_update(g, b, hp, 1, bin_start[bin], constant, m2, aux_for(ctx, k));
+            else
+                p1_update(g, b, bin, b.order + bin_start[bin], level_cnt[bin], 1, bin_start[bin], constant, m2,
+                          aux_for(ctx, k));
+        }
+        join(ctx);
+        if ((s = check(cudaMemcpyAsync(h, b.stats, sizeof(DevStats), cudaMemcpyDeviceToHost, st), "start partition")) ||
+            (s = sync_check(st, "start partition")))
+            return s;
+    }
     double q = q_from_sums(h->sum_in, h->sum_tot2, m2, h->sum_tot2_hi);
     if (trace) trace->push_back(q);
     if (verbose) printf("Iteration:%d Q:%f\n", 0, q);
@@ -427,7 +449,7 @@ gala_status phase1(gala_context *ctx, const LevelGraph &g, long long &m2, double
                     p1_hub_decide(g, b, hp, constant, m2, fp64_only, aux_for(ctx, k));
                 else
                     p1_decide(g, b, bin, lists + bin_start[bin], counts + bin, level_cnt[bin], constant, m2,
-                              fp64_only, iteration == 1 && g.distinct, aux_for(ctx, k));
+                              fp64_only, iteration == 1 && g.distinct && !init, aux_for(ctx, k));
             }
             join(ctx);
             rec(ctx->ev[3]);
@@ -720,6 +742,24 @@ gala_status run_levels(gala_context *ctx, int32_t n0, int64_t E0, const int64_t 
         set_error("proposal modes are not available for float-weight graphs");
         return GALA_ERR_INVALID;
     }
+    const bool refine = opt && opt->refine == 1;
+    if (refine && (bt || wide || pr.mode != GALA_PROPOSAL_OFF || level_dir)) {
+        set_error("refinement is available for single integer-weight graphs without proposals or checkpoints");
+        return GALA_ERR_INVALID;
+    }
+    if (refine && !ctx->ref.R) {
+        RefineBuffers &rb = ctx->ref;
+        const size_t nc = (size_t)ctx->n_cap + 1;
+        if (!(dalloc(ctx, &rb.R, nc) && dalloc(ctx, &rb.target, nc) && dalloc(ctx, &rb.marks, nc) &&
+              dalloc(ctx, &rb.sz, nc) && dalloc(ctx, &rb.wC, nc) && dalloc(ctx, &rb.ext, nc) &&
+              dalloc(ctx, &rb.Kr, nc) && dalloc(ctx, &rb.pmin, nc) && dalloc(ctx, &rb.init, nc) &&
+              dalloc(ctx, &rb.moved, 1))) {
+            rb = RefineBuffers{};
+            set_error("refinement: out of device memory");
+            return GALA_ERR_CAPACITY;
+        }
+    }
+    bool have_init = false;  // this round starts from the previous round's communities
     LevelGraph g{n0, E0, offs0, nbr0, w0, wide, distinct0 || (opt && opt->distinct_rows == 1)};
     int buf = 0;
     double prev_mod = -1, cur_mod = -1;
@@ -736,8 +776,9 @@ gala_status run_levels(gala_context *ctx, int32_t n0, int64_t E0, const int64_t 
         if (verbose) printf("===============round:%d===============\n", round);
         Phase1Out po;
         pr.level = round;
+        const bool started_refined = have_init;
         if ((s = phase1(ctx, g, m2, min_mod, verbose, &trace, &po, opt ? opt->fp64_gains : 0, &pr, bt,
-                        opt && opt->use_graphs)))
+                        opt && opt->use_graphs, have_init ? ctx->ref.init : nullptr)))
             return s;
         if (bt)  // communities per graph, for the graphs' id ranges at the next level
             batch_graph_sums(kCountComm, bt->G, bt->goff, nullptr, ctx->p1, bt->sums(), st);
@@ -754,16 +795,31 @@ gala_status run_levels(gala_context *ctx, int32_t n0, int64_t E0, const int64_t 
         // contraction into the other ping-pong buffer; the last round (the
         // stop rule below decides it from this round's Q already) only needs
         // the labels, unless the level graph is checkpointed
+        // (a round that started from refined communities and gained less
+        // than min_mod is not the last: the next contracts the communities)
+        const bool gained = po.q - cur_mod >= min_mod;
         const bool last = !bt && !level_dir &&
-                          (!(po.q - cur_mod >= min_mod) || (max_levels > 0 && round + 1 >= max_levels) ||
+                          ((!gained && !started_refined) || (max_levels > 0 && round + 1 >= max_levels) ||
                            round + 1 >= GALA_MAX_LEVELS);
+        const bool do_refine = refine && !last && gained;
         cudaEventRecord(ctx->ev[0], st);
         int64_t newE = 0;
         gala_status cs = GALA_OK;
-        C = contract_run(g, ctx->p1.comm, ctx->cb, ctx->offs[buf], ctx->nbr[buf], ctx->w[buf], ctx->orig, n0, &newE,
-                         st, &cs, false, opt && opt->sorted_levels == 1,
-                         NextLevelInit{ctx->p1.Tot, ctx->p1.K, ctx->p1.Self}, last);
+        // the refinement (counted with the contraction) replaces the labels
+        // the contraction groups by and the totals of the new vertices
+        const int32_t *ccomm = ctx->p1.comm;
+        NextLevelInit nli{ctx->p1.Tot, ctx->p1.K, ctx->p1.Self};
+        if (do_refine) {
+            if (refine_run(g, ctx->p1.comm, ctx->p1.K, ctx->p1.Tot, m2, ctx->ref, ctx->d_stats, st, &cs) < 0)
+                return cs;
+            ccomm = ctx->ref.R;
+            nli.tot = ctx->ref.Kr;
+        }
+        C = contract_run(g, ccomm, ctx->cb, ctx->offs[buf], ctx->nbr[buf], ctx->w[buf], ctx->orig, n0, &newE, st,
+                         &cs, false, opt && opt->sorted_levels == 1, nli, last);
         if (C < 0) return cs;
+        if (do_refine) refine_next_init(ctx->p1.comm, ctx->cb.lab, g.n, ctx->ref, st);
+        have_init = do_refine;
         cudaEventRecord(ctx->ev[1], st);
         if ((s = sync_check(st, "contraction"))) return s;
         float cms = ev_ms(ctx->ev[0], ctx->ev[1]);
@@ -823,7 +879,8 @@ gala_status run_levels(gala_context *ctx, int32_t n0, int64_t E0, const int64_t 
             continue;
         }
         // louvain.cu:202: continue while the round gained at least min_mod
-        if (!(cur_mod - prev_mod >= min_mod)) break;
+        // (or, refining, while it started from refined communities)
+        if (!(cur_mod - prev_mod >= min_mod) && !started_refined) break;
         if (max_levels > 0 && round >= max_levels) break;
         if (round >= GALA_MAX_LEVELS) break;
     }

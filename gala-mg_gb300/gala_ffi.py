@@ -50,7 +50,7 @@ class Options(ctypes.Structure):
                 ("proposal_mode", ctypes.c_int32), ("proposal_threshold", ctypes.c_float),
                 ("trace_sample_shift", ctypes.c_int32), ("sorted_levels", ctypes.c_int32), ("proposal", ctypes.c_void_p),
                 ("distinct_rows", ctypes.c_int32), ("bin5_block", ctypes.c_int32),
-                ("bin_max", ctypes.c_int32 * 3), ("reserved3", ctypes.c_int32), ("level_dir", ctypes.c_char_p)]
+                ("bin_max", ctypes.c_int32 * 3), ("refine", ctypes.c_int32), ("level_dir", ctypes.c_char_p)]
 
 
 class Tuning(ctypes.Structure):
@@ -377,10 +377,11 @@ class Context:
 
     def louvain(self, graph, min_mod=1e-6, max_levels=0, verbose=False, iter_capacity=4096, fp64_gains=False,
                 proposal=None, mode=PROPOSAL_OFF, threshold=0.5, sample_shift=0, sorted_levels=False,
-                use_graphs=False, tuning=None, level_dir=None):
+                use_graphs=False, tuning=None, level_dir=None, refine=False):
         """gala_louvain: host graph in, host labels out.  `proposal` (a
         Proposal) with mode PROPOSAL_TRACE records training samples, with
-        PROPOSAL_SKIP decides only the vertices it proposes."""
+        PROPOSAL_SKIP decides only the vertices it proposes; `refine` turns
+        on the Leiden-style refinement."""
         n, _, _ = graph.info()
         labels = np.zeros(n, dtype=np.int32)
         trace = np.zeros(iter_capacity, dtype=np.float64)
@@ -391,7 +392,7 @@ class Context:
                             fp64_gains=int(fp64_gains), proposal_mode=int(mode),
                             proposal_threshold=float(threshold), trace_sample_shift=int(sample_shift),
                             sorted_levels=int(sorted_levels), use_graphs=int(use_graphs),
-                            proposal=proposal.h if proposal is not None else None)
+                            proposal=proposal.h if proposal is not None else None, refine=int(refine))
         if tuning:
             o.bin_max = (ctypes.c_int32 * 3)(*tuning["bin_max"])
             o.bin5_block = tuning["bin5_block"]

@@ -89,7 +89,14 @@ typedef struct {
                                    rows go to the next bin, above bin 6 to the
                                    multi-CTA hub path.  Any values give the same
                                    partition; gala_autotune picks fast ones. */
-    int32_t reserved3;
+    int32_t refine;             /* 1 = Leiden-style refinement (no counterpart in
+                                   the reference): a round that gained at least
+                                   min_modularity contracts the refinement of its
+                                   communities into well-connected
+                                   sub-communities, and the next round starts
+                                   from the communities; integer-weight single
+                                   graphs only (not with batches, proposals or
+                                   level_dir).  0 = the reference's rounds. */
     /* Checkpoints (no counterpart in the reference, which never writes its
        partition, louvain.cu:226): when set, after every round r the
        contracted graph is written to <level_dir>/level_<r+1>.bin (the .bin

@@ -140,9 +140,13 @@ static int32_t decide_vertex(int32_t v, const int64_t *offs, const int32_t *nbr,
     return cur;
 }
 
+/* init (NULL: singletons) is the starting partition of a refined level (no
+ * counterpart in the reference): Tot and size follow it, In is the weight
+ * update of compute_In on it, and every vertex starts active. */
 static int32_t phase1_w64(int32_t n, const int64_t *offs, const int32_t *nbr, const int64_t *w,
                           int64_t m2, double min_mod, int32_t *labels_out, double *q_out,
-                          double *iter_q, int32_t iter_cap, int32_t *n_iter_q, int32_t nthreads)
+                          double *iter_q, int32_t iter_cap, int32_t *n_iter_q, int32_t nthreads,
+                          const int32_t *init)
 {
     if (n <= 0 || m2 <= 0) return -1;
 #ifdef _OPENMP
@@ -191,7 +195,28 @@ static int32_t phase1_w64(int32_t n, const int64_t *offs, const int32_t *nbr, co
         sum_in += sf;
         active[v] = 1;
     }
-    for (int32_t v = 0; v < n; ++v) sum_tot2 += (u128)(uint64_t)K[v] * (uint64_t)K[v];
+    if (init) {
+        for (int32_t v = 0; v < n; ++v) {
+            Tot[v] = 0;
+            size[v] = 0;
+        }
+        for (int32_t v = 0; v < n; ++v) {
+            prev[v] = cur[v] = init[v];
+            Tot[init[v]] += K[v];
+            size[init[v]] += 1;
+        }
+        sum_in = 0;
+        for (int32_t v = 0; v < n; ++v) {
+            int64_t s = 0;
+            for (int64_t e = offs[v]; e < offs[v + 1]; ++e)
+                if (init[nbr[e]] == init[v]) s += w ? w[e] : 1;
+            In[v] = s;
+            sum_in += s;
+        }
+        for (int32_t c = 0; c < n; ++c) sum_tot2 += (u128)(uint64_t)Tot[c] * (uint64_t)Tot[c];
+    } else {
+        for (int32_t v = 0; v < n; ++v) sum_tot2 += (u128)(uint64_t)K[v] * (uint64_t)K[v];
+    }
     double q = q_of(sum_in, sum_tot2, m2);
     int32_t nq = 0;
     if (iter_q && nq < iter_cap) iter_q[nq] = q;
@@ -295,7 +320,7 @@ int32_t orc_phase1(int32_t n, const int64_t *offs, const int32_t *nbr, const int
     if (n <= 0) return -1;
     int64_t *w64 = promote(w, offs[n]);
     int32_t r = phase1_w64(n, offs, nbr, w64, m2, min_mod, labels_out, q_out, iter_q, iter_cap, n_iter_q,
-                           nthreads);
+                           nthreads, NULL);
     free(w64);
     return r;
 }
@@ -373,11 +398,125 @@ int32_t orc_contract(int32_t n, const int64_t *offs, const int32_t *nbr, const i
     return C;
 }
 
+/* Leiden-style refinement of a level's phase-1 partition P (no counterpart in
+ * the reference; the deterministic synchronous rule the engine implements):
+ * every vertex starts as its own sub-community of its P-community C.  Per
+ * sweep, a singleton v of degree 1..kRefineMaxDeg that is well connected,
+ * w(v, C - v) m2 >= K_v (Tot_C - K_v), picks among the well connected
+ * sub-communities r of C next to it, ext(r) m2 >= K_r (Tot_C - K_r) with ext(r)
+ * the weight from r to the rest of C, the one of largest
+ * X = w(v, r) m2 - K_v K_r (lowest id on ties) and targets it when X > 0.
+ * A vertex moves to its target unless another vertex targets it, except when
+ * exactly one does and that is its own target with a lower id (a mutual pair
+ * joins the lower id).  Sweeps repeat while vertices move, at most
+ * kRefineSweeps times.  R receives the sub-community labels (vertex ids). */
+enum { kRefineMaxDeg = 256, kRefineSweeps = 8 };
+typedef __int128 i128;
+static void refine_w64(int32_t n, const int64_t *offs, const int32_t *nbr, const int64_t *w, int64_t m2,
+                       const int32_t *P, int32_t *R)
+{
+    int64_t *K = (int64_t *)calloc((size_t)n, sizeof(int64_t));
+    int64_t *totC = (int64_t *)calloc((size_t)n, sizeof(int64_t));
+    int64_t *wC = (int64_t *)calloc((size_t)n, sizeof(int64_t));
+    int64_t *ext = (int64_t *)calloc((size_t)n, sizeof(int64_t));
+    int64_t *Kr = (int64_t *)calloc((size_t)n, sizeof(int64_t));
+    int32_t *sz = (int32_t *)calloc((size_t)n, sizeof(int32_t));
+    int32_t *target = (int32_t *)malloc((size_t)n * sizeof(int32_t));
+    int32_t *marks = (int32_t *)calloc((size_t)n, sizeof(int32_t));
+    int64_t *acc = (int64_t *)calloc((size_t)n, sizeof(int64_t));
+    int32_t *touched = (int32_t *)malloc((size_t)n * sizeof(int32_t));
+    for (int32_t v = 0; v < n; ++v) {
+        int64_t k = 0, s = 0;
+        for (int64_t e = offs[v]; e < offs[v + 1]; ++e) {
+            const int64_t wt = w ? w[e] : 1;
+            k += wt;
+            if (nbr[e] != v && P[nbr[e]] == P[v]) s += wt;
+        }
+        K[v] = k;
+        wC[v] = s;
+        R[v] = v;
+    }
+    for (int32_t v = 0; v < n; ++v) totC[P[v]] += K[v];
+    for (int sweep = 0; sweep < kRefineSweeps; ++sweep) {
+        memset(Kr, 0, (size_t)n * sizeof(int64_t));
+        memset(sz, 0, (size_t)n * sizeof(int32_t));
+        memset(ext, 0, (size_t)n * sizeof(int64_t));
+        for (int32_t v = 0; v < n; ++v) {
+            Kr[R[v]] += K[v];
+            sz[R[v]] += 1;
+            for (int64_t e = offs[v]; e < offs[v + 1]; ++e) {
+                const int32_t u = nbr[e];
+                if (u != v && P[u] == P[v] && R[u] != R[v]) ext[R[v]] += w ? w[e] : 1;
+            }
+        }
+        for (int32_t v = 0; v < n; ++v) {
+            target[v] = -1;
+            const int64_t deg = offs[v + 1] - offs[v];
+            if (R[v] != v || sz[v] != 1 || deg < 1 || deg > kRefineMaxDeg) continue;
+            const int32_t p = P[v];
+            if (!((i128)wC[v] * m2 >= (i128)K[v] * (totC[p] - K[v]))) continue;
+            int32_t nt = 0;
+            for (int64_t e = offs[v]; e < offs[v + 1]; ++e) {
+                const int32_t u = nbr[e];
+                if (u == v || P[u] != p || R[u] == v) continue;
+                if (acc[R[u]] == 0) touched[nt++] = R[u];
+                acc[R[u]] += w ? w[e] : 1;
+            }
+            i128 bx = 0;
+            int32_t best = -1;
+            for (int32_t i = 0; i < nt; ++i) {
+                const int32_t r = touched[i];
+                if ((i128)ext[r] * m2 >= (i128)Kr[r] * (totC[p] - Kr[r])) {
+                    const i128 x = (i128)acc[r] * m2 - (i128)K[v] * Kr[r];
+                    if (x > 0 && (best < 0 || x > bx || (x == bx && r < best))) {
+                        bx = x;
+                        best = r;
+                    }
+                }
+                acc[r] = 0;
+            }
+            target[v] = best;
+        }
+        memset(marks, 0, (size_t)n * sizeof(int32_t));
+        for (int32_t v = 0; v < n; ++v)
+            if (target[v] >= 0) marks[target[v]]++;
+        int64_t moved = 0;
+        for (int32_t v = 0; v < n; ++v) {
+            const int32_t t = target[v];
+            if (t < 0) continue;
+            if (marks[v] == 0 || (marks[v] == 1 && target[t] == v && t < v)) {
+                R[v] = t;
+                moved++;
+            }
+        }
+        if (!moved) break;
+    }
+    free(K); free(totC); free(wC); free(ext); free(Kr); free(sz); free(target); free(marks); free(acc); free(touched);
+}
+
+void orc_refine(int32_t n, const int64_t *offs, const int32_t *nbr, const int32_t *w, const int32_t *P,
+                int32_t *R)
+{
+    const int64_t E = offs[n];
+    int64_t *w64 = promote(w, E);
+    int64_t m2 = 0;
+    for (int64_t e = 0; e < E; ++e) m2 += w ? w[e] : 1;
+    refine_w64(n, offs, nbr, w64, m2, P, R);
+    free(w64);
+}
+
 /* Multi-round driver on int64 weights (NULL = all 1). */
+/* refine: a round that gained at least min_mod contracts the refined
+ * partition (see refine_w64), and the next round starts from the phase-1
+ * communities, each labelled by its sub-community of lowest new id.  A round
+ * that started so and gained less contracts its phase-1 communities instead
+ * and the rounds go on (merging whole communities needs the plain
+ * aggregation); a round that started from singletons and gained less is the
+ * last, as without refinement. */
 static int32_t louvain_w64(int32_t n, const int64_t *offs, const int32_t *nbr, const int64_t *w,
                            double min_mod, int32_t max_levels, int32_t *comm_out, double *level_q,
                            int32_t *level_c, int32_t *level_iters, int32_t level_cap, double *iter_q,
-                           int32_t iter_cap, int32_t *n_iter_q, int32_t nthreads)
+                           int32_t iter_cap, int32_t *n_iter_q, int32_t nthreads, int refine)
 {
     if (n <= 0) return -1;
     int64_t E = offs[n];
@@ -393,6 +532,10 @@ static int32_t louvain_w64(int32_t n, const int64_t *offs, const int32_t *nbr, c
     int64_t *nw = (int64_t *)malloc((size_t)(E > 0 ? E : 1) * sizeof(int64_t));
     int32_t *lab = (int32_t *)malloc((size_t)n * sizeof(int32_t));
     int32_t *rl = (int32_t *)malloc((size_t)n * sizeof(int32_t));
+    int32_t *rlab = refine ? (int32_t *)malloc((size_t)n * sizeof(int32_t)) : NULL;
+    int32_t *init = refine ? (int32_t *)malloc((size_t)n * sizeof(int32_t)) : NULL;
+    int32_t *pmin = refine ? (int32_t *)malloc((size_t)n * sizeof(int32_t)) : NULL;
+    int have_init = 0;
     memcpy(go, offs, ((size_t)n + 1) * sizeof(int64_t));
     memcpy(gn, nbr, (size_t)E * sizeof(int32_t));
     for (int64_t e = 0; e < E; ++e) gw[e] = w ? w[e] : 1;
@@ -405,10 +548,25 @@ static int32_t louvain_w64(int32_t n, const int64_t *offs, const int32_t *nbr, c
         int32_t nq = 0;
         double *tr = iter_q ? iter_q + (nq_total < iter_cap ? nq_total : iter_cap) : NULL;
         int32_t cap = iter_q ? (iter_cap > nq_total ? iter_cap - nq_total : 0) : 0;
-        int32_t it = phase1_w64(cn, go, gn, gw, m2, min_mod, lab, &q, tr, cap, &nq, nthreads);
+        int32_t it = phase1_w64(cn, go, gn, gw, m2, min_mod, lab, &q, tr, cap, &nq, nthreads,
+                                have_init ? init : NULL);
         nq_total += nq;
         int64_t ne = 0;
-        int32_t C = contract_w64(cn, go, gn, gw, lab, rl, no, nn, nw, &ne);
+        const int started_refined = have_init;
+        const int gained = q - cur_mod >= min_mod;
+        const int last = (!gained && !started_refined) || (max_levels > 0 && rounds + 1 >= max_levels);
+        int32_t C;
+        if (refine && !last && gained) {
+            refine_w64(cn, go, gn, gw, m2, lab, rlab);
+            C = contract_w64(cn, go, gn, gw, rlab, rl, no, nn, nw, &ne);
+            for (int32_t v = 0; v < cn; ++v) pmin[v] = 0x7fffffff;
+            for (int32_t v = 0; v < cn; ++v)
+                if (rl[v] < pmin[lab[v]]) pmin[lab[v]] = rl[v];
+            for (int32_t v = 0; v < cn; ++v) init[rl[v]] = pmin[lab[v]];
+        } else {
+            C = contract_w64(cn, go, gn, gw, lab, rl, no, nn, nw, &ne);
+        }
+        have_init = refine && !last && gained;
         /* labels of the input vertices follow the contraction (the gather of
          * louvain.cu:188-189, composed in the intended direction) */
         for (int32_t i = 0; i < n; ++i) comm_out[i] = rl[comm_out[i]];
@@ -424,12 +582,14 @@ static int32_t louvain_w64(int32_t n, const int64_t *offs, const int32_t *nbr, c
         int32_t *t32 = gn; gn = nn; nn = t32;
         t64 = gw; gw = nw; nw = t64;
         cn = C;
-        /* round loop condition, louvain.cu:202 */
-        if (!(cur_mod - prev_mod >= min_mod)) break;
+        /* round loop condition, louvain.cu:202 (a refined round that gained
+         * less goes on with a plain contraction) */
+        if (!(cur_mod - prev_mod >= min_mod) && !started_refined) break;
         if (max_levels > 0 && rounds >= max_levels) break;
     }
     if (n_iter_q) *n_iter_q = nq_total;
     free(go); free(gn); free(gw); free(no); free(nn); free(nw); free(lab); free(rl);
+    free(rlab); free(init); free(pmin);
     return rounds;
 }
 
@@ -441,7 +601,20 @@ int32_t orc_louvain(int32_t n, const int64_t *offs, const int32_t *nbr, const in
     if (n <= 0) return -1;
     int64_t *w64 = promote(w, offs[n]);
     int32_t r = louvain_w64(n, offs, nbr, w64, min_mod, max_levels, comm_out, level_q, level_c, level_iters,
-                            level_cap, iter_q, iter_cap, n_iter_q, nthreads);
+                            level_cap, iter_q, iter_cap, n_iter_q, nthreads, 0);
+    free(w64);
+    return r;
+}
+
+int32_t orc_louvain_refine(int32_t n, const int64_t *offs, const int32_t *nbr, const int32_t *w,
+                           double min_mod, int32_t max_levels, int32_t *comm_out, double *level_q,
+                           int32_t *level_c, int32_t *level_iters, int32_t level_cap, double *iter_q,
+                           int32_t iter_cap, int32_t *n_iter_q, int32_t nthreads)
+{
+    if (n <= 0) return -1;
+    int64_t *w64 = promote(w, offs[n]);
+    int32_t r = louvain_w64(n, offs, nbr, w64, min_mod, max_levels, comm_out, level_q, level_c, level_iters,
+                            level_cap, iter_q, iter_cap, n_iter_q, nthreads, 1);
     free(w64);
     return r;
 }
@@ -452,7 +625,7 @@ int32_t orc_louvain_fixed(int32_t n, const int64_t *offs, const int32_t *nbr, co
                           int32_t iter_cap, int32_t *n_iter_q, int32_t nthreads)
 {
     return louvain_w64(n, offs, nbr, w, min_mod, max_levels, comm_out, level_q, level_c, level_iters, level_cap,
-                       iter_q, iter_cap, n_iter_q, nthreads);
+                       iter_q, iter_cap, n_iter_q, nthreads, 0);
 }
 
 double orc_modularity_f32(int32_t n, const int64_t *offs, const int32_t *nbr, const float *w,

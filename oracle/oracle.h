@@ -40,6 +40,14 @@ int32_t orc_contract(int32_t n, const int64_t *offs, const int32_t *nbr, const i
 
 /* Multi-round driver (the loop at louvain.cu:193-226).  comm_out[n] receives
  * the final community of every input vertex.  Returns the number of rounds. */
+/* Leiden-style refinement of a partition P (see louvain_oracle.c) and the
+ * multi-round driver that contracts refined partitions. */
+void orc_refine(int32_t n, const int64_t *offs, const int32_t *nbr, const int32_t *w, const int32_t *P,
+                int32_t *R);
+int32_t orc_louvain_refine(int32_t n, const int64_t *offs, const int32_t *nbr, const int32_t *w,
+                           double min_mod, int32_t max_levels, int32_t *comm_out, double *level_q,
+                           int32_t *level_c, int32_t *level_iters, int32_t level_cap, double *iter_q,
+                           int32_t iter_cap, int32_t *n_iter_q, int32_t nthreads);
 int32_t orc_louvain(int32_t n, const int64_t *offs, const int32_t *nbr, const int32_t *w,
                     double min_mod, int32_t max_levels, int32_t *comm_out, double *level_q,
                     int32_t *level_c, int32_t *level_iters, int32_t level_cap, double *iter_q,

@@ -57,6 +57,10 @@ class Oracle:
         L.orc_louvain.argtypes = [ctypes.c_int32, _i64p, _i32p, _i32p, ctypes.c_double, ctypes.c_int32,
                                   _i32p, _f64p, _i32p, _i32p, ctypes.c_int32, _f64p, ctypes.c_int32, _i32p,
                                   ctypes.c_int32]
+        L.orc_louvain_refine.restype = ctypes.c_int32
+        L.orc_louvain_refine.argtypes = L.orc_louvain.argtypes
+        L.orc_refine.restype = None
+        L.orc_refine.argtypes = [ctypes.c_int32, _i64p, _i32p, _i32p, _i32p, _i32p]
         L.orc_modularity.restype = ctypes.c_double
         L.orc_modularity.argtypes = [ctypes.c_int32, _i64p, _i32p, _i32p, _i32p]
         _f32p = ctypes.POINTER(ctypes.c_float)
@@ -106,7 +110,16 @@ class Oracle:
         e = ne.value
         return {"C": C, "relabel": rl, "offs": no[:C + 1].copy(), "nbr": nn[:e].copy(), "w": nw[:e].copy()}
 
-    def louvain(self, offs, nbr, w=None, min_mod=1e-6, max_levels=0, nthreads=1, iter_cap=65536):
+    def refine(self, offs, nbr, w, P):
+        """Sub-community labels of the refinement of partition P."""
+        offs, nbr, w = self._arrs(offs, nbr, w)
+        P = np.ascontiguousarray(P, dtype=np.int32)
+        R = np.zeros(P.shape[0], dtype=np.int32)
+        self.lib.orc_refine(P.shape[0], _p(offs, _i64p), _p(nbr, _i32p), _p(w, _i32p), _p(P, _i32p),
+                            _p(R, _i32p))
+        return R
+
+    def louvain(self, offs, nbr, w=None, min_mod=1e-6, max_levels=0, nthreads=1, iter_cap=65536, refine=False):
         offs, nbr, w = self._arrs(offs, nbr, w)
         n = offs.shape[0] - 1
         comm = np.zeros(n, dtype=np.int32)
@@ -115,7 +128,8 @@ class Oracle:
         li = np.zeros(64, dtype=np.int32)
         iq = np.zeros(iter_cap, dtype=np.float64)
         nq = ctypes.c_int32()
-        r = self.lib.orc_louvain(n, _p(offs, _i64p), _p(nbr, _i32p), _p(w, _i32p), min_mod, max_levels,
+        fn = self.lib.orc_louvain_refine if refine else self.lib.orc_louvain
+        r = fn(n, _p(offs, _i64p), _p(nbr, _i32p), _p(w, _i32p), min_mod, max_levels,
                                  _p(comm, _i32p), _p(lq, _f64p), _p(lc, _i32p), _p(li, _i32p), 64,
                                  _p(iq, _f64p), iter_cap, ctypes.byref(nq), nthreads)
         return {"rounds": r, "labels": comm, "level_q": lq[:r].tolist(), "level_c": lc[:r].tolist(),
