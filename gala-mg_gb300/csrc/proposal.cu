@@ -748,12 +748,37 @@ gala_status gala_proposal_train(gala_proposal *p, int32_t epochs, int32_t batch_
         return GALA_ERR_INVALID;
     }
     cudaStream_t st = p->stream;
+    // The sweeps append their samples with an atomic cursor, so the row order
+    // of the sample set varies from run to run.  Training walks a canonical
+    // order instead (rows sorted by vertex, features and label; equal rows
+    // are interchangeable), shuffled by the seed: the same samples give the
+    // same network.
+    std::vector<int64_t> base((size_t)n);
+    {
+        std::vector<float> X((size_t)n * kIn), Y((size_t)n);
+        std::vector<int32_t> V((size_t)n);
+        cudaError_t ce = cudaMemcpyAsync(X.data(), p->X, X.size() * sizeof(float), cudaMemcpyDeviceToHost, st);
+        if (ce == cudaSuccess)
+            ce = cudaMemcpyAsync(Y.data(), p->Y, Y.size() * sizeof(float), cudaMemcpyDeviceToHost, st);
+        if (ce == cudaSuccess)
+            ce = cudaMemcpyAsync(V.data(), p->V, V.size() * sizeof(int32_t), cudaMemcpyDeviceToHost, st);
+        if (ce == cudaSuccess) ce = cudaStreamSynchronize(st);
+        if (ce != cudaSuccess) return cuda_fail(ce, "gala_proposal_train: samples");
+        for (int64_t i = 0; i < n; ++i) base[i] = i;
+        std::sort(base.begin(), base.end(), [&](int64_t a, int64_t b) {
+            if (V[a] != V[b]) return V[a] < V[b];
+            const int c = memcmp(&X[(size_t)a * kIn], &X[(size_t)b * kIn], kIn * sizeof(float));
+            if (c != 0) return c < 0;
+            return memcmp(&Y[a], &Y[b], sizeof(float)) < 0;
+        });
+    }
     std::mt19937_64 rng(seed);
-    std::vector<int64_t> perm((size_t)n);
-    for (int64_t i = 0; i < n; ++i) perm[i] = i;
+    std::vector<int64_t> order((size_t)n), perm((size_t)n);
+    for (int64_t i = 0; i < n; ++i) order[i] = i;
     float epoch_loss = 0.f;
     for (int e = 0; e < epochs; ++e) {
-        std::shuffle(perm.begin(), perm.end(), rng);
+        std::shuffle(order.begin(), order.end(), rng);
+        for (int64_t i = 0; i < n; ++i) perm[i] = base[order[i]];
         cudaMemsetAsync(p->loss, 0, sizeof(float), st);
         cudaMemcpyAsync(p->idx, perm.data(), (size_t)n * sizeof(int64_t), cudaMemcpyHostToDevice, st);
         for (int64_t b0 = 0; b0 < n; b0 += batch_size) {
