@@ -62,6 +62,7 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-learned", action="store_true", help="skip the learned-proposal arm")
     p.add_argument("--no-batch", action="store_true", help="skip the batched-graphs arm")
+    p.add_argument("--no-refine", action="store_true", help="skip the Leiden-style refinement arm")
     p.add_argument("--no-weighted", action="store_true", help="skip the float-weight LFR arm")
     p.add_argument("--tune-cache", default=None, help="JSON file caching autotuned degree bins per workload")
     p.add_argument("--threshold", type=float, default=0.3, help="proposal probability threshold")
@@ -248,6 +249,52 @@ def learned_arm(ffi, ctx, g, stream, args, torch, plain_ms, plain):
             "iterations": r["total_iterations"], "plain_iterations": plain["total_iterations"],
             "phase_ms": {"decide": r["time_decide_ms"], "update": r["time_update_ms"],
                          "contract": r["time_contract_ms"]}}
+
+
+REFINE_LFR = {"workload": "lfr-2M-unit", "vertices": 2_000_000, "tau1": 2.5, "dmin": 10, "dmax": 2000, "tau2": 1.5,
+              "cmin": 20, "cmax": 5000, "mu": 0.3, "seed": 3}
+
+
+def refine_arm(ffi, ctx, g, stream, args, torch, plain_ms, plain):
+    """The Leiden-style refinement (gala_options.refine) end to end on the
+    same graph: time and final modularity against the plain rounds."""
+    times, r = [], None
+    for i in range(args.warmup + args.steps):
+        torch.cuda.synchronize()
+        with torch.cuda.stream(stream):
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            r = ctx.louvain(g, refine=True)
+            b.record(stream)
+        torch.cuda.synchronize()
+        if i >= args.warmup:
+            times.append(a.elapsed_time(b))
+    ms = sum(times) / len(times)
+    # a graph with planted communities (LFR-style, unit weights), where the
+    # refinement is meant to help
+    lg = ffi.Graph.lfr(REFINE_LFR["vertices"], REFINE_LFR["tau1"], REFINE_LFR["dmin"], REFINE_LFR["dmax"],
+                       REFINE_LFR["tau2"], REFINE_LFR["cmin"], REFINE_LFR["cmax"], REFINE_LFR["mu"], False,
+                       REFINE_LFR["seed"])
+    lfr = {"config": REFINE_LFR}
+    for key, flag in (("plain", False), ("refine", True)):
+        ts = []
+        for i in range(3):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            rr = ctx.louvain(lg, refine=flag)
+            torch.cuda.synchronize()
+            if i:
+                ts.append((time.perf_counter() - t0) * 1e3)
+        lfr[key] = {"ms": sum(ts) / len(ts), "modularity": rr["modularity"], "rounds": rr["rounds"],
+                    "communities": rr["num_communities"]}
+    lfr["dq_refine_vs_plain"] = lfr["refine"]["modularity"] - lfr["plain"]["modularity"]
+    return {"ms_per_step": ms, "time_vs_plain": ms / plain_ms, "modularity": r["modularity"], "lfr": lfr,
+            "dq_vs_plain": r["modularity"] - plain["modularity"], "modularity_host_fp64": g.modularity(r["labels"]),
+            "rounds": r["rounds"], "plain_rounds": plain["rounds"], "communities": r["num_communities"],
+            "plain_communities": plain["num_communities"], "iterations": r["total_iterations"],
+            "phase_ms": {"decide": r["time_decide_ms"], "update": r["time_update_ms"],
+                         "contract_and_refine": r["time_contract_ms"]}}
 
 
 WEIGHTED = {"workload": "lfr-16M-200M-f32", "generator": "LFR-style", "vertices": 16_000_000, "tau1": 2.5,
@@ -483,6 +530,8 @@ def main():
             "roofline": roof, "clocks": clk, "gpu_launches": launches}
     if not args.no_learned:
         line["learned"] = learned_arm(ffi, ctx, g, stream, args, torch, e2e_step, r_e2e)
+    if not args.no_refine:
+        line["refine"] = refine_arm(ffi, ctx, g, stream, args, torch, e2e_step, r_e2e)
     if not args.no_batch:
         line["batch"] = batch_arm(ffi, args, torch, local)
     if not args.no_weighted:

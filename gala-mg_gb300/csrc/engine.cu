@@ -171,6 +171,7 @@ struct Phase1Out {
     long long skipped = 0;        // active vertices the network let stay
     long long verify_sweeps = 0;  // full plain sweeps run to judge convergence
     long long movers = 0;         // moves applied (kept or dropped)
+    long long nv = 0;             // vertices with edges (the degree-bin order)
     long long active_entries = 0; // row entries decided
 };
 
@@ -392,6 +393,7 @@ gala_status phase1(gala_context *ctx, const LevelGraph &g, long long &m2, double
     k_set_act_counts<<<1, 1, 0, st>>>(b.stats, 0, c8, (int)nv_all, (unsigned long long)g.E);
     note_launch(1);
     long long act_nv = nv_all, act_ne = g.E;
+    out->nv = nv_all;
     int cur = 0;
     const long long min_tot_init = (!g.wide && m2 > 0x7fffffffLL) ? 0x7fffffffLL : m2;
     unsigned long long skipped0 = h->skipped, skipped_e0 = h->skipped_edges;
@@ -753,7 +755,7 @@ gala_status run_levels(gala_context *ctx, int32_t n0, int64_t E0, const int64_t 
         if (!(dalloc(ctx, &rb.R, nc) && dalloc(ctx, &rb.target, nc) && dalloc(ctx, &rb.marks, nc) &&
               dalloc(ctx, &rb.sz, nc) && dalloc(ctx, &rb.wC, nc) && dalloc(ctx, &rb.ext, nc) &&
               dalloc(ctx, &rb.Kr, nc) && dalloc(ctx, &rb.pmin, nc) && dalloc(ctx, &rb.init, nc) &&
-              dalloc(ctx, &rb.moved, 1))) {
+              dalloc(ctx, &rb.list, nc) && dalloc(ctx, &rb.list2, nc) && dalloc(ctx, &rb.moved, 4))) {
             rb = RefineBuffers{};
             set_error("refinement: out of device memory");
             return GALA_ERR_CAPACITY;
@@ -810,7 +812,8 @@ gala_status run_levels(gala_context *ctx, int32_t n0, int64_t E0, const int64_t 
         const int32_t *ccomm = ctx->p1.comm;
         NextLevelInit nli{ctx->p1.Tot, ctx->p1.K, ctx->p1.Self};
         if (do_refine) {
-            if (refine_run(g, ctx->p1.comm, ctx->p1.K, ctx->p1.Tot, m2, ctx->ref, ctx->d_stats, st, &cs) < 0)
+            if (refine_run(g, ctx->p1.comm, ctx->p1.K, ctx->p1.Tot, m2, ctx->p1.order, (int)po.nv, ctx->ref,
+                           ctx->d_stats, st, &cs) < 0)
                 return cs;
             ccomm = ctx->ref.R;
             nli.tot = ctx->ref.Kr;

@@ -233,14 +233,18 @@ struct RefineBuffers {
     int32_t *Kr = nullptr;      // weighted degree of a sub-community
     int32_t *pmin = nullptr;    // per community: its sub-community of lowest new id
     int32_t *init = nullptr;    // starting community of every vertex of the next level
-    int32_t *moved = nullptr;   // 1 int: moves of the sweep
+    int32_t *moved = nullptr;   // 3 ints: moves of the sweep, long rows listed, candidates listed
+    int32_t *list = nullptr;    // vertices with rows longer than 32 entries
+    int32_t *list2 = nullptr;   // the singletons that may move
 };
 // Refines the partition P of level g into R (returns the sweeps run, or -1
 // on a CUDA error with *status set); K and TotC are the level's weighted
 // degrees and community totals.  Afterwards b.Kr holds the sub-community
 // totals (the K of the next level's vertices).
+// order[0, nv): the level's vertices with edges (the degree-bin order).
 int refine_run(const LevelGraph &g, const int32_t *P, const int32_t *K, const int32_t *TotC, long long m2,
-               RefineBuffers &b, DevStats *stats, cudaStream_t st, gala_status *status);
+               const int32_t *order, int nv, RefineBuffers &b, DevStats *stats, cudaStream_t st,
+               gala_status *status);
 // The next level's starting partition: b.init[lab[v]] = the lowest new id of a
 // sub-community in v's community P[v] (lab: the contraction's new id of every
 // level vertex).

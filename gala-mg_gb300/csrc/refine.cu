@@ -29,13 +29,15 @@ constexpr int kRefLog = 9;
 constexpr int kRefWarps = 8;
 
 // Per vertex: R = own id, wC = weight to the rest of its community.
-__global__ void __launch_bounds__(256) k_ref_start(int n, const int64_t *__restrict__ offs,
+__global__ void __launch_bounds__(256) k_ref_start(const int32_t *__restrict__ order, int nv,
+                                                   const int64_t *__restrict__ offs,
                                                    const int32_t *__restrict__ nbr, const int32_t *__restrict__ w,
-                                                   const int32_t *__restrict__ P, int32_t *R, int32_t *wC)
+                                                   const int32_t *__restrict__ P, int32_t *wC)
 {
     const int lane = threadIdx.x & 31;
     const int nw = (gridDim.x * blockDim.x) >> 5;
-    for (int v = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; v < n; v += nw) {
+    for (int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < nv; i += nw) {
+        const int v = order[i];
         const int p = P[v];
         int s = 0;
         for (long long j = offs[v] + lane; j < offs[v + 1]; j += 32) {
@@ -43,23 +45,59 @@ __global__ void __launch_bounds__(256) k_ref_start(int n, const int64_t *__restr
             if (u != v && P[u] == p) s += w ? w[j] : 1;
         }
         s = warp_sum(s);
-        if (lane == 0) {
-            wC[v] = s;
-            R[v] = v;
-        }
+        if (lane == 0) wC[v] = s;
     }
 }
 
+__global__ void k_iota(int32_t *a, int n)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) a[i] = i;
+}
+
 // Per sweep: ext, Kr and sz of every sub-community (zeroed by the caller).
-__global__ void __launch_bounds__(256) k_ref_sums(int n, const int64_t *__restrict__ offs,
+// One thread per vertex; rows longer than 32 entries are listed for the warp
+// kernel below, which adds their ext share.
+__global__ void __launch_bounds__(256) k_ref_sums(const int32_t *__restrict__ order, int n,
+                                                  const int64_t *__restrict__ offs,
                                                   const int32_t *__restrict__ nbr, const int32_t *__restrict__ w,
                                                   const int32_t *__restrict__ P, const int32_t *__restrict__ R,
                                                   const int32_t *__restrict__ K, int32_t *ext, int32_t *Kr,
-                                                  int32_t *sz)
+                                                  int32_t *sz, int32_t *big, int32_t *nbig)
+{
+    const int lane = threadIdx.x & 31;
+    for (int i0 = blockIdx.x * blockDim.x + threadIdx.x - lane; i0 < n; i0 += gridDim.x * blockDim.x) {
+        const int v = i0 + lane < n ? order[i0 + lane] : 0;
+        bool is_big = false;
+        if (i0 + lane < n) {
+            const int p = P[v], r = R[v];
+            const long long s0 = offs[v], e0 = offs[v + 1];
+            is_big = e0 - s0 > 32;
+            if (!is_big) {
+                int s = 0;
+                for (long long j = s0; j < e0; ++j) {
+                    const int u = nbr[j];
+                    if (u != v && P[u] == p && R[u] != r) s += w ? w[j] : 1;
+                }
+                if (s) atomicAdd(&ext[r], s);
+            }
+            atomicAdd(&Kr[r], K[v]);
+            atomicAdd(&sz[r], 1);
+        }
+        warp_append(is_big, v, big, nbig);
+    }
+}
+
+__global__ void __launch_bounds__(256) k_ref_sums_big(const int32_t *__restrict__ big, const int32_t *__restrict__ nbig,
+                                                      const int64_t *__restrict__ offs,
+                                                      const int32_t *__restrict__ nbr, const int32_t *__restrict__ w,
+                                                      const int32_t *__restrict__ P, const int32_t *__restrict__ R,
+                                                      int32_t *ext)
 {
     const int lane = threadIdx.x & 31;
     const int nw = (gridDim.x * blockDim.x) >> 5;
-    for (int v = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; v < n; v += nw) {
+    const int cnt = *nbig;
+    for (int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < cnt; i += nw) {
+        const int v = big[i];
         const int p = P[v], r = R[v];
         int s = 0;
         for (long long j = offs[v] + lane; j < offs[v + 1]; j += 32) {
@@ -67,16 +105,37 @@ __global__ void __launch_bounds__(256) k_ref_sums(int n, const int64_t *__restri
             if (u != v && P[u] == p && R[u] != r) s += w ? w[j] : 1;
         }
         s = warp_sum(s);
-        if (lane == 0) {
-            if (s) atomicAdd(&ext[r], s);
-            atomicAdd(&Kr[r], K[v]);
-            atomicAdd(&sz[r], 1);
+        if (lane == 0 && s) atomicAdd(&ext[r], s);
+    }
+}
+
+// Per sweep: the singletons that may move (listed; every target starts -1).
+__global__ void __launch_bounds__(256) k_ref_cand(const int32_t *__restrict__ order, int n,
+                                                  const int64_t *__restrict__ offs,
+                                                  const int32_t *__restrict__ P, const int32_t *__restrict__ R,
+                                                  const int32_t *__restrict__ K, const int32_t *__restrict__ wC,
+                                                  const int32_t *__restrict__ TotC, const int32_t *__restrict__ sz,
+                                                  long long m2, int32_t *target, int32_t *cand, int32_t *ncand)
+{
+    const int lane = threadIdx.x & 31;
+    for (int i0 = blockIdx.x * blockDim.x + threadIdx.x - lane; i0 < n; i0 += gridDim.x * blockDim.x) {
+        const int v = i0 + lane < n ? order[i0 + lane] : 0;
+        bool ok = false;
+        if (i0 + lane < n) {
+            target[v] = -1;
+            const long long deg = offs[v + 1] - offs[v];
+            if (R[v] == v && sz[v] == 1 && deg >= 1 && deg <= kRefineMaxDeg) {
+                const long long kv = K[v], tc = TotC[P[v]];
+                ok = (long long)wC[v] * m2 >= kv * (tc - kv);
+            }
         }
+        warp_append(ok, v, cand, ncand);
     }
 }
 
 // Per sweep: the target of every singleton (or -1).
-__global__ void __launch_bounds__(256) k_ref_decide(int n, const int64_t *__restrict__ offs,
+__global__ void __launch_bounds__(256) k_ref_decide(const int32_t *__restrict__ cand, const int32_t *__restrict__ ncand,
+                                                    const int64_t *__restrict__ offs,
                                                     const int32_t *__restrict__ nbr, const int32_t *__restrict__ w,
                                                     const int32_t *__restrict__ P, const int32_t *__restrict__ R,
                                                     const int32_t *__restrict__ K, const int32_t *__restrict__ wC,
@@ -96,17 +155,13 @@ __global__ void __launch_bounds__(256) k_ref_decide(int n, const int64_t *__rest
     }
     __syncwarp();
     const int nw = (gridDim.x * blockDim.x) >> 5;
-    for (int v = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; v < n; v += nw) {
+    const int cnt = *ncand;
+    for (int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < cnt; i += nw) {
+        const int v = cand[i];
         const long long s = offs[v];
         const int deg = (int)(offs[v + 1] - s);
         const int p = P[v];
         const long long kv = K[v], tc = TotC[p];
-        const bool movable = R[v] == v && sz[v] == 1 && deg >= 1 && deg <= kRefineMaxDeg &&
-                             (long long)wC[v] * m2 >= kv * (tc - kv);
-        if (!movable) {  // warp-uniform
-            if (lane == 0) target[v] = -1;
-            continue;
-        }
         int nocc = 0;
         for (int e0 = 0; e0 < deg; e0 += 32) {
             const int e = e0 + lane;
@@ -175,19 +230,24 @@ __global__ void __launch_bounds__(256) k_ref_decide(int n, const int64_t *__rest
     }
 }
 
-__global__ void k_ref_mark(int n, const int32_t *__restrict__ target, int32_t *marks)
+__global__ void k_ref_mark(const int32_t *__restrict__ cand, const int32_t *__restrict__ ncand,
+                           const int32_t *__restrict__ target, int32_t *marks)
 {
-    for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) {
-        const int t = target[v];
+    const int n = *ncand;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const int t = target[cand[i]];
         if (t >= 0) atomicAdd(&marks[t], 1);
     }
 }
 
-__global__ void k_ref_move(int n, const int32_t *__restrict__ target, const int32_t *__restrict__ marks,
-                           int32_t *R, int32_t *moved)
+__global__ void k_ref_move(const int32_t *__restrict__ cand, const int32_t *__restrict__ ncand,
+                           const int32_t *__restrict__ target, const int32_t *__restrict__ marks, int32_t *R,
+                           int32_t *moved)
 {
     int cnt = 0;
-    for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) {
+    const int n = *ncand;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const int v = cand[i];
         const int t = target[v];
         if (t < 0) continue;
         const int m = marks[v];
@@ -228,27 +288,35 @@ int grid_for(long long items, int per_block)
 }  // namespace
 
 int refine_run(const LevelGraph &g, const int32_t *P, const int32_t *K, const int32_t *TotC, long long m2,
-               RefineBuffers &b, DevStats *stats, cudaStream_t st, gala_status *status)
+               const int32_t *order, int nv, RefineBuffers &b, DevStats *stats, cudaStream_t st,
+               gala_status *status)
 {
+    // vertices without edges stay singletons: the passes walk the level's
+    // degree-bin order (every vertex with an edge), not all n ids
     const int n = g.n;
     const int32_t *w = (const int32_t *)g.w;
-    const int gw = grid_for((long long)n * 32, 256);  // one warp per vertex
-    const int gt = grid_for(n, 256);
-    k_ref_start<<<gw, 256, 0, st>>>(n, g.offs, g.nbr, w, P, b.R, b.wC);
-    note_launch(1);
+    const int gw = grid_for((long long)nv * 32, 256);  // one warp per vertex
+    const int gt = grid_for(nv, 256);
+    k_iota<<<grid_for(n, 256), 256, 0, st>>>(b.R, n);
+    k_ref_start<<<gw, 256, 0, st>>>(order, nv, g.offs, g.nbr, w, P, b.wC);
+    note_launch(2);
     int sweeps = 0;
     for (; sweeps < kRefineSweeps; ++sweeps) {
         cudaMemsetAsync(b.ext, 0, (size_t)n * sizeof(int32_t), st);
         cudaMemsetAsync(b.Kr, 0, (size_t)n * sizeof(int32_t), st);
         cudaMemsetAsync(b.sz, 0, (size_t)n * sizeof(int32_t), st);
         cudaMemsetAsync(b.marks, 0, (size_t)n * sizeof(int32_t), st);
-        cudaMemsetAsync(b.moved, 0, sizeof(int32_t), st);
-        k_ref_sums<<<gw, 256, 0, st>>>(n, g.offs, g.nbr, w, P, b.R, K, b.ext, b.Kr, b.sz);
-        k_ref_decide<<<gw, 256, 0, st>>>(n, g.offs, g.nbr, w, P, b.R, K, b.wC, TotC, b.ext, b.Kr, b.sz, m2, b.target,
-                                         stats);
-        k_ref_mark<<<gt, 256, 0, st>>>(n, b.target, b.marks);
-        k_ref_move<<<gt, 256, 0, st>>>(n, b.target, b.marks, b.R, b.moved);
-        note_launch(4);
+        cudaMemsetAsync(b.moved, 0, 3 * sizeof(int32_t), st);
+        k_ref_sums<<<gt, 256, 0, st>>>(order, nv, g.offs, g.nbr, w, P, b.R, K, b.ext, b.Kr, b.sz, b.list,
+                                       b.moved + 1);
+        k_ref_sums_big<<<gw, 256, 0, st>>>(b.list, b.moved + 1, g.offs, g.nbr, w, P, b.R, b.ext);
+        k_ref_cand<<<gt, 256, 0, st>>>(order, nv, g.offs, P, b.R, K, b.wC, TotC, b.sz, m2, b.target, b.list2,
+                                       b.moved + 2);
+        k_ref_decide<<<gw, 256, 0, st>>>(b.list2, b.moved + 2, g.offs, g.nbr, w, P, b.R, K, b.wC, TotC, b.ext, b.Kr,
+                                         b.sz, m2, b.target, stats);
+        k_ref_mark<<<gt, 256, 0, st>>>(b.list2, b.moved + 2, b.target, b.marks);
+        k_ref_move<<<gt, 256, 0, st>>>(b.list2, b.moved + 2, b.target, b.marks, b.R, b.moved);
+        note_launch(6);
         int moved = 0, err = 0;
         cudaError_t ce = cudaGetLastError();
         if (ce == cudaSuccess) ce = cudaMemcpyAsync(&moved, b.moved, sizeof(int), cudaMemcpyDeviceToHost, st);
@@ -269,7 +337,9 @@ int refine_run(const LevelGraph &g, const int32_t *P, const int32_t *K, const in
     cudaMemsetAsync(b.ext, 0, (size_t)n * sizeof(int32_t), st);
     cudaMemsetAsync(b.Kr, 0, (size_t)n * sizeof(int32_t), st);
     cudaMemsetAsync(b.sz, 0, (size_t)n * sizeof(int32_t), st);
-    k_ref_sums<<<gw, 256, 0, st>>>(n, g.offs, g.nbr, w, P, b.R, K, b.ext, b.Kr, b.sz);
+    cudaMemsetAsync(b.moved + 1, 0, sizeof(int32_t), st);
+    k_ref_sums<<<gt, 256, 0, st>>>(order, nv, g.offs, g.nbr, w, P, b.R, K, b.ext, b.Kr, b.sz, b.list,
+                                   b.moved + 1);
     note_launch(1);
     return sweeps;
 }
