@@ -5,7 +5,7 @@
 // Extra options: -o <file> writes the final community of every vertex (one
 // int32 per vertex, binary), -t <threshold> (default 1e-6), -l <max rounds>,
 // -d <device>, -s <dir> writes every round's contracted graph and labels
-// (checkpoints to resume from).
+// (checkpoints to resume from), -r turns on the Leiden-style refinement.
 #include <stdio.h>
 #include <stdlib.h>
 #include <sys/time.h>
@@ -28,7 +28,7 @@ int main(int argc, char **argv)
     int weighted = 0, device = 0, opt;
     gala_options o;
     gala_default_options(&o);
-    while ((opt = getopt(argc, argv, "f:wo:t:l:d:s:")) != -1) {
+    while ((opt = getopt(argc, argv, "f:wo:t:l:d:s:r")) != -1) {
         switch (opt) {
         case 'f': file = optarg; break;
         case 'w': weighted = 1; break;
@@ -37,10 +37,11 @@ int main(int argc, char **argv)
         case 'l': o.max_levels = atoi(optarg); break;
         case 'd': device = atoi(optarg); break;
         case 's': o.level_dir = optarg; break;
+        case 'r': o.refine = 1; break;
         default:
             fprintf(stderr,
                     "Usage: %s -f <graph.bin> [-w] [-o labels.bin] [-t threshold] [-l rounds] [-d device] "
-                    "[-s level_dir]\n",
+                    "[-s level_dir] [-r]\n",
                     argv[0]);
             return 1;
         }
