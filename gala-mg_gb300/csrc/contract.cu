@@ -629,7 +629,7 @@ __global__ void k_big_plan(AggArgs<WT> a, BigArgs b)
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < cnt; i += gridDim.x * blockDim.x) {
         const long long E = a.ec[b.list[i]];
         const long long cap = E < a.C ? E : a.C;
-        long long T = next_pow2_ll(2LL * cap);
+        long long T = next_pow2_ll(cap + cap / 2);  // load at most 2/3
         int dense = T >= a.C;
         if (dense) T = a.C;
         b.T[i] = T;
