@@ -94,3 +94,25 @@ def test_gpu_refine_rejected_for_float_weights(ffi, torch_cuda):
     with pytest.raises(RuntimeError, match="refinement"):
         ctx.louvain(gf, refine=True)
     ctx.close()
+
+
+@pytest.mark.gpu
+def test_gpu_refine_single_round_equals_plain(ffi, torch_cuda):
+    # one round: the round is the last, so nothing is refined
+    g = ffi.Graph.sbm(2048, 32, 0.2, 0.01, 4)
+    n, e, _ = g.info()
+    ctx = ffi.Context(n, e)
+    a = ctx.louvain(g, max_levels=1)
+    b = ctx.louvain(g, max_levels=1, refine=True)
+    ctx.close()
+    assert np.array_equal(a["labels"], b["labels"]) and a["iter_q"] == b["iter_q"]
+
+
+@pytest.mark.gpu
+def test_gpu_refine_rejected_with_checkpoints(ffi, torch_cuda, tmp_path):
+    g = ffi.Graph.sbm(512, 16, 0.3, 0.01, 5)
+    n, e, _ = g.info()
+    ctx = ffi.Context(n, e)
+    with pytest.raises(RuntimeError, match="refinement"):
+        ctx.louvain(g, refine=True, level_dir=str(tmp_path))
+    ctx.close()
