@@ -745,21 +745,25 @@ gala_status run_levels(gala_context *ctx, int32_t n0, int64_t E0, const int64_t 
         return GALA_ERR_INVALID;
     }
     const bool refine = opt && opt->refine == 1;
-    if (refine && (bt || wide || pr.mode != GALA_PROPOSAL_OFF || level_dir)) {
-        set_error("refinement is available for single integer-weight graphs without proposals or checkpoints");
+    if (refine && (bt || pr.mode != GALA_PROPOSAL_OFF || level_dir)) {
+        set_error("refinement is available for single graphs without proposals or checkpoints");
         return GALA_ERR_INVALID;
     }
     if (refine && !ctx->ref.R) {
         RefineBuffers &rb = ctx->ref;
         const size_t nc = (size_t)ctx->n_cap + 1;
+        long long *wC = nullptr, *ext = nullptr, *Kr = nullptr;  // 8 bytes a vertex: either weight width
         if (!(dalloc(ctx, &rb.R, nc) && dalloc(ctx, &rb.target, nc) && dalloc(ctx, &rb.marks, nc) &&
-              dalloc(ctx, &rb.sz, nc) && dalloc(ctx, &rb.wC, nc) && dalloc(ctx, &rb.ext, nc) &&
-              dalloc(ctx, &rb.Kr, nc) && dalloc(ctx, &rb.pmin, nc) && dalloc(ctx, &rb.init, nc) &&
-              dalloc(ctx, &rb.list, nc) && dalloc(ctx, &rb.list2, nc) && dalloc(ctx, &rb.moved, 4))) {
+              dalloc(ctx, &rb.sz, nc) && dalloc(ctx, &wC, nc) && dalloc(ctx, &ext, nc) && dalloc(ctx, &Kr, nc) &&
+              dalloc(ctx, &rb.pmin, nc) && dalloc(ctx, &rb.init, nc) && dalloc(ctx, &rb.list, nc) &&
+              dalloc(ctx, &rb.list2, nc) && dalloc(ctx, &rb.moved, 4))) {
             rb = RefineBuffers{};
             set_error("refinement: out of device memory");
             return GALA_ERR_CAPACITY;
         }
+        rb.wC = wC;
+        rb.ext = ext;
+        rb.Kr = Kr;
     }
     bool have_init = false;  // this round starts from the previous round's communities
     LevelGraph g{n0, E0, offs0, nbr0, w0, wide, distinct0 || (opt && opt->distinct_rows == 1)};

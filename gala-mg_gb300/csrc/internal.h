@@ -228,9 +228,10 @@ struct RefineBuffers {
     int32_t *target = nullptr;  // the sub-community a singleton joins this sweep, or -1
     int32_t *marks = nullptr;   // vertices that target a vertex's sub-community
     int32_t *sz = nullptr;      // members per sub-community
-    int32_t *wC = nullptr;      // weight from a vertex to the rest of its community
-    int32_t *ext = nullptr;     // weight from a sub-community to the rest of its community
-    int32_t *Kr = nullptr;      // weighted degree of a sub-community
+    // weights (WT per vertex: int32, or int64 for fixed-point float weights)
+    void *wC = nullptr;         // weight from a vertex to the rest of its community
+    void *ext = nullptr;        // weight from a sub-community to the rest of its community
+    void *Kr = nullptr;         // weighted degree of a sub-community
     int32_t *pmin = nullptr;    // per community: its sub-community of lowest new id
     int32_t *init = nullptr;    // starting community of every vertex of the next level
     int32_t *moved = nullptr;   // 3 ints: moves of the sweep, long rows listed, candidates listed
@@ -239,18 +240,18 @@ struct RefineBuffers {
 };
 // Refines the partition P of level g into R (returns the sweeps run, or -1
 // on a CUDA error with *status set); K and TotC are the level's weighted
-// degrees and community totals.  Afterwards b.Kr holds the sub-community
-// totals (the K of the next level's vertices).
+// degrees and community totals (WT per vertex, as g.wide says).  Afterwards
+// b.Kr holds the sub-community totals (the K of the next level's vertices).
 // order[0, nv): the level's vertices with edges (the degree-bin order).
-int refine_run(const LevelGraph &g, const int32_t *P, const int32_t *K, const int32_t *TotC, long long m2,
+int refine_run(const LevelGraph &g, const int32_t *P, const void *K, const void *TotC, long long m2,
                const int32_t *order, int nv, RefineBuffers &b, DevStats *stats, cudaStream_t st,
                gala_status *status);
 // The next level's starting partition: b.init[lab[v]] = the lowest new id of a
 // sub-community in v's community P[v] (lab: the contraction's new id of every
 // level vertex).
 void refine_next_init(const int32_t *P, const int32_t *lab, int n, RefineBuffers &b, cudaStream_t st);
-// Level start from a given partition (integer weights): comm = init, Tot and
-// size of its communities from K.
+// Level start from a given partition: comm = init, Tot and size of its
+// communities from K (32- or 64-bit weights, as b.wide says).
 void p1_start_partition(Phase1Buffers &b, const int32_t *init, int n, cudaStream_t st);
 
 // labels_only: the new labels (renumbering and orig_map composition) and the

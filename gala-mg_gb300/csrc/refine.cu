@@ -12,9 +12,11 @@
 //   when exactly one does and that is its own target with a lower id;
 //   sweeps repeat while vertices move, at most kRefineSweeps times.
 //
-// Integer weights only: every sum is below m2 < 2^31 and every product below
-// 2^62, so int64 arithmetic is exact.  One warp per vertex; the candidate
-// sub-communities of a vertex are summed in a per-warp shared-memory table.
+// Integer weights (WT = int): every sum is below m2 < 2^31 and every product
+// below 2^62, exact in int64.  Fixed-point float weights (WT = long long):
+// sums below 2^62, products in 128 bits.  Passes walk the level's vertices
+// with edges (the degree-bin order); candidates are decided one warp each,
+// their candidate sub-communities summed in a per-warp shared-memory table.
 #include "common.cuh"
 #include "internal.h"
 
@@ -26,23 +28,55 @@ constexpr int kRefineMaxDeg = 256;  // rows longer than this stay singletons
 constexpr int kRefineSweeps = 8;
 constexpr int kRefTable = 512;      // per-warp slots (>= 2 x kRefineMaxDeg)
 constexpr int kRefLog = 9;
-constexpr int kRefWarps = 8;
 
-// Per vertex: R = own id, wC = weight to the rest of its community.
+// Exact products of the refinement's conditions and gains.
+template <typename WT>
+struct RefMath {
+    using X = long long;
+    static __device__ __forceinline__ X mul(long long a, long long b) { return a * b; }
+    static __device__ __forceinline__ X shfl_xor(X v, int o) { return __shfl_xor_sync(GALA_FULL_MASK, v, o); }
+};
+template <>
+struct RefMath<long long> {
+    using X = __int128;
+    static __device__ __forceinline__ X mul(long long a, long long b) { return (__int128)a * b; }
+    static __device__ __forceinline__ X shfl_xor(X v, int o)
+    {
+        const unsigned long long lo = __shfl_xor_sync(GALA_FULL_MASK, (unsigned long long)v, o);
+        const long long hi = __shfl_xor_sync(GALA_FULL_MASK, (long long)(v >> 64), o);
+        return ((__int128)hi << 64) | (__int128)lo;
+    }
+};
+// warps per decide block: the per-warp tables stay within 48 KB of static
+// shared memory (10 bytes per slot for int weights, 14 for 64-bit ones)
+template <typename WT>
+__host__ __device__ constexpr int ref_warps()
+{
+    return sizeof(WT) == 4 ? 8 : 4;
+}
+
+template <typename WT>
+__device__ __forceinline__ WT wt_of(const WT *w, long long j)
+{
+    return w ? w[j] : (WT)1;
+}
+
+// Per vertex with edges: wC = weight to the rest of its community.
+template <typename WT>
 __global__ void __launch_bounds__(256) k_ref_start(const int32_t *__restrict__ order, int nv,
                                                    const int64_t *__restrict__ offs,
-                                                   const int32_t *__restrict__ nbr, const int32_t *__restrict__ w,
-                                                   const int32_t *__restrict__ P, int32_t *wC)
+                                                   const int32_t *__restrict__ nbr, const WT *__restrict__ w,
+                                                   const int32_t *__restrict__ P, WT *wC)
 {
     const int lane = threadIdx.x & 31;
     const int nw = (gridDim.x * blockDim.x) >> 5;
     for (int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < nv; i += nw) {
         const int v = order[i];
         const int p = P[v];
-        int s = 0;
+        WT s = 0;
         for (long long j = offs[v] + lane; j < offs[v + 1]; j += 32) {
             const int u = nbr[j];
-            if (u != v && P[u] == p) s += w ? w[j] : 1;
+            if (u != v && P[u] == p) s += wt_of(w, j);
         }
         s = warp_sum(s);
         if (lane == 0) wC[v] = s;
@@ -57,12 +91,13 @@ __global__ void k_iota(int32_t *a, int n)
 // Per sweep: ext, Kr and sz of every sub-community (zeroed by the caller).
 // One thread per vertex; rows longer than 32 entries are listed for the warp
 // kernel below, which adds their ext share.
+template <typename WT>
 __global__ void __launch_bounds__(256) k_ref_sums(const int32_t *__restrict__ order, int n,
                                                   const int64_t *__restrict__ offs,
-                                                  const int32_t *__restrict__ nbr, const int32_t *__restrict__ w,
+                                                  const int32_t *__restrict__ nbr, const WT *__restrict__ w,
                                                   const int32_t *__restrict__ P, const int32_t *__restrict__ R,
-                                                  const int32_t *__restrict__ K, int32_t *ext, int32_t *Kr,
-                                                  int32_t *sz, int32_t *big, int32_t *nbig)
+                                                  const WT *__restrict__ K, WT *ext, WT *Kr, int32_t *sz,
+                                                  int32_t *big, int32_t *nbig)
 {
     const int lane = threadIdx.x & 31;
     for (int i0 = blockIdx.x * blockDim.x + threadIdx.x - lane; i0 < n; i0 += gridDim.x * blockDim.x) {
@@ -73,25 +108,26 @@ __global__ void __launch_bounds__(256) k_ref_sums(const int32_t *__restrict__ or
             const long long s0 = offs[v], e0 = offs[v + 1];
             is_big = e0 - s0 > 32;
             if (!is_big) {
-                int s = 0;
+                WT s = 0;
                 for (long long j = s0; j < e0; ++j) {
                     const int u = nbr[j];
-                    if (u != v && P[u] == p && R[u] != r) s += w ? w[j] : 1;
+                    if (u != v && P[u] == p && R[u] != r) s += wt_of(w, j);
                 }
-                if (s) atomicAdd(&ext[r], s);
+                if (s) atomic_add_w(&ext[r], s);
             }
-            atomicAdd(&Kr[r], K[v]);
+            atomic_add_w(&Kr[r], K[v]);
             atomicAdd(&sz[r], 1);
         }
         warp_append(is_big, v, big, nbig);
     }
 }
 
+template <typename WT>
 __global__ void __launch_bounds__(256) k_ref_sums_big(const int32_t *__restrict__ big, const int32_t *__restrict__ nbig,
                                                       const int64_t *__restrict__ offs,
-                                                      const int32_t *__restrict__ nbr, const int32_t *__restrict__ w,
+                                                      const int32_t *__restrict__ nbr, const WT *__restrict__ w,
                                                       const int32_t *__restrict__ P, const int32_t *__restrict__ R,
-                                                      int32_t *ext)
+                                                      WT *ext)
 {
     const int lane = threadIdx.x & 31;
     const int nw = (gridDim.x * blockDim.x) >> 5;
@@ -99,24 +135,26 @@ __global__ void __launch_bounds__(256) k_ref_sums_big(const int32_t *__restrict_
     for (int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < cnt; i += nw) {
         const int v = big[i];
         const int p = P[v], r = R[v];
-        int s = 0;
+        WT s = 0;
         for (long long j = offs[v] + lane; j < offs[v + 1]; j += 32) {
             const int u = nbr[j];
-            if (u != v && P[u] == p && R[u] != r) s += w ? w[j] : 1;
+            if (u != v && P[u] == p && R[u] != r) s += wt_of(w, j);
         }
         s = warp_sum(s);
-        if (lane == 0 && s) atomicAdd(&ext[r], s);
+        if (lane == 0 && s) atomic_add_w(&ext[r], s);
     }
 }
 
 // Per sweep: the singletons that may move (listed; every target starts -1).
+template <typename WT>
 __global__ void __launch_bounds__(256) k_ref_cand(const int32_t *__restrict__ order, int n,
                                                   const int64_t *__restrict__ offs,
                                                   const int32_t *__restrict__ P, const int32_t *__restrict__ R,
-                                                  const int32_t *__restrict__ K, const int32_t *__restrict__ wC,
-                                                  const int32_t *__restrict__ TotC, const int32_t *__restrict__ sz,
+                                                  const WT *__restrict__ K, const WT *__restrict__ wC,
+                                                  const WT *__restrict__ TotC, const int32_t *__restrict__ sz,
                                                   long long m2, int32_t *target, int32_t *cand, int32_t *ncand)
 {
+    using M = RefMath<WT>;
     const int lane = threadIdx.x & 31;
     for (int i0 = blockIdx.x * blockDim.x + threadIdx.x - lane; i0 < n; i0 += gridDim.x * blockDim.x) {
         const int v = i0 + lane < n ? order[i0 + lane] : 0;
@@ -126,28 +164,31 @@ __global__ void __launch_bounds__(256) k_ref_cand(const int32_t *__restrict__ or
             const long long deg = offs[v + 1] - offs[v];
             if (R[v] == v && sz[v] == 1 && deg >= 1 && deg <= kRefineMaxDeg) {
                 const long long kv = K[v], tc = TotC[P[v]];
-                ok = (long long)wC[v] * m2 >= kv * (tc - kv);
+                ok = M::mul(wC[v], m2) >= M::mul(kv, tc - kv);
             }
         }
         warp_append(ok, v, cand, ncand);
     }
 }
 
-// Per sweep: the target of every singleton (or -1).
-__global__ void __launch_bounds__(256) k_ref_decide(const int32_t *__restrict__ cand, const int32_t *__restrict__ ncand,
-                                                    const int64_t *__restrict__ offs,
-                                                    const int32_t *__restrict__ nbr, const int32_t *__restrict__ w,
-                                                    const int32_t *__restrict__ P, const int32_t *__restrict__ R,
-                                                    const int32_t *__restrict__ K, const int32_t *__restrict__ wC,
-                                                    const int32_t *__restrict__ TotC, const int32_t *__restrict__ ext,
-                                                    const int32_t *__restrict__ Kr, const int32_t *__restrict__ sz,
-                                                    long long m2, int32_t *target, DevStats *st)
+// Per sweep: the target of every listed candidate (or -1).
+template <typename WT>
+__global__ void __launch_bounds__(32 * ref_warps<WT>())
+    k_ref_decide(const int32_t *__restrict__ cand, const int32_t *__restrict__ ncand,
+                 const int64_t *__restrict__ offs, const int32_t *__restrict__ nbr, const WT *__restrict__ w,
+                 const int32_t *__restrict__ P, const int32_t *__restrict__ R, const WT *__restrict__ K,
+                 const WT *__restrict__ TotC, const WT *__restrict__ ext, const WT *__restrict__ Kr, long long m2,
+                 int32_t *target, DevStats *st)
 {
-    __shared__ int s_keys[kRefWarps][kRefTable];
-    __shared__ int s_vals[kRefWarps][kRefTable];
-    __shared__ unsigned short s_occ[kRefWarps][kRefTable];
+    using M = RefMath<WT>;
+    using X = typename M::X;
+    constexpr int NW = ref_warps<WT>();
+    __shared__ int s_keys[NW][kRefTable];
+    __shared__ WT s_vals[NW][kRefTable];
+    __shared__ unsigned short s_occ[NW][kRefTable];
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-    int *keys = s_keys[wib], *vals = s_vals[wib];
+    int *keys = s_keys[wib];
+    WT *vals = s_vals[wib];
     unsigned short *occ = s_occ[wib];
     for (int j = lane; j < kRefTable; j += 32) {
         keys[j] = -1;
@@ -165,12 +206,13 @@ __global__ void __launch_bounds__(256) k_ref_decide(const int32_t *__restrict__ 
         int nocc = 0;
         for (int e0 = 0; e0 < deg; e0 += 32) {
             const int e = e0 + lane;
-            int r = -1, wt = 0;
+            int r = -1;
+            WT wt = 0;
             if (e < deg) {
                 const int u = nbr[s + e];
                 if (u != v && P[u] == p) {
                     r = R[u];
-                    wt = w ? w[s + e] : 1;
+                    wt = wt_of(w, s + e);
                     if (r == v) r = -1;
                 }
             }
@@ -182,7 +224,7 @@ __global__ void __launch_bounds__(256) k_ref_decide(const int32_t *__restrict__ 
                     const int k = atomicCAS(&keys[h], -1, r);
                     if (k == -1 || k == r) {
                         created = k == -1;
-                        atomicAdd(&vals[h], wt);
+                        atomic_add_w(&vals[h], wt);
                         slot = (int)h;
                         break;
                     }
@@ -196,14 +238,14 @@ __global__ void __launch_bounds__(256) k_ref_decide(const int32_t *__restrict__ 
         }
         __syncwarp();
         // best well-connected candidate: largest X > 0, lowest id on ties
-        long long bx = 0;
+        X bx = 0;
         int best = -1;
         for (int q = lane; q < nocc; q += 32) {
             const int j = occ[q];
             const int r = keys[j];
             const long long kr = Kr[r];
-            if ((long long)ext[r] * m2 >= kr * (tc - kr)) {
-                const long long x = (long long)vals[j] * m2 - kv * kr;
+            if (M::mul(ext[r], m2) >= M::mul(kr, tc - kr)) {
+                const X x = M::mul(vals[j], m2) - M::mul(kv, kr);
                 if (x > 0 && (best < 0 || x > bx || (x == bx && r < best))) {
                     bx = x;
                     best = r;
@@ -212,7 +254,7 @@ __global__ void __launch_bounds__(256) k_ref_decide(const int32_t *__restrict__ 
         }
 #pragma unroll
         for (int o = 16; o >= 1; o >>= 1) {
-            const long long ox = __shfl_xor_sync(GALA_FULL_MASK, bx, o);
+            const X ox = M::shfl_xor(bx, o);
             const int ob = __shfl_xor_sync(GALA_FULL_MASK, best, o);
             if (ob >= 0 && (best < 0 || ox > bx || (ox == bx && ob < best))) {
                 bx = ox;
@@ -278,6 +320,18 @@ __global__ void k_fill(int32_t *a, int n, int32_t value)
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) a[i] = value;
 }
 
+template <typename WT>
+__global__ void k_start_partition(int n, const int32_t *__restrict__ init, const WT *__restrict__ K, int32_t *comm,
+                                  WT *Tot, int32_t *size)
+{
+    for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) {
+        const int c = init[v];
+        comm[v] = c;
+        atomic_add_w(&Tot[c], K[v]);
+        atomicAdd(&size[c], 1);
+    }
+}
+
 int grid_for(long long items, int per_block)
 {
     const long long cap = (long long)hub_grid_size() * 8;
@@ -285,35 +339,34 @@ int grid_for(long long items, int per_block)
     return (int)(g < 1 ? 1 : (g > cap ? cap : g));
 }
 
-}  // namespace
-
-int refine_run(const LevelGraph &g, const int32_t *P, const int32_t *K, const int32_t *TotC, long long m2,
-               const int32_t *order, int nv, RefineBuffers &b, DevStats *stats, cudaStream_t st,
-               gala_status *status)
+template <typename WT>
+int refine_t(const LevelGraph &g, const int32_t *P, const WT *K, const WT *TotC, long long m2, const int32_t *order,
+             int nv, RefineBuffers &b, DevStats *stats, cudaStream_t st, gala_status *status)
 {
-    // vertices without edges stay singletons: the passes walk the level's
-    // degree-bin order (every vertex with an edge), not all n ids
     const int n = g.n;
-    const int32_t *w = (const int32_t *)g.w;
+    const WT *w = (const WT *)g.w;
+    WT *wC = (WT *)b.wC, *ext = (WT *)b.ext, *Kr = (WT *)b.Kr;
+    constexpr int kDecideBlock = 32 * ref_warps<WT>();
     const int gw = grid_for((long long)nv * 32, 256);  // one warp per vertex
+    const int gd = grid_for((long long)nv * 32, kDecideBlock);
     const int gt = grid_for(nv, 256);
     k_iota<<<grid_for(n, 256), 256, 0, st>>>(b.R, n);
-    k_ref_start<<<gw, 256, 0, st>>>(order, nv, g.offs, g.nbr, w, P, b.wC);
+    k_ref_start<WT><<<gw, 256, 0, st>>>(order, nv, g.offs, g.nbr, w, P, wC);
     note_launch(2);
     int sweeps = 0;
     for (; sweeps < kRefineSweeps; ++sweeps) {
-        cudaMemsetAsync(b.ext, 0, (size_t)n * sizeof(int32_t), st);
-        cudaMemsetAsync(b.Kr, 0, (size_t)n * sizeof(int32_t), st);
+        cudaMemsetAsync(ext, 0, (size_t)n * sizeof(WT), st);
+        cudaMemsetAsync(Kr, 0, (size_t)n * sizeof(WT), st);
         cudaMemsetAsync(b.sz, 0, (size_t)n * sizeof(int32_t), st);
         cudaMemsetAsync(b.marks, 0, (size_t)n * sizeof(int32_t), st);
         cudaMemsetAsync(b.moved, 0, 3 * sizeof(int32_t), st);
-        k_ref_sums<<<gt, 256, 0, st>>>(order, nv, g.offs, g.nbr, w, P, b.R, K, b.ext, b.Kr, b.sz, b.list,
-                                       b.moved + 1);
-        k_ref_sums_big<<<gw, 256, 0, st>>>(b.list, b.moved + 1, g.offs, g.nbr, w, P, b.R, b.ext);
-        k_ref_cand<<<gt, 256, 0, st>>>(order, nv, g.offs, P, b.R, K, b.wC, TotC, b.sz, m2, b.target, b.list2,
-                                       b.moved + 2);
-        k_ref_decide<<<gw, 256, 0, st>>>(b.list2, b.moved + 2, g.offs, g.nbr, w, P, b.R, K, b.wC, TotC, b.ext, b.Kr,
-                                         b.sz, m2, b.target, stats);
+        k_ref_sums<WT><<<gt, 256, 0, st>>>(order, nv, g.offs, g.nbr, w, P, b.R, K, ext, Kr, b.sz, b.list,
+                                           b.moved + 1);
+        k_ref_sums_big<WT><<<gw, 256, 0, st>>>(b.list, b.moved + 1, g.offs, g.nbr, w, P, b.R, ext);
+        k_ref_cand<WT><<<gt, 256, 0, st>>>(order, nv, g.offs, P, b.R, K, wC, TotC, b.sz, m2, b.target, b.list2,
+                                           b.moved + 2);
+        k_ref_decide<WT><<<gd, kDecideBlock, 0, st>>>(b.list2, b.moved + 2, g.offs, g.nbr, w, P, b.R, K, TotC, ext,
+                                                      Kr, m2, b.target, stats);
         k_ref_mark<<<gt, 256, 0, st>>>(b.list2, b.moved + 2, b.target, b.marks);
         k_ref_move<<<gt, 256, 0, st>>>(b.list2, b.moved + 2, b.target, b.marks, b.R, b.moved);
         note_launch(6);
@@ -334,34 +387,37 @@ int refine_run(const LevelGraph &g, const int32_t *P, const int32_t *K, const in
         if (moved == 0) break;
     }
     // totals of the final sub-communities (the next level's weighted degrees)
-    cudaMemsetAsync(b.ext, 0, (size_t)n * sizeof(int32_t), st);
-    cudaMemsetAsync(b.Kr, 0, (size_t)n * sizeof(int32_t), st);
+    cudaMemsetAsync(ext, 0, (size_t)n * sizeof(WT), st);
+    cudaMemsetAsync(Kr, 0, (size_t)n * sizeof(WT), st);
     cudaMemsetAsync(b.sz, 0, (size_t)n * sizeof(int32_t), st);
     cudaMemsetAsync(b.moved + 1, 0, sizeof(int32_t), st);
-    k_ref_sums<<<gt, 256, 0, st>>>(order, nv, g.offs, g.nbr, w, P, b.R, K, b.ext, b.Kr, b.sz, b.list,
-                                   b.moved + 1);
+    k_ref_sums<WT><<<gt, 256, 0, st>>>(order, nv, g.offs, g.nbr, w, P, b.R, K, ext, Kr, b.sz, b.list, b.moved + 1);
     note_launch(1);
     return sweeps;
 }
 
-namespace {
-__global__ void k_start_partition(int n, const int32_t *__restrict__ init, const int32_t *__restrict__ K,
-                                  int32_t *comm, int32_t *Tot, int32_t *size)
-{
-    for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) {
-        const int c = init[v];
-        comm[v] = c;
-        atomicAdd(&Tot[c], K[v]);
-        atomicAdd(&size[c], 1);
-    }
-}
 }  // namespace
+
+int refine_run(const LevelGraph &g, const int32_t *P, const void *K, const void *TotC, long long m2,
+               const int32_t *order, int nv, RefineBuffers &b, DevStats *stats, cudaStream_t st,
+               gala_status *status)
+{
+    if (g.wide)
+        return refine_t<long long>(g, P, (const long long *)K, (const long long *)TotC, m2, order, nv, b, stats, st,
+                                   status);
+    return refine_t<int>(g, P, (const int *)K, (const int *)TotC, m2, order, nv, b, stats, st, status);
+}
 
 void p1_start_partition(Phase1Buffers &b, const int32_t *init, int n, cudaStream_t st)
 {
-    cudaMemsetAsync(b.Tot, 0, (size_t)n * sizeof(int32_t), st);
+    const size_t ws = b.wide ? sizeof(long long) : sizeof(int);
+    cudaMemsetAsync(b.Tot, 0, (size_t)n * ws, st);
     cudaMemsetAsync(b.size, 0, (size_t)n * sizeof(int32_t), st);
-    k_start_partition<<<grid_for(n, 256), 256, 0, st>>>(n, init, b.K, b.comm, b.Tot, b.size);
+    if (b.wide)
+        k_start_partition<long long><<<grid_for(n, 256), 256, 0, st>>>(n, init, (const long long *)b.K, b.comm,
+                                                                       (long long *)b.Tot, b.size);
+    else
+        k_start_partition<int><<<grid_for(n, 256), 256, 0, st>>>(n, init, b.K, b.comm, b.Tot, b.size);
     note_launch(1);
 }
 

@@ -628,6 +628,15 @@ int32_t orc_louvain_fixed(int32_t n, const int64_t *offs, const int32_t *nbr, co
                        iter_q, iter_cap, n_iter_q, nthreads, 0);
 }
 
+int32_t orc_louvain_fixed_refine(int32_t n, const int64_t *offs, const int32_t *nbr, const int64_t *w,
+                                 double min_mod, int32_t max_levels, int32_t *comm_out, double *level_q,
+                                 int32_t *level_c, int32_t *level_iters, int32_t level_cap, double *iter_q,
+                                 int32_t iter_cap, int32_t *n_iter_q, int32_t nthreads)
+{
+    return louvain_w64(n, offs, nbr, w, min_mod, max_levels, comm_out, level_q, level_c, level_iters, level_cap,
+                       iter_q, iter_cap, n_iter_q, nthreads, 1);
+}
+
 double orc_modularity_f32(int32_t n, const int64_t *offs, const int32_t *nbr, const float *w,
                           const int32_t *labels)
 {

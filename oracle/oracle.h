@@ -69,6 +69,11 @@ int32_t orc_louvain_fixed(int32_t n, const int64_t *offs, const int32_t *nbr, co
                           double min_mod, int32_t max_levels, int32_t *comm_out, double *level_q,
                           int32_t *level_c, int32_t *level_iters, int32_t level_cap, double *iter_q,
                           int32_t iter_cap, int32_t *n_iter_q, int32_t nthreads);
+/* the same with the refinement of orc_louvain_refine */
+int32_t orc_louvain_fixed_refine(int32_t n, const int64_t *offs, const int32_t *nbr, const int64_t *w,
+                                 double min_mod, int32_t max_levels, int32_t *comm_out, double *level_q,
+                                 int32_t *level_c, int32_t *level_iters, int32_t level_cap, double *iter_q,
+                                 int32_t iter_cap, int32_t *n_iter_q, int32_t nthreads);
 double orc_modularity_f32(int32_t n, const int64_t *offs, const int32_t *nbr, const float *w,
                           const int32_t *labels);
 /* Q from a 128-bit sum of Tot^2 (hi, lo words): hi * 2^64 + lo in FP64. */

@@ -72,6 +72,8 @@ class Oracle:
         L.orc_louvain_fixed.argtypes = [ctypes.c_int32, _i64p, _i32p, _i64p, ctypes.c_double, ctypes.c_int32,
                                         _i32p, _f64p, _i32p, _i32p, ctypes.c_int32, _f64p, ctypes.c_int32,
                                         ctypes.POINTER(ctypes.c_int32), ctypes.c_int32]
+        L.orc_louvain_fixed_refine.restype = ctypes.c_int32
+        L.orc_louvain_fixed_refine.argtypes = L.orc_louvain_fixed.argtypes
         L.orc_modularity_f32.restype = ctypes.c_double
         L.orc_modularity_f32.argtypes = [ctypes.c_int32, _i64p, _i32p, _f32p, _i32p]
 
@@ -152,7 +154,7 @@ class Oracle:
         self.lib.orc_fixed_weights(_p(wf, f32), wf.shape[0], shift, _p(out, _i64p))
         return shift, out
 
-    def louvain_f32(self, offs, nbr, wf, min_mod=1e-6, max_levels=0, nthreads=1, iter_cap=65536):
+    def louvain_f32(self, offs, nbr, wf, min_mod=1e-6, max_levels=0, nthreads=1, iter_cap=65536, refine=False):
         """Multi-round run of a float-weight graph on its fixed-point weights."""
         offs = np.ascontiguousarray(offs, dtype=np.int64)
         nbr = np.ascontiguousarray(nbr, dtype=np.int32)
@@ -165,9 +167,9 @@ class Oracle:
         li = np.zeros(64, dtype=np.int32)
         iq = np.zeros(iter_cap, dtype=np.float64)
         nq = ctypes.c_int32()
-        r = self.lib.orc_louvain_fixed(n, _p(offs, _i64p), _p(nbr, _i32p), _p(w64, _i64p), min_mod, max_levels,
-                                       _p(comm, _i32p), _p(lq, _f64p), _p(lc, _i32p), _p(li, _i32p), 64,
-                                       _p(iq, _f64p), iter_cap, ctypes.byref(nq), nthreads)
+        fn = self.lib.orc_louvain_fixed_refine if refine else self.lib.orc_louvain_fixed
+        r = fn(n, _p(offs, _i64p), _p(nbr, _i32p), _p(w64, _i64p), min_mod, max_levels, _p(comm, _i32p),
+               _p(lq, _f64p), _p(lc, _i32p), _p(li, _i32p), 64, _p(iq, _f64p), iter_cap, ctypes.byref(nq), nthreads)
         return {"rounds": r, "labels": comm, "level_q": lq[:r].tolist(), "level_c": lc[:r].tolist(),
                 "level_iters": li[:r].tolist(), "iter_q": iq[:min(nq.value, iter_cap)].tolist(),
                 "modularity": float(lq[r - 1]) if r > 0 else float("nan"), "shift": shift}

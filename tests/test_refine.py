@@ -85,15 +85,41 @@ def test_gpu_refine_matches_oracle(ffi, oracle, torch_cuda):
         assert np.array_equal(plain["labels"], po["labels"]), name
 
 
-@pytest.mark.gpu
-def test_gpu_refine_rejected_for_float_weights(ffi, torch_cuda):
+def _float_graphs(ffi):
     rng = np.random.default_rng(3)
-    offs, nbr, w = _sym_graph(rng, 500, 3000, True)
-    gf = ffi.Graph.from_csr_f32(offs, nbr, w.astype(np.float32))
-    ctx = ffi.Context(500, offs[-1])
-    with pytest.raises(RuntimeError, match="refinement"):
-        ctx.louvain(gf, refine=True)
-    ctx.close()
+    offs, nbr, w = _sym_graph(rng, 4000, 24000, True)
+    # symmetric float weights: a function of the unordered pair
+    src = np.repeat(np.arange(offs.shape[0] - 1), np.diff(offs))
+    lo, hi = np.minimum(src, nbr).astype(np.int64), np.maximum(src, nbr).astype(np.int64)
+    wsym = (w * (1.0 + ((lo * 7919 + hi * 104729) % 97) / 64.0)).astype(np.float32)
+    out = [("random", offs, nbr, wsym, ffi.Graph.from_csr_f32(offs, nbr, wsym))]
+    g = ffi.Graph.lfr(20000, dmin=4, dmax=200, cmin=20, cmax=1000, seed=5)
+    lo_, ln, _ = g.arrays()
+    out.append(("lfr", lo_, ln, g.weights_f32(), g))
+    return out
+
+
+def test_oracle_refined_float_rounds(ffi, oracle):
+    for name, offs, nbr, wf, _ in _float_graphs(ffi):
+        a = oracle.louvain_f32(offs, nbr, wf)
+        b = oracle.louvain_f32(offs, nbr, wf, refine=True)
+        assert b["modularity"] >= a["modularity"] - 0.002, name
+        assert abs(oracle.modularity_f32(offs, nbr, wf, b["labels"]) - b["modularity"]) < 1e-6, name
+
+
+@pytest.mark.gpu
+def test_gpu_refine_float_matches_oracle(ffi, oracle, torch_cuda):
+    for name, offs, nbr, wf, g in _float_graphs(ffi):
+        n, e, _ = g.info()
+        ctx = ffi.Context(n, e)
+        r = ctx.louvain(g, refine=True)
+        r2 = ctx.louvain(g, refine=True)
+        ctx.close()
+        o = oracle.louvain_f32(offs, nbr, wf, refine=True)
+        assert np.array_equal(r["labels"], o["labels"]), name
+        assert r["iter_q"] == o["iter_q"], name
+        assert r["level_c"] == o["level_c"], name
+        assert np.array_equal(r["labels"], r2["labels"]) and r["iter_q"] == r2["iter_q"], name
 
 
 @pytest.mark.gpu
