@@ -94,9 +94,10 @@ typedef struct {
                                    min_modularity contracts the refinement of its
                                    communities into well-connected
                                    sub-communities, and the next round starts
-                                   from the communities; integer-weight single
-                                   graphs only (not with batches, proposals or
-                                   level_dir).  0 = the reference's rounds. */
+                                   from the communities; single graphs only
+                                   (integer or float weights; not with batches,
+                                   proposals or level_dir).  0 = the
+                                   reference's rounds. */
     /* Checkpoints (no counterpart in the reference, which never writes its
        partition, louvain.cu:226): when set, after every round r the
        contracted graph is written to <level_dir>/level_<r+1>.bin (the .bin
