@@ -806,10 +806,11 @@ __device__ __forceinline__ void scan_list(const DecideArgs<WT> &a, const Scale &
 constexpr int kWarpTable = 512;
 constexpr int kWarpLog = 9;
 constexpr int kWarpWarps = 8;  // warps per block
+constexpr int kWarpOcc = kMaxWarpDeg;  // claimed slots per vertex <= its row length
 template <typename WT>
 constexpr size_t warp_smem()
 {
-    return (size_t)kWarpWarps * kWarpTable * (sizeof(int) + sizeof(WT) + sizeof(unsigned short));
+    return (size_t)kWarpWarps * (kWarpTable * (sizeof(int) + sizeof(WT)) + kWarpOcc * sizeof(unsigned short));
 }
 template <typename WT, bool W>
 __global__ void __launch_bounds__(256) k_decide_warp(DecideArgs<WT> a, const int32_t *__restrict__ list,
@@ -821,7 +822,7 @@ __global__ void __launch_bounds__(256) k_decide_warp(DecideArgs<WT> a, const int
     int *keys = (int *)((WT *)wsm_ll + kWarpWarps * kWarpTable) + wib * kWarpTable;
     unsigned short *occ =
         (unsigned short *)((int *)((WT *)wsm_ll + kWarpWarps * kWarpTable) + kWarpWarps * kWarpTable) +
-        wib * kWarpTable;
+        wib * kWarpOcc;
     for (int j = lane; j < kWarpTable; j += 32) {
         keys[j] = -1;
         vals[j] = 0;
@@ -892,13 +893,32 @@ __global__ void __launch_bounds__(256) k_decide_warp(DecideArgs<WT> a, const int
     }
 }
 
+// Resident 256-thread blocks per SM of the 33-256 kernel (occupancy query,
+// cached per instantiation).
+template <typename WT>
+int warp_resident(bool W)
+{
+    static int cached[2] = {0, 0};
+    int &r = cached[W ? 1 : 0];
+    if (r == 0) {
+        int k = 0;
+        if (W)
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&k, k_decide_warp<WT, true>, 256, warp_smem<WT>());
+        else
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&k, k_decide_warp<WT, false>, 256, warp_smem<WT>());
+        r = k > 0 ? k : 1;
+    }
+    return r;
+}
+
 // Degree 257-8192: one CTA per vertex with a shared-memory hash table of tmax
 // slots (int keys, WT values) and the list of claimed slots, cleared once per
 // CTA and then slot by slot after every vertex.
 template <typename WT>
 constexpr size_t cta_smem(int tmax)
 {
-    return (size_t)tmax * (sizeof(int) + sizeof(WT) + sizeof(unsigned short));
+    // a vertex claims at most deg <= tmax / 2 slots
+    return (size_t)tmax * (sizeof(int) + sizeof(WT)) + (size_t)(tmax / 2) * sizeof(unsigned short);
 }
 template <typename WT, int BLOCK, bool W>
 __global__ void __launch_bounds__(BLOCK) k_decide_cta(DecideArgs<WT> a, const int32_t *__restrict__ list,
@@ -1186,6 +1206,24 @@ __global__ void __launch_bounds__(BLOCK) k_first_cta(DecideArgs<WT> a, const int
 
 constexpr int kCtaTable5 = 4096;
 constexpr int kCtaTable6 = 16384;
+// Resident 256-thread blocks per SM of the 257-2048 kernel (cached).
+template <typename WT>
+int cta256_resident(bool W)
+{
+    static int cached[2] = {0, 0};
+    int &r = cached[W ? 1 : 0];
+    if (r == 0) {
+        int k = 0;
+        if (W)
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&k, k_decide_cta<WT, 256, true>, 256,
+                                                          cta_smem<WT>(kCtaTable5));
+        else
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&k, k_decide_cta<WT, 256, false>, 256,
+                                                          cta_smem<WT>(kCtaTable5));
+        r = k > 0 ? k : 1;
+    }
+    return r;
+}
 
 // Arguments of the decide kernels for the weight type WT.
 template <typename WT>
@@ -1257,8 +1295,9 @@ static void decide_t(const LevelGraph &g, Phase1Buffers &b, int bin, const int32
     case 2: GALA_DG(16); break;
     case 3: GALA_DG(32); break;
     case 4: {
-        // as many CTAs as the tables let reside (5 per SM): no second wave
-        const int g4 = grid_lanes(32) < num_sms() * 5 ? grid_lanes(32) : num_sms() * 5;
+        // as many CTAs as can reside (tables and registers): no second wave
+        const int cap4 = num_sms() * warp_resident<WT>(W);
+        const int g4 = grid_lanes(32) < cap4 ? grid_lanes(32) : cap4;
         if (W)
             k_decide_warp<WT, true><<<g4, 256, warp_smem<WT>(), st>>>(a, list, count_ptr);
         else
@@ -1268,7 +1307,8 @@ static void decide_t(const LevelGraph &g, Phase1Buffers &b, int bin, const int32
     case 5: {  // 256 (default) or 512 threads per vertex
         const size_t sm = cta_smem<WT>(kCtaTable5);
         if (b.b5_block == 256) {
-            int grid = level_count < num_sms() * 5 ? level_count : num_sms() * 5;
+            const int cap5 = num_sms() * cta256_resident<WT>(W);
+            int grid = level_count < cap5 ? level_count : cap5;
             if (W)
                 k_decide_cta<WT, 256, true><<<grid, 256, sm, st>>>(a, list, count_ptr, kCtaTable5);
             else
