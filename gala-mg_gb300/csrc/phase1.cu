@@ -922,7 +922,8 @@ constexpr size_t cta_smem(int tmax)
 }
 template <typename WT, int BLOCK, bool W>
 __global__ void __launch_bounds__(BLOCK) k_decide_cta(DecideArgs<WT> a, const int32_t *__restrict__ list,
-                                                      const int *__restrict__ count_ptr, int tmax)
+                                                      const int *__restrict__ count_ptr, int tmax, int dlo,
+                                                      int dhi)
 {
     extern __shared__ long long dyn_smem_ll[];
     __shared__ double r_dq[BLOCK / 32];
@@ -953,6 +954,7 @@ __global__ void __launch_bounds__(BLOCK) k_decide_cta(DecideArgs<WT> a, const in
         const long long e = a.offs[v + 1];
         const int deg = (int)(e - s);
         const int cur = a.comm[v];
+        if (deg <= dlo || deg > dhi) continue;  // the other launch of this bin decides it
         if (2LL * deg > tmax) {  // cannot happen for the bin limits; recorded, vertex stays
             if (threadIdx.x == 0) atomicOr(&a.st->err, kErrHashOverflow);
             continue;
@@ -1206,20 +1208,19 @@ __global__ void __launch_bounds__(BLOCK) k_first_cta(DecideArgs<WT> a, const int
 
 constexpr int kCtaTable5 = 4096;
 constexpr int kCtaTable6 = 16384;
-// Resident 256-thread blocks per SM of the 257-2048 kernel (cached).
-template <typename WT>
-int cta256_resident(bool W)
+// Resident blocks per SM of a CTA decide kernel with a tmax-slot table (cached).
+template <typename WT, int BLOCK>
+int cta_resident(bool W, int tmax)
 {
-    static int cached[2] = {0, 0};
-    int &r = cached[W ? 1 : 0];
+    static int cached[2][32] = {};
+    int &r = cached[W ? 1 : 0][__builtin_ctz((unsigned)tmax)];
     if (r == 0) {
         int k = 0;
         if (W)
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&k, k_decide_cta<WT, 256, true>, 256,
-                                                          cta_smem<WT>(kCtaTable5));
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&k, k_decide_cta<WT, BLOCK, true>, BLOCK, cta_smem<WT>(tmax));
         else
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&k, k_decide_cta<WT, 256, false>, 256,
-                                                          cta_smem<WT>(kCtaTable5));
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&k, k_decide_cta<WT, BLOCK, false>, BLOCK,
+                                                          cta_smem<WT>(tmax));
         r = k > 0 ? k : 1;
     }
     return r;
@@ -1305,30 +1306,42 @@ static void decide_t(const LevelGraph &g, Phase1Buffers &b, int bin, const int32
         break;
     }
     case 5: {  // 256 (default) or 512 threads per vertex
-        const size_t sm = cta_smem<WT>(kCtaTable5);
         if (b.b5_block == 256) {
-            const int cap5 = num_sms() * cta256_resident<WT>(W);
-            int grid = level_count < cap5 ? level_count : cap5;
-            if (W)
-                k_decide_cta<WT, 256, true><<<grid, 256, sm, st>>>(a, list, count_ptr, kCtaTable5);
-            else
-                k_decide_cta<WT, 256, false><<<grid, 256, sm, st>>>(a, list, count_ptr, kCtaTable5);
+            // two launches: rows up to 1024 entries with a 2048-slot table
+            // (more resident CTAs), longer rows with the 4096-slot table
+            const int splits[2][3] = {{kCtaTable5 / 2, 0, kCtaTable5 / 4}, {kCtaTable5, kCtaTable5 / 4, INT_MAX}};
+            for (const auto &sp : splits) {
+                const int cap5 = num_sms() * cta_resident<WT, 256>(W, sp[0]);
+                const int grid = level_count < cap5 ? level_count : cap5;
+                const size_t sm = cta_smem<WT>(sp[0]);
+                if (W)
+                    k_decide_cta<WT, 256, true><<<grid, 256, sm, st>>>(a, list, count_ptr, sp[0], sp[1], sp[2]);
+                else
+                    k_decide_cta<WT, 256, false><<<grid, 256, sm, st>>>(a, list, count_ptr, sp[0], sp[1], sp[2]);
+            }
+            note_launch(1);
         } else {
+            const size_t sm = cta_smem<WT>(kCtaTable5);
             int grid = level_count < num_sms() * 4 ? level_count : num_sms() * 4;
             if (W)
-                k_decide_cta<WT, 512, true><<<grid, 512, sm, st>>>(a, list, count_ptr, kCtaTable5);
+                k_decide_cta<WT, 512, true><<<grid, 512, sm, st>>>(a, list, count_ptr, kCtaTable5, 0, INT_MAX);
             else
-                k_decide_cta<WT, 512, false><<<grid, 512, sm, st>>>(a, list, count_ptr, kCtaTable5);
+                k_decide_cta<WT, 512, false><<<grid, 512, sm, st>>>(a, list, count_ptr, kCtaTable5, 0, INT_MAX);
         }
         break;
     }
     case 6: {
-        int grid = level_count < num_sms() ? level_count : num_sms();
-        const size_t sm = cta_smem<WT>(kCtaTable6);
-        if (W)
-            k_decide_cta<WT, 1024, true><<<grid, 1024, sm, st>>>(a, list, count_ptr, kCtaTable6);
-        else
-            k_decide_cta<WT, 1024, false><<<grid, 1024, sm, st>>>(a, list, count_ptr, kCtaTable6);
+        const int splits[2][3] = {{kCtaTable6 / 2, 0, kCtaTable6 / 4}, {kCtaTable6, kCtaTable6 / 4, INT_MAX}};
+        for (const auto &sp : splits) {
+            const int cap6 = num_sms() * cta_resident<WT, 1024>(W, sp[0]);
+            const int grid = level_count < cap6 ? level_count : cap6;
+            const size_t sm = cta_smem<WT>(sp[0]);
+            if (W)
+                k_decide_cta<WT, 1024, true><<<grid, 1024, sm, st>>>(a, list, count_ptr, sp[0], sp[1], sp[2]);
+            else
+                k_decide_cta<WT, 1024, false><<<grid, 1024, sm, st>>>(a, list, count_ptr, sp[0], sp[1], sp[2]);
+        }
+        note_launch(1);
         break;
     }
     default: return;  // hub vertices: p1_hub_decide
