@@ -1691,11 +1691,14 @@ static void update_t(const LevelGraph &g, Phase1Buffers &b, int bin, const int32
         else                                                                                           \
             k_update_group<WT, GV, false><<<grid_lanes(GV), 256, 0, st>>>(a, list, count);             \
     } while (0)
+    // bins 2 and 3 use groups of half their largest degree: a lane sums at
+    // most two entries (independent loads) and a warp serves twice the
+    // vertices of one lane per entry
     switch (bin) {
     case 0: GALA_UG(4); break;
     case 1: GALA_UG(8); break;
-    case 2: GALA_UG(16); break;
-    case 3:
+    case 2: GALA_UG(8); break;
+    case 3: GALA_UG(16); break;
     case 4:
     case 5: GALA_UG(32); break;
     default: {
@@ -1771,7 +1774,19 @@ __device__ __forceinline__ WT *hub_vals(const HubPlan &p, long long i)
 template <typename WT, bool W>
 __global__ void __launch_bounds__(256) k_hub_insert(DecideArgs<WT> a, HubPlan p, const uint8_t *__restrict__ flag)
 {
-    const int lane = threadIdx.x & 31;
+    // a small shared-memory table in front of the hub's global table: an
+    // entry whose community finds a slot within kHubCacheProbe probes is
+    // summed there, the rest go to the global table directly; the cached sums
+    // are added to the global table at the end of the chunk (integer adds:
+    // the totals do not depend on the split)
+    constexpr int kHubCache = 512, kHubCacheLog = 9, kHubCacheProbe = 2;
+    __shared__ int ckeys[kHubCache];
+    __shared__ WT cvals[kHubCache];
+    for (int q = threadIdx.x; q < kHubCache; q += blockDim.x) {
+        ckeys[q] = -1;
+        cvals[q] = 0;
+    }
+    __syncthreads();
     for (long long wi = blockIdx.x; wi < p.nwork; wi += gridDim.x) {
         const int i = p.work[wi];
         const int v = p.hubs[i];
@@ -1785,18 +1800,34 @@ __global__ void __launch_bounds__(256) k_hub_insert(DecideArgs<WT> a, HubPlan p,
         WT *vals = hub_vals<WT>(p, i);
         for (long long b0 = s; b0 < e2; b0 += blockDim.x) {
             const long long j = b0 + threadIdx.x;
-            const bool valid = j < e2;
-            int c = -1;
-            WT wt = 0;
-            if (valid) {
-                c = a.comm[a.nbr[j]];
-                wt = W ? a.w[j] : 1;
+            if (j < e2) {
+                const int c = a.comm[a.nbr[j]];
+                const WT wt = W ? a.w[j] : 1;
+                unsigned h = hash_slot(c, kHubCacheLog);
+                bool cached = false;
+#pragma unroll
+                for (int q = 0; q < kHubCacheProbe; ++q) {
+                    const int k = atomicCAS(&ckeys[h], -1, c);
+                    if (k == -1 || k == c) {
+                        atomic_add_w(&cvals[h], wt);
+                        cached = true;
+                        break;
+                    }
+                    h = (h + 1) & (unsigned)(kHubCache - 1);
+                }
+                if (!cached && !hash_add(keys, vals, T, lg, c, wt)) atomicOr(&a.st->err, kErrHashOverflow);
             }
-            // entries go to the hub's table one by one (no warp-level key
-            // match: measured faster on the hub rows of R-MAT levels)
-            if (valid)
-                if (!hash_add(keys, vals, T, lg, c, wt)) atomicOr(&a.st->err, kErrHashOverflow);
         }
+        __syncthreads();
+        for (int q = threadIdx.x; q < kHubCache; q += blockDim.x) {
+            const int k = ckeys[q];
+            if (k != -1) {
+                if (!hash_add(keys, vals, T, lg, k, cvals[q])) atomicOr(&a.st->err, kErrHashOverflow);
+                ckeys[q] = -1;
+                cvals[q] = 0;
+            }
+        }
+        __syncthreads();
     }
 }
 
