@@ -1691,15 +1691,15 @@ static void update_t(const LevelGraph &g, Phase1Buffers &b, int bin, const int32
         else                                                                                           \
             k_update_group<WT, GV, false><<<grid_lanes(GV), 256, 0, st>>>(a, list, count);             \
     } while (0)
-    // bins 2 and 3 use groups of half their largest degree: a lane sums at
-    // most two entries (independent loads) and a warp serves twice the
-    // vertices of one lane per entry
+    // bins 2-4 use groups narrower than their rows: a lane sums several
+    // entries (independent loads) and a warp serves several vertices, more
+    // rows in flight than one lane per entry (measured on R-MAT levels)
     switch (bin) {
     case 0: GALA_UG(4); break;
     case 1: GALA_UG(8); break;
     case 2: GALA_UG(8); break;
     case 3: GALA_UG(16); break;
-    case 4:
+    case 4: GALA_UG(8); break;
     case 5: GALA_UG(32); break;
     default: {
         int grid = count < cap ? count : cap;
