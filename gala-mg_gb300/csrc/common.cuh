@@ -15,7 +15,8 @@ namespace gala {
 //   bin 0..3: deg 1-4 / 5-8 / 9-16 / 17-32 -> a group of 4/8/16/32 lanes per
 //             vertex, one neighbour per lane, aggregation by shuffles (groups
 //             of 4-16 lanes) or __match_any_sync (whole warps)
-//   bin 4   : deg 33-256     -> one warp per vertex, 512-slot smem hash
+//   bin 4   : deg 33-256     -> one warp per vertex, 256-slot smem hash up to
+//                               128 entries, else 512
 //   bin 5   : deg 257-2048   -> one 256-thread CTA per vertex (512 by option),
 //                               2048-slot smem hash up to 1024 entries, else 4096
 //   bin 6   : deg 2049-8192  -> one 1024-thread CTA per vertex, 8192-slot smem

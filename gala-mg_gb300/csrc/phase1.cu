@@ -801,29 +801,32 @@ __device__ __forceinline__ void scan_list(const DecideArgs<WT> &a, const Scale &
 }
 
 // Degree 33-256: one warp per vertex with a private shared-memory hash table
-// of kWarpTable slots.  The table is cleared once per warp; per vertex the
-// slots it claims are listed, and only those are scanned and cleared again.
-constexpr int kWarpTable = 512;
-constexpr int kWarpLog = 9;
+// of TW slots (two launches: 256 slots for rows up to 128 entries, with eight
+// resident blocks per SM at 32 registers a thread, and 512 slots for longer
+// rows).  The table is cleared once per warp; per vertex the slots it claims
+// are listed, and only those are scanned and cleared again.
+constexpr int kWarpTable = 512;  // the full table; rows up to kWarpTable / 4 use half of it
 constexpr int kWarpWarps = 8;  // warps per block
-constexpr int kWarpOcc = kMaxWarpDeg;  // claimed slots per vertex <= its row length
-template <typename WT>
+// TW slots per warp for rows up to TW / 2 entries (a vertex claims at most
+// as many slots as it has entries)
+template <typename WT, int TW>
 constexpr size_t warp_smem()
 {
-    return (size_t)kWarpWarps * (kWarpTable * (sizeof(int) + sizeof(WT)) + kWarpOcc * sizeof(unsigned short));
+    return (size_t)kWarpWarps * (TW * (sizeof(int) + sizeof(WT)) + (TW / 2) * sizeof(unsigned short));
 }
-template <typename WT, bool W>
-__global__ void __launch_bounds__(256) k_decide_warp(DecideArgs<WT> a, const int32_t *__restrict__ list,
-                                                     const int *__restrict__ count_ptr)
+template <typename WT, bool W, int TW, int MINB>
+__global__ void __launch_bounds__(256, MINB) k_decide_warp(DecideArgs<WT> a, const int32_t *__restrict__ list,
+                                                     const int *__restrict__ count_ptr, int dlo, int dhi)
 {
     extern __shared__ long long wsm_ll[];
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-    WT *vals = (WT *)wsm_ll + wib * kWarpTable;
-    int *keys = (int *)((WT *)wsm_ll + kWarpWarps * kWarpTable) + wib * kWarpTable;
+    constexpr int TL = TW == 256 ? 8 : 9;
+    static_assert((1 << TL) == TW, "table size");
+    WT *vals = (WT *)wsm_ll + wib * TW;
+    int *keys = (int *)((WT *)wsm_ll + kWarpWarps * TW) + wib * TW;
     unsigned short *occ =
-        (unsigned short *)((int *)((WT *)wsm_ll + kWarpWarps * kWarpTable) + kWarpWarps * kWarpTable) +
-        wib * kWarpOcc;
-    for (int j = lane; j < kWarpTable; j += 32) {
+        (unsigned short *)((int *)((WT *)wsm_ll + kWarpWarps * TW) + kWarpWarps * TW) + wib * (TW / 2);
+    for (int j = lane; j < TW; j += 32) {
         keys[j] = -1;
         vals[j] = 0;
     }
@@ -837,6 +840,7 @@ __global__ void __launch_bounds__(256) k_decide_warp(DecideArgs<WT> a, const int
         const Scale sc = scale_of(a, v);
         const long long s = a.offs[v];
         const int deg = (int)(a.offs[v + 1] - s);
+        if (deg <= dlo || deg > dhi) continue;  // the other launch of this bin decides it
         const int cur = a.comm[v];
         int nocc = 0;
         const int32_t *rn = a.nbr + s;
@@ -856,7 +860,7 @@ __global__ void __launch_bounds__(256) k_decide_warp(DecideArgs<WT> a, const int
             bool created = false;
             int slot = -1;
             if (valid) {
-                slot = hash_add_slot(keys, vals, kWarpTable, kWarpLog, c, wt, created);
+                slot = hash_add_slot(keys, vals, TW, TL, c, wt, created);
                 if (slot < 0) atomicOr(&a.st->err, kErrHashOverflow);
             }
             const unsigned cb = __ballot_sync(GALA_FULL_MASK, created);
@@ -895,7 +899,7 @@ __global__ void __launch_bounds__(256) k_decide_warp(DecideArgs<WT> a, const int
 
 // Resident 256-thread blocks per SM of the 33-256 kernel (occupancy query,
 // cached per instantiation).
-template <typename WT>
+template <typename WT, int TW, int MINB>
 int warp_resident(bool W)
 {
     static int cached[2] = {0, 0};
@@ -903,9 +907,11 @@ int warp_resident(bool W)
     if (r == 0) {
         int k = 0;
         if (W)
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&k, k_decide_warp<WT, true>, 256, warp_smem<WT>());
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&k, k_decide_warp<WT, true, TW, MINB>, 256,
+                                                          warp_smem<WT, TW>());
         else
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&k, k_decide_warp<WT, false>, 256, warp_smem<WT>());
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&k, k_decide_warp<WT, false, TW, MINB>, 256,
+                                                          warp_smem<WT, TW>());
         r = k > 0 ? k : 1;
     }
     return r;
@@ -1297,12 +1303,27 @@ static void decide_t(const LevelGraph &g, Phase1Buffers &b, int bin, const int32
     case 3: GALA_DG(32); break;
     case 4: {
         // as many CTAs as can reside (tables and registers): no second wave
-        const int cap4 = num_sms() * warp_resident<WT>(W);
-        const int g4 = grid_lanes(32) < cap4 ? grid_lanes(32) : cap4;
-        if (W)
-            k_decide_warp<WT, true><<<g4, 256, warp_smem<WT>(), st>>>(a, list, count_ptr);
-        else
-            k_decide_warp<WT, false><<<g4, 256, warp_smem<WT>(), st>>>(a, list, count_ptr);
+        // two launches: rows up to 128 entries with 256-slot tables (more
+        // resident warps), longer rows with 512-slot tables
+        {
+            const int cap4 = num_sms() * warp_resident<WT, kWarpTable / 2, 8>(W);
+            const int g4 = grid_lanes(32) < cap4 ? grid_lanes(32) : cap4;
+            const size_t sm = warp_smem<WT, kWarpTable / 2>();
+            if (W)
+                k_decide_warp<WT, true, kWarpTable / 2, 8><<<g4, 256, sm, st>>>(a, list, count_ptr, 0, kWarpTable / 4);
+            else
+                k_decide_warp<WT, false, kWarpTable / 2, 8><<<g4, 256, sm, st>>>(a, list, count_ptr, 0, kWarpTable / 4);
+        }
+        {
+            const int cap4 = num_sms() * warp_resident<WT, kWarpTable, 1>(W);
+            const int g4 = grid_lanes(32) < cap4 ? grid_lanes(32) : cap4;
+            const size_t sm = warp_smem<WT, kWarpTable>();
+            if (W)
+                k_decide_warp<WT, true, kWarpTable, 1><<<g4, 256, sm, st>>>(a, list, count_ptr, kWarpTable / 4, INT_MAX);
+            else
+                k_decide_warp<WT, false, kWarpTable, 1><<<g4, 256, sm, st>>>(a, list, count_ptr, kWarpTable / 4, INT_MAX);
+        }
+        note_launch(1);
         break;
     }
     case 5: {  // 256 (default) or 512 threads per vertex
@@ -1375,10 +1396,14 @@ static void configure_t()
                          (int)cta_smem<WT>(kCtaTable5));
     cudaFuncSetAttribute(k_decide_cta<WT, 512, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)cta_smem<WT>(kCtaTable5));
-    cudaFuncSetAttribute(k_decide_warp<WT, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)warp_smem<WT>());
-    cudaFuncSetAttribute(k_decide_warp<WT, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)warp_smem<WT>());
+    cudaFuncSetAttribute(k_decide_warp<WT, true, kWarpTable, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)warp_smem<WT, kWarpTable>());
+    cudaFuncSetAttribute(k_decide_warp<WT, false, kWarpTable, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)warp_smem<WT, kWarpTable>());
+    cudaFuncSetAttribute(k_decide_warp<WT, true, kWarpTable / 2, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)warp_smem<WT, kWarpTable / 2>());
+    cudaFuncSetAttribute(k_decide_warp<WT, false, kWarpTable / 2, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)warp_smem<WT, kWarpTable / 2>());
 }
 
 void p1_configure_kernels()
