@@ -9,9 +9,13 @@ round of phase 1 + contraction until the round gain is below 1e-6.
           with CUDA events on the stream the engine runs on
   e2e     the same through gala_louvain with host buffers: pinned CSR copied
           host->device, all rounds, labels copied device->host, every step
-  roofline of the decide-and-move sweeps (algorithmic bytes / sweep time)
+  e2e.learned_vs_plain  the learned move proposal's end-to-end time over
+          the plain run's, and its final modularity difference
+  roofline of the decide-and-move sweeps (algorithmic bytes / sweep time);
+  roofline_contract  the same for the contractions
   cpu_baseline  the CPU oracle (the reference's algorithm restated on the
-          host) on the same graph
+          host, all cores) on the same graph, and (cpu_baseline.sequential)
+          the classic sequential Louvain on one core
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 N > 1 runs under torchrun: one independent replica per GPU (the path does
@@ -25,6 +29,8 @@ import subprocess
 import sys
 import threading
 import time
+
+import numpy as np
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
 PKG = os.path.join(ROOT, "gala-mg_gb300")
@@ -77,7 +83,7 @@ def parse():
 def make_graph(wl):
     import gala_ffi as ffi
     return ffi.Graph.rmat(wl["scale"], wl["raw_edges"], wl["a"], wl["b"], wl["c"], seed=wl["seed"],
-                          keep_isolated=wl["keep_isolated_ids"])
+                          noise=wl.get("noise", 0.0), keep_isolated=wl["keep_isolated_ids"])
 
 
 def measured_peak():
@@ -99,6 +105,40 @@ def profile_traffic():
         return float(m.group(1)) if m else None
     except OSError:
         return None
+
+
+def contraction_bytes(levels, r, weighted0=False):
+    """Algorithmic bytes of the full contraction after round r (a round
+    followed by another): read the row offsets (8 B), the label (4 B) of every
+    vertex and write its new id (4 B); read every entry's neighbour id (4 B),
+    the neighbour's label (4 B) and its weight (4 B, levels >= 1 or weighted
+    input); write the new CSR: offsets (8 B per row + 1) and entries (4 B id +
+    4 B weight)."""
+    a, b = levels[r], levels[r + 1]
+    wt = 4 if (r > 0 or weighted0) else 0
+    return (a["vertices"] * (8 + 4 + 4) + a["entries"] * (4 + 4 + wt) + (b["vertices"] + 1) * 8 +
+            b["entries"] * (4 + 4))
+
+
+def contraction_roofline(runs, peak, peak_kind):
+    """HBM roofline of the contractions that build a next level (all rounds
+    but the last, which only relabels): algorithmic bytes / CUDA-event time."""
+    byt = ms = 0.0
+    for r in runs:
+        lv = r["levels"]
+        for i in range(len(lv) - 1):
+            byt += contraction_bytes(lv, i)
+            ms += lv[i]["contract_ms"]
+    if ms <= 0:
+        return None
+    ach = byt / (ms / 1000.0) / 1e9
+    lv = runs[-1]["levels"]
+    return {"bound": "hbm", "kernel": "contraction (renumber, member buckets, row aggregation, CSR write) of "
+                                      "every round that builds a next level",
+            "achieved": ach, "peak": peak, "peak_kind": peak_kind, "unit": "GB/s", "frac": ach / peak,
+            "algorithmic_bytes_per_run": byt / len(runs), "ms_per_run": ms / len(runs),
+            "level0_ms": lv[0]["contract_ms"], "level0_bytes": contraction_bytes(lv, 0) if len(lv) > 1 else None,
+            "last_round_relabel_ms": lv[-1]["contract_ms"]}
 
 
 class Clocks:
@@ -182,15 +222,47 @@ def cpu_model():
     return "unknown"
 
 
+def workload_config(wl, n, E, max_deg, world):
+    """The `config` object of both arms (identical for the same workload)."""
+    cfg = {k: v for k, v in wl.items()}
+    cfg.update({"vertices": int(n), "edges": int(E) // 2, "csr_entries": int(E), "max_degree": int(max_deg),
+                "l2": ("inputs larger than L2 (CSR %.0f MB > 129 MB)" if (E * 4 + (n + 1) * 8) > 129e6 else
+                       "inputs smaller than L2 (CSR %.0f MB < 129 MB): a check run, not a bench value")
+                      % ((E * 4 + (n + 1) * 8) / 1e6),
+                "parallelism": f"replicas x{world}"})
+    return cfg
+
+
+def oracle_graph(wl):
+    """The workload's graph built by the CPU oracle's generator
+    (oracle/generators.c), identical to the engine library's (CPU test), so
+    the CPU arm never loads the engine library."""
+    from oracle_ffi import Oracle
+    return Oracle().generate_rmat(wl["scale"], wl["raw_edges"], wl["a"], wl["b"], wl["c"], noise=wl.get("noise", 0.0),
+                                  keep_isolated=wl["keep_isolated_ids"], seed=wl["seed"])
+
+
+def seq_louvain_run(offs, nbr):
+    from oracle_ffi import Oracle
+    o = Oracle()
+    t = time.perf_counter()
+    r = o.seq_louvain(offs, nbr, None, 1e-6)
+    return time.perf_counter() - t, r
+
+
 def reference_arm(args, wl):
     """The reference's path on the host cores: the oracle port (the
-    reference's GPU algorithm restated on the CPU, all host threads)."""
+    reference's GPU algorithm restated on the CPU, all host threads).  The
+    graph comes from the oracle's generator: nothing of the engine (its
+    library, kernels or Python binding) is loaded in this process."""
     rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
     if rank != 0:
         return
-    g = make_graph(wl)
-    offs, nbr, _ = g.arrays()
-    m = int(offs[-1]) // 2
+    offs, nbr = oracle_graph(wl)
+    n = offs.shape[0] - 1
+    E = int(offs[-1])
+    m = E // 2
     threads = os.cpu_count() or 1
     for _ in range(args.warmup):
         cpu_oracle_run(offs, nbr, threads)
@@ -200,15 +272,15 @@ def reference_arm(args, wl):
         times.append(dt)
     sec = sum(times) / len(times)
     val = m / sec
-    cfg = {k: v for k, v in wl.items()}
-    cfg.update({"vertices": int(offs.shape[0] - 1), "edges": m})
+    cfg = workload_config(wl, n, E, int(np.diff(offs).max()), world)
     line = {"impl": "reference", "metric": METRIC, "value": val, "unit": "edges/s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": sec * 1000, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "int32/f64", "data": "synthetic", "config": cfg,
             "modularity": r["modularity"], "communities": r["level_c"][-1], "rounds": r["rounds"],
             "cpu_baseline": {"value": val, "unit": "edges/s", "cores": threads, "kind": "port",
                              "cpu_model": cpu_model(),
-                             "sample": "full run on the whole workload (all rounds), oracle/louvain_oracle.c"},
+                             "sample": "full run on the whole workload (all rounds), oracle/louvain_oracle.c; "
+                                       "graph from oracle/generators.c"},
             "e2e": {"value": val, "unit": "edges/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -513,37 +585,58 @@ def main():
             "sweep_ms": dec_ms / max(sweeps, 1), "sweeps_per_run": sweeps / args.steps}
 
     last = runs[-1]
-    cfg = {k: v for k, v in wl.items()}
-    cfg.update({"vertices": n, "edges": m, "csr_entries": E, "max_degree": max_deg,
-                "l2": "inputs larger than L2 (CSR %.0f MB > 129 MB)" % ((E * 4 + (n + 1) * 8) / 1e6),
-                "parallelism": f"replicas x{world}"})
-    line = {"metric": METRIC, "value": value, "unit": "edges/s", "n_gpus": world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "int32/f64", "data": "synthetic", "config": cfg,
-            "seconds_per_run": ms / 1000.0, "modularity": last["modularity"],
-            "communities": last["num_communities"], "rounds": last["rounds"],
-            "iterations": last["total_iterations"], "fp64_decisions": last["fp64_decisions"],
-            "phase_ms": {"phase1": last["time_phase1_ms"], "decide": last["time_decide_ms"],
-                         "update": last["time_update_ms"], "contract": last["time_contract_ms"]},
-            "e2e": {"value": world * m / (e2e_step / 1000.0), "unit": "edges/s", "ms_per_step": e2e_step,
-                    "h2d_bytes_per_step": r_e2e["h2d_bytes"], "d2h_bytes_per_step": r_e2e["d2h_bytes"]},
-            "roofline": roof, "clocks": clk, "gpu_launches": launches}
-    if not args.no_learned:
-        line["learned"] = learned_arm(ffi, ctx, g, stream, args, torch, e2e_step, r_e2e)
+    contract_roof = contraction_roofline(runs, peak, peak_kind)
+    cfg = workload_config(wl, n, E, max_deg, world)
+    e2e = {"value": world * m / (e2e_step / 1000.0), "unit": "edges/s", "ms_per_step": e2e_step,
+           "h2d_bytes_per_step": r_e2e["h2d_bytes"], "d2h_bytes_per_step": r_e2e["d2h_bytes"]}
+    # bulky secondary arms first, the headline keys after them (the end of
+    # the line is what a truncated log keeps)
+    line = {}
     if not args.no_refine:
         line["refine"] = refine_arm(ffi, ctx, g, stream, args, torch, e2e_step, r_e2e)
     if not args.no_batch:
         line["batch"] = batch_arm(ffi, args, torch, local)
     if not args.no_weighted:
         line["weighted"] = weighted_arm(ffi, args, torch, local)
+    line.update({"metric": METRIC, "value": value, "unit": "edges/s", "n_gpus": world, "steps": args.steps,
+                 "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+                 "vs_baseline": None, "dtype": "int32/f64", "data": "synthetic", "config": cfg,
+                 "seconds_per_run": ms / 1000.0, "modularity": last["modularity"],
+                 "communities": last["num_communities"], "rounds": last["rounds"],
+                 "iterations": last["total_iterations"], "fp64_decisions": last["fp64_decisions"],
+                 "phase_ms": {"phase1": last["time_phase1_ms"], "decide": last["time_decide_ms"],
+                              "update": last["time_update_ms"], "contract": last["time_contract_ms"]},
+                 "gpu_launches": launches})
+    if not args.no_learned:
+        lr = learned_arm(ffi, ctx, g, stream, args, torch, e2e_step, r_e2e)
+        line["learned"] = lr
+        # the second half of the headline metric: learned-prune time / plain
+        # time end to end, at |dQ| <= 0.002
+        e2e["learned_vs_plain"] = {"time_vs_plain": lr["time_vs_plain"], "dq_vs_plain": lr["dq_vs_plain"],
+                                   "plain_ms": e2e_step, "learned_ms": lr["ms_per_step"],
+                                   "threshold": lr["threshold"], "decisions": lr["decisions"],
+                                   "plain_decisions": lr["plain_decisions"], "target": "<= 0.5 at |dQ| <= 0.002"}
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
         dt, ro = cpu_oracle_run(offs, nbr, threads)
+        sdt, so = seq_louvain_run(offs, nbr)
         line["cpu_baseline"] = {"value": m / dt, "unit": "edges/s", "cores": threads, "kind": "port",
                                 "cpu_model": cpu_model(),
                                 "sample": "one full run (all rounds) of the oracle on the whole workload",
                                 "seconds": dt, "modularity": ro["modularity"],
-                                "labels_equal_gpu": bool((ro["labels"] == r_e2e["labels"]).all())}
+                                "labels_equal_gpu": bool((ro["labels"] == r_e2e["labels"]).all()),
+                                "sequential": {"value": m / sdt, "unit": "edges/s", "cores": 1,
+                                               "kind": "sequential",
+                                               "algorithm": "Blondel et al. 2008 asynchronous Louvain, "
+                                                            "oracle/seq_louvain.c, -O3, 1 thread",
+                                               "sample": "one full run (all levels) on the whole workload",
+                                               "seconds": sdt, "modularity": so["modularity"],
+                                               "levels": so["levels"], "communities": so["level_c"][-1]}}
+    line["e2e"] = e2e
+    line["roofline"] = roof
+    if contract_roof:
+        line["roofline_contract"] = contract_roof
+    line["clocks"] = clk
     if rank == 0:
         print(json.dumps(line), flush=True)
     ctx.close()

@@ -44,6 +44,8 @@ struct gala_context {
     double *hub_pdq = nullptr;
     int32_t *hub_pfc = nullptr;
     cudaEvent_t ev[8] = {};
+    // slots of the largest hub table (gala_context_set_hub_table_cap; 0 = by degree)
+    long long hub_table_cap = 0;
     // the degree bins of one sweep are independent: they run concurrently on
     // auxiliary streams, forked from and joined back into `stream`
     static constexpr int kAux = 4;
@@ -308,6 +310,7 @@ gala_status phase1(gala_context *ctx, const LevelGraph &g, long long &m2, double
         hp.pwc = ctx->hub_pwc;
         hp.pdq = ctx->hub_pdq;
         hp.pfc = ctx->hub_pfc;
+        hp.t_cap = ctx->hub_table_cap;
         p1_hub_plan_launch(g, b, hp, st);
         if ((s = check(cudaMemcpyAsync(h, b.stats, sizeof(DevStats), cudaMemcpyDeviceToHost, st), "hub plan")) ||
             (s = sync_check(st, "hub plan")))
@@ -1086,6 +1089,17 @@ gala_status gala_context_set_stream(gala_context *ctx, void *stream)
     gala_status s = sync_check(ctx->stream, "gala_context_set_stream");
     if (s) return s;
     ctx->stream = stream ? (cudaStream_t)stream : ctx->own_stream;
+    return GALA_OK;
+}
+
+gala_status gala_context_set_hub_table_cap(gala_context *ctx, int64_t slots)
+{
+    clear_error();
+    if (!ctx || slots < 0 || (slots > 0 && (slots < 32 || (slots & (slots - 1)) != 0))) {
+        set_error("gala_context_set_hub_table_cap: slots must be 0 or a power of two >= 32");
+        return GALA_ERR_INVALID;
+    }
+    ctx->hub_table_cap = slots;
     return GALA_OK;
 }
 

@@ -129,6 +129,7 @@ struct HubPlan {
     int32_t *work, *twork;
     int32_t *pool;
     long long half;       // keys at pool[0, half), values at pool[half, 2 half)
+    long long t_cap;      // largest table (power of two; 0 = sized by degree only)
     long long nwork, ntwork;
     long long *px;        // per table chunk: best exact gain numerator
     int32_t *pc, *pw, *pt, *pwc;

@@ -1761,7 +1761,8 @@ __global__ void k_hub_plan(HubPlan p, const int64_t *__restrict__ offs)
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < p.H; i += gridDim.x * blockDim.x) {
         const int v = p.hubs[i];
         const long long deg = offs[v + 1] - offs[v];
-        const long long T = next_pow2_ll(deg + deg / 2);  // load at most 2/3
+        long long T = next_pow2_ll(deg + deg / 2);  // load at most 2/3
+        if (p.t_cap > 0 && T > p.t_cap) T = p.t_cap;  // capped: inserts may run out of slots
         p.T[i] = T;
         p.chunks[i] = (deg + kHubChunk - 1) / kHubChunk;
         p.tchunks[i] = (T + kHubChunk - 1) / kHubChunk;

@@ -27,7 +27,8 @@ EXPORTS = ["gala_last_error", "gala_status_string", "gala_kernel_launch_count", 
            "gala_proposal_destroy", "gala_proposal_get_params", "gala_proposal_set_params", "gala_proposal_samples",
            "gala_proposal_clear_samples", "gala_proposal_read_samples", "gala_proposal_gradient",
            "gala_proposal_logits", "gala_proposal_train", "gala_louvain_batch", "gala_generate_sbm_batch",
-           "gala_graph_from_csr_f32", "gala_graph_weights_f32", "gala_generate_lfr", "gala_autotune"]
+           "gala_graph_from_csr_f32", "gala_graph_weights_f32", "gala_generate_lfr", "gala_autotune",
+           "gala_context_set_hub_table_cap"]
 
 PROPOSAL_OFF, PROPOSAL_TRACE, PROPOSAL_SKIP = 0, 1, 2
 PROPOSAL_PARAMS = 32 * 8 + 32 + 32 * 32 + 32 + 32 + 1
@@ -155,6 +156,8 @@ def load(path=LIB_PATH):
     L.gala_context_destroy.argtypes = [_vp]
     L.gala_context_destroy.restype = None
     L.gala_context_set_stream.argtypes = [_vp, _vp]
+    L.gala_context_set_hub_table_cap.argtypes = [_vp, ctypes.c_int64]
+    L.gala_context_set_hub_table_cap.restype = ctypes.c_int
     L.gala_graph_pin.argtypes = [_vp]
     L.gala_louvain.argtypes = [_vp, _vp, ctypes.POINTER(Options), _i32p, ctypes.POINTER(Result)]
     L.gala_louvain_device.argtypes = [_vp, ctypes.c_int32, _vp, _vp, _vp, ctypes.POINTER(Options), _vp,
@@ -369,6 +372,11 @@ class Context:
 
     def __del__(self):
         self.close()
+
+    def set_hub_table_cap(self, slots):
+        """Cap every hub's global hash table at `slots` (0 = by degree); for
+        tests of the overflow status."""
+        _check(load().gala_context_set_hub_table_cap(self.h, slots))
 
     def set_stream(self, stream_handle):
         """Order the context's work on a caller CUDA stream (an int handle,

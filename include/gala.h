@@ -260,6 +260,15 @@ void gala_context_destroy(gala_context *ctx);
  * (louvain_main_process.cu:594-857); here all work of a context is ordered
  * on one stream and only that stream is synchronised. */
 gala_status gala_context_set_stream(gala_context *ctx, void *stream);
+/* Cap the global hash table of every hub (a vertex of degree > 8192 whose
+ * neighbour communities are summed by many CTAs) at `slots` (a power of two
+ * >= 32; 0 = sized by degree, at most 2/3 full, the default).  A cap below a
+ * hub's count of distinct neighbour communities makes that table's bounded
+ * probes run out: the run stops with GALA_ERR_OVERFLOW instead of dropping
+ * weight (the reference drops it silently,
+ * src/louvain_gpu/kernel_functions.cu:217), and the context stays usable.
+ * For tests of that error path; no counterpart in the reference. */
+gala_status gala_context_set_hub_table_cap(gala_context *ctx, int64_t slots);
 /* Page-lock the host arrays of g so host<->device copies run at full
  * bandwidth; gala_graph_destroy unpins them.  Needs a CUDA device. */
 gala_status gala_graph_pin(gala_graph *g);
@@ -391,8 +400,15 @@ gala_status gala_modularity_host(const gala_graph *g, const int32_t *community, 
  * The first call on a device looks up the array's device address (make it
  * before any stream capture).  All calls on a device share the scratch and
  * clear it first; calls that overlap on the GPU (several host threads at
- * once on one device) race.  Runs on the default stream and returns after
- * the result is on the host. */
+ * once on one device) race.  Runs on the legacy default stream and returns
+ * after the result is on the host.  That stream is not ordered after
+ * non-blocking streams (e.g. PyTorch's side streams): the caller must finish
+ * the work that wrote d_offsets, d_neighbors, d_weights and d_community
+ * (synchronise that stream, or make the default stream wait on an event
+ * recorded on it) before the call.  Weights must be positive (as in every
+ * graph of this library); sums are exact (Tot^2 in 128 bits), so any total
+ * weight below 2^64 gives the right Q.  A label outside [0, n) or a weight
+ * that is not positive returns GALA_ERR_INVALID. */
 gala_status gala_modularity_device_static(int32_t n, const int64_t *d_offsets,
                                           const int32_t *d_neighbors, const int32_t *d_weights,
                                           const int32_t *d_community, double *modularity);

@@ -79,6 +79,23 @@ double orc_modularity_f32(int32_t n, const int64_t *offs, const int32_t *nbr, co
 /* Q from a 128-bit sum of Tot^2 (hi, lo words): hi * 2^64 + lo in FP64. */
 double orc_q_from_sums128(int64_t sum_in, uint64_t tot2_lo, uint64_t tot2_hi, int64_t m2);
 
+/* Seeded R-MAT graph (generators.c), byte-identical to the engine library's
+ * gala_generate_rmat: *offs_out (n+1, leading 0) and *nbr_out are malloc'd;
+ * release them with orc_free.  Returns 0, or -1 on bad arguments. */
+int32_t orc_generate_rmat(int32_t scale, int64_t nedges, double a, double b, double c, double noise,
+                          int32_t keep_isolated, uint64_t seed, int32_t nthreads, int32_t *n_out,
+                          int64_t **offs_out, int32_t **nbr_out);
+void orc_free(void *p);
+
+/* The classic sequential (asynchronous, Blondel et al. 2008) Louvain method
+ * on one thread (seq_louvain.c): the timed sequential CPU baseline, not a
+ * restatement of the reference.  comm_out[n] receives the final community of
+ * every vertex; level_q/level_c the Q and community count of every level;
+ * *moves_out the number of moves.  Returns the number of levels. */
+int32_t orc_seq_louvain(int32_t n, const int64_t *offs, const int32_t *nbr, const int32_t *w, double min_mod,
+                        int32_t max_levels, int32_t *comm_out, double *level_q, int32_t *level_c, int32_t level_cap,
+                        int64_t *moves_out);
+
 #ifdef __cplusplus
 }
 #endif

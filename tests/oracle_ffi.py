@@ -76,6 +76,16 @@ class Oracle:
         L.orc_louvain_fixed_refine.argtypes = L.orc_louvain_fixed.argtypes
         L.orc_modularity_f32.restype = ctypes.c_double
         L.orc_modularity_f32.argtypes = [ctypes.c_int32, _i64p, _i32p, _f32p, _i32p]
+        L.orc_generate_rmat.restype = ctypes.c_int32
+        L.orc_generate_rmat.argtypes = [ctypes.c_int32, ctypes.c_int64, ctypes.c_double, ctypes.c_double,
+                                        ctypes.c_double, ctypes.c_double, ctypes.c_int32, ctypes.c_uint64,
+                                        ctypes.c_int32, ctypes.POINTER(ctypes.c_int32),
+                                        ctypes.POINTER(_i64p), ctypes.POINTER(_i32p)]
+        L.orc_free.restype = None
+        L.orc_free.argtypes = [ctypes.c_void_p]
+        L.orc_seq_louvain.restype = ctypes.c_int32
+        L.orc_seq_louvain.argtypes = [ctypes.c_int32, _i64p, _i32p, _i32p, ctypes.c_double, ctypes.c_int32,
+                                      _i32p, _f64p, _i32p, ctypes.c_int32, _i64p]
 
     @staticmethod
     def _arrs(offs, nbr, w):
@@ -184,3 +194,39 @@ class Oracle:
 
     def q_from_sums(self, sum_in, sum_tot2, m2):
         return self.lib.orc_q_from_sums(sum_in, sum_tot2, m2)
+
+    def generate_rmat(self, scale, nedges, a=0.57, b=0.19, c=0.19, noise=0.0, keep_isolated=True, seed=1,
+                      nthreads=0):
+        """Seeded R-MAT graph built on the CPU (oracle/generators.c), identical
+        to the engine library's generator: (offs[n+1] with leading 0, nbr)."""
+        n = ctypes.c_int32()
+        po = _i64p()
+        pn = _i32p()
+        rc = self.lib.orc_generate_rmat(scale, nedges, a, b, c, noise, int(keep_isolated), seed, nthreads,
+                                        ctypes.byref(n), ctypes.byref(po), ctypes.byref(pn))
+        if rc != 0:
+            raise ValueError("orc_generate_rmat: bad arguments or out of memory")
+        try:
+            offs = np.ctypeslib.as_array(po, shape=(n.value + 1,)).copy()
+            e = int(offs[-1])
+            nbr = np.ctypeslib.as_array(pn, shape=(max(e, 1),))[:e].copy()
+        finally:
+            self.lib.orc_free(ctypes.cast(po, ctypes.c_void_p))
+            self.lib.orc_free(ctypes.cast(pn, ctypes.c_void_p))
+        return offs, nbr
+
+    def seq_louvain(self, offs, nbr, w=None, min_mod=1e-6, max_levels=0):
+        """The sequential (Blondel et al.) Louvain method on one thread."""
+        offs, nbr, w = self._arrs(offs, nbr, w)
+        n = offs.shape[0] - 1
+        comm = np.zeros(n, dtype=np.int32)
+        lq = np.zeros(64, dtype=np.float64)
+        lc = np.zeros(64, dtype=np.int32)
+        mv = ctypes.c_int64()
+        r = self.lib.orc_seq_louvain(n, _p(offs, _i64p), _p(nbr, _i32p), _p(w, _i32p), min_mod, max_levels,
+                                     _p(comm, _i32p), _p(lq, _f64p), _p(lc, _i32p), 64, ctypes.byref(mv))
+        if r < 0:
+            raise ValueError("orc_seq_louvain: bad input or out of memory")
+        k = min(r, 64)
+        return {"levels": r, "labels": comm, "level_q": lq[:k].tolist(), "level_c": lc[:k].tolist(),
+                "modularity": float(lq[k - 1]), "moves": mv.value}

@@ -29,11 +29,17 @@ def _dev(torch, a):
     return torch.from_numpy(np.ascontiguousarray(a)).cuda()
 
 
-@pytest.mark.parametrize("case", ["karate", "rmat_weighted"])
+@pytest.mark.parametrize("case", ["karate", "karate_heavy", "rmat_weighted"])
 def test_static_modularity_matches_host_two_calls(ffi, golden, torch_cuda, case):
     torch = torch_cuda
     if case == "karate":
         g = ffi.Graph.load_bin(os.path.join(golden, "karate.txt.bin"))
+    elif case == "karate_heavy":
+        # every weight 2^30: m2 = 156 * 2^30 > 2^32, so a community's Tot^2
+        # passes 2^64 and the sum of squares needs 128 bits
+        k = ffi.Graph.load_bin(os.path.join(golden, "karate.txt.bin"))
+        offs, nbr, _ = k.arrays()
+        g = ffi.Graph.from_csr(offs, nbr, np.full(nbr.shape[0], 1 << 30, dtype=np.int32))
     else:
         r = ffi.Graph.rmat(14, 120000, seed=13)
         offs, nbr, _ = r.arrays()
@@ -63,3 +69,28 @@ def test_static_modularity_rejects_oversized_graph(ffi, torch_cuda):
     with pytest.raises(ffi.GalaError) as e:
         ffi.modularity_device_static(n, d.data_ptr(), d.data_ptr(), None, d.data_ptr())
     assert e.value.status == 8
+
+
+def test_static_modularity_rejects_bad_labels_and_weights(ffi, golden, torch_cuda):
+    torch = torch_cuda
+    g = ffi.Graph.load_bin(os.path.join(golden, "karate.txt.bin"))
+    offs, nbr, _ = g.arrays()
+    n = offs.shape[0] - 1
+    d_offs, d_nbr = _dev(torch, offs), _dev(torch, nbr)
+    lab = np.arange(n, dtype=np.int32)
+    lab[5] = n  # outside [0, n)
+    with pytest.raises(ffi.GalaError) as e:
+        ffi.modularity_device_static(n, d_offs.data_ptr(), d_nbr.data_ptr(), None, _dev(torch, lab).data_ptr())
+    assert e.value.status == 1
+    w = np.ones(nbr.shape[0], dtype=np.int32)
+    w[3] = 0  # not positive
+    d_w = _dev(torch, w)
+    with pytest.raises(ffi.GalaError) as e:
+        ffi.modularity_device_static(n, d_offs.data_ptr(), d_nbr.data_ptr(), d_w.data_ptr(),
+                                     _dev(torch, np.arange(n, dtype=np.int32)).data_ptr())
+    assert e.value.status == 1
+    # the scratch is cleared on the next call: a valid call right after agrees
+    # with the host entry point again
+    lab = np.arange(n, dtype=np.int32) % 4
+    q = ffi.modularity_device_static(n, d_offs.data_ptr(), d_nbr.data_ptr(), None, _dev(torch, lab).data_ptr())
+    assert abs(q - g.modularity(lab)) < 1e-9
