@@ -74,6 +74,8 @@ def parse():
     p.add_argument("--threshold", type=float, default=0.3, help="proposal probability threshold")
     p.add_argument("--profile", action="store_true",
                    help="one device-resident run and a short summary (for ncu captures)")
+    p.add_argument("--profile-learned", action="store_true",
+                   help="one learned-proposal run (SKIP mode) after one plain run (for ncu launch lists)")
     p.add_argument("--fp64-gains", action="store_true", help="evaluate every gain in FP64")
     p.add_argument("--scale", type=int, default=0,
                    help="R-MAT scale of a smaller case of the same workload (raw samples scaled by 2^(scale-22))")
@@ -300,21 +302,32 @@ def learned_arm(ffi, ctx, g, stream, args, torch, plain_ms, plain):
     else:
         proposal_tool.train_on_rmat(prop, range(1000, 1008), [18, 19, 20], sample_shift=2, epochs=6, ctx=ctx)
         source = "trained in this run: 8 R-MAT graphs (scales 18-20, seeds 1000-1007)"
-    times, r = [], None
-    for i in range(args.warmup + args.steps):
-        torch.cuda.synchronize()
-        with torch.cuda.stream(stream):
-            a = torch.cuda.Event(enable_timing=True)
-            b = torch.cuda.Event(enable_timing=True)
-            a.record(stream)
-            r = ctx.louvain(g, proposal=prop, mode=ffi.PROPOSAL_SKIP, threshold=args.threshold)
-            b.record(stream)
-        torch.cuda.synchronize()
-        if i >= args.warmup:
-            times.append(a.elapsed_time(b))
-    ms = sum(times) / len(times)
+    def timed(threshold, steps):
+        times, r = [], None
+        for i in range(args.warmup + steps):
+            torch.cuda.synchronize()
+            with torch.cuda.stream(stream):
+                a = torch.cuda.Event(enable_timing=True)
+                b = torch.cuda.Event(enable_timing=True)
+                a.record(stream)
+                r = ctx.louvain(g, proposal=prop, mode=ffi.PROPOSAL_SKIP, threshold=threshold)
+                b.record(stream)
+            torch.cuda.synchronize()
+            if i >= args.warmup:
+                times.append(a.elapsed_time(b))
+        return sum(times) / len(times), r
+
+    ms, r = timed(args.threshold, args.steps)
+    # the proposal threshold against decisions, sweeps, time and final Q
+    curve = []
+    for th in (0.1, 0.2, 0.3, 0.4, 0.5):
+        tms, tr = timed(th, min(args.steps, 3))
+        curve.append({"threshold": th, "ms": tms, "time_vs_plain": tms / plain_ms, "decisions": tr["decisions"],
+                      "skipped": tr["skipped"], "sweeps": tr["total_iterations"],
+                      "verify_sweeps": tr["verify_sweeps"], "dq_vs_plain": tr["modularity"] - plain["modularity"]})
     prop.close()
     return {"mode": "skip", "threshold": args.threshold, "weights": source, "ms_per_step": ms,
+            "threshold_curve": curve,
             "time_vs_plain": ms / plain_ms, "modularity": r["modularity"],
             "dq_vs_plain": r["modularity"] - plain["modularity"], "decisions": r["decisions"],
             "plain_decisions": plain["decisions"], "skipped": r["skipped"], "verify_sweeps": r["verify_sweeps"],
@@ -402,7 +415,9 @@ def weighted_arm(ffi, args, torch, device):
     q_host = g.modularity(r["labels"])
     return {"config": dict(c, edges=m, csr_entries=e, generation_s=gen_s),
             "metric": "end-to-end Louvain edges/s (float weights, all rounds to dQ<1e-6)", "value": m / sec,
-            "unit": "edges/s", "seconds": sec, "device_ms": r["time_total_ms"], "steps": steps, "warmup": 1,
+            "unit": "edges/s", "seconds": sec, "seconds_each": times, "device_ms": r["time_total_ms"],
+            "h2d_ms": r["time_h2d_ms"], "d2h_ms": r["time_d2h_ms"], "host_ms": r["host_ms"], "steps": steps,
+            "warmup": 1,
             "phase_ms": {"decide": r["time_decide_ms"], "update": r["time_update_ms"],
                          "contract": r["time_contract_ms"]},
             "modularity": r["modularity"], "modularity_host_fp64": q_host,
@@ -460,7 +475,10 @@ def batch_arm(ffi, args, torch, device):
     seq_est = st / len(sample) * b["graphs"]
     return {"config": dict(b, vertices=sum(ns), edges=m, max_vertices=max(ns), min_vertices=min(ns)),
             "metric": "batched Louvain edges/s (host graphs in, labels out)", "value": m / sec, "unit": "edges/s",
-            "seconds": sec, "device_ms": r["time_total_ms"], "phase1_ms": r["time_phase1_ms"],
+            "seconds": sec, "device_ms": r["time_total_ms"], "h2d_ms": r["time_h2d_ms"], "d2h_ms": r["time_d2h_ms"],
+            "input": "host graphs (not page-locked): raw copies into the context's pinned staging, one transfer, "
+                     "ids shifted on the device",
+            "phase1_ms": r["time_phase1_ms"],
             "contract_ms": r["time_contract_ms"], "levels": r["num_levels"], "iterations": r["total_iterations"],
             "kernel_launches": r["kernel_launches"], "tuning": tuning, "cuda_graphs": True,
             "sequential_single_runs_s_est": seq_est, "speedup_vs_sequential": seq_est / sec,
@@ -507,6 +525,20 @@ def main():
         return ctx.louvain_device(n, d_offs.data_ptr(), d_nbr.data_ptr(), None, d_out.data_ptr(),
                                   fp64_gains=args.fp64_gains, distinct_rows=True)
 
+    if args.profile_learned:
+        import numpy as np
+        prop = ffi.Proposal(max_samples=1 << 16, seed=7)
+        prop.set_params(np.load(WEIGHTS))
+        r0 = ctx.louvain(g)
+        r = ctx.louvain(g, proposal=prop, mode=ffi.PROPOSAL_SKIP, threshold=args.threshold)
+        torch.cuda.synchronize()
+        print(json.dumps({"profile_learned": wl["workload"], "plain_ms": r0["time_total_ms"],
+                          "learned_ms": r["time_total_ms"], "decisions": r["decisions"],
+                          "plain_decisions": r0["decisions"], "sweeps": r["total_iterations"],
+                          "plain_sweeps": r0["total_iterations"]}), flush=True)
+        prop.close()
+        ctx.close()
+        return
     if args.profile:
         r = run_device()
         torch.cuda.synchronize()
@@ -588,7 +620,8 @@ def main():
     contract_roof = contraction_roofline(runs, peak, peak_kind)
     cfg = workload_config(wl, n, E, max_deg, world)
     e2e = {"value": world * m / (e2e_step / 1000.0), "unit": "edges/s", "ms_per_step": e2e_step,
-           "h2d_bytes_per_step": r_e2e["h2d_bytes"], "d2h_bytes_per_step": r_e2e["d2h_bytes"]}
+           "h2d_bytes_per_step": r_e2e["h2d_bytes"], "d2h_bytes_per_step": r_e2e["d2h_bytes"],
+           "h2d_ms": r_e2e["time_h2d_ms"], "d2h_ms": r_e2e["time_d2h_ms"], "host_ms": r_e2e["host_ms"]}
     # bulky secondary arms first, the headline keys after them (the end of
     # the line is what a truncated log keeps)
     line = {}

@@ -124,7 +124,104 @@ __global__ void k_gid_fill(int G, const int64_t *__restrict__ goff, int32_t *gid
 
 int grid_for(int G) { return G < 65535 ? G : 65535; }
 
+// Union CSR of page-locked host graphs, read by the GPU through their
+// device-mapped addresses: one block per graph shifts the graph's offsets by
+// its first entry and its neighbour ids by its first vertex.  Four loads in
+// flight per thread (host memory behind the chip-to-chip link has a long
+// latency).
+__global__ void __launch_bounds__(256) k_batch_gather(int G, BatchSrc s, int64_t *offs, int32_t *nbr, int32_t *w)
+{
+    if (blockIdx.x == 0 && threadIdx.x == 0) offs[0] = 0;
+    for (int g = blockIdx.x; g < G; g += gridDim.x) {
+        const long long v0 = s.vstart[g], n = s.vstart[g + 1] - v0;
+        const long long e0 = s.estart[g], E = s.estart[g + 1] - e0;
+        const int64_t *so = s.offs[g];
+        const int32_t *sn = s.nbr[g];
+        const int32_t *sw = s.w[g];
+        const int32_t shift = (int32_t)v0;
+        for (long long v = threadIdx.x; v < n; v += blockDim.x) offs[v0 + v + 1] = e0 + so[v];
+        constexpr int U = 4;
+        for (long long j0 = 0; j0 < E; j0 += (long long)U * blockDim.x) {
+            int32_t t[U];
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                const long long j = j0 + u * blockDim.x + threadIdx.x;
+                t[u] = j < E ? sn[j] : 0;
+            }
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                const long long j = j0 + u * blockDim.x + threadIdx.x;
+                if (j < E) nbr[e0 + j] = t[u] + shift;
+            }
+        }
+        if (w) {
+            for (long long j0 = 0; j0 < E; j0 += (long long)U * blockDim.x) {
+                int32_t t[U];
+#pragma unroll
+                for (int u = 0; u < U; ++u) {
+                    const long long j = j0 + u * blockDim.x + threadIdx.x;
+                    t[u] = (j < E && sw) ? sw[j] : 1;
+                }
+#pragma unroll
+                for (int u = 0; u < U; ++u) {
+                    const long long j = j0 + u * blockDim.x + threadIdx.x;
+                    if (j < E) w[e0 + j] = t[u];
+                }
+            }
+        }
+    }
+}
+
+// In-place shift of a union CSR whose per-graph parts were copied raw:
+// graph g's inclusive offsets (at offs[vstart[g]+1 ...]) by its first entry,
+// its neighbour ids by its first vertex.
+__global__ void __launch_bounds__(256) k_batch_shift(int G, const int64_t *__restrict__ vstart,
+                                                     const int64_t *__restrict__ estart, int64_t *offs, int32_t *nbr)
+{
+    if (blockIdx.x == 0 && threadIdx.x == 0) offs[0] = 0;
+    for (int g = blockIdx.x; g < G; g += gridDim.x) {
+        const long long v0 = vstart[g], v1 = vstart[g + 1], e0 = estart[g], e1 = estart[g + 1];
+        const int32_t shift = (int32_t)v0;
+        if (e0 != 0)
+            for (long long v = v0 + threadIdx.x; v < v1; v += blockDim.x) offs[v + 1] += e0;
+        if (shift != 0)
+            for (long long j = e0 + threadIdx.x; j < e1; j += blockDim.x) nbr[j] += shift;
+    }
+}
+
+// Union community ids -> ids local to each graph (graph g's vertices are
+// [vstart[g], vstart[g+1]) of the input; its communities start at goff[g]).
+__global__ void k_batch_local_labels(int G, const int64_t *__restrict__ vstart, const int64_t *__restrict__ goff,
+                                     int32_t *labels)
+{
+    for (int g = blockIdx.x; g < G; g += gridDim.x) {
+        const int32_t base = (int32_t)goff[g];
+        for (long long v = vstart[g] + threadIdx.x; v < vstart[g + 1]; v += blockDim.x) labels[v] -= base;
+    }
+}
+
 }  // namespace
+
+void batch_gather(int G, const BatchSrc &src, int64_t *offs, int32_t *nbr, int32_t *w, cudaStream_t st)
+{
+    if (G <= 0) return;
+    k_batch_gather<<<grid_for(G), 256, 0, st>>>(G, src, offs, nbr, w);
+    note_launch(1);
+}
+
+void batch_shift(int G, const int64_t *vstart, const int64_t *estart, int64_t *offs, int32_t *nbr, cudaStream_t st)
+{
+    if (G <= 0) return;
+    k_batch_shift<<<grid_for(G), 256, 0, st>>>(G, vstart, estart, offs, nbr);
+    note_launch(1);
+}
+
+void batch_local_labels(int G, const int64_t *vstart, const int64_t *goff, int32_t *labels, cudaStream_t st)
+{
+    if (G <= 0) return;
+    k_batch_local_labels<<<grid_for(G), 256, 0, st>>>(G, vstart, goff, labels);
+    note_launch(1);
+}
 
 void batch_graph_sums(int what, int G, const int64_t *goff, const uint8_t *stop, const Phase1Buffers &b,
                       const GraphSums &out, cudaStream_t st)

@@ -182,6 +182,50 @@ __device__ __forceinline__ void for_entries(const int64_t *offs, const long long
     }
 }
 
+// for_entries with two per-row values: when the window moves, lane l loads
+// pa/pb of window row vbase + l once (rowval(row, &pa, &pb), row < n), and
+// every entry of that row receives them by a shuffle instead of gathering
+// them itself.  f(j, row, pa, pb) is called for every entry of [j0, j1);
+// all 32 lanes of the warp must call.
+template <typename RV, typename F>
+__device__ __forceinline__ void for_entries_rows(const long long *offs_ll, int n, long long j0, long long j1,
+                                                 RV rowval, F f)
+{
+    const int lane = threadIdx.x & 31;
+    RowWindow w{nullptr, offs_ll, n, 0, 0};
+    long long pa = 0, pb = 0;
+    auto load = [&]() {
+        w.load();
+        const int r = w.vbase + lane;
+        pa = -1;  // rows outside [0, n) keep (-1, 0): the callers record them
+        pb = 0;
+        if (r < n) rowval(r, pa, pb);
+    };
+    w.vbase = owner_row(nullptr, offs_ll, n, j0);
+    load();
+    for (long long jb = j0; jb < j1; jb += 32) {
+        const int adv = w.count_le(jb);
+        if (adv > 0) {
+            w.vbase += adv;
+            load();
+        }
+        const long long j = jb + lane;
+        bool done = j >= j1;
+        while (!__all_sync(GALA_FULL_MASK, done)) {
+            const int idx = w.count_le(j);
+            const bool here = !done && idx < 32;
+            const long long a = __shfl_sync(GALA_FULL_MASK, pa, idx & 31);
+            const long long b = __shfl_sync(GALA_FULL_MASK, pb, idx & 31);
+            if (here) f(j, w.vbase + idx, a, b);
+            done = done || here;
+            if (!__all_sync(GALA_FULL_MASK, done)) {
+                w.vbase += 32;
+                load();
+            }
+        }
+    }
+}
+
 // Caller-supplied labels must lie in [0, n) before they index any array.
 __global__ void k_check_labels(const int32_t *__restrict__ comm, int n, DevStats *st)
 {
@@ -237,7 +281,8 @@ __global__ void k_member_scatter(const int32_t *__restrict__ lab, const int64_t 
 
 // Community-ordered edge stream over contiguous entry ranges: entry j of row
 // v goes to medge[mpos[v]] + (j - offs[v]).  Rows are walked through the
-// list of rows with entries (nz_rows / nz_offs).
+// list of rows with entries (nz_rows / nz_offs); each row's destination
+// (medge[mpos[v]] - offs[v]) is loaded once per row window.
 template <typename WT, bool W>
 __global__ void __launch_bounds__(256) k_stream_fill(int n, long long E, const int64_t *__restrict__ offs,
                                                      const int32_t *__restrict__ nbr, const WT *__restrict__ w,
@@ -250,17 +295,20 @@ __global__ void __launch_bounds__(256) k_stream_fill(int n, long long E, const i
     const long long wg = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
     const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
     const int nnz = st->nz_rows;
+    // per row: pa = destination of the row's entry j minus j, pb = 1 when the
+    // row id is valid
+    auto rowval = [&](int r, long long &pa, long long &pb) {
+        const int v = nz_rows[r];
+        if (v < 0 || v >= n) return;
+        pa = medge[mpos[v]] - offs[v];
+        pb = 1;
+    };
     for (long long t = wg; t * kRangeEntries < E; t += nw) {
         const long long j0 = t * kRangeEntries;
         const long long j1 = j0 + kRangeEntries < E ? j0 + kRangeEntries : E;
-        for_entries(nullptr, nz_offs, nnz, j0, j1, [&](long long j, int r) {
-            const int v = (r >= 0 && r < nnz) ? nz_rows[r] : -1;
-            if (v < 0 || v >= n) {  // recorded, never written
-                atomicOr(&st->err, kErrBadIndex);
-                return;
-            }
-            const long long dst = medge[mpos[v]] + (j - offs[v]);
-            if (dst < 0 || dst >= E) {
+        for_entries_rows(nz_offs, nnz, j0, j1, rowval, [&](long long j, int, long long d, long long ok) {
+            const long long dst = j + d;
+            if (!ok || dst < 0 || dst >= E) {  // recorded, never written
                 atomicOr(&st->err, kErrBadIndex);
                 return;
             }
@@ -952,7 +1000,8 @@ __global__ void __launch_bounds__(1024) k_big_sort(AggArgs<WT> a, BigArgs b)
 }
 
 // Compaction over contiguous output ranges: output entry j of community c
-// comes from tmp_off[c] + (j - new_offs[c]).
+// comes from tmp_off[c] + (j - new_offs[c]); c and that shift are loaded once
+// per row window.
 template <typename WT>
 __global__ void __launch_bounds__(256) k_compact(int C, long long Enew, const int64_t *__restrict__ new_offs,
                                                  const long long *__restrict__ tmp_off,
@@ -965,17 +1014,19 @@ __global__ void __launch_bounds__(256) k_compact(int C, long long Enew, const in
     const long long wg = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
     const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
     const int nnz = st->nz_rows;
+    // per row: pa = the community (-1 when out of range), pb = source shift
+    auto rowval = [&](int r, long long &pa, long long &pb) {
+        const int c = nz_rows[r];
+        if (c < 0 || c >= C) return;
+        pa = c;
+        pb = tmp_off[c] - new_offs[c];
+    };
     for (long long t = wg; t * kRangeEntries < Enew; t += nw) {
         const long long j0 = t * kRangeEntries;
         const long long j1 = j0 + kRangeEntries < Enew ? j0 + kRangeEntries : Enew;
-        for_entries(nullptr, nz_offs, nnz, j0, j1, [&](long long j, int r) {
-            const int c = (r >= 0 && r < nnz) ? nz_rows[r] : -1;
-            if (c < 0 || c >= C) {  // recorded, never read or written
-                atomicOr(&st->err, kErrBadIndex);
-                return;
-            }
-            const long long src = tmp_off[c] + (j - new_offs[c]);
-            if (src < 0 || src >= tmp_cap) {
+        for_entries_rows(nz_offs, nnz, j0, j1, rowval, [&](long long j, int, long long c, long long d) {
+            const long long src = j + d;
+            if (c < 0 || src < 0 || src >= tmp_cap) {  // recorded, never read or written
                 atomicOr(&st->err, kErrBadIndex);
                 return;
             }
@@ -1065,7 +1116,7 @@ static int grid_cap(long long items, int per_block, int cap)
 static void build_walk_list(const int64_t *offs, int n, long long E, ContractBuffers &b, cudaStream_t st)
 {
     const int cap = sm_count() * 8;
-    exclusive_scan(offs, b.nz_pos, n, OpRowNonEmpty{offs}, b.scan_partial, &b.stats->total, st);
+    exclusive_scan(offs, b.nz_pos, n, OpRowNonEmpty{offs}, b.scan_partial, &b.stats->total, st, &b.stats->err);
     k_nz_tail<<<1, 1, 0, st>>>(b.stats, b.nz_offs, E);
     k_nz_scatter<<<grid_cap(n, 256, cap), 256, 0, st>>>(offs, n, b.nz_pos, b.nz_rows, b.nz_offs);
     note_launch(2);
@@ -1108,9 +1159,9 @@ static bool contract_long_rows(const AggArgs<WT> &a, ContractBuffers &b, int cnt
     ba.gofs = b.big_gofs;
     ba.pool = b.big_pool;
     k_big_plan<WT><<<grid_cap(cnt3, 256, cap), 256, 0, st>>>(a, ba);
-    exclusive_scan(b.big_T, b.big_toff, cnt3, OpIdentity(), b.scan_partial, &b.stats->total, st);
-    exclusive_scan(b.big_chunks, b.big_coff, cnt3, OpIdentity(), b.scan_partial, &b.stats->total2, st);
-    exclusive_scan(b.big_tchunks, b.big_tcoff, cnt3, OpIdentity(), b.scan_partial, &b.stats->total3, st);
+    exclusive_scan(b.big_T, b.big_toff, cnt3, OpIdentity(), b.scan_partial, &b.stats->total, st, &b.stats->err);
+    exclusive_scan(b.big_chunks, b.big_coff, cnt3, OpIdentity(), b.scan_partial, &b.stats->total2, st, &b.stats->err);
+    exclusive_scan(b.big_tchunks, b.big_tcoff, cnt3, OpIdentity(), b.scan_partial, &b.stats->total3, st, &b.stats->err);
     k_big_tail<<<1, 1, 0, st>>>(ba, b.stats);
     note_launch(2);
     if (!read_stats(&hs, b.stats, st, status, "contraction: long rows")) return false;
@@ -1135,7 +1186,7 @@ static bool contract_long_rows(const AggArgs<WT> &a, ContractBuffers &b, int cnt
         // rows in table order: collect from the slot lists, no table scans
         long long *lch = b.big_tchunks, *lcoff = b.big_tcoff;
         k_big_lchunks<<<grid_cap(cnt3, 256, cap), 256, 0, st>>>(ba.cursor, cnt3, lch);
-        exclusive_scan(lch, lcoff, cnt3, OpIdentity(), b.scan_partial, &b.stats->total3, st);
+        exclusive_scan(lch, lcoff, cnt3, OpIdentity(), b.scan_partial, &b.stats->total3, st, &b.stats->err);
         k_big_collect_list<WT><<<(int)(nwork < nsm * 8 ? nwork : nsm * 8), 256, 0, st>>>(a, ba, lcoff,
                                                                                           &b.stats->total3);
         k_big_len<WT><<<grid_cap(cnt3, 256, cap), 256, 0, st>>>(a, ba);
@@ -1143,7 +1194,7 @@ static bool contract_long_rows(const AggArgs<WT> &a, ContractBuffers &b, int cnt
         return true;
     }
     k_big_mark<WT><<<grid_cap(cnt3, 256, cap), 256, 0, st>>>(a, ba, sort_rows ? 1 : 0);
-    exclusive_scan(b.big_gwords, b.big_gofs, cnt3, OpIdentity(), b.scan_partial, &b.stats->total, st);
+    exclusive_scan(b.big_gwords, b.big_gofs, cnt3, OpIdentity(), b.scan_partial, &b.stats->total, st, &b.stats->err);
     note_launch(3);
     if (!read_stats(&hs, b.stats, st, status, "contraction: long-row bitmaps")) return false;
     const long long words = hs.total;
@@ -1159,7 +1210,7 @@ static bool contract_long_rows(const AggArgs<WT> &a, ContractBuffers &b, int cnt
     k_big_collect<WT><<<tgrid, 256, 0, st>>>(a, ba, ntwork);
     note_launch(1);
     if (words > 0) {
-        exclusive_scan(ba.bits, ba.pref, words, OpPopc(), b.scan_partial, &b.stats->total, st);
+        exclusive_scan(ba.bits, ba.pref, words, OpPopc(), b.scan_partial, &b.stats->total, st, &b.stats->err);
         k_big_rank<WT><<<tgrid, 256, 0, st>>>(a, ba, ntwork);
         note_launch(1);
     }
@@ -1198,7 +1249,7 @@ static int contract_t(const LevelGraph &g, const int32_t *comm, ContractBuffers 
     }
     cudaMemsetAsync(b.cnt, 0, ((size_t)n + 1) * sizeof(int32_t), st);
     k_hist<<<grid_cap(n, 256, cap), 256, 0, st>>>(comm, n, b.cnt);
-    exclusive_scan(b.cnt, b.newid, n, OpPositive(), b.scan_partial, &b.stats->total, st);
+    exclusive_scan(b.cnt, b.newid, n, OpPositive(), b.scan_partial, &b.stats->total, st, &b.stats->err);
     note_launch(1);
     if (!read_stats(&hs, b.stats, st, status, "contraction: community count")) return -1;
     const int C = (int)hs.total;
@@ -1212,11 +1263,11 @@ static int contract_t(const LevelGraph &g, const int32_t *comm, ContractBuffers 
         *new_E = 0;
         return C;
     }
-    exclusive_scan(b.csz, b.moff, C, OpIdentity(), b.scan_partial, &b.stats->total, st);
+    exclusive_scan(b.csz, b.moff, C, OpIdentity(), b.scan_partial, &b.stats->total, st, &b.stats->err);
     cudaMemcpyAsync(b.cursor, b.moff, (size_t)C * sizeof(int32_t), cudaMemcpyDeviceToDevice, st);
     cudaMemsetAsync(b.ec, 0, ((size_t)C + 1) * sizeof(long long), st);
     k_member_scatter<<<grid_cap(n, 256, cap), 256, 0, st>>>(b.lab, g.offs, n, b.cursor, b.members, b.mpos, b.ec);
-    exclusive_scan(b.members, b.medge, n, OpDegOf{g.offs}, b.scan_partial, &b.stats->total, st);
+    exclusive_scan(b.members, b.medge, n, OpDegOf{g.offs}, b.scan_partial, &b.stats->total, st, &b.stats->err);
     // moff[C] = n and medge[n] = E close the last segments
     k_contract_set_tail<<<1, 1, 0, st>>>(b.moff, C, n, b.medge, g.E);
     const int fill_grid = grid_cap((g.E + kRangeEntries - 1) / kRangeEntries * 32, 256, cap);
@@ -1233,7 +1284,7 @@ static int contract_t(const LevelGraph &g, const int32_t *comm, ContractBuffers 
                                                                b.nz_offs, b.stats);
     }
     k_classify<<<grid_cap(C, 256, cap), 256, 0, st>>>(C, b.ec, b.cls_list, b.kc, b.stats, sort_rows ? 1 : 0);
-    exclusive_scan(b.ec, b.tmp_off, C, OpCap{C}, b.scan_partial, &b.stats->total, st);
+    exclusive_scan(b.ec, b.tmp_off, C, OpCap{C}, b.scan_partial, &b.stats->total, st, &b.stats->err);
     note_launch(6 + (orig_map ? 1 : 0));
     if (!read_stats(&hs, b.stats, st, status, "contraction: classification")) return -1;
 
@@ -1278,7 +1329,7 @@ static int contract_t(const LevelGraph &g, const int32_t *comm, ContractBuffers 
     if (hs.small_cnt[kLongCls] > 0 &&
         !contract_long_rows(a, b, hs.small_cnt[kLongCls], C, hs, st, status, sort_rows))
         return -1;
-    exclusive_scan(b.kc, new_offs, C, OpIdentity(), b.scan_partial, &b.stats->total, st);
+    exclusive_scan(b.kc, new_offs, C, OpIdentity(), b.scan_partial, &b.stats->total, st, &b.stats->err);
     k_set_last_offset<<<1, 1, 0, st>>>(new_offs, C, &b.stats->total);
     note_launch(1);
     if (!read_stats(&hs, b.stats, st, status, "contraction: offsets")) return -1;

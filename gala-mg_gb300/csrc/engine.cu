@@ -12,6 +12,7 @@
 
 #include <algorithm>
 #include <atomic>
+#include <chrono>
 #include <thread>
 #include <type_traits>
 #include <vector>
@@ -20,6 +21,10 @@
 #include "internal.h"
 
 using namespace gala;
+
+namespace {
+struct BatchRun;
+}
 
 struct gala_context {
     int device = 0;
@@ -46,6 +51,9 @@ struct gala_context {
     cudaEvent_t ev[8] = {};
     // slots of the largest hub table (gala_context_set_hub_table_cap; 0 = by degree)
     long long hub_table_cap = 0;
+    // per-graph state of gala_louvain_batch, kept between calls (reallocated
+    // only for a larger batch)
+    BatchRun *batch = nullptr;
     // the degree bins of one sweep are independent: they run concurrently on
     // auxiliary streams, forked from and joined back into `stream`
     static constexpr int kAux = 4;
@@ -202,6 +210,18 @@ struct BatchRun {
     int32_t *h_ncomm = nullptr;
     uint8_t *h_stop = nullptr, *h_reject = nullptr;
     int64_t *h_goff = nullptr;
+    // source table of the input graphs, 5G+2 words: device-mapped offsets,
+    // neighbour and weight addresses (G each), then the first vertex and the
+    // first entry of every graph in the union (G+1 each); pinned host copy
+    // and device copy
+    int64_t *h_tab = nullptr, *tab = nullptr;
+    int cap = 0;       // graphs the per-graph arrays hold
+    int n_cap = 0;     // vertices gid / gid2 hold
+    // pinned staging of the raw graph arrays (graphs that are not
+    // page-locked): the context's vertex and entry capacity
+    int64_t *h_offs = nullptr;
+    int32_t *h_nbr = nullptr, *h_w = nullptr;
+    std::vector<void *> stage;
     // per-graph host state
     std::vector<long long> m2;
     std::vector<double> prev_q;  // accepted Q of the current level
@@ -209,10 +229,29 @@ struct BatchRun {
     std::vector<char> finished;  // no further round
     std::vector<void *> dev, host;
     GraphSums sums() const { return GraphSums{sum_in, sum_tot2, sum_k, min_tot, ncomm}; }
-    ~BatchRun()
+    int64_t *h_vstart() const { return h_tab + 3LL * cap; }
+    int64_t *h_estart() const { return h_tab + 4LL * cap + 1; }
+    int64_t *vstart() const { return tab + 3LL * cap; }
+    int64_t *estart() const { return tab + 4LL * cap + 1; }
+    BatchSrc src() const
+    {
+        return BatchSrc{(const int64_t *const *)tab, (const int32_t *const *)(tab + cap),
+                        (const int32_t *const *)(tab + 2LL * cap), tab + 3LL * cap, tab + 4LL * cap + 1};
+    }
+    void release()
     {
         for (void *p : dev) cudaFree(p);
         for (void *p : host) cudaFreeHost(p);
+        dev.clear();
+        host.clear();
+        cap = n_cap = 0;
+    }
+    void release_stage()
+    {
+        for (void *p : stage) cudaFreeHost(p);
+        stage.clear();
+        h_offs = nullptr;
+        h_nbr = h_w = nullptr;
     }
 };
 
@@ -963,6 +1002,11 @@ void gala_context_destroy(gala_context *ctx)
     cudaGetDevice(&prev);
     cudaSetDevice(ctx->device);
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    if (ctx->batch) {
+        ctx->batch->release();
+        ctx->batch->release_stage();
+        delete ctx->batch;
+    }
     for (void *p : ctx->allocs) cudaFree(p);
     if (ctx->h_stats) cudaFreeHost(ctx->h_stats);
     for (auto &e : ctx->ev)
@@ -1158,6 +1202,10 @@ gala_status gala_louvain(gala_context *ctx, const gala_graph *g, const gala_opti
     }
     long long l0 = gala_kernel_launch_count();
     cudaStream_t st = ctx->stream;
+    const auto host0 = std::chrono::steady_clock::now();
+    auto host_ms = [&]() {
+        return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - host0).count();
+    };
     // host -> device: offsets with a leading 0, neighbours, weights
     cudaEventRecord(ctx->ev[6], st);
     cudaMemsetAsync(ctx->offs[1], 0, sizeof(int64_t), st);
@@ -1179,8 +1227,10 @@ gala_status gala_louvain(gala_context *ctx, const gala_graph *g, const gala_opti
         return s;
     }
     float h2d = ev_ms(ctx->ev[6], ctx->ev[7]);
+    const double t_h2d = host_ms();
     // level 0 lives in buffer 1; the first contraction writes buffer 0
     s = run_levels(ctx, n, E, ctx->offs[1], ctx->nbr[1], dw, opt, res, nullptr, g->float_w, g->rows_distinct);
+    const double t_run = host_ms();
     if (s == GALA_OK) {
         cudaEventRecord(ctx->ev[6], st);
         cudaMemcpyAsync(community_out, ctx->orig, (size_t)n * sizeof(int32_t), cudaMemcpyDeviceToHost, st);
@@ -1188,6 +1238,11 @@ gala_status gala_louvain(gala_context *ctx, const gala_graph *g, const gala_opti
         s = sync_check(st, "device to host copy");
         res->time_d2h_ms = ev_ms(ctx->ev[6], ctx->ev[7]);
     }
+    const double t_end = host_ms();
+    res->host_total_ms = t_end;
+    res->host_h2d_ms = t_h2d;
+    res->host_run_ms = t_run - t_h2d;
+    res->host_d2h_ms = t_end - t_run;
     res->time_h2d_ms = h2d;
     res->h2d_bytes = (long long)n * 8 + E * 4 + ((g->weighted || g->float_w) ? E * 4 : 0);
     res->d2h_bytes = (long long)n * 4;
@@ -1337,30 +1392,111 @@ gala_status gala_louvain_batch(gala_context *ctx, const gala_graph *const *graph
     cudaStream_t st = ctx->stream;
     const int G = count;
     const int32_t n = (int32_t)n_tot;
-    // union CSR on the host (device layout: leading 0, ids shifted per graph)
-    std::vector<int64_t> offs((size_t)n + 1);
-    std::vector<int32_t> nbr((size_t)e_tot);
-    std::vector<int32_t> w(weighted ? (size_t)e_tot : 0);
-    std::vector<int64_t> vstart((size_t)G + 1), estart((size_t)G + 1);
-    vstart[0] = estart[0] = 0;
-    for (int i = 0; i < G; ++i) {
-        vstart[i + 1] = vstart[i] + graphs[i]->n;
-        estart[i + 1] = estart[i] + graphs[i]->entries();
+    // per-graph state, kept in the context between calls
+    if (!ctx->batch) ctx->batch = new BatchRun();
+    BatchRun &bt = *ctx->batch;
+    if (bt.cap < G || bt.n_cap < ctx->n_cap) {
+        if ((s = sync_check(st, "batch state"))) return s;
+        bt.release();
+        bool ok = true;
+        auto dal = [&](auto **p, size_t cnt) {
+            void *q = nullptr;
+            if (ok && cudaMalloc(&q, (cnt ? cnt : 1) * sizeof(**p)) == cudaSuccess) {
+                bt.dev.push_back(q);
+                *p = (std::remove_reference_t<decltype(*p)>)q;
+            } else {
+                ok = false;
+            }
+        };
+        auto hal = [&](auto **p, size_t cnt) {
+            void *q = nullptr;
+            if (ok && cudaMallocHost(&q, (cnt ? cnt : 1) * sizeof(**p)) == cudaSuccess) {
+                bt.host.push_back(q);
+                *p = (std::remove_reference_t<decltype(*p)>)q;
+            } else {
+                ok = false;
+            }
+        };
+        const size_t nc = (size_t)ctx->n_cap;
+        dal(&bt.gid, nc);
+        dal(&bt.gid2, nc);
+        dal(&bt.m2g, G);
+        dal(&bt.cg, G);
+        dal(&bt.stop, G);
+        dal(&bt.reject, G);
+        dal(&bt.min_tot, G);
+        dal(&bt.ncomm, G);
+        dal(&bt.sum_in, G);
+        dal(&bt.sum_tot2, G);
+        dal(&bt.sum_k, G);
+        dal(&bt.goff, (size_t)G + 1);
+        dal(&bt.tab, 5 * (size_t)G + 2);
+        hal(&bt.h_sum_in, G);
+        hal(&bt.h_sum_tot2, G);
+        hal(&bt.h_sum_k, G);
+        hal(&bt.h_ncomm, G);
+        hal(&bt.h_stop, G);
+        hal(&bt.h_reject, G);
+        hal(&bt.h_goff, (size_t)G + 1);
+        hal(&bt.h_tab, 5 * (size_t)G + 2);
+        if (!ok) {
+            cudaGetLastError();
+            bt.release();
+            set_error("gala_louvain_batch: allocation of the per-graph state failed (%d graphs)", G);
+            return GALA_ERR_OOM;
+        }
+        bt.cap = G;
+        bt.n_cap = ctx->n_cap;
     }
-    offs[0] = 0;
-    {
+    bt.G = G;
+    bt.m2.clear();
+    bt.prev_q.clear();
+    bt.finished.assign(G, 0);
+    bt.prev_mod.assign(G, -1.0);
+    bt.cur_mod.assign(G, -1.0);
+    int64_t *vstart = bt.h_vstart(), *estart = bt.h_estart();
+    vstart[0] = estart[0] = 0;
+    bool mapped = true;  // every graph readable in place by the GPU (gala_graph_pin)
+    for (int i = 0; i < G; ++i) {
+        const gala_graph *gg = graphs[i];
+        vstart[i + 1] = vstart[i] + gg->n;
+        estart[i + 1] = estart[i] + gg->entries();
+        mapped = mapped && gg->dev_offs && (gg->entries() == 0 || gg->dev_nbr) && (!gg->weighted || gg->dev_w);
+    }
+    memcpy(bt.h_goff, vstart, ((size_t)G + 1) * sizeof(int64_t));
+    if (!mapped) {
+        // raw copies of every graph into the context's pinned staging, one
+        // transfer of it, ids and offsets shifted on the device
+        if (!bt.h_offs || (weighted && !bt.h_w)) {
+            if ((s = sync_check(st, "batch staging"))) return s;
+            bt.release_stage();
+            void *a = nullptr, *b2 = nullptr, *c = nullptr;
+            const size_t nc = (size_t)ctx->n_cap + 1, ec = (size_t)std::max<int64_t>(ctx->e_cap, 1);
+            if (cudaMallocHost(&a, nc * sizeof(int64_t)) != cudaSuccess ||
+                (bt.stage.push_back(a), cudaMallocHost(&b2, ec * sizeof(int32_t)) != cudaSuccess) ||
+                (bt.stage.push_back(b2), weighted && cudaMallocHost(&c, ec * sizeof(int32_t)) != cudaSuccess)) {
+                cudaGetLastError();
+                bt.release_stage();
+                set_error("gala_louvain_batch: pinned staging of %lld entries failed", (long long)ctx->e_cap);
+                return GALA_ERR_OOM;
+            }
+            if (c) bt.stage.push_back(c);
+            bt.h_offs = (int64_t *)a;
+            bt.h_nbr = (int32_t *)b2;
+            bt.h_w = (int32_t *)c;
+        }
         std::atomic<int> next{0};
         auto copy = [&] {
             for (int i = next++; i < G; i = next++) {
                 const gala_graph *gg = graphs[i];
                 const long long v0 = vstart[i], e0 = estart[i], E = gg->entries();
-                for (int v = 0; v < gg->n; ++v) offs[v0 + v + 1] = e0 + gg->offs[v];
-                for (long long j = 0; j < E; ++j) nbr[e0 + j] = (int32_t)(gg->nbr[j] + v0);
+                memcpy(bt.h_offs + v0 + 1, gg->offs.data(), (size_t)gg->n * sizeof(int64_t));
+                if (E) memcpy(bt.h_nbr + e0, gg->nbr.data(), (size_t)E * sizeof(int32_t));
                 if (weighted) {
                     if (gg->weighted)
-                        memcpy(w.data() + e0, gg->w.data(), (size_t)E * sizeof(int32_t));
+                        memcpy(bt.h_w + e0, gg->w.data(), (size_t)E * sizeof(int32_t));
                     else
-                        std::fill(w.begin() + e0, w.begin() + e0 + E, 1);
+                        std::fill(bt.h_w + e0, bt.h_w + e0 + E, 1);
                 }
             }
         };
@@ -1370,64 +1506,30 @@ gala_status gala_louvain_batch(gala_context *ctx, const gala_graph *const *graph
         for (int t = 1; t < nt; ++t) th.emplace_back(copy);
         copy();
         for (auto &x : th) x.join();
-    }
-    BatchRun bt;
-    bt.G = G;
-    bool ok = true;
-    auto dal = [&](auto **p, size_t cnt) {
-        void *q = nullptr;
-        if (ok && cudaMalloc(&q, (cnt ? cnt : 1) * sizeof(**p)) == cudaSuccess) {
-            bt.dev.push_back(q);
-            *p = (std::remove_reference_t<decltype(*p)>)q;
-        } else {
-            ok = false;
+        bt.h_offs[0] = 0;
+    } else {
+        for (int i = 0; i < G; ++i) {
+            bt.h_tab[i] = (int64_t)(uintptr_t)graphs[i]->dev_offs;
+            bt.h_tab[bt.cap + i] = (int64_t)(uintptr_t)graphs[i]->dev_nbr;
+            bt.h_tab[2LL * bt.cap + i] = (int64_t)(uintptr_t)graphs[i]->dev_w;
         }
-    };
-    auto hal = [&](auto **p, size_t cnt) {
-        void *q = nullptr;
-        if (ok && cudaMallocHost(&q, (cnt ? cnt : 1) * sizeof(**p)) == cudaSuccess) {
-            bt.host.push_back(q);
-            *p = (std::remove_reference_t<decltype(*p)>)q;
-        } else {
-            ok = false;
-        }
-    };
-    dal(&bt.gid, n);
-    dal(&bt.gid2, n);
-    dal(&bt.m2g, G);
-    dal(&bt.cg, G);
-    dal(&bt.stop, G);
-    dal(&bt.reject, G);
-    dal(&bt.min_tot, G);
-    dal(&bt.ncomm, G);
-    dal(&bt.sum_in, G);
-    dal(&bt.sum_tot2, G);
-    dal(&bt.sum_k, G);
-    dal(&bt.goff, (size_t)G + 1);
-    hal(&bt.h_sum_in, G);
-    hal(&bt.h_sum_tot2, G);
-    hal(&bt.h_sum_k, G);
-    hal(&bt.h_ncomm, G);
-    hal(&bt.h_stop, G);
-    hal(&bt.h_reject, G);
-    hal(&bt.h_goff, (size_t)G + 1);
-    if (!ok) {
-        cudaGetLastError();
-        set_error("gala_louvain_batch: allocation of the per-graph state failed (%d graphs)", G);
-        return GALA_ERR_OOM;
     }
-    bt.finished.assign(G, 0);
-    bt.prev_mod.assign(G, -1.0);
-    bt.cur_mod.assign(G, -1.0);
-    memcpy(bt.h_goff, vstart.data(), ((size_t)G + 1) * sizeof(int64_t));
     long long l0 = gala_kernel_launch_count();
     cudaEventRecord(ctx->ev[6], st);
-    cudaMemcpyAsync(ctx->offs[1], offs.data(), ((size_t)n + 1) * sizeof(int64_t), cudaMemcpyHostToDevice, st);
-    cudaMemcpyAsync(ctx->nbr[1], nbr.data(), (size_t)e_tot * sizeof(int32_t), cudaMemcpyHostToDevice, st);
-    const int32_t *dw = nullptr;
-    if (weighted) {
-        cudaMemcpyAsync(ctx->w[1], w.data(), (size_t)e_tot * sizeof(int32_t), cudaMemcpyHostToDevice, st);
-        dw = ctx->w[1];
+    const int32_t *dw = weighted ? ctx->w[1] : nullptr;
+    // the source table (or, staged, just the vertex and entry starts)
+    // (laid out for bt.cap graphs; this batch fills the first G of each part)
+    cudaMemcpyAsync(bt.vstart(), bt.h_vstart(), ((size_t)G + 1) * sizeof(int64_t), cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(bt.estart(), bt.h_estart(), ((size_t)G + 1) * sizeof(int64_t), cudaMemcpyHostToDevice, st);
+    if (mapped) {
+        cudaMemcpyAsync(bt.tab, bt.h_tab, 3 * (size_t)bt.cap * sizeof(int64_t), cudaMemcpyHostToDevice, st);
+        batch_gather(G, bt.src(), ctx->offs[1], ctx->nbr[1], weighted ? ctx->w[1] : nullptr, st);
+    } else {
+        cudaMemcpyAsync(ctx->offs[1], bt.h_offs, ((size_t)n + 1) * sizeof(int64_t), cudaMemcpyHostToDevice, st);
+        cudaMemcpyAsync(ctx->nbr[1], bt.h_nbr, (size_t)e_tot * sizeof(int32_t), cudaMemcpyHostToDevice, st);
+        if (weighted)
+            cudaMemcpyAsync(ctx->w[1], bt.h_w, (size_t)e_tot * sizeof(int32_t), cudaMemcpyHostToDevice, st);
+        batch_shift(G, bt.vstart(), bt.estart(), ctx->offs[1], ctx->nbr[1], st);
     }
     cudaMemcpyAsync(bt.goff, bt.h_goff, ((size_t)G + 1) * sizeof(int64_t), cudaMemcpyHostToDevice, st);
     cudaEventRecord(ctx->ev[7], st);
@@ -1450,15 +1552,14 @@ gala_status gala_louvain_batch(gala_context *ctx, const gala_graph *const *graph
     b.gstop = nullptr;
     b.min_tot_g = nullptr;
     if (s) return s;
+    // union community ids -> ids local to each graph, on the device
+    batch_local_labels(G, bt.vstart(), bt.goff, ctx->orig, st);
     cudaEventRecord(ctx->ev[6], st);
     cudaMemcpyAsync(community_out, ctx->orig, (size_t)n * sizeof(int32_t), cudaMemcpyDeviceToHost, st);
     cudaEventRecord(ctx->ev[7], st);
     if ((s = sync_check(st, "batch device to host copy"))) return s;
     res->time_d2h_ms = ev_ms(ctx->ev[6], ctx->ev[7]);
-    // union community ids -> ids local to each graph
     for (int i = 0; i < G; ++i) {
-        const int32_t base = (int32_t)bt.h_goff[i];
-        for (long long v = vstart[i]; v < vstart[i + 1]; ++v) community_out[v] -= base;
         if (modularity_out) modularity_out[i] = bt.m2[i] > 0 ? bt.cur_mod[i] : 0.0;
         if (communities_out) communities_out[i] = (int32_t)(bt.h_goff[i + 1] - bt.h_goff[i]);
     }
@@ -1470,7 +1571,8 @@ gala_status gala_louvain_batch(gala_context *ctx, const gala_graph *const *graph
     res->time_total_ms = r.time_total_ms;
     res->time_phase1_ms = r.time_phase1_ms;
     res->time_contract_ms = r.time_contract_ms;
-    res->h2d_bytes = ((long long)n + 1) * 8 + e_tot * 4 * (weighted ? 2 : 1) + ((long long)G + 1) * 8;
+    res->h2d_bytes = ((long long)n + 1) * 8 + e_tot * 4 * (weighted ? 2 : 1) + ((long long)G + 1) * 8 +
+                     (mapped ? 3LL * bt.cap + 2LL * G + 2 : 2LL * G + 2) * 8;
     res->d2h_bytes = (long long)n * 4;
     res->kernel_launches = gala_kernel_launch_count() - l0;
     return GALA_OK;

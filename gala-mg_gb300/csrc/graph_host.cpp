@@ -253,6 +253,16 @@ gala_status gala_graph_pin(gala_graph *g)
         return cuda_fail(e, "gala_graph_pin");
     }
     g->pinned = true;
+    // device-mapped addresses, for kernels that read the graph in place
+    // (registered memory is mapped under unified addressing); a graph
+    // without them is copied by the host instead
+    void *p = nullptr;
+    if (!g->offs.empty() && cudaHostGetDevicePointer(&p, g->offs.data(), 0) == cudaSuccess)
+        g->dev_offs = (const int64_t *)p;
+    if (!g->nbr.empty() && cudaHostGetDevicePointer(&p, g->nbr.data(), 0) == cudaSuccess)
+        g->dev_nbr = (const int32_t *)p;
+    if (!g->w.empty() && cudaHostGetDevicePointer(&p, g->w.data(), 0) == cudaSuccess) g->dev_w = (const int32_t *)p;
+    cudaGetLastError();
     return GALA_OK;
 }
 

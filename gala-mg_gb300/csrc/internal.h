@@ -23,6 +23,10 @@ struct gala_graph {
     int32_t fixed_shift = 0;    // float graphs: weights are round(w * 2^fixed_shift)
     bool rows_distinct = false; // every row lists a neighbour at most once (built here)
     bool pinned = false;  // arrays registered with cudaHostRegister
+    // device-mapped addresses of the registered arrays (null when not pinned)
+    const int64_t *dev_offs = nullptr;
+    const int32_t *dev_nbr = nullptr;
+    const int32_t *dev_w = nullptr;
     int64_t entries() const { return n ? offs[n - 1] : 0; }
     ~gala_graph();
 };
@@ -171,6 +175,25 @@ void batch_graph_sums(int what, int G, const int64_t *goff, const uint8_t *stop,
                       const GraphSums &out, cudaStream_t st);
 void batch_revert(Phase1Buffers &b, const int32_t *gid, const uint8_t *reject, int n, cudaStream_t st);
 void batch_gid_fill(int G, const int64_t *goff, int32_t *gid, cudaStream_t st);
+// Source arrays of a batch of page-locked host graphs (device-mapped
+// addresses, one per graph) and each graph's first vertex and entry in the
+// union (G+1 entries each).
+struct BatchSrc {
+    const int64_t *const *offs;  // inclusive offsets, n_g entries
+    const int32_t *const *nbr;
+    const int32_t *const *w;     // null entries: unweighted graphs
+    const int64_t *vstart;
+    const int64_t *estart;
+};
+// Union CSR (device layout, ids shifted per graph) gathered from the host
+// graphs by the GPU; w may be null (no graph weighted).
+void batch_gather(int G, const BatchSrc &src, int64_t *offs, int32_t *nbr, int32_t *w, cudaStream_t st);
+// Union CSR whose graphs were copied raw (inclusive offsets of graph g at
+// offs[vstart[g]+1 ...], its entries at nbr[estart[g] ...]): shift them into
+// union ids and offsets in place.
+void batch_shift(int G, const int64_t *vstart, const int64_t *estart, int64_t *offs, int32_t *nbr, cudaStream_t st);
+// labels[v] -= goff[g] for the input vertices v of every graph g.
+void batch_local_labels(int G, const int64_t *vstart, const int64_t *goff, int32_t *labels, cudaStream_t st);
 
 // ---- contraction (contract.cu) ----
 struct ContractBuffers {

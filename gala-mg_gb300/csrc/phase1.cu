@@ -386,7 +386,7 @@ void p1_level_init(const LevelGraph &g, Phase1Buffers &b, cudaStream_t st)
         k_init_vertices<int><<<grid, 256, 0, st>>>(n, b.comm, b.K, b.Self, b.Tot, b.size, b.In);
     k_bin_count<<<nblk, kCountBlock, 0, st>>>(n, g.offs, b.blockcnt, nblk, b.stats, b.lim);
     exclusive_scan(b.blockcnt, b.blockoff, (long long)kNumBinSlots * nblk, OpIdentity(), b.scan_partial,
-                   &b.stats->total, st);
+                   &b.stats->total, st, &b.stats->err);
     k_bin_scatter<<<nblk, kCountBlock, 0, st>>>(n, g.offs, b.blockoff, nblk, b.order, b.stats, b.lim);
     note_launch(3);
 }
@@ -1994,9 +1994,9 @@ void p1_hub_plan_launch(const LevelGraph &g, Phase1Buffers &b, HubPlan &p, cudaS
 {
     const int grid = (p.H + 255) / 256;
     k_hub_plan<<<grid, 256, 0, st>>>(p, g.offs);
-    exclusive_scan(p.T, p.toff, p.H, OpIdentity(), b.scan_partial, &b.stats->total, st);
-    exclusive_scan(p.chunks, p.coff, p.H, OpIdentity(), b.scan_partial, &b.stats->total2, st);
-    exclusive_scan(p.tchunks, p.tcoff, p.H, OpIdentity(), b.scan_partial, &b.stats->total3, st);
+    exclusive_scan(p.T, p.toff, p.H, OpIdentity(), b.scan_partial, &b.stats->total, st, &b.stats->err);
+    exclusive_scan(p.chunks, p.coff, p.H, OpIdentity(), b.scan_partial, &b.stats->total2, st, &b.stats->err);
+    exclusive_scan(p.tchunks, p.tcoff, p.H, OpIdentity(), b.scan_partial, &b.stats->total3, st, &b.stats->err);
     k_hub_tail<<<1, 1, 0, st>>>(p, b.stats);
     note_launch(2);
 }

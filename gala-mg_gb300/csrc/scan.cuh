@@ -1,5 +1,5 @@
-// scan.cuh - exclusive prefix sum over device arrays (three passes: block
-// sums, scan of the block sums in one CTA, block-local rescan with offsets).
+// scan.cuh - exclusive prefix sum over device arrays in one pass (tiles chained
+// by decoupled look-back).
 // Used for the degree-bin counting sort, the community renumbering and the
 // CSR offsets of the contraction.  Input values pass through a functor, so a
 // flag (x > 0) or a cap (min(x, C)) needs no separate pass.
@@ -59,84 +59,121 @@ __device__ __forceinline__ T block_exclusive_scan(T v, T *warp_tot, T *block_tot
     return r;
 }
 
-template <typename Tin, typename Op>
-__global__ void __launch_bounds__(kScanThreads) k_scan_reduce(const Tin *__restrict__ in, long long n, Op op,
-                                                              long long *__restrict__ partial)
+// Single-pass exclusive scan with decoupled look-back (Merrill & Garland,
+// "Single-pass Parallel Prefix Scan with Decoupled Look-back", 2016).  Each
+// tile of kScanTile items takes its id from a counter in launch order, so it
+// only ever waits for tiles that already run; it publishes its aggregate,
+// then (after looking back) its inclusive prefix, as one 64-bit word:
+// flag in the top two bits, value below (values are non-negative and below
+// 2^62).  The look-back reads 32 predecessors per step, one per lane of
+// warp 0.  Every wait is bounded: a tile that waited kScanSpinLimit rounds
+// records kScanErrBit in *err and counts that predecessor as 0.
+constexpr unsigned long long kScanFlagAgg = 1ull << 62;
+constexpr unsigned long long kScanFlagPre = 2ull << 62;
+constexpr unsigned long long kScanValMask = (1ull << 62) - 1;
+constexpr int kScanSpinLimit = 1 << 20;
+constexpr int kScanErrBit = 2;  // the engine's probe-limit error bit
+
+__device__ __forceinline__ unsigned long long scan_ld(const unsigned long long *p)
 {
-    __shared__ long long wt[32];
-    __shared__ long long tot;
-    long long base = (long long)blockIdx.x * kScanTile;
-    long long s = 0;
-#pragma unroll
-    for (int i = 0; i < kScanItems; ++i) {
-        long long idx = base + (long long)i * kScanThreads + threadIdx.x;
-        if (idx < n) s += op(in[idx], idx);
-    }
-    block_exclusive_scan<long long>(s, wt, &tot);
-    if (threadIdx.x == 0) partial[blockIdx.x] = tot;
+    unsigned long long v;
+    asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void scan_st(unsigned long long *p, unsigned long long v)
+{
+    asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
 }
 
-// Exclusive scan of the block sums in one CTA (in place); writes the grand
-// total to *total_out.
-template <int kDummy = 0>
-__global__ void __launch_bounds__(1024) k_scan_partials(long long *partial, int nb, long long *total_out)
-{
-    __shared__ long long wt[32];
-    __shared__ long long tot;
-    long long carry = 0;
-    for (int base = 0; base < nb; base += 1024) {
-        int i = base + threadIdx.x;
-        long long v = i < nb ? partial[i] : 0;
-        long long ex = block_exclusive_scan<long long>(v, wt, &tot);
-        if (i < nb) partial[i] = ex + carry;
-        carry += tot;
-        __syncthreads();
-    }
-    if (threadIdx.x == 0) {
-        partial[nb] = carry;
-        if (total_out) *total_out = carry;
-    }
-}
-
+// status: nb + 2 words, zero on entry; status[nb] is the tile counter.
 template <typename Tin, typename Tout, typename Op>
-__global__ void __launch_bounds__(kScanThreads) k_scan_down(const Tin *__restrict__ in, Tout *__restrict__ out,
-                                                            long long n, Op op,
-                                                            const long long *__restrict__ partial)
+__global__ void __launch_bounds__(kScanThreads) k_scan_onepass(const Tin *__restrict__ in, Tout *__restrict__ out,
+                                                               long long n, Op op, unsigned long long *status, int nb,
+                                                               long long *total_out, int *err)
 {
     __shared__ long long wt[32];
     __shared__ long long tot;
-    long long base = (long long)blockIdx.x * kScanTile + (long long)threadIdx.x * kScanItems;
+    __shared__ int s_tile;
+    __shared__ long long s_excl;
+    if (threadIdx.x == 0) s_tile = (int)atomicAdd(&status[nb], 1ull);
+    __syncthreads();
+    const int tile = s_tile;
+    const long long base = (long long)tile * kScanTile + (long long)threadIdx.x * kScanItems;
     long long v[kScanItems];
     long long s = 0;
 #pragma unroll
     for (int i = 0; i < kScanItems; ++i) {
-        long long idx = base + i;
+        const long long idx = base + i;
         v[i] = idx < n ? op(in[idx], idx) : 0;
         s += v[i];
     }
-    long long pre = block_exclusive_scan<long long>(s, wt, &tot) + partial[blockIdx.x];
+    long long pre = block_exclusive_scan<long long>(s, wt, &tot);
+    if (threadIdx.x < 32) {
+        const int lane = threadIdx.x;
+        const unsigned long long agg = (unsigned long long)tot & kScanValMask;
+        long long excl = 0;
+        if (tile == 0) {
+            if (lane == 0) scan_st(&status[0], kScanFlagPre | agg);
+        } else {
+            if (lane == 0) scan_st(&status[tile], kScanFlagAgg | agg);
+            int p = tile - 1;  // lane k looks at tile p - k
+            bool timed_out = false;
+            for (;;) {
+                const int t = p - lane;
+                unsigned long long w = kScanFlagPre;  // tiles before 0 count as prefix 0
+                if (t >= 0) {
+                    int it = 0;
+                    for (;;) {
+                        w = scan_ld(&status[t]);
+                        if (w >> 62) break;
+                        if (++it > kScanSpinLimit) {
+                            timed_out = true;
+                            w = kScanFlagPre;
+                            break;
+                        }
+                        __nanosleep(32);
+                    }
+                }
+                const unsigned pm = __ballot_sync(GALA_FULL_MASK, (w >> 62) == 2ull);
+                const int kstar = pm ? __ffs(pm) - 1 : 32;
+                long long c = lane <= kstar ? (long long)(w & kScanValMask) : 0;
+#pragma unroll
+                for (int o = 16; o >= 1; o >>= 1) c += __shfl_xor_sync(GALA_FULL_MASK, c, o);
+                excl += c;
+                if (pm) break;
+                p -= 32;
+            }
+            if (__any_sync(GALA_FULL_MASK, timed_out) && lane == 0 && err) atomicOr(err, kScanErrBit);
+            if (lane == 0) scan_st(&status[tile], kScanFlagPre | (((unsigned long long)excl + agg) & kScanValMask));
+        }
+        if (lane == 0) s_excl = excl;
+    }
+    __syncthreads();
+    pre += s_excl;
 #pragma unroll
     for (int i = 0; i < kScanItems; ++i) {
-        long long idx = base + i;
+        const long long idx = base + i;
         if (idx < n) out[idx] = (Tout)pre;
         pre += v[i];
     }
+    if (tile == nb - 1 && threadIdx.x == 0 && total_out) *total_out = s_excl + tot;
 }
 
 // Host wrapper: out[i] = sum_{j<i} op(in[j]); *total_out (device) = sum of all.
-// partial needs ceil(n / kScanTile) + 1 slots.
+// partial needs ceil(n / kScanTile) + 2 slots (the tile status words and the
+// counter).  err (device, may be null) receives kScanErrBit if a wait ran out.
 void note_launch(int k);
 
 template <typename Tin, typename Tout, typename Op>
-void exclusive_scan(const Tin *in, Tout *out, long long n, Op op, long long *partial,
-                    long long *total_out, cudaStream_t st)
+void exclusive_scan(const Tin *in, Tout *out, long long n, Op op, long long *partial, long long *total_out,
+                    cudaStream_t st, int *err = nullptr)
 {
     int nb = (int)((n + kScanTile - 1) / kScanTile);
     if (nb < 1) nb = 1;
-    k_scan_reduce<Tin, Op><<<nb, kScanThreads, 0, st>>>(in, n, op, partial);
-    k_scan_partials<0><<<1, 1024, 0, st>>>(partial, nb, total_out);
-    k_scan_down<Tin, Tout, Op><<<nb, kScanThreads, 0, st>>>(in, out, n, op, partial);
-    note_launch(3);
+    unsigned long long *status = (unsigned long long *)partial;
+    cudaMemsetAsync(status, 0, ((size_t)nb + 2) * sizeof(unsigned long long), st);
+    k_scan_onepass<Tin, Tout, Op><<<nb, kScanThreads, 0, st>>>(in, out, n, op, status, nb, total_out, err);
+    note_launch(1);
 }
 
 }  // namespace gala

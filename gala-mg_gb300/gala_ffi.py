@@ -87,7 +87,9 @@ class Result(ctypes.Structure):
                 ("level_update_ms", ctypes.c_double * GALA_MAX_LEVELS),
                 ("level_contract_ms", ctypes.c_double * GALA_MAX_LEVELS),
                 ("level_movers", ctypes.c_int64 * GALA_MAX_LEVELS),
-                ("level_active_entries", ctypes.c_int64 * GALA_MAX_LEVELS)]
+                ("level_active_entries", ctypes.c_int64 * GALA_MAX_LEVELS),
+                ("host_total_ms", ctypes.c_double), ("host_h2d_ms", ctypes.c_double),
+                ("host_run_ms", ctypes.c_double), ("host_d2h_ms", ctypes.c_double)]
 
     def to_dict(self, trace=None):
         L = self.num_levels
@@ -103,6 +105,8 @@ class Result(ctypes.Structure):
              "kernel_launches": self.kernel_launches, "h2d_bytes": self.h2d_bytes, "d2h_bytes": self.d2h_bytes,
              "fp64_decisions": self.fp64_decisions, "decisions": self.decisions, "skipped": self.skipped,
              "verify_sweeps": self.verify_sweeps, "samples": self.samples,
+             "host_ms": {"total": self.host_total_ms, "h2d": self.host_h2d_ms, "run": self.host_run_ms,
+                         "d2h": self.host_d2h_ms},
              "levels": [{"vertices": self.level_vertices[i], "entries": self.level_entries[i],
                          "phase1_ms": self.level_phase1_ms[i], "decide_ms": self.level_decide_ms[i],
                          "update_ms": self.level_update_ms[i], "contract_ms": self.level_contract_ms[i],

@@ -166,6 +166,12 @@ typedef struct {
     double level_contract_ms[GALA_MAX_LEVELS];
     int64_t level_movers[GALA_MAX_LEVELS];       /* moves applied, all sweeps */
     int64_t level_active_entries[GALA_MAX_LEVELS]; /* row entries decided, all sweeps */
+    /* host wall time (ms) of gala_louvain: the whole call, up to the end of
+       the host->device copy, the rounds, the device->host copy of labels */
+    double host_total_ms;
+    double host_h2d_ms;
+    double host_run_ms;
+    double host_d2h_ms;
 } gala_result;
 
 /* ---- errors / info --------------------------------------------------- */

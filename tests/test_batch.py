@@ -105,3 +105,40 @@ def test_batch_max_levels_and_single_graph(ffi, torch_cuda):
     s2 = ctx.louvain(g)
     assert np.array_equal(s2["labels"], s["labels"])
     ctx.close()
+
+
+@pytest.mark.gpu
+def test_batch_staged_and_page_locked_inputs_agree(ffi, torch_cuda):
+    """A batch's graphs reach the device either staged (raw copies into the
+    context's pinned buffer, one transfer, ids shifted on the device) or,
+    when every graph is page-locked, read in place by the GPU.  Both give the
+    same partitions; the per-graph state is kept between calls of different
+    batch sizes."""
+    rng = np.random.default_rng(21)
+    big = ffi.Graph.sbm_batch(20, n_min=2000, n_max=40000, seed=23)
+    small = big[:3]
+    w_rows = []
+    for n in (5000, 9000):  # weighted graphs beside unweighted ones
+        offs, nbr, _ = ffi.Graph.sbm(n, 16, 0.02, 0.0005, int(rng.integers(1 << 30))).arrays()
+        rows = np.repeat(np.arange(n), np.diff(offs))
+        w_rows.append(ffi.Graph.from_csr(offs, nbr, (1 + (rows + nbr) % 5).astype(np.int32)))
+    mixed = big[3:8] + w_rows
+    tot_n = sum(g.info()[0] for g in big + w_rows)
+    tot_e = sum(g.info()[1] for g in big + w_rows)
+    ctx = ffi.Context(tot_n, tot_e)
+    staged = {k: ctx.louvain_batch(gs) for k, gs in (("small", small), ("big", big), ("mixed", mixed))}
+    pinned = 0
+    for g in big + w_rows:
+        try:
+            g.pin()
+            pinned += 1
+        except ffi.GalaError:
+            pass  # arrays sharing a page with one already registered: staged
+    again = {k: ctx.louvain_batch(gs) for k, gs in (("small", small), ("mixed", mixed), ("big", big))}
+    ctx.close()
+    assert pinned > 0
+    for k in staged:
+        for a, b in zip(staged[k]["labels"], again[k]["labels"]):
+            assert np.array_equal(a, b), k
+        assert np.array_equal(staged[k]["modularity"], again[k]["modularity"]), k
+        assert np.array_equal(staged[k]["communities"], again[k]["communities"]), k
