@@ -70,8 +70,12 @@ def parse():
     p.add_argument("--no-batch", action="store_true", help="skip the batched-graphs arm")
     p.add_argument("--no-refine", action="store_true", help="skip the Leiden-style refinement arm")
     p.add_argument("--no-weighted", action="store_true", help="skip the float-weight LFR arm")
+    p.add_argument("--no-calibrated", action="store_true",
+                   help="skip the R-MAT stand-in without isolated vertices (scale 24)")
     p.add_argument("--tune-cache", default=None, help="JSON file caching autotuned degree bins per workload")
     p.add_argument("--threshold", type=float, default=0.3, help="proposal probability threshold")
+    p.add_argument("--proposal-from", type=int, default=2,
+                   help="first sweep of a level that decides only proposed vertices")
     p.add_argument("--profile", action="store_true",
                    help="one device-resident run and a short summary (for ncu captures)")
     p.add_argument("--profile-learned", action="store_true",
@@ -302,7 +306,7 @@ def learned_arm(ffi, ctx, g, stream, args, torch, plain_ms, plain):
     else:
         proposal_tool.train_on_rmat(prop, range(1000, 1008), [18, 19, 20], sample_shift=2, epochs=6, ctx=ctx)
         source = "trained in this run: 8 R-MAT graphs (scales 18-20, seeds 1000-1007)"
-    def timed(threshold, steps):
+    def timed(threshold, steps, start=args.proposal_from):
         times, r = [], None
         for i in range(args.warmup + steps):
             torch.cuda.synchronize()
@@ -310,7 +314,8 @@ def learned_arm(ffi, ctx, g, stream, args, torch, plain_ms, plain):
                 a = torch.cuda.Event(enable_timing=True)
                 b = torch.cuda.Event(enable_timing=True)
                 a.record(stream)
-                r = ctx.louvain(g, proposal=prop, mode=ffi.PROPOSAL_SKIP, threshold=threshold)
+                r = ctx.louvain(g, proposal=prop, mode=ffi.PROPOSAL_SKIP, threshold=threshold,
+                                proposal_from=start)
                 b.record(stream)
             torch.cuda.synchronize()
             if i >= args.warmup:
@@ -318,16 +323,18 @@ def learned_arm(ffi, ctx, g, stream, args, torch, plain_ms, plain):
         return sum(times) / len(times), r
 
     ms, r = timed(args.threshold, args.steps)
-    # the proposal threshold against decisions, sweeps, time and final Q
+    # the proposal threshold (and the first sweep that may skip) against
+    # decisions, sweeps, time and final Q
     curve = []
-    for th in (0.1, 0.2, 0.3, 0.4, 0.5):
-        tms, tr = timed(th, min(args.steps, 3))
-        curve.append({"threshold": th, "ms": tms, "time_vs_plain": tms / plain_ms, "decisions": tr["decisions"],
+    for start, th in [(2, x) for x in (0.1, 0.2, 0.3, 0.4, 0.5)] + [(3, x) for x in (0.1, 0.3, 0.5)]:
+        tms, tr = timed(th, min(args.steps, 3), start)
+        curve.append({"threshold": th, "proposal_from": start, "ms": tms, "time_vs_plain": tms / plain_ms,
+                      "decisions": tr["decisions"],
                       "skipped": tr["skipped"], "sweeps": tr["total_iterations"],
                       "verify_sweeps": tr["verify_sweeps"], "dq_vs_plain": tr["modularity"] - plain["modularity"]})
     prop.close()
-    return {"mode": "skip", "threshold": args.threshold, "weights": source, "ms_per_step": ms,
-            "threshold_curve": curve,
+    return {"mode": "skip", "threshold": args.threshold, "proposal_from": args.proposal_from, "weights": source,
+            "ms_per_step": ms, "threshold_curve": curve,
             "time_vs_plain": ms / plain_ms, "modularity": r["modularity"],
             "dq_vs_plain": r["modularity"] - plain["modularity"], "decisions": r["decisions"],
             "plain_decisions": plain["decisions"], "skipped": r["skipped"], "verify_sweeps": r["verify_sweeps"],
@@ -380,6 +387,54 @@ def refine_arm(ffi, ctx, g, stream, args, torch, plain_ms, plain):
             "plain_communities": plain["num_communities"], "iterations": r["total_iterations"],
             "phase_ms": {"decide": r["time_decide_ms"], "update": r["time_update_ms"],
                          "contract_and_refine": r["time_contract_ms"]}}
+
+
+# A second stand-in for config 2 whose vertices all have edges (ids without
+# edges dropped, as the reference's preprocess does): scale 24, raw samples
+# chosen so that m is about 34.7M after deduplication.
+CALIBRATED = dict(WORKLOAD, workload="rmat-s24-m34.7M-no-isolated", scale=24, raw_edges=34_940_000,
+                  keep_isolated_ids=False)
+
+
+def calibrated_arm(ffi, args, torch, device):
+    """Plain Louvain on the calibrated R-MAT (device-resident and end to end)."""
+    c = CALIBRATED
+    g = make_graph(c)
+    offs, nbr, _ = g.arrays()
+    n, E = offs.shape[0] - 1, int(offs[-1])
+    g.pin()
+    ctx = ffi.Context(n, E, device=device)
+    stream = torch.cuda.Stream()
+    ctx.set_stream(stream.cuda_stream)
+    d_offs = torch.from_numpy(offs).to(f"cuda:{device}")
+    d_nbr = torch.from_numpy(nbr).to(f"cuda:{device}")
+    d_out = torch.empty(n, dtype=torch.int32, device=f"cuda:{device}")
+    dev, e2e, r, re_ = [], [], None, None
+    for i in range(args.warmup + args.steps):
+        torch.cuda.synchronize()
+        r = ctx.louvain_device(n, d_offs.data_ptr(), d_nbr.data_ptr(), None, d_out.data_ptr(), distinct_rows=True)
+        torch.cuda.synchronize()
+        if i >= args.warmup:
+            dev.append(r["time_total_ms"])
+    for i in range(args.warmup + args.steps):
+        with torch.cuda.stream(stream):
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            re_ = ctx.louvain(g)
+            b.record(stream)
+        torch.cuda.synchronize()
+        if i >= args.warmup:
+            e2e.append(a.elapsed_time(b))
+    ctx.close()
+    ms, ems = sum(dev) / len(dev), sum(e2e) / len(e2e)
+    return {"config": workload_config(c, n, E, int(np.diff(offs).max()), 1), "ms_per_step": ms,
+            "edges_per_s": (E // 2) / (ms / 1000.0), "e2e_ms": ems, "e2e_edges_per_s": (E // 2) / (ems / 1000.0),
+            "modularity": r["modularity"], "rounds": r["rounds"], "iterations": r["total_iterations"],
+            "communities": r["num_communities"],
+            "labels_equal_e2e": bool((d_out.cpu().numpy() == re_["labels"]).all()),
+            "phase_ms": {"decide": r["time_decide_ms"], "update": r["time_update_ms"],
+                         "contract": r["time_contract_ms"]}}
 
 
 WEIGHTED = {"workload": "lfr-16M-200M-f32", "generator": "LFR-style", "vertices": 16_000_000, "tau1": 2.5,
@@ -440,26 +495,44 @@ def batch_arm(ffi, args, torch, device):
     es = [g.info()[1] for g in gs]
     m = sum(es) // 2
     ctx = ffi.Context(sum(ns), sum(es), device=device)
+    # page-lock the host graphs (untimed, as for the main graph): when every
+    # graph is page-locked the GPU reads them in place; otherwise the run
+    # copies them through the context's pinned staging
+    pinned = 0
+    for g in gs:
+        try:
+            g.pin()
+            pinned += 1
+        except ffi.GalaError:
+            pass
     # degree bins tuned on this batch (untimed; cached in --tune-cache when given)
     tuning = None
     if args.tune_cache and os.path.exists(args.tune_cache):
         tuning = json.load(open(args.tune_cache)).get(b["workload"])
     if tuning is None:
-        tuning = ctx.autotune(gs, repeats=1, use_graphs=1)
+        tuning = ctx.autotune(gs, repeats=1, use_graphs=1, batch_mode=1)  # the bins tune the union run
         if args.tune_cache:
             cache = json.load(open(args.tune_cache)) if os.path.exists(args.tune_cache) else {}
             cache[b["workload"]] = tuning
             json.dump(cache, open(args.tune_cache, "w"))
-    times, r = [], None
-    for i in range(args.warmup + args.steps):
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        r = ctx.louvain_batch(gs, use_graphs=True, tuning=tuning)
-        torch.cuda.synchronize()
-        if i >= args.warmup:
-            times.append(time.perf_counter() - t0)
+    def timed(mode):
+        times, r = [], None
+        for i in range(args.warmup + args.steps):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            r = ctx.louvain_batch(gs, use_graphs=True, tuning=tuning, batch_mode=mode)
+            torch.cuda.synchronize()
+            if i >= args.warmup:
+                times.append(time.perf_counter() - t0)
+        return statistics.median(times), r
+
+    # the union run (every sweep one set of launches for all graphs), for
+    # comparison; then the default: one persistent launch, one CTA per graph
+    usec, ur = timed(1)
+    sec, r = timed(0)
+    for a, b_ in zip(r["labels"], ur["labels"]):
+        assert (a == b_).all()
     ctx.close()
-    sec = statistics.median(times)
     sample = list(range(0, b["graphs"], 128))
     single = ffi.Context(max(ns), max(es), device=device)
     st, equal, maxdq = 0.0, 0, 0.0
@@ -476,11 +549,15 @@ def batch_arm(ffi, args, torch, device):
     return {"config": dict(b, vertices=sum(ns), edges=m, max_vertices=max(ns), min_vertices=min(ns)),
             "metric": "batched Louvain edges/s (host graphs in, labels out)", "value": m / sec, "unit": "edges/s",
             "seconds": sec, "device_ms": r["time_total_ms"], "h2d_ms": r["time_h2d_ms"], "d2h_ms": r["time_d2h_ms"],
-            "input": "host graphs (not page-locked): raw copies into the context's pinned staging, one transfer, "
-                     "ids shifted on the device",
+            "input": ("page-locked host graphs, read in place by the GPU (one gather kernel)" if pinned == len(gs)
+                      else "host graphs (%d of %d page-locked): raw copies into the context's pinned staging, one "
+                           "transfer, ids shifted on the device" % (pinned, len(gs))),
             "phase1_ms": r["time_phase1_ms"],
             "contract_ms": r["time_contract_ms"], "levels": r["num_levels"], "iterations": r["total_iterations"],
-            "kernel_launches": r["kernel_launches"], "tuning": tuning, "cuda_graphs": True,
+            "kernel_launches": r["kernel_launches"],
+            "mode": "one persistent launch, one CTA per graph (all rounds)" if r["kernel_launches"] < 10 else "union",
+            "union_run": {"seconds": usec, "device_ms": ur["time_total_ms"], "kernel_launches": ur["kernel_launches"],
+                          "tuning": tuning, "cuda_graphs": True, "labels_equal": True},
             "sequential_single_runs_s_est": seq_est, "speedup_vs_sequential": seq_est / sec,
             "checked_graphs": len(sample), "labels_equal_single_runs": equal, "max_dq_vs_single": maxdq}
 
@@ -631,6 +708,8 @@ def main():
         line["batch"] = batch_arm(ffi, args, torch, local)
     if not args.no_weighted:
         line["weighted"] = weighted_arm(ffi, args, torch, local)
+    if not args.no_calibrated:
+        line["calibrated"] = calibrated_arm(ffi, args, torch, local)
     line.update({"metric": METRIC, "value": value, "unit": "edges/s", "n_gpus": world, "steps": args.steps,
                  "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
                  "vs_baseline": None, "dtype": "int32/f64", "data": "synthetic", "config": cfg,
@@ -647,7 +726,8 @@ def main():
         # time end to end, at |dQ| <= 0.002
         e2e["learned_vs_plain"] = {"time_vs_plain": lr["time_vs_plain"], "dq_vs_plain": lr["dq_vs_plain"],
                                    "plain_ms": e2e_step, "learned_ms": lr["ms_per_step"],
-                                   "threshold": lr["threshold"], "decisions": lr["decisions"],
+                                   "threshold": lr["threshold"], "proposal_from": lr["proposal_from"],
+                                   "decisions": lr["decisions"],
                                    "plain_decisions": lr["plain_decisions"], "target": "<= 0.5 at |dQ| <= 0.002"}
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1

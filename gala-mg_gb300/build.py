@@ -23,7 +23,8 @@ OUT = os.path.join(PKG, "_build")
 INC = os.path.join(os.path.dirname(PKG), "include")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CU_UNITS = ["phase1.cu", "contract.cu", "engine.cu", "modularity_static.cu", "proposal.cu", "batch.cu", "refine.cu"]
+CU_UNITS = ["phase1.cu", "contract.cu", "engine.cu", "modularity_static.cu", "proposal.cu", "batch.cu", "refine.cu",
+            "batch_cta.cu"]
 CPP_UNITS = ["graph_host.cpp"]
 CLIS = ["gala_main.cpp", "gala_preprocess.cpp"]
 HEADERS = ["common.cuh", "scan.cuh", "internal.h", "binlimits.h"]

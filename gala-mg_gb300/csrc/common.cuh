@@ -73,7 +73,7 @@ struct DevStats {
     int nz_rows;                    // contraction: rows with entries (walk list)
     int bin_start[kNumBinSlots + 1];  // order list: start of each bin
     int act_count[2][kNumBins];       // active list counts (ping-pong)
-    int small_cnt[5];                 // contraction: communities per size class
+    int small_cnt[6];                 // contraction: communities per size class
     long long total2;                 // scratch total of a second scan
     long long total3;                 // scratch total of a third scan
     long long total;                  // scratch total of the last scan

@@ -55,6 +55,9 @@ constexpr int kMid1Max = 512;
 constexpr int kMid2Max = 4096;
 constexpr int kMid3Max = 8192;  // rows in hash-table order only (a 16384-slot table)
 constexpr int kLongCls = 4;     // class of the rows aggregated in global tables
+constexpr int kWarpCls = 5;     // rows of 33..kWarpAggMax entries in table order: one warp each
+constexpr int kWarpAggMax = 128;
+constexpr int kNumCls = 6;
 constexpr int kChunk = 4096;
 constexpr int kSortMax = 16384;
 constexpr int kRangeEntries = 1024;  // CSR entries per warp task
@@ -322,6 +325,7 @@ __device__ __forceinline__ int row_class(long long E, int sort_rows)
 {
     if (E == 0) return -1;
     if (E <= kSmallMax) return 0;
+    if (E <= kWarpAggMax && !sort_rows) return kWarpCls;
     if (E <= kMid1Max) return 1;
     if (E <= kMid2Max) return 2;
     if (E <= kMid3Max && !sort_rows) return 3;
@@ -339,7 +343,7 @@ __global__ void __launch_bounds__(256) k_classify(int C, const long long *__rest
         const int cls = c < C ? row_class(ec[c], sort_rows) : -2;
         if (cls == -1) kc[c] = 0;
 #pragma unroll
-        for (int k = 0; k <= kLongCls; ++k) warp_append(cls == k, c, lists + (long long)k * C, &st->small_cnt[k]);
+        for (int k = 0; k < kNumCls; ++k) warp_append(cls == k, c, lists + (long long)k * C, &st->small_cnt[k]);
     }
 }
 
@@ -543,6 +547,63 @@ __device__ __forceinline__ void agg_insert_list(const AggArgs<WT> &a, long long 
             base = __shfl_sync(GALA_FULL_MASK, base, leader);
             if (created == 1) occ[base + __popc(cb & lanemask_lt())] = (unsigned short)slot;
         }
+    }
+}
+
+// Rows of 33..kWarpAggMax entries in hash-table order: one warp per
+// community with its own shared-memory table (2 kWarpAggMax slots) and list
+// of claimed slots; warps work independently (no block barriers), so eight
+// communities per block are in flight.
+template <typename WT>
+__global__ void __launch_bounds__(256) k_agg_warp_list(AggArgs<WT> a, const int32_t *__restrict__ list)
+{
+    constexpr int T = 2 * kWarpAggMax, LG = 8;
+    static_assert((1 << LG) == T, "table size");
+    __shared__ int skeys[8][T];
+    __shared__ WT svals[8][T];
+    __shared__ unsigned char socc[8][kWarpAggMax];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    int *keys = skeys[wid];
+    WT *vals = svals[wid];
+    unsigned char *occ = socc[wid];
+    for (int j = lane; j < T; j += 32) {
+        keys[j] = -1;
+        vals[j] = 0;
+    }
+    __syncwarp();
+    const int cnt = a.st->small_cnt[kWarpCls];
+    const int wg = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nw = (gridDim.x * blockDim.x) >> 5;
+    for (int i = wg; i < cnt; i += nw) {
+        const int c = list[i];
+        const long long st = a.medge[a.moff[c]];
+        const int E = (int)a.ec[c];  // 33..kWarpAggMax
+        int nocc = 0;
+        for (int b0 = 0; b0 < E; b0 += 32) {
+            const int j = b0 + lane;
+            int created = 0, slot = -1;
+            if (j < E) {
+                created = table_add(keys, vals, T, LG, a.skey[st + j], a.sw[st + j], slot);
+                if (created < 0) {
+                    atomicOr(&a.st->err, kErrHashOverflow);
+                    created = 0;
+                }
+            }
+            const unsigned cb = __ballot_sync(GALA_FULL_MASK, created == 1);
+            if (created == 1) occ[nocc + __popc(cb & lanemask_lt())] = (unsigned char)slot;
+            nocc += __popc(cb);
+        }
+        __syncwarp();
+        const long long o = a.tmp_off[c];
+        for (int q = lane; q < nocc; q += 32) {
+            const int j = occ[q];
+            a.tmp_nbr[o + q] = keys[j];
+            a.tmp_w[o + q] = vals[j];
+            keys[j] = -1;
+            vals[j] = 0;
+        }
+        if (lane == 0) a.kc[c] = nocc;
+        __syncwarp();
     }
 }
 
@@ -1049,7 +1110,7 @@ __global__ void k_set_last_offset(int64_t *offs, int C, const long long *total) 
 
 __global__ void k_contract_reset(DevStats *st)
 {
-    for (int k = 0; k <= kLongCls; ++k) st->small_cnt[k] = 0;
+    for (int k = 0; k < kNumCls; ++k) st->small_cnt[k] = 0;
     st->err = 0;
 }
 
@@ -1303,6 +1364,11 @@ static int contract_t(const LevelGraph &g, const int32_t *comm, ContractBuffers 
     const int nsm = sm_count();
     if (hs.small_cnt[0] > 0) {
         k_agg_small<WT><<<grid_cap((long long)hs.small_cnt[0] * 32, 256, cap), 256, 0, st>>>(a, b.cls_list);
+        note_launch(1);
+    }
+    if (hs.small_cnt[kWarpCls] > 0) {
+        k_agg_warp_list<WT><<<grid_cap((long long)hs.small_cnt[kWarpCls] * 32, 256, nsm * 8), 256, 0, st>>>(
+            a, b.cls_list + (long long)kWarpCls * C);
         note_launch(1);
     }
     if (hs.small_cnt[1] > 0) {

@@ -192,6 +192,7 @@ struct PropRun {
     float threshold = 0.5f;
     int sample_shift = 0;
     int level = 0;
+    int from = 2;  // SKIP: first sweep of a level that may skip vertices
 };
 
 // State of a batch of graphs run as one union graph (gala_louvain_batch).
@@ -222,6 +223,14 @@ struct BatchRun {
     int64_t *h_offs = nullptr;
     int32_t *h_nbr = nullptr, *h_w = nullptr;
     std::vector<void *> stage;
+    // workspace of the one-CTA-per-graph path (allocated on its first use,
+    // for the context's vertex and entry capacity)
+    BatchCtaArgs cta{};
+    int32_t *h_order = nullptr;   // pinned: graphs, largest first
+    double *h_q = nullptr;
+    int32_t *h_c = nullptr, *h_rounds = nullptr, *h_iters = nullptr;
+    int cta_cap = 0;              // graphs the per-graph outputs hold
+    std::vector<void *> cta_dev, cta_host;
     // per-graph host state
     std::vector<long long> m2;
     std::vector<double> prev_q;  // accepted Q of the current level
@@ -245,6 +254,18 @@ struct BatchRun {
         dev.clear();
         host.clear();
         cap = n_cap = 0;
+    }
+    void release_cta()
+    {
+        for (void *p : cta_dev) cudaFree(p);
+        for (void *p : cta_host) cudaFreeHost(p);
+        cta_dev.clear();
+        cta_host.clear();
+        cta = BatchCtaArgs{};
+        h_order = nullptr;
+        h_q = nullptr;
+        h_c = h_rounds = h_iters = nullptr;
+        cta_cap = 0;
     }
     void release_stage()
     {
@@ -458,7 +479,7 @@ gala_status phase1(gala_context *ctx, const LevelGraph &g, long long &m2, double
         const int32_t *lists = iteration == 1 ? b.order : b.act[cur];
         const int *counts = &b.stats->act_count[cur][0];
         // sweep kind: the first sweep of a level and verification sweeps are plain
-        const bool proposal_sweep = pmode == GALA_PROPOSAL_SKIP && iteration > 1 && !verify;
+        const bool proposal_sweep = pmode == GALA_PROPOSAL_SKIP && iteration >= pr->from && !verify;
         ProposalStep ps{};
         if (pmode != GALA_PROPOSAL_OFF) {
             ps.mode = pmode;
@@ -764,6 +785,11 @@ gala_status run_levels(gala_context *ctx, int32_t n0, int64_t E0, const int64_t 
         pr.pv = proposal_view(opt->proposal);
         pr.threshold = opt->proposal_threshold;
         pr.sample_shift = opt->trace_sample_shift;
+        if (opt->proposal_from < 0) {
+            set_error("proposal_from must be >= 0");
+            return GALA_ERR_INVALID;
+        }
+        pr.from = opt->proposal_from > 2 ? opt->proposal_from : 2;
         if (pr.mode == GALA_PROPOSAL_TRACE && pr.pv.cap <= 0) {
             set_error("trace mode needs a proposal with sample capacity");
             return GALA_ERR_INVALID;
@@ -1005,6 +1031,7 @@ void gala_context_destroy(gala_context *ctx)
     if (ctx->batch) {
         ctx->batch->release();
         ctx->batch->release_stage();
+        ctx->batch->release_cta();
         delete ctx->batch;
     }
     for (void *p : ctx->allocs) cudaFree(p);
@@ -1077,7 +1104,7 @@ gala_status gala_context_create(int32_t device, int32_t max_vertices, int64_t ma
          dalloc(ctx, &c.members, n) && dalloc(ctx, &c.mpos, n) && dalloc(ctx, &c.ec, n + 1) &&
          dalloc(ctx, &c.medge, n + 1) && dalloc(ctx, &c.stream_key, E) && dalloc8(ctx, &c.stream_w, E) &&
          dalloc(ctx, &c.tmp_off, n + 1) && dalloc(ctx, &c.tmp_nbr, E) && dalloc8(ctx, &c.tmp_w, E) &&
-         dalloc(ctx, &c.kc, n + 1) && dalloc(ctx, &c.cls_list, 5 * n);
+         dalloc(ctx, &c.kc, n + 1) && dalloc(ctx, &c.cls_list, 6 * n);
     // tables of the rows longer than 4096 entries: at most 4 slots per entry
     // (keys + values), chunk list of at most E / 4096 + n entries
     c.big_pool_ints = 8LL * (long long)E + 64;
@@ -1335,6 +1362,133 @@ gala_status gala_autotune(gala_context *ctx, const gala_graph *const *graphs, in
     return GALA_OK;
 }
 
+namespace {
+
+// One persistent launch over the batch's graphs (batch_cta.cu): each CTA runs
+// whole graphs.  The union CSR is in ctx->offs[1] / nbr[1] / w[1].
+gala_status batch_per_graph(gala_context *ctx, BatchRun &bt, const gala_graph *const *graphs, int G, int32_t n,
+                            long long e_tot, int nmax, bool weighted, const gala_options *opt, int32_t *community_out,
+                            double *modularity_out, int32_t *communities_out, gala_batch_result *res)
+{
+    cudaStream_t st = ctx->stream;
+    gala_status s;
+    if (!bt.cta.K || bt.cta_cap < G) {
+        if ((s = sync_check(st, "batch workspace"))) return s;
+        bt.release_cta();
+        bool ok = true;
+        auto dal = [&](auto **p, size_t cnt) {
+            void *q = nullptr;
+            if (ok && cudaMalloc(&q, (cnt ? cnt : 1) * sizeof(**p)) == cudaSuccess) {
+                bt.cta_dev.push_back(q);
+                *p = (std::remove_reference_t<decltype(*p)>)q;
+            } else {
+                ok = false;
+            }
+        };
+        auto hal = [&](auto **p, size_t cnt) {
+            void *q = nullptr;
+            if (ok && cudaMallocHost(&q, (cnt ? cnt : 1) * sizeof(**p)) == cudaSuccess) {
+                bt.cta_host.push_back(q);
+                *p = (std::remove_reference_t<decltype(*p)>)q;
+            } else {
+                ok = false;
+            }
+        };
+        BatchCtaArgs &a = bt.cta;
+        const size_t nv = (size_t)ctx->n_cap, nvo = nv + (size_t)G + 1, ne = (size_t)std::max<int64_t>(ctx->e_cap, 1);
+        int32_t **vert[] = {&a.K, &a.Self, &a.Tot, &a.In, &a.prev, &a.cur, &a.size, &a.cnt, &a.newid, &a.rl,
+                            &a.cursor, &a.members, &a.kc};
+        for (auto p : vert) dal(p, nv);
+        dal(&a.moff, nvo);
+        dal(&a.active, nv);
+        for (int k = 0; k < 2; ++k) {
+            dal(&a.loffs[k], nvo);
+            dal(&a.lnbr[k], ne);
+            dal(&a.lw[k], ne);
+        }
+        int32_t *order = nullptr;
+        dal(&order, G);
+        a.order = order;
+        dal(&a.q_out, G);
+        dal(&a.c_out, G);
+        dal(&a.rounds_out, G);
+        dal(&a.iters_out, G);
+        dal(&a.queue, 2);
+        // dense tables of long rows: one per warp of the largest grid
+        dal(&a.gacc, batch_cta_gacc_ints(batch_cta_grid(1 << 30), kCtaMaxN));
+        hal(&bt.h_order, G);
+        hal(&bt.h_q, G);
+        hal(&bt.h_c, G);
+        hal(&bt.h_rounds, G);
+        hal(&bt.h_iters, G);
+        if (!ok) {
+            cudaGetLastError();
+            bt.release_cta();
+            set_error("gala_louvain_batch: workspace of the per-graph run could not be allocated");
+            return GALA_ERR_OOM;
+        }
+        a.err = a.queue + 1;
+        bt.cta_cap = G;
+    }
+    BatchCtaArgs a = bt.cta;
+    a.G = G;
+    a.vstart = bt.vstart();
+    a.estart = bt.estart();
+    a.u_offs = ctx->offs[1];
+    a.u_nbr = ctx->nbr[1];
+    a.u_w = weighted ? ctx->w[1] : nullptr;
+    a.labels = ctx->orig;
+    a.min_mod = opt ? opt->min_modularity : 1e-6;
+    a.max_levels = opt ? opt->max_levels : 0;
+    a.nmax = nmax;
+    // largest graphs first: the queue's tail holds the short ones
+    for (int i = 0; i < G; ++i) bt.h_order[i] = i;
+    std::sort(bt.h_order, bt.h_order + G, [&](int x, int y) {
+        const int64_t ex = graphs[x]->entries(), ey = graphs[y]->entries();
+        return ex != ey ? ex > ey : x < y;
+    });
+    const int grid = batch_cta_grid(G);
+    cudaMemcpyAsync((void *)a.order, bt.h_order, (size_t)G * sizeof(int32_t), cudaMemcpyHostToDevice, st);
+    cudaMemsetAsync(a.queue, 0, 2 * sizeof(int), st);
+    cudaMemsetAsync(a.gacc, 0, batch_cta_gacc_ints(grid, nmax) * sizeof(int32_t), st);
+    cudaEventRecord(ctx->ev[0], st);
+    batch_cta_launch(a, grid, st);
+    cudaEventRecord(ctx->ev[1], st);
+    int herr = 0;
+    cudaMemcpyAsync(bt.h_q, a.q_out, (size_t)G * sizeof(double), cudaMemcpyDeviceToHost, st);
+    cudaMemcpyAsync(bt.h_c, a.c_out, (size_t)G * sizeof(int32_t), cudaMemcpyDeviceToHost, st);
+    cudaMemcpyAsync(bt.h_rounds, a.rounds_out, (size_t)G * sizeof(int32_t), cudaMemcpyDeviceToHost, st);
+    cudaMemcpyAsync(bt.h_iters, a.iters_out, (size_t)G * sizeof(int32_t), cudaMemcpyDeviceToHost, st);
+    cudaMemcpyAsync(&herr, a.err, sizeof(int), cudaMemcpyDeviceToHost, st);
+    cudaEventRecord(ctx->ev[6], st);
+    cudaMemcpyAsync(community_out, ctx->orig, (size_t)n * sizeof(int32_t), cudaMemcpyDeviceToHost, st);
+    cudaEventRecord(ctx->ev[7], st);
+    if ((s = sync_check(st, "per-graph batch run"))) return s;
+    if (herr) {
+        set_error("gala_louvain_batch: a graph's total weight exceeds the int32 range");
+        return GALA_ERR_INVALID;
+    }
+    res->time_total_ms = ev_ms(ctx->ev[0], ctx->ev[1]);
+    res->time_phase1_ms = res->time_total_ms;
+    res->time_contract_ms = 0;
+    res->time_d2h_ms = ev_ms(ctx->ev[6], ctx->ev[7]);
+    int rounds = 0, iters = 0;
+    for (int i = 0; i < G; ++i) {
+        if (modularity_out) modularity_out[i] = bt.h_q[i];
+        if (communities_out) communities_out[i] = bt.h_c[i];
+        rounds = std::max(rounds, bt.h_rounds[i]);
+        iters = std::max(iters, bt.h_iters[i]);
+    }
+    res->num_graphs = G;
+    res->num_levels = rounds;
+    res->total_iterations = iters;
+    res->vertices = n;
+    res->entries = e_tot;
+    return GALA_OK;
+}
+
+}  // namespace
+
 gala_status gala_louvain_batch(gala_context *ctx, const gala_graph *const *graphs, int32_t count,
                                const gala_options *opt, int32_t *community_out, double *modularity_out,
                                int32_t *communities_out, gala_batch_result *res)
@@ -1536,6 +1690,18 @@ gala_status gala_louvain_batch(gala_context *ctx, const gala_graph *const *graph
     batch_gid_fill(G, bt.goff, bt.gid, st);
     if ((s = sync_check(st, "batch host to device copy"))) return s;
     res->time_h2d_ms = ev_ms(ctx->ev[6], ctx->ev[7]);
+    int nmax = 0;
+    for (int i = 0; i < G; ++i) nmax = std::max(nmax, graphs[i]->n);
+    if (!(opt && opt->batch_mode == 1) && nmax <= kCtaMaxN) {
+        s = batch_per_graph(ctx, bt, graphs, G, n, e_tot, nmax, weighted, opt, community_out, modularity_out,
+                            communities_out, res);
+        if (s) return s;
+        res->h2d_bytes = ((long long)n + 1) * 8 + e_tot * 4 * (weighted ? 2 : 1) + ((long long)G + 1) * 8 +
+                         (mapped ? 3LL * bt.cap + 2LL * G + 2 : 2LL * G + 2) * 8 + (long long)G * 4;
+        res->d2h_bytes = (long long)n * 4 + (long long)G * (8 + 3 * 4);
+        res->kernel_launches = gala_kernel_launch_count() - l0;
+        return GALA_OK;
+    }
     Phase1Buffers &b = ctx->p1;
     b.gid = bt.gid;
     b.m2g = bt.m2g;

@@ -192,6 +192,34 @@ void batch_gather(int G, const BatchSrc &src, int64_t *offs, int32_t *nbr, int32
 // offs[vstart[g]+1 ...], its entries at nbr[estart[g] ...]): shift them into
 // union ids and offsets in place.
 void batch_shift(int G, const int64_t *vstart, const int64_t *estart, int64_t *offs, int32_t *nbr, cudaStream_t st);
+// A batch whose graphs all have at most kCtaMaxN vertices runs in one
+// persistent launch, one CTA per graph at a time (batch_cta.cu).  All arrays
+// are union-indexed: vertex arrays at the graph's first vertex, offsets
+// arrays (one more entry per graph) at first vertex + graph index, entry
+// arrays at the graph's first entry.
+constexpr int kCtaMaxN = 4096;
+struct BatchCtaArgs {
+    int G;
+    const int32_t *order;  // graphs, largest first
+    const int64_t *vstart, *estart;
+    const int64_t *u_offs;  // union CSR (device layout)
+    const int32_t *u_nbr;
+    const int32_t *u_w;     // null: unit weights
+    int32_t *K, *Self, *Tot, *In, *prev, *cur, *size, *cnt, *newid, *rl, *cursor, *members, *kc, *moff;
+    uint8_t *active;
+    int32_t *loffs[2], *lnbr[2], *lw[2];  // contracted level graphs (ping-pong)
+    int32_t *labels;  // out: every input vertex's community, local to its graph
+    double *q_out;
+    int32_t *c_out, *rounds_out, *iters_out;
+    int *queue, *err;
+    double min_mod;
+    int max_levels;
+    int nmax;       // largest graph (vertices)
+    int32_t *gacc;  // per warp of the grid: nmax ints, zero (dense tables of long rows)
+};
+int batch_cta_grid(int G);
+size_t batch_cta_gacc_ints(int grid, int nmax);
+void batch_cta_launch(const BatchCtaArgs &a, int grid, cudaStream_t st);
 // labels[v] -= goff[g] for the input vertices v of every graph g.
 void batch_local_labels(int G, const int64_t *vstart, const int64_t *goff, int32_t *labels, cudaStream_t st);
 

@@ -51,7 +51,8 @@ class Options(ctypes.Structure):
                 ("proposal_mode", ctypes.c_int32), ("proposal_threshold", ctypes.c_float),
                 ("trace_sample_shift", ctypes.c_int32), ("sorted_levels", ctypes.c_int32), ("proposal", ctypes.c_void_p),
                 ("distinct_rows", ctypes.c_int32), ("bin5_block", ctypes.c_int32),
-                ("bin_max", ctypes.c_int32 * 3), ("refine", ctypes.c_int32), ("level_dir", ctypes.c_char_p)]
+                ("bin_max", ctypes.c_int32 * 3), ("refine", ctypes.c_int32), ("level_dir", ctypes.c_char_p),
+                ("proposal_from", ctypes.c_int32), ("batch_mode", ctypes.c_int32)]
 
 
 class Tuning(ctypes.Structure):
@@ -331,9 +332,13 @@ class Graph:
         _check(load().gala_graph_pin(self.h))
 
     def info(self):
-        n, e, w = ctypes.c_int32(), ctypes.c_int64(), ctypes.c_int32()
-        _check(load().gala_graph_info(self.h, ctypes.byref(n), ctypes.byref(e), ctypes.byref(w)))
-        return n.value, e.value, w.value  # 0 unweighted, 1 int32, 2 float32 weights
+        """(vertices, CSR entries, weight kind: 0 none, 1 int32, 2 float32);
+        a graph never changes, so the answer is kept after the first call."""
+        if getattr(self, "_info", None) is None:
+            n, e, w = ctypes.c_int32(), ctypes.c_int64(), ctypes.c_int32()
+            _check(load().gala_graph_info(self.h, ctypes.byref(n), ctypes.byref(e), ctypes.byref(w)))
+            self._info = (n.value, e.value, w.value)
+        return self._info
 
     def arrays(self):
         """(offs[n+1] with leading 0, nbr, w or None) as numpy copies."""
@@ -389,7 +394,7 @@ class Context:
 
     def louvain(self, graph, min_mod=1e-6, max_levels=0, verbose=False, iter_capacity=4096, fp64_gains=False,
                 proposal=None, mode=PROPOSAL_OFF, threshold=0.5, sample_shift=0, sorted_levels=False,
-                use_graphs=False, tuning=None, level_dir=None, refine=False):
+                use_graphs=False, tuning=None, level_dir=None, refine=False, proposal_from=0):
         """gala_louvain: host graph in, host labels out.  `proposal` (a
         Proposal) with mode PROPOSAL_TRACE records training samples, with
         PROPOSAL_SKIP decides only the vertices it proposes; `refine` turns
@@ -404,7 +409,8 @@ class Context:
                             fp64_gains=int(fp64_gains), proposal_mode=int(mode),
                             proposal_threshold=float(threshold), trace_sample_shift=int(sample_shift),
                             sorted_levels=int(sorted_levels), use_graphs=int(use_graphs),
-                            proposal=proposal.h if proposal is not None else None, refine=int(refine))
+                            proposal=proposal.h if proposal is not None else None, refine=int(refine),
+                            proposal_from=int(proposal_from))
         if tuning:
             o.bin_max = (ctypes.c_int32 * 3)(*tuning["bin_max"])
             o.bin5_block = tuning["bin5_block"]
@@ -426,7 +432,7 @@ class Context:
         _check(load().gala_autotune(self.h, hs, len(graphs), ctypes.byref(o), repeats, ctypes.byref(t)))
         return t.to_dict()
 
-    def louvain_batch(self, graphs, min_mod=1e-6, max_levels=0, use_graphs=False, tuning=None):
+    def louvain_batch(self, graphs, min_mod=1e-6, max_levels=0, use_graphs=False, tuning=None, batch_mode=0):
         """gala_louvain_batch: many host graphs in one union run.  Returns the
         per-graph labels (local community ids), modularity and community
         counts plus the batch timings."""
@@ -437,7 +443,8 @@ class Context:
         c = np.zeros(G, dtype=np.int32)
         hs = (_vp * G)(*[g.h for g in graphs])
         r = BatchResult()
-        o = default_options(min_modularity=min_mod, max_levels=max_levels, use_graphs=int(use_graphs))
+        o = default_options(min_modularity=min_mod, max_levels=max_levels, use_graphs=int(use_graphs),
+                            batch_mode=int(batch_mode))
         if tuning:
             o.bin_max = (ctypes.c_int32 * 3)(*tuning["bin_max"])
             o.bin5_block = tuning["bin5_block"]

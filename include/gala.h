@@ -107,6 +107,17 @@ typedef struct {
        composed with labels_<r+1> are the full run's.  Not for batches or
        float-weight graphs. */
     const char *level_dir;
+    int32_t proposal_from;      /* SKIP: the first sweep of a level that decides
+                                   only proposed vertices (0 = 2, the sweep after
+                                   the level's first; larger values keep more
+                                   sweeps of every level plain) */
+    int32_t batch_mode;         /* gala_louvain_batch: 0 = one persistent launch
+                                   in which each CTA runs a whole graph (every
+                                   round) when all graphs have at most 4096
+                                   vertices, else the union run; 1 = always the
+                                   union run (every sweep one set of launches
+                                   for all graphs).  Both give the same
+                                   partitions. */
 } gala_options;
 
 /* Tuning of the degree bins (the fields of gala_options they set). */

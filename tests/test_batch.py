@@ -142,3 +142,68 @@ def test_batch_staged_and_page_locked_inputs_agree(ffi, torch_cuda):
             assert np.array_equal(a, b), k
         assert np.array_equal(staged[k]["modularity"], again[k]["modularity"]), k
         assert np.array_equal(staged[k]["communities"], again[k]["communities"]), k
+
+
+def _random_weighted(rng, n, deg, wmax, isolated=0):
+    """Random symmetric int-weighted graph; the last `isolated` vertices have
+    no edges."""
+    m = n * deg // 2
+    live = n - isolated
+    u = rng.integers(0, live, m)
+    v = rng.integers(0, live, m)
+    keep = u != v
+    u, v = u[keep], v[keep]
+    key = np.unique(np.minimum(u, v).astype(np.int64) * n + np.maximum(u, v))
+    a, b = key // n, key % n
+    rows = np.concatenate([a, b])
+    cols = np.concatenate([b, a]).astype(np.int32)
+    wt = rng.integers(1, wmax + 1, a.shape[0])
+    ww = np.concatenate([wt, wt]).astype(np.int32)
+    order = np.lexsort((cols, rows))
+    rows, cols, ww = rows[order], cols[order], ww[order]
+    offs = np.zeros(n + 1, dtype=np.int64)
+    np.add.at(offs, rows + 1, 1)
+    return np.cumsum(offs), cols, ww
+
+
+@pytest.mark.gpu
+def test_batch_one_cta_per_graph_equals_union_run_singles_and_oracle(ffi, oracle, torch_cuda):
+    """Batches whose graphs all have at most 4096 vertices run in one
+    persistent launch, each CTA running whole graphs (every sweep, the
+    contraction, every round).  Their partitions, modularity and community
+    counts must equal the union run's, the single-graph runs' and the
+    oracle's, bit for bit."""
+    rng = np.random.default_rng(31)
+    graphs = ffi.Graph.sbm_batch(40, n_min=50, n_max=4000, seed=17)
+    graphs.append(ffi.Graph.sbm(1024, 32, 0.3, 0.005, 5))
+    for n, deg, wmax, iso in ((300, 8, 6, 0), (2500, 14, 9, 40), (4096, 6, 3, 0), (60, 3, 2, 7)):
+        graphs.append(ffi.Graph.from_csr(*_random_weighted(rng, n, deg, wmax, iso)))
+    graphs.append(ffi.Graph.from_csr(*_random_weighted(rng, 2, 1, 1)))  # one edge
+    tot_n = sum(g.info()[0] for g in graphs)
+    tot_e = sum(g.info()[1] for g in graphs)
+    assert max(g.info()[0] for g in graphs) <= 4096
+    ctx = ffi.Context(tot_n, tot_e)
+    r = ctx.louvain_batch(graphs)
+    r2 = ctx.louvain_batch(graphs)  # the workspace is reused
+    u = ctx.louvain_batch(graphs, batch_mode=1)
+    r1 = ctx.louvain_batch(graphs, max_levels=1)
+    u1 = ctx.louvain_batch(graphs, max_levels=1, batch_mode=1)
+    ctx.close()
+    assert r["kernel_launches"] < 10 < u["kernel_launches"]
+    for i in range(len(graphs)):
+        for other in (r2, u):
+            assert np.array_equal(r["labels"][i], other["labels"][i]), i
+            assert r["modularity"][i] == other["modularity"][i], i
+            assert r["communities"][i] == other["communities"][i], i
+        assert np.array_equal(r1["labels"][i], u1["labels"][i]), i
+        assert r1["modularity"][i] == u1["modularity"][i], i
+    singles = _singles(ffi, graphs)
+    for i, (g, s) in enumerate(zip(graphs, singles)):
+        assert np.array_equal(r["labels"][i], s["labels"]), i
+        assert r["modularity"][i] == s["modularity"], i
+        assert abs(g.modularity(r["labels"][i]) - r["modularity"][i]) <= 1e-9
+    for i in (0, 17, len(graphs) - 6, len(graphs) - 3, len(graphs) - 2):
+        offs, nbr, w = graphs[i].arrays()
+        o = oracle.louvain(offs, nbr, w)
+        assert np.array_equal(r["labels"][i], o["labels"]), i
+        assert r["modularity"][i] == o["modularity"], i
