@@ -26,7 +26,7 @@ namespace gala {
 
 namespace {
 
-constexpr int kCtaThreads = 256;
+constexpr int kCtaThreads = 512;
 constexpr int kCtaWarps = kCtaThreads / 32;
 constexpr int kWT = 512;  // slots of a warp's shared-memory table
 constexpr int kWTLog = 9;
@@ -55,7 +55,7 @@ struct WarpTable {
 };
 
 struct CtaShared {
-    WarpTable tab[kCtaWarps];
+    WarpTable *tab;  // kCtaWarps tables in dynamic shared memory
     long long red_ll[kCtaWarps];
     unsigned long long red_u[kCtaWarps];
     int red_i[kCtaWarps];
@@ -456,7 +456,9 @@ __device__ int cta_contract(const BatchCtaArgs &a, const LevelView &g, int n, in
 
 __global__ void __launch_bounds__(kCtaThreads) k_batch_cta(BatchCtaArgs a)
 {
+    extern __shared__ WarpTable cta_tabs[];
     __shared__ CtaShared sh;
+    sh.tab = cta_tabs;  // every thread stores the same address before using it
     const int wid = threadIdx.x >> 5;
     // this warp's dense table for long rows (zero, and left zero by every use)
     int *gacc = a.gacc + ((size_t)blockIdx.x * kCtaWarps + wid) * (size_t)a.nmax;
@@ -527,10 +529,17 @@ __global__ void __launch_bounds__(kCtaThreads) k_batch_cta(BatchCtaArgs a)
 
 }  // namespace
 
+constexpr size_t kCtaSmem = sizeof(WarpTable) * kCtaWarps;
+
+void batch_cta_configure()
+{
+    cudaFuncSetAttribute(k_batch_cta, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kCtaSmem);
+}
+
 int batch_cta_grid(int G)
 {
     int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch_cta, kCtaThreads, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch_cta, kCtaThreads, kCtaSmem);
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -542,7 +551,7 @@ size_t batch_cta_gacc_ints(int grid, int nmax) { return (size_t)grid * kCtaWarps
 
 void batch_cta_launch(const BatchCtaArgs &a, int grid, cudaStream_t st)
 {
-    k_batch_cta<<<grid, kCtaThreads, 0, st>>>(a);
+    k_batch_cta<<<grid, kCtaThreads, kCtaSmem, st>>>(a);
     note_launch(1);
 }
 

@@ -1140,6 +1140,7 @@ gala_status gala_context_create(int32_t device, int32_t max_vertices, int64_t ma
     cudaMemsetAsync(ctx->d_stats, 0, sizeof(DevStats), ctx->stream);
     p1_configure_kernels();
     contract_configure_kernels();
+    batch_cta_configure();
     bind_contract_buffers(ctx);
     if ((ce = cudaStreamSynchronize(ctx->stream)) != cudaSuccess) {
         gala_context_destroy(ctx);

@@ -217,6 +217,7 @@ struct BatchCtaArgs {
     int nmax;       // largest graph (vertices)
     int32_t *gacc;  // per warp of the grid: nmax ints, zero (dense tables of long rows)
 };
+void batch_cta_configure();
 int batch_cta_grid(int G);
 size_t batch_cta_gacc_ints(int grid, int nmax);
 void batch_cta_launch(const BatchCtaArgs &a, int grid, cudaStream_t st);
