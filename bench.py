@@ -78,6 +78,8 @@ def parse():
                    help="first sweep of a level that decides only proposed vertices")
     p.add_argument("--profile", action="store_true",
                    help="one device-resident run and a short summary (for ncu captures)")
+    p.add_argument("--profile-batch", type=int, default=0, metavar="G",
+                   help="one batched run of the first G graphs of the batch workload (for ncu captures)")
     p.add_argument("--profile-learned", action="store_true",
                    help="one learned-proposal run (SKIP mode) after one plain run (for ncu launch lists)")
     p.add_argument("--fp64-gains", action="store_true", help="evaluate every gain in FP64")
@@ -573,6 +575,17 @@ def main():
         return
     import torch
     import gala_ffi as ffi
+    if args.profile_batch:
+        b = BATCH
+        gs = ffi.Graph.sbm_batch(args.profile_batch, b["n_min"], b["n_max"], b["k_min"], b["k_max"], b["deg_min"],
+                                 b["deg_max"], b["mix_min"], b["mix_max"], seed=b["seed"])
+        bctx = ffi.Context(sum(g.info()[0] for g in gs), sum(g.info()[1] for g in gs))
+        r = bctx.louvain_batch(gs)
+        torch.cuda.synchronize()
+        print(json.dumps({"profile_batch": args.profile_batch, "device_ms": r["time_total_ms"],
+                          "kernel_launches": r["kernel_launches"], "levels": r["num_levels"]}), flush=True)
+        bctx.close()
+        return
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
