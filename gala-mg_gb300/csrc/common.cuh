@@ -83,12 +83,20 @@ struct DevStats {
     long long trace_mark;              // sample count before the current sweep
     unsigned long long skipped;        // active vertices not decided (proposal said stay)
     unsigned long long skipped_edges;  // row entries of the skipped vertices
+    // contraction counts that stay on the device between its kernels
+    long long ccount;       // communities C
+    long long new_entries;  // entries of the contracted level
+    long long big_slots;    // long rows: table slots
+    long long big_nwork;    // long rows: stream chunks
+    long long big_ntwork;   // long rows: table chunks
+    long long big_lwork;    // long rows: slot-list chunks
 };
 
 constexpr int kErrHashOverflow = 1;
 constexpr int kErrProbeLimit = 2;
 constexpr int kErrBadLabel = 4;
 constexpr int kErrBadIndex = 8;
+constexpr int kErrCapacity = 16;  // contraction: long-row tables exceed their scratch
 
 // ---------------------------------------------------------------------------
 // Weight types.  Integer graphs (the reference's int32 weights) run with

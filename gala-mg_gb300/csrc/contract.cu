@@ -83,16 +83,19 @@ struct OpRowNonEmpty {  // in = offs: row idx has entries
 // Walk list of the rows that have entries: nz_rows[i] (row id) and
 // nz_offs[i] (its first entry), nz_offs[count] = E, count in st->nz_rows.
 // Row walks over it never step through runs of empty rows.
-__global__ void k_nz_tail(DevStats *st, long long *nz_offs, long long E)
+// (E, or *dE on the device when dE is set)
+__global__ void k_nz_tail(DevStats *st, long long *nz_offs, long long E, const long long *dE)
 {
     const int cnt = (int)st->total;
     st->nz_rows = cnt;
-    nz_offs[cnt] = E;
+    nz_offs[cnt] = dE ? *dE : E;
 }
 
+// rows [0, n), or [0, min(n, *dn)) when dn is set
 __global__ void k_nz_scatter(const int64_t *__restrict__ offs, int n, const int32_t *__restrict__ pos,
-                             int32_t *nz_rows, long long *nz_offs)
+                             int32_t *nz_rows, long long *nz_offs, const long long *dn)
 {
+    if (dn && *dn < n) n = (int)*dn;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const long long s = offs[i];
         if (offs[i + 1] > s) {
@@ -244,13 +247,14 @@ __global__ void k_hist(const int32_t *__restrict__ comm, int n, int32_t *cnt)
         atomicAdd(&cnt[comm[v]], 1);
 }
 
-// New label of every vertex and member count of every new community; with
-// tot/k_out, K_new of community c is its total Tot[c] (the weight of the new
-// row equals the weighted degrees of its members, exactly).
+// New label of every vertex and member count of every new community (its
+// entry count ec and, with self_out, its Self start at 0); with tot/k_out,
+// K_new of community c is its total Tot[c] (the weight of the new row equals
+// the weighted degrees of its members, exactly).
 template <typename WT>
 __global__ void k_relabel(const int32_t *__restrict__ comm, const int32_t *__restrict__ newid,
-                          const int32_t *__restrict__ cnt, int n, int32_t *lab, int32_t *csz,
-                          const WT *__restrict__ tot, WT *k_out)
+                          const int32_t *__restrict__ cnt, int n, int32_t *lab, int32_t *csz, long long *ec,
+                          const WT *__restrict__ tot, WT *k_out, WT *self_out)
 {
     for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) {
         lab[v] = newid[comm[v]];
@@ -258,7 +262,9 @@ __global__ void k_relabel(const int32_t *__restrict__ comm, const int32_t *__res
         if (k > 0) {
             const int c = newid[v];
             csz[c] = k;
+            ec[c] = 0;
             if (k_out) k_out[c] = tot[v];
+            if (self_out) self_out[c] = 0;
         }
     }
 }
@@ -269,12 +275,15 @@ __global__ void k_compose(int32_t *orig, int n_orig, const int32_t *__restrict__
         orig[i] = lab[orig[i]];
 }
 
+// Member buckets: csz[c] counts down to 0, so the members of c fill
+// [moff[c], moff[c] + size) from the end (no cursor copy of moff).
 __global__ void k_member_scatter(const int32_t *__restrict__ lab, const int64_t *__restrict__ offs, int n,
-                                 int32_t *cursor, int32_t *members, int32_t *mpos, long long *ec)
+                                 const int32_t *__restrict__ moff, int32_t *csz, int32_t *members, int32_t *mpos,
+                                 long long *ec)
 {
     for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) {
         int c = lab[v];
-        int p = atomicAdd(&cursor[c], 1);
+        int p = moff[c] + atomicSub(&csz[c], 1) - 1;
         members[p] = v;
         mpos[v] = p;
         long long d = offs[v + 1] - offs[v];
@@ -283,7 +292,8 @@ __global__ void k_member_scatter(const int32_t *__restrict__ lab, const int64_t 
 }
 
 // Community-ordered edge stream over contiguous entry ranges: entry j of row
-// v goes to medge[mpos[v]] + (j - offs[v]).  Rows are walked through the
+// v goes to medge[mpos[v]] + (j - offs[v]).  Unweighted levels (W false)
+// write no weights: the aggregation counts every entry as 1.  Rows are walked through the
 // list of rows with entries (nz_rows / nz_offs); each row's destination
 // (medge[mpos[v]] - offs[v]) is loaded once per row window.
 template <typename WT, bool W>
@@ -316,7 +326,7 @@ __global__ void __launch_bounds__(256) k_stream_fill(int n, long long E, const i
                 return;
             }
             skey[dst] = lab[nbr[j]];
-            sw[dst] = W ? w[j] : 1;
+            if (W) sw[dst] = w[j];
         });
     }
 }
@@ -332,18 +342,20 @@ __device__ __forceinline__ int row_class(long long E, int sort_rows)
     return kLongCls;
 }
 
-// Size classes with warp-aggregated appends (one atomic per warp and class);
-// communities without entries get an empty row right away.
-__global__ void __launch_bounds__(256) k_classify(int C, const long long *__restrict__ ec, int32_t *lists,
+// Size classes with warp-aggregated appends (one atomic per warp and class;
+// class k lists its communities from lists + k * lstride); communities without
+// entries get an empty row right away.
+__global__ void __launch_bounds__(256) k_classify(const long long *__restrict__ ec, int32_t *lists, long long lstride,
                                                   int32_t *kc, DevStats *st, int sort_rows)
 {
+    const int C = (int)st->ccount;
     const int stride = gridDim.x * blockDim.x;
     for (int base = blockIdx.x * blockDim.x; base < C; base += stride) {
         const int c = base + threadIdx.x;
         const int cls = c < C ? row_class(ec[c], sort_rows) : -2;
         if (cls == -1) kc[c] = 0;
 #pragma unroll
-        for (int k = 0; k < kNumCls; ++k) warp_append(cls == k, c, lists + (long long)k * C, &st->small_cnt[k]);
+        for (int k = 0; k < kNumCls; ++k) warp_append(cls == k, c, lists + k * lstride, &st->small_cnt[k]);
     }
 }
 
@@ -353,13 +365,13 @@ struct AggArgs {
     const long long *__restrict__ medge;
     const long long *__restrict__ ec;
     const int32_t *__restrict__ skey;
-    const WT *__restrict__ sw;
+    const WT *__restrict__ sw;  // null: unweighted level, every entry weighs 1
     const long long *__restrict__ tmp_off;
     int32_t *tmp_nbr;
     WT *tmp_w;
     int32_t *kc;
-    DevStats *st;
-    int C;
+    DevStats *st;  // st->ccount = C
+    __device__ __forceinline__ WT w_at(long long i) const { return sw ? sw[i] : (WT)1; }
 };
 
 // Rows of at most 32 entries: one warp, rank of each distinct key by a
@@ -380,7 +392,7 @@ __global__ void __launch_bounds__(256) k_agg_small(AggArgs<WT> a, const int32_t 
         WT wt = 0;
         if (valid) {
             key = a.skey[st + lane];
-            wt = a.sw[st + lane];
+            wt = a.w_at(st + lane);
         }
         const unsigned m = __match_any_sync(GALA_FULL_MASK, key);
         const WT sum = group_sum(m, wt);
@@ -446,7 +458,7 @@ __device__ __forceinline__ int agg_insert(const AggArgs<WT> &a, long long st, in
         WT wt = 0;
         if (valid) {
             key = a.skey[st + j];
-            wt = a.sw[st + j];
+            wt = a.w_at(st + j);
         }
         const unsigned m = __match_any_sync(GALA_FULL_MASK, key);
         const WT sum = group_sum(m, wt);
@@ -526,7 +538,7 @@ __device__ __forceinline__ void agg_insert_list(const AggArgs<WT> &a, long long 
         WT wt = 0;
         if (valid) {
             key = a.skey[st + j];
-            wt = a.sw[st + j];
+            wt = a.w_at(st + j);
         }
         // shared-memory tables take every entry on its own (cheaper than a
         // warp-level match of equal keys); the global tables of long rows do
@@ -583,7 +595,7 @@ __global__ void __launch_bounds__(256) k_agg_warp_list(AggArgs<WT> a, const int3
             const int j = b0 + lane;
             int created = 0, slot = -1;
             if (j < E) {
-                created = table_add(keys, vals, T, LG, a.skey[st + j], a.sw[st + j], slot);
+                created = table_add(keys, vals, T, LG, a.skey[st + j], a.w_at(st + j), slot);
                 if (created < 0) {
                     atomicOr(&a.st->err, kErrHashOverflow);
                     created = 0;
@@ -666,7 +678,8 @@ __global__ void __launch_bounds__(BLOCK) k_agg_mid(AggArgs<WT> a, const int32_t 
         const int c = list[i];
         const long long st = a.medge[a.moff[c]];
         const int E = (int)a.ec[c];
-        const int cap = E < a.C ? E : a.C;
+        const int C = (int)a.st->ccount;
+        const int cap = E < C ? E : C;
         int T = next_pow2_int(2LL * cap);
         if (T < 64) T = 64;
         if (T > TMAX) T = TMAX;
@@ -724,10 +737,15 @@ struct BigArgs {
     long long *gwords;
     const long long *__restrict__ gofs;
     int32_t *pool;
-    long long pool_half;  // keys at pool[0, half), values at pool[half, 2 half)
+    long long pool_half;  // keys at pool[0, half), values (WT, 8-byte aligned) from pool[half]
+    long long work_cap;   // capacity of work
+    long long twork_cap;  // capacity of twork
     unsigned *bits;       // bitmaps of the rows ranked by bitmap
     unsigned *pref;       // exclusive prefix of their popcounts
 };
+
+// Long-row kernels run only while the tables fit their scratch.
+__device__ __forceinline__ bool big_off(const DevStats *st) { return (st->err & kErrCapacity) != 0; }
 
 // Table size and chunk counts of every class-3 community.  A dense table
 // (slot = community id) is used when a hash table would not be smaller.
@@ -735,12 +753,13 @@ template <typename WT>
 __global__ void k_big_plan(AggArgs<WT> a, BigArgs b)
 {
     const int cnt = a.st->small_cnt[kLongCls];
+    const long long C = a.st->ccount;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < cnt; i += gridDim.x * blockDim.x) {
         const long long E = a.ec[b.list[i]];
-        const long long cap = E < a.C ? E : a.C;
+        const long long cap = E < C ? E : C;
         long long T = next_pow2_ll(cap + cap / 2);  // load at most 2/3
-        int dense = T >= a.C;
-        if (dense) T = a.C;
+        int dense = T >= C;
+        if (dense) T = C;
         b.T[i] = T;
         b.mode[i] = dense;
         b.chunks[i] = (E + kChunk - 1) / kChunk;
@@ -750,13 +769,31 @@ __global__ void k_big_plan(AggArgs<WT> a, BigArgs b)
     }
 }
 
-__global__ void k_big_tail(BigArgs b, const DevStats *st)
+// toff[cnt] / coff[cnt] / tcoff[cnt] close the last segments; tables or
+// chunk lists beyond their scratch set kErrCapacity, which stops the other
+// long-row kernels (the host reports it after the contraction).
+__global__ void k_big_tail(BigArgs b, DevStats *st)
 {
-    // toff[cnt] / coff[cnt] / tcoff[cnt] close the last segments
     const int cnt = st->small_cnt[kLongCls];
-    ((long long *)b.toff)[cnt] = st->total;
-    ((long long *)b.coff)[cnt] = st->total2;
-    ((long long *)b.tcoff)[cnt] = st->total3;
+    ((long long *)b.toff)[cnt] = st->big_slots;
+    ((long long *)b.coff)[cnt] = st->big_nwork;
+    ((long long *)b.tcoff)[cnt] = st->big_ntwork;
+    if (st->big_slots > b.pool_half || st->big_nwork > b.work_cap || st->big_ntwork > b.twork_cap)
+        st->err |= kErrCapacity;
+}
+
+// Empty tables: keys -1, values 0, over the slots the plan counted.
+template <typename WT>
+__global__ void k_big_clear(BigArgs b, const DevStats *st)
+{
+    if (big_off(st)) return;
+    const long long slots = st->big_slots;
+    WT *vals = (WT *)(b.pool + b.pool_half);
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < slots;
+         i += (long long)gridDim.x * blockDim.x) {
+        b.pool[i] = -1;
+        vals[i] = 0;
+    }
 }
 
 // stream chunk -> community and table chunk -> community, one warp per
@@ -767,7 +804,7 @@ __global__ void k_big_work(AggArgs<WT> a, BigArgs b)
     const int lane = threadIdx.x & 31;
     const int wg = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int nw = (gridDim.x * blockDim.x) >> 5;
-    const int cnt = a.st->small_cnt[kLongCls];
+    const int cnt = big_off(a.st) ? 0 : a.st->small_cnt[kLongCls];
     for (int i = wg; i < cnt; i += nw) {
         long long o = b.coff[i], k = b.coff[i + 1] - o;
         for (long long j = lane; j < k; j += 32) b.work[o + j] = i;
@@ -794,8 +831,10 @@ constexpr size_t big_sm_smem()
     return (size_t)kSmT * (sizeof(WT) + sizeof(int) + sizeof(unsigned short));
 }
 template <typename WT>
-__global__ void __launch_bounds__(512) k_big_insert_sm(AggArgs<WT> a, BigArgs b, long long nwork, int lists)
+__global__ void __launch_bounds__(512) k_big_insert_sm(AggArgs<WT> a, BigArgs b, int lists)
 {
+    const long long nwork = big_off(a.st) ? 0 : a.st->big_nwork;
+    if (nwork <= blockIdx.x) return;
     extern __shared__ long long bsm_ll[];
     WT *svals = (WT *)bsm_ll;
     int *skeys = (int *)(svals + kSmT);
@@ -823,7 +862,7 @@ __global__ void __launch_bounds__(512) k_big_insert_sm(AggArgs<WT> a, BigArgs b,
         const int lg = keys ? __ffs((int)T) - 1 : 0;
         for (int q = threadIdx.x; q < len; q += blockDim.x) {
             const int key = a.skey[st + q];
-            const WT wt = a.sw[st + q];
+            const WT wt = a.w_at(st + q);
             unsigned h = hash_slot(key, slg);
             for (int p = 0; p < kSmT; ++p) {
                 const int k = atomicCAS(&skeys[h], -1, key);
@@ -900,7 +939,7 @@ template <typename WT>
 __global__ void k_big_mark(AggArgs<WT> a, BigArgs b, int sort_rows)
 {
     const int cnt = a.st->small_cnt[kLongCls];
-    const long long words = ((long long)a.C + 31) >> 5;
+    const long long words = (a.st->ccount + 31) >> 5;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < cnt; i += gridDim.x * blockDim.x) {
         const int k = b.kdist[i];
         b.gwords[i] = (sort_rows && k > kSortMax) ? words : 0;
@@ -951,8 +990,9 @@ __global__ void k_big_len(AggArgs<WT> a, BigArgs b)
         a.kc[b.list[i]] = b.cursor[i];
 }
 
-__global__ void k_big_lchunks(const int *cursor, int cnt, long long *lch)
+__global__ void k_big_lchunks(const int *cursor, const DevStats *st, long long *lch)
 {
+    const int cnt = st->small_cnt[kLongCls];
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < cnt; i += gridDim.x * blockDim.x)
         lch[i] = (cursor[i] + kChunk - 1) / kChunk;
 }
@@ -1062,9 +1102,9 @@ __global__ void __launch_bounds__(1024) k_big_sort(AggArgs<WT> a, BigArgs b)
 
 // Compaction over contiguous output ranges: output entry j of community c
 // comes from tmp_off[c] + (j - new_offs[c]); c and that shift are loaded once
-// per row window.
+// per row window.  C and the entry count are read on the device.
 template <typename WT>
-__global__ void __launch_bounds__(256) k_compact(int C, long long Enew, const int64_t *__restrict__ new_offs,
+__global__ void __launch_bounds__(256) k_compact(const int64_t *__restrict__ new_offs,
                                                  const long long *__restrict__ tmp_off,
                                                  const int32_t *__restrict__ tmp_nbr, const WT *__restrict__ tmp_w,
                                                  int32_t *out_nbr, WT *out_w, long long tmp_cap,
@@ -1075,6 +1115,8 @@ __global__ void __launch_bounds__(256) k_compact(int C, long long Enew, const in
     const long long wg = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
     const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
     const int nnz = st->nz_rows;
+    const int C = (int)st->ccount;
+    const long long Enew = st->new_entries;
     // per row: pa = the community (-1 when out of range), pb = source shift
     auto rowval = [&](int r, long long &pa, long long &pb) {
         const int c = nz_rows[r];
@@ -1100,18 +1142,21 @@ __global__ void __launch_bounds__(256) k_compact(int C, long long Enew, const in
     }
 }
 
-__global__ void k_contract_set_tail(int32_t *moff, int C, int n, long long *medge, long long E)
+__global__ void k_contract_set_tail(int32_t *moff, const DevStats *st, int n, long long *medge, long long E)
 {
-    moff[C] = n;
+    moff[st->ccount] = n;
     medge[n] = E;
 }
 
-__global__ void k_set_last_offset(int64_t *offs, int C, const long long *total) { offs[C] = *total; }
+__global__ void k_set_last_offset(int64_t *offs, const DevStats *st) { offs[st->ccount] = st->new_entries; }
 
 __global__ void k_contract_reset(DevStats *st)
 {
     for (int k = 0; k < kNumCls; ++k) st->small_cnt[k] = 0;
     st->err = 0;
+    st->ccount = 0;
+    st->new_entries = 0;
+    st->big_slots = st->big_nwork = st->big_ntwork = st->big_lwork = 0;
 }
 
 // Shared memory of the table kernels: int keys plus WT values per slot.
@@ -1174,12 +1219,19 @@ static int grid_cap(long long items, int per_block, int cap)
 }
 
 // Walk list of the rows of (offs, n) that have entries (E entries in total).
-static void build_walk_list(const int64_t *offs, int n, long long E, ContractBuffers &b, cudaStream_t st)
+// With dn / dE (device) the rows are [0, min(n, *dn)) and the entries *dE:
+// nothing waits for the host.
+static void build_walk_list(const int64_t *offs, int n, long long E, ContractBuffers &b, cudaStream_t st,
+                            const long long *dn = nullptr, const long long *dE = nullptr)
 {
     const int cap = sm_count() * 8;
-    exclusive_scan(offs, b.nz_pos, n, OpRowNonEmpty{offs}, b.scan_partial, &b.stats->total, st, &b.stats->err);
-    k_nz_tail<<<1, 1, 0, st>>>(b.stats, b.nz_offs, E);
-    k_nz_scatter<<<grid_cap(n, 256, cap), 256, 0, st>>>(offs, n, b.nz_pos, b.nz_rows, b.nz_offs);
+    if (dn)
+        exclusive_scan_dev(offs, b.nz_pos, n, dn, OpRowNonEmpty{offs}, b.scan_partial, &b.stats->total, st,
+                           &b.stats->err);
+    else
+        exclusive_scan(offs, b.nz_pos, n, OpRowNonEmpty{offs}, b.scan_partial, &b.stats->total, st, &b.stats->err);
+    k_nz_tail<<<1, 1, 0, st>>>(b.stats, b.nz_offs, E, dE);
+    k_nz_scatter<<<grid_cap(n, 256, cap), 256, 0, st>>>(offs, n, b.nz_pos, b.nz_rows, b.nz_offs, dn);
     note_launch(2);
 }
 
@@ -1195,16 +1247,28 @@ static bool read_stats(DevStats *h, DevStats *d, cudaStream_t st, gala_status *s
     return true;
 }
 
-// Rows longer than kMid3Max entries (kMid2Max when sorted; class kLongCls).
-// Returns false on failure.
+// Keys of the long-row tables take pool[0, half), their values (WT) the rest.
 template <typename WT>
-static bool contract_long_rows(const AggArgs<WT> &a, ContractBuffers &b, int cnt3, int C, DevStats &hs,
+static long long big_pool_half(const ContractBuffers &b)
+{
+    constexpr long long vints = sizeof(WT) / sizeof(int32_t);
+    return (b.big_pool_ints / (1 + vints)) & ~1LL;  // even: the values start 8-byte aligned
+}
+
+// Rows longer than kMid3Max entries (kMid2Max when sorted; class kLongCls),
+// at most cnt_max of them.  Counts, table sizes and the scratch check stay on
+// the device; only sorted rows read their bitmap sizes on the host.  Returns
+// false on failure.
+template <typename WT>
+static bool contract_long_rows(const AggArgs<WT> &a, ContractBuffers &b, const int32_t *list, int cnt_max,
                                cudaStream_t st, gala_status *status, bool sort_rows)
 {
     const int nsm = sm_count();
     const int cap = nsm * 8;
+    DevStats *ds = b.stats;
+    const int *dcnt = &ds->small_cnt[kLongCls];
     BigArgs ba{};
-    ba.list = b.cls_list + (long long)kLongCls * C;
+    ba.list = list;
     ba.T = b.big_T;
     ba.chunks = b.big_chunks;
     ba.tchunks = b.big_tchunks;
@@ -1219,45 +1283,41 @@ static bool contract_long_rows(const AggArgs<WT> &a, ContractBuffers &b, int cnt
     ba.gwords = b.big_gwords;
     ba.gofs = b.big_gofs;
     ba.pool = b.big_pool;
-    k_big_plan<WT><<<grid_cap(cnt3, 256, cap), 256, 0, st>>>(a, ba);
-    exclusive_scan(b.big_T, b.big_toff, cnt3, OpIdentity(), b.scan_partial, &b.stats->total, st, &b.stats->err);
-    exclusive_scan(b.big_chunks, b.big_coff, cnt3, OpIdentity(), b.scan_partial, &b.stats->total2, st, &b.stats->err);
-    exclusive_scan(b.big_tchunks, b.big_tcoff, cnt3, OpIdentity(), b.scan_partial, &b.stats->total3, st, &b.stats->err);
-    k_big_tail<<<1, 1, 0, st>>>(ba, b.stats);
-    note_launch(2);
-    if (!read_stats(&hs, b.stats, st, status, "contraction: long rows")) return false;
-    const long long slots = hs.total, nwork = hs.total2, ntwork = hs.total3;
-    // keys, then the values 8-byte aligned (slot count rounded up to even)
-    const long long half = (slots + 1) & ~1LL;
-    constexpr long long vints = sizeof(WT) / sizeof(int32_t);
-    if (half + vints * slots > b.big_pool_ints || nwork > b.big_work_cap || ntwork > b.big_twork_cap) {
-        set_error("contraction: long rows need %lld table slots / %lld + %lld chunks, pool holds %lld ints / %lld / "
-                  "%lld",
-                  slots, nwork, ntwork, b.big_pool_ints, b.big_work_cap, b.big_twork_cap);
-        *status = GALA_ERR_CAPACITY;
-        return false;
-    }
-    ba.pool_half = half;
-    cudaMemsetAsync(b.big_pool, 0xff, (size_t)slots * sizeof(int32_t), st);
-    cudaMemsetAsync(b.big_pool + half, 0, (size_t)slots * sizeof(WT), st);
-    k_big_work<WT><<<grid_cap((long long)cnt3 * 32, 256, cap), 256, 0, st>>>(a, ba);
-    k_big_insert_sm<WT><<<(int)(nwork < nsm * 2 ? nwork : nsm * 2), 512, big_sm_smem<WT>(), st>>>(
-        a, ba, nwork, sort_rows ? 0 : 1);
+    ba.pool_half = big_pool_half<WT>(b);
+    ba.work_cap = b.big_work_cap;
+    ba.twork_cap = b.big_twork_cap;
+    k_big_plan<WT><<<grid_cap(cnt_max, 256, cap), 256, 0, st>>>(a, ba);
+    exclusive_scan_dev(b.big_T, b.big_toff, cnt_max, dcnt, OpIdentity(), b.scan_partial, &ds->big_slots, st,
+                       &ds->err);
+    exclusive_scan_dev(b.big_chunks, b.big_coff, cnt_max, dcnt, OpIdentity(), b.scan_partial, &ds->big_nwork, st,
+                       &ds->err);
+    exclusive_scan_dev(b.big_tchunks, b.big_tcoff, cnt_max, dcnt, OpIdentity(), b.scan_partial, &ds->big_ntwork,
+                       st, &ds->err);
+    k_big_tail<<<1, 1, 0, st>>>(ba, ds);
+    k_big_clear<WT><<<cap, 256, 0, st>>>(ba, ds);
+    k_big_work<WT><<<grid_cap((long long)cnt_max * 32, 256, cap), 256, 0, st>>>(a, ba);
+    k_big_insert_sm<WT><<<nsm * 2, 512, big_sm_smem<WT>(), st>>>(a, ba, sort_rows ? 0 : 1);
+    note_launch(5);
     if (!sort_rows) {
         // rows in table order: collect from the slot lists, no table scans
         long long *lch = b.big_tchunks, *lcoff = b.big_tcoff;
-        k_big_lchunks<<<grid_cap(cnt3, 256, cap), 256, 0, st>>>(ba.cursor, cnt3, lch);
-        exclusive_scan(lch, lcoff, cnt3, OpIdentity(), b.scan_partial, &b.stats->total3, st, &b.stats->err);
-        k_big_collect_list<WT><<<(int)(nwork < nsm * 8 ? nwork : nsm * 8), 256, 0, st>>>(a, ba, lcoff,
-                                                                                          &b.stats->total3);
-        k_big_len<WT><<<grid_cap(cnt3, 256, cap), 256, 0, st>>>(a, ba);
-        note_launch(4);
+        k_big_lchunks<<<grid_cap(cnt_max, 256, cap), 256, 0, st>>>(ba.cursor, ds, lch);
+        exclusive_scan_dev(lch, lcoff, cnt_max, dcnt, OpIdentity(), b.scan_partial, &ds->big_lwork, st, &ds->err);
+        k_big_collect_list<WT><<<nsm * 8, 256, 0, st>>>(a, ba, lcoff, &ds->big_lwork);
+        k_big_len<WT><<<grid_cap(cnt_max, 256, cap), 256, 0, st>>>(a, ba);
+        note_launch(3);
         return true;
     }
-    k_big_mark<WT><<<grid_cap(cnt3, 256, cap), 256, 0, st>>>(a, ba, sort_rows ? 1 : 0);
-    exclusive_scan(b.big_gwords, b.big_gofs, cnt3, OpIdentity(), b.scan_partial, &b.stats->total, st, &b.stats->err);
-    note_launch(3);
-    if (!read_stats(&hs, b.stats, st, status, "contraction: long-row bitmaps")) return false;
+    // sorted rows: the bitmap sizes come back to the host
+    DevStats hs;
+    if (!read_stats(&hs, ds, st, status, "contraction: long rows")) return false;
+    const int cnt3 = hs.small_cnt[kLongCls];
+    if (cnt3 == 0 || (hs.err & kErrCapacity)) return true;  // a capacity error is reported at the end
+    const long long ntwork = hs.big_ntwork;
+    k_big_mark<WT><<<grid_cap(cnt3, 256, cap), 256, 0, st>>>(a, ba, 1);
+    exclusive_scan(b.big_gwords, b.big_gofs, cnt3, OpIdentity(), b.scan_partial, &ds->total, st, &ds->err);
+    note_launch(1);
+    if (!read_stats(&hs, ds, st, status, "contraction: long-row bitmaps")) return false;
     const long long words = hs.total;
     if (2 * words > b.big_bitmap_words) {
         set_error("contraction: %lld bitmap words needed, scratch holds %lld", 2 * words, b.big_bitmap_words);
@@ -1268,23 +1328,25 @@ static bool contract_long_rows(const AggArgs<WT> &a, ContractBuffers &b, int cnt
     ba.pref = (unsigned *)b.big_bitmap + words;
     if (words > 0) cudaMemsetAsync(ba.bits, 0, (size_t)words * sizeof(unsigned), st);
     const int tgrid = (int)(ntwork < nsm * 8 ? ntwork : nsm * 8);
-    k_big_collect<WT><<<tgrid, 256, 0, st>>>(a, ba, ntwork);
-    note_launch(1);
-    if (words > 0) {
-        exclusive_scan(ba.bits, ba.pref, words, OpPopc(), b.scan_partial, &b.stats->total, st, &b.stats->err);
+    if (tgrid > 0) {
+        k_big_collect<WT><<<tgrid, 256, 0, st>>>(a, ba, ntwork);
+        note_launch(1);
+    }
+    if (words > 0 && tgrid > 0) {
+        exclusive_scan(ba.bits, ba.pref, words, OpPopc(), b.scan_partial, &ds->total, st, &ds->err);
         k_big_rank<WT><<<tgrid, 256, 0, st>>>(a, ba, ntwork);
         note_launch(1);
     }
-    if (sort_rows) {
-        k_big_sort<WT><<<cnt3 < nsm * 2 ? cnt3 : nsm * 2, 1024, sort_smem<WT>(), st>>>(a, ba);
-        note_launch(1);
-    }
+    k_big_sort<WT><<<cnt3 < nsm * 2 ? cnt3 : nsm * 2, 1024, sort_smem<WT>(), st>>>(a, ba);
+    note_launch(1);
     return true;
 }
 
 // Returns the community count C (>= 1) or -1 on failure (*status set).
 // new_offs receives C+1 offsets (leading 0).  orig_map (length n_orig) is
-// composed with the new labels.
+// composed with the new labels.  C, the size classes and the new entry count
+// stay on the device: the host reads them once, after the compaction (and,
+// for sorted long rows, once more for their bitmap sizes).
 template <typename WT>
 static int contract_t(const LevelGraph &g, const int32_t *comm, ContractBuffers &b, int64_t *new_offs,
                       int32_t *new_nbr, WT *new_w, int32_t *orig_map, int32_t n_orig, int64_t *new_E,
@@ -1292,16 +1354,20 @@ static int contract_t(const LevelGraph &g, const int32_t *comm, ContractBuffers 
                       const NextLevelInit &nli, bool labels_only)
 {
     const int n = g.n;
-    const int cap = sm_count() * 8;
+    const long long E = g.E;
+    const int nsm = sm_count();
+    const int cap = nsm * 8;
     *status = GALA_OK;
     DevStats hs;
+    DevStats *ds = b.stats;
+    const long long *dC = &ds->ccount;
 
-    k_contract_reset<<<1, 1, 0, st>>>(b.stats);
+    k_contract_reset<<<1, 1, 0, st>>>(ds);
     note_launch(1);
     if (validate_labels) {
-        k_check_labels<<<grid_cap(n, 256, cap), 256, 0, st>>>(comm, n, b.stats);
+        k_check_labels<<<grid_cap(n, 256, cap), 256, 0, st>>>(comm, n, ds);
         note_launch(1);
-        if (!read_stats(&hs, b.stats, st, status, "contraction: label check")) return -1;
+        if (!read_stats(&hs, ds, st, status, "contraction: label check")) return -1;
         if (hs.err) {
             set_error("contraction: a community label lies outside [0, %d)", n);
             *status = GALA_ERR_INVALID;
@@ -1310,111 +1376,122 @@ static int contract_t(const LevelGraph &g, const int32_t *comm, ContractBuffers 
     }
     cudaMemsetAsync(b.cnt, 0, ((size_t)n + 1) * sizeof(int32_t), st);
     k_hist<<<grid_cap(n, 256, cap), 256, 0, st>>>(comm, n, b.cnt);
-    exclusive_scan(b.cnt, b.newid, n, OpPositive(), b.scan_partial, &b.stats->total, st, &b.stats->err);
-    note_launch(1);
-    if (!read_stats(&hs, b.stats, st, status, "contraction: community count")) return -1;
-    const int C = (int)hs.total;
-
-    k_relabel<WT><<<grid_cap(n, 256, cap), 256, 0, st>>>(comm, b.newid, b.cnt, n, b.lab, b.csz,
-                                                         (const WT *)nli.tot, (WT *)nli.k);
-    if (nli.self) cudaMemsetAsync(nli.self, 0, (size_t)C * sizeof(WT), st);
-    if (orig_map) k_compose<<<grid_cap(n_orig, 256, cap), 256, 0, st>>>(orig_map, n_orig, b.lab);
+    exclusive_scan(b.cnt, b.newid, n, OpPositive(), b.scan_partial, &ds->ccount, st, &ds->err);
+    k_relabel<WT><<<grid_cap(n, 256, cap), 256, 0, st>>>(comm, b.newid, b.cnt, n, b.lab, b.csz, b.ec,
+                                                         (const WT *)nli.tot, (WT *)nli.k, (WT *)nli.self);
+    note_launch(2);
+    if (orig_map) {
+        k_compose<<<grid_cap(n_orig, 256, cap), 256, 0, st>>>(orig_map, n_orig, b.lab);
+        note_launch(1);
+    }
     if (labels_only) {
-        note_launch(1 + (orig_map ? 1 : 0));
+        if (!read_stats(&hs, ds, st, status, "contraction: community count")) return -1;
         *new_E = 0;
-        return C;
+        return (int)hs.ccount;
     }
-    exclusive_scan(b.csz, b.moff, C, OpIdentity(), b.scan_partial, &b.stats->total, st, &b.stats->err);
-    cudaMemcpyAsync(b.cursor, b.moff, (size_t)C * sizeof(int32_t), cudaMemcpyDeviceToDevice, st);
-    cudaMemsetAsync(b.ec, 0, ((size_t)C + 1) * sizeof(long long), st);
-    k_member_scatter<<<grid_cap(n, 256, cap), 256, 0, st>>>(b.lab, g.offs, n, b.cursor, b.members, b.mpos, b.ec);
-    exclusive_scan(b.members, b.medge, n, OpDegOf{g.offs}, b.scan_partial, &b.stats->total, st, &b.stats->err);
+    exclusive_scan_dev(b.csz, b.moff, n, dC, OpIdentity(), b.scan_partial, &ds->total, st, &ds->err);
+    k_member_scatter<<<grid_cap(n, 256, cap), 256, 0, st>>>(b.lab, g.offs, n, b.moff, b.csz, b.members, b.mpos,
+                                                            b.ec);
+    exclusive_scan(b.members, b.medge, n, OpDegOf{g.offs}, b.scan_partial, &ds->total, st, &ds->err);
     // moff[C] = n and medge[n] = E close the last segments
-    k_contract_set_tail<<<1, 1, 0, st>>>(b.moff, C, n, b.medge, g.E);
-    const int fill_grid = grid_cap((g.E + kRangeEntries - 1) / kRangeEntries * 32, 256, cap);
-    if (g.E > 0) {
-        build_walk_list(g.offs, n, g.E, b, st);
-        WT *sw = (WT *)b.stream_w;
-        if (g.w)
-            k_stream_fill<WT, true><<<fill_grid, 256, 0, st>>>(n, g.E, g.offs, g.nbr, (const WT *)g.w, b.lab, b.mpos,
-                                                              b.medge, b.stream_key, sw, b.nz_rows, b.nz_offs,
-                                                              b.stats);
+    k_contract_set_tail<<<1, 1, 0, st>>>(b.moff, ds, n, b.medge, E);
+    note_launch(2);
+    const bool weighted = g.w != nullptr;
+    if (E > 0) {
+        build_walk_list(g.offs, n, E, b, st);
+        const int fill_grid = grid_cap((E + kRangeEntries - 1) / kRangeEntries * 32, 256, cap);
+        if (weighted)
+            k_stream_fill<WT, true><<<fill_grid, 256, 0, st>>>(n, E, g.offs, g.nbr, (const WT *)g.w, b.lab, b.mpos,
+                                                              b.medge, b.stream_key, (WT *)b.stream_w, b.nz_rows,
+                                                              b.nz_offs, ds);
         else
-            k_stream_fill<WT, false><<<fill_grid, 256, 0, st>>>(n, g.E, g.offs, g.nbr, (const WT *)g.w, b.lab,
-                                                               b.mpos, b.medge, b.stream_key, sw, b.nz_rows,
-                                                               b.nz_offs, b.stats);
+            k_stream_fill<WT, false><<<fill_grid, 256, 0, st>>>(n, E, g.offs, g.nbr, nullptr, b.lab, b.mpos,
+                                                               b.medge, b.stream_key, nullptr, b.nz_rows,
+                                                               b.nz_offs, ds);
+        note_launch(1);
     }
-    k_classify<<<grid_cap(C, 256, cap), 256, 0, st>>>(C, b.ec, b.cls_list, b.kc, b.stats, sort_rows ? 1 : 0);
-    exclusive_scan(b.ec, b.tmp_off, C, OpCap{C}, b.scan_partial, &b.stats->total, st, &b.stats->err);
-    note_launch(6 + (orig_map ? 1 : 0));
-    if (!read_stats(&hs, b.stats, st, status, "contraction: classification")) return -1;
+    k_classify<<<grid_cap(n, 256, cap), 256, 0, st>>>(b.ec, b.cls_list, n, b.kc, ds, sort_rows ? 1 : 0);
+    exclusive_scan_dev(b.ec, b.tmp_off, n, dC, OpCapDev{dC}, b.scan_partial, &ds->total, st, &ds->err);
+    note_launch(1);
 
     AggArgs<WT> a;
     a.moff = b.moff;
     a.medge = b.medge;
     a.ec = b.ec;
     a.skey = b.stream_key;
-    a.sw = (const WT *)b.stream_w;
+    a.sw = weighted ? (const WT *)b.stream_w : nullptr;
     a.tmp_off = b.tmp_off;
     a.tmp_nbr = b.tmp_nbr;
     a.tmp_w = (WT *)b.tmp_w;
     a.kc = b.kc;
-    a.st = b.stats;
-    a.C = C;
-    const int nsm = sm_count();
-    if (hs.small_cnt[0] > 0) {
-        k_agg_small<WT><<<grid_cap((long long)hs.small_cnt[0] * 32, 256, cap), 256, 0, st>>>(a, b.cls_list);
+    a.st = ds;
+    // Every class kernel reads its count on the device; its grid is bounded
+    // by the most communities the class can hold (E / its shortest row).
+    auto most = [&](long long min_entries) -> int {
+        const long long c = E / min_entries;
+        return (int)(c < n ? c : n);
+    };
+    const int n_small = most(1), n_warp = sort_rows ? 0 : most(kSmallMax + 1);
+    const int n_mid1 = most(sort_rows ? kSmallMax + 1 : kWarpAggMax + 1), n_mid2 = most(kMid1Max + 1);
+    const int n_mid3 = sort_rows ? 0 : most(kMid2Max + 1), n_long = most((sort_rows ? kMid2Max : kMid3Max) + 1);
+    if (n_small > 0) {
+        k_agg_small<WT><<<grid_cap((long long)n_small * 32, 256, cap), 256, 0, st>>>(a, b.cls_list);
         note_launch(1);
     }
-    if (hs.small_cnt[kWarpCls] > 0) {
-        k_agg_warp_list<WT><<<grid_cap((long long)hs.small_cnt[kWarpCls] * 32, 256, nsm * 8), 256, 0, st>>>(
-            a, b.cls_list + (long long)kWarpCls * C);
+    if (n_warp > 0) {
+        k_agg_warp_list<WT><<<grid_cap((long long)n_warp * 32, 256, cap), 256, 0, st>>>(
+            a, b.cls_list + (long long)kWarpCls * n);
         note_launch(1);
     }
-    if (hs.small_cnt[1] > 0) {
-        int grid = hs.small_cnt[1] < nsm * 16 ? hs.small_cnt[1] : nsm * 16;
+    if (n_mid1 > 0) {
+        const int grid = n_mid1 < nsm * 16 ? n_mid1 : nsm * 16;
         if (sort_rows)
-            k_agg_mid<WT, 128, 1024, kMid1Max><<<grid, 128, mid1_smem<WT>(), st>>>(a, b.cls_list + (long long)C, 1);
+            k_agg_mid<WT, 128, 1024, kMid1Max><<<grid, 128, mid1_smem<WT>(), st>>>(a, b.cls_list + (long long)n, 1);
         else
-            k_agg_mid_list<WT, 128, 1024><<<grid, 128, list_smem<WT>(1024), st>>>(a, b.cls_list + (long long)C, 1);
+            k_agg_mid_list<WT, 128, 1024><<<grid, 128, list_smem<WT>(1024), st>>>(a, b.cls_list + (long long)n, 1);
         note_launch(1);
     }
-    if (hs.small_cnt[2] > 0) {
-        int grid = hs.small_cnt[2] < nsm * 2 ? hs.small_cnt[2] : nsm * 2;
+    if (n_mid2 > 0) {
+        const int grid = n_mid2 < nsm * 2 ? n_mid2 : nsm * 2;
         if (sort_rows)
-            k_agg_mid<WT, 256, 8192, kMid2Max><<<grid, 256, mid2_smem<WT>(), st>>>(a, b.cls_list + 2LL * C, 2);
+            k_agg_mid<WT, 256, 8192, kMid2Max><<<grid, 256, mid2_smem<WT>(), st>>>(a, b.cls_list + 2LL * n, 2);
         else
-            k_agg_mid_list<WT, 1024, 8192><<<grid, 1024, list_smem<WT>(8192), st>>>(a, b.cls_list + 2LL * C, 2);
+            k_agg_mid_list<WT, 1024, 8192><<<grid, 1024, list_smem<WT>(8192), st>>>(a, b.cls_list + 2LL * n, 2);
         note_launch(1);
     }
-    if (hs.small_cnt[3] > 0) {  // 4097-8192 entries, rows in table order
-        int grid = hs.small_cnt[3] < nsm ? hs.small_cnt[3] : nsm;
-        k_agg_mid_list<WT, 1024, 16384><<<grid, 1024, list_smem<WT>(16384), st>>>(a, b.cls_list + 3LL * C, 3);
+    if (n_mid3 > 0) {  // 4097-8192 entries, rows in table order
+        const int grid = n_mid3 < nsm ? n_mid3 : nsm;
+        k_agg_mid_list<WT, 1024, 16384><<<grid, 1024, list_smem<WT>(16384), st>>>(a, b.cls_list + 3LL * n, 3);
         note_launch(1);
     }
-    if (hs.small_cnt[kLongCls] > 0 &&
-        !contract_long_rows(a, b, hs.small_cnt[kLongCls], C, hs, st, status, sort_rows))
+    if (n_long > 0 &&
+        !contract_long_rows(a, b, b.cls_list + (long long)kLongCls * n, n_long, st, status, sort_rows))
         return -1;
-    exclusive_scan(b.kc, new_offs, C, OpIdentity(), b.scan_partial, &b.stats->total, st, &b.stats->err);
-    k_set_last_offset<<<1, 1, 0, st>>>(new_offs, C, &b.stats->total);
+    exclusive_scan_dev(b.kc, new_offs, n, dC, OpIdentity(), b.scan_partial, &ds->new_entries, st, &ds->err);
+    k_set_last_offset<<<1, 1, 0, st>>>(new_offs, ds);
     note_launch(1);
-    if (!read_stats(&hs, b.stats, st, status, "contraction: offsets")) return -1;
-    const long long Enew = hs.total;
-    if (Enew > 0) {
-        build_walk_list(new_offs, C, Enew, b, st);
-        k_compact<WT><<<grid_cap((Enew + kRangeEntries - 1) / kRangeEntries * 32, 256, cap), 256, 0, st>>>(
-            C, Enew, new_offs, b.tmp_off, b.tmp_nbr, (const WT *)b.tmp_w, new_nbr, new_w, g.E, b.nz_rows, b.nz_offs,
-            b.stats, (WT *)nli.self);
+    if (E > 0) {  // the new level has at most E entries
+        build_walk_list(new_offs, n, 0, b, st, dC, &ds->new_entries);
+        k_compact<WT><<<grid_cap((E + kRangeEntries - 1) / kRangeEntries * 32, 256, cap), 256, 0, st>>>(
+            new_offs, b.tmp_off, b.tmp_nbr, (const WT *)b.tmp_w, new_nbr, new_w, E, b.nz_rows, b.nz_offs, ds,
+            (WT *)nli.self);
         note_launch(1);
     }
-    if (!read_stats(&hs, b.stats, st, status, "contraction: compaction")) return -1;
+    if (!read_stats(&hs, ds, st, status, "contraction")) return -1;
+    if (hs.err & kErrCapacity) {
+        set_error("contraction: long rows need %lld table slots / %lld + %lld chunks, scratch holds %lld / %lld / "
+                  "%lld",
+                  hs.big_slots, hs.big_nwork, hs.big_ntwork, big_pool_half<WT>(b), b.big_work_cap, b.big_twork_cap);
+        *status = GALA_ERR_CAPACITY;
+        return -1;
+    }
     if (hs.err) {
         set_error("contraction: hash table overflow (error bits %d)", hs.err);
         *status = GALA_ERR_OVERFLOW;
         return -1;
     }
-    *new_E = Enew;
-    return C;
+    *new_E = hs.new_entries;
+    return (int)hs.ccount;
 }
 
 int contract_run(const LevelGraph &g, const int32_t *comm, ContractBuffers &b, int64_t *new_offs,

@@ -28,6 +28,15 @@ struct OpCap {
         return (long long)x < cap ? (long long)x : cap;
     }
 };
+struct OpCapDev {  // cap read on the device
+    const long long *cap;
+    template <typename T>
+    __device__ __forceinline__ long long operator()(T x, long long) const
+    {
+        const long long c = *cap;
+        return (long long)x < c ? (long long)x : c;
+    }
+};
 
 template <typename T>
 __device__ __forceinline__ T block_exclusive_scan(T v, T *warp_tot, T *block_total)
@@ -86,16 +95,22 @@ __device__ __forceinline__ void scan_st(unsigned long long *p, unsigned long lon
 }
 
 // status: nb + 2 words, zero on entry; status[nb] is the tile counter.
-template <typename Tin, typename Tout, typename Op>
+// With dlen, the length is min(*dlen, n), read on the device (n bounds the
+// grid): items past it count as 0 and are not written.
+template <typename Tin, typename Tout, typename Op, typename Tlen>
 __global__ void __launch_bounds__(kScanThreads) k_scan_onepass(const Tin *__restrict__ in, Tout *__restrict__ out,
                                                                long long n, Op op, unsigned long long *status, int nb,
-                                                               long long *total_out, int *err)
+                                                               long long *total_out, int *err, const Tlen *dlen)
 {
     __shared__ long long wt[32];
     __shared__ long long tot;
     __shared__ int s_tile;
     __shared__ long long s_excl;
     if (threadIdx.x == 0) s_tile = (int)atomicAdd(&status[nb], 1ull);
+    if (dlen) {
+        const long long d = (long long)*dlen;
+        n = d < 0 ? 0 : (d < n ? d : n);
+    }
     __syncthreads();
     const int tile = s_tile;
     const long long base = (long long)tile * kScanTile + (long long)threadIdx.x * kScanItems;
@@ -172,7 +187,23 @@ void exclusive_scan(const Tin *in, Tout *out, long long n, Op op, long long *par
     if (nb < 1) nb = 1;
     unsigned long long *status = (unsigned long long *)partial;
     cudaMemsetAsync(status, 0, ((size_t)nb + 2) * sizeof(unsigned long long), st);
-    k_scan_onepass<Tin, Tout, Op><<<nb, kScanThreads, 0, st>>>(in, out, n, op, status, nb, total_out, err);
+    k_scan_onepass<Tin, Tout, Op, int><<<nb, kScanThreads, 0, st>>>(in, out, n, op, status, nb, total_out, err,
+                                                                    nullptr);
+    note_launch(1);
+}
+
+// The same over the first min(*dlen, nmax) items, dlen on the device: the
+// host needs no count, so nothing waits for the device.
+template <typename Tin, typename Tout, typename Op, typename Tlen>
+void exclusive_scan_dev(const Tin *in, Tout *out, long long nmax, const Tlen *dlen, Op op, long long *partial,
+                        long long *total_out, cudaStream_t st, int *err = nullptr)
+{
+    int nb = (int)((nmax + kScanTile - 1) / kScanTile);
+    if (nb < 1) nb = 1;
+    unsigned long long *status = (unsigned long long *)partial;
+    cudaMemsetAsync(status, 0, ((size_t)nb + 2) * sizeof(unsigned long long), st);
+    k_scan_onepass<Tin, Tout, Op, Tlen><<<nb, kScanThreads, 0, st>>>(in, out, nmax, op, status, nb, total_out, err,
+                                                                     dlen);
     note_launch(1);
 }
 
