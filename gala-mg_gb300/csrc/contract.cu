@@ -32,6 +32,8 @@
 // vertices).
 #include <limits.h>
 
+#include <algorithm>
+
 #include "common.cuh"
 #include "internal.h"
 #include "scan.cuh"
@@ -141,96 +143,78 @@ struct RowWindow {
     }
 };
 
-// Owner row of entry j0: the last v with offs[v] <= j0 and offs[v+1] > j0.
-__device__ __forceinline__ int owner_row(const int64_t *offs, const long long *offs_ll, int n, long long j0)
+// Owner row of entry j0 (the last v with offs_ll[v] <= j0), found by the
+// whole warp: every round the 32 lanes probe 32 evenly spaced rows of
+// [lo, hi] and the ballot keeps the interval of the last row starting at or
+// before j0 (5 rounds for 2^25 rows instead of 25 dependent loads).
+// offs_ll[0] <= j0 < offs_ll[n]; all lanes call.
+__device__ __forceinline__ int warp_owner_row(const long long *offs_ll, int n, long long j0)
 {
-    int lo = 0, hi = n - 1;  // rows [0, n); offs[n] = E > j0
-    while (lo < hi) {
-        const int mid = (lo + hi + 1) >> 1;
-        const long long o = offs ? (long long)offs[mid] : offs_ll[mid];
-        if (o <= j0)
-            lo = mid;
-        else
-            hi = mid - 1;
+    const int lane = threadIdx.x & 31;
+    int lo = 0, hi = n - 1;
+    while (hi > lo) {
+        const long long span = (long long)(hi - lo) + 1;
+        const int p = lo + (int)((span * lane) >> 5);
+        const unsigned m = __ballot_sync(GALA_FULL_MASK, offs_ll[p] <= j0);
+        const int k = m ? 31 - __clz((int)m) : 0;
+        const int nlo = lo + (int)((span * k) >> 5);
+        hi = (k == 31) ? hi : lo + (int)((span * (k + 1)) >> 5) - 1;
+        lo = nlo;
     }
     return lo;
 }
 
-// Walk entries [j0, j1) of a CSR (rows [0, n), offsets offs or offs_ll) and
-// call f(j, row) for every entry; all 32 lanes of the warp must call.
-template <typename F>
-__device__ __forceinline__ void for_entries(const int64_t *offs, const long long *offs_ll, int n, long long j0,
-                                            long long j1, F f)
-{
-    const int lane = threadIdx.x & 31;
-    RowWindow w{offs, offs_ll, n, 0, 0};
-    w.vbase = owner_row(offs, offs_ll, n, j0);
-    w.load();
-    for (long long jb = j0; jb < j1; jb += 32) {
-        // slide the window to the owner of the round's first entry
-        const int adv = w.count_le(jb);
-        if (adv > 0) {
-            w.vbase += adv;
-            w.load();
-        }
-        const long long j = jb + lane;
-        bool done = j >= j1;
-        while (!__all_sync(GALA_FULL_MASK, done)) {
-            const int idx = w.count_le(j);
-            const bool here = !done && idx < 32;
-            if (here) f(j, w.vbase + idx);
-            done = done || here;
-            if (!__all_sync(GALA_FULL_MASK, done)) {
-                w.vbase += 32;
-                w.load();
-            }
-        }
-    }
-}
-
-// for_entries with two per-row values: when the window moves, lane l loads
-// pa/pb of window row vbase + l once (rowval(row, &pa, &pb), row < n), and
-// every entry of that row receives them by a shuffle instead of gathering
-// them itself.  f(j, row, pa, pb) is called for every entry of [j0, j1);
-// all 32 lanes of the warp must call.
-template <typename RV, typename F>
-__device__ __forceinline__ void for_entries_rows(const long long *offs_ll, int n, long long j0, long long j1,
-                                                 RV rowval, F f)
-{
-    const int lane = threadIdx.x & 31;
-    RowWindow w{nullptr, offs_ll, n, 0, 0};
-    long long pa = 0, pb = 0;
-    auto load = [&]() {
+// Cursor over a walk list (rows that all have entries, row ends in offs_ll):
+// a window of 32 rows, one per lane, with their ends and two values per row
+// (rowval(row, &pa, &pb), loaded when the window moves; rows past the list
+// keep (-1, 0)).  32 consecutive entries span at most 32 such rows, so once
+// the window starts at the owner of a batch's first entry it holds the whole
+// batch.  The window moves only when a batch ends past it: with rows of a
+// few dozen entries it is loaded once or twice per 1024-entry task, not once
+// per batch.
+template <typename RV>
+struct RowCursor {
+    RowWindow w;
+    RV rowval;
+    long long pa, pb;
+    __device__ __forceinline__ void load()
+    {
         w.load();
-        const int r = w.vbase + lane;
-        pa = -1;  // rows outside [0, n) keep (-1, 0): the callers record them
+        const int r = w.vbase + (int)(threadIdx.x & 31);
+        pa = -1;
         pb = 0;
-        if (r < n) rowval(r, pa, pb);
-    };
-    w.vbase = owner_row(nullptr, offs_ll, n, j0);
-    load();
-    for (long long jb = j0; jb < j1; jb += 32) {
-        const int adv = w.count_le(jb);
-        if (adv > 0) {
-            w.vbase += adv;
+        if (r < w.n) rowval(r, pa, pb);
+    }
+    __device__ __forceinline__ void start(long long j0)
+    {
+        w.vbase = warp_owner_row(w.offs_ll, w.n, j0);
+        load();
+    }
+    // Batches are resolved in ascending order.  Entry j (this lane's entry of
+    // the batch [jb, jl]) receives its row's values; returns false when j lies
+    // outside the window, which a walk list never produces.  All lanes call.
+    __device__ __forceinline__ bool resolve(long long jb, long long jl, long long j, long long &a, long long &b)
+    {
+        if (w.count_le(jl) == 32) {  // the batch ends past the window
+            w.vbase += w.count_le(jb);
             load();
         }
-        const long long j = jb + lane;
-        bool done = j >= j1;
-        while (!__all_sync(GALA_FULL_MASK, done)) {
-            const int idx = w.count_le(j);
-            const bool here = !done && idx < 32;
-            const long long a = __shfl_sync(GALA_FULL_MASK, pa, idx & 31);
-            const long long b = __shfl_sync(GALA_FULL_MASK, pb, idx & 31);
-            if (here) f(j, w.vbase + idx, a, b);
-            done = done || here;
-            if (!__all_sync(GALA_FULL_MASK, done)) {
-                w.vbase += 32;
-                load();
-            }
-        }
+        const int idx = w.count_le(j);
+        a = __shfl_sync(GALA_FULL_MASK, pa, idx & 31);
+        b = __shfl_sync(GALA_FULL_MASK, pb, idx & 31);
+        return idx < 32;
     }
+};
+
+template <typename RV>
+__device__ __forceinline__ RowCursor<RV> row_cursor(const long long *offs_ll, int n, RV rv)
+{
+    return RowCursor<RV>{RowWindow{nullptr, offs_ll, n, 0, 0}, rv, -1, 0};
 }
+
+// Batches of 32 entries a warp keeps in flight in the walk kernels (their
+// loads are independent; one batch at a time leaves them latency-bound).
+constexpr int kWalkUnroll = 4;
 
 // Caller-supplied labels must lie in [0, n) before they index any array.
 __global__ void k_check_labels(const int32_t *__restrict__ comm, int n, DevStats *st)
@@ -310,24 +294,60 @@ __global__ void __launch_bounds__(256) k_stream_fill(int n, long long E, const i
     const int nnz = st->nz_rows;
     // per row: pa = destination of the row's entry j minus j, pb = 1 when the
     // row id is valid
-    auto rowval = [&](int r, long long &pa, long long &pb) {
+    auto rowval = [=](int r, long long &pa, long long &pb) {
         const int v = nz_rows[r];
         if (v < 0 || v >= n) return;
         pa = medge[mpos[v]] - offs[v];
         pb = 1;
     };
+    constexpr int U = kWalkUnroll;
+    const int lane = threadIdx.x & 31;
+    auto cur = row_cursor(nz_offs, nnz, rowval);
     for (long long t = wg; t * kRangeEntries < E; t += nw) {
         const long long j0 = t * kRangeEntries;
         const long long j1 = j0 + kRangeEntries < E ? j0 + kRangeEntries : E;
-        for_entries_rows(nz_offs, nnz, j0, j1, rowval, [&](long long j, int, long long d, long long ok) {
-            const long long dst = j + d;
-            if (!ok || dst < 0 || dst >= E) {  // recorded, never written
-                atomicOr(&st->err, kErrBadIndex);
-                return;
+        cur.start(j0);
+        for (long long jb = j0; jb < j1; jb += 32 * U) {
+            long long src[U], dst[U];
+            bool ok[U];
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                const long long b0 = jb + 32 * u;
+                ok[u] = false;
+                src[u] = dst[u] = 0;
+                if (b0 < j1) {  // warp-uniform
+                    const long long j = b0 + lane;
+                    long long d, valid;
+                    const bool in = cur.resolve(b0, b0 + 31 < j1 ? b0 + 31 : j1 - 1, j, d, valid);
+                    if (j < j1) {
+                        const long long to = j + d;
+                        if (!in || !valid || to < 0 || to >= E)  // recorded, never written
+                            atomicOr(&st->err, kErrBadIndex);
+                        else {
+                            ok[u] = true;
+                            src[u] = j;
+                            dst[u] = to;
+                        }
+                    }
+                }
             }
-            skey[dst] = lab[nbr[j]];
-            if (W) sw[dst] = w[j];
-        });
+            int key[U];
+            WT wv[U];
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                key[u] = ok[u] ? nbr[src[u]] : 0;
+                wv[u] = (W && ok[u]) ? w[src[u]] : (WT)0;
+            }
+#pragma unroll
+            for (int u = 0; u < U; ++u)
+                if (ok[u]) key[u] = lab[key[u]];
+#pragma unroll
+            for (int u = 0; u < U; ++u)
+                if (ok[u]) {
+                    skey[dst[u]] = key[u];
+                    if (W) sw[dst[u]] = wv[u];
+                }
+        }
     }
 }
 
@@ -1118,27 +1138,60 @@ __global__ void __launch_bounds__(256) k_compact(const int64_t *__restrict__ new
     const int C = (int)st->ccount;
     const long long Enew = st->new_entries;
     // per row: pa = the community (-1 when out of range), pb = source shift
-    auto rowval = [&](int r, long long &pa, long long &pb) {
+    auto rowval = [=](int r, long long &pa, long long &pb) {
         const int c = nz_rows[r];
         if (c < 0 || c >= C) return;
         pa = c;
         pb = tmp_off[c] - new_offs[c];
     };
+    constexpr int U = kWalkUnroll;
+    const int lane = threadIdx.x & 31;
+    auto cur = row_cursor(nz_offs, nnz, rowval);
     for (long long t = wg; t * kRangeEntries < Enew; t += nw) {
         const long long j0 = t * kRangeEntries;
         const long long j1 = j0 + kRangeEntries < Enew ? j0 + kRangeEntries : Enew;
-        for_entries_rows(nz_offs, nnz, j0, j1, rowval, [&](long long j, int, long long c, long long d) {
-            const long long src = j + d;
-            if (c < 0 || src < 0 || src >= tmp_cap) {  // recorded, never read or written
-                atomicOr(&st->err, kErrBadIndex);
-                return;
+        cur.start(j0);
+        for (long long jb = j0; jb < j1; jb += 32 * U) {
+            long long src[U], com[U];
+            bool ok[U];
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                const long long b0 = jb + 32 * u;
+                ok[u] = false;
+                src[u] = 0;
+                com[u] = -1;
+                if (b0 < j1) {  // warp-uniform
+                    const long long j = b0 + lane;
+                    long long c, d;
+                    const bool in = cur.resolve(b0, b0 + 31 < j1 ? b0 + 31 : j1 - 1, j, c, d);
+                    if (j < j1) {
+                        const long long from = j + d;
+                        if (!in || c < 0 || from < 0 || from >= tmp_cap)  // recorded, never read or written
+                            atomicOr(&st->err, kErrBadIndex);
+                        else {
+                            ok[u] = true;
+                            src[u] = from;
+                            com[u] = c;
+                        }
+                    }
+                }
             }
-            const int32_t u = tmp_nbr[src];
-            const WT wt = tmp_w[src];
-            out_nbr[j] = u;
-            out_w[j] = wt;
-            if (self_out && u == c) self_out[c] = wt;
-        });
+            int32_t nb[U];
+            WT wt[U];
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                nb[u] = ok[u] ? tmp_nbr[src[u]] : 0;
+                wt[u] = ok[u] ? tmp_w[src[u]] : (WT)0;
+            }
+#pragma unroll
+            for (int u = 0; u < U; ++u)
+                if (ok[u]) {
+                    const long long j = jb + 32 * u + lane;
+                    out_nbr[j] = nb[u];
+                    out_w[j] = wt[u];
+                    if (self_out && nb[u] == com[u]) self_out[com[u]] = wt[u];
+                }
+        }
     }
 }
 
@@ -1216,6 +1269,19 @@ static int grid_cap(long long items, int per_block, int cap)
     if (g > cap) g = cap;
     if (g < 1) g = 1;
     return (int)g;
+}
+
+// Blocks of a grid-stride kernel that are resident at once (threads per
+// block, dynamic shared memory): a larger grid runs a second, partial wave.
+template <typename K>
+static int resident_grid(K kernel, int threads, size_t smem = 0)
+{
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, smem) != cudaSuccess || per_sm < 1) {
+        cudaGetLastError();
+        per_sm = 1;
+    }
+    return per_sm * sm_count();
 }
 
 // Walk list of the rows of (offs, n) that have entries (E entries in total).
@@ -1399,15 +1465,16 @@ static int contract_t(const LevelGraph &g, const int32_t *comm, ContractBuffers 
     const bool weighted = g.w != nullptr;
     if (E > 0) {
         build_walk_list(g.offs, n, E, b, st);
-        const int fill_grid = grid_cap((E + kRangeEntries - 1) / kRangeEntries * 32, 256, cap);
-        if (weighted)
-            k_stream_fill<WT, true><<<fill_grid, 256, 0, st>>>(n, E, g.offs, g.nbr, (const WT *)g.w, b.lab, b.mpos,
-                                                              b.medge, b.stream_key, (WT *)b.stream_w, b.nz_rows,
-                                                              b.nz_offs, ds);
-        else
-            k_stream_fill<WT, false><<<fill_grid, 256, 0, st>>>(n, E, g.offs, g.nbr, nullptr, b.lab, b.mpos,
-                                                               b.medge, b.stream_key, nullptr, b.nz_rows,
-                                                               b.nz_offs, ds);
+        const int tasks = grid_cap((E + kRangeEntries - 1) / kRangeEntries * 32, 256, cap);
+        if (weighted) {
+            const int grid = std::min(tasks, resident_grid(k_stream_fill<WT, true>, 256));
+            k_stream_fill<WT, true><<<grid, 256, 0, st>>>(n, E, g.offs, g.nbr, (const WT *)g.w, b.lab, b.mpos, b.medge,
+                                                          b.stream_key, (WT *)b.stream_w, b.nz_rows, b.nz_offs, ds);
+        } else {
+            const int grid = std::min(tasks, resident_grid(k_stream_fill<WT, false>, 256));
+            k_stream_fill<WT, false><<<grid, 256, 0, st>>>(n, E, g.offs, g.nbr, nullptr, b.lab, b.mpos, b.medge,
+                                                           b.stream_key, nullptr, b.nz_rows, b.nz_offs, ds);
+        }
         note_launch(1);
     }
     k_classify<<<grid_cap(n, 256, cap), 256, 0, st>>>(b.ec, b.cls_list, n, b.kc, ds, sort_rows ? 1 : 0);
@@ -1434,45 +1501,62 @@ static int contract_t(const LevelGraph &g, const int32_t *comm, ContractBuffers 
     const int n_small = most(1), n_warp = sort_rows ? 0 : most(kSmallMax + 1);
     const int n_mid1 = most(sort_rows ? kSmallMax + 1 : kWarpAggMax + 1), n_mid2 = most(kMid1Max + 1);
     const int n_mid3 = sort_rows ? 0 : most(kMid2Max + 1), n_long = most((sort_rows ? kMid2Max : kMid3Max) + 1);
-    if (n_small > 0) {
-        k_agg_small<WT><<<grid_cap((long long)n_small * 32, 256, cap), 256, 0, st>>>(a, b.cls_list);
+    // The classes are independent (disjoint tmp ranges and kc entries): with
+    // auxiliary streams they aggregate concurrently, the long rows (the
+    // longest chain of launches) first.
+    cudaStream_t cs[ContractBuffers::kAux];
+    const bool par = b.aux[0] != nullptr && b.fork_ev != nullptr;
+    if (par) cudaEventRecord(b.fork_ev, st);
+    for (int i = 0; i < ContractBuffers::kAux; ++i) {
+        cs[i] = par ? b.aux[i] : st;
+        if (par) cudaStreamWaitEvent(cs[i], b.fork_ev, 0);
+    }
+    bool ok = n_long == 0 ||
+              contract_long_rows(a, b, b.cls_list + (long long)kLongCls * n, n_long, cs[3], status, sort_rows);
+    if (ok && n_mid2 > 0) {
+        const int grid = n_mid2 < nsm * 2 ? n_mid2 : nsm * 2;
+        if (sort_rows)
+            k_agg_mid<WT, 256, 8192, kMid2Max><<<grid, 256, mid2_smem<WT>(), cs[2]>>>(a, b.cls_list + 2LL * n, 2);
+        else
+            k_agg_mid_list<WT, 1024, 8192><<<grid, 1024, list_smem<WT>(8192), cs[2]>>>(a, b.cls_list + 2LL * n, 2);
         note_launch(1);
     }
-    if (n_warp > 0) {
-        k_agg_warp_list<WT><<<grid_cap((long long)n_warp * 32, 256, cap), 256, 0, st>>>(
+    if (ok && n_mid3 > 0) {  // 4097-8192 entries, rows in table order
+        const int grid = n_mid3 < nsm ? n_mid3 : nsm;
+        k_agg_mid_list<WT, 1024, 16384><<<grid, 1024, list_smem<WT>(16384), cs[2]>>>(a, b.cls_list + 3LL * n, 3);
+        note_launch(1);
+    }
+    if (ok && n_mid1 > 0) {
+        const int grid = n_mid1 < nsm * 16 ? n_mid1 : nsm * 16;
+        if (sort_rows)
+            k_agg_mid<WT, 128, 1024, kMid1Max><<<grid, 128, mid1_smem<WT>(), cs[1]>>>(a, b.cls_list + (long long)n, 1);
+        else
+            k_agg_mid_list<WT, 128, 1024><<<grid, 128, list_smem<WT>(1024), cs[1]>>>(a, b.cls_list + (long long)n,
+                                                                                      1);
+        note_launch(1);
+    }
+    if (ok && n_small > 0) {
+        k_agg_small<WT><<<grid_cap((long long)n_small * 32, 256, cap), 256, 0, cs[0]>>>(a, b.cls_list);
+        note_launch(1);
+    }
+    if (ok && n_warp > 0) {
+        k_agg_warp_list<WT><<<grid_cap((long long)n_warp * 32, 256, cap), 256, 0, cs[0]>>>(
             a, b.cls_list + (long long)kWarpCls * n);
         note_launch(1);
     }
-    if (n_mid1 > 0) {
-        const int grid = n_mid1 < nsm * 16 ? n_mid1 : nsm * 16;
-        if (sort_rows)
-            k_agg_mid<WT, 128, 1024, kMid1Max><<<grid, 128, mid1_smem<WT>(), st>>>(a, b.cls_list + (long long)n, 1);
-        else
-            k_agg_mid_list<WT, 128, 1024><<<grid, 128, list_smem<WT>(1024), st>>>(a, b.cls_list + (long long)n, 1);
-        note_launch(1);
-    }
-    if (n_mid2 > 0) {
-        const int grid = n_mid2 < nsm * 2 ? n_mid2 : nsm * 2;
-        if (sort_rows)
-            k_agg_mid<WT, 256, 8192, kMid2Max><<<grid, 256, mid2_smem<WT>(), st>>>(a, b.cls_list + 2LL * n, 2);
-        else
-            k_agg_mid_list<WT, 1024, 8192><<<grid, 1024, list_smem<WT>(8192), st>>>(a, b.cls_list + 2LL * n, 2);
-        note_launch(1);
-    }
-    if (n_mid3 > 0) {  // 4097-8192 entries, rows in table order
-        const int grid = n_mid3 < nsm ? n_mid3 : nsm;
-        k_agg_mid_list<WT, 1024, 16384><<<grid, 1024, list_smem<WT>(16384), st>>>(a, b.cls_list + 3LL * n, 3);
-        note_launch(1);
-    }
-    if (n_long > 0 &&
-        !contract_long_rows(a, b, b.cls_list + (long long)kLongCls * n, n_long, st, status, sort_rows))
-        return -1;
+    if (par)
+        for (int i = 0; i < ContractBuffers::kAux; ++i) {
+            cudaEventRecord(b.join_ev[i], cs[i]);
+            cudaStreamWaitEvent(st, b.join_ev[i], 0);
+        }
+    if (!ok) return -1;
     exclusive_scan_dev(b.kc, new_offs, n, dC, OpIdentity(), b.scan_partial, &ds->new_entries, st, &ds->err);
     k_set_last_offset<<<1, 1, 0, st>>>(new_offs, ds);
     note_launch(1);
     if (E > 0) {  // the new level has at most E entries
         build_walk_list(new_offs, n, 0, b, st, dC, &ds->new_entries);
-        k_compact<WT><<<grid_cap((E + kRangeEntries - 1) / kRangeEntries * 32, 256, cap), 256, 0, st>>>(
+        const int tasks = grid_cap((E + kRangeEntries - 1) / kRangeEntries * 32, 256, cap);
+        k_compact<WT><<<std::min(tasks, resident_grid(k_compact<WT>, 256)), 256, 0, st>>>(
             new_offs, b.tmp_off, b.tmp_nbr, (const WT *)b.tmp_w, new_nbr, new_w, E, b.nz_rows, b.nz_offs, ds,
             (WT *)nli.self);
         note_launch(1);

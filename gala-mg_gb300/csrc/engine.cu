@@ -687,6 +687,12 @@ void bind_contract_buffers(gala_context *ctx)
     cb.scan_partial = ctx->p1.scan_partial;
     cb.big_bitmap = ctx->scratch;
     cb.big_bitmap_words = ctx->scratch_ints;
+    static_assert(ContractBuffers::kAux == gala_context::kAux, "auxiliary streams");
+    for (int i = 0; i < gala_context::kAux; ++i) {
+        cb.aux[i] = ctx->aux[i];
+        cb.join_ev[i] = ctx->join_ev[i];
+    }
+    cb.fork_ev = ctx->fork_ev;
 }
 
 struct RunOut {

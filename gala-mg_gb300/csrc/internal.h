@@ -269,6 +269,11 @@ struct ContractBuffers {
     long long big_bitmap_words;
     long long *scan_partial;
     DevStats *stats;
+    // auxiliary streams (null: none): the size classes aggregate concurrently
+    static constexpr int kAux = 4;
+    cudaStream_t aux[kAux] = {};
+    cudaEvent_t fork_ev = nullptr;
+    cudaEvent_t join_ev[kAux] = {};
 };
 // sort_rows = false (the level-to-level contraction of a Louvain run) leaves
 // every new row in hash-table order: phase 1 does not depend on the order of
