@@ -24,10 +24,10 @@ INC = os.path.join(os.path.dirname(PKG), "include")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CU_UNITS = ["phase1.cu", "contract.cu", "engine.cu", "modularity_static.cu", "proposal.cu", "batch.cu", "refine.cu",
-            "batch_cta.cu"]
+            "batch_cta.cu", "update_push.cu"]
 CPP_UNITS = ["graph_host.cpp"]
 CLIS = ["gala_main.cpp", "gala_preprocess.cpp"]
-HEADERS = ["common.cuh", "scan.cuh", "internal.h", "binlimits.h"]
+HEADERS = ["common.cuh", "scan.cuh", "walk.cuh", "internal.h", "binlimits.h"]
 
 
 def _nvcc():

@@ -90,6 +90,12 @@ struct DevStats {
     long long big_nwork;    // long rows: stream chunks
     long long big_ntwork;   // long rows: table chunks
     long long big_lwork;    // long rows: slot-list chunks
+    // incremental weight update
+    unsigned long long mv_edges;  // row entries of this sweep's movers
+    long long push_total;         // the same, summed by the movers' prefix
+    unsigned long long sym_hash;  // 0 when the graph is symmetric (hash of every entry minus its mirror)
+    int push_mode;                // 1: this sweep updates In incrementally (the per-bin updates return at once)
+    int push_len;                 // movers in the prefix scan (0 unless push_mode)
 };
 
 constexpr int kErrHashOverflow = 1;
@@ -290,6 +296,39 @@ __device__ __forceinline__ T warp_sum(T v)
 #pragma unroll
     for (int o = 16; o >= 1; o >>= 1) v += __shfl_xor_sync(GALA_FULL_MASK, v, o);
     return v;
+}
+
+// ---------------------------------------------------------------------------
+// Block reductions into the device counters (all threads must call).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void block_add_u64(unsigned long long v, unsigned long long *dst)
+{
+    __shared__ unsigned long long red[32];
+    v = warp_sum(v);
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (lane == 0) red[wid] = v;
+    __syncthreads();
+    if (wid == 0) {
+        unsigned long long t = lane < (int)(blockDim.x >> 5) ? red[lane] : 0ull;
+        t = warp_sum(t);
+        if (lane == 0 && t) atomicAdd(dst, t);
+    }
+    __syncthreads();
+}
+
+__device__ __forceinline__ void block_add_i32(int v, int *dst)
+{
+    __shared__ int red[32];
+    v = warp_sum(v);
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (lane == 0) red[wid] = v;
+    __syncthreads();
+    if (wid == 0) {
+        int t = lane < (int)(blockDim.x >> 5) ? red[lane] : 0;
+        t = warp_sum(t);
+        if (lane == 0 && t) atomicAdd(dst, t);
+    }
+    __syncthreads();
 }
 
 }  // namespace gala

@@ -51,6 +51,12 @@ struct gala_context {
     cudaEvent_t ev[8] = {};
     // slots of the largest hub table (gala_context_set_hub_table_cap; 0 = by degree)
     long long hub_table_cap = 0;
+    // weight update of the sweeps (gala_context_set_update_mode): 0 = the
+    // incremental update when the movers' rows are few, 1 = always the full
+    // update, 2 = incremental whenever allowed
+    int update_mode = 0;
+    // symmetry of the current run's graph: -1 = not known yet, 0 / 1
+    int sym_state = -1;
     // per-graph state of gala_louvain_batch, kept between calls (reallocated
     // only for a larger batch)
     BatchRun *batch = nullptr;
@@ -183,6 +189,7 @@ struct Phase1Out {
     long long movers = 0;         // moves applied (kept or dropped)
     long long nv = 0;             // vertices with edges (the degree-bin order)
     long long active_entries = 0; // row entries decided
+    long long incr_sweeps = 0;    // sweeps with the incremental weight update
 };
 
 // Move-proposal settings of one run (mode GALA_PROPOSAL_OFF / TRACE / SKIP).
@@ -388,6 +395,14 @@ gala_status phase1(gala_context *ctx, const LevelGraph &g, long long &m2, double
         p1_hub_work_launch(hp, st);
     }
     cudaMemsetAsync(b.act_flag, 1, (size_t)g.n, st);
+    // incremental weight updates: plain runs of one graph on a symmetric
+    // graph (the symmetry hash of the run's first level, summed by its
+    // level-init row kernels, is 0)
+    const bool incr_level = !bt && pmode == GALA_PROPOSAL_OFF && ctx->update_mode != 1;
+    if (incr_level) {
+        cudaMemsetAsync(b.moved, 0, (size_t)g.n, st);
+        if (ctx->sym_state < 0) ctx->sym_state = (!g.ks_ready && h->sym_hash == 0) ? 1 : 0;
+    }
     b.features_on = pmode != GALA_PROPOSAL_OFF;
     b.wide = g.wide;
     if (b.features_on) p1_features_init(b, g.n, st);
@@ -463,16 +478,20 @@ gala_status phase1(gala_context *ctx, const LevelGraph &g, long long &m2, double
     bool verify = false;  // proposals stalled: the rest of the level runs plain sweeps
     // CUDA graphs of the repeated sweeps (plain runs): one per active-list slot
     const bool graphs = use_graphs && pmode == GALA_PROPOSAL_OFF;
-    cudaGraphExec_t gexec[2] = {nullptr, nullptr};
-    long long glaunch[2] = {0, 0};
+    // (and per kind of weight update: with or without the incremental path)
+    cudaGraphExec_t gexec[4] = {nullptr, nullptr, nullptr, nullptr};
+    long long glaunch[4] = {0, 0, 0, 0};
     struct GraphGuard {
         cudaGraphExec_t *e;
         ~GraphGuard()
         {
-            for (int i = 0; i < 2; ++i)
+            for (int i = 0; i < 4; ++i)
                 if (e[i]) cudaGraphExecDestroy(e[i]);
         }
     } gguard{gexec};
+    // row entries of the previous sweep's movers (the incremental update is
+    // enqueued only after a sweep that moved under a third of them)
+    unsigned long long prev_mv_edges = ~0ull;
     cudaEventRecord(ctx->ev[0], st);
     for (;;) {
         const int nxt = cur ^ 1;
@@ -489,6 +508,14 @@ gala_status phase1(gala_context *ctx, const LevelGraph &g, long long &m2, double
             ps.iteration = iteration;
             ps.level = pr->level;
         }
+        // incremental weight update of this sweep (its kernels decide on the
+        // device whether it runs): from a level's second sweep on, on levels
+        // of at least 2^23 entries (below, the full update takes tens of
+        // microseconds), after a sweep whose movers held under a third of the
+        // entries (otherwise its launches would mostly return at once)
+        const bool incr = incr_level && ctx->sym_state == 1 && iteration > 1 &&
+                          (ctx->update_mode == 2 ||
+                           (g.E >= (1LL << 23) && prev_mv_edges * 3 < (unsigned long long)g.E));
         // the sweep: decide, apply, reductions, update, counters to the host
         auto enqueue = [&](bool capturing) {
             // timing events become event nodes of a captured graph
@@ -518,13 +545,17 @@ gala_status phase1(gala_context *ctx, const LevelGraph &g, long long &m2, double
             }
             join(ctx);
             rec(ctx->ev[3]);
-            p1_apply_movers(b, +1, g.n, st, iteration);
+            p1_apply_movers(b, +1, g.n, st, iteration, g.offs, incr ? b.moved : nullptr);
             if (pmode == GALA_PROPOSAL_TRACE && iteration > 1) p1_trace_labels(b, ps, st);
             if (bt)
                 batch_graph_sums(kMinTot | kSumTot2, G, bt->goff, bt->stop, b, bt->sums(), st);
             else
                 p1_tot_reduce(b, g.n, st);
             rec(ctx->ev[4]);
+            // the incremental update decides on the device whether it runs
+            // (the per-bin updates below then return at once); In is exact
+            // from the first sweep's update on
+            if (incr) p1_push_update(g, b, bin_start, nxt, constant, m2, 1, ctx->update_mode == 2 ? 1 : 0, st);
             fork(ctx);
             for (int k = 0; k < kNumBins; ++k) {
                 const int bin = kBinLaunchOrder[k];
@@ -548,21 +579,22 @@ gala_status phase1(gala_context *ctx, const LevelGraph &g, long long &m2, double
         if (graphs && iteration > 1) {
             // sweeps after the first repeat the same launches with the active
             // lists of slot `cur`: captured once per level and slot, replayed
-            if (!gexec[cur]) {
+            const int gi = cur + (incr ? 2 : 0);
+            if (!gexec[gi]) {
                 const long long l0 = gala_kernel_launch_count();
                 cudaGraph_t gr = nullptr;
                 if ((s = check(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal), "graph capture")))
                     return s;
                 enqueue(true);
                 if ((s = check(cudaStreamEndCapture(st, &gr), "graph capture"))) return s;
-                const cudaError_t ie = cudaGraphInstantiate(&gexec[cur], gr, 0);
+                const cudaError_t ie = cudaGraphInstantiate(&gexec[gi], gr, 0);
                 cudaGraphDestroy(gr);
                 if ((s = check(ie, "graph instantiate"))) return s;
-                glaunch[cur] = gala_kernel_launch_count() - l0;
-                note_launch((int)-glaunch[cur]);  // counted when replayed
+                glaunch[gi] = gala_kernel_launch_count() - l0;
+                note_launch((int)-glaunch[gi]);  // counted when replayed
             }
-            if ((s = check(cudaGraphLaunch(gexec[cur], st), "graph launch"))) return s;
-            note_launch((int)glaunch[cur]);
+            if ((s = check(cudaGraphLaunch(gexec[gi], st), "graph launch"))) return s;
+            note_launch((int)glaunch[gi]);
         } else {
             enqueue(false);
         }
@@ -586,7 +618,13 @@ gala_status phase1(gala_context *ctx, const LevelGraph &g, long long &m2, double
         out->decide_ms += ev_ms(ctx->ev[2], ctx->ev[3]);
         out->update_ms += ev_ms(ctx->ev[4], ctx->ev[5]);
         out->decide_bytes += decide_bytes_for(dec_nv, dec_ne, weighted);
-        out->update_bytes += nv_all * (2 * 8 + 4 * 4) + g.E * (8 + (weighted ? 4 : 0));
+        prev_mv_edges = h->mv_edges;
+        if (h->push_mode) {  // the movers' rows, then one pass over the vertices
+            out->incr_sweeps += 1;
+            out->update_bytes += h->push_total * (8 + (weighted ? 4 : 0)) + nv_all * (4 * 4 + 4 + 4 + 1 + 2 * 8);
+        } else {
+            out->update_bytes += nv_all * (2 * 8 + 4 * 4) + g.E * (8 + (weighted ? 4 : 0));
+        }
         out->sweeps += 1;
         if (verify) out->verify_sweeps += 1;
         act_nv = h->act_vertices[nxt];
@@ -755,6 +793,7 @@ gala_status run_levels(gala_context *ctx, int32_t n0, int64_t E0, const int64_t 
                   ctx->n_cap, (long long)ctx->e_cap);
         return GALA_ERR_CAPACITY;
     }
+    ctx->sym_state = -1;  // checked with the first level
     // degree-bin tuning
     {
         BinLimits lim;
@@ -850,7 +889,7 @@ gala_status run_levels(gala_context *ctx, int32_t n0, int64_t E0, const int64_t 
     std::vector<double> trace;
     double contract_ms = 0, p1_ms = 0, dec_ms = 0, upd_ms = 0;
     long long dec_bytes = 0, upd_bytes = 0, sweeps = 0;
-    long long decisions = 0, skipped = 0, verify_sweeps = 0;
+    long long decisions = 0, skipped = 0, verify_sweeps = 0, incr_sweeps = 0;
     int C = n0;
     for (;;) {
         if (verbose) printf("===============round:%d===============\n", round);
@@ -865,6 +904,7 @@ gala_status run_levels(gala_context *ctx, int32_t n0, int64_t E0, const int64_t 
         decisions += po.decisions;
         skipped += po.skipped;
         verify_sweeps += po.verify_sweeps;
+        incr_sweeps += po.incr_sweeps;
         p1_ms += po.total_ms;
         dec_ms += po.decide_ms;
         upd_ms += po.update_ms;
@@ -988,6 +1028,7 @@ gala_status run_levels(gala_context *ctx, int32_t n0, int64_t E0, const int64_t 
     res->decisions = decisions;
     res->skipped = skipped;
     res->verify_sweeps = verify_sweeps;
+    res->incremental_sweeps = (int32_t)incr_sweeps;
     res->samples = 0;
     if (pr.mode == GALA_PROPOSAL_TRACE) {
         long long cnt = 0;
@@ -1122,6 +1163,7 @@ gala_status gala_context_create(int32_t device, int32_t max_vertices, int64_t ma
          dalloc(ctx, &c.big_tchunks, n) && dalloc(ctx, &c.big_tcoff, n + 1) &&
          dalloc(ctx, &c.big_twork, (size_t)c.big_twork_cap) && dalloc(ctx, &c.big_kdist, n) &&
          dalloc(ctx, &c.big_cursor, n) && dalloc(ctx, &c.big_gwords, n) && dalloc(ctx, &c.big_gofs, n + 1);
+    ok = ok && dalloc(ctx, &b.moved, n) && dalloc(ctx, &b.mv_pre, (size_t)n + 1);
     ok = ok && dalloc(ctx, &b.act_flag, n) && dalloc(ctx, &ctx->hub_px, (size_t)c.big_twork_cap) &&
          dalloc(ctx, &ctx->hub_pc, (size_t)c.big_twork_cap) && dalloc8(ctx, &ctx->hub_pw, (size_t)c.big_twork_cap) &&
          dalloc(ctx, &ctx->hub_pt, (size_t)c.big_twork_cap) && dalloc8(ctx, &ctx->hub_pwc, (size_t)c.big_twork_cap) &&
@@ -1178,6 +1220,17 @@ gala_status gala_context_set_hub_table_cap(gala_context *ctx, int64_t slots)
         return GALA_ERR_INVALID;
     }
     ctx->hub_table_cap = slots;
+    return GALA_OK;
+}
+
+gala_status gala_context_set_update_mode(gala_context *ctx, int32_t mode)
+{
+    clear_error();
+    if (!ctx || mode < 0 || mode > 2) {
+        set_error("gala_context_set_update_mode: mode must be 0, 1 or 2");
+        return GALA_ERR_INVALID;
+    }
+    ctx->update_mode = mode;
     return GALA_OK;
 }
 
@@ -1777,6 +1830,7 @@ gala_status gala_phase1_device(gala_context *ctx, int32_t n, const int64_t *d_of
     long long m2 = 0;
     std::vector<double> trace;
     Phase1Out po;
+    ctx->sym_state = -1;  // a new graph: checked with its first sweep
     if ((s = phase1(ctx, g, m2, min_modularity, false, &trace, &po))) return s;
     if ((s = check(cudaMemcpyAsync(d_community_out, ctx->p1.comm, (size_t)n * sizeof(int32_t),
                                    cudaMemcpyDeviceToDevice, st),

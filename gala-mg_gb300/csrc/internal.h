@@ -86,6 +86,10 @@ struct Phase1Buffers {
     int32_t *hub_table;        // global hash tables of the largest bin
     long long hub_table_slots; // capacity in int32 pairs
     uint8_t *act_flag;         // 1 = vertex is in the current active set
+    // incremental weight update: movers of the sweep flagged (cleared by the
+    // prune pass) and the prefix of their row lengths
+    uint8_t *moved;
+    long long *mv_pre;
     // move-proposal features (written only when a proposal mode is on)
     float *feat_gain;          // best corrected gain at the last decision / (K m2)
     int32_t *feat_ndist;       // distinct neighbour communities at the last decision (-1 = unknown)
@@ -148,7 +152,22 @@ void p1_iter_reset(Phase1Buffers &b, int next, long long min_tot_init, cudaStrea
 void p1_decide(const LevelGraph &g, Phase1Buffers &b, int bin, const int32_t *list,
                const int *count_ptr, int level_count, double constant, long long m2,
                int fp64_only, bool first, cudaStream_t st);
-void p1_apply_movers(Phase1Buffers &b, int sign, int n, cudaStream_t st, int iteration = 0);
+// offs: the movers' row lengths are summed into stats->mv_edges (sign +1);
+// moved: movers are flagged for the incremental weight update.
+void p1_apply_movers(Phase1Buffers &b, int sign, int n, cudaStream_t st, int iteration = 0,
+                     const int64_t *offs = nullptr, uint8_t *moved = nullptr);
+// Incremental weight update of a sweep, enqueued after the movers are
+// applied and before the per-bin updates: a device flag (stats->push_mode)
+// picks it when `allow` (In exact from the previous sweep, symmetric graph)
+// and the movers' rows hold under a third of the entries (always with
+// `force`); the per-bin update kernels then return at once.  It sums In of
+// every mover over its row, pushes +-w from every mover to its neighbours
+// that did not move, then runs one pass over the vertices of bins 0-7 for the
+// pruning bound, the next active lists and the sums.  bin_start: the level's
+// order-list bin starts (host copy).
+void p1_push_update(const LevelGraph &g, Phase1Buffers &b, const int *bin_start, int next, double constant,
+                    long long m2, int allow, int force, cudaStream_t st);
+
 void p1_tot_reduce(Phase1Buffers &b, int n, cudaStream_t st);
 void p1_update(const LevelGraph &g, Phase1Buffers &b, int bin, const int32_t *list, int count, int next,
                int bin_start, double constant, long long m2, cudaStream_t st);

@@ -32,38 +32,6 @@ int hub_grid_size() { return num_sms(); }
 
 constexpr int kCountBlock = 1024;
 
-// ------------------------------------------------------------------------
-// Block reductions into the device counters (all threads must call).
-// ------------------------------------------------------------------------
-__device__ __forceinline__ void block_add_u64(unsigned long long v, unsigned long long *dst)
-{
-    __shared__ unsigned long long red[32];
-    v = warp_sum(v);
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    if (lane == 0) red[wid] = v;
-    __syncthreads();
-    if (wid == 0) {
-        unsigned long long t = lane < (int)(blockDim.x >> 5) ? red[lane] : 0ull;
-        t = warp_sum(t);
-        if (lane == 0 && t) atomicAdd(dst, t);
-    }
-    __syncthreads();
-}
-
-__device__ __forceinline__ void block_add_i32(int v, int *dst)
-{
-    __shared__ int red[32];
-    v = warp_sum(v);
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    if (lane == 0) red[wid] = v;
-    __syncthreads();
-    if (wid == 0) {
-        int t = lane < (int)(blockDim.x >> 5) ? red[lane] : 0;
-        t = warp_sum(t);
-        if (lane == 0 && t) atomicAdd(dst, t);
-    }
-    __syncthreads();
-}
 
 // Exact 128-bit block sum added to the (lo, hi) counter pair (carry from the
 // low word's atomic result, so the total does not depend on the order).
@@ -207,9 +175,33 @@ __global__ void __launch_bounds__(kCountBlock) k_bin_scatter(int n, const int64_
         st->bin_start[threadIdx.x] = threadIdx.x < kNumBinSlots ? blockoff[threadIdx.x * nblk] : n;
 }
 
+// Symmetry hash of one entry: h(v, u, w) - h(u, v, w), summed over all
+// entries modulo 2^64 (stats->sym_hash), is 0 when every entry has a mirror.
+// Two rounds of the murmur3 finaliser per 32-bit half.
+__device__ __forceinline__ unsigned fmix32(unsigned h)
+{
+    h ^= h >> 16;
+    h *= 0x85EBCA6Bu;
+    h ^= h >> 13;
+    h *= 0xC2B2AE35u;
+    return h ^ (h >> 16);
+}
+__device__ __forceinline__ unsigned long long dir_hash(int a, int b, unsigned long long w)
+{
+    const unsigned wl = (unsigned)w, wh = (unsigned)(w >> 32);
+    const unsigned x = fmix32((unsigned)a ^ fmix32((unsigned)b ^ 0x9E3779B9u) ^ wl);
+    const unsigned y = fmix32((unsigned)b + fmix32((unsigned)a + 0x7F4A7C15u) + wh * 0x85EBCA77u + wl);
+    return ((unsigned long long)x << 32) | y;
+}
+__device__ __forceinline__ unsigned long long sym_term(int v, int u, unsigned long long w)
+{
+    return dir_hash(v, u, w) - dir_hash(u, v, w);
+}
+
 // K = row weight sum, Self = self-loop weight (init_communities,
 // kernel_functions.cu:34-73); Tot = K, In = Self.  Accumulates sum(K),
-// sum(K^2) and sum(Self) for the modularity of the singleton partition.
+// sum(K^2) and sum(Self) for the modularity of the singleton partition, and
+// the symmetry hash.
 template <typename WT, int G, bool W>
 __global__ void __launch_bounds__(256) k_init_rows_group(const int32_t *__restrict__ list, int count,
                                                          const int64_t *__restrict__ offs,
@@ -221,7 +213,7 @@ __global__ void __launch_bounds__(256) k_init_rows_group(const int32_t *__restri
     constexpr int GPW = 32 / G;
     const int wg = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int nw = (gridDim.x * blockDim.x) >> 5;
-    unsigned long long sk = 0, ss = 0;
+    unsigned long long sk = 0, ss = 0, hs = 0;
     typename SqSum<WT>::T sk2 = 0;
     for (int base = wg * GPW; base < count; base += nw * GPW) {
         const int idx = base + gw;
@@ -236,8 +228,10 @@ __global__ void __launch_bounds__(256) k_init_rows_group(const int32_t *__restri
         WT k = 0, sf = 0;
         for (long long j = s + sub; j < e; j += G) {
             WT wt = W ? w[j] : 1;
+            const int u = nbr[j];
             k += wt;
-            if (nbr[j] == v) sf = wt;
+            if (u == v) sf = wt;
+            hs += sym_term(v, u, (unsigned long long)wt);
         }
 #pragma unroll
         for (int o = G / 2; o >= 1; o >>= 1) {
@@ -257,6 +251,7 @@ __global__ void __launch_bounds__(256) k_init_rows_group(const int32_t *__restri
     block_add_u64(sk, &st->sum_k);
     SqSum<WT>::add(sk2, st);
     block_add_u64(ss, &st->sum_in);
+    block_add_u64(hs, &st->sym_hash);
 }
 
 template <typename WT, bool W>
@@ -267,7 +262,7 @@ __global__ void __launch_bounds__(256) k_init_rows_cta(const int32_t *__restrict
                                                        DevStats *st)
 {
     __shared__ WT rk[8], rs[8];
-    unsigned long long sk = 0, ss = 0;
+    unsigned long long sk = 0, ss = 0, hs = 0;
     typename SqSum<WT>::T sk2 = 0;
     for (int i = blockIdx.x; i < count; i += gridDim.x) {
         int v = list[i];
@@ -275,8 +270,10 @@ __global__ void __launch_bounds__(256) k_init_rows_cta(const int32_t *__restrict
         WT k = 0, sf = 0;
         for (long long j = s + threadIdx.x; j < e; j += blockDim.x) {
             WT wt = W ? w[j] : 1;
+            const int u = nbr[j];
             k += wt;
-            if (nbr[j] == v) sf = wt;
+            if (u == v) sf = wt;
+            hs += sym_term(v, u, (unsigned long long)wt);
         }
         k = warp_sum(k);
         sf = warp_sum(sf);
@@ -305,6 +302,7 @@ __global__ void __launch_bounds__(256) k_init_rows_cta(const int32_t *__restrict
     block_add_u64(sk, &st->sum_k);
     SqSum<WT>::add(sk2, st);
     block_add_u64(ss, &st->sum_in);
+    block_add_u64(hs, &st->sym_hash);
 }
 
 __global__ void k_reset_level_stats(DevStats *st)
@@ -317,6 +315,7 @@ __global__ void k_reset_level_stats(DevStats *st)
     st->max_deg = 0;
     st->err = 0;
     st->n_movers = 0;
+    st->sym_hash = 0;
 }
 
 void p1_reset_level_stats(Phase1Buffers &b, cudaStream_t st)
@@ -1418,15 +1417,16 @@ void p1_configure_kernels()
 // ------------------------------------------------------------------------
 template <typename WT>
 __global__ void k_apply_movers(const int32_t *__restrict__ mv_v, const int32_t *__restrict__ mv_old,
-                               const int32_t *__restrict__ mv_new, const DevStats *__restrict__ stp, int sign,
-                               int32_t *comm, WT *Tot, int32_t *size, const WT *__restrict__ K,
-                               int32_t *last_move, int iteration)
+                               const int32_t *__restrict__ mv_new, DevStats *stp, int sign, int32_t *comm, WT *Tot,
+                               int32_t *size, const WT *__restrict__ K, int32_t *last_move, int iteration,
+                               const int64_t *__restrict__ offs, uint8_t *moved)
 {
     // whole warps step together: movers of one warp that share a source or a
     // target community add to its Tot and size once (many movers of a sweep
     // head for the same large community)
     const int nm = stp->n_movers;
     const int lane = threadIdx.x & 31;
+    unsigned long long deg = 0;
     for (int i0 = blockIdx.x * blockDim.x + threadIdx.x - lane; i0 < nm; i0 += gridDim.x * blockDim.x) {
         const int i = i0 + lane;
         const bool valid = i < nm;
@@ -1439,6 +1439,8 @@ __global__ void k_apply_movers(const int32_t *__restrict__ mv_v, const int32_t *
             k = K[v];
             comm[v] = to;
             if (last_move && sign > 0) last_move[v] = iteration;
+            if (offs) deg += (unsigned long long)(offs[v + 1] - offs[v]);
+            if (moved) moved[v] = 1;
         }
         const unsigned mt = __match_any_sync(GALA_FULL_MASK, to);
         const WT kt = group_sum(mt, k);
@@ -1453,10 +1455,13 @@ __global__ void k_apply_movers(const int32_t *__restrict__ mv_v, const int32_t *
             atomicSub(&size[from], __popc(mf));
         }
     }
+    if (offs) block_add_u64(deg, &stp->mv_edges);
 }
 
-void p1_apply_movers(Phase1Buffers &b, int sign, int n, cudaStream_t st, int iteration)
+void p1_apply_movers(Phase1Buffers &b, int sign, int n, cudaStream_t st, int iteration, const int64_t *offs,
+                     uint8_t *moved)
 {
+    if (sign < 0) offs = nullptr, moved = nullptr;
     int grid = (n + 255) / 256;
     int cap = num_sms() * 4;
     if (grid > cap) grid = cap;
@@ -1464,10 +1469,10 @@ void p1_apply_movers(Phase1Buffers &b, int sign, int n, cudaStream_t st, int ite
     if (b.wide)
         k_apply_movers<long long><<<grid, 256, 0, st>>>(b.mv_v, b.mv_old, b.mv_new, b.stats, sign, b.comm,
                                                         (long long *)b.Tot, b.size, (const long long *)b.K, nullptr,
-                                                        iteration);
+                                                        iteration, offs, moved);
     else
         k_apply_movers<int><<<grid, 256, 0, st>>>(b.mv_v, b.mv_old, b.mv_new, b.stats, sign, b.comm, b.Tot, b.size,
-                                                  b.K, b.features_on ? b.last_move : nullptr, iteration);
+                                                  b.K, b.features_on ? b.last_move : nullptr, iteration, offs, moved);
     note_launch(1);
 }
 
@@ -1506,6 +1511,9 @@ void p1_tot_reduce(Phase1Buffers &b, int n, cudaStream_t st)
 __global__ void k_iter_reset(DevStats *st, int next, long long min_tot_init)
 {
     st->n_movers = 0;
+    st->mv_edges = 0;
+    st->push_mode = 0;
+    st->push_len = 0;
     st->sum_in = 0;
     st->sum_tot2 = 0;
     st->sum_tot2_hi = 0;
@@ -1572,6 +1580,7 @@ __device__ __forceinline__ PruneScale prune_scale(const UpdateArgs<WT> &a, int v
 template <typename WT, int G, bool W>
 __global__ void __launch_bounds__(256) k_update_group(UpdateArgs<WT> a, const int32_t *__restrict__ list, int count)
 {
+    if (a.st->push_mode) return;  // the incremental update runs instead
     const int lane = threadIdx.x & 31, sub = lane & (G - 1), gw = lane / G;
     constexpr int GPW = 32 / G;
     const int wg = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -1629,6 +1638,7 @@ __global__ void __launch_bounds__(256) k_update_group(UpdateArgs<WT> a, const in
 template <typename WT, bool W>
 __global__ void __launch_bounds__(256) k_update_cta(UpdateArgs<WT> a, const int32_t *__restrict__ list, int count)
 {
+    if (a.st->push_mode) return;  // the incremental update runs instead
     __shared__ WT red[8];
     const long long min_tot = a.st->min_tot;
     unsigned long long s_in = 0, s_edges = 0;
@@ -2044,14 +2054,16 @@ void p1_hub_decide(const LevelGraph &g, Phase1Buffers &b, const HubPlan &p, doub
 // then one thread per hub evaluates the pruning bound.
 // ------------------------------------------------------------------------
 template <typename WT>
-__global__ void k_hub_in_zero(HubPlan p, WT *In)
+__global__ void k_hub_in_zero(HubPlan p, WT *In, const DevStats *st)
 {
+    if (st->push_mode) return;  // the incremental update runs instead
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < p.H; i += gridDim.x * blockDim.x) In[p.hubs[i]] = 0;
 }
 
 template <typename WT, bool W>
 __global__ void __launch_bounds__(256) k_hub_in_partial(UpdateArgs<WT> a, HubPlan p)
 {
+    if (a.st->push_mode) return;  // the incremental update runs instead
     __shared__ WT red[8];
     for (long long wi = blockIdx.x; wi < p.nwork; wi += gridDim.x) {
         const int i = p.work[wi];
@@ -2080,6 +2092,7 @@ __global__ void __launch_bounds__(256) k_hub_in_partial(UpdateArgs<WT> a, HubPla
 template <typename WT>
 __global__ void __launch_bounds__(256) k_hub_in_final(UpdateArgs<WT> a, HubPlan p)
 {
+    if (a.st->push_mode) return;  // the incremental update runs instead
     const long long min_tot = a.st->min_tot;
     unsigned long long s_in = 0, s_edges = 0;
     int s_act = 0;
@@ -2119,7 +2132,7 @@ static void hub_update_t(const LevelGraph &g, Phase1Buffers &b, const HubPlan &p
     UpdateArgs<WT> a = update_args<WT>(g, b, 7, next, bin_start, constant, m2);
     const int cap = num_sms() * 8;
     const int hg = (p.H + 255) / 256;
-    k_hub_in_zero<WT><<<hg, 256, 0, st>>>(p, a.In);
+    k_hub_in_zero<WT><<<hg, 256, 0, st>>>(p, a.In, b.stats);
     const int g1 = (int)(p.nwork < cap ? p.nwork : cap);
     if (g.w)
         k_hub_in_partial<WT, true><<<g1, 256, 0, st>>>(a, p);

@@ -96,7 +96,9 @@ __device__ __forceinline__ void scan_st(unsigned long long *p, unsigned long lon
 
 // status: nb + 2 words, zero on entry; status[nb] is the tile counter.
 // With dlen, the length is min(*dlen, n), read on the device (n bounds the
-// grid): items past it count as 0 and are not written.
+// grid): items past it are not written, tiles wholly past it leave at once
+// (tiles look back only at tiles of lower id, and ids follow launch order),
+// and the tile of the last item writes the total.
 template <typename Tin, typename Tout, typename Op, typename Tlen>
 __global__ void __launch_bounds__(kScanThreads) k_scan_onepass(const Tin *__restrict__ in, Tout *__restrict__ out,
                                                                long long n, Op op, unsigned long long *status, int nb,
@@ -113,6 +115,8 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_onepass(const Tin *__rest
     }
     __syncthreads();
     const int tile = s_tile;
+    const int last_tile = dlen ? (n > 0 ? (int)((n - 1) / kScanTile) : 0) : nb - 1;
+    if (tile > last_tile) return;  // block-uniform
     const long long base = (long long)tile * kScanTile + (long long)threadIdx.x * kScanItems;
     long long v[kScanItems];
     long long s = 0;
@@ -171,7 +175,7 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_onepass(const Tin *__rest
         if (idx < n) out[idx] = (Tout)pre;
         pre += v[i];
     }
-    if (tile == nb - 1 && threadIdx.x == 0 && total_out) *total_out = s_excl + tot;
+    if (tile == last_tile && threadIdx.x == 0 && total_out) *total_out = s_excl + tot;
 }
 
 // Host wrapper: out[i] = sum_{j<i} op(in[j]); *total_out (device) = sum of all.

@@ -28,7 +28,7 @@ EXPORTS = ["gala_last_error", "gala_status_string", "gala_kernel_launch_count", 
            "gala_proposal_clear_samples", "gala_proposal_read_samples", "gala_proposal_gradient",
            "gala_proposal_logits", "gala_proposal_train", "gala_louvain_batch", "gala_generate_sbm_batch",
            "gala_graph_from_csr_f32", "gala_graph_weights_f32", "gala_generate_lfr", "gala_autotune",
-           "gala_context_set_hub_table_cap"]
+           "gala_context_set_hub_table_cap", "gala_context_set_update_mode"]
 
 PROPOSAL_OFF, PROPOSAL_TRACE, PROPOSAL_SKIP = 0, 1, 2
 PROPOSAL_PARAMS = 32 * 8 + 32 + 32 * 32 + 32 + 32 + 1
@@ -80,7 +80,7 @@ class Result(ctypes.Structure):
                 ("kernel_launches", ctypes.c_int64), ("h2d_bytes", ctypes.c_int64),
                 ("d2h_bytes", ctypes.c_int64), ("fp64_decisions", ctypes.c_int64),
                 ("decisions", ctypes.c_int64), ("skipped", ctypes.c_int64), ("verify_sweeps", ctypes.c_int32),
-                ("reserved2", ctypes.c_int32), ("samples", ctypes.c_int64),
+                ("incremental_sweeps", ctypes.c_int32), ("samples", ctypes.c_int64),
                 ("level_vertices", ctypes.c_int32 * GALA_MAX_LEVELS),
                 ("level_entries", ctypes.c_int64 * GALA_MAX_LEVELS),
                 ("level_phase1_ms", ctypes.c_double * GALA_MAX_LEVELS),
@@ -105,7 +105,8 @@ class Result(ctypes.Structure):
              "decide_bytes": self.decide_bytes, "update_bytes": self.update_bytes,
              "kernel_launches": self.kernel_launches, "h2d_bytes": self.h2d_bytes, "d2h_bytes": self.d2h_bytes,
              "fp64_decisions": self.fp64_decisions, "decisions": self.decisions, "skipped": self.skipped,
-             "verify_sweeps": self.verify_sweeps, "samples": self.samples,
+             "verify_sweeps": self.verify_sweeps, "incremental_sweeps": self.incremental_sweeps,
+             "samples": self.samples,
              "host_ms": {"total": self.host_total_ms, "h2d": self.host_h2d_ms, "run": self.host_run_ms,
                          "d2h": self.host_d2h_ms},
              "levels": [{"vertices": self.level_vertices[i], "entries": self.level_entries[i],
@@ -163,6 +164,8 @@ def load(path=LIB_PATH):
     L.gala_context_set_stream.argtypes = [_vp, _vp]
     L.gala_context_set_hub_table_cap.argtypes = [_vp, ctypes.c_int64]
     L.gala_context_set_hub_table_cap.restype = ctypes.c_int
+    L.gala_context_set_update_mode.argtypes = [_vp, ctypes.c_int32]
+    L.gala_context_set_update_mode.restype = ctypes.c_int
     L.gala_graph_pin.argtypes = [_vp]
     L.gala_louvain.argtypes = [_vp, _vp, ctypes.POINTER(Options), _i32p, ctypes.POINTER(Result)]
     L.gala_louvain_device.argtypes = [_vp, ctypes.c_int32, _vp, _vp, _vp, ctypes.POINTER(Options), _vp,
@@ -386,6 +389,11 @@ class Context:
         """Cap every hub's global hash table at `slots` (0 = by degree); for
         tests of the overflow status."""
         _check(load().gala_context_set_hub_table_cap(self.h, slots))
+
+    def set_update_mode(self, mode):
+        """Weight update of the sweeps: 0 = incremental when few rows moved
+        (default), 1 = always full, 2 = incremental whenever allowed."""
+        _check(load().gala_context_set_update_mode(self.h, mode))
 
     def set_stream(self, stream_handle):
         """Order the context's work on a caller CUDA stream (an int handle,

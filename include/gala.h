@@ -166,7 +166,8 @@ typedef struct {
     int64_t skipped;            /* active vertices the network skipped (SKIP) */
     int32_t verify_sweeps;      /* plain sweeps run because a proposal sweep
                                    gained less than min_modularity (SKIP) */
-    int32_t reserved2;
+    int32_t incremental_sweeps; /* sweeps whose weight update was incremental
+                                   (gala_context_set_update_mode) */
     int64_t samples;            /* training samples recorded (TRACE) */
     /* per round: the level graph it ran on, its times and its moves */
     int32_t level_vertices[GALA_MAX_LEVELS];
@@ -286,6 +287,19 @@ gala_status gala_context_set_stream(gala_context *ctx, void *stream);
  * src/louvain_gpu/kernel_functions.cu:217), and the context stays usable.
  * For tests of that error path; no counterpart in the reference. */
 gala_status gala_context_set_hub_table_cap(gala_context *ctx, int64_t slots);
+/* Weight update of the phase-1 sweeps (compute_In / compute_In_blk,
+ * src/louvain_gpu/kernel_functions.cu:890-1034, sums In over every row after
+ * every sweep).  mode 0 (default): on levels of at least 2^23 entries, a
+ * sweep whose movers' rows (like those of the sweep before it) hold under a
+ * third of the level's entries updates In incrementally - each mover's In is
+ * summed again over its row and +-w is pushed from each mover to its
+ * neighbours that did not move - on graphs whose every entry (v, u, w) has a
+ * mirror (u, v, w), checked once per run; mode 1: always the full update;
+ * mode 2: incrementally whenever allowed (symmetric graph, from a level's
+ * second sweep on).  Integer sums: every mode gives the same In, active sets
+ * and results bit for bit.  Plain runs of one graph only; proposal runs and
+ * batches always take the full update. */
+gala_status gala_context_set_update_mode(gala_context *ctx, int32_t mode);
 /* Page-lock the host arrays of g so host<->device copies run at full
  * bandwidth; gala_graph_destroy unpins them.  Needs a CUDA device. */
 gala_status gala_graph_pin(gala_graph *g);
