@@ -57,6 +57,18 @@ struct gala_context {
     int update_mode = 0;
     // symmetry of the current run's graph: -1 = not known yet, 0 / 1
     int sym_state = -1;
+    // gala_louvain of a pinned unweighted graph copies the neighbours in
+    // row-range chunks on copy_stream while level 0 starts on the rows that
+    // arrived (gala_context_set_copy_overlap)
+    int copy_overlap = 4;            // row chunks (0: one copy up front)
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t copy_ev[2] = {};     // start and end of a chunked copy (timing)
+    PendingRows pend_store;
+    PendingRows *pending = nullptr;  // set by gala_louvain, consumed by the first phase 1
+    int32_t *d_chunk = nullptr;      // vstart[kMax + 1], lo[(kMax + 1) x 8], cnt[kMax x 8]
+    int32_t *h_chunk = nullptr;      // page-locked copy of vstart and lo
+    DevStats *d_stats2 = nullptr;    // level-init sums of a level whose rows were still in flight
+    DevStats *h_stats2 = nullptr;
     // per-graph state of gala_louvain_batch, kept between calls (reallocated
     // only for a larger batch)
     BatchRun *batch = nullptr;
@@ -317,22 +329,49 @@ gala_status phase1(gala_context *ctx, const LevelGraph &g, long long &m2, double
     const bool weighted = g.w != nullptr;
     gala_status s;
 
+    // Level-0 rows still being copied (gala_louvain of a pinned unweighted
+    // graph): the level init needs only the offsets, K = Tot = degree, and
+    // the first sweep initialises and decides each degree bin's vertices of a
+    // row chunk as soon as that chunk has arrived.  Other runs wait for the
+    // whole copy first.
+    PendingRows *pend = ctx->pending;
+    ctx->pending = nullptr;
+    if (pend && (bt || pmode != GALA_PROPOSAL_OFF || init || g.w || g.wide || g.ks_ready)) {
+        cudaStreamWaitEvent(st, pend->ev[pend->P - 1], 0);
+        pend = nullptr;
+    }
+    int32_t *const d_vstart = ctx->d_chunk;
+    int32_t *const d_lo = d_vstart + PendingRows::kMax + 1;
+    int32_t *const d_cnt = d_lo + (PendingRows::kMax + 1) * kNumBins;
+    const int32_t *const h_lo = ctx->h_chunk + PendingRows::kMax + 1;
+
     p1_reset_level_stats(b, st);
     p1_level_init(g, b, st);
+    if (pend) {
+        p1_init_degree(g, b, st);
+        memcpy(ctx->h_chunk, pend->vstart, (size_t)(pend->P + 1) * sizeof(int32_t));
+        cudaMemcpyAsync(d_vstart, ctx->h_chunk, (size_t)(pend->P + 1) * sizeof(int32_t), cudaMemcpyHostToDevice, st);
+        p1_chunk_bounds(b, d_vstart, pend->P, d_lo, d_cnt, st);
+        cudaMemcpyAsync(ctx->h_chunk + PendingRows::kMax + 1, d_lo, (size_t)(pend->P + 1) * kNumBins * sizeof(int32_t),
+                        cudaMemcpyDeviceToHost, st);
+        cudaMemsetAsync(ctx->d_stats2, 0, sizeof(DevStats), st);
+    }
     if ((s = check(cudaMemcpyAsync(h, b.stats, sizeof(DevStats), cudaMemcpyDeviceToHost, st), "level init")) ||
         (s = sync_check(st, "level init")))
         return s;
     int bin_start[kNumBinSlots + 1];
     memcpy(bin_start, h->bin_start, sizeof(bin_start));
     const int max_deg = h->max_deg;
-    if (!g.ks_ready) {
+    if (!g.ks_ready && !pend) {
         p1_level_init_rows(g, b, bin_start, st);
         if ((s = check(cudaMemcpyAsync(h, b.stats, sizeof(DevStats), cudaMemcpyDeviceToHost, st), "level rows")) ||
             (s = sync_check(st, "level rows")))
             return s;
     }
     if (m2 == 0) {  // first level: total weight m2 = sum of K (louvain.cu:165-167)
-        m2 = (long long)h->sum_k;
+        // rows in flight: unweighted, so the sum of K is the entry count (the
+        // row kernels' own sum is checked after the first sweep)
+        m2 = pend ? (long long)g.E : (long long)h->sum_k;
         if (m2 <= 0) {
             set_error("graph has no edges (total weight 0)");
             return GALA_ERR_INVALID;
@@ -342,7 +381,7 @@ gala_status phase1(gala_context *ctx, const LevelGraph &g, long long &m2, double
             return GALA_ERR_INVALID;
         }
     }
-    if ((long long)h->sum_k != m2) {
+    if (!pend && (long long)h->sum_k != m2) {
         set_error("level weight %llu differs from total weight %lld", h->sum_k, m2);
         return GALA_ERR_INVALID;
     }
@@ -401,7 +440,7 @@ gala_status phase1(gala_context *ctx, const LevelGraph &g, long long &m2, double
     const bool incr_level = !bt && pmode == GALA_PROPOSAL_OFF && ctx->update_mode != 1;
     if (incr_level) {
         cudaMemsetAsync(b.moved, 0, (size_t)g.n, st);
-        if (ctx->sym_state < 0) ctx->sym_state = (!g.ks_ready && h->sym_hash == 0) ? 1 : 0;
+        if (ctx->sym_state < 0 && !pend) ctx->sym_state = (!g.ks_ready && h->sym_hash == 0) ? 1 : 0;
     }
     b.features_on = pmode != GALA_PROPOSAL_OFF;
     b.wide = g.wide;
@@ -460,9 +499,13 @@ gala_status phase1(gala_context *ctx, const LevelGraph &g, long long &m2, double
             (s = sync_check(st, "start partition")))
             return s;
     }
-    double q = q_from_sums(h->sum_in, h->sum_tot2, m2, h->sum_tot2_hi);
-    if (trace) trace->push_back(q);
-    if (verbose) printf("Iteration:%d Q:%f\n", 0, q);
+    // Q of the singleton partition (with rows in flight: after the first
+    // sweep, from the sums of the row kernels)
+    double q = pend ? 0.0 : q_from_sums(h->sum_in, h->sum_tot2, m2, h->sum_tot2_hi);
+    if (!pend) {
+        if (trace) trace->push_back(q);
+        if (verbose) printf("Iteration:%d Q:%f\n", 0, q);
+    }
     double prev_q = q;
     int iteration = 1;
 
@@ -535,13 +578,47 @@ gala_status phase1(gala_context *ctx, const LevelGraph &g, long long &m2, double
                 }
             }
             fork(ctx);
-            for (int k = 0; k < kNumBins; ++k) {
-                const int bin = kBinLaunchOrder[k];
-                if (bin == 7)
-                    p1_hub_decide(g, b, hp, constant, m2, fp64_only, aux_for(ctx, k));
-                else
-                    p1_decide(g, b, bin, lists + bin_start[bin], counts + bin, level_cnt[bin], constant, m2,
-                              fp64_only, iteration == 1 && g.distinct && !init, aux_for(ctx, k));
+            if (pend && iteration == 1) {
+                // rows in flight: per chunk and bin, the init rows and the
+                // first sweep of the bin's vertices in that chunk; hubs after
+                // the last chunk
+                const cudaEvent_t last = pend->ev[pend->P - 1];
+                for (int c = 0; c < pend->P; ++c)
+                    for (int k = 0; k < kNumBins; ++k) {
+                        const int bin = kBinLaunchOrder[k];
+                        if (bin == 7) continue;
+                        const int lo = h_lo[c * kNumBins + bin], cnt = h_lo[(c + 1) * kNumBins + bin] - lo;
+                        if (cnt <= 0) continue;
+                        cudaStream_t sb = aux_for(ctx, k);
+                        cudaStreamWaitEvent(sb, pend->ev[c], 0);
+                        const int32_t *lst = b.order + bin_start[bin] + lo;
+                        p1_init_rows_range(g, b, bin, lst, cnt, ctx->d_stats2, sb);
+                        p1_decide(g, b, bin, lst, d_cnt + c * kNumBins + bin, cnt, constant, m2, fp64_only,
+                                  g.distinct, sb);
+                    }
+                // hubs (few, long rows) once the chunk with the last of them
+                // has arrived
+                int hub_chunk = -1;
+                for (int c = 0; c < pend->P; ++c)
+                    if (h_lo[(c + 1) * kNumBins + 7] > h_lo[c * kNumBins + 7]) hub_chunk = c;
+                for (int k = 0; k < kNumBins; ++k) {
+                    if (kBinLaunchOrder[k] == 7 && hub_chunk >= 0) {
+                        cudaStreamWaitEvent(aux_for(ctx, k), pend->ev[hub_chunk], 0);
+                        p1_init_rows_range(g, b, 7, b.order + bin_start[7], level_cnt[7], ctx->d_stats2,
+                                           aux_for(ctx, k));
+                        p1_hub_decide(g, b, hp, constant, m2, fp64_only, aux_for(ctx, k));
+                    }
+                }
+                for (int k = 0; k < kNumBins; ++k) cudaStreamWaitEvent(aux_for(ctx, k), last, 0);
+            } else {
+                for (int k = 0; k < kNumBins; ++k) {
+                    const int bin = kBinLaunchOrder[k];
+                    if (bin == 7)
+                        p1_hub_decide(g, b, hp, constant, m2, fp64_only, aux_for(ctx, k));
+                    else
+                        p1_decide(g, b, bin, lists + bin_start[bin], counts + bin, level_cnt[bin], constant, m2,
+                                  fp64_only, iteration == 1 && g.distinct && !init, aux_for(ctx, k));
+                }
             }
             join(ctx);
             rec(ctx->ev[3]);
@@ -575,6 +652,8 @@ gala_status phase1(gala_context *ctx, const LevelGraph &g, long long &m2, double
             }
             rec(ctx->ev[5]);
             cudaMemcpyAsync(h, b.stats, sizeof(DevStats), cudaMemcpyDeviceToHost, st);
+            if (pend && iteration == 1)
+                cudaMemcpyAsync(ctx->h_stats2, ctx->d_stats2, sizeof(DevStats), cudaMemcpyDeviceToHost, st);
         };
         if (graphs && iteration > 1) {
             // sweeps after the first repeat the same launches with the active
@@ -602,6 +681,17 @@ gala_status phase1(gala_context *ctx, const LevelGraph &g, long long &m2, double
         if (h->err) {
             set_error("phase 1: device error bits %d", h->err);
             return GALA_ERR_OVERFLOW;
+        }
+        if (pend && iteration == 1) {  // the level init's sums, from the row kernels of the first sweep
+            const DevStats *h2 = ctx->h_stats2;
+            if ((long long)h2->sum_k != m2) {
+                set_error("level weight %llu differs from total weight %lld", h2->sum_k, m2);
+                return GALA_ERR_INVALID;
+            }
+            prev_q = q_from_sums(h2->sum_in, h2->sum_tot2, m2, h2->sum_tot2_hi);
+            if (trace) trace->push_back(prev_q);
+            if (verbose) printf("Iteration:%d Q:%f\n", 0, prev_q);
+            if (incr_level && ctx->sym_state < 0) ctx->sym_state = h2->sym_hash == 0 ? 1 : 0;
         }
         long long dec_nv = act_nv, dec_ne = act_ne;
         if (proposal_sweep) {
@@ -1090,6 +1180,16 @@ void gala_context_destroy(gala_context *ctx)
         if (ctx->join_ev[i]) cudaEventDestroy(ctx->join_ev[i]);
     }
     if (ctx->fork_ev) cudaEventDestroy(ctx->fork_ev);
+    for (auto &e : ctx->pend_store.ev)
+        if (e) cudaEventDestroy(e);
+    if (ctx->copy_stream) {
+        cudaStreamSynchronize(ctx->copy_stream);
+        cudaStreamDestroy(ctx->copy_stream);
+    }
+    for (auto &e : ctx->copy_ev)
+        if (e) cudaEventDestroy(e);
+    if (ctx->h_chunk) cudaFreeHost(ctx->h_chunk);
+    if (ctx->h_stats2) cudaFreeHost(ctx->h_stats2);
     if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
     cudaSetDevice(prev);
     delete ctx;
@@ -1134,6 +1234,13 @@ gala_status gala_context_create(int32_t device, int32_t max_vertices, int64_t ma
         ok = ok && cudaEventCreateWithFlags(&ctx->join_ev[i], cudaEventDisableTiming) == cudaSuccess;
     }
     ok = ok && cudaMallocHost(&ctx->h_stats, sizeof(DevStats)) == cudaSuccess;
+    ok = ok && cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking) == cudaSuccess;
+    for (auto &e : ctx->copy_ev) ok = ok && cudaEventCreate(&e) == cudaSuccess;
+    for (auto &e : ctx->pend_store.ev) ok = ok && cudaEventCreateWithFlags(&e, cudaEventDisableTiming) == cudaSuccess;
+    constexpr int kChunkInts = (PendingRows::kMax + 1) + (PendingRows::kMax + 1) * kNumBins + PendingRows::kMax * kNumBins;
+    ok = ok && cudaMallocHost(&ctx->h_chunk, kChunkInts * sizeof(int32_t)) == cudaSuccess;
+    ok = ok && cudaMallocHost(&ctx->h_stats2, sizeof(DevStats)) == cudaSuccess;
+    ok = ok && dalloc(ctx, &ctx->d_chunk, kChunkInts) && dalloc(ctx, &ctx->d_stats2, 1);
     for (int i = 0; i < 2 && ok; ++i)
         ok = dalloc(ctx, &ctx->offs[i], n + 1) && dalloc(ctx, &ctx->nbr[i], E) && dalloc8(ctx, &ctx->w[i], E);
     Phase1Buffers &b = ctx->p1;
@@ -1223,6 +1330,17 @@ gala_status gala_context_set_hub_table_cap(gala_context *ctx, int64_t slots)
     return GALA_OK;
 }
 
+gala_status gala_context_set_copy_overlap(gala_context *ctx, int32_t chunks)
+{
+    clear_error();
+    if (!ctx || chunks < 0 || chunks == 1 || chunks > PendingRows::kMax) {
+        set_error("gala_context_set_copy_overlap: chunks must be 0 or 2..%d", PendingRows::kMax);
+        return GALA_ERR_INVALID;
+    }
+    ctx->copy_overlap = chunks;
+    return GALA_OK;
+}
+
 gala_status gala_context_set_update_mode(gala_context *ctx, int32_t mode)
 {
     clear_error();
@@ -1297,7 +1415,35 @@ gala_status gala_louvain(gala_context *ctx, const gala_graph *g, const gala_opti
     cudaEventRecord(ctx->ev[6], st);
     cudaMemsetAsync(ctx->offs[1], 0, sizeof(int64_t), st);
     cudaMemcpyAsync(ctx->offs[1] + 1, g->offs.data(), (size_t)n * sizeof(int64_t), cudaMemcpyHostToDevice, st);
-    cudaMemcpyAsync(ctx->nbr[1], g->nbr.data(), (size_t)E * sizeof(int32_t), cudaMemcpyHostToDevice, st);
+    // a pinned unweighted graph: the neighbours go in row-range chunks of
+    // about equal entries on the copy stream, and level 0 starts on the rows
+    // that arrived (phase 1 consumes ctx->pending); otherwise one copy
+    const bool chunked = ctx->copy_overlap >= 2 && g->pinned && !g->weighted && !g->float_w && E >= (1LL << 22);
+    if (chunked) {
+        PendingRows &pr = ctx->pend_store;
+        pr.P = ctx->copy_overlap;
+        pr.vstart[0] = 0;
+        pr.vstart[pr.P] = n;
+        for (int k = 1; k < pr.P; ++k) {  // rows that end at or before k E / P
+            const int64_t target = E / pr.P * k;
+            pr.vstart[k] = (int32_t)(std::upper_bound(g->offs.begin(), g->offs.end(), target) - g->offs.begin());
+            if (pr.vstart[k] < pr.vstart[k - 1]) pr.vstart[k] = pr.vstart[k - 1];
+        }
+        cudaStreamWaitEvent(ctx->copy_stream, ctx->ev[6], 0);  // after earlier work on the level buffers
+        cudaEventRecord(ctx->copy_ev[0], ctx->copy_stream);
+        for (int k = 0; k < pr.P; ++k) {
+            const int64_t e0 = pr.vstart[k] ? g->offs[pr.vstart[k] - 1] : 0;
+            const int64_t e1 = pr.vstart[k + 1] ? g->offs[pr.vstart[k + 1] - 1] : 0;
+            if (e1 > e0)
+                cudaMemcpyAsync(ctx->nbr[1] + e0, g->nbr.data() + e0, (size_t)(e1 - e0) * sizeof(int32_t),
+                                cudaMemcpyHostToDevice, ctx->copy_stream);
+            cudaEventRecord(pr.ev[k], ctx->copy_stream);
+        }
+        cudaEventRecord(ctx->copy_ev[1], ctx->copy_stream);
+        ctx->pending = &pr;
+    } else {
+        cudaMemcpyAsync(ctx->nbr[1], g->nbr.data(), (size_t)E * sizeof(int32_t), cudaMemcpyHostToDevice, st);
+    }
     const void *dw = nullptr;
     if (g->weighted) {
         cudaMemcpyAsync(ctx->w[1], g->w.data(), (size_t)E * sizeof(int32_t), cudaMemcpyHostToDevice, st);
@@ -1308,15 +1454,25 @@ gala_status gala_louvain(gala_context *ctx, const gala_graph *g, const gala_opti
         fixed_from_f32((const float *)ctx->w[0], (long long *)ctx->w[1], E, g->fixed_shift, st);
         dw = ctx->w[1];
     }
-    cudaEventRecord(ctx->ev[7], st);
-    if ((s = sync_check(st, "host to device copy"))) {
-        if (own) gala_context_destroy(own);
-        return s;
+    float h2d = 0;
+    if (!chunked) {
+        cudaEventRecord(ctx->ev[7], st);
+        if ((s = sync_check(st, "host to device copy"))) {
+            if (own) gala_context_destroy(own);
+            return s;
+        }
+        h2d = ev_ms(ctx->ev[6], ctx->ev[7]);
     }
-    float h2d = ev_ms(ctx->ev[6], ctx->ev[7]);
     const double t_h2d = host_ms();
     // level 0 lives in buffer 1; the first contraction writes buffer 0
     s = run_levels(ctx, n, E, ctx->offs[1], ctx->nbr[1], dw, opt, res, nullptr, g->float_w, g->rows_distinct);
+    if (chunked) {  // the copy has ended (phase 1 waited for it); also when a run stopped early
+        ctx->pending = nullptr;
+        cudaStreamWaitEvent(st, ctx->copy_ev[1], 0);
+        gala_status s2 = sync_check(st, "host to device copy");
+        if (s == GALA_OK) s = s2;
+        h2d = ev_ms(ctx->copy_ev[0], ctx->copy_ev[1]);
+    }
     const double t_run = host_ms();
     if (s == GALA_OK) {
         cudaEventRecord(ctx->ev[6], st);

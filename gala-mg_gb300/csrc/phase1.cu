@@ -326,9 +326,10 @@ void p1_reset_level_stats(Phase1Buffers &b, cudaStream_t st)
 
 template <typename WT>
 static void launch_init_rows(const LevelGraph &g, Phase1Buffers &b, int bin, const int32_t *list, int cnt,
-                             cudaStream_t st)
+                             cudaStream_t st, DevStats *stats = nullptr)
 {
     if (cnt <= 0) return;
+    if (!stats) stats = b.stats;
     const bool W = g.w != nullptr;
     const WT *w = (const WT *)g.w;
     WT *K = (WT *)b.K, *Self = (WT *)b.Self, *Tot = (WT *)b.Tot, *In = (WT *)b.In;
@@ -341,10 +342,10 @@ static void launch_init_rows(const LevelGraph &g, Phase1Buffers &b, int bin, con
     do {                                                                                                 \
         if (W)                                                                                           \
             k_init_rows_group<WT, GV, true><<<grid_for(GV), 256, 0, st>>>(list, cnt, g.offs, g.nbr, w, K,  \
-                                                                          Self, Tot, In, b.stats);       \
+                                                                          Self, Tot, In, stats);         \
         else                                                                                             \
             k_init_rows_group<WT, GV, false><<<grid_for(GV), 256, 0, st>>>(list, cnt, g.offs, g.nbr, w, K, \
-                                                                           Self, Tot, In, b.stats);      \
+                                                                           Self, Tot, In, stats);        \
     } while (0)
     switch (bin) {
     case 0: GALA_INIT_GROUP(4); break;
@@ -356,9 +357,9 @@ static void launch_init_rows(const LevelGraph &g, Phase1Buffers &b, int bin, con
     default: {
         int grid = cnt < cap ? cnt : cap;
         if (W)
-            k_init_rows_cta<WT, true><<<grid, 256, 0, st>>>(list, cnt, g.offs, g.nbr, w, K, Self, Tot, In, b.stats);
+            k_init_rows_cta<WT, true><<<grid, 256, 0, st>>>(list, cnt, g.offs, g.nbr, w, K, Self, Tot, In, stats);
         else
-            k_init_rows_cta<WT, false><<<grid, 256, 0, st>>>(list, cnt, g.offs, g.nbr, w, K, Self, Tot, In, b.stats);
+            k_init_rows_cta<WT, false><<<grid, 256, 0, st>>>(list, cnt, g.offs, g.nbr, w, K, Self, Tot, In, stats);
     }
     }
 #undef GALA_INIT_GROUP
@@ -388,6 +389,65 @@ void p1_level_init(const LevelGraph &g, Phase1Buffers &b, cudaStream_t st)
                    &b.stats->total, st, &b.stats->err);
     k_bin_scatter<<<nblk, kCountBlock, 0, st>>>(n, g.offs, b.blockoff, nblk, b.order, b.stats, b.lim);
     note_launch(3);
+}
+
+// Unweighted level whose rows are still being copied: K = Tot = degree of
+// every vertex from the offsets alone, so a vertex's first sweep needs only
+// its own row.
+__global__ void k_init_degree(int n, const int64_t *__restrict__ offs, int32_t *K, int32_t *Tot)
+{
+    for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) {
+        const int d = (int)(offs[v + 1] - offs[v]);
+        K[v] = d;
+        Tot[v] = d;
+    }
+}
+
+// Sub-ranges of the degree bins per row chunk: lo[k][bin] = first position in
+// the bin's segment of the order list (ascending ids within a bin) of a vertex
+// id >= vstart[k]; cnt[k][bin] = lo[k + 1][bin] - lo[k][bin].
+__global__ void k_chunk_bounds(const int32_t *__restrict__ order, const DevStats *__restrict__ st,
+                               const int32_t *__restrict__ vstart, int P, int32_t *lo, int32_t *cnt)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (P + 1) * kNumBins) return;
+    const int k = t / kNumBins, bin = t % kNumBins;
+    const int bs = st->bin_start[bin], be = st->bin_start[bin + 1];
+    auto first_ge = [&](int id) {
+        int l = bs, h = be;  // first position in [bs, be) with order >= id
+        while (l < h) {
+            const int m = (l + h) >> 1;
+            if (order[m] < id) l = m + 1;
+            else h = m;
+        }
+        return l - bs;
+    };
+    const int a = k < P ? first_ge(vstart[k]) : be - bs;
+    lo[k * kNumBins + bin] = a;
+    if (k < P) cnt[k * kNumBins + bin] = (k + 1 < P ? first_ge(vstart[k + 1]) : be - bs) - a;
+}
+
+void p1_init_degree(const LevelGraph &g, Phase1Buffers &b, cudaStream_t st)
+{
+    const int grid = std::min((g.n + 255) / 256, num_sms() * 8);
+    k_init_degree<<<grid > 0 ? grid : 1, 256, 0, st>>>(g.n, g.offs, b.K, b.Tot);
+    note_launch(1);
+}
+
+void p1_chunk_bounds(Phase1Buffers &b, const int32_t *d_vstart, int P, int32_t *d_lo, int32_t *d_cnt, cudaStream_t st)
+{
+    const int t = (P + 1) * kNumBins;
+    k_chunk_bounds<<<(t + 127) / 128, 128, 0, st>>>(b.order, b.stats, d_vstart, P, d_lo, d_cnt);
+    note_launch(1);
+}
+
+void p1_init_rows_range(const LevelGraph &g, Phase1Buffers &b, int bin, const int32_t *list, int cnt, DevStats *stats,
+                        cudaStream_t st)
+{
+    if (g.wide)
+        launch_init_rows<long long>(g, b, bin, list, cnt, st, stats);
+    else
+        launch_init_rows<int>(g, b, bin, list, cnt, st, stats);
 }
 
 void p1_level_init_rows(const LevelGraph &g, Phase1Buffers &b, const int *bin_start, cudaStream_t st)

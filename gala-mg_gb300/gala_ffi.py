@@ -28,7 +28,7 @@ EXPORTS = ["gala_last_error", "gala_status_string", "gala_kernel_launch_count", 
            "gala_proposal_clear_samples", "gala_proposal_read_samples", "gala_proposal_gradient",
            "gala_proposal_logits", "gala_proposal_train", "gala_louvain_batch", "gala_generate_sbm_batch",
            "gala_graph_from_csr_f32", "gala_graph_weights_f32", "gala_generate_lfr", "gala_autotune",
-           "gala_context_set_hub_table_cap", "gala_context_set_update_mode"]
+           "gala_context_set_hub_table_cap", "gala_context_set_update_mode", "gala_context_set_copy_overlap"]
 
 PROPOSAL_OFF, PROPOSAL_TRACE, PROPOSAL_SKIP = 0, 1, 2
 PROPOSAL_PARAMS = 32 * 8 + 32 + 32 * 32 + 32 + 32 + 1
@@ -166,6 +166,8 @@ def load(path=LIB_PATH):
     L.gala_context_set_hub_table_cap.restype = ctypes.c_int
     L.gala_context_set_update_mode.argtypes = [_vp, ctypes.c_int32]
     L.gala_context_set_update_mode.restype = ctypes.c_int
+    L.gala_context_set_copy_overlap.argtypes = [_vp, ctypes.c_int32]
+    L.gala_context_set_copy_overlap.restype = ctypes.c_int
     L.gala_graph_pin.argtypes = [_vp]
     L.gala_louvain.argtypes = [_vp, _vp, ctypes.POINTER(Options), _i32p, ctypes.POINTER(Result)]
     L.gala_louvain_device.argtypes = [_vp, ctypes.c_int32, _vp, _vp, _vp, ctypes.POINTER(Options), _vp,
@@ -394,6 +396,14 @@ class Context:
         """Weight update of the sweeps: 0 = incremental when few rows moved
         (default), 1 = always full, 2 = incremental whenever allowed."""
         _check(load().gala_context_set_update_mode(self.h, mode))
+
+    def set_copy_overlap(self, chunks):
+        """gala_louvain of a pinned unweighted graph: copy the neighbours in
+        `chunks` row chunks overlapped with the first sweep (4, the default;
+        True = 4, False or 0 = one copy up front)."""
+        if chunks is True:
+            chunks = 4
+        _check(load().gala_context_set_copy_overlap(self.h, int(chunks)))
 
     def set_stream(self, stream_handle):
         """Order the context's work on a caller CUDA stream (an int handle,
