@@ -60,9 +60,10 @@ struct gala_context {
     // gala_louvain of a pinned unweighted graph copies the neighbours in
     // row-range chunks on copy_stream while level 0 starts on the rows that
     // arrived (gala_context_set_copy_overlap)
-    int copy_overlap = 4;            // row chunks (0: one copy up front)
+    int copy_overlap = 8;            // row chunks (0: one copy up front)
     cudaStream_t copy_stream = nullptr;
     cudaEvent_t copy_ev[2] = {};     // start and end of a chunked copy (timing)
+    cudaEvent_t offs_ev = nullptr;   // the offsets have been copied
     PendingRows pend_store;
     PendingRows *pending = nullptr;  // set by gala_louvain, consumed by the first phase 1
     int32_t *d_chunk = nullptr;      // vstart[kMax + 1], lo[(kMax + 1) x 8], cnt[kMax x 8]
@@ -349,9 +350,10 @@ gala_status phase1(gala_context *ctx, const LevelGraph &g, long long &m2, double
     p1_level_init(g, b, st);
     if (pend) {
         p1_init_degree(g, b, st);
-        memcpy(ctx->h_chunk, pend->vstart, (size_t)(pend->P + 1) * sizeof(int32_t));
-        cudaMemcpyAsync(d_vstart, ctx->h_chunk, (size_t)(pend->P + 1) * sizeof(int32_t), cudaMemcpyHostToDevice, st);
-        p1_chunk_bounds(b, d_vstart, pend->P, d_lo, d_cnt, st);
+        ChunkStarts vs{};
+        static_assert(sizeof(vs.v) / sizeof(vs.v[0]) == PendingRows::kMax + 1, "chunk starts");
+        memcpy(vs.v, pend->vstart, (size_t)(pend->P + 1) * sizeof(int32_t));
+        p1_chunk_bounds(b, vs, pend->P, d_lo, d_cnt, st);
         cudaMemcpyAsync(ctx->h_chunk + PendingRows::kMax + 1, d_lo, (size_t)(pend->P + 1) * kNumBins * sizeof(int32_t),
                         cudaMemcpyDeviceToHost, st);
         cudaMemsetAsync(ctx->d_stats2, 0, sizeof(DevStats), st);
@@ -1188,6 +1190,7 @@ void gala_context_destroy(gala_context *ctx)
     }
     for (auto &e : ctx->copy_ev)
         if (e) cudaEventDestroy(e);
+    if (ctx->offs_ev) cudaEventDestroy(ctx->offs_ev);
     if (ctx->h_chunk) cudaFreeHost(ctx->h_chunk);
     if (ctx->h_stats2) cudaFreeHost(ctx->h_stats2);
     if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
@@ -1236,6 +1239,7 @@ gala_status gala_context_create(int32_t device, int32_t max_vertices, int64_t ma
     ok = ok && cudaMallocHost(&ctx->h_stats, sizeof(DevStats)) == cudaSuccess;
     ok = ok && cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking) == cudaSuccess;
     for (auto &e : ctx->copy_ev) ok = ok && cudaEventCreate(&e) == cudaSuccess;
+    ok = ok && cudaEventCreateWithFlags(&ctx->offs_ev, cudaEventDisableTiming) == cudaSuccess;
     for (auto &e : ctx->pend_store.ev) ok = ok && cudaEventCreateWithFlags(&e, cudaEventDisableTiming) == cudaSuccess;
     constexpr int kChunkInts = (PendingRows::kMax + 1) + (PendingRows::kMax + 1) * kNumBins + PendingRows::kMax * kNumBins;
     ok = ok && cudaMallocHost(&ctx->h_chunk, kChunkInts * sizeof(int32_t)) == cudaSuccess;
@@ -1411,14 +1415,15 @@ gala_status gala_louvain(gala_context *ctx, const gala_graph *g, const gala_opti
     auto host_ms = [&]() {
         return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - host0).count();
     };
-    // host -> device: offsets with a leading 0, neighbours, weights
-    cudaEventRecord(ctx->ev[6], st);
-    cudaMemsetAsync(ctx->offs[1], 0, sizeof(int64_t), st);
-    cudaMemcpyAsync(ctx->offs[1] + 1, g->offs.data(), (size_t)n * sizeof(int64_t), cudaMemcpyHostToDevice, st);
     // a pinned unweighted graph: the neighbours go in row-range chunks of
     // about equal entries on the copy stream, and level 0 starts on the rows
     // that arrived (phase 1 consumes ctx->pending); otherwise one copy
     const bool chunked = ctx->copy_overlap >= 2 && g->pinned && !g->weighted && !g->float_w && E >= (1LL << 22);
+    // host -> device: offsets with a leading 0, neighbours, weights
+    cudaEventRecord(ctx->ev[6], st);
+    if (chunked) cudaEventRecord(ctx->copy_ev[0], st);
+    cudaMemsetAsync(ctx->offs[1], 0, sizeof(int64_t), st);
+    cudaMemcpyAsync(ctx->offs[1] + 1, g->offs.data(), (size_t)n * sizeof(int64_t), cudaMemcpyHostToDevice, st);
     if (chunked) {
         PendingRows &pr = ctx->pend_store;
         pr.P = ctx->copy_overlap;
@@ -1429,8 +1434,11 @@ gala_status gala_louvain(gala_context *ctx, const gala_graph *g, const gala_opti
             pr.vstart[k] = (int32_t)(std::upper_bound(g->offs.begin(), g->offs.end(), target) - g->offs.begin());
             if (pr.vstart[k] < pr.vstart[k - 1]) pr.vstart[k] = pr.vstart[k - 1];
         }
-        cudaStreamWaitEvent(ctx->copy_stream, ctx->ev[6], 0);  // after earlier work on the level buffers
-        cudaEventRecord(ctx->copy_ev[0], ctx->copy_stream);
+        // after the offsets (which the level init needs first: copies that
+        // share the host link would otherwise finish together) and after
+        // earlier work on the level buffers
+        cudaEventRecord(ctx->offs_ev, st);
+        cudaStreamWaitEvent(ctx->copy_stream, ctx->offs_ev, 0);
         for (int k = 0; k < pr.P; ++k) {
             const int64_t e0 = pr.vstart[k] ? g->offs[pr.vstart[k] - 1] : 0;
             const int64_t e1 = pr.vstart[k + 1] ? g->offs[pr.vstart[k + 1] - 1] : 0;

@@ -175,15 +175,20 @@ void p1_level_init_rows(const LevelGraph &g, Phase1Buffers &b, const int *bin_st
 // Level-0 rows still in flight (unweighted graphs): K = Tot = degree from the
 // offsets; per row chunk k and bin, the bin's sub-range of the order list
 // (d_lo[(P + 1) x 8], d_cnt[P x 8]); init rows of one sub-range into `stats`.
+// (The chunk starts go as a kernel argument: a small copy to the device would
+// queue behind the chunks themselves.)
+struct ChunkStarts {
+    int32_t v[17];
+};
 void p1_init_degree(const LevelGraph &g, Phase1Buffers &b, cudaStream_t st);
-void p1_chunk_bounds(Phase1Buffers &b, const int32_t *d_vstart, int P, int32_t *d_lo, int32_t *d_cnt, cudaStream_t st);
+void p1_chunk_bounds(Phase1Buffers &b, const ChunkStarts &vs, int P, int32_t *d_lo, int32_t *d_cnt, cudaStream_t st);
 void p1_init_rows_range(const LevelGraph &g, Phase1Buffers &b, int bin, const int32_t *list, int cnt, DevStats *stats,
                         cudaStream_t st);
 // Neighbour arrays of a level-0 graph still being copied: row-range chunks on
 // another stream, one event per chunk (chunk k holds the rows of vertices
 // [vstart[k], vstart[k + 1])).
 struct PendingRows {
-    static constexpr int kMax = 16;
+    static constexpr int kMax = 16;  // ChunkStarts holds kMax + 1 starts
     int P = 0;
     int32_t vstart[kMax + 1] = {};
     cudaEvent_t ev[kMax] = {};

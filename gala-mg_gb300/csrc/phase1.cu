@@ -406,9 +406,10 @@ __global__ void k_init_degree(int n, const int64_t *__restrict__ offs, int32_t *
 // Sub-ranges of the degree bins per row chunk: lo[k][bin] = first position in
 // the bin's segment of the order list (ascending ids within a bin) of a vertex
 // id >= vstart[k]; cnt[k][bin] = lo[k + 1][bin] - lo[k][bin].
-__global__ void k_chunk_bounds(const int32_t *__restrict__ order, const DevStats *__restrict__ st,
-                               const int32_t *__restrict__ vstart, int P, int32_t *lo, int32_t *cnt)
+__global__ void k_chunk_bounds(const int32_t *__restrict__ order, const DevStats *__restrict__ st, ChunkStarts vs,
+                               int P, int32_t *lo, int32_t *cnt)
 {
+    const int32_t *vstart = vs.v;
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= (P + 1) * kNumBins) return;
     const int k = t / kNumBins, bin = t % kNumBins;
@@ -434,10 +435,10 @@ void p1_init_degree(const LevelGraph &g, Phase1Buffers &b, cudaStream_t st)
     note_launch(1);
 }
 
-void p1_chunk_bounds(Phase1Buffers &b, const int32_t *d_vstart, int P, int32_t *d_lo, int32_t *d_cnt, cudaStream_t st)
+void p1_chunk_bounds(Phase1Buffers &b, const ChunkStarts &vs, int P, int32_t *d_lo, int32_t *d_cnt, cudaStream_t st)
 {
     const int t = (P + 1) * kNumBins;
-    k_chunk_bounds<<<(t + 127) / 128, 128, 0, st>>>(b.order, b.stats, d_vstart, P, d_lo, d_cnt);
+    k_chunk_bounds<<<(t + 127) / 128, 128, 0, st>>>(b.order, b.stats, vs, P, d_lo, d_cnt);
     note_launch(1);
 }
 

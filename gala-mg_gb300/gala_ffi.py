@@ -399,10 +399,10 @@ class Context:
 
     def set_copy_overlap(self, chunks):
         """gala_louvain of a pinned unweighted graph: copy the neighbours in
-        `chunks` row chunks overlapped with the first sweep (4, the default;
-        True = 4, False or 0 = one copy up front)."""
+        `chunks` row chunks overlapped with the first sweep (8, the default;
+        True = 8, False or 0 = one copy up front)."""
         if chunks is True:
-            chunks = 4
+            chunks = 8
         _check(load().gala_context_set_copy_overlap(self.h, int(chunks)))
 
     def set_stream(self, stream_handle):

@@ -300,7 +300,7 @@ gala_status gala_context_set_hub_table_cap(gala_context *ctx, int64_t slots);
  * and results bit for bit.  Plain runs of one graph only; proposal runs and
  * batches always take the full update. */
 gala_status gala_context_set_update_mode(gala_context *ctx, int32_t mode);
-/* Host -> device copy of gala_louvain: with chunks = 2..16 (4 by default) a
+/* Host -> device copy of gala_louvain: with chunks = 2..16 (8 by default) a
  * page-locked (gala_graph_pin) unweighted graph of at least 2^22 entries has
  * its neighbour array copied in that many row-range chunks on a second
  * stream, and the first sweep of level 0 initialises and decides the
