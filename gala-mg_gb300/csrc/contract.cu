@@ -94,20 +94,42 @@ __global__ void k_nz_tail(DevStats *st, long long *nz_offs, long long E, const l
     nz_offs[cnt] = dE ? *dE : E;
 }
 
-// rows [0, n), or [0, min(n, *dn)) when dn is set
+// Rows [0, n), or [0, min(n, *dn)) when dn is set.  Besides the row and its
+// first entry, every listed row gets the value its walk kernel adds to an
+// entry index (nz_shift, from shift(row, first entry)), and every 1024-entry
+// task its first row (task_row): a walk then loads one coalesced value per
+// row and starts its tasks without a search.
+template <typename Shift>
 __global__ void k_nz_scatter(const int64_t *__restrict__ offs, int n, const int32_t *__restrict__ pos,
-                             int32_t *nz_rows, long long *nz_offs, const long long *dn)
+                             int32_t *nz_rows, long long *nz_offs, long long *nz_shift, int32_t *task_row,
+                             const long long *dn, Shift shift)
 {
     if (dn && *dn < n) n = (int)*dn;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const long long s = offs[i];
-        if (offs[i + 1] > s) {
+        const long long s = offs[i], e = offs[i + 1];
+        if (e > s) {
             const int p = pos[i];
             nz_rows[p] = i;
             nz_offs[p] = s;
+            nz_shift[p] = shift(i, s);
+            for (long long t = (s + kRangeEntries - 1) / kRangeEntries; t * kRangeEntries < e; ++t)
+                task_row[t] = p;
         }
     }
 }
+
+// Shifts of the two walks: the stream fill writes entry j of vertex v's row
+// to medge[mpos[v]] + (j - offs[v]); the compaction reads entry j of
+// community c's new row from tmp_off[c] + (j - new_offs[c]).
+struct ShiftStream {
+    const int32_t *__restrict__ mpos;
+    const long long *__restrict__ medge;
+    __device__ __forceinline__ long long operator()(int v, long long s) const { return medge[mpos[v]] - s; }
+};
+struct ShiftCompact {
+    const long long *__restrict__ tmp_off;
+    __device__ __forceinline__ long long operator()(int c, long long s) const { return tmp_off[c] - s; }
+};
 
 // Caller-supplied labels must lie in [0, n) before they index any array.
 __global__ void k_check_labels(const int32_t *__restrict__ comm, int n, DevStats *st)
@@ -174,23 +196,20 @@ __global__ void k_member_scatter(const int32_t *__restrict__ lab, const int64_t 
 // list of rows with entries (nz_rows / nz_offs); each row's destination
 // (medge[mpos[v]] - offs[v]) is loaded once per row window.
 template <typename WT, bool W>
-__global__ void __launch_bounds__(256) k_stream_fill(int n, long long E, const int64_t *__restrict__ offs,
-                                                     const int32_t *__restrict__ nbr, const WT *__restrict__ w,
-                                                     const int32_t *__restrict__ lab,
-                                                     const int32_t *__restrict__ mpos,
-                                                     const long long *__restrict__ medge, int32_t *skey, WT *sw,
-                                                     const int32_t *__restrict__ nz_rows,
-                                                     const long long *__restrict__ nz_offs, DevStats *st)
+__global__ void __launch_bounds__(256) k_stream_fill(long long E, const int32_t *__restrict__ nbr,
+                                                     const WT *__restrict__ w, const int32_t *__restrict__ lab,
+                                                     int32_t *skey, WT *sw,
+                                                     const long long *__restrict__ nz_offs,
+                                                     const long long *__restrict__ nz_shift,
+                                                     const int32_t *__restrict__ task_row, DevStats *st)
 {
     const long long wg = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
     const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
     const int nnz = st->nz_rows;
-    // per row: pa = destination of the row's entry j minus j, pb = 1 when the
-    // row id is valid
+    // per row: pa = destination of the row's entry j minus j, pb = 1 (rows
+    // past the list keep pb = 0)
     auto rowval = [=](int r, long long &pa, long long &pb) {
-        const int v = nz_rows[r];
-        if (v < 0 || v >= n) return;
-        pa = medge[mpos[v]] - offs[v];
+        pa = nz_shift[r];
         pb = 1;
     };
     constexpr int U = kWalkUnroll;
@@ -199,7 +218,7 @@ __global__ void __launch_bounds__(256) k_stream_fill(int n, long long E, const i
     for (long long t = wg; t * kRangeEntries < E; t += nw) {
         const long long j0 = t * kRangeEntries;
         const long long j1 = j0 + kRangeEntries < E ? j0 + kRangeEntries : E;
-        cur.start(j0);
+        cur.start_row(task_row[t]);
         for (long long jb = j0; jb < j1; jb += 32 * U) {
             long long src[U], dst[U];
             bool ok[U];
@@ -1022,7 +1041,9 @@ __global__ void __launch_bounds__(256) k_compact(const int64_t *__restrict__ new
                                                  const int32_t *__restrict__ tmp_nbr, const WT *__restrict__ tmp_w,
                                                  int32_t *out_nbr, WT *out_w, long long tmp_cap,
                                                  const int32_t *__restrict__ nz_rows,
-                                                 const long long *__restrict__ nz_offs, DevStats *st,
+                                                 const long long *__restrict__ nz_offs,
+                                                 const long long *__restrict__ nz_shift,
+                                                 const int32_t *__restrict__ task_row, DevStats *st,
                                                  WT *self_out)
 {
     const long long wg = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
@@ -1035,7 +1056,7 @@ __global__ void __launch_bounds__(256) k_compact(const int64_t *__restrict__ new
         const int c = nz_rows[r];
         if (c < 0 || c >= C) return;
         pa = c;
-        pb = tmp_off[c] - new_offs[c];
+        pb = nz_shift[r];
     };
     constexpr int U = kWalkUnroll;
     const int lane = threadIdx.x & 31;
@@ -1043,7 +1064,7 @@ __global__ void __launch_bounds__(256) k_compact(const int64_t *__restrict__ new
     for (long long t = wg; t * kRangeEntries < Enew; t += nw) {
         const long long j0 = t * kRangeEntries;
         const long long j1 = j0 + kRangeEntries < Enew ? j0 + kRangeEntries : Enew;
-        cur.start(j0);
+        cur.start_row(task_row[t]);
         for (long long jb = j0; jb < j1; jb += 32 * U) {
             long long src[U], com[U];
             bool ok[U];
@@ -1180,7 +1201,8 @@ static int resident_grid(K kernel, int threads, size_t smem = 0)
 // Walk list of the rows of (offs, n) that have entries (E entries in total).
 // With dn / dE (device) the rows are [0, min(n, *dn)) and the entries *dE:
 // nothing waits for the host.
-static void build_walk_list(const int64_t *offs, int n, long long E, ContractBuffers &b, cudaStream_t st,
+template <typename Shift>
+static void build_walk_list(const int64_t *offs, int n, long long E, ContractBuffers &b, cudaStream_t st, Shift shift,
                             const long long *dn = nullptr, const long long *dE = nullptr)
 {
     const int cap = sm_count() * 8;
@@ -1190,7 +1212,8 @@ static void build_walk_list(const int64_t *offs, int n, long long E, ContractBuf
     else
         exclusive_scan(offs, b.nz_pos, n, OpRowNonEmpty{offs}, b.scan_partial, &b.stats->total, st, &b.stats->err);
     k_nz_tail<<<1, 1, 0, st>>>(b.stats, b.nz_offs, E, dE);
-    k_nz_scatter<<<grid_cap(n, 256, cap), 256, 0, st>>>(offs, n, b.nz_pos, b.nz_rows, b.nz_offs, dn);
+    k_nz_scatter<Shift><<<grid_cap(n, 256, cap), 256, 0, st>>>(offs, n, b.nz_pos, b.nz_rows, b.nz_offs, b.nz_shift,
+                                                               b.task_row, dn, shift);
     note_launch(2);
 }
 
@@ -1357,16 +1380,16 @@ static int contract_t(const LevelGraph &g, const int32_t *comm, ContractBuffers 
     note_launch(2);
     const bool weighted = g.w != nullptr;
     if (E > 0) {
-        build_walk_list(g.offs, n, E, b, st);
+        build_walk_list(g.offs, n, E, b, st, ShiftStream{b.mpos, b.medge});
         const int tasks = grid_cap((E + kRangeEntries - 1) / kRangeEntries * 32, 256, cap);
         if (weighted) {
             const int grid = std::min(tasks, resident_grid(k_stream_fill<WT, true>, 256));
-            k_stream_fill<WT, true><<<grid, 256, 0, st>>>(n, E, g.offs, g.nbr, (const WT *)g.w, b.lab, b.mpos, b.medge,
-                                                          b.stream_key, (WT *)b.stream_w, b.nz_rows, b.nz_offs, ds);
+            k_stream_fill<WT, true><<<grid, 256, 0, st>>>(E, g.nbr, (const WT *)g.w, b.lab, b.stream_key,
+                                                          (WT *)b.stream_w, b.nz_offs, b.nz_shift, b.task_row, ds);
         } else {
             const int grid = std::min(tasks, resident_grid(k_stream_fill<WT, false>, 256));
-            k_stream_fill<WT, false><<<grid, 256, 0, st>>>(n, E, g.offs, g.nbr, nullptr, b.lab, b.mpos, b.medge,
-                                                           b.stream_key, nullptr, b.nz_rows, b.nz_offs, ds);
+            k_stream_fill<WT, false><<<grid, 256, 0, st>>>(E, g.nbr, nullptr, b.lab, b.stream_key, nullptr, b.nz_offs,
+                                                           b.nz_shift, b.task_row, ds);
         }
         note_launch(1);
     }
@@ -1447,11 +1470,11 @@ static int contract_t(const LevelGraph &g, const int32_t *comm, ContractBuffers 
     k_set_last_offset<<<1, 1, 0, st>>>(new_offs, ds);
     note_launch(1);
     if (E > 0) {  // the new level has at most E entries
-        build_walk_list(new_offs, n, 0, b, st, dC, &ds->new_entries);
+        build_walk_list(new_offs, n, 0, b, st, ShiftCompact{b.tmp_off}, dC, &ds->new_entries);
         // a second wave of blocks measured faster here than a resident grid
         k_compact<WT><<<grid_cap((E + kRangeEntries - 1) / kRangeEntries * 32, 256, cap), 256, 0, st>>>(
-            new_offs, b.tmp_off, b.tmp_nbr, (const WT *)b.tmp_w, new_nbr, new_w, E, b.nz_rows, b.nz_offs, ds,
-            (WT *)nli.self);
+            new_offs, b.tmp_off, b.tmp_nbr, (const WT *)b.tmp_w, new_nbr, new_w, E, b.nz_rows, b.nz_offs, b.nz_shift,
+            b.task_row, ds, (WT *)nli.self);
         note_launch(1);
     }
     if (!read_stats(&hs, ds, st, status, "contraction")) return -1;

@@ -1279,7 +1279,8 @@ gala_status gala_context_create(int32_t device, int32_t max_vertices, int64_t ma
          dalloc(ctx, &ctx->hub_pc, (size_t)c.big_twork_cap) && dalloc8(ctx, &ctx->hub_pw, (size_t)c.big_twork_cap) &&
          dalloc(ctx, &ctx->hub_pt, (size_t)c.big_twork_cap) && dalloc8(ctx, &ctx->hub_pwc, (size_t)c.big_twork_cap) &&
          dalloc(ctx, &ctx->hub_pdq, (size_t)c.big_twork_cap) && dalloc(ctx, &ctx->hub_pfc, (size_t)c.big_twork_cap) &&
-         dalloc(ctx, &c.nz_pos, n + 1) && dalloc(ctx, &c.nz_rows, n + 1) && dalloc(ctx, &c.nz_offs, n + 1);
+         dalloc(ctx, &c.nz_pos, n + 1) && dalloc(ctx, &c.nz_rows, n + 1) && dalloc(ctx, &c.nz_offs, n + 1) &&
+         dalloc(ctx, &c.nz_shift, n + 1) && dalloc(ctx, &c.task_row, E / 1024 + 2);
     // scratch pool for hub tables (phase 1) and the emission bitmaps of the
     // contraction: 8 ints per entry+vertex, 16 MB .. 512 MB
     long long want = 8LL * ((long long)E + (long long)n);

@@ -285,6 +285,8 @@ struct ContractBuffers {
     int32_t *nz_pos;     // n+1: rows with entries, compacted (walk list)
     int32_t *nz_rows;    // n+1
     long long *nz_offs;  // n+1
+    long long *nz_shift; // n+1: per listed row, the value its walk adds to an entry index
+    int32_t *task_row;   // E / 1024 + 2: first listed row of every 1024-entry walk task
     int32_t *cls_list;   // n: communities by size class
     // rows of more than 4096 entries: one global table per community, filled
     // by many CTAs (chunks of the stream), then emitted by one CTA each

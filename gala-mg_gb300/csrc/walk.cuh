@@ -93,6 +93,12 @@ struct RowCursor {
         w.vbase = warp_owner_row(w.offs_ll, w.n, j0);
         load();
     }
+    // start at row r, the owner of the task's first entry (known)
+    __device__ __forceinline__ void start_row(int r)
+    {
+        w.vbase = r;
+        load();
+    }
     // Batches are resolved in ascending order.  Entry j (this lane's entry of
     // the batch [jb, jl]) receives its row's values; returns false when j lies
     // outside the window, which a walk list never produces.  All lanes call.
