@@ -80,9 +80,11 @@ struct RowCursor {
     RowWindow w;
     RV rowval;
     long long pa, pb;
+    long long wend;  // end of the window's last row
     __device__ __forceinline__ void load()
     {
         w.load();
+        wend = __shfl_sync(GALA_FULL_MASK, w.rowend, 31);
         const int r = w.vbase + (int)(threadIdx.x & 31);
         pa = -1;
         pb = 0;
@@ -99,16 +101,24 @@ struct RowCursor {
         w.vbase = r;
         load();
     }
-    // Batches are resolved in ascending order.  Entry j (this lane's entry of
-    // the batch [jb, jl]) receives its row's values; returns false when j lies
-    // outside the window, which a walk list never produces.  All lanes call.
+    // Batches are resolved in ascending order.  Entry j = jb + lane (this
+    // lane's entry of the batch [jb, jl]) receives its row's values; returns
+    // false when j lies outside the window, which a walk list never produces.
+    // All lanes call.  The row of entry jb + k is the number of window rows
+    // that end at or before it: the rows ending at or before jb (one ballot)
+    // plus the row ends inside the batch, which are distinct (rows have
+    // entries) and so form a bit mask over the batch (one OR-reduction).
     __device__ __forceinline__ bool resolve(long long jb, long long jl, long long j, long long &a, long long &b)
     {
-        if (w.count_le(jl) == 32) {  // the batch ends past the window
+        if (jl >= wend) {  // the batch ends past the window
             w.vbase += w.count_le(jb);
             load();
         }
-        const int idx = w.count_le(j);
+        const int before = __popc(__ballot_sync(GALA_FULL_MASK, w.rowend <= jb));
+        const long long q = w.rowend - jb;  // the row's end, relative to the batch
+        const unsigned ends = __reduce_or_sync(GALA_FULL_MASK, (q >= 1 && q <= 31) ? (1u << (int)q) : 0u);
+        const int k = (int)(j - jb);  // == lane
+        const int idx = before + __popc(ends & ((2u << k) - 2u));
         a = __shfl_sync(GALA_FULL_MASK, pa, idx & 31);
         b = __shfl_sync(GALA_FULL_MASK, pb, idx & 31);
         return idx < 32;
