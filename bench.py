@@ -103,11 +103,12 @@ def measured_peak():
         return FALLBACK_HBM_GBS, "fallback"
 
 
-def profile_traffic():
-    """DRAM bytes per algorithmic byte of the decide sweeps, from the committed
-    ncu summary (a line 'traffic_per_algorithmic_byte: X'), if any."""
+def profile_traffic(name="decide_traffic_rmat-s21.md"):
+    """DRAM bytes per algorithmic byte of a kernel family (the decide sweeps by
+    default), from its committed ncu summary (a line
+    'traffic_per_algorithmic_byte: X'), if any."""
     import re
-    p = os.path.join(ROOT, "profiles", "decide_traffic_rmat-s21.md")
+    p = os.path.join(ROOT, "profiles", name)
     try:
         m = re.search(r"traffic_per_algorithmic_byte:\s*([0-9.]+)", open(p).read())
         return float(m.group(1)) if m else None
@@ -141,9 +142,13 @@ def contraction_roofline(runs, peak, peak_kind):
         return None
     ach = byt / (ms / 1000.0) / 1e9
     lv = runs[-1]["levels"]
+    tr = profile_traffic("contract_dram_rmat-s21.md")
     return {"bound": "hbm", "kernel": "contraction (renumber, member buckets, row aggregation, CSR write) of "
                                       "every round that builds a next level",
             "achieved": ach, "peak": peak, "peak_kind": peak_kind, "unit": "GB/s", "frac": ach / peak,
+            "traffic": tr * byt / len(runs) if tr else None,
+            "traffic_note": "DRAM bytes per run: ncu ratio (traffic / algorithmic bytes) measured at scale 21 "
+                            "times this run's algorithmic bytes" if tr else None,
             "algorithmic_bytes_per_run": byt / len(runs), "ms_per_run": ms / len(runs),
             "level0_ms": lv[0]["contract_ms"], "level0_bytes": contraction_bytes(lv, 0) if len(lv) > 1 else None,
             "last_round_relabel_ms": lv[-1]["contract_ms"]}
