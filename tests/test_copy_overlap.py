@@ -65,6 +65,25 @@ def test_chunked_copy_with_graphs_and_refine(ffi, torch_cuda):
         _same(out[True][k], out[False][k])
 
 
+@pytest.mark.parametrize("mode", ["trace", "skip"])
+def test_chunked_copy_with_proposals(ffi, torch_cuda, mode):
+    """Proposal runs take level 0 after the whole copy (the chunked first
+    sweep is for plain runs): the same partitions with and without chunks."""
+    g = ffi.Graph.rmat(19, 5_000_000, seed=6)
+    offs, _, _ = g.arrays()
+    g.pin()
+    ctx = ffi.Context(offs.shape[0] - 1, offs[-1])
+    out = {}
+    for on in (8, 0):
+        ctx.set_copy_overlap(on)
+        prop = ffi.Proposal(max_samples=1 << 16, seed=1)
+        kw = {"mode": ffi.PROPOSAL_TRACE} if mode == "trace" else {"mode": ffi.PROPOSAL_SKIP, "threshold": 0.5}
+        out[on] = ctx.louvain(g, proposal=prop, **kw)
+        prop.close()
+    ctx.close()
+    _same(out[8], out[0])
+
+
 @pytest.mark.parametrize("chunks", [2, 16])
 def test_chunk_counts(ffi, torch_cuda, chunks):
     g = ffi.Graph.rmat(19, 5_000_000, seed=2)
