@@ -90,6 +90,16 @@ struct DevStats {
     long long big_nwork;    // long rows: stream chunks
     long long big_ntwork;   // long rows: table chunks
     long long big_lwork;    // long rows: slot-list chunks
+    // long rows by key range: pool offsets (ints) and counts
+    long long rad_offm;     // per-chunk bucket offsets (uint16)
+    long long rad_items;    // work items
+    long long rad_acc;      // accumulators of buckets split over several CTAs
+    long long rad_max_items;
+    long long rad_max_acc;
+    int rad_nb;             // buckets per row: ceil(C / 8192)
+    int rad_nitems;         // items planned
+    int rad_nacc;           // accumulators taken
+    int rad_next;           // item queue head
     // incremental weight update
     unsigned long long mv_edges;  // row entries of this sweep's movers
     long long push_total;         // the same, summed by the movers' prefix

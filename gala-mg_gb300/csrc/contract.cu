@@ -929,6 +929,533 @@ __global__ void k_big_lchunks(const int *cursor, const DevStats *st, long long *
         lch[i] = (cursor[i] + kChunk - 1) / kChunk;
 }
 
+// ---- long rows by key range (rows in table order) ----------------------
+//
+// Every kChunk-entry chunk of a long row is summed per key in shared memory
+// first; its distinct (key, sum) pairs go back to the chunk's own stream
+// range, ordered by bucket (key >> kRadLg: 8192 communities each), together
+// with the chunk's bucket offsets and the pair counts per (row, bucket).
+// Work items then cover one bucket, or a run of small buckets, of one row: a
+// CTA sums the item's pairs from every chunk of the row in one shared-memory
+// table (dense over the bucket's 8192 keys, or hashed) and appends the
+// distinct keys to the row.  A bucket of more than kRadPiece pairs is split
+// by chunk range over several CTAs that add their sums into a global dense
+// table of the bucket; the last of them emits it.  Against the global hash
+// tables of the other path this takes no table clear, no global probing and
+// no slot-list collection.
+constexpr int kRadLg = 13;
+constexpr int kRadW = 1 << kRadLg;  // communities per bucket
+constexpr int kRadNbMax = 2048;     // buckets per row (C <= 2^24)
+constexpr int kRadH = 2048;         // buckets of at most kRadH pairs are grouped (< 2 kRadH pairs per item)
+constexpr int kRadPiece = 32768;    // pairs per CTA of a split bucket
+static_assert(kSmT == kRadW, "the chunk table and a bucket have the same size");
+
+struct RadItem {
+    int i;       // row (list index)
+    int b0, b1;  // buckets [b0, b1)
+    int k0, k1;  // chunks [k0, k1) of the row
+    int acc;     // global table of a split bucket (-1: none)
+    int pieces;  // CTAs of the bucket
+    int total;   // pairs of the buckets over all chunks of the row
+};
+constexpr int kRadItemInts = (int)(sizeof(RadItem) / sizeof(int));
+
+// Global table of a split bucket: kRadW values, a bitmap of the slots that
+// received a non-positive sum, a counter of finished pieces.
+__host__ __device__ constexpr long long rad_acc_ints(long long vints) { return kRadW * vints + kRadW / 32 + 8; }
+
+struct RadLayout {
+    long long offm, items, acc, max_items, max_acc, end;
+};
+__host__ __device__ inline long long rad_up8(long long x) { return (x + 7) & ~7LL; }
+// Pool layout (ints): pair counts per (row, bucket) at 0, then the chunks'
+// bucket offsets (uint16, nb + 1 per chunk), the items and the global tables.
+// Items per row are at most pairs (4 / kRadH + 1 / kRadPiece) + 2: big
+// buckets, the runs after them and one run per kRadH-pair window, plus the
+// extra pieces of split buckets.
+__host__ __device__ inline RadLayout rad_layout(long long cnt, long long nwork, long long nb, long long vints)
+{
+    RadLayout L;
+    L.offm = rad_up8(cnt * nb);
+    L.items = rad_up8(L.offm + (nwork * (nb + 1) + 1) / 2);
+    L.max_items = 5 * nwork * kChunk / kRadH + 2 * cnt + 16;
+    L.acc = rad_up8(L.items + L.max_items * kRadItemInts);
+    L.max_acc = nwork * kChunk / kRadPiece + 1;
+    L.end = L.acc + L.max_acc * rad_acc_ints(vints);
+    return L;
+}
+
+// Exclusive prefix of x over the block (all threads call; ws: 33 ints);
+// total receives the block sum.  Ends with a barrier.
+__device__ __forceinline__ int block_excl_scan(int x, int *ws, int &total)
+{
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    int incl = x;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int t = __shfl_up_sync(GALA_FULL_MASK, incl, o);
+        if (lane >= o) incl += t;
+    }
+    if (lane == 31) ws[wid] = incl;
+    __syncthreads();
+    if (wid == 0) {
+        const int w = lane < nw ? ws[lane] : 0;
+        int wi = w;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int t = __shfl_up_sync(GALA_FULL_MASK, wi, o);
+            if (lane >= o) wi += t;
+        }
+        if (lane < nw) ws[lane] = wi - w;
+        if (lane == 31) ws[32] = wi;
+    }
+    __syncthreads();
+    total = ws[32];
+    const int r = ws[wid] + incl - x;
+    __syncthreads();
+    return r;
+}
+
+// Chunk counts per row, cursors, zeroed pair counts, buckets per row.
+template <typename WT>
+__global__ void k_rad_plan(AggArgs<WT> a, BigArgs b, int32_t *tot, long long pool_ints)
+{
+    const int cnt = a.st->small_cnt[kLongCls];
+    const long long C = a.st->ccount;
+    const int nb = (int)((C + kRadW - 1) >> kRadLg);
+    const long long tid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    const long long nt = (long long)gridDim.x * blockDim.x;
+    for (long long i = tid; i < cnt; i += nt) {
+        const long long E = a.ec[b.list[i]];
+        b.chunks[i] = (E + kChunk - 1) / kChunk;
+        b.cursor[i] = 0;
+    }
+    const long long ntot = (long long)cnt * nb;
+    if (nb <= kRadNbMax && ntot <= pool_ints)
+        for (long long q = tid; q < ntot; q += nt) tot[q] = 0;
+    if (tid == 0) a.st->rad_nb = nb;
+}
+
+// coff[cnt] closes the chunk list; the layout is fixed and checked against
+// the pool (kErrCapacity stops the other kernels).
+__global__ void k_rad_tail(BigArgs b, DevStats *st, long long vints, long long pool_ints)
+{
+    const int cnt = st->small_cnt[kLongCls];
+    const long long nwork = st->big_nwork;
+    ((long long *)b.coff)[cnt] = nwork;
+    const int nb = st->rad_nb;
+    const RadLayout L = rad_layout(cnt, nwork, nb, vints);
+    st->rad_offm = L.offm;
+    st->rad_items = L.items;
+    st->rad_acc = L.acc;
+    st->rad_max_items = L.max_items;
+    st->rad_max_acc = L.max_acc;
+    if (nb > kRadNbMax || L.end > pool_ints) st->err |= kErrCapacity;
+}
+
+template <typename WT>
+constexpr size_t rad_combine_smem()
+{
+    return (size_t)kSmT * (sizeof(WT) + sizeof(int) + sizeof(unsigned short)) + (kRadNbMax + 1) * sizeof(int);
+}
+
+// One chunk per CTA iteration: sum the chunk's entries per key (shared-memory
+// hash table), then write the distinct pairs back over the chunk in bucket
+// order.  pk / pw are the stream's keys and weight slots (the weight slots
+// are written even on an unweighted level, where the stream has no weights).
+template <typename WT>
+__global__ void __launch_bounds__(512) k_rad_combine(AggArgs<WT> a, BigArgs b, int32_t *pool, int32_t *pk, WT *pw)
+{
+    DevStats *st = a.st;
+    const long long nwork = big_off(st) ? 0 : st->big_nwork;
+    if (nwork <= blockIdx.x) return;
+    const int cnt = st->small_cnt[kLongCls];
+    const int nb = st->rad_nb;
+    int32_t *tot = pool;
+    unsigned short *offm = (unsigned short *)(pool + st->rad_offm);
+    extern __shared__ long long rsm_ll[];
+    WT *svals = (WT *)rsm_ll;
+    int *skeys = (int *)(svals + kSmT);
+    int *hist = skeys + kSmT;
+    unsigned short *socc = (unsigned short *)(hist + kRadNbMax + 1);
+    __shared__ int s_n;
+    __shared__ int ws[33];
+    for (int q = threadIdx.x; q < kSmT; q += blockDim.x) {
+        skeys[q] = -1;
+        svals[q] = 0;
+    }
+    for (int q = threadIdx.x; q <= kRadNbMax; q += blockDim.x) hist[q] = 0;
+    if (threadIdx.x == 0) s_n = 0;
+    __syncthreads();
+    for (long long wi = blockIdx.x; wi < nwork; wi += gridDim.x) {
+        int lo = 0, hi = cnt - 1;  // row of the chunk: last i with coff[i] <= wi
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (b.coff[mid] <= wi) lo = mid;
+            else hi = mid - 1;
+        }
+        const int i = lo;
+        const int c = b.list[i];
+        const long long j = wi - b.coff[i];
+        const long long E = a.ec[c];
+        const long long s0 = a.medge[a.moff[c]] + j * kChunk;
+        const int len = (int)((E - j * kChunk) < kChunk ? (E - j * kChunk) : kChunk);
+        for (int q = threadIdx.x; q < len; q += blockDim.x) {
+            const int key = pk[s0 + q];
+            const WT wt = a.sw ? pw[s0 + q] : (WT)1;
+            unsigned h = hash_slot(key, kRadLg);
+            for (int p = 0; p < kSmT; ++p) {
+                const int k = atomicCAS(&skeys[h], -1, key);
+                if (k == -1 || k == key) {
+                    atomic_add_w(&svals[h], wt);
+                    if (k == -1) {
+                        socc[atomicAdd(&s_n, 1)] = (unsigned short)h;
+                        const int bk = key >> kRadLg;
+                        if (bk < nb) atomicAdd(&hist[bk], 1);
+                        else atomicOr(&st->err, kErrBadIndex);
+                    }
+                    break;
+                }
+                h = (h + 1) & (unsigned)(kSmT - 1);
+            }
+        }
+        __syncthreads();
+        const int n = s_n;
+        // bucket offsets of the chunk: exclusive scan of hist, 4 buckets per thread
+        int v[4], sum = 0;
+        const int t4 = threadIdx.x * 4;
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            v[u] = (t4 + u < nb) ? hist[t4 + u] : 0;
+            sum += v[u];
+        }
+        int total;
+        int run = block_excl_scan(sum, ws, total);
+        unsigned short *orow = offm + wi * (nb + 1);
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const int bk = t4 + u;
+            if (bk < nb) {
+                if (v[u]) atomicAdd(&tot[(long long)i * nb + bk], v[u]);
+                orow[bk] = (unsigned short)run;
+                hist[bk] = run;  // the scatter's cursor of the bucket
+                run += v[u];
+            }
+        }
+        if (threadIdx.x == 0) orow[nb] = (unsigned short)n;
+        __syncthreads();
+        for (int q = threadIdx.x; q < n; q += blockDim.x) {
+            const int h = socc[q];
+            const int key = skeys[h];
+            const int bk = key >> kRadLg;
+            if (bk < nb) {
+                const int p = atomicAdd(&hist[bk], 1);
+                pk[s0 + p] = key;
+                pw[s0 + p] = svals[h];
+            }
+            skeys[h] = -1;
+            svals[h] = 0;
+        }
+        __syncthreads();
+        for (int q = threadIdx.x; q < nb; q += blockDim.x) hist[q] = 0;
+        if (threadIdx.x == 0) s_n = 0;
+        __syncthreads();
+    }
+}
+
+// Work items of every long row, one warp per row: a bucket of more than
+// kRadH pairs is an item of its own (split into pieces of about kRadPiece
+// pairs by chunk range), runs of smaller buckets are grouped while their
+// pair prefix stays in one kRadH window.  Split buckets get a zeroed global
+// table.
+template <typename WT>
+__global__ void k_rad_items(AggArgs<WT> a, BigArgs b, int32_t *pool, long long vints)
+{
+    DevStats *st = a.st;
+    const int cnt = big_off(st) ? 0 : st->small_cnt[kLongCls];
+    const int nb = st->rad_nb;
+    const int lane = threadIdx.x & 31;
+    const int wg = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nw = (gridDim.x * blockDim.x) >> 5;
+    RadItem *items = (RadItem *)(pool + st->rad_items);
+    int32_t *accs = pool + st->rad_acc;
+    const long long max_items = st->rad_max_items, max_acc = st->rad_max_acc;
+    const long long acc_ints = rad_acc_ints(vints);
+    for (int i = wg; i < cnt; i += nw) {
+        const int nch = (int)b.chunks[i];
+        const int32_t *trow = pool + (long long)i * nb;
+        long long carry = 0;  // pairs of the buckets before the tile
+        int prev_big = 0;
+        long long prev_win = -1;
+        int open_b = -1;  // first bucket of the item still open, and its prefix
+        long long open_s = 0;
+        for (int t0 = 0; t0 <= nb; t0 += 32) {  // bucket nb closes the last item
+            const int bk = t0 + lane;
+            const int m = bk < nb ? trow[bk] : 0;
+            int incl = m;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int t = __shfl_up_sync(GALA_FULL_MASK, incl, o);
+                if (lane >= o) incl += t;
+            }
+            const long long S = carry + incl - m;
+            const int big = m > kRadH;
+            const long long win = S / kRadH;
+            int pb = __shfl_up_sync(GALA_FULL_MASK, big, 1);
+            long long pwin = __shfl_up_sync(GALA_FULL_MASK, win, 1);
+            if (lane == 0) {
+                pb = prev_big;
+                pwin = prev_win;
+            }
+            const bool start = bk <= nb && (bk == 0 || bk == nb || big || pb || win != pwin);
+            const unsigned sm = __ballot_sync(GALA_FULL_MASK, start);
+            // every start closes the item that began at the previous start
+            const unsigned below = sm & lanemask_lt();
+            const int pl = below ? 31 - __clz(below) : 0;
+            const int sb = __shfl_sync(GALA_FULL_MASK, bk, pl);
+            const long long sS = __shfl_sync(GALA_FULL_MASK, S, pl);
+            const int ps = below ? sb : open_b;
+            const long long pS = below ? sS : open_s;
+            int np = 0;
+            RadItem it{};
+            if (start && ps >= 0) {
+                const long long t = S - pS;
+                if (t > 0) {
+                    np = 1;
+                    if (bk - ps == 1 && t > kRadH) {
+                        const long long P = (t + kRadPiece - 1) / kRadPiece;
+                        np = (int)(P < nch ? P : nch);
+                    }
+                    it.i = i;
+                    it.b0 = ps;
+                    it.b1 = bk;
+                    it.acc = -1;
+                    it.pieces = np;
+                    it.total = (int)t;
+                }
+            }
+            int ex = np;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int t = __shfl_up_sync(GALA_FULL_MASK, ex, o);
+                if (lane >= o) ex += t;
+            }
+            const int wsum = __shfl_sync(GALA_FULL_MASK, ex, 31);
+            ex -= np;
+            long long base = 0;
+            if (lane == 0 && wsum) base = atomicAdd(&st->rad_nitems, wsum);
+            base = __shfl_sync(GALA_FULL_MASK, base, 0);
+            int acc = -1;
+            if (np) {
+                if (base + ex + np > max_items) {
+                    atomicOr(&st->err, kErrCapacity);
+                } else {
+                    if (np > 1) {
+                        acc = atomicAdd(&st->rad_nacc, 1);
+                        if (acc >= max_acc) {
+                            atomicOr(&st->err, kErrCapacity);
+                            acc = -1;
+                        }
+                    }
+                    if (np == 1 || acc >= 0) {
+                        it.acc = acc;
+                        for (int p = 0; p < np; ++p) {
+                            it.k0 = (int)((long long)p * nch / np);
+                            it.k1 = (int)((long long)(p + 1) * nch / np);
+                            items[base + ex + p] = it;
+                        }
+                    }
+                }
+            }
+            unsigned am = __ballot_sync(GALA_FULL_MASK, acc >= 0);
+            while (am) {  // zero the global tables this warp took
+                const int l = __ffs(am) - 1;
+                am &= am - 1;
+                const long long ac = __shfl_sync(GALA_FULL_MASK, acc, l);
+                int4 *z = (int4 *)(accs + ac * acc_ints);
+                for (long long q = lane; q < acc_ints / 4; q += 32) z[q] = make_int4(0, 0, 0, 0);
+            }
+            carry += __shfl_sync(GALA_FULL_MASK, incl, 31);
+            prev_big = __shfl_sync(GALA_FULL_MASK, big, 31);
+            prev_win = __shfl_sync(GALA_FULL_MASK, win, 31);
+            if (sm) {
+                const int hl = 31 - __clz(sm);
+                open_b = __shfl_sync(GALA_FULL_MASK, bk, hl);
+                open_s = __shfl_sync(GALA_FULL_MASK, S, hl);
+            }
+        }
+    }
+}
+
+template <typename WT>
+constexpr size_t rad_agg_smem()
+{
+    return (size_t)kRadW * (sizeof(WT) + sizeof(int) + sizeof(unsigned short));
+}
+
+// Appends the present slots of a dense bucket table (values v, bitmap nb of
+// non-positive sums) to the row: keys kbase + slot.  GLOBAL: the table is a
+// split bucket's global one (read past L1).
+template <typename WT, bool GLOBAL>
+__device__ __forceinline__ void rad_emit_dense(const AggArgs<WT> &a, const BigArgs &b, int i, long long o,
+                                               int kbase, WT *v, unsigned *nbits, int *ws, long long *s_base)
+{
+    constexpr int kPer = kRadW / 512;
+    int present = 0;
+#pragma unroll
+    for (int r = 0; r < kPer; ++r) {
+        const int s = threadIdx.x + r * 512;
+        const WT x = GLOBAL ? __ldcg(&v[s]) : v[s];
+        const unsigned w = GLOBAL ? __ldcg(&nbits[s >> 5]) : nbits[s >> 5];
+        if (x != 0 || ((w >> (s & 31)) & 1u)) present |= 1 << r;
+    }
+    int total;
+    int p = block_excl_scan(__popc(present), ws, total);
+    if (threadIdx.x == 0) *s_base = total ? atomicAdd(&b.cursor[i], total) : 0;
+    __syncthreads();
+    const long long dst = o + *s_base;
+#pragma unroll
+    for (int r = 0; r < kPer; ++r) {
+        const int s = threadIdx.x + r * 512;
+        if (present & (1 << r)) {
+            a.tmp_nbr[dst + p] = kbase + s;
+            a.tmp_w[dst + p] = GLOBAL ? __ldcg(&v[s]) : v[s];
+            ++p;
+        }
+        if (!GLOBAL) v[s] = 0;
+    }
+}
+
+// The items, taken from a queue by persistent CTAs of 512 threads.
+template <typename WT>
+__global__ void __launch_bounds__(512) k_rad_agg(AggArgs<WT> a, BigArgs b, int32_t *pool, const int32_t *pk,
+                                                 const WT *pw, long long vints)
+{
+    DevStats *st = a.st;
+    if (big_off(st)) return;
+    long long nitems = st->rad_nitems;
+    if (nitems > st->rad_max_items) nitems = st->rad_max_items;
+    const int nb1 = st->rad_nb + 1;
+    const RadItem *items = (const RadItem *)(pool + st->rad_items);
+    const unsigned short *offm = (const unsigned short *)(pool + st->rad_offm);
+    int32_t *accs = pool + st->rad_acc;
+    const long long acc_ints = rad_acc_ints(vints);
+    extern __shared__ long long asm_ll[];
+    WT *vals = (WT *)asm_ll;
+    int *keys = (int *)(vals + kRadW);
+    unsigned *bits = (unsigned *)keys;  // dense items: the first kRadW / 32 key slots
+    unsigned short *occ = (unsigned short *)(keys + kRadW);
+    __shared__ int s_it, s_n, s_last;
+    __shared__ long long s_base;
+    __shared__ int ws[33];
+    for (int q = threadIdx.x; q < kRadW; q += blockDim.x) {
+        keys[q] = -1;
+        vals[q] = 0;
+    }
+    if (threadIdx.x == 0) s_n = 0;
+    for (;;) {
+        __syncthreads();
+        if (threadIdx.x == 0) s_it = atomicAdd(&st->rad_next, 1);
+        __syncthreads();
+        const int itn = s_it;
+        if (itn >= nitems) break;
+        const RadItem it = items[itn];
+        const int c = b.list[it.i];
+        const long long sbase = a.medge[a.moff[c]];
+        const long long w0 = b.coff[it.i];
+        const bool dense = it.b1 - it.b0 == 1 && it.total > kRadH;
+        const int kbase = it.b0 << kRadLg;
+        int T = kRadW, lg = kRadLg;
+        if (dense) {
+            for (int q = threadIdx.x; q < kRadW / 32; q += blockDim.x) bits[q] = 0;
+            __syncthreads();
+        } else {
+            T = next_pow2_int(2LL * it.total);
+            if (T < 64) T = 64;
+            if (T > kRadW) T = kRadW;
+            lg = __ffs(T) - 1;
+        }
+        // G threads per chunk: enough groups for the chunks, up to a warp per
+        // chunk when the chunks hold many of the item's pairs
+        const int nk = it.k1 - it.k0;
+        const long long per = (long long)it.total / it.pieces / (nk > 0 ? nk : 1);
+        int g1 = 1, g2 = 1;
+        while (g1 * 2 * nk <= 512) g1 <<= 1;
+        while (g2 * 2 <= per && g2 < 32) g2 <<= 1;
+        const int G = g1 > g2 ? g1 : g2;
+        const int gid = threadIdx.x / G, gl = threadIdx.x % G, ng = blockDim.x / G;
+        const long long erow = a.ec[c];
+        for (int k = it.k0 + gid; k < it.k1; k += ng) {
+            const unsigned short *orow = offm + (w0 + k) * nb1;
+            const long long base = sbase + (long long)k * kChunk;
+            const long long len = erow - (long long)k * kChunk;
+            const int lo = orow[it.b0];
+            const int hi = (long long)orow[it.b1] < len ? orow[it.b1] : (int)len;
+            for (int q = lo + gl; q < hi; q += G) {
+                const int key = pk[base + q];
+                const WT v = pw[base + q];
+                if (dense) {
+                    const unsigned s = (unsigned)(key - kbase);
+                    if (s < (unsigned)kRadW) {
+                        atomic_add_w(&vals[s], v);
+                        if (v <= 0) atomicOr(&bits[s >> 5], 1u << (s & 31));
+                    } else {
+                        atomicOr(&st->err, kErrBadIndex);
+                    }
+                } else {
+                    int slot;
+                    const int r = table_add(keys, vals, T, lg, key, v, slot);
+                    if (r < 0) atomicOr(&st->err, kErrHashOverflow);
+                    else if (r == 1) occ[atomicAdd(&s_n, 1)] = (unsigned short)slot;
+                }
+            }
+        }
+        __syncthreads();
+        const long long o = a.tmp_off[c];
+        if (!dense) {
+            const int n = s_n;
+            if (threadIdx.x == 0) s_base = n ? atomicAdd(&b.cursor[it.i], n) : 0;
+            __syncthreads();
+            const long long dst = o + s_base;
+            for (int q = threadIdx.x; q < n; q += blockDim.x) {
+                const int h = occ[q];
+                a.tmp_nbr[dst + q] = keys[h];
+                a.tmp_w[dst + q] = vals[h];
+                keys[h] = -1;
+                vals[h] = 0;
+            }
+            __syncthreads();
+            if (threadIdx.x == 0) s_n = 0;
+        } else if (it.pieces == 1) {
+            rad_emit_dense<WT, false>(a, b, it.i, o, kbase, vals, bits, ws, &s_base);
+        } else {
+            // add this piece to the bucket's global table; the last piece emits it
+            WT *gv = (WT *)(accs + it.acc * acc_ints);
+            unsigned *gb = (unsigned *)(gv + kRadW);
+            int *gcnt = (int *)(gb + kRadW / 32);
+            for (int s = threadIdx.x; s < kRadW; s += blockDim.x) {
+                const WT x = vals[s];
+                if (x != 0) atomic_add_w(&gv[s], x);
+                vals[s] = 0;
+            }
+            for (int q = threadIdx.x; q < kRadW / 32; q += blockDim.x)
+                if (bits[q]) atomicOr(&gb[q], bits[q]);
+            __threadfence();
+            __syncthreads();
+            if (threadIdx.x == 0) s_last = atomicAdd(gcnt, 1) == it.pieces - 1;
+            __syncthreads();
+            if (s_last) {
+                __threadfence();
+                rad_emit_dense<WT, true>(a, b, it.i, o, kbase, gv, gb, ws, &s_base);
+            }
+        }
+        if (dense) {
+            __syncthreads();
+            for (int q = threadIdx.x; q < kRadW / 32; q += blockDim.x) keys[q] = -1;
+        }
+    }
+}
+
 // Table chunks: distinct entries of sorted rows go to the row unsorted
 // (atomic cursor); rows ranked by bitmap set their bits.
 template <typename WT>
@@ -1124,6 +1651,7 @@ __global__ void k_contract_reset(DevStats *st)
     st->ccount = 0;
     st->new_entries = 0;
     st->big_slots = st->big_nwork = st->big_ntwork = st->big_lwork = 0;
+    st->rad_nb = st->rad_nitems = st->rad_nacc = st->rad_next = 0;
 }
 
 // Shared memory of the table kernels: int keys plus WT values per slot.
@@ -1165,6 +1693,8 @@ static void configure_t()
 
     cudaFuncSetAttribute(k_big_sort<WT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sort_smem<WT>());
     cudaFuncSetAttribute(k_big_insert_sm<WT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)big_sm_smem<WT>());
+    cudaFuncSetAttribute(k_rad_combine<WT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rad_combine_smem<WT>());
+    cudaFuncSetAttribute(k_rad_agg<WT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rad_agg_smem<WT>());
     cudaFuncSetAttribute(k_agg_mid_list<WT, 1024, 8192>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)list_smem<WT>(8192));
     cudaFuncSetAttribute(k_agg_mid_list<WT, 1024, 16384>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -1241,9 +1771,22 @@ static long long big_pool_half(const ContractBuffers &b)
 // at most cnt_max of them.  Counts, table sizes and the scratch check stay on
 // the device; only sorted rows read their bitmap sizes on the host.  Returns
 // false on failure.
+// Whether the key-range path fits the pool for any level of n rows and E
+// entries (C <= n, every long row longer than kMid3Max entries).
+template <typename WT>
+static bool rad_fits(long long n, long long E, const ContractBuffers &b)
+{
+    constexpr long long vints = sizeof(WT) / sizeof(int32_t);
+    if (E >= (1LL << 31)) return false;  // pair counts are 32-bit
+    const long long nb = (n + kRadW - 1) / kRadW;
+    if (nb > kRadNbMax) return false;
+    const long long cnt = std::min(n, E / (kMid3Max + 1));
+    return rad_layout(cnt, E / kChunk + cnt, nb, vints).end <= b.big_pool_ints;
+}
+
 template <typename WT>
 static bool contract_long_rows(const AggArgs<WT> &a, ContractBuffers &b, const int32_t *list, int cnt_max,
-                               cudaStream_t st, gala_status *status, bool sort_rows)
+                               cudaStream_t st, gala_status *status, bool sort_rows, long long n, long long E)
 {
     const int nsm = sm_count();
     const int cap = nsm * 8;
@@ -1268,6 +1811,21 @@ static bool contract_long_rows(const AggArgs<WT> &a, ContractBuffers &b, const i
     ba.pool_half = big_pool_half<WT>(b);
     ba.work_cap = b.big_work_cap;
     ba.twork_cap = b.big_twork_cap;
+    if (!sort_rows && b.long_rows_mode == 0 && rad_fits<WT>(n, E, b)) {
+        constexpr long long vints = sizeof(WT) / sizeof(int32_t);
+        k_rad_plan<WT><<<grid_cap(cnt_max, 256, cap), 256, 0, st>>>(a, ba, b.big_pool, b.big_pool_ints);
+        exclusive_scan_dev(b.big_chunks, b.big_coff, cnt_max, dcnt, OpIdentity(), b.scan_partial, &ds->big_nwork, st,
+                           &ds->err);
+        k_rad_tail<<<1, 1, 0, st>>>(ba, ds, vints, b.big_pool_ints);
+        k_rad_combine<WT><<<resident_grid(k_rad_combine<WT>, 512, rad_combine_smem<WT>()), 512,
+                            rad_combine_smem<WT>(), st>>>(a, ba, b.big_pool, b.stream_key, (WT *)b.stream_w);
+        k_rad_items<WT><<<grid_cap((long long)cnt_max * 32, 256, cap), 256, 0, st>>>(a, ba, b.big_pool, vints);
+        k_rad_agg<WT><<<resident_grid(k_rad_agg<WT>, 512, rad_agg_smem<WT>()), 512, rad_agg_smem<WT>(), st>>>(
+            a, ba, b.big_pool, b.stream_key, (const WT *)b.stream_w, vints);
+        k_big_len<WT><<<grid_cap(cnt_max, 256, cap), 256, 0, st>>>(a, ba);
+        note_launch(6);
+        return true;
+    }
     k_big_plan<WT><<<grid_cap(cnt_max, 256, cap), 256, 0, st>>>(a, ba);
     exclusive_scan_dev(b.big_T, b.big_toff, cnt_max, dcnt, OpIdentity(), b.scan_partial, &ds->big_slots, st,
                        &ds->err);
@@ -1428,7 +1986,7 @@ static int contract_t(const LevelGraph &g, const int32_t *comm, ContractBuffers 
         if (par) cudaStreamWaitEvent(cs[i], b.fork_ev, 0);
     }
     bool ok = n_long == 0 ||
-              contract_long_rows(a, b, b.cls_list + (long long)kLongCls * n, n_long, cs[3], status, sort_rows);
+              contract_long_rows(a, b, b.cls_list + (long long)kLongCls * n, n_long, cs[3], status, sort_rows, n, E);
     if (ok && n_mid2 > 0) {
         const int grid = n_mid2 < nsm * 2 ? n_mid2 : nsm * 2;
         if (sort_rows)

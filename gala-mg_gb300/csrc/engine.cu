@@ -1346,6 +1346,17 @@ gala_status gala_context_set_copy_overlap(gala_context *ctx, int32_t chunks)
     return GALA_OK;
 }
 
+gala_status gala_context_set_long_rows(gala_context *ctx, int32_t mode)
+{
+    clear_error();
+    if (!ctx || mode < 0 || mode > 1) {
+        set_error("gala_context_set_long_rows: mode must be 0 or 1");
+        return GALA_ERR_INVALID;
+    }
+    ctx->cb.long_rows_mode = mode;
+    return GALA_OK;
+}
+
 gala_status gala_context_set_update_mode(gala_context *ctx, int32_t mode)
 {
     clear_error();

@@ -291,6 +291,7 @@ struct ContractBuffers {
     // rows of more than 4096 entries: one global table per community, filled
     // by many CTAs (chunks of the stream), then emitted by one CTA each
     int32_t *big_pool;        // keys then values of all tables
+    int long_rows_mode = 0;   // 0: by key range when it fits, 1: global tables only
     long long big_pool_ints;
     long long *big_T;         // n: table slots per community (list order)
     long long *big_chunks;    // n: stream chunks per community

@@ -28,7 +28,8 @@ EXPORTS = ["gala_last_error", "gala_status_string", "gala_kernel_launch_count", 
            "gala_proposal_clear_samples", "gala_proposal_read_samples", "gala_proposal_gradient",
            "gala_proposal_logits", "gala_proposal_train", "gala_louvain_batch", "gala_generate_sbm_batch",
            "gala_graph_from_csr_f32", "gala_graph_weights_f32", "gala_generate_lfr", "gala_autotune",
-           "gala_context_set_hub_table_cap", "gala_context_set_update_mode", "gala_context_set_copy_overlap"]
+           "gala_context_set_hub_table_cap", "gala_context_set_update_mode", "gala_context_set_copy_overlap",
+           "gala_context_set_long_rows"]
 
 PROPOSAL_OFF, PROPOSAL_TRACE, PROPOSAL_SKIP = 0, 1, 2
 PROPOSAL_PARAMS = 32 * 8 + 32 + 32 * 32 + 32 + 32 + 1
@@ -166,6 +167,8 @@ def load(path=LIB_PATH):
     L.gala_context_set_hub_table_cap.restype = ctypes.c_int
     L.gala_context_set_update_mode.argtypes = [_vp, ctypes.c_int32]
     L.gala_context_set_update_mode.restype = ctypes.c_int
+    L.gala_context_set_long_rows.argtypes = [_vp, ctypes.c_int32]
+    L.gala_context_set_long_rows.restype = ctypes.c_int
     L.gala_context_set_copy_overlap.argtypes = [_vp, ctypes.c_int32]
     L.gala_context_set_copy_overlap.restype = ctypes.c_int
     L.gala_graph_pin.argtypes = [_vp]
@@ -396,6 +399,11 @@ class Context:
         """Weight update of the sweeps: 0 = incremental when few rows moved
         (default), 1 = always full, 2 = incremental whenever allowed."""
         _check(load().gala_context_set_update_mode(self.h, mode))
+
+    def set_long_rows(self, mode):
+        """Contraction rows of more than 8192 entries: 0 = by key range
+        (default), 1 = global hash tables only."""
+        _check(load().gala_context_set_long_rows(self.h, mode))
 
     def set_copy_overlap(self, chunks):
         """gala_louvain of a pinned unweighted graph: copy the neighbours in

@@ -300,6 +300,20 @@ gala_status gala_context_set_hub_table_cap(gala_context *ctx, int64_t slots);
  * and results bit for bit.  Plain runs of one graph only; proposal runs and
  * batches always take the full update. */
 gala_status gala_context_set_update_mode(gala_context *ctx, int32_t mode);
+
+/* Aggregation of the contraction rows longer than 8192 entries inside a
+ * Louvain run (rows in any order; the reference's contraction,
+ * build_compressed_graph.cu:5-173 with kernel_functions.cu:1083-1694, builds
+ * every row with a per-community hash table).  mode 0 (default): each
+ * 4096-entry chunk of a
+ * row is summed per neighbour community in shared memory, its distinct
+ * communities are partitioned by id range (8192 ids per bucket) and every
+ * (row, bucket) is summed in one shared-memory table, whenever the level has
+ * at most 2^24 rows and the scratch holds the work lists; mode 1: every chunk
+ * adds its sums into a global hash table of the row.  Both give the same rows
+ * up to their order, and the same results.  Sorted rows
+ * (gala_contract_device) always take the global tables. */
+gala_status gala_context_set_long_rows(gala_context *ctx, int32_t mode);
 /* Host -> device copy of gala_louvain: with chunks = 2..16 (8 by default) a
  * page-locked (gala_graph_pin) unweighted graph of at least 2^22 entries has
  * its neighbour array copied in that many row-range chunks on a second
