@@ -951,12 +951,16 @@ constexpr int kRadPiece = 32768;    // pairs per CTA of a split bucket
 static_assert(kSmT == kRadW, "the chunk table and a bucket have the same size");
 
 struct RadItem {
-    int i;       // row (list index)
-    int b0, b1;  // buckets [b0, b1)
-    int k0, k1;  // chunks [k0, k1) of the row
-    int acc;     // global table of a split bucket (-1: none)
-    int pieces;  // CTAs of the bucket
-    int total;   // pairs of the buckets over all chunks of the row
+    long long sbase;  // first stream entry of the row
+    long long dst;    // first tmp entry of the row
+    long long w0;     // first chunk of the row (index over all long rows)
+    long long erow;   // entries of the row
+    int i;            // row (list index)
+    int b0, b1;       // buckets [b0, b1)
+    int k0, k1;       // chunks [k0, k1) of the row
+    int acc;          // global table of a split bucket (-1: none)
+    int pieces;       // CTAs of the bucket
+    int total;        // pairs of the buckets over all chunks of the row
 };
 constexpr int kRadItemInts = (int)(sizeof(RadItem) / sizeof(int));
 
@@ -1100,9 +1104,24 @@ __global__ void __launch_bounds__(512) k_rad_combine(AggArgs<WT> a, BigArgs b, i
         const long long E = a.ec[c];
         const long long s0 = a.medge[a.moff[c]] + j * kChunk;
         const int len = (int)((E - j * kChunk) < kChunk ? (E - j * kChunk) : kChunk);
-        for (int q = threadIdx.x; q < len; q += blockDim.x) {
-            const int key = pk[s0 + q];
-            const WT wt = a.sw ? pw[s0 + q] : (WT)1;
+        constexpr int kPer = kChunk / 512;  // entries per thread, loaded before the inserts
+        int kk[kPer];
+        WT ww[kPer];
+#pragma unroll
+        for (int u = 0; u < kPer; ++u) {
+            const int q = threadIdx.x + u * 512;
+            kk[u] = 0;
+            ww[u] = 0;
+            if (q < len) {
+                kk[u] = pk[s0 + q];
+                ww[u] = a.sw ? pw[s0 + q] : (WT)1;
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < kPer; ++u) {
+            if (threadIdx.x + u * 512 >= len) break;
+            const int key = kk[u];
+            const WT wt = ww[u];
             unsigned h = hash_slot(key, kRadLg);
             for (int p = 0; p < kSmT; ++p) {
                 const int k = atomicCAS(&skeys[h], -1, key);
@@ -1183,6 +1202,8 @@ __global__ void k_rad_items(AggArgs<WT> a, BigArgs b, int32_t *pool, long long v
     const long long acc_ints = rad_acc_ints(vints);
     for (int i = wg; i < cnt; i += nw) {
         const int nch = (int)b.chunks[i];
+        const int c = b.list[i];
+        const long long r_sbase = a.medge[a.moff[c]], r_dst = a.tmp_off[c], r_w0 = b.coff[i], r_e = a.ec[c];
         const int32_t *trow = pool + (long long)i * nb;
         long long carry = 0;  // pairs of the buckets before the tile
         int prev_big = 0;
@@ -1226,6 +1247,10 @@ __global__ void k_rad_items(AggArgs<WT> a, BigArgs b, int32_t *pool, long long v
                         const long long P = (t + kRadPiece - 1) / kRadPiece;
                         np = (int)(P < nch ? P : nch);
                     }
+                    it.sbase = r_sbase;
+                    it.dst = r_dst;
+                    it.w0 = r_w0;
+                    it.erow = r_e;
                     it.i = i;
                     it.b0 = ps;
                     it.b1 = bk;
@@ -1293,40 +1318,48 @@ constexpr size_t rad_agg_smem()
     return (size_t)kRadW * (sizeof(WT) + sizeof(int) + sizeof(unsigned short));
 }
 
-// Appends the present slots of a dense bucket table (values v, bitmap nb of
-// non-positive sums) to the row: keys kbase + slot.  GLOBAL: the table is a
-// split bucket's global one (read past L1).
+// One warp appends the present slots [wid * 512, wid * 512 + 512) of a
+// dense bucket table (values v, bitmap nbits of non-positive sums) to row i
+// with one cursor add: keys kbase + slot.  GLOBAL: the table is a split
+// bucket's global one (read past L1); otherwise the values are zeroed.
 template <typename WT, bool GLOBAL>
-__device__ __forceinline__ void rad_emit_dense(const AggArgs<WT> &a, const BigArgs &b, int i, long long o,
-                                               int kbase, WT *v, unsigned *nbits, int *ws, long long *s_base)
+__device__ __forceinline__ void rad_emit_warp(const AggArgs<WT> &a, int32_t *cursor, int i, long long dst,
+                                              int kbase, WT *v, const unsigned *nbits)
 {
-    constexpr int kPer = kRadW / 512;
-    int present = 0;
-#pragma unroll
-    for (int r = 0; r < kPer; ++r) {
-        const int s = threadIdx.x + r * 512;
+    const int lane = threadIdx.x & 31;
+    const int s0 = (threadIdx.x >> 5) * 512;
+    auto present = [&](int s) -> unsigned {
         const WT x = GLOBAL ? __ldcg(&v[s]) : v[s];
-        const unsigned w = GLOBAL ? __ldcg(&nbits[s >> 5]) : nbits[s >> 5];
-        if (x != 0 || ((w >> (s & 31)) & 1u)) present |= 1 << r;
-    }
-    int total;
-    int p = block_excl_scan(__popc(present), ws, total);
-    if (threadIdx.x == 0) *s_base = total ? atomicAdd(&b.cursor[i], total) : 0;
-    __syncthreads();
-    const long long dst = o + *s_base;
-#pragma unroll
-    for (int r = 0; r < kPer; ++r) {
-        const int s = threadIdx.x + r * 512;
-        if (present & (1 << r)) {
-            a.tmp_nbr[dst + p] = kbase + s;
-            a.tmp_w[dst + p] = GLOBAL ? __ldcg(&v[s]) : v[s];
-            ++p;
+        const unsigned wb = GLOBAL ? __ldcg(&nbits[s >> 5]) : nbits[s >> 5];
+        return __ballot_sync(GALA_FULL_MASK, x != 0 || ((wb >> lane) & 1u));
+    };
+    int cnt = 0;
+#pragma unroll 4
+    for (int r = 0; r < 16; ++r) cnt += __popc(present(s0 + r * 32 + lane));
+    long long base = 0;
+    if (lane == 0 && cnt) base = atomicAdd(&cursor[i], cnt);
+    long long d = dst + __shfl_sync(GALA_FULL_MASK, base, 0);
+    const unsigned lt = lanemask_lt();
+#pragma unroll 4
+    for (int r = 0; r < 16; ++r) {
+        const int s = s0 + r * 32 + lane;
+        const unsigned m = present(s);
+        if ((m >> lane) & 1u) {
+            const long long p = d + __popc(m & lt);
+            a.tmp_nbr[p] = kbase + s;
+            a.tmp_w[p] = GLOBAL ? __ldcg(&v[s]) : v[s];
         }
+        d += __popc(m);
         if (!GLOBAL) v[s] = 0;
     }
 }
 
-// The items, taken from a queue by persistent CTAs of 512 threads.
+// The items, taken from a queue by persistent CTAs of 512 threads (the next
+// index is fetched while an item runs).  An item's pairs are spread over all
+// threads: the chunks' pair ranges (up to 512 chunks at a time) are scanned
+// into a prefix in shared memory, and every thread walks it forward to find
+// the chunk of its next pair.  Every warp emits its share of the distinct
+// keys with its own cursor add.
 template <typename WT>
 __global__ void __launch_bounds__(512) k_rad_agg(AggArgs<WT> a, BigArgs b, int32_t *pool, const int32_t *pk,
                                                  const WT *pw, long long vints)
@@ -1346,88 +1379,114 @@ __global__ void __launch_bounds__(512) k_rad_agg(AggArgs<WT> a, BigArgs b, int32
     unsigned *bits = (unsigned *)keys;  // dense items: the first kRadW / 32 key slots
     unsigned short *occ = (unsigned short *)(keys + kRadW);
     __shared__ int s_it, s_n, s_last;
-    __shared__ long long s_base;
     __shared__ int ws[33];
+    __shared__ int cps[513];  // prefix of the pair ranges of a batch of chunks
+    __shared__ int clo[512];  // first pair of each chunk of the batch
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     for (int q = threadIdx.x; q < kRadW; q += blockDim.x) {
         keys[q] = -1;
         vals[q] = 0;
     }
-    if (threadIdx.x == 0) s_n = 0;
+    int nxt = 0;
+    if (threadIdx.x == 0) s_it = atomicAdd(&st->rad_next, 1);
     for (;;) {
-        __syncthreads();
-        if (threadIdx.x == 0) s_it = atomicAdd(&st->rad_next, 1);
         __syncthreads();
         const int itn = s_it;
         if (itn >= nitems) break;
+        if (threadIdx.x == 0) {
+            nxt = atomicAdd(&st->rad_next, 1);
+            s_n = 0;
+        }
         const RadItem it = items[itn];
-        const int c = b.list[it.i];
-        const long long sbase = a.medge[a.moff[c]];
-        const long long w0 = b.coff[it.i];
         const bool dense = it.b1 - it.b0 == 1 && it.total > kRadH;
         const int kbase = it.b0 << kRadLg;
         int T = kRadW, lg = kRadLg;
         if (dense) {
             for (int q = threadIdx.x; q < kRadW / 32; q += blockDim.x) bits[q] = 0;
-            __syncthreads();
         } else {
             T = next_pow2_int(2LL * it.total);
             if (T < 64) T = 64;
             if (T > kRadW) T = kRadW;
             lg = __ffs(T) - 1;
         }
-        // G threads per chunk: enough groups for the chunks, up to a warp per
-        // chunk when the chunks hold many of the item's pairs
-        const int nk = it.k1 - it.k0;
-        const long long per = (long long)it.total / it.pieces / (nk > 0 ? nk : 1);
-        int g1 = 1, g2 = 1;
-        while (g1 * 2 * nk <= 512) g1 <<= 1;
-        while (g2 * 2 <= per && g2 < 32) g2 <<= 1;
-        const int G = g1 > g2 ? g1 : g2;
-        const int gid = threadIdx.x / G, gl = threadIdx.x % G, ng = blockDim.x / G;
-        const long long erow = a.ec[c];
-        for (int k = it.k0 + gid; k < it.k1; k += ng) {
-            const unsigned short *orow = offm + (w0 + k) * nb1;
-            const long long base = sbase + (long long)k * kChunk;
-            const long long len = erow - (long long)k * kChunk;
-            const int lo = orow[it.b0];
-            const int hi = (long long)orow[it.b1] < len ? orow[it.b1] : (int)len;
-            for (int q = lo + gl; q < hi; q += G) {
-                const int key = pk[base + q];
-                const WT v = pw[base + q];
-                if (dense) {
-                    const unsigned s = (unsigned)(key - kbase);
-                    if (s < (unsigned)kRadW) {
-                        atomic_add_w(&vals[s], v);
-                        if (v <= 0) atomicOr(&bits[s >> 5], 1u << (s & 31));
-                    } else {
-                        atomicOr(&st->err, kErrBadIndex);
+        // (the barriers of the scan below order the resets before the inserts)
+        for (int kb = it.k0; kb < it.k1; kb += 512) {
+            const int kn = it.k1 - kb < 512 ? it.k1 - kb : 512;
+            int lo = 0, len = 0;
+            if (threadIdx.x < kn) {
+                const long long k = kb + threadIdx.x;
+                const unsigned short *orow = offm + (it.w0 + k) * nb1;
+                const long long rem = it.erow - k * kChunk;  // entries of the chunk
+                lo = orow[it.b0];
+                long long hi = orow[it.b1];
+                if (hi > rem) hi = rem;
+                len = hi > lo ? (int)hi - lo : 0;
+            }
+            int tot;
+            const int ex = block_excl_scan(len, ws, tot);
+            if (threadIdx.x < kn) {
+                cps[threadIdx.x] = ex;
+                clo[threadIdx.x] = lo;
+            }
+            if (threadIdx.x == 0) cps[kn] = tot;
+            __syncthreads();
+            constexpr int U = 4;
+            int ch = 0;
+            for (int q0 = 0; q0 < tot; q0 += 512 * U) {
+                int key[U];
+                WT v[U];
+#pragma unroll
+                for (int u = 0; u < U; ++u) {
+                    const int q = q0 + u * 512 + threadIdx.x;
+                    key[u] = 0;
+                    v[u] = 0;
+                    if (q < tot) {
+                        while (cps[ch + 1] <= q) ++ch;
+                        const long long pos = it.sbase + (long long)(kb + ch) * kChunk + clo[ch] + (q - cps[ch]);
+                        key[u] = pk[pos];
+                        v[u] = pw[pos];
                     }
-                } else {
-                    int slot;
-                    const int r = table_add(keys, vals, T, lg, key, v, slot);
-                    if (r < 0) atomicOr(&st->err, kErrHashOverflow);
-                    else if (r == 1) occ[atomicAdd(&s_n, 1)] = (unsigned short)slot;
+                }
+#pragma unroll
+                for (int u = 0; u < U; ++u) {
+                    if (q0 + u * 512 + threadIdx.x >= tot) break;
+                    if (dense) {
+                        const unsigned s = (unsigned)(key[u] - kbase);
+                        if (s < (unsigned)kRadW) {
+                            atomic_add_w(&vals[s], v[u]);
+                            if (v[u] <= 0) atomicOr(&bits[s >> 5], 1u << (s & 31));
+                        } else {
+                            atomicOr(&st->err, kErrBadIndex);
+                        }
+                    } else {
+                        int slot;
+                        const int r = table_add(keys, vals, T, lg, key[u], v[u], slot);
+                        if (r < 0) atomicOr(&st->err, kErrHashOverflow);
+                        else if (r == 1) occ[atomicAdd(&s_n, 1)] = (unsigned short)slot;
+                    }
                 }
             }
+            __syncthreads();  // the inserts are done; cps / clo are free
         }
-        __syncthreads();
-        const long long o = a.tmp_off[c];
         if (!dense) {
             const int n = s_n;
-            if (threadIdx.x == 0) s_base = n ? atomicAdd(&b.cursor[it.i], n) : 0;
-            __syncthreads();
-            const long long dst = o + s_base;
-            for (int q = threadIdx.x; q < n; q += blockDim.x) {
-                const int h = occ[q];
-                a.tmp_nbr[dst + q] = keys[h];
-                a.tmp_w[dst + q] = vals[h];
-                keys[h] = -1;
-                vals[h] = 0;
+            const int per = ((n + 15) / 16 + 31) & ~31;  // list entries per warp
+            const int wlo = wid * per;
+            const int whi = wlo + per < n ? wlo + per : n;
+            if (wlo < whi) {
+                long long base = 0;
+                if (lane == 0) base = atomicAdd(&b.cursor[it.i], whi - wlo);
+                const long long d = it.dst + __shfl_sync(GALA_FULL_MASK, base, 0) - wlo;
+                for (int q = wlo + lane; q < whi; q += 32) {
+                    const int h = occ[q];
+                    a.tmp_nbr[d + q] = keys[h];
+                    a.tmp_w[d + q] = vals[h];
+                    keys[h] = -1;
+                    vals[h] = 0;
+                }
             }
-            __syncthreads();
-            if (threadIdx.x == 0) s_n = 0;
         } else if (it.pieces == 1) {
-            rad_emit_dense<WT, false>(a, b, it.i, o, kbase, vals, bits, ws, &s_base);
+            rad_emit_warp<WT, false>(a, b.cursor, it.i, it.dst, kbase, vals, bits);
         } else {
             // add this piece to the bucket's global table; the last piece emits it
             WT *gv = (WT *)(accs + it.acc * acc_ints);
@@ -1446,13 +1505,11 @@ __global__ void __launch_bounds__(512) k_rad_agg(AggArgs<WT> a, BigArgs b, int32
             __syncthreads();
             if (s_last) {
                 __threadfence();
-                rad_emit_dense<WT, true>(a, b, it.i, o, kbase, gv, gb, ws, &s_base);
+                rad_emit_warp<WT, true>(a, b.cursor, it.i, it.dst, kbase, gv, gb);
             }
         }
-        if (dense) {
-            __syncthreads();
-            for (int q = threadIdx.x; q < kRadW / 32; q += blockDim.x) keys[q] = -1;
-        }
+        if (dense && lane < 16) keys[wid * 16 + lane] = -1;  // the bitmap words of this warp's slots
+        if (threadIdx.x == 0) s_it = nxt;
     }
 }
 
