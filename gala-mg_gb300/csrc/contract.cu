@@ -274,20 +274,63 @@ __device__ __forceinline__ int row_class(long long E, int sort_rows)
     return kLongCls;
 }
 
-// Size classes with warp-aggregated appends (one atomic per warp and class;
-// class k lists its communities from lists + k * lstride); communities without
-// entries get an empty row right away.
+// Size classes: every block lists the communities of a contiguous range with
+// one counter add per class (a first pass counts the range); class k lists
+// its communities from lists + k * lstride.  Communities without entries get
+// an empty row right away.
 __global__ void __launch_bounds__(256) k_classify(const long long *__restrict__ ec, int32_t *lists, long long lstride,
                                                   int32_t *kc, DevStats *st, int sort_rows)
 {
+    __shared__ int wc[8][kNumCls];  // per-warp counts of a tile
+    __shared__ int next[kNumCls];   // the block's next list position per class
     const int C = (int)st->ccount;
-    const int stride = gridDim.x * blockDim.x;
-    for (int base = blockIdx.x * blockDim.x; base < C; base += stride) {
-        const int c = base + threadIdx.x;
-        const int cls = c < C ? row_class(ec[c], sort_rows) : -2;
-        if (cls == -1) kc[c] = 0;
+    const long long per = ((long long)C + gridDim.x - 1) / gridDim.x;
+    const int c0 = (int)((long long)blockIdx.x * per < C ? (long long)blockIdx.x * per : C);
+    const int c1 = (int)(c0 + per < C ? c0 + per : C);
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    int cnt[kNumCls];
 #pragma unroll
-        for (int k = 0; k < kNumCls; ++k) warp_append(cls == k, c, lists + k * lstride, &st->small_cnt[k]);
+    for (int k = 0; k < kNumCls; ++k) cnt[k] = 0;
+    for (int c = c0 + threadIdx.x; c < c1; c += blockDim.x) {
+        const int cls = row_class(ec[c], sort_rows);
+#pragma unroll
+        for (int k = 0; k < kNumCls; ++k) cnt[k] += cls == k;
+    }
+    if (threadIdx.x < kNumCls) next[threadIdx.x] = 0;
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < kNumCls; ++k) {
+        const int t = __reduce_add_sync(GALA_FULL_MASK, (unsigned)cnt[k]);
+        if (lane == 0 && t) atomicAdd(&next[k], t);
+    }
+    __syncthreads();
+    if (threadIdx.x < kNumCls && next[threadIdx.x])
+        next[threadIdx.x] = atomicAdd(&st->small_cnt[threadIdx.x], next[threadIdx.x]);
+    __syncthreads();
+    for (int t0 = c0; t0 < c1; t0 += blockDim.x) {  // block-uniform
+        const int c = t0 + threadIdx.x;
+        const int cls = c < c1 ? row_class(ec[c], sort_rows) : -2;
+        if (cls == -1) kc[c] = 0;
+        int rank = 0;
+#pragma unroll
+        for (int k = 0; k < kNumCls; ++k) {
+            const unsigned b = __ballot_sync(GALA_FULL_MASK, cls == k);
+            if (cls == k) rank = __popc(b & lanemask_lt());
+            if (lane == 0) wc[wid][k] = __popc(b);
+        }
+        __syncthreads();
+        if (cls >= 0) {
+            int off = next[cls] + rank;
+            for (int w = 0; w < wid; ++w) off += wc[w][cls];
+            lists[cls * lstride + off] = c;
+        }
+        __syncthreads();
+        if (threadIdx.x < kNumCls) {
+            int s = 0;
+            for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s += wc[w][threadIdx.x];
+            next[threadIdx.x] += s;
+        }
+        __syncthreads();
     }
 }
 
