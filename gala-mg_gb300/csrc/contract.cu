@@ -840,7 +840,8 @@ __global__ void __launch_bounds__(512) k_big_insert_sm(AggArgs<WT> a, BigArgs b,
             const WT wt = a.w_at(st + q);
             unsigned h = hash_slot(key, slg);
             for (int p = 0; p < kSmT; ++p) {
-                const int k = atomicCAS(&skeys[h], -1, key);
+                int k = *(volatile int *)&skeys[h];  // a repeated key skips the claim
+                if (k == -1) k = atomicCAS(&skeys[h], -1, key);
                 if (k == -1 || k == key) {
                     atomic_add_w(&svals[h], wt);
                     if (k == -1) socc[atomicAdd(&s_n, 1)] = (unsigned short)h;
@@ -1167,7 +1168,8 @@ __global__ void __launch_bounds__(512) k_rad_combine(AggArgs<WT> a, BigArgs b, i
             const WT wt = ww[u];
             unsigned h = hash_slot(key, kRadLg);
             for (int p = 0; p < kSmT; ++p) {
-                const int k = atomicCAS(&skeys[h], -1, key);
+                int k = *(volatile int *)&skeys[h];  // a repeated key skips the claim
+                if (k == -1) k = atomicCAS(&skeys[h], -1, key);
                 if (k == -1 || k == key) {
                     atomic_add_w(&svals[h], wt);
                     if (k == -1) {
