@@ -1111,8 +1111,9 @@ constexpr size_t rad_combine_smem()
 // hash table), then write the distinct pairs back over the chunk in bucket
 // order.  pk / pw are the stream's keys and weight slots (the weight slots
 // are written even on an unweighted level, where the stream has no weights).
+constexpr int kRadCombineThreads = 1024;  // two CTAs per SM: 32 registers a thread
 template <typename WT>
-__global__ void __launch_bounds__(512) k_rad_combine(AggArgs<WT> a, BigArgs b, int32_t *pool, int32_t *pk, WT *pw)
+__global__ void __launch_bounds__(kRadCombineThreads, 2) k_rad_combine(AggArgs<WT> a, BigArgs b, int32_t *pool, int32_t *pk, WT *pw)
 {
     DevStats *st = a.st;
     const long long nwork = big_off(st) ? 0 : st->big_nwork;
@@ -1148,12 +1149,12 @@ __global__ void __launch_bounds__(512) k_rad_combine(AggArgs<WT> a, BigArgs b, i
         const long long E = a.ec[c];
         const long long s0 = a.medge[a.moff[c]] + j * kChunk;
         const int len = (int)((E - j * kChunk) < kChunk ? (E - j * kChunk) : kChunk);
-        constexpr int kPer = kChunk / 512;  // entries per thread, loaded before the inserts
+        constexpr int kPer = kChunk / kRadCombineThreads;  // entries per thread, loaded before the inserts
         int kk[kPer];
         WT ww[kPer];
 #pragma unroll
         for (int u = 0; u < kPer; ++u) {
-            const int q = threadIdx.x + u * 512;
+            const int q = threadIdx.x + u * kRadCombineThreads;
             kk[u] = 0;
             ww[u] = 0;
             if (q < len) {
@@ -1163,7 +1164,7 @@ __global__ void __launch_bounds__(512) k_rad_combine(AggArgs<WT> a, BigArgs b, i
         }
 #pragma unroll
         for (int u = 0; u < kPer; ++u) {
-            if (threadIdx.x + u * 512 >= len) break;
+            if (threadIdx.x + u * kRadCombineThreads >= len) break;
             const int key = kk[u];
             const WT wt = ww[u];
             unsigned h = hash_slot(key, kRadLg);
@@ -1185,11 +1186,12 @@ __global__ void __launch_bounds__(512) k_rad_combine(AggArgs<WT> a, BigArgs b, i
         }
         __syncthreads();
         const int n = s_n;
-        // bucket offsets of the chunk: exclusive scan of hist, 4 buckets per thread
-        int v[4], sum = 0;
-        const int t4 = threadIdx.x * 4;
+        // bucket offsets of the chunk: exclusive scan of hist, kHistPer buckets per thread
+        constexpr int kHistPer = kRadNbMax / kRadCombineThreads;
+        int v[kHistPer], sum = 0;
+        const int t4 = threadIdx.x * kHistPer;
 #pragma unroll
-        for (int u = 0; u < 4; ++u) {
+        for (int u = 0; u < kHistPer; ++u) {
             v[u] = (t4 + u < nb) ? hist[t4 + u] : 0;
             sum += v[u];
         }
@@ -1197,7 +1199,7 @@ __global__ void __launch_bounds__(512) k_rad_combine(AggArgs<WT> a, BigArgs b, i
         int run = block_excl_scan(sum, ws, total);
         unsigned short *orow = offm + wi * (nb + 1);
 #pragma unroll
-        for (int u = 0; u < 4; ++u) {
+        for (int u = 0; u < kHistPer; ++u) {
             const int bk = t4 + u;
             if (bk < nb) {
                 if (v[u]) atomicAdd(&tot[(long long)i * nb + bk], v[u]);
@@ -1919,7 +1921,8 @@ static bool contract_long_rows(const AggArgs<WT> &a, ContractBuffers &b, const i
         exclusive_scan_dev(b.big_chunks, b.big_coff, cnt_max, dcnt, OpIdentity(), b.scan_partial, &ds->big_nwork, st,
                            &ds->err);
         k_rad_tail<<<1, 1, 0, st>>>(ba, ds, vints, b.big_pool_ints);
-        k_rad_combine<WT><<<resident_grid(k_rad_combine<WT>, 512, rad_combine_smem<WT>()), 512,
+        k_rad_combine<WT><<<resident_grid(k_rad_combine<WT>, kRadCombineThreads, rad_combine_smem<WT>()),
+                            kRadCombineThreads,
                             rad_combine_smem<WT>(), st>>>(a, ba, b.big_pool, b.stream_key, (WT *)b.stream_w);
         k_rad_items<WT><<<grid_cap((long long)cnt_max * 32, 256, cap), 256, 0, st>>>(a, ba, b.big_pool, vints);
         k_rad_agg<WT><<<resident_grid(k_rad_agg<WT>, 512, rad_agg_smem<WT>()), 512, rad_agg_smem<WT>(), st>>>(
