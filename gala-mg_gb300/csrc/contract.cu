@@ -1359,10 +1359,15 @@ __global__ void k_rad_items(AggArgs<WT> a, BigArgs b, int32_t *pool, long long v
     }
 }
 
+// Hashed items hold under 2 kRadH pairs, so their slot lists need 2 kRadH
+// entries; chunk ranges are scanned kRadBatch at a time.  With int weights
+// three CTAs fit an SM.
+constexpr int kRadOcc = 2 * kRadH;
+constexpr int kRadBatch = 256;
 template <typename WT>
 constexpr size_t rad_agg_smem()
 {
-    return (size_t)kRadW * (sizeof(WT) + sizeof(int) + sizeof(unsigned short));
+    return (size_t)kRadW * (sizeof(WT) + sizeof(int)) + kRadOcc * sizeof(unsigned short);
 }
 
 // One warp appends the present slots [wid * 512, wid * 512 + 512) of a
@@ -1403,7 +1408,7 @@ __device__ __forceinline__ void rad_emit_warp(const AggArgs<WT> &a, int32_t *cur
 
 // The items, taken from a queue by persistent CTAs of 512 threads (the next
 // index is fetched while an item runs).  An item's pairs are spread over all
-// threads: the chunks' pair ranges (up to 512 chunks at a time) are scanned
+// threads: the chunks' pair ranges (kRadBatch chunks at a time) are scanned
 // into a prefix in shared memory, and every thread walks it forward to find
 // the chunk of its next pair.  Every warp emits its share of the distinct
 // keys with its own cursor add.
@@ -1427,8 +1432,8 @@ __global__ void __launch_bounds__(512) k_rad_agg(AggArgs<WT> a, BigArgs b, int32
     unsigned short *occ = (unsigned short *)(keys + kRadW);
     __shared__ int s_it, s_n, s_last;
     __shared__ int ws[33];
-    __shared__ int cps[513];  // prefix of the pair ranges of a batch of chunks
-    __shared__ int clo[512];  // first pair of each chunk of the batch
+    __shared__ int cps[kRadBatch + 1];  // prefix of the pair ranges of a batch of chunks
+    __shared__ int clo[kRadBatch];      // first pair of each chunk of the batch
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     for (int q = threadIdx.x; q < kRadW; q += blockDim.x) {
         keys[q] = -1;
@@ -1457,8 +1462,8 @@ __global__ void __launch_bounds__(512) k_rad_agg(AggArgs<WT> a, BigArgs b, int32
             lg = __ffs(T) - 1;
         }
         // (the barriers of the scan below order the resets before the inserts)
-        for (int kb = it.k0; kb < it.k1; kb += 512) {
-            const int kn = it.k1 - kb < 512 ? it.k1 - kb : 512;
+        for (int kb = it.k0; kb < it.k1; kb += kRadBatch) {
+            const int kn = it.k1 - kb < kRadBatch ? it.k1 - kb : kRadBatch;
             int lo = 0, len = 0;
             if (threadIdx.x < kn) {
                 const long long k = kb + threadIdx.x;
@@ -1509,14 +1514,18 @@ __global__ void __launch_bounds__(512) k_rad_agg(AggArgs<WT> a, BigArgs b, int32
                         int slot;
                         const int r = table_add(keys, vals, T, lg, key[u], v[u], slot);
                         if (r < 0) atomicOr(&st->err, kErrHashOverflow);
-                        else if (r == 1) occ[atomicAdd(&s_n, 1)] = (unsigned short)slot;
+                        else if (r == 1) {
+                            const int o = atomicAdd(&s_n, 1);
+                            if (o < kRadOcc) occ[o] = (unsigned short)slot;
+                            else atomicOr(&st->err, kErrHashOverflow);
+                        }
                     }
                 }
             }
             __syncthreads();  // the inserts are done; cps / clo are free
         }
         if (!dense) {
-            const int n = s_n;
+            const int n = s_n < kRadOcc ? s_n : kRadOcc;
             const int per = ((n + 15) / 16 + 31) & ~31;  // list entries per warp
             const int wlo = wid * per;
             const int whi = wlo + per < n ? wlo + per : n;
