@@ -202,3 +202,13 @@ def test_cli_binaries_exist(ffi):
     d = os.path.dirname(ffi.LIB_PATH)
     for exe in ("gala_main", "gala_preprocess"):
         assert os.access(os.path.join(d, exe), os.X_OK)
+
+
+def test_context_setters_reject_a_null_context(ffi):
+    """The per-context switches check their arguments before any device work:
+    a null context is GALA_ERR_INVALID (1), on a machine with or without a GPU."""
+    L = ffi.load()
+    assert L.gala_context_set_update_mode(None, 0) == 1
+    assert L.gala_context_set_copy_overlap(None, 8) == 1
+    assert L.gala_context_set_long_rows(None, 0) == 1
+    assert L.gala_context_set_hub_table_cap(None, 0) == 1
